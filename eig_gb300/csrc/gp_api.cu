@@ -1,0 +1,678 @@
+/*
+ * C ABI of the smartpca hot path: handle management and the pass orchestration
+ * (gp_xtx, gp_eigvecs, gp_snp_weights, gp_lsqproj) plus the host-side outlier rule.
+ * The numerical work runs in the kernels of the other .cu files on the handle's stream.
+ */
+#include <cuda_runtime.h>
+#include <cusolverDn.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdlib.h>
+#include <vector>
+
+#include "gp_geno_gemm.h"
+#include "gp_internal.h"
+
+#define GP_VERSION 10000
+
+static char g_open_err[GP_ERRLEN];
+
+extern "C" int gp_version(void) { return GP_VERSION; }
+
+extern "C" const char *gp_last_error(const gp_ctx *ctx) { return ctx ? ctx->err : g_open_err; }
+
+int gp_fail(gp_ctx *ctx, int code, const char *fmt, ...)
+{
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(ctx ? ctx->err : g_open_err, GP_ERRLEN, fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+extern "C" int gp_fail_msg(gp_ctx *ctx, int code, const char *fmt, ...)
+{
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(ctx ? ctx->err : g_open_err, GP_ERRLEN, fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+int gp_cuda_fail(gp_ctx *ctx, cudaError_t e, const char *what)
+{
+  return gp_fail(ctx, e == cudaErrorMemoryAllocation ? GP_ERR_NOMEM : GP_ERR_CUDA,
+                 "%s: %s", what, cudaGetErrorString(e));
+}
+
+static int grow(gp_ctx *ctx, void **buf, size_t *cap, size_t bytes)
+{
+  if (bytes <= *cap && *buf) return GP_OK;
+  if (*buf) {
+    cudaFree(*buf);
+    *buf = NULL;
+    *cap = 0;
+  }
+  size_t want = bytes < 256 ? 256 : bytes;
+  cudaError_t e = cudaMalloc(buf, want);
+  if (e != cudaSuccess) {
+    *buf = NULL;
+    return gp_fail(ctx, GP_ERR_NOMEM, "device allocation of %zu bytes failed: %s", want,
+                   cudaGetErrorString(e));
+  }
+  *cap = want;
+  return GP_OK;
+}
+
+int gp_scratch(gp_ctx *ctx, size_t bytes, void **out)
+{
+  int rc = grow(ctx, &ctx->d_scratch, &ctx->scratch_cap, bytes);
+  *out = ctx->d_scratch;
+  return rc;
+}
+
+int gp_scratch2(gp_ctx *ctx, size_t bytes, void **out)
+{
+  int rc = grow(ctx, &ctx->d_scratch2, &ctx->scratch2_cap, bytes);
+  *out = ctx->d_scratch2;
+  return rc;
+}
+
+int gp_realloc(gp_ctx *ctx, void **ptr, size_t bytes)
+{
+  if (*ptr) cudaFree(*ptr);
+  *ptr = NULL;
+  cudaError_t e = cudaMalloc(ptr, bytes < 256 ? 256 : bytes);
+  if (e != cudaSuccess) {
+    *ptr = NULL;
+    return gp_fail(ctx, GP_ERR_NOMEM, "device allocation of %zu bytes failed: %s", bytes,
+                   cudaGetErrorString(e));
+  }
+  return GP_OK;
+}
+
+extern "C" int gp_open(int device, gp_ctx **out)
+{
+  if (!out) return gp_fail(NULL, GP_ERR_ARG, "gp_open: out is NULL");
+  *out = NULL;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0)
+    return gp_fail(NULL, GP_ERR_CUDA, "gp_open: no CUDA device (%s)", cudaGetErrorString(e));
+  if (device < 0 || device >= ndev)
+    return gp_fail(NULL, GP_ERR_ARG, "gp_open: device %d out of range", device);
+  gp_ctx *ctx = (gp_ctx *)calloc(1, sizeof(gp_ctx));
+  if (!ctx) return gp_fail(NULL, GP_ERR_NOMEM, "gp_open: host allocation failed");
+  ctx->device = device;
+  e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    gp_fail(NULL, GP_ERR_CUDA, "gp_open: %s", cudaGetErrorString(e));
+    free(ctx);
+    return GP_ERR_CUDA;
+  }
+  if (cusolverDnCreate(&ctx->solver) != CUSOLVER_STATUS_SUCCESS ||
+      cusolverDnSetStream(ctx->solver, ctx->stream) != CUSOLVER_STATUS_SUCCESS) {
+    cudaStreamDestroy(ctx->stream);
+    free(ctx);
+    return gp_fail(NULL, GP_ERR_SOLVER, "gp_open: cusolverDnCreate failed");
+  }
+  *out = ctx;
+  return GP_OK;
+}
+
+extern "C" void gp_close(gp_ctx *ctx)
+{
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  void *bufs[] = {ctx->d_geno,   ctx->d_rows,    ctx->d_rowmask, ctx->d_cols,    ctx->d_cnt,
+                  ctx->d_killed, ctx->d_vtab,    ctx->d_xmean,   ctx->d_xfancy,  ctx->d_kept,
+                  ctx->d_xtx,    ctx->d_evals,   ctx->d_evecs,   ctx->d_ffvecs,  ctx->d_fxscal,
+                  ctx->d_scratch, ctx->d_scratch2};
+  for (size_t i = 0; i < sizeof(bufs) / sizeof(bufs[0]); ++i)
+    if (bufs[i]) cudaFree(bufs[i]);
+  if (ctx->solver) cusolverDnDestroy(ctx->solver);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  free(ctx);
+}
+
+extern "C" int gp_device_bytes(const gp_ctx *ctx, int64_t *bytes)
+{
+  if (!ctx || !bytes) return GP_ERR_ARG;
+  int64_t b = (int64_t)ctx->rlen_dev * ctx->nsnp_all + (int64_t)ctx->scratch_cap +
+              (int64_t)ctx->scratch2_cap + (int64_t)sizeof(double) * ctx->xtx_cap;
+  *bytes = b;
+  return GP_OK;
+}
+
+/* ------------------------------------------------------------------------------------ */
+
+__global__ void k_scale(double *x, int64_t n, double s)
+{
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    x[i] = x[i] * s;
+}
+
+extern "C" int gp_xtx(gp_ctx *ctx, const gp_xtx_opts *opts, int32_t *n0, int32_t *n1,
+                      int32_t *nmiss, uint8_t *killed, double *xmean, double *xfancy,
+                      double *XTX, double *trace, int32_t *nused)
+{
+  if (!ctx || !opts) return GP_ERR_ARG;
+  if (!ctx->d_geno || ctx->nrows < 1 || ctx->ncols < 1)
+    return gp_fail(ctx, GP_ERR_STATE, "gp_xtx: genotypes, samples and SNPs must be set first");
+  if (opts->precision != GP_PREC_FP64 && opts->precision != GP_PREC_SPLIT_BF16)
+    return gp_fail(ctx, GP_ERR_ARG, "gp_xtx: unknown precision %d", opts->precision);
+  GP_CUDA(ctx, cudaSetDevice(ctx->device));
+  const int32_t n = ctx->nrows, nc = ctx->ncols;
+  int64_t need = (int64_t)n * n;
+  if (need > ctx->xtx_cap) {
+    int rc = gp_realloc(ctx, (void **)&ctx->d_xtx, sizeof(double) * (size_t)need);
+    if (rc) {
+      ctx->xtx_cap = 0;
+      return rc;
+    }
+    ctx->xtx_cap = need;
+  }
+  ctx->xtx_valid = ctx->eig_valid = ctx->weights_valid = 0;
+  int rc = gp_launch_snp_stats(ctx, opts);
+  if (rc) return rc;
+
+  /* kept-column list (ascending) built from the kill flags */
+  std::vector<uint8_t> hk((size_t)nc);
+  GP_CUDA(ctx, cudaMemcpyAsync(hk.data(), ctx->d_killed, (size_t)nc, cudaMemcpyDeviceToHost,
+                               ctx->stream));
+  GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  std::vector<int32_t> kept;
+  kept.reserve((size_t)nc);
+  for (int32_t c = 0; c < nc; ++c)
+    if (!hk[(size_t)c]) kept.push_back(c);
+  ctx->nkept = (int32_t)kept.size();
+  if (ctx->nkept)
+    GP_CUDA(ctx, cudaMemcpyAsync(ctx->d_kept, kept.data(), sizeof(int32_t) * kept.size(),
+                                 cudaMemcpyHostToDevice, ctx->stream));
+
+  if (opts->precision == GP_PREC_FP64)
+    rc = gp_gram_fp64(ctx);
+  else
+    rc = gp_gram_split_bf16(ctx);
+  if (rc) return rc;
+
+  double *d_tr;
+  rc = gp_scratch(ctx, sizeof(double), (void **)&d_tr);
+  if (rc) return rc;
+  rc = gp_launch_symmetrize_trace(ctx, d_tr);
+  if (rc) return rc;
+  double tr = 0.0;
+  GP_CUDA(ctx, cudaMemcpyAsync(&tr, d_tr, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  if (n0 || n1 || nmiss) {
+    std::vector<int32_t> cnt((size_t)nc * 3);
+    GP_CUDA(ctx, cudaMemcpyAsync(cnt.data(), ctx->d_cnt, sizeof(int32_t) * cnt.size(),
+                                 cudaMemcpyDeviceToHost, ctx->stream));
+    GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int32_t c = 0; c < nc; ++c) {
+      if (n0) n0[c] = cnt[3 * (size_t)c];
+      if (n1) n1[c] = cnt[3 * (size_t)c + 1];
+      if (nmiss) nmiss[c] = cnt[3 * (size_t)c + 2];
+    }
+  }
+  if (killed) memcpy(killed, hk.data(), (size_t)nc);
+  if (xmean)
+    GP_CUDA(ctx, cudaMemcpyAsync(xmean, ctx->d_xmean, sizeof(double) * nc,
+                                 cudaMemcpyDeviceToHost, ctx->stream));
+  if (xfancy)
+    GP_CUDA(ctx, cudaMemcpyAsync(xfancy, ctx->d_xfancy, sizeof(double) * nc,
+                                 cudaMemcpyDeviceToHost, ctx->stream));
+  if (XTX)
+    GP_CUDA(ctx, cudaMemcpyAsync(XTX, ctx->d_xtx, sizeof(double) * (size_t)need,
+                                 cudaMemcpyDeviceToHost, ctx->stream));
+  GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  ctx->trace = tr;
+  if (trace) *trace = tr;
+  if (nused) *nused = ctx->nkept;
+  ctx->xtx_valid = 1;
+  return GP_OK;
+}
+
+/* ------------------------------------------------------------------------------------ */
+
+/* evecs[j*n + i] = A[(n-1-j)*n + i]: the top nvec eigenvectors (columns) in descending order */
+__global__ void k_take_top(double *evecs, const double *A, int32_t n, int32_t nvec)
+{
+  int64_t total = (int64_t)n * nvec;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int64_t j = idx / n, i = idx - j * n;
+    evecs[idx] = A[(int64_t)(n - 1 - j) * n + i];
+  }
+}
+
+extern "C" int gp_eigvecs(gp_ctx *ctx, int32_t nvec, double *evals, double *evecs)
+{
+  if (!ctx) return GP_ERR_ARG;
+  if (!ctx->xtx_valid) return gp_fail(ctx, GP_ERR_STATE, "gp_eigvecs: no Gram (call gp_xtx)");
+  const int32_t n = ctx->nrows;
+  if (nvec < 0 || nvec > n) return gp_fail(ctx, GP_ERR_ARG, "gp_eigvecs: nvec %d", nvec);
+  GP_CUDA(ctx, cudaSetDevice(ctx->device));
+  /* y = trace/(n-1); XTX *= 1/y  (smartpca.c:1230-1236) */
+  double y = ctx->trace / (double)(n - 1);
+  if (isnan(y)) return gp_fail(ctx, GP_ERR_NODATA, "bad XTX matrix");
+  if (y <= 0.0) return gp_fail(ctx, GP_ERR_NODATA, "XTX has zero trace (perhaps no data)");
+  int64_t nn = (int64_t)n * n;
+  int blocks = (int)((nn + 255) / 256);
+  if (blocks > ctx->num_sms * 16) blocks = ctx->num_sms * 16;
+  k_scale<<<blocks, 256, 0, ctx->stream>>>(ctx->d_xtx, nn, 1.0 / y);
+  GP_LAUNCH_CHECK(ctx, "k_scale");
+
+  int rc = gp_realloc(ctx, (void **)&ctx->d_evals, sizeof(double) * (size_t)n);
+  if (rc) return rc;
+  int32_t keep = nvec > 0 ? nvec : 1;
+  rc = gp_realloc(ctx, (void **)&ctx->d_evecs, sizeof(double) * (size_t)n * keep);
+  if (rc) return rc;
+  int lwork = 0;
+  if (cusolverDnDsyevd_bufferSize(ctx->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
+                                  n, ctx->d_xtx, n, ctx->d_evals, &lwork) !=
+      CUSOLVER_STATUS_SUCCESS)
+    return gp_fail(ctx, GP_ERR_SOLVER, "cusolverDnDsyevd_bufferSize failed");
+  uint8_t *ws;
+  rc = gp_scratch(ctx, sizeof(double) * (size_t)lwork + 256, (void **)&ws);
+  if (rc) return rc;
+  int *d_info = (int *)(ws + sizeof(double) * (size_t)lwork);
+  if (cusolverDnDsyevd(ctx->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n,
+                       ctx->d_xtx, n, ctx->d_evals, (double *)ws, lwork,
+                       d_info) != CUSOLVER_STATUS_SUCCESS)
+    return gp_fail(ctx, GP_ERR_SOLVER, "cusolverDnDsyevd failed to launch");
+  int info = 0;
+  GP_CUDA(ctx, cudaMemcpyAsync(&info, d_info, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  if (nvec > 0) {
+    int64_t tot = (int64_t)n * nvec;
+    int b2 = (int)((tot + 255) / 256);
+    if (b2 > ctx->num_sms * 16) b2 = ctx->num_sms * 16;
+    k_take_top<<<b2, 256, 0, ctx->stream>>>(ctx->d_evecs, ctx->d_xtx, n, nvec);
+    GP_LAUNCH_CHECK(ctx, "k_take_top");
+  }
+  std::vector<double> w((size_t)n);
+  GP_CUDA(ctx, cudaMemcpyAsync(w.data(), ctx->d_evals, sizeof(double) * (size_t)n,
+                               cudaMemcpyDeviceToHost, ctx->stream));
+  if (evecs && nvec > 0)
+    GP_CUDA(ctx, cudaMemcpyAsync(evecs, ctx->d_evecs, sizeof(double) * (size_t)n * nvec,
+                                 cudaMemcpyDeviceToHost, ctx->stream));
+  GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  ctx->xtx_valid = 0; /* the solver overwrote the Gram with eigenvectors */
+  if (info != 0) return gp_fail(ctx, GP_ERR_SOLVER, "eigensolver info = %d", info);
+  if (evals)
+    for (int32_t i = 0; i < n; ++i) evals[i] = w[(size_t)(n - 1 - i)];
+  ctx->nvec = nvec;
+  ctx->eig_valid = 1;
+  ctx->weights_valid = 0;
+  return GP_OK;
+}
+
+/* ------------------------------------------------------------------------------------ */
+
+extern "C" int gp_ridoutlier(const double *evecs, int32_t n, int32_t neigs, double thresh,
+                             int32_t mode, int32_t *badlist, int32_t *vecno, double *score)
+{
+  /* restates ridoutlier (src/eigensrc/smartsubs.c:18-91) with the same operation order */
+  if (!evecs || !badlist || n < 0 || neigs < 0) return GP_ERR_ARG;
+  if (mode > 1) return 0;
+  if (n < 3) return 0;
+  std::vector<double> ww((size_t)n), w2((size_t)n);
+  std::vector<int> vbad((size_t)n, 0), vno((size_t)n, -1);
+  std::vector<double> sc((size_t)n, 0.0);
+  for (int32_t i = 0; i < neigs; ++i) {
+    memcpy(ww.data(), evecs + (size_t)i * n, sizeof(double) * (size_t)n);
+    if (mode == 0) {
+      double y1 = 0.0;
+      for (int32_t j = 0; j < n; ++j) y1 += ww[(size_t)j];
+      y1 = y1 / (double)n;
+      for (int32_t j = 0; j < n; ++j) ww[(size_t)j] = ww[(size_t)j] + (-y1);
+      double y2 = 0.0;
+      for (int32_t j = 0; j < n; ++j) y2 += ww[(size_t)j] * ww[(size_t)j];
+      y2 = y2 / (double)n;
+      y2 = sqrt(y2);
+      double inv = 1.0 / y2;
+      for (int32_t j = 0; j < n; ++j) ww[(size_t)j] = ww[(size_t)j] * inv;
+      for (int32_t j = 0; j < n; ++j) {
+        if (fabs(ww[(size_t)j]) > thresh) {
+          vbad[(size_t)j] = 1;
+          if (vno[(size_t)j] < 0) {
+            vno[(size_t)j] = i;
+            sc[(size_t)j] = ww[(size_t)j];
+          }
+        }
+      }
+    } else {
+      for (int32_t j = 0; j < n; ++j) {
+        double yy = ww[(size_t)j];
+        ww[(size_t)j] = 0;
+        double y1 = 0.0;
+        for (int32_t t = 0; t < n; ++t) y1 += ww[(size_t)t];
+        y1 = y1 / (double)(n - 1);
+        for (int32_t t = 0; t < n; ++t) w2[(size_t)t] = ww[(size_t)t] + (-y1);
+        w2[(size_t)j] = 0;
+        double y2 = 0.0;
+        for (int32_t t = 0; t < n; ++t) y2 += w2[(size_t)t] * w2[(size_t)t];
+        y2 = y2 / (double)n;
+        y2 = sqrt(y2);
+        double zz = yy - y1;
+        zz /= y2;
+        if (fabs(zz) > thresh) {
+          vbad[(size_t)j] = 1;
+          if (vno[(size_t)j] < 0) {
+            vno[(size_t)j] = i;
+            sc[(size_t)j] = zz;
+          }
+        }
+        ww[(size_t)j] = yy;
+      }
+    }
+  }
+  int32_t nbad = 0;
+  for (int32_t j = 0; j < n; ++j) {
+    if (vecno) vecno[j] = vno[(size_t)j];
+    if (score) score[j] = sc[(size_t)j];
+    if (vbad[(size_t)j] == 1) badlist[nbad++] = j;
+  }
+  return nbad;
+}
+
+/* ------------------------------------------------------------------------------------ */
+
+/* B[r*K + j] = 10 * evecs[j*n + r]   (setfvecs src/qpsubs.c:489-507) */
+__global__ void k_fvecs_T(double *B, const double *evecs, int32_t n, int32_t K)
+{
+  int64_t total = (int64_t)n * K;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int64_t r = idx / K, j = idx - r * K;
+    B[idx] = evecs[j * n + r] * 10.0;
+  }
+}
+
+/* per kept column: record index, value table (vtab) and the fixxrow table
+ * r(g) = g*fancy - xmean (src/qpsubs.c:338-348), missing -> 0 */
+__global__ void k_kept_tables(const int32_t *kept, int32_t nkept, const int32_t *cols,
+                              const double *vtab, const double *xmean, const double *xfancy,
+                              int32_t *snprec, double *vt, double *rt, double *ot)
+{
+  for (int32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nkept; k += gridDim.x * blockDim.x) {
+    int32_t c = kept[k];
+    snprec[k] = cols[c];
+    for (int t = 0; t < 4; ++t) vt[4 * k + t] = vtab[4 * c + t];
+    double f = xfancy[c], m = xmean[c];
+    for (int g = 0; g < 3; ++g) {
+      double x = __dmul_rn((double)g, f);
+      rt[4 * k + g] = (x < -0.001) ? 0.0 : __dsub_rn(x, m);
+    }
+    rt[4 * k + 3] = 0.0;
+    ot[4 * k] = ot[4 * k + 1] = ot[4 * k + 2] = 1.0;
+    ot[4 * k + 3] = 0.0;
+  }
+}
+
+/* ffvecs[j*ncols + kept[k]] = ffvT[k*K + j] (killed columns stay 0) */
+__global__ void k_scatter_ffvecs(double *ffvecs, const double *ffvT, const int32_t *kept,
+                                 int32_t nkept, int32_t ncols, int32_t K)
+{
+  int64_t total = (int64_t)nkept * K;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int64_t k = idx / K, j = idx - k * K;
+    ffvecs[j * ncols + kept[k]] = ffvT[idx];
+  }
+}
+
+struct kept_tables {
+  int32_t *snprec;
+  double *vt, *rt, *ot;
+};
+
+static int build_kept_tables(gp_ctx *ctx, uint8_t *base, kept_tables *t)
+{
+  int32_t nk = ctx->nkept;
+  t->vt = (double *)base;
+  t->rt = t->vt + 4 * (size_t)nk;
+  t->ot = t->rt + 4 * (size_t)nk;
+  t->snprec = (int32_t *)(t->ot + 4 * (size_t)nk);
+  if (nk == 0) return GP_OK;
+  int blocks = (nk + 255) / 256;
+  if (blocks > ctx->num_sms * 8) blocks = ctx->num_sms * 8;
+  k_kept_tables<<<blocks, 256, 0, ctx->stream>>>(ctx->d_kept, nk, ctx->d_cols, ctx->d_vtab,
+                                                 ctx->d_xmean, ctx->d_xfancy, t->snprec, t->vt,
+                                                 t->rt, t->ot);
+  GP_LAUNCH_CHECK(ctx, "k_kept_tables");
+  return GP_OK;
+}
+
+static size_t kept_tables_bytes(int32_t nk) { return (size_t)nk * (12 * sizeof(double) + 4) + 256; }
+
+extern "C" int gp_snp_weights(gp_ctx *ctx, int32_t numeigs, double *ffvecs, double *fxvecs,
+                              double *fxscal)
+{
+  if (!ctx || !fxscal) return GP_ERR_ARG;
+  if (!ctx->eig_valid) return gp_fail(ctx, GP_ERR_STATE, "gp_snp_weights: call gp_eigvecs first");
+  if (numeigs < 1 || numeigs > ctx->nvec)
+    return gp_fail(ctx, GP_ERR_ARG, "gp_snp_weights: numeigs %d > resident vectors %d", numeigs,
+                   ctx->nvec);
+  GP_CUDA(ctx, cudaSetDevice(ctx->device));
+  const int32_t n = ctx->nrows, nc = ctx->ncols, nk = ctx->nkept, K = numeigs;
+  int rc = gp_realloc(ctx, (void **)&ctx->d_ffvecs, sizeof(double) * (size_t)K * nc);
+  if (!rc) rc = gp_realloc(ctx, (void **)&ctx->d_fxscal, sizeof(double) * (size_t)K);
+  if (rc) return rc;
+  size_t off_tab = kept_tables_bytes(nk);
+  size_t bytes = off_tab + sizeof(double) * ((size_t)n * K + (size_t)nk * K + (size_t)n * K) + 256;
+  uint8_t *base;
+  rc = gp_scratch(ctx, bytes, (void **)&base);
+  if (rc) return rc;
+  kept_tables kt;
+  rc = build_kept_tables(ctx, base, &kt);
+  if (rc) return rc;
+  double *d_B = (double *)(base + off_tab);
+  double *d_ffvT = d_B + (size_t)n * K;
+  double *d_fxT = d_ffvT + (size_t)nk * K;
+  int blocks = (int)(((int64_t)n * K + 255) / 256);
+  if (blocks > ctx->num_sms * 16) blocks = ctx->num_sms * 16;
+  k_fvecs_T<<<blocks, 256, 0, ctx->stream>>>(d_B, ctx->d_evecs, n, K);
+  GP_LAUNCH_CHECK(ctx, "k_fvecs_T");
+  /* ffvecs^T[k][j] = sum_r v(r,k) * 10 evec_j[r] */
+  rc = gp_geno_gemm_f64(ctx, 0, ctx->d_rows, n, kt.snprec, kt.vt, nk, d_B, K, K, d_ffvT, K);
+  if (rc) return rc;
+  GP_CUDA(ctx, cudaMemsetAsync(ctx->d_ffvecs, 0, sizeof(double) * (size_t)K * nc, ctx->stream));
+  if (nk) {
+    int b2 = (int)(((int64_t)nk * K + 255) / 256);
+    if (b2 > ctx->num_sms * 16) b2 = ctx->num_sms * 16;
+    k_scatter_ffvecs<<<b2, 256, 0, ctx->stream>>>(ctx->d_ffvecs, d_ffvT, ctx->d_kept, nk, nc, K);
+    GP_LAUNCH_CHECK(ctx, "k_scatter_ffvecs");
+  }
+  /* fxvecs^T[i][j] = xrow_i . ffvecs_j  (fixxrow values) */
+  rc = gp_geno_gemm_f64(ctx, 1, ctx->d_rows, n, kt.snprec, kt.rt, nk, d_ffvT, K, K, d_fxT, K);
+  if (rc) return rc;
+  std::vector<double> fx((size_t)n * K);
+  GP_CUDA(ctx, cudaMemcpyAsync(fx.data(), d_fxT, sizeof(double) * fx.size(),
+                               cudaMemcpyDeviceToHost, ctx->stream));
+  if (ffvecs)
+    GP_CUDA(ctx, cudaMemcpyAsync(ffvecs, ctx->d_ffvecs, sizeof(double) * (size_t)K * nc,
+                                 cudaMemcpyDeviceToHost, ctx->stream));
+  GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  /* fxscal_j = 1/sqrt(sum_i fxvecs^2) in row order (smartpca.c:1504-1525) */
+  for (int32_t j = 0; j < K; ++j) {
+    double s = 0.0;
+    for (int32_t i = 0; i < n; ++i) {
+      double y = fx[(size_t)i * K + j];
+      if (fxvecs) fxvecs[(size_t)j * n + i] = y;
+      s += y * y;
+    }
+    fxscal[j] = 1.0 / sqrt(s);
+  }
+  GP_CUDA(ctx, cudaMemcpyAsync(ctx->d_fxscal, fxscal, sizeof(double) * K, cudaMemcpyHostToDevice,
+                               ctx->stream));
+  GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  ctx->nweights = K;
+  ctx->weights_valid = 1;
+  return GP_OK;
+}
+
+/* ------------------------------------------------------------------------------------ */
+
+/* E[k*K + j] = fxscal_j * ffvecs_j[kept k];  P[k*ldp + pair(a,b)] = E_a E_b (a<=b), then 1 */
+__global__ void k_build_EP(const double *ffvecs, const double *fxscal, const int32_t *kept,
+                           int32_t nkept, int32_t ncols, int32_t K, double *E, double *P,
+                           int32_t ldp)
+{
+  for (int32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nkept; k += gridDim.x * blockDim.x) {
+    int32_t c = kept[k];
+    double e[64];
+    for (int j = 0; j < K; ++j) {
+      e[j] = fxscal[j] * ffvecs[(int64_t)j * ncols + c];
+      E[(int64_t)k * K + j] = e[j];
+    }
+    double *p = P + (int64_t)k * ldp;
+    int t = 0;
+    for (int a = 0; a < K; ++a)
+      for (int b = a; b < K; ++b) p[t++] = e[a] * e[b];
+    p[t] = 1.0;
+  }
+}
+
+/*
+ * Per sample: assemble co (K x K) from the pair sums, check NaN, Cholesky (choldc
+ * src/nicksrc/linsubs.c:361-380) and the two triangular solves (cholsl :331-358), with the
+ * reference's loop order and no contraction.  One thread per sample.
+ */
+__global__ void k_lsq_solve(const double *co, int32_t ldco, const double *rr, int32_t K,
+                            int32_t nproj, double *acoef, double *bcoef, int32_t *nobs,
+                            int32_t *status, double *work)
+{
+  for (int32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nproj;
+       q += gridDim.x * blockDim.x) {
+    double *a = work + (int64_t)q * (K * K + 2 * K);
+    double *p = a + K * K, *x = p + K;
+    const double *cq = co + (int64_t)q * ldco;
+    const double *rq = rr + (int64_t)q * K;
+    int32_t nob = (int32_t)llrint(cq[K * (K + 1) / 2]);
+    nobs[q] = nob;
+    for (int j = 0; j < K; ++j) bcoef[(int64_t)j * nproj + q] = rq[j];
+    if (nob <= K) {
+      status[q] = 1;
+      continue;
+    }
+    int t = 0, bad = 0;
+    for (int i = 0; i < K; ++i)
+      for (int j = i; j < K; ++j) {
+        double v = cq[t++];
+        a[i * K + j] = v;
+        a[j * K + i] = v;
+        if (isnan(v)) bad = 1;
+      }
+    for (int j = 0; j < K; ++j)
+      if (isnan(rq[j])) bad = 1;
+    if (!bad) {
+      for (int i = 0; i < K && !bad; ++i) {
+        for (int j = i; j < K; ++j) {
+          double sum = a[i * K + j];
+          for (int k = i - 1; k >= 0; --k) sum = __dsub_rn(sum, __dmul_rn(a[i * K + k], a[j * K + k]));
+          if (i == j) {
+            if (sum <= 0.0) {
+              bad = 1;
+              break;
+            }
+            p[i] = __dsqrt_rn(sum);
+          } else {
+            a[j * K + i] = __ddiv_rn(sum, p[i]);
+          }
+        }
+      }
+    }
+    if (bad) {
+      status[q] = 2;
+      continue;
+    }
+    for (int i = 0; i < K; ++i) {
+      double sum = rq[i];
+      for (int k = i - 1; k >= 0; --k) sum = __dsub_rn(sum, __dmul_rn(a[i * K + k], x[k]));
+      x[i] = __ddiv_rn(sum, p[i]);
+    }
+    for (int i = K - 1; i >= 0; --i) {
+      double sum = x[i];
+      for (int k = i + 1; k < K; ++k) sum = __dsub_rn(sum, __dmul_rn(a[k * K + i], x[k]));
+      x[i] = __ddiv_rn(sum, p[i]);
+    }
+    for (int j = 0; j < K; ++j) acoef[(int64_t)j * nproj + q] = x[j];
+    status[q] = 0;
+  }
+}
+
+extern "C" int gp_lsqproj(gp_ctx *ctx, int32_t numeigs, const int32_t *samples, int32_t nproj,
+                          double *acoeffs, double *bcoeffs, int32_t *nobs, int32_t *status)
+{
+  if (!ctx || !acoeffs || (nproj > 0 && !samples)) return GP_ERR_ARG;
+  if (!ctx->weights_valid)
+    return gp_fail(ctx, GP_ERR_STATE, "gp_lsqproj: call gp_snp_weights first");
+  if (numeigs < 1 || numeigs > ctx->nweights || numeigs > 64)
+    return gp_fail(ctx, GP_ERR_ARG, "gp_lsqproj: numeigs %d out of range", numeigs);
+  if (nproj == 0) return GP_OK;
+  for (int32_t q = 0; q < nproj; ++q)
+    if (samples[q] < 0 || samples[q] >= ctx->nind_all)
+      return gp_fail(ctx, GP_ERR_ARG, "gp_lsqproj: sample %d out of range", samples[q]);
+  GP_CUDA(ctx, cudaSetDevice(ctx->device));
+  const int32_t K = numeigs, nk = ctx->nkept, nc = ctx->ncols;
+  const int32_t npair = K * (K + 1) / 2, ldp = npair + 1;
+  size_t off_tab = kept_tables_bytes(nk);
+  size_t nE = (size_t)nk * K, nP = (size_t)nk * ldp;
+  size_t nco = (size_t)nproj * ldp, nrr = (size_t)nproj * K;
+  size_t nwork = (size_t)nproj * (K * K + 2 * K);
+  size_t bytes = off_tab + sizeof(double) * (nE + nP + nco + nrr + nwork + 2 * nrr) +
+                 sizeof(int32_t) * (3 * (size_t)nproj) + 1024;
+  uint8_t *base;
+  int rc = gp_scratch(ctx, bytes, (void **)&base);
+  if (rc) return rc;
+  kept_tables kt;
+  rc = build_kept_tables(ctx, base, &kt);
+  if (rc) return rc;
+  double *d_E = (double *)(base + off_tab);
+  double *d_P = d_E + nE, *d_co = d_P + nP, *d_rr = d_co + nco, *d_work = d_rr + nrr;
+  double *d_a = d_work + nwork, *d_b = d_a + nrr;
+  int32_t *d_samp = (int32_t *)(d_b + nrr), *d_nobs = d_samp + nproj, *d_st = d_nobs + nproj;
+  GP_CUDA(ctx, cudaMemcpyAsync(d_samp, samples, sizeof(int32_t) * (size_t)nproj,
+                               cudaMemcpyHostToDevice, ctx->stream));
+  if (nk) {
+    int blocks = (nk + 127) / 128;
+    if (blocks > ctx->num_sms * 8) blocks = ctx->num_sms * 8;
+    k_build_EP<<<blocks, 128, 0, ctx->stream>>>(ctx->d_ffvecs, ctx->d_fxscal, ctx->d_kept, nk, nc,
+                                                K, d_E, d_P, ldp);
+    GP_LAUNCH_CHECK(ctx, "k_build_EP");
+  }
+  /* masked normal equations: co = O P (pair sums + observed count), rr = R E */
+  rc = gp_geno_gemm_f64(ctx, 1, d_samp, nproj, kt.snprec, kt.ot, nk, d_P, ldp, ldp, d_co, ldp);
+  if (rc) return rc;
+  rc = gp_geno_gemm_f64(ctx, 1, d_samp, nproj, kt.snprec, kt.rt, nk, d_E, K, K, d_rr, K);
+  if (rc) return rc;
+  GP_CUDA(ctx, cudaMemsetAsync(d_a, 0, sizeof(double) * nrr, ctx->stream));
+  int blocks = (nproj + 127) / 128;
+  k_lsq_solve<<<blocks, 128, 0, ctx->stream>>>(d_co, ldp, d_rr, K, nproj, d_a, d_b, d_nobs, d_st,
+                                               d_work);
+  GP_LAUNCH_CHECK(ctx, "k_lsq_solve");
+  std::vector<int32_t> st((size_t)nproj);
+  std::vector<double> ha(nrr);
+  GP_CUDA(ctx, cudaMemcpyAsync(ha.data(), d_a, sizeof(double) * nrr, cudaMemcpyDeviceToHost,
+                               ctx->stream));
+  GP_CUDA(ctx, cudaMemcpyAsync(st.data(), d_st, sizeof(int32_t) * (size_t)nproj,
+                               cudaMemcpyDeviceToHost, ctx->stream));
+  if (bcoeffs)
+    GP_CUDA(ctx, cudaMemcpyAsync(bcoeffs, d_b, sizeof(double) * nrr, cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+  if (nobs)
+    GP_CUDA(ctx, cudaMemcpyAsync(nobs, d_nobs, sizeof(int32_t) * (size_t)nproj,
+                                 cudaMemcpyDeviceToHost, ctx->stream));
+  GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  for (int32_t q = 0; q < nproj; ++q) {
+    if (status) status[q] = st[(size_t)q];
+    if (st[(size_t)q] == 2) continue; /* left untouched, as the reference keeps regans */
+    for (int32_t j = 0; j < K; ++j)
+      acoeffs[(size_t)j * nproj + q] = ha[(size_t)j * nproj + q];
+  }
+  return GP_OK;
+}

@@ -1,0 +1,95 @@
+/* Internal state of a gpupca handle and helpers shared by the .cu files. */
+#ifndef GP_INTERNAL_H
+#define GP_INTERNAL_H
+
+#include <cuda_runtime.h>
+#include <cusolverDn.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#include "../../include/gpupca.h"
+
+#define GP_ERRLEN 512
+
+struct gp_ctx {
+  int device;
+  int num_sms;
+  cudaStream_t stream;
+  cusolverDnHandle_t solver;
+  char err[GP_ERRLEN];
+
+  /* genotype panel: nsnp_all records of rlen_dev bytes (packed 2-bit, MSB first) */
+  uint8_t *d_geno;
+  int64_t nsnp_all;
+  int32_t nind_all;
+  int64_t rlen_dev;  /* padded to a multiple of 16 bytes; pad bytes are 0xFF (missing) */
+
+  /* analysis rows/columns */
+  int32_t *d_rows;       /* [nrows] ascending sample indices */
+  uint32_t *d_rowmask;   /* [rlen_dev/4] 2-bit selection mask (0b11 per selected sample) */
+  int32_t nrows;
+  int32_t *d_cols;       /* [ncols] SNP indices into the records */
+  int32_t ncols;
+
+  /* per-column state of the last gp_xtx */
+  int32_t *d_cnt;        /* [3*ncols]: n0, n1, nmiss */
+  uint8_t *d_killed;     /* [ncols] */
+  double *d_vtab;        /* [4*ncols]: value of code 0,1,2,3(missing)=0 */
+  double *d_xmean;       /* [ncols] */
+  double *d_xfancy;      /* [ncols] */
+  int32_t *d_kept;       /* [ncols] compacted list of kept columns (positions in cols) */
+  int32_t nkept;
+  int xtx_valid;
+  double trace;        /* unscaled trace of the last Gram */
+
+  /* Gram and eigen state */
+  double *d_xtx;         /* [nrows*nrows] */
+  int64_t xtx_cap;
+  double *d_evals;       /* [nrows] */
+  double *d_evecs;       /* [nvec*nrows] top vectors, descending */
+  int32_t nvec;
+  int eig_valid;
+
+  /* weights */
+  double *d_ffvecs;      /* [nvec*ncols] */
+  double *d_fxscal;      /* [nvec] */
+  int weights_valid;
+  int32_t nweights;
+
+  /* scratch arena (grows on demand, freed at close) */
+  void *d_scratch;
+  size_t scratch_cap;
+  void *d_scratch2;
+  size_t scratch2_cap;
+};
+
+int gp_fail(gp_ctx *ctx, int code, const char *fmt, ...);
+int gp_cuda_fail(gp_ctx *ctx, cudaError_t e, const char *what);
+int gp_scratch(gp_ctx *ctx, size_t bytes, void **out);
+int gp_scratch2(gp_ctx *ctx, size_t bytes, void **out);
+int gp_realloc(gp_ctx *ctx, void **ptr, size_t bytes);
+
+#define GP_CUDA(ctx, call)                                   \
+  do {                                                       \
+    cudaError_t _e = (call);                                 \
+    if (_e != cudaSuccess) return gp_cuda_fail(ctx, _e, #call); \
+  } while (0)
+
+#define GP_LAUNCH_CHECK(ctx, what)                          \
+  do {                                                       \
+    cudaError_t _e = cudaGetLastError();                     \
+    if (_e != cudaSuccess) return gp_cuda_fail(ctx, _e, what); \
+  } while (0)
+
+/* kernels, by file */
+int gp_launch_valid_counts(gp_ctx *ctx, const uint8_t *d_sample_use, const uint8_t *d_snp_use,
+                           int32_t *d_snp_valid, int32_t *d_sample_valid);
+int gp_launch_snp_stats(gp_ctx *ctx, const gp_xtx_opts *o);
+int gp_gram_fp64(gp_ctx *ctx);
+int gp_gram_split_bf16(gp_ctx *ctx);
+int gp_launch_symmetrize_trace(gp_ctx *ctx, double *d_trace);
+int gp_launch_materialize_f64(gp_ctx *ctx, int32_t k0, int32_t kc, int32_t pitch, double *d_x,
+                              double scale);
+
+#endif

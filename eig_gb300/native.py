@@ -1,0 +1,377 @@
+"""ctypes binding of the gpupca C ABI (include/gpupca.h, include/gpupca_run.h).
+
+This is the Python-side caller of the same entry points the drop-in CLI uses.  Loading
+fails loudly when the CUDA library has not been built: there is no CPU fallback.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_DIR = os.path.join(_HERE, "_lib")
+LIB_PATH = os.path.join(LIB_DIR, "libgpupca.so")
+SYNTH_PATH = os.path.join(LIB_DIR, "libgpsynth.so")
+
+GP_OK = 0
+GP_ERR = {-1: "GP_ERR_ARG", -2: "GP_ERR_CUDA", -3: "GP_ERR_NOMEM", -4: "GP_ERR_STATE",
+          -5: "GP_ERR_SOLVER", -6: "GP_ERR_NODATA", -7: "GP_ERR_TIMEOUT", -8: "GP_ERR_FULL",
+          -9: "GP_ERR_NOTBUILT"}
+GP_CODE_PACKED, GP_CODE_BED = 0, 1
+GP_PREC_FP64, GP_PREC_SPLIT_BF16 = 0, 1
+PHASES = ["load", "filter", "gram", "eig", "outlier", "weights", "lsqproj", "total"]
+
+# every symbol the headers declare (checked by the CPU test suite)
+EXPORTED = ["gp_version", "gp_last_error", "gp_open", "gp_close", "gp_device_bytes",
+            "gp_load_genotypes", "gp_set_missing", "gp_valid_counts", "gp_set_samples",
+            "gp_set_snps", "gp_xtx", "gp_eigvecs", "gp_ridoutlier", "gp_snp_weights",
+            "gp_lsqproj", "gp_fastpca", "gp_smartpca_defaults", "gp_smartpca_run",
+            "gp_fail_msg"]
+
+i32p = C.POINTER(C.c_int32)
+i64p = C.POINTER(C.c_int64)
+u8p = C.POINTER(C.c_uint8)
+f64p = C.POINTER(C.c_double)
+vp = C.c_void_p
+
+
+class XtxOpts(C.Structure):
+    _fields_ = [("fancynorm", C.c_int32), ("altnormstyle", C.c_int32),
+                ("minallelecnt", C.c_int32), ("maxmissing", C.c_int32),
+                ("precision", C.c_int32)]
+
+
+class SmartpcaOpts(C.Structure):
+    _fields_ = [("numeigs", C.c_int32), ("numoutliter", C.c_int32), ("numoutleigs", C.c_int32),
+                ("outlthresh", C.c_double), ("outliermode", C.c_int32),
+                ("fancynorm", C.c_int32), ("altnormstyle", C.c_int32),
+                ("minallelecnt", C.c_int32), ("maxmissing", C.c_int32),
+                ("lsqproject", C.c_int32), ("noxdata", C.c_int32), ("numchrom", C.c_int32),
+                ("precision", C.c_int32), ("fastmode", C.c_int32), ("fastdim", C.c_int32),
+                ("fastiter", C.c_int32), ("seed", C.c_int64)]
+
+
+class Panel(C.Structure):
+    _fields_ = [("records", u8p), ("record_bytes", C.c_int64), ("nsnp", C.c_int64),
+                ("nind", C.c_int32), ("code", C.c_int32), ("snp_chrom", i32p),
+                ("snp_ignore", u8p), ("ind_ignore", u8p), ("ind_affstatus", u8p),
+                ("ind_male", u8p)]
+
+
+class RunResult(C.Structure):
+    _fields_ = [("xindex", i32p), ("evals", f64p), ("evecs", f64p), ("coords", f64p),
+                ("ind_out", u8p), ("snp_state", u8p), ("outlier_idx", i32p),
+                ("outlier_iter", i32p), ("outlier_vec", i32p), ("outlier_score", f64p),
+                ("nrows", C.c_int32), ("ncols", C.c_int32), ("numeigs", C.c_int32),
+                ("noutliers", C.c_int32), ("npasses", C.c_int32),
+                ("t_phase", C.c_double * 8)]
+
+
+_lib = None
+_synth = None
+
+
+def load_library():
+    """Load libgpupca.so (raises if it is missing: the CUDA path is mandatory)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError("libgpupca.so is not built (%s); run __graft_entry__.build()" % LIB_PATH)
+    lib = C.CDLL(LIB_PATH)
+    sig = {
+        "gp_version": (C.c_int, []),
+        "gp_last_error": (C.c_char_p, [vp]),
+        "gp_open": (C.c_int, [C.c_int, C.POINTER(vp)]),
+        "gp_close": (None, [vp]),
+        "gp_device_bytes": (C.c_int, [vp, i64p]),
+        "gp_load_genotypes": (C.c_int, [vp, u8p, C.c_int64, C.c_int64, C.c_int32, C.c_int32]),
+        "gp_set_missing": (C.c_int, [vp, i64p, C.c_int64]),
+        "gp_valid_counts": (C.c_int, [vp, u8p, u8p, i32p, i32p]),
+        "gp_set_samples": (C.c_int, [vp, i32p, C.c_int32]),
+        "gp_set_snps": (C.c_int, [vp, i32p, C.c_int32]),
+        "gp_xtx": (C.c_int, [vp, C.POINTER(XtxOpts), i32p, i32p, i32p, u8p, f64p, f64p, f64p,
+                             f64p, i32p]),
+        "gp_eigvecs": (C.c_int, [vp, C.c_int32, f64p, f64p]),
+        "gp_ridoutlier": (C.c_int, [f64p, C.c_int32, C.c_int32, C.c_double, C.c_int32, i32p,
+                                    i32p, f64p]),
+        "gp_snp_weights": (C.c_int, [vp, C.c_int32, f64p, f64p, f64p]),
+        "gp_lsqproj": (C.c_int, [vp, C.c_int32, i32p, C.c_int32, f64p, f64p, i32p, i32p]),
+        "gp_fastpca": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, f64p,
+                                 C.c_int32, f64p, f64p]),
+        "gp_smartpca_defaults": (None, [C.POINTER(SmartpcaOpts)]),
+        "gp_smartpca_run": (C.c_int, [vp, C.POINTER(SmartpcaOpts), C.POINTER(Panel),
+                                      C.POINTER(RunResult)]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def load_synth():
+    global _synth
+    if _synth is not None:
+        return _synth
+    if not os.path.exists(SYNTH_PATH):
+        raise RuntimeError("libgpsynth.so is not built; run __graft_entry__.build()")
+    s = C.CDLL(SYNTH_PATH)
+    s.gp_packed_rlen.restype = C.c_int64
+    s.gp_packed_rlen.argtypes = [C.c_int32]
+    s.gp_synth_records.restype = C.c_int
+    s.gp_synth_records.argtypes = [vp, u8p, C.c_int64, i32p, C.c_int]
+    s.gp_synth_write_dataset.restype = C.c_int
+    s.gp_synth_write_dataset.argtypes = [vp, C.c_char_p, C.c_int]
+    s.gp_hash_string.restype = C.c_int32
+    s.gp_hash_string.argtypes = [C.c_char_p]
+    _synth = s
+    return s
+
+
+def ptr(a, ctype):
+    if a is None:
+        return None
+    assert a.flags["C_CONTIGUOUS"], "array must be C-contiguous"
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+class GpuError(RuntimeError):
+    pass
+
+
+class Handle:
+    """One gpupca handle (its own CUDA stream) on device `device`."""
+
+    def __init__(self, device=0):
+        self.lib = load_library()
+        h = vp()
+        rc = self.lib.gp_open(device, C.byref(h))
+        if rc != GP_OK:
+            raise GpuError("gp_open: %s (%s)" % (GP_ERR.get(rc, rc),
+                                                 self.lib.gp_last_error(None).decode()))
+        self.h = h
+
+    def check(self, rc, what):
+        if rc < 0:
+            msg = self.lib.gp_last_error(self.h).decode(errors="replace")
+            raise GpuError("%s: %s: %s" % (what, GP_ERR.get(rc, rc), msg))
+        return rc
+
+    def close(self):
+        if self.h:
+            self.lib.gp_close(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- entry points -----------------------------------------------------------------
+    def load_genotypes(self, records, nind, code=GP_CODE_PACKED):
+        records = np.ascontiguousarray(records, dtype=np.uint8)
+        nsnp, rb = records.shape
+        self.check(self.lib.gp_load_genotypes(self.h, ptr(records, C.c_uint8), rb, nsnp, nind,
+                                              code), "gp_load_genotypes")
+        self.nind, self.nsnp = nind, nsnp
+
+    def set_missing(self, pairs):
+        pairs = np.ascontiguousarray(pairs, dtype=np.int64).reshape(-1, 2)
+        self.check(self.lib.gp_set_missing(self.h, ptr(pairs, C.c_int64), len(pairs)),
+                   "gp_set_missing")
+
+    def valid_counts(self, sample_use=None, snp_use=None):
+        su = None if sample_use is None else np.ascontiguousarray(sample_use, dtype=np.uint8)
+        pu = None if snp_use is None else np.ascontiguousarray(snp_use, dtype=np.uint8)
+        sv = np.zeros(self.nsnp, np.int32)
+        iv = np.zeros(self.nind, np.int32)
+        self.check(self.lib.gp_valid_counts(self.h, ptr(su, C.c_uint8), ptr(pu, C.c_uint8),
+                                            ptr(sv, C.c_int32), ptr(iv, C.c_int32)),
+                   "gp_valid_counts")
+        return sv, iv
+
+    def set_samples(self, xindex):
+        x = np.ascontiguousarray(xindex, dtype=np.int32)
+        self.check(self.lib.gp_set_samples(self.h, ptr(x, C.c_int32), len(x)), "gp_set_samples")
+        self.nrows = len(x)
+
+    def set_snps(self, cols):
+        c = np.ascontiguousarray(cols, dtype=np.int32)
+        self.check(self.lib.gp_set_snps(self.h, ptr(c, C.c_int32), len(c)), "gp_set_snps")
+        self.ncols = len(c)
+
+    def xtx(self, precision=GP_PREC_FP64, fancynorm=1, altnormstyle=1, minallelecnt=1,
+            maxmissing=9999999, want_xtx=True):
+        o = XtxOpts(fancynorm, altnormstyle, minallelecnt, maxmissing, precision)
+        nc, n = self.ncols, self.nrows
+        n0 = np.zeros(nc, np.int32)
+        n1 = np.zeros(nc, np.int32)
+        nm = np.zeros(nc, np.int32)
+        kl = np.zeros(nc, np.uint8)
+        xm = np.zeros(nc)
+        xf = np.zeros(nc)
+        X = np.zeros((n, n)) if want_xtx else None
+        tr = C.c_double()
+        nu = C.c_int32()
+        self.check(self.lib.gp_xtx(self.h, C.byref(o), ptr(n0, C.c_int32), ptr(n1, C.c_int32),
+                                   ptr(nm, C.c_int32), ptr(kl, C.c_uint8), ptr(xm, C.c_double),
+                                   ptr(xf, C.c_double), ptr(X, C.c_double), C.byref(tr),
+                                   C.byref(nu)), "gp_xtx")
+        return dict(n0=n0, n1=n1, nmiss=nm, killed=kl, xmean=xm, xfancy=xf, XTX=X,
+                    trace=tr.value, nused=nu.value)
+
+    def eigvecs(self, nvec):
+        n = self.nrows
+        ev = np.zeros(n)
+        V = np.zeros((nvec, n))
+        self.check(self.lib.gp_eigvecs(self.h, nvec, ptr(ev, C.c_double), ptr(V, C.c_double)),
+                   "gp_eigvecs")
+        return ev, V
+
+    def snp_weights(self, numeigs):
+        ff = np.zeros((numeigs, self.ncols))
+        fx = np.zeros((numeigs, self.nrows))
+        sc = np.zeros(numeigs)
+        self.check(self.lib.gp_snp_weights(self.h, numeigs, ptr(ff, C.c_double),
+                                           ptr(fx, C.c_double), ptr(sc, C.c_double)),
+                   "gp_snp_weights")
+        return ff, fx, sc
+
+    def lsqproj(self, numeigs, samples):
+        s = np.ascontiguousarray(samples, dtype=np.int32)
+        q = len(s)
+        a = np.zeros((numeigs, q))
+        b = np.zeros((numeigs, q))
+        nobs = np.zeros(q, np.int32)
+        st = np.zeros(q, np.int32)
+        self.check(self.lib.gp_lsqproj(self.h, numeigs, ptr(s, C.c_int32), q, ptr(a, C.c_double),
+                                       ptr(b, C.c_double), ptr(nobs, C.c_int32),
+                                       ptr(st, C.c_int32)), "gp_lsqproj")
+        return a, b, nobs, st
+
+    def fastpca(self, K, L, I, seed=0, omega=None, precision=GP_PREC_FP64):
+        n = self.nrows
+        ev = np.zeros(K)
+        V = np.zeros((K, n))
+        om = None if omega is None else np.ascontiguousarray(omega, dtype=np.float64)
+        self.check(self.lib.gp_fastpca(self.h, K, L, I, seed, ptr(om, C.c_double), precision,
+                                       ptr(ev, C.c_double), ptr(V, C.c_double)), "gp_fastpca")
+        return ev, V
+
+
+def ridoutlier(evecs, neigs, thresh=6.0, mode=0):
+    lib = load_library()
+    E = np.ascontiguousarray(evecs, dtype=np.float64)
+    n = E.shape[1]
+    bad = np.zeros(n, np.int32)
+    vec = np.zeros(n, np.int32)
+    sc = np.zeros(n)
+    nb = lib.gp_ridoutlier(ptr(E, C.c_double), n, neigs, thresh, mode, ptr(bad, C.c_int32),
+                           ptr(vec, C.c_int32), ptr(sc, C.c_double))
+    if nb < 0:
+        raise GpuError("gp_ridoutlier: %s" % GP_ERR.get(nb, nb))
+    return bad[:nb], vec, sc
+
+
+def default_opts(**kw):
+    lib = load_library()
+    o = SmartpcaOpts()
+    lib.gp_smartpca_defaults(C.byref(o))
+    for k, v in kw.items():
+        if not hasattr(o, k):
+            raise KeyError(k)
+        setattr(o, k, v)
+    return o
+
+
+def smartpca_run(handle, records, nind, opts, code=GP_CODE_PACKED, snp_chrom=None,
+                 snp_ignore=None, ind_ignore=None, ind_affstatus=None, ind_male=None):
+    """Run the whole smartpca hot path (gp_smartpca_run) on in-memory records."""
+    lib = handle.lib
+    rec = np.ascontiguousarray(records, dtype=np.uint8)
+    nsnp, rb = rec.shape
+    keep = []
+
+    def arr(a, dt):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(a, dtype=dt)
+        keep.append(a)
+        return a
+
+    chrom = arr(snp_chrom, np.int32)
+    p = Panel(ptr(rec, C.c_uint8), rb, nsnp, nind, code, ptr(chrom, C.c_int32),
+              ptr(arr(snp_ignore, np.uint8), C.c_uint8), ptr(arr(ind_ignore, np.uint8), C.c_uint8),
+              ptr(arr(ind_affstatus, np.uint8), C.c_uint8), ptr(arr(ind_male, np.uint8), C.c_uint8))
+    K = max(opts.numeigs, 1)
+    out = dict(xindex=np.zeros(nind, np.int32), evals=np.zeros(nind), evecs=np.zeros(K * nind),
+               coords=np.zeros(K * nind), ind_out=np.zeros(nind, np.uint8),
+               snp_state=np.zeros(nsnp, np.uint8), outlier_idx=np.zeros(nind, np.int32),
+               outlier_iter=np.zeros(nind, np.int32), outlier_vec=np.zeros(nind, np.int32),
+               outlier_score=np.zeros(nind))
+    r = RunResult(ptr(out["xindex"], C.c_int32), ptr(out["evals"], C.c_double),
+                  ptr(out["evecs"], C.c_double), ptr(out["coords"], C.c_double),
+                  ptr(out["ind_out"], C.c_uint8), ptr(out["snp_state"], C.c_uint8),
+                  ptr(out["outlier_idx"], C.c_int32), ptr(out["outlier_iter"], C.c_int32),
+                  ptr(out["outlier_vec"], C.c_int32), ptr(out["outlier_score"], C.c_double))
+    handle.check(lib.gp_smartpca_run(handle.h, C.byref(opts), C.byref(p), C.byref(r)),
+                 "gp_smartpca_run")
+    n, k = r.nrows, r.numeigs
+    res = dict(nrows=n, ncols=r.ncols, numeigs=k, npasses=r.npasses,
+               xindex=out["xindex"][:n].copy(),
+               evals=out["evals"][: (k if opts.fastmode else n)].copy(),
+               evecs=out["evecs"][: k * n].reshape(k, n).copy(),
+               coords=out["coords"][: k * nind].reshape(k, nind).copy(),
+               ind_out=out["ind_out"].astype(bool), snp_state=out["snp_state"],
+               outliers=[(int(out["outlier_idx"][i]), int(out["outlier_iter"][i]),
+                          int(out["outlier_vec"][i]), float(out["outlier_score"][i]))
+                         for i in range(min(r.noutliers, nind))],
+               t_phase={PHASES[i]: r.t_phase[i] for i in range(8)})
+    return res
+
+
+class SynthSpec(C.Structure):
+    _fields_ = [("nsnp", C.c_int64), ("nind", C.c_int32), ("npops", C.c_int32),
+                ("pop_sizes", i32p), ("fst", f64p), ("p_lo", C.c_double), ("p_hi", C.c_double),
+                ("miss_lo", C.c_double), ("miss_hi", C.c_double), ("seed", C.c_uint64)]
+
+
+def synth_records(nsnp, pop_sizes, fst, miss=0.01, miss_hi=None, n_admixed=0, seed=1,
+                  p_lo=0.05, p_hi=0.95, nthreads=None):
+    """Seeded Balding-Nichols packed records (nsnp x rlen uint8) and per-sample labels."""
+    s = load_synth()
+    ps = np.ascontiguousarray(pop_sizes, dtype=np.int32)
+    fs = np.ascontiguousarray(fst, dtype=np.float64)
+    nind = int(ps.sum()) + int(n_admixed)
+    spec = SynthSpec(nsnp, nind, len(ps), ptr(ps, C.c_int32), ptr(fs, C.c_double), p_lo, p_hi,
+                     miss, miss if miss_hi is None else miss_hi, seed)
+    rlen = s.gp_packed_rlen(nind)
+    rec = np.zeros((nsnp, rlen), np.uint8)
+    pop = np.zeros(nind, np.int32)
+    rc = s.gp_synth_records(C.byref(spec), ptr(rec, C.c_uint8), rlen, ptr(pop, C.c_int32),
+                            nthreads or os.cpu_count() or 1)
+    if rc != 0:
+        raise RuntimeError("gp_synth_records failed: %d" % rc)
+    return rec, pop
+
+
+def synth_write_dataset(prefix, nsnp, pop_sizes, fst, miss=0.01, miss_hi=None, n_admixed=0,
+                        seed=1, p_lo=0.05, p_hi=0.95, nthreads=None):
+    s = load_synth()
+    ps = np.ascontiguousarray(pop_sizes, dtype=np.int32)
+    fs = np.ascontiguousarray(fst, dtype=np.float64)
+    nind = int(ps.sum()) + int(n_admixed)
+    spec = SynthSpec(nsnp, nind, len(ps), ptr(ps, C.c_int32), ptr(fs, C.c_double), p_lo, p_hi,
+                     miss, miss if miss_hi is None else miss_hi, seed)
+    rc = s.gp_synth_write_dataset(C.byref(spec), prefix.encode(), nthreads or os.cpu_count() or 1)
+    if rc != 0:
+        raise RuntimeError("gp_synth_write_dataset failed: %d" % rc)

@@ -1,0 +1,178 @@
+/*
+ * gpupca.h — C ABI of the GB300 (sm_103a) smartpca hot path.
+ *
+ * The reference smartpca (EIGENSOFT 8.0.0) has no plugin API: its hot path is a set of
+ * internal C functions called from main() in src/eigensrc/smartpca.c with globals as
+ * hidden parameters.  Each entry point below replaces one of them and says which
+ * (file:line in the reference).  Conventions:
+ *
+ *   * every call returns int status: GP_OK (0) or a negative GP_ERR_* code; nothing exits
+ *     the process (the reference calls fatalx/exit);  gp_last_error() has the message;
+ *   * buffers passed in and out are caller-owned HOST memory with plain C types; the
+ *     genotype panel, the Gram matrix and the eigenvectors live in device memory owned by
+ *     the handle, which does all of its work on its own CUDA stream;
+ *   * one handle is used by one host thread at a time; separate handles are independent.
+ *
+ * Genotype codes: per sample a 2-bit count of the FIRST allele 0/1/2, 3 = missing, packed
+ * four samples per byte, sample k at byte k>>2, bits (3-(k&3))*2 (packedancestrymap,
+ * src/admutils.c:718-735), or the PLINK .bed code (LSB first, 00->2, 01->missing, 10->1,
+ * 11->0, src/mcio.c:3995-4009) which is recoded on upload.
+ */
+#ifndef GPUPCA_H
+#define GPUPCA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GP_OK 0
+#define GP_ERR_ARG (-1)      /* bad argument or size */
+#define GP_ERR_CUDA (-2)     /* CUDA runtime / launch failure */
+#define GP_ERR_NOMEM (-3)    /* device or host allocation failed */
+#define GP_ERR_STATE (-4)    /* call out of order (e.g. no genotypes loaded) */
+#define GP_ERR_SOLVER (-5)   /* eigensolver / factorisation failure */
+#define GP_ERR_NODATA (-6)   /* zero or NaN trace: "XTX has zero trace (perhaps no data)" */
+#define GP_ERR_TIMEOUT (-7)  /* bounded device wait ran out (serving loop) */
+#define GP_ERR_FULL (-8)     /* serving: no slot or memory free for the request */
+#define GP_ERR_NOTBUILT (-9) /* feature not compiled into this library */
+
+#define GP_CODE_PACKED 0     /* packedancestrymap 2-bit, MSB first, 3 = missing */
+#define GP_CODE_BED 1        /* PLINK .bed, LSB first, 01 = missing */
+
+#define GP_PREC_FP64 0       /* plain FP64 Gram: the drop-in */
+#define GP_PREC_SPLIT_BF16 1 /* hi+lo BF16 tcgen05 MMAs, FP32 in a SNP tile, FP64 across */
+
+typedef struct gp_ctx gp_ctx;
+
+/* Library version (major*10000 + minor*100 + patch) and the last error text of a handle
+ * (or of the last failed gp_open when ctx is NULL). */
+int gp_version(void);
+const char *gp_last_error(const gp_ctx *ctx);
+
+/* Open a handle on CUDA device `device` (creates its stream and solver handles). */
+int gp_open(int device, gp_ctx **out);
+void gp_close(gp_ctx *ctx);
+
+/* Device memory the handle currently holds, in bytes. */
+int gp_device_bytes(const gp_ctx *ctx, int64_t *bytes);
+
+/*
+ * Upload the genotype panel: nsnp records of record_bytes bytes, SNP-major, in the order
+ * of the caller's SNP list (after the reference's (chrom, genpos, physpos) sort), nind
+ * samples each.  Replaces reading packgenos into cupt->pbuff (inpack src/mcio.c:2769-2865)
+ * and the BED re-encode (getbedgenos src/mcio.c:3893-3992).  Invalidates earlier sample and
+ * SNP selections.
+ */
+int gp_load_genotypes(gp_ctx *ctx, const uint8_t *records, int64_t record_bytes,
+                      int64_t nsnp, int32_t nind, int32_t code);
+
+/*
+ * Set a genotype to missing in the device panel (the male-X-het rule, checkxval
+ * src/mcio.c:1606-1619, applied by putgtypes(cupt, k, -1) in inpack :2856-2863).
+ * pairs = npairs (snp, sample) index pairs.
+ */
+int gp_set_missing(gp_ctx *ctx, const int64_t *pairs, int64_t npairs);
+
+/*
+ * Valid-genotype counts used by the reference's pre-filters: per SNP over the samples with
+ * sample_use[k] != 0 (numvalidgtx src/admutils.c:1136, numvalidgt :1118), and per sample over
+ * the SNPs with snp_use[s] != 0 (numvalidgtallind :1075).  Either output may be NULL.
+ */
+int gp_valid_counts(gp_ctx *ctx, const uint8_t *sample_use, const uint8_t *snp_use,
+                    int32_t *snp_valid, int32_t *sample_valid);
+
+/* The rows of the analysis: ascending sample indices (loadindx src/qpsubs.c:202). */
+int gp_set_samples(gp_ctx *ctx, const int32_t *xindex, int32_t nrows);
+
+/* The columns of the analysis: SNP indices into the loaded records (loadsnpx
+ * src/qpsubs.c:222). */
+int gp_set_snps(gp_ctx *ctx, const int32_t *snp_index, int32_t ncols);
+
+typedef struct {
+  int32_t fancynorm;    /* usenorm / fancynorm (default 1): divide by sqrt(p(1-p)) */
+  int32_t altnormstyle; /* altnormstyle (default 1): p = mean/2, else (c0+1)/(2n+2) */
+  int32_t minallelecnt; /* default 1 */
+  int32_t maxmissing;   /* default 9999999 */
+  int32_t precision;    /* GP_PREC_FP64 or GP_PREC_SPLIT_BF16 */
+} gp_xtx_opts;
+
+/*
+ * One Gram pass of the outlier loop over the current rows and columns.  Per selected SNP:
+ * counts n0 = sum g, n1 = sum (2-g), nmiss over the rows (getcolxz_binary1
+ * src/eigensrc/smartpca.c:3219-3301), the kill rule min(n0,n1) < minallelecnt,
+ * nmiss > maxmissing, min == 0 or no data (:1131-1144), the normalised value table
+ * (fvadjust_binary :2282-2313), then XTX = sum over kept SNPs of v v^T
+ * (domult_increment_lookup :3426 / domult_increment_normal :3531, symit2 :480).
+ * Outputs (host, may be NULL): n0, n1, nmiss, killed [ncols]; xmean = mean*fancy and
+ * xfancy = fancy [ncols] (zero for a SNP with no data, as the reference);
+ * XTX [nrows*nrows] full symmetric (unscaled); trace (unscaled); nused = kept SNPs.
+ * The Gram stays resident in device memory for gp_eigvecs.
+ */
+int gp_xtx(gp_ctx *ctx, const gp_xtx_opts *opts, int32_t *n0, int32_t *n1, int32_t *nmiss,
+           uint8_t *killed, double *xmean, double *xfancy, double *XTX, double *trace,
+           int32_t *nused);
+
+/*
+ * Scale the resident Gram by (nrows-1)/trace (smartpca.c:1230-1236) and solve the dense
+ * symmetric eigenproblem in FP64 on the device (eigvecs src/eigensrc/eigsubs.c:39-55 ->
+ * dspev).  evals [nrows] all eigenvalues in descending order; evecs [nvec*nrows] the top
+ * nvec eigenvectors, eigenvector j at evecs[j*nrows] with unit norm (sign is arbitrary, as
+ * with LAPACK).  Either output may be NULL; the top nvec vectors stay resident for
+ * gp_snp_weights.
+ */
+int gp_eigvecs(gp_ctx *ctx, int32_t nvec, double *evals, double *evecs);
+
+/*
+ * Outlier z-scores (ridoutlier src/eigensrc/smartsubs.c:18-91), a host function: for each
+ * of the first neigs eigenvectors (evecs[i*n..]) z = (v - mean)/sd with sd over n; mode 0
+ * flags |z| > thresh, mode 1 is the leave-one-out variant, mode >= 2 flags nothing.
+ * badlist receives the flagged rows ascending; vecno/score the first eigenvector that
+ * flagged each row (may be NULL, size n).  Returns the number flagged (>= 0) or an error.
+ */
+int gp_ridoutlier(const double *evecs, int32_t n, int32_t neigs, double thresh, int32_t mode,
+                  int32_t *badlist, int32_t *vecno, double *score);
+
+/*
+ * SNP weights and sample scores after the last pass (smartpca.c:1485-1525): with
+ * fvecs = 10*evecs (setfvecs src/qpsubs.c:489), ffvecs[j*ncols+s] = sum_k fvecs_j[k] x_s[k]
+ * over the rows (killed SNPs give 0), fxvecs[j*nrows+i] = xrow_i . ffvecs_j (fixxrow
+ * src/qpsubs.c:338) and fxscal[j] = 1/sqrt(sum_i fxvecs^2).  Uses the resident top
+ * eigenvectors of gp_eigvecs.  Outputs may be NULL except fxscal.
+ */
+int gp_snp_weights(gp_ctx *ctx, int32_t numeigs, double *ffvecs, double *fxvecs,
+                   double *fxscal);
+
+/*
+ * lsqproject (lsqproj src/eigensrc/smartpca.c:4606-4757 -> regressit src/regsubs.c:8 ->
+ * solvit/choldc/cholsl src/nicksrc/linsubs.c:296-380): for each listed sample, over the
+ * kept columns where it has a genotype, solve the masked normal equations
+ * (E^T E) a = E^T r with E_sj = fxscal_j ffvecs_js and r_s = g fancy_s - xmean_s by
+ * Cholesky; b_j = fxscal_j (xrow . ffvecs_j) is the orthogonal projection.
+ * samples [nproj] indices into the loaded samples; acoeffs/bcoeffs [numeigs*nproj]
+ * (coefficient j of sample q at [j*nproj+q]); nobs [nproj] observed kept SNPs;
+ * status [nproj]: 0 ok, 1 = nobs <= numeigs (sample dropped, "insufficient data"),
+ * 2 = not positive definite (acoeffs left untouched, as the reference keeps the previous
+ * regans).  Requires gp_snp_weights first.  Outputs other than acoeffs may be NULL.
+ */
+int gp_lsqproj(gp_ctx *ctx, int32_t numeigs, const int32_t *samples, int32_t nproj,
+               double *acoeffs, double *bcoeffs, int32_t *nobs, int32_t *status);
+
+/*
+ * fastmode randomized block-Krylov PCA (kjg_fpca src/ksrc/kjg_fpca.c:24-102 with the data
+ * table of setgval src/gval.c:31-87): X (ncols x nrows) holds ((g - mean) fancy)/sqrt(2),
+ * missing 0; Omega (nrows x L) Gaussian from `seed` (or the caller's omega, row-major,
+ * when not NULL); I power steps G <- X^T X G / M; Q = [X G_0 .. X G_I]; Q <- orthonormal
+ * basis; B = X^T Q; SVD(B).  evals [K] = S^2/M, evecs [K*nrows] (vector j at [j*nrows]).
+ * precision selects FP64 or split-BF16 products; orthogonalisation and Rayleigh-Ritz are
+ * FP64.
+ */
+int gp_fastpca(gp_ctx *ctx, int32_t K, int32_t L, int32_t I, uint64_t seed,
+               const double *omega, int32_t precision, double *evals, double *evecs);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GPUPCA_H */

@@ -1,0 +1,91 @@
+/*
+ * gpupca_run.h — the whole smartpca hot path as one C call (host flow in C over the entry
+ * points of gpupca.h).  Replaces the body of main() in src/eigensrc/smartpca.c from the
+ * SNP/sample pre-filters (:795-937) through the outlier loop (:1077-1265), SNP weights
+ * (:1485-1525), lsqproj + eigscale (:1549-1565) and the fastmode branch (:950-980).
+ * Reading the parfile and the genotype files, and writing .evec/.eval, stay in the CLI
+ * (gpusmartpca) so that this call works on in-memory arrays.
+ */
+#ifndef GPUPCA_RUN_H
+#define GPUPCA_RUN_H
+
+#include <stdint.h>
+
+#include "gpupca.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+  int32_t numeigs;      /* numoutevec (default 10) */
+  int32_t numoutliter;  /* numoutlieriter (5) */
+  int32_t numoutleigs;  /* numoutlierevec (10) */
+  double outlthresh;    /* outliersigmathresh (6.0) */
+  int32_t outliermode;  /* outliermode (0) */
+  int32_t fancynorm;    /* usenorm (YES) */
+  int32_t altnormstyle; /* altnormstyle (YES) */
+  int32_t minallelecnt; /* minallelecnt (1) */
+  int32_t maxmissing;   /* maxmissing (9999999) */
+  int32_t lsqproject;   /* lsqproject (YES) */
+  int32_t noxdata;      /* noxdata (YES) */
+  int32_t numchrom;     /* numchrom (22) */
+  int32_t precision;    /* GP_PREC_FP64 (drop-in) or GP_PREC_SPLIT_BF16 */
+  int32_t fastmode;     /* fastmode (NO) */
+  int32_t fastdim;      /* fastdim (-1: 2*numeigs) */
+  int32_t fastiter;     /* fastiter (-1: numeigs) */
+  int64_t seed;         /* seed (fastmode Omega) */
+} gp_smartpca_opts;
+
+typedef struct {
+  const uint8_t *records;      /* nsnp records, SNP-major, sorted SNP order */
+  int64_t record_bytes;
+  int64_t nsnp;
+  int32_t nind;
+  int32_t code;                /* GP_CODE_PACKED / GP_CODE_BED */
+  const int32_t *snp_chrom;    /* [nsnp] chromosome numbers (X = numchrom+1), NULL = all 1 */
+  const uint8_t *snp_ignore;   /* [nsnp] pre-ignored SNPs (badsnpname), may be NULL */
+  const uint8_t *ind_ignore;   /* [nind] population "Ignore", may be NULL */
+  const uint8_t *ind_affstatus;/* [nind] 1 = in a poplistname population (NULL = all) */
+  const uint8_t *ind_male;     /* [nind] 1 = gender M (male-X-het rule), may be NULL */
+} gp_panel;
+
+enum {
+  GP_PH_LOAD = 0,
+  GP_PH_FILTER = 1,
+  GP_PH_GRAM = 2,
+  GP_PH_EIG = 3,
+  GP_PH_OUTLIER = 4,
+  GP_PH_WEIGHTS = 5,
+  GP_PH_LSQ = 6,
+  GP_PH_TOTAL = 7
+};
+
+typedef struct {
+  /* caller-allocated outputs (sizes in brackets) */
+  int32_t *xindex;         /* [nind]  final PCA rows (sample indices) */
+  double *evals;           /* [nind]  eigenvalues, descending (nrows valid; K in fastmode) */
+  double *evecs;           /* [numeigs*nind] top eigenvectors over the rows, j at j*nrows */
+  double *coords;          /* [numeigs*nind] .evec coordinates, sample k of vector j at j*nind+k */
+  uint8_t *ind_out;        /* [nind]  1 = sample is written to .evec */
+  uint8_t *snp_state;      /* [nsnp]  0 used, 1 pre-filtered, 2 killed by the allele-count rule */
+  int32_t *outlier_idx;    /* [nind]  removed samples in removal order (may be NULL) */
+  int32_t *outlier_iter;   /* [nind]  outlier-loop pass (1-based) */
+  int32_t *outlier_vec;    /* [nind]  eigenvector that flagged it (0-based) */
+  double *outlier_score;   /* [nind]  its z-score */
+  /* scalar results */
+  int32_t nrows, ncols, numeigs, noutliers, npasses;
+  double t_phase[8];       /* wall seconds per GP_PH_* phase */
+} gp_run_result;
+
+void gp_smartpca_defaults(gp_smartpca_opts *o);
+int gp_smartpca_run(gp_ctx *ctx, const gp_smartpca_opts *o, const gp_panel *p,
+                    gp_run_result *r);
+
+/* set the handle's error text (used by host code layered on the ABI) and return code */
+int gp_fail_msg(gp_ctx *ctx, int code, const char *fmt, ...);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

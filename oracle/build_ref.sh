@@ -1,0 +1,58 @@
+#!/bin/sh
+# Test infrastructure only: builds the UNMODIFIED reference `smartpca` (EIGENSOFT 8.0.0,
+# DReichLab/EIG) from its own C sources where they lie, into oracle/_ref/ (git-ignored).
+# The result is used to pin the oracle restatement and to generate the golden fixtures
+# under tests/golden/.  Nothing of the product links or runs it.
+#
+# Recipe (the reference's own Makefile needs system OpenBLAS + GSL, absent here):
+#   * gcc -O2 -fcommon: globals are defined in headers (include/globals.h:4-5).
+#   * LAPACK symbols (dspev_, dpotrf_, ...) are forwarded to the scipy-bundled OpenBLAS,
+#     which exports them with a `scipy_` prefix (ref_lapack_shim.c).
+#   * fastmode (src/ksrc, needs GSL) is replaced by a stub that exits with an error.
+#   * fprintf is wrapped (-Wl,--wrap=fprintf, ref_fullprec.c): unchanged output unless
+#     EIG_REF_FULLPREC=1, in which case the .eval/.evec number formats print %.17g so that
+#     1e-10 parity can be checked.  No reference source is modified or copied.
+set -eu
+HERE=$(cd "$(dirname "$0")" && pwd)
+REF=${EIG_REFERENCE_DIR:-/root/reference}
+OUT="$HERE/_ref"
+if [ ! -d "$REF/src" ]; then
+  echo "build_ref.sh: reference sources not present ($REF); nothing to build" >&2
+  exit 0
+fi
+OPENBLAS=$(python3 - <<'EOF'
+import glob, os, scipy
+d = os.path.join(os.path.dirname(os.path.dirname(scipy.__file__)), "scipy.libs")
+libs = sorted(glob.glob(os.path.join(d, "libscipy_openblas*.so")))
+print(libs[0] if libs else "")
+EOF
+)
+if [ -z "$OPENBLAS" ]; then
+  echo "build_ref.sh: scipy-bundled OpenBLAS not found" >&2
+  exit 1
+fi
+mkdir -p "$OUT/obj"
+CFLAGS="-O2 -fcommon -w -U_FORTIFY_SOURCE -D_FORTIFY_SOURCE=0 -fno-builtin-fprintf -I$REF/include"
+SRCS="$REF/src/nicksrc/gauss.c $REF/src/nicksrc/gds.c $REF/src/nicksrc/getpars.c
+      $REF/src/nicksrc/linsubs.c $REF/src/nicksrc/sortit.c $REF/src/nicksrc/statsubs.c
+      $REF/src/nicksrc/strsubs.c $REF/src/nicksrc/vsubs.c $REF/src/nicksrc/xsearch.c
+      $REF/src/eigensrc/smartpca.c $REF/src/eigensrc/eigsubs.c $REF/src/eigensrc/exclude.c
+      $REF/src/eigensrc/smartsubs.c $REF/src/eigensrc/eigx.c
+      $REF/src/mcio.c $REF/src/qpsubs.c $REF/src/admutils.c $REF/src/egsubs.c
+      $REF/src/regsubs.c $REF/src/gval.c $REF/src/twsubs.c"
+OBJS=""
+pids=""
+for s in $SRCS; do
+  o="$OUT/obj/$(basename "$(dirname "$s")")_$(basename "$s" .c).o"
+  gcc $CFLAGS -c "$s" -o "$o" &
+  pids="$pids $!"
+  OBJS="$OBJS $o"
+done
+for p in $pids; do wait "$p"; done
+gcc -O2 -c "$HERE/ref_lapack_shim.c" -o "$OUT/obj/ref_lapack_shim.o"
+gcc -O2 -c "$HERE/ref_fullprec.c" -o "$OUT/obj/ref_fullprec.o"
+gcc -O2 -c "$HERE/ref_fastmode_stub.c" -o "$OUT/obj/ref_fastmode_stub.o"
+gcc -o "$OUT/smartpca" $OBJS "$OUT/obj/ref_lapack_shim.o" "$OUT/obj/ref_fullprec.o" \
+    "$OUT/obj/ref_fastmode_stub.o" -Wl,--wrap=fprintf \
+    "$OPENBLAS" -Wl,-rpath,"$(dirname "$OPENBLAS")" -lm -lpthread
+echo "built $OUT/smartpca"

@@ -1,0 +1,261 @@
+"""ORACLE — test infrastructure only.
+
+CPU restatement of the reference smartpca hot path (EIGENSOFT 8.0.0), used as the checker
+by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg; never imported by the
+product.  The O(N*M) loops are in oracle/smartpca_oracle.c (liboracle.so, built by
+eig_gb300/build.py); this module composes them the way main() in src/eigensrc/smartpca.c
+does, with numpy/LAPACK (dsyevd) standing in for the reference's LAPACK dspev call.
+
+Pinned against the reference binary (oracle/build_ref.sh) through the golden fixtures in
+tests/golden/ (generated by tests/golden/make_golden.py) and the reference's own example
+outputs (EIGENSTRAT/example.eval, CONVERTF/example.*).
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_bin", "liboracle.so")
+_lib = None
+
+i32p = C.POINTER(C.c_int32)
+u8p = C.POINTER(C.c_uint8)
+f64p = C.POINTER(C.c_double)
+
+
+def _p(a, t):
+    return None if a is None else a.ctypes.data_as(C.POINTER(t))
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("oracle/_bin/liboracle.so is not built; run __graft_entry__.build()")
+        L = C.CDLL(LIB_PATH)
+        L.orc_pass_columns.argtypes = [u8p, C.c_int64, i32p, C.c_int32, i32p, C.c_int32, C.c_int,
+                                       C.c_int, C.c_int, C.c_int, i32p, i32p, i32p, u8p, f64p,
+                                       f64p, f64p]
+        L.orc_pass_columns.restype = None
+        L.orc_gram_plain.argtypes = [u8p, C.c_int64, i32p, C.c_int32, u8p, f64p, i32p, C.c_int32,
+                                     f64p]
+        L.orc_gram_plain.restype = None
+        L.orc_gram_lookup.argtypes = [u8p, C.c_int64, i32p, C.c_int32, u8p, f64p, i32p, C.c_int32,
+                                      C.c_int, f64p]
+        L.orc_gram_lookup.restype = None
+        L.orc_ridoutlier.argtypes = [f64p, C.c_int32, C.c_int32, C.c_double, C.c_int, i32p, i32p,
+                                     f64p]
+        L.orc_ridoutlier.restype = C.c_int
+        L.orc_weights.argtypes = [u8p, C.c_int64, i32p, C.c_int32, u8p, f64p, f64p, f64p, i32p,
+                                  C.c_int32, f64p, C.c_int32, f64p, f64p, f64p]
+        L.orc_weights.restype = None
+        L.orc_lsqproj.argtypes = [u8p, C.c_int64, i32p, C.c_int32, u8p, f64p, f64p, f64p, f64p,
+                                  C.c_int32, i32p, C.c_int32, f64p, f64p, i32p, i32p]
+        L.orc_lsqproj.restype = None
+        _lib = L
+    return _lib
+
+
+def unpack(records, nind):
+    """Genotype matrix (nsnp x nind) int8 with -1 for missing, from packed records."""
+    rec = np.asarray(records, dtype=np.uint8)
+    shifts = np.array([6, 4, 2, 0], dtype=np.uint8)
+    g = ((rec[:, :, None] >> shifts[None, None, :]) & 3).reshape(rec.shape[0], -1)[:, :nind]
+    g = g.astype(np.int8)
+    g[g == 3] = -1
+    return g
+
+
+def bed_to_packed(bed_records, nind):
+    """PLINK .bed records -> packedancestrymap records (ancval src/mcio.c:3995-4009)."""
+    bed = np.asarray(bed_records, dtype=np.uint8)
+    x = ((bed[:, :, None] >> np.array([0, 2, 4, 6], np.uint8)[None, None, :]) & 3).reshape(
+        bed.shape[0], -1)[:, :nind]
+    code = np.array([2, 3, 1, 0], np.uint8)[x]
+    return pack(np.where(code == 3, -1, code.astype(np.int8)).astype(np.int8))
+
+
+def pack(g):
+    """Genotype matrix (nsnp x nind, -1 missing) -> packed records (rlen = max(ceil(N/4),48))."""
+    g = np.asarray(g)
+    nsnp, nind = g.shape
+    rlen = max((nind + 3) // 4, 48)
+    codes = np.where(g < 0, 3, g).astype(np.uint8)
+    pad = np.zeros((nsnp, rlen * 4 - nind), np.uint8)  # the reference writer pads with 0
+    c = np.concatenate([codes, pad], axis=1).reshape(nsnp, rlen, 4)
+    out = (c[:, :, 0] << 6) | (c[:, :, 1] << 4) | (c[:, :, 2] << 2) | c[:, :, 3]
+    return np.ascontiguousarray(out.astype(np.uint8))
+
+
+class PassState:
+    pass
+
+
+def pass_columns(records, cols, xindex, fancynorm=1, altnormstyle=1, minallelecnt=1,
+                 maxmissing=9999999):
+    rec = np.ascontiguousarray(records, dtype=np.uint8)
+    cols = np.ascontiguousarray(cols, dtype=np.int32)
+    xi = np.ascontiguousarray(xindex, dtype=np.int32)
+    nc = len(cols)
+    s = PassState()
+    s.n0 = np.zeros(nc, np.int32)
+    s.n1 = np.zeros(nc, np.int32)
+    s.nmiss = np.zeros(nc, np.int32)
+    s.killed = np.zeros(nc, np.uint8)
+    s.tab = np.zeros(4 * nc)
+    s.xmean = np.zeros(nc)
+    s.xfancy = np.zeros(nc)
+    lib().orc_pass_columns(_p(rec, C.c_uint8), rec.shape[1], _p(cols, C.c_int32), nc,
+                           _p(xi, C.c_int32), len(xi), fancynorm, altnormstyle, minallelecnt,
+                           maxmissing, _p(s.n0, C.c_int32), _p(s.n1, C.c_int32),
+                           _p(s.nmiss, C.c_int32), _p(s.killed, C.c_uint8), _p(s.tab, C.c_double),
+                           _p(s.xmean, C.c_double), _p(s.xfancy, C.c_double))
+    s.rec, s.cols, s.xindex = rec, cols, xi
+    return s
+
+
+def gram(s, lookup=False, nthreads=1):
+    n = len(s.xindex)
+    X = np.zeros((n, n))
+    args = (_p(s.rec, C.c_uint8), s.rec.shape[1], _p(s.cols, C.c_int32), len(s.cols),
+            _p(s.killed, C.c_uint8), _p(s.tab, C.c_double), _p(s.xindex, C.c_int32), n)
+    if lookup:
+        lib().orc_gram_lookup(*args, nthreads, _p(X, C.c_double))
+    else:
+        lib().orc_gram_plain(*args, _p(X, C.c_double))
+    return X
+
+
+def eig_scaled(X):
+    """trace scale (smartpca.c:1230-1236) + all eigenpairs, descending (eigvecs -> dspev)."""
+    n = X.shape[0]
+    y = np.trace(X) / (n - 1)
+    if np.isnan(y) or y <= 0:
+        raise ValueError("XTX has zero trace (perhaps no data)")
+    Xs = X * (1.0 / y)
+    w, V = np.linalg.eigh(Xs)
+    return w[::-1].copy(), np.ascontiguousarray(V[:, ::-1].T)
+
+
+def ridoutlier(evecs, neigs, thresh=6.0, mode=0):
+    E = np.ascontiguousarray(evecs, dtype=np.float64)
+    n = E.shape[1]
+    bad = np.zeros(n, np.int32)
+    vec = np.zeros(n, np.int32)
+    sc = np.zeros(n)
+    nb = lib().orc_ridoutlier(_p(E, C.c_double), n, neigs, thresh, mode, _p(bad, C.c_int32),
+                              _p(vec, C.c_int32), _p(sc, C.c_double))
+    return bad[:nb], vec, sc
+
+
+def weights(s, evecs, K):
+    n, nc = len(s.xindex), len(s.cols)
+    E = np.ascontiguousarray(evecs[:K], dtype=np.float64)
+    ff = np.zeros((K, nc))
+    fx = np.zeros((K, n))
+    sc = np.zeros(K)
+    lib().orc_weights(_p(s.rec, C.c_uint8), s.rec.shape[1], _p(s.cols, C.c_int32), nc,
+                      _p(s.killed, C.c_uint8), _p(s.tab, C.c_double), _p(s.xmean, C.c_double),
+                      _p(s.xfancy, C.c_double), _p(s.xindex, C.c_int32), n, _p(E, C.c_double), K,
+                      _p(ff, C.c_double), _p(fx, C.c_double), _p(sc, C.c_double))
+    return ff, fx, sc
+
+
+def lsqproj(s, ffvecs, fxscal, K, samples):
+    smp = np.ascontiguousarray(samples, dtype=np.int32)
+    q = len(smp)
+    ff = np.ascontiguousarray(ffvecs[:K])
+    a = np.zeros((K, q))
+    b = np.zeros((K, q))
+    nobs = np.zeros(q, np.int32)
+    st = np.zeros(q, np.int32)
+    lib().orc_lsqproj(_p(s.rec, C.c_uint8), s.rec.shape[1], _p(s.cols, C.c_int32), len(s.cols),
+                      _p(s.killed, C.c_uint8), _p(s.xmean, C.c_double), _p(s.xfancy, C.c_double),
+                      _p(ff, C.c_double), _p(np.ascontiguousarray(fxscal), C.c_double), K,
+                      _p(smp, C.c_int32), q, _p(a, C.c_double), _p(b, C.c_double),
+                      _p(nobs, C.c_int32), _p(st, C.c_int32))
+    return a, b, nobs, st
+
+
+def smartpca(records, nind, numeigs=10, numoutliter=5, numoutleigs=10, outlthresh=6.0,
+             outliermode=0, fancynorm=1, altnormstyle=1, minallelecnt=1, maxmissing=9999999,
+             lsqproject=1, snp_chrom=None, noxdata=1, numchrom=22, ind_ignore=None,
+             ind_affstatus=None, gram_lookup=False, nthreads=1):
+    """The hot path of smartpca main() on packed records (sorted SNP order).
+
+    Returns evals (all, descending), evecs (top K over the rows), xindex, the per-sample
+    .evec coordinates, the set of printed samples and the outliers (sample, pass, evec, z).
+    """
+    rec = np.ascontiguousarray(records, dtype=np.uint8)
+    nsnp = rec.shape[0]
+    g = unpack(rec, nind)
+    ind_ign = np.zeros(nind, bool) if ind_ignore is None else np.asarray(ind_ignore, bool).copy()
+    aff = np.ones(nind, bool) if ind_affstatus is None else np.asarray(ind_affstatus, bool)
+    aff = aff & ~ind_ign
+    chrom = np.ones(nsnp, np.int32) if snp_chrom is None else np.asarray(snp_chrom)
+    snp_ign = np.zeros(nsnp, np.uint8)
+    snp_ign[(bool(noxdata) & (chrom == numchrom + 1)) | (chrom == 0) | (chrom > numchrom + 1)] = 1
+    valid = g >= 0
+    nodata = valid[:, ~ind_ign & aff].sum(axis=1) <= 1
+    snp_ign[(snp_ign == 0) & nodata] = 1
+    per_ind = valid[snp_ign == 0].sum(axis=0)
+    ind_ign |= per_ind == 0
+
+    def rows():
+        return np.nonzero(~ind_ign & aff)[0].astype(np.int32)
+
+    def columns():
+        ok = (snp_ign == 0) & (valid[:, ~ind_ign].sum(axis=1) > 0)
+        return np.nonzero(ok)[0].astype(np.int32)
+
+    xindex = rows()
+    cols = columns()
+    numoutiter = numoutliter + 1 if numoutliter >= 1 else 1
+    mode = outliermode if numoutliter >= 1 else 2
+    outliers = []
+    for it in range(1, numoutiter + 1):
+        if it > 1:
+            cols = columns()
+        s = pass_columns(rec, cols, xindex, fancynorm, altnormstyle, minallelecnt, maxmissing)
+        snp_ign[cols[s.killed == 1]] = 2
+        X = gram(s, lookup=gram_lookup, nthreads=nthreads)
+        evals, evecs = eig_scaled(X)
+        if it > numoutliter:
+            break
+        numoutleigs = min(numoutleigs, len(xindex) - 1)
+        bad, vec, sc = ridoutlier(evecs, numoutleigs, outlthresh, mode)
+        if len(bad) == 0:
+            break
+        for r in bad:
+            outliers.append((int(xindex[r]), it, int(vec[r]), float(sc[r])))
+            ind_ign[xindex[r]] = True
+        xindex = rows()
+    n = len(xindex)
+    K = min(numeigs, n, len(cols))
+    coords = np.zeros((K, nind))
+    out = ~ind_ign
+    if K > 0:
+        ff, fx, fxscal = weights(s, evecs, K)
+        if lsqproject:
+            proj = np.nonzero(~ind_ign)[0].astype(np.int32)
+            a, b, nobs, st = lsqproj(s, ff, fxscal, K, proj)
+            prev = np.zeros(K)
+            for q, k in enumerate(proj):
+                if st[q] == 1:
+                    ind_ign[k] = True
+                    a[:, q] = 0.0
+                    b[:, q] = 0.0
+                    continue
+                if st[q] == 2:
+                    a[:, q] = prev
+                prev = a[:, q].copy()
+            pos = {int(k): q for q, k in enumerate(proj)}
+            for j in range(K):
+                av = np.array([a[j, pos[k]] if k in pos else 0.0 for k in xindex])
+                bv = np.array([b[j, pos[k]] if k in pos else 0.0 for k in xindex])
+                scale = np.dot(av, bv) / np.dot(av, av)
+                coords[j, proj] = scale * a[j]
+        out = ~ind_ign
+    return dict(evals=evals, evecs=evecs[:K], xindex=xindex, coords=coords, ind_out=out,
+                outliers=outliers, ncols=len(cols), nrows=n, numeigs=K, snp_state=snp_ign)

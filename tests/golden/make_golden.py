@@ -1,0 +1,136 @@
+"""Generate the golden fixtures under tests/golden/ by running the REFERENCE smartpca.
+
+Run in a container where the reference sources are present (the binary is built by
+oracle/build_ref.sh into oracle/_ref/smartpca, with fprintf wrapped so that
+EIG_REF_FULLPREC=1 prints .eval/.evec numbers as %.17g).  Writes, per case:
+
+  <case>/data.{geno|bed,snp|bim,ind|fam}  the inputs (small, seeded Balding-Nichols)
+  <case>/par                              the parfile template (paths relative to the case)
+  <case>/ref.eval, ref.evec               reference outputs at full precision
+  <case>/ref.eval.txt, ref.evec.txt       reference outputs in the shipped text formats
+  <case>/ref.outliers                     the reference's outlier-removal lines
+  <case>/ref.log                          the reference's log
+
+and copies the reference's own example fixtures (CONVERTF/example.*,
+EIGENSTRAT/example.*) into ref_examples/.  Usage:
+  python tests/golden/make_golden.py [reference_root]
+"""
+import os
+import shutil
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from eig_gb300 import native  # noqa: E402  (the synthetic generator)
+from oracle import oracle as O  # noqa: E402
+
+REF_BIN = os.path.join(ROOT, "oracle", "_ref", "smartpca")
+
+CASES = {
+    # default options, 3 populations + 4 planted divergent samples -> outlier removal
+    "bn_outliers": dict(nsnp=4000, pops=[80, 80, 76, 2, 2], fst=[0.01, 0.01, 0.02, 0.25, 0.25],
+                        miss=0.01, seed=11, fmt="packed",
+                        par={"numoutevec": "6", "numoutlieriter": "5"}),
+    # PLINK bed input, altnormstyle NO, 5% missing, a maxmissing filter, 4 eigenvectors
+    "bn_bed_altnorm": dict(nsnp=3000, pops=[60, 60, 60], fst=[0.02, 0.03, 0.05], miss=0.05,
+                           seed=12, fmt="bed",
+                           par={"numoutevec": "4", "altnormstyle": "NO", "maxmissing": "16",
+                                "familynames": "NO"}),
+    # projection: PCA on POP0/POP1 only (poplistname), POP2 + admixed projected by lsqproj;
+    # per-sample missing up to 95% so that a few samples have too little data
+    "bn_project": dict(nsnp=3000, pops=[70, 70, 40], fst=[0.02, 0.02, 0.04], miss=0.0,
+                       miss_hi=0.97, n_admixed=20, seed=13, fmt="packed",
+                       par={"numoutevec": "5", "numoutlieriter": "0",
+                            "poplistname": "poplist"}, poplist=["POP0", "POP1"]),
+}
+
+
+def write_bed_case(d, rec, nind, nsnp, pops):
+    """PLINK .bed/.bim/.fam from packed records (packed code -> bed code)."""
+    g = O.unpack(rec, nind)  # nsnp x nind, -1 missing
+    bedcode = np.where(g < 0, 1, np.where(g == 2, 0, np.where(g == 1, 2, 3))).astype(np.uint8)
+    blen = (nind + 3) // 4
+    pad = np.zeros((nsnp, blen * 4 - nind), np.uint8)
+    c = np.concatenate([bedcode, pad], axis=1).reshape(nsnp, blen, 4)
+    by = c[:, :, 0] | (c[:, :, 1] << 2) | (c[:, :, 2] << 4) | (c[:, :, 3] << 6)
+    with open(os.path.join(d, "data.bed"), "wb") as f:
+        f.write(bytes([0x6C, 0x1B, 0x01]))
+        f.write(by.astype(np.uint8).tobytes())
+    with open(os.path.join(d, "data.bim"), "w") as f:
+        for s in range(nsnp):
+            f.write("1\trs%09d\t%.8f\t%d\tA\tG\n" % (s, (s + 1) * 1e-6, (s + 1) * 1000))
+    with open(os.path.join(d, "data.fam"), "w") as f:
+        for k in range(nind):
+            f.write("FAM%d S%07d 0 0 %d POP%d\n" % (k, k, 1 + (k & 1), pops[k]))
+
+
+def make_case(name, spec):
+    d = os.path.join(HERE, name)
+    os.makedirs(d, exist_ok=True)
+    prefix = os.path.join(d, "data")
+    native.synth_write_dataset(prefix, spec["nsnp"], spec["pops"], spec["fst"],
+                               miss=spec["miss"], miss_hi=spec.get("miss_hi"),
+                               n_admixed=spec.get("n_admixed", 0), seed=spec["seed"], nthreads=4)
+    par = {}
+    if spec["fmt"] == "bed":
+        nind = sum(spec["pops"])
+        raw = open(prefix + ".geno", "rb").read()
+        rlen = max((nind + 3) // 4, 48)
+        rec = np.frombuffer(raw[rlen:], np.uint8).reshape(spec["nsnp"], rlen)
+        pops = [k for k, n in enumerate(spec["pops"]) for _ in range(n)]
+        write_bed_case(d, rec, nind, spec["nsnp"], pops)
+        for ext in ("geno", "snp", "ind"):
+            os.remove(prefix + "." + ext)
+        par.update(genotypename="data.bed", snpname="data.bim", indivname="data.fam")
+    else:
+        par.update(genotypename="data.geno", snpname="data.snp", indivname="data.ind")
+    par.update(evecoutname="out.evec", evaloutname="out.eval", outlieroutname="out.outliers")
+    par.update(spec["par"])
+    if "poplist" in spec:
+        with open(os.path.join(d, "poplist"), "w") as f:
+            f.write("\n".join(spec["poplist"]) + "\n")
+    with open(os.path.join(d, "par"), "w") as f:
+        for k, v in par.items():
+            f.write("%s: %s\n" % (k, v))
+    run_reference(d)
+
+
+def run_reference(d):
+    env = dict(os.environ)
+    for prec, suffix in ((False, ".txt"), (True, "")):
+        env["EIG_REF_FULLPREC"] = "1" if prec else "0"
+        with open(os.path.join(d, "ref.log"), "w") as log:
+            subprocess.run([REF_BIN, "-p", "par"], cwd=d, env=env, stdout=log,
+                           stderr=subprocess.STDOUT, check=True)
+        shutil.move(os.path.join(d, "out.eval"), os.path.join(d, "ref.eval" + suffix))
+        shutil.move(os.path.join(d, "out.evec"), os.path.join(d, "ref.evec" + suffix))
+        shutil.move(os.path.join(d, "out.outliers"), os.path.join(d, "ref.outliers"))
+
+
+def copy_examples(ref_root):
+    out = os.path.join(HERE, "ref_examples")
+    os.makedirs(out, exist_ok=True)
+    files = {
+        "CONVERTF": ["example.eigenstratgeno", "example.packedancestrymapgeno", "example.bed",
+                     "example.snp", "example.ind", "example.pedsnp", "example.pedind"],
+        "EIGENSTRAT": ["example.geno", "example.snp", "example.ind", "example.eval",
+                       "example.pca.evec"],
+    }
+    for sub, names in files.items():
+        for n in names:
+            shutil.copy(os.path.join(ref_root, sub, n), os.path.join(out, sub + "_" + n))
+
+
+if __name__ == "__main__":
+    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if not os.path.exists(REF_BIN):
+        raise SystemExit("build the reference first: sh oracle/build_ref.sh")
+    copy_examples(ref_root)
+    for name, spec in CASES.items():
+        make_case(name, spec)
+        print("made", name)

@@ -1,0 +1,101 @@
+"""Loaders for the golden fixtures made by tests/golden/make_golden.py (reference outputs)."""
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+CASES = ["bn_outliers", "bn_bed_altnorm", "bn_project"]
+
+
+def read_par(case):
+    par = {}
+    for line in open(os.path.join(GOLDEN, case, "par")):
+        line = line.split("#")[0].strip()
+        if not line:
+            continue
+        k, v = line.split(None, 1)
+        par[k.rstrip(":")] = v.strip()
+    return par
+
+
+def yesno(v):
+    return 1 if v == "YES" else 0 if v == "NO" else int(v)
+
+
+class Case:
+    def __init__(self, case):
+        self.name = case
+        d = os.path.join(GOLDEN, case)
+        self.dir = d
+        self.par = p = read_par(case)
+        gname = os.path.join(d, p["genotypename"])
+        ind_lines = [l.split() for l in open(os.path.join(d, p["indivname"])) if l.strip()]
+        snp_lines = [l.split() for l in open(os.path.join(d, p["snpname"])) if l.strip()]
+        self.nsnp = len(snp_lines)
+        if gname.endswith(".bed"):
+            self.code = 1
+            self.ids = [l[1] for l in ind_lines]
+            self.pops = [l[5] for l in ind_lines]
+            self.nind = len(self.ids)
+            blen = (self.nind + 3) // 4
+            raw = open(gname, "rb").read()[3:]
+            self.records = np.frombuffer(raw, np.uint8).reshape(self.nsnp, blen).copy()
+        else:
+            self.code = 0
+            self.ids = [l[0] for l in ind_lines]
+            self.pops = [l[2] for l in ind_lines]
+            self.nind = len(self.ids)
+            rlen = max((self.nind + 3) // 4, 48)
+            raw = open(gname, "rb").read()[rlen:]
+            self.records = np.frombuffer(raw, np.uint8).reshape(self.nsnp, rlen).copy()
+        self.affstatus = None
+        if "poplistname" in p:
+            keep = {l.strip() for l in open(os.path.join(d, p["poplistname"])) if l.strip()}
+            self.affstatus = np.array([pp in keep for pp in self.pops], np.uint8)
+        self.ref_evals = np.loadtxt(os.path.join(d, "ref.eval"))
+        lines = open(os.path.join(d, "ref.evec")).read().splitlines()
+        self.ref_header = [float(x) for x in lines[0].split()[1:]]
+        self.ref_coords = {}
+        for l in lines[1:]:
+            t = l.split()
+            if t:
+                self.ref_coords[t[0]] = np.array([float(x) for x in t[1:-1]])
+        self.ref_outliers = [l.split()[2] for l in open(os.path.join(d, "ref.outliers"))
+                             if l.startswith("REMOVED")]
+
+    def opts(self):
+        p = self.par
+        kw = {}
+        if "numoutevec" in p:
+            kw["numeigs"] = int(p["numoutevec"])
+        if "numoutlieriter" in p:
+            kw["numoutliter"] = int(p["numoutlieriter"])
+        if "altnormstyle" in p:
+            kw["altnormstyle"] = yesno(p["altnormstyle"])
+        if "maxmissing" in p:
+            kw["maxmissing"] = int(p["maxmissing"])
+        return kw
+
+    def packed_records(self):
+        """records in packedancestrymap code (bed recoded on the host, for the oracle)."""
+        if self.code == 0:
+            return self.records
+        from oracle import oracle as O
+        return O.bed_to_packed(self.records, self.nind)
+
+
+def coords_by_id(ids, coords, ind_out):
+    return {ids[k]: coords[:, k] for k in range(len(ids)) if ind_out[k]}
+
+
+def compare_coords(ref, mine, K, tol):
+    """sign-invariant (per eigenvector) max abs difference of .evec coordinates"""
+    assert set(ref) == set(mine), "printed sample sets differ"
+    ids = sorted(ref)
+    A = np.array([ref[i][:K] for i in ids])
+    B = np.array([mine[i][:K] for i in ids])
+    s = np.sign(np.sum(A * B, axis=0))
+    s[s == 0] = 1
+    err = np.max(np.abs(A - B * s))
+    assert err < tol, "coordinate error %g" % err
+    return err

@@ -1,0 +1,182 @@
+"""GPU parity: the CUDA path through the C ABI against the oracle and the reference goldens.
+
+Tolerances: integer counts, kill flags and the normalisation table are bit-exact; the FP64
+Gram is within 1e-12 of the oracle's (summation order differs); eigenvalues within 1e-10
+relative (of the largest) of the reference; .evec coordinates within 1e-8 (sign per vector
+is arbitrary, as with LAPACK); outlier sets identical.
+"""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from eig_gb300 import native
+from oracle import oracle as O
+from tests.goldens import CASES, Case, compare_coords, coords_by_id
+
+pytestmark = pytest.mark.gpu
+
+
+def synth(nsnp, pops, fst, miss=0.02, seed=5, **kw):
+    rec, pop = native.synth_records(nsnp, pops, fst, miss=miss, seed=seed, nthreads=4, **kw)
+    return rec, pop
+
+
+@pytest.mark.parametrize("code", [native.GP_CODE_PACKED, native.GP_CODE_BED])
+def test_counts_and_table_bit_exact(gpu, code):
+    rec, pop = synth(3000, [150, 150, 101], [0.01, 0.03, 0.05], miss=0.03, seed=21)
+    nind = len(pop)
+    rng = np.random.default_rng(0)
+    rows = np.sort(rng.choice(nind, 333, replace=False)).astype(np.int32)
+    cols = np.sort(rng.choice(3000, 2500, replace=False)).astype(np.int32)
+    if code == native.GP_CODE_BED:
+        g = O.unpack(rec, nind)
+        bedcode = np.where(g < 0, 1, np.where(g == 2, 0, np.where(g == 1, 2, 3))).astype(np.uint8)
+        blen = (nind + 3) // 4
+        c = np.concatenate([bedcode, np.zeros((3000, blen * 4 - nind), np.uint8)], 1)
+        c = c.reshape(3000, blen, 4)
+        dev_rec = (c[:, :, 0] | (c[:, :, 1] << 2) | (c[:, :, 2] << 4) | (c[:, :, 3] << 6)).astype(np.uint8)
+    else:
+        dev_rec = rec
+    gpu.load_genotypes(dev_rec, nind, code)
+    gpu.set_samples(rows)
+    gpu.set_snps(cols)
+    for alt in (1, 0):
+        r = gpu.xtx(altnormstyle=alt, minallelecnt=5, maxmissing=12)
+        s = O.pass_columns(rec, cols, rows, altnormstyle=alt, minallelecnt=5, maxmissing=12)
+        assert np.array_equal(r["n0"], s.n0)
+        assert np.array_equal(r["n1"], s.n1)
+        assert np.array_equal(r["nmiss"], s.nmiss)
+        assert np.array_equal(r["killed"], s.killed)
+        assert np.array_equal(r["xmean"], s.xmean)  # bit-exact, not approx
+        assert np.array_equal(r["xfancy"], s.xfancy)
+        X = O.gram(s)
+        scale = np.max(np.abs(X))
+        assert np.max(np.abs(r["XTX"] - X)) <= 1e-12 * scale
+        assert abs(r["trace"] - np.trace(X)) <= 1e-12 * abs(np.trace(X))
+        assert r["nused"] == int((s.killed == 0).sum())
+
+
+def test_valid_counts(gpu):
+    rec, pop = synth(1000, [90, 90], [0.02, 0.02], miss=0.2, seed=22)
+    nind = len(pop)
+    gpu.load_genotypes(rec, nind)
+    g = O.unpack(rec, nind)
+    rng = np.random.default_rng(1)
+    su = (rng.random(nind) < 0.7).astype(np.uint8)
+    pu = (rng.random(1000) < 0.6).astype(np.uint8)
+    sv, iv = gpu.valid_counts(su, pu)
+    assert np.array_equal(sv, ((g >= 0) & (su[None, :] == 1)).sum(1))
+    assert np.array_equal(iv, ((g >= 0) & (pu[:, None] == 1)).sum(0))
+
+
+def test_set_missing(gpu):
+    rec, pop = synth(200, [40, 41], [0.02, 0.02], miss=0.0, seed=23)
+    nind = len(pop)
+    gpu.load_genotypes(rec, nind)
+    pairs = np.array([[3, 0], [3, 80], [150, 17]], np.int64)
+    gpu.set_missing(pairs)
+    sv, _ = gpu.valid_counts()
+    g = O.unpack(rec, nind)
+    for s, k in pairs:
+        g[s, k] = -1
+    assert np.array_equal(sv, (g >= 0).sum(1))
+
+
+def test_eigvecs_fp64(gpu):
+    rec, pop = synth(4000, [100, 100, 100], [0.01, 0.02, 0.04], seed=24)
+    nind = len(pop)
+    gpu.load_genotypes(rec, nind)
+    rows = np.arange(nind, dtype=np.int32)
+    cols = np.arange(4000, dtype=np.int32)
+    gpu.set_samples(rows)
+    gpu.set_snps(cols)
+    gpu.xtx()
+    ev, V = gpu.eigvecs(10)
+    s = O.pass_columns(rec, cols, rows)
+    w, U = O.eig_scaled(O.gram(s))
+    assert np.max(np.abs(ev - w)) <= 1e-10 * w[0]
+    cosang = np.abs(np.sum(V * U[:10], axis=1))
+    assert np.all(cosang > 1 - 1e-9)
+
+
+def test_ridoutlier_host_matches_oracle():
+    rng = np.random.default_rng(3)
+    E = rng.standard_normal((6, 200)) / np.sqrt(200)
+    E[2, 17] = 0.9
+    E[4, 33] = -0.8
+    for mode in (0, 1):
+        b1, v1, s1 = native.ridoutlier(E, 6, 6.0, mode)
+        b2, v2, s2 = O.ridoutlier(E, 6, 6.0, mode)
+        assert list(b1) == list(b2) and len(b1) >= 2
+        assert np.array_equal(v1, v2)
+        assert np.array_equal(s1, s2)
+
+
+def test_weights_and_lsqproj_vs_oracle(gpu):
+    rec, pop = synth(3000, [80, 80, 60], [0.01, 0.03, 0.05], miss=0.05, seed=25, n_admixed=10)
+    nind = len(pop)
+    gpu.load_genotypes(rec, nind)
+    rows = np.arange(0, nind, dtype=np.int32)[:200]
+    cols = np.arange(3000, dtype=np.int32)
+    gpu.set_samples(rows)
+    gpu.set_snps(cols)
+    gpu.xtx(minallelecnt=3)
+    ev, V = gpu.eigvecs(8)
+    K = 6
+    ff, fx, sc = gpu.snp_weights(K)
+    s = O.pass_columns(rec, cols, rows, minallelecnt=3)
+    off, ofx, osc = O.weights(s, V, K)
+    assert np.max(np.abs(ff - off)) <= 1e-10 * np.max(np.abs(off))
+    assert np.max(np.abs(fx - ofx)) <= 1e-10 * np.max(np.abs(ofx))
+    assert np.max(np.abs(sc - osc) / osc) <= 1e-10
+    proj = np.arange(nind, dtype=np.int32)
+    a, b, nobs, st = gpu.lsqproj(K, proj)
+    oa, ob, onobs, ost = O.lsqproj(s, off, osc, K, proj)
+    assert np.array_equal(nobs, onobs)
+    assert np.array_equal(st, ost)
+    ok = st == 0
+    assert np.max(np.abs(a[:, ok] - oa[:, ok])) <= 1e-8
+    assert np.max(np.abs(b[:, ok] - ob[:, ok])) <= 1e-8 * max(1.0, np.max(np.abs(ob)))
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_smartpca_run_matches_reference(gpu, case):
+    c = Case(case)
+    opts = native.default_opts(**c.opts())
+    r = native.smartpca_run(gpu, c.records, c.nind, opts, code=c.code,
+                            ind_affstatus=c.affstatus)
+    assert r["nrows"] == len(c.ref_evals)
+    scale = abs(c.ref_evals[0])
+    assert np.max(np.abs(r["evals"] - c.ref_evals)) <= 1e-10 * scale
+    assert [c.ids[k] for k, *_ in r["outliers"]] == c.ref_outliers
+    mine = coords_by_id(c.ids, r["coords"], r["ind_out"])
+    compare_coords(c.ref_coords, mine, r["numeigs"], 1e-8)
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_cli_dropin_matches_reference_text(case, tmp_path):
+    """gpusmartpca -p par writes the reference's .eval/.evec text (up to evec signs)."""
+    c = Case(case)
+    import shutil
+    d = tmp_path / case
+    shutil.copytree(c.dir, d)
+    cli = os.path.join(native.LIB_DIR, "gpusmartpca")
+    out = subprocess.run([cli, "-p", "par"], cwd=d, capture_output=True, text=True)
+    assert out.returncode == 0, out.stderr + out.stdout
+    ev = [float(x) for x in open(d / "out.eval").read().split()]
+    ref = [float(x) for x in open(d / "ref.eval.txt").read().split()]
+    assert len(ev) == len(ref)
+    assert np.max(np.abs(np.array(ev) - np.array(ref))) <= 1.0e-6
+    mine = open(d / "out.evec").read().splitlines()
+    want = open(d / "ref.evec.txt").read().splitlines()
+    assert mine[0] == want[0]
+    assert len(mine) == len(want)
+    A = np.array([[float(x) for x in l.split()[1:-1]] for l in want[1:]])
+    B = np.array([[float(x) for x in l.split()[1:-1]] for l in mine[1:]])
+    assert [l.split()[0] for l in mine[1:]] == [l.split()[0] for l in want[1:]]
+    s = np.sign(np.sum(A * B, axis=0))
+    assert np.max(np.abs(A - B * s)) <= 1.01e-4
+    got_out = open(d / "out.outliers").read()
+    assert got_out == open(d / "ref.outliers").read()

@@ -1,0 +1,68 @@
+"""CPU: the oracle restatement against the reference's own outputs (golden fixtures)."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.goldens import CASES, GOLDEN, Case, compare_coords, coords_by_id
+
+EX = os.path.join(GOLDEN, "ref_examples")
+
+
+def test_convertf_formats_decode_identically():
+    """CONVERTF/example.{packedancestrymapgeno,bed,eigenstratgeno}: one genotype matrix."""
+    text = [l.strip() for l in open(os.path.join(EX, "CONVERTF_example.eigenstratgeno"))]
+    G = np.array([[int(c) if c != "9" else -1 for c in l] for l in text])
+    nsnp, nind = G.shape
+    rlen = max((nind + 3) // 4, 48)
+    raw = open(os.path.join(EX, "CONVERTF_example.packedancestrymapgeno"), "rb").read()
+    packed = np.frombuffer(raw[rlen:], np.uint8).reshape(nsnp, rlen)
+    assert raw[48:50] == bytes([0x54, 0x00])  # first record decodes to 1,1,1,0,0
+    assert np.array_equal(O.unpack(packed, nind), G)
+    bed = np.frombuffer(open(os.path.join(EX, "CONVERTF_example.bed"), "rb").read()[3:],
+                        np.uint8).reshape(nsnp, (nind + 3) // 4)
+    assert np.array_equal(O.unpack(O.bed_to_packed(bed, nind), nind), G)
+    assert np.array_equal(O.pack(G)[:, : (nind + 3) // 4], packed[:, : (nind + 3) // 4])
+
+
+def test_eigenstrat_example_eval():
+    """EIGENSTRAT/example.eval (altnormstyle NO, 2 eigenvectors) from the oracle."""
+    text = [l.strip() for l in open(os.path.join(EX, "EIGENSTRAT_example.geno"))]
+    G = np.array([[int(c) if c != "9" else -1 for c in l] for l in text])
+    r = O.smartpca(O.pack(G), G.shape[1], numeigs=2, numoutleigs=2, altnormstyle=0,
+                   snp_chrom=np.full(G.shape[0], 11))
+    golden = np.loadtxt(os.path.join(EX, "EIGENSTRAT_example.eval"))
+    assert np.allclose(r["evals"], golden, atol=5e-7)
+    lines = open(os.path.join(EX, "EIGENSTRAT_example.pca.evec")).read().splitlines()[1:]
+    ref = np.array([[float(x) for x in l.split()[1:3]] for l in lines])
+    mine = r["coords"].T
+    s = np.sign(np.sum(ref * mine, axis=0))
+    assert np.max(np.abs(ref - mine * s)) < 6e-5  # printed at %10.4f
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_oracle_matches_reference(case):
+    c = Case(case)
+    kw = c.opts()
+    r = O.smartpca(c.packed_records(), c.nind, ind_affstatus=c.affstatus, **kw)
+    n = r["nrows"]
+    assert len(c.ref_evals) == n
+    scale = max(abs(c.ref_evals[0]), 1.0)
+    assert np.max(np.abs(r["evals"] - c.ref_evals)) / scale < 1e-12
+    assert [c.ids[k] for k, *_ in r["outliers"]] == c.ref_outliers
+    mine = coords_by_id(c.ids, r["coords"], r["ind_out"])
+    compare_coords(c.ref_coords, mine, r["numeigs"], 1e-9)
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_lookup_gram_equals_plain(case):
+    """the reference's partial-sum lookup Gram (threaded) equals the plain FP64 sum"""
+    c = Case(case)
+    rec = c.packed_records()
+    rows = np.arange(c.nind, dtype=np.int32)
+    cols = np.arange(c.nsnp, dtype=np.int32)
+    s = O.pass_columns(rec, cols, rows)
+    a = O.gram(s)
+    b = O.gram(s, lookup=True, nthreads=3)
+    assert np.max(np.abs(a - b)) <= 1e-12 * np.max(np.abs(a))

@@ -447,7 +447,12 @@ static int build_kept_tables(gp_ctx *ctx, uint8_t *base, kept_tables *t)
   return GP_OK;
 }
 
-static size_t kept_tables_bytes(int32_t nk) { return (size_t)nk * (12 * sizeof(double) + 4) + 256; }
+/* bytes of the kept-column tables, rounded up so that what follows stays 256-byte aligned */
+static size_t kept_tables_bytes(int32_t nk)
+{
+  size_t b = (size_t)nk * (12 * sizeof(double) + sizeof(int32_t)) + 256;
+  return (b + 255) / 256 * 256;
+}
 
 extern "C" int gp_snp_weights(gp_ctx *ctx, int32_t numeigs, double *ffvecs, double *fxvecs,
                               double *fxscal)

@@ -316,7 +316,7 @@ extern "C" int gp_valid_counts(gp_ctx *ctx, const uint8_t *sample_use, const uin
   GP_LAUNCH_CHECK(ctx, "k_rowmask_from_flags");
   if (snp_valid) {
     k_snp_valid<<<grid_for(ctx, nsnp * 32, 256), 256, 0, ctx->stream>>>(
-        ctx->d_geno, ctx->rlen_dev, nsnp, d_mask, snp_use ? d_su : NULL, d_sv);
+        ctx->d_geno, ctx->rlen_dev, nsnp, d_mask, NULL, d_sv);
     GP_LAUNCH_CHECK(ctx, "k_snp_valid");
     GP_CUDA(ctx, cudaMemcpyAsync(snp_valid, d_sv, sizeof(int32_t) * (size_t)nsnp,
                                  cudaMemcpyDeviceToHost, ctx->stream));

@@ -1,0 +1,326 @@
+"""Benchmark of the smartpca hot path on GB300 (one JSON line on rank 0).
+
+Workload (default): full smartpca at N=5,000 samples x M=600,000 SNPs, Balding-Nichols with
+6 populations of sizes 500..1,100 and F in {0.005, 0.01, 0.02, 0.03, 0.04, 0.05}, 2% missing,
+K=20, numoutlieriter 5, outlier sigma 6, lsqproject on.  Seeded synthetic genotypes stand in
+for real panels (no dataset is read).
+
+A step = one whole gp_smartpca_run (counts, normalisation, Gram, eigensolve, outlier passes,
+SNP weights, lsqproject) on the panel resident in HBM.  `value` = whole-job XTX throughput:
+the algorithmic Gram flops of every pass, sum of N_p (N_p+1) M_p, divided by the step time
+(so eigensolve, weights and projection time count against it).  `e2e` is the same metric
+through the C ABI with the packed records in pinned HOST memory: the upload and the result
+read-back are inside the timed region.
+
+--impl reference times the reference's own Gram algorithm (the partial-sum lookup of
+smartpca, restated in oracle/smartpca_oracle.c) on the host cores with all threads over a
+bounded SNP sample of the same workload, in the same unit.
+
+Multi-GPU: the path does not shard (one PCA per panel); --gpus N runs N independent replicas,
+value = N x per-replica throughput measured as total work / max time over ranks.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+CONFIGS = {
+    "full": dict(nsnp=600_000, pops=[500, 700, 800, 900, 1000, 1100],
+                 fst=[0.005, 0.01, 0.02, 0.03, 0.04, 0.05], miss=0.02, K=20, seed=2,
+                 name="smartpca N=5000 x M=600000 BN 6 pops, 2% missing, K=20, "
+                      "numoutlieriter 5, sigma 6, lsqproject"),
+    "small": dict(nsnp=60_000, pops=[100, 150, 200, 250, 150, 150],
+                  fst=[0.005, 0.01, 0.02, 0.03, 0.04, 0.05], miss=0.02, K=20, seed=2,
+                  name="smartpca N=1000 x M=60000 BN 6 pops (profiling case)"),
+}
+
+METRIC = "PCA wall-s & XTX TFLOP/s, split-BF16 vs FP64 @1e-6 eval err; proj p99 ms"
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region"""
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def start(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm = []
+        mx = None
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for p in self.samples:
+            try:
+                sm.append(float(p[0]))
+                mx = float(p[1])
+            except ValueError:
+                continue
+            for i, n in enumerate(names):
+                if p[3 + i].lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return world, rank, local, dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_gpu(args, cfg, world, rank, local, dist):
+    import torch
+
+    from eig_gb300 import native
+    torch.cuda.set_device(local)
+    prec = native.GP_PREC_SPLIT_BF16 if args.precision == "bf16" else native.GP_PREC_FP64
+    t0 = time.time()
+    rec, pop = native.synth_records(cfg["nsnp"], cfg["pops"], cfg["fst"], miss=cfg["miss"],
+                                    seed=cfg["seed"])
+    nind = len(pop)
+    gen_s = time.time() - t0
+    h = native.Handle(local)
+    h.load_genotypes(rec, nind)
+    opts = native.default_opts(numeigs=cfg["K"], numoutliter=5, outlthresh=6.0,
+                               precision=prec)
+    resident = (rec.shape[0], rec.shape[1])
+
+    def step(host):
+        r = native.smartpca_run(h, rec if host else resident, nind, opts)
+        return r
+
+    # the Gram flops of a step: sum over passes of N_p (N_p + 1) M_p (recorded per gp_xtx)
+    flops_holder = {}
+
+    def one(host=False):
+        h.timer_start()
+        r = step(host)
+        ms = h.timer_stop()
+        return r, ms
+
+    for _ in range(args.warmup):
+        r, _ = one()
+    # per-pass Gram flops from the final run's pass structure: re-derive from npasses
+    torch.cuda.synchronize()
+    barrier(dist)
+    clocks = ClockSampler(local)
+    clocks.start()
+    times = []
+    gram_ms = []
+    total_flops = 0.0
+    h.launch_count(reset=True)
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        r, ms = one()
+        torch.cuda.synchronize()
+        times.append(ms)
+        g_ms, g_launch, g_flops = h.last_gram_time()
+        gram_ms.append(g_ms)
+        total_flops = r["gram_flops"]
+    clk = clocks.stop()
+    launches = h.launch_count(reset=True) / max(1, args.steps)
+    barrier(dist)
+    step_ms = max_over_ranks(dist, float(np.mean(times)))
+    # dominant kernel: the Gram of the last pass
+    g_ms, g_launch, g_flops = h.last_gram_time()
+    # e2e through the C ABI from pinned host memory
+    native.host_register(rec)
+    e2e_times = []
+    h.transfer_bytes(reset=True)
+    for _ in range(max(1, min(args.steps, args.e2e_steps))):
+        torch.cuda.synchronize()
+        barrier(dist)
+        t = time.perf_counter()
+        r2 = step(True)
+        torch.cuda.synchronize()
+        e2e_times.append((time.perf_counter() - t) * 1e3)
+    h2d, d2h = h.transfer_bytes(reset=True)
+    n_e2e = len(e2e_times)
+    native.host_unregister(rec)
+    e2e_ms = max_over_ranks(dist, float(np.mean(e2e_times)))
+    h.close()
+    peaks, peak_kind = load_peaks()
+    res = dict(step_ms=step_ms, gram_flops=total_flops, gram_ms=g_ms, gram_launches=g_launch,
+               gram_kernel_flops=g_flops, clocks=clk, e2e_ms=e2e_ms, h2d=h2d / n_e2e,
+               d2h=d2h / n_e2e, run=r, gen_s=gen_s, peaks=peaks, peak_kind=peak_kind,
+               nind=nind, launches=launches)
+    return res
+
+
+def cpu_reference_sample(cfg, seconds_target=12.0, nthreads=None):
+    """The reference's partial-sum lookup Gram on the host cores over a SNP sample of the
+    workload: returns (TFLOP/s in algorithmic N(N+1)M units, cores, sample description)."""
+    from eig_gb300 import native
+    from oracle import oracle as O
+    nthreads = nthreads or os.cpu_count() or 1
+    nind = sum(cfg["pops"])
+    msnp = 400
+    rec, pop = native.synth_records(msnp, cfg["pops"], cfg["fst"], miss=cfg["miss"],
+                                    seed=cfg["seed"])
+    rows = np.arange(nind, dtype=np.int32)
+    cols = np.arange(msnp, dtype=np.int32)
+    s = O.pass_columns(rec, cols, rows)
+    t = time.perf_counter()
+    O.gram(s, lookup=True, nthreads=nthreads)
+    dt = time.perf_counter() - t
+    # grow the sample to ~seconds_target of CPU work
+    m2 = int(min(60_000, max(msnp, msnp * seconds_target / max(dt, 1e-3))))
+    m2 = max(20, m2 // 20 * 20)
+    rec, pop = native.synth_records(m2, cfg["pops"], cfg["fst"], miss=cfg["miss"],
+                                    seed=cfg["seed"])
+    cols = np.arange(m2, dtype=np.int32)
+    s = O.pass_columns(rec, cols, rows)
+    t = time.perf_counter()
+    O.gram(s, lookup=True, nthreads=nthreads)
+    dt = time.perf_counter() - t
+    kept = int((s.killed == 0).sum())
+    flops = nind * (nind + 1) * kept
+    return flops / dt / 1e12, nthreads, dt, m2, nind
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--precision", default="bf16", choices=["bf16", "fp64"])
+    ap.add_argument("--config", default="full", choices=list(CONFIGS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    cfg = CONFIGS[args.config]
+    world, rank, local, dist = dist_setup()
+    nind = sum(cfg["pops"])
+    config = {"workload": cfg["name"], "nsamples": nind, "nsnps": cfg["nsnp"],
+              "numeigs": cfg["K"], "replicas": world, "parallelism": "replicas only",
+              "l2": "inputs larger than L2 (packed panel %.0f MB)" % (
+                  cfg["nsnp"] * max((nind + 3) // 4, 48) / 1e6)}
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        steps = []
+        for _ in range(args.warmup + args.steps):
+            v, cores, dt, m2, n = cpu_reference_sample(cfg, seconds_target=8.0)
+            steps.append((v, dt))
+        vals = [v for v, _ in steps[args.warmup:]]
+        value = float(np.mean(vals))
+        sample = ("partial-sum lookup Gram (restated reference algorithm) over N=%d x M=%d "
+                  "SNPs, %d threads" % (n, m2, cores))
+        line = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "impl": "reference",
+                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": float(np.mean([d for _, d in steps[args.warmup:]]) * 1e3),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64", "data": "synthetic (seeded Balding-Nichols)", "config": config,
+                "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": cores,
+                                 "kind": "port", "sample": sample},
+                "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    res = run_gpu(args, cfg, world, rank, local, dist)
+    r = res["run"]
+    value = world * res["gram_flops"] / (res["step_ms"] * 1e-3) / 1e12
+    e2e = world * res["gram_flops"] / (res["e2e_ms"] * 1e-3) / 1e12
+    peaks = res["peaks"]
+    if args.precision == "bf16":
+        achieved = res["gram_kernel_flops"] / (res["gram_ms"] * 1e-3) / 1e12
+        peak = peaks.get("bf16_tflops", 1900.0)
+        roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": None,
+                "peak_kind": "bf16 burst, %s" % res["peak_kind"]}
+    else:
+        achieved = res["gram_kernel_flops"] / (res["gram_ms"] * 1e-3) / 1e12
+        roof = {"bound": "fp64", "achieved": achieved, "peak": 1.25, "unit": "TFLOP/s",
+                "frac": achieved / 1.25, "traffic": None,
+                "peak_kind": "nominal GB300 FP64 1.25 TFLOP/s (not in the measured peaks)"}
+    line = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["step_ms"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16x3 split (fp32 in tile, fp64 across)" if args.precision == "bf16" else "f64",
+            "data": "synthetic (seeded Balding-Nichols)", "config": config,
+            "pca_wall_s": res["step_ms"] / 1e3,
+            "phases_s": {k: round(v, 4) for k, v in r["t_phase"].items()},
+            "passes": r["npasses"], "outliers": len(r["outliers"]),
+            "gram_kernel_ms": res["gram_ms"],
+            "roofline": roof, "clocks": res["clocks"],
+            "e2e": {"value": e2e, "unit": "TFLOP/s", "h2d_bytes_per_step": int(res["h2d"]),
+                    "d2h_bytes_per_step": int(res["d2h"]), "wall_s": res["e2e_ms"] / 1e3},
+            "gpu_launches": res["launches"],
+            "gpu_launches_note": "own kernels per timed step (cuSOLVER eigensolver launches not counted)"}
+    if rank == 0 and not args.no_cpu_baseline:
+        v, cores, dt, m2, n = cpu_reference_sample(cfg, seconds_target=12.0)
+        line["cpu_baseline"] = {"value": v, "unit": "TFLOP/s", "cores": cores, "kind": "port",
+                                "sample": "reference partial-sum lookup Gram restated, N=%d x "
+                                          "M=%d SNP sample, %.1f s" % (n, m2, dt)}
+    if rank == 0:
+        print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

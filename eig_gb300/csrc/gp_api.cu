@@ -39,6 +39,14 @@ extern "C" int gp_fail_msg(gp_ctx *ctx, int code, const char *fmt, ...)
   return code;
 }
 
+cudaError_t gp_memcpy(gp_ctx *ctx, void *dst, const void *src, size_t bytes, cudaMemcpyKind kind,
+                      cudaStream_t stream)
+{
+  if (kind == cudaMemcpyHostToDevice) ctx->h2d_bytes += (int64_t)bytes;
+  if (kind == cudaMemcpyDeviceToHost) ctx->d2h_bytes += (int64_t)bytes;
+  return cudaMemcpyAsync(dst, src, bytes, kind, stream);
+}
+
 int gp_cuda_fail(gp_ctx *ctx, cudaError_t e, const char *what)
 {
   return gp_fail(ctx, e == cudaErrorMemoryAllocation ? GP_ERR_NOMEM : GP_ERR_CUDA,
@@ -112,6 +120,15 @@ extern "C" int gp_open(int device, gp_ctx **out)
     free(ctx);
     return GP_ERR_CUDA;
   }
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_t0);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_t1);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_g0);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_g1);
+  if (e != cudaSuccess) {
+    gp_fail(NULL, GP_ERR_CUDA, "gp_open: %s", cudaGetErrorString(e));
+    free(ctx);
+    return GP_ERR_CUDA;
+  }
   if (cusolverDnCreate(&ctx->solver) != CUSOLVER_STATUS_SUCCESS ||
       cusolverDnSetStream(ctx->solver, ctx->stream) != CUSOLVER_STATUS_SUCCESS) {
     cudaStreamDestroy(ctx->stream);
@@ -134,6 +151,10 @@ extern "C" void gp_close(gp_ctx *ctx)
   for (size_t i = 0; i < sizeof(bufs) / sizeof(bufs[0]); ++i)
     if (bufs[i]) cudaFree(bufs[i]);
   if (ctx->solver) cusolverDnDestroy(ctx->solver);
+  if (ctx->ev_t0) cudaEventDestroy(ctx->ev_t0);
+  if (ctx->ev_t1) cudaEventDestroy(ctx->ev_t1);
+  if (ctx->ev_g0) cudaEventDestroy(ctx->ev_g0);
+  if (ctx->ev_g1) cudaEventDestroy(ctx->ev_g1);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   free(ctx);
 }
@@ -182,7 +203,7 @@ extern "C" int gp_xtx(gp_ctx *ctx, const gp_xtx_opts *opts, int32_t *n0, int32_t
 
   /* kept-column list (ascending) built from the kill flags */
   std::vector<uint8_t> hk((size_t)nc);
-  GP_CUDA(ctx, cudaMemcpyAsync(hk.data(), ctx->d_killed, (size_t)nc, cudaMemcpyDeviceToHost,
+  GP_CUDA(ctx, gp_memcpy(ctx, hk.data(), ctx->d_killed, (size_t)nc, cudaMemcpyDeviceToHost,
                                ctx->stream));
   GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   std::vector<int32_t> kept;
@@ -191,14 +212,17 @@ extern "C" int gp_xtx(gp_ctx *ctx, const gp_xtx_opts *opts, int32_t *n0, int32_t
     if (!hk[(size_t)c]) kept.push_back(c);
   ctx->nkept = (int32_t)kept.size();
   if (ctx->nkept)
-    GP_CUDA(ctx, cudaMemcpyAsync(ctx->d_kept, kept.data(), sizeof(int32_t) * kept.size(),
+    GP_CUDA(ctx, gp_memcpy(ctx, ctx->d_kept, kept.data(), sizeof(int32_t) * kept.size(),
                                  cudaMemcpyHostToDevice, ctx->stream));
 
+  GP_CUDA(ctx, cudaEventRecord(ctx->ev_g0, ctx->stream));
+  ctx->gram_launches = 0;
   if (opts->precision == GP_PREC_FP64)
     rc = gp_gram_fp64(ctx);
   else
     rc = gp_gram_split_bf16(ctx);
   if (rc) return rc;
+  GP_CUDA(ctx, cudaEventRecord(ctx->ev_g1, ctx->stream));
 
   double *d_tr;
   rc = gp_scratch(ctx, sizeof(double), (void **)&d_tr);
@@ -206,10 +230,10 @@ extern "C" int gp_xtx(gp_ctx *ctx, const gp_xtx_opts *opts, int32_t *n0, int32_t
   rc = gp_launch_symmetrize_trace(ctx, d_tr);
   if (rc) return rc;
   double tr = 0.0;
-  GP_CUDA(ctx, cudaMemcpyAsync(&tr, d_tr, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  GP_CUDA(ctx, gp_memcpy(ctx, &tr, d_tr, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   if (n0 || n1 || nmiss) {
     std::vector<int32_t> cnt((size_t)nc * 3);
-    GP_CUDA(ctx, cudaMemcpyAsync(cnt.data(), ctx->d_cnt, sizeof(int32_t) * cnt.size(),
+    GP_CUDA(ctx, gp_memcpy(ctx, cnt.data(), ctx->d_cnt, sizeof(int32_t) * cnt.size(),
                                  cudaMemcpyDeviceToHost, ctx->stream));
     GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     for (int32_t c = 0; c < nc; ++c) {
@@ -220,15 +244,19 @@ extern "C" int gp_xtx(gp_ctx *ctx, const gp_xtx_opts *opts, int32_t *n0, int32_t
   }
   if (killed) memcpy(killed, hk.data(), (size_t)nc);
   if (xmean)
-    GP_CUDA(ctx, cudaMemcpyAsync(xmean, ctx->d_xmean, sizeof(double) * nc,
+    GP_CUDA(ctx, gp_memcpy(ctx, xmean, ctx->d_xmean, sizeof(double) * nc,
                                  cudaMemcpyDeviceToHost, ctx->stream));
   if (xfancy)
-    GP_CUDA(ctx, cudaMemcpyAsync(xfancy, ctx->d_xfancy, sizeof(double) * nc,
+    GP_CUDA(ctx, gp_memcpy(ctx, xfancy, ctx->d_xfancy, sizeof(double) * nc,
                                  cudaMemcpyDeviceToHost, ctx->stream));
   if (XTX)
-    GP_CUDA(ctx, cudaMemcpyAsync(XTX, ctx->d_xtx, sizeof(double) * (size_t)need,
+    GP_CUDA(ctx, gp_memcpy(ctx, XTX, ctx->d_xtx, sizeof(double) * (size_t)need,
                                  cudaMemcpyDeviceToHost, ctx->stream));
   GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  float gms = 0.f;
+  GP_CUDA(ctx, cudaEventElapsedTime(&gms, ctx->ev_g0, ctx->ev_g1));
+  ctx->gram_ms = gms;
+  ctx->gram_flops = (double)n * (double)(n + 1) * (double)ctx->nkept;
   ctx->trace = tr;
   if (trace) *trace = tr;
   if (nused) *nused = ctx->nkept;
@@ -285,7 +313,7 @@ extern "C" int gp_eigvecs(gp_ctx *ctx, int32_t nvec, double *evals, double *evec
                        d_info) != CUSOLVER_STATUS_SUCCESS)
     return gp_fail(ctx, GP_ERR_SOLVER, "cusolverDnDsyevd failed to launch");
   int info = 0;
-  GP_CUDA(ctx, cudaMemcpyAsync(&info, d_info, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  GP_CUDA(ctx, gp_memcpy(ctx, &info, d_info, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   if (nvec > 0) {
     int64_t tot = (int64_t)n * nvec;
     int b2 = (int)((tot + 255) / 256);
@@ -294,10 +322,10 @@ extern "C" int gp_eigvecs(gp_ctx *ctx, int32_t nvec, double *evals, double *evec
     GP_LAUNCH_CHECK(ctx, "k_take_top");
   }
   std::vector<double> w((size_t)n);
-  GP_CUDA(ctx, cudaMemcpyAsync(w.data(), ctx->d_evals, sizeof(double) * (size_t)n,
+  GP_CUDA(ctx, gp_memcpy(ctx, w.data(), ctx->d_evals, sizeof(double) * (size_t)n,
                                cudaMemcpyDeviceToHost, ctx->stream));
   if (evecs && nvec > 0)
-    GP_CUDA(ctx, cudaMemcpyAsync(evecs, ctx->d_evecs, sizeof(double) * (size_t)n * nvec,
+    GP_CUDA(ctx, gp_memcpy(ctx, evecs, ctx->d_evecs, sizeof(double) * (size_t)n * nvec,
                                  cudaMemcpyDeviceToHost, ctx->stream));
   GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   ctx->xtx_valid = 0; /* the solver overwrote the Gram with eigenvectors */
@@ -496,10 +524,10 @@ extern "C" int gp_snp_weights(gp_ctx *ctx, int32_t numeigs, double *ffvecs, doub
   rc = gp_geno_gemm_f64(ctx, 1, ctx->d_rows, n, kt.snprec, kt.rt, nk, d_ffvT, K, K, d_fxT, K);
   if (rc) return rc;
   std::vector<double> fx((size_t)n * K);
-  GP_CUDA(ctx, cudaMemcpyAsync(fx.data(), d_fxT, sizeof(double) * fx.size(),
+  GP_CUDA(ctx, gp_memcpy(ctx, fx.data(), d_fxT, sizeof(double) * fx.size(),
                                cudaMemcpyDeviceToHost, ctx->stream));
   if (ffvecs)
-    GP_CUDA(ctx, cudaMemcpyAsync(ffvecs, ctx->d_ffvecs, sizeof(double) * (size_t)K * nc,
+    GP_CUDA(ctx, gp_memcpy(ctx, ffvecs, ctx->d_ffvecs, sizeof(double) * (size_t)K * nc,
                                  cudaMemcpyDeviceToHost, ctx->stream));
   GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   /* fxscal_j = 1/sqrt(sum_i fxvecs^2) in row order (smartpca.c:1504-1525) */
@@ -512,7 +540,7 @@ extern "C" int gp_snp_weights(gp_ctx *ctx, int32_t numeigs, double *ffvecs, doub
     }
     fxscal[j] = 1.0 / sqrt(s);
   }
-  GP_CUDA(ctx, cudaMemcpyAsync(ctx->d_fxscal, fxscal, sizeof(double) * K, cudaMemcpyHostToDevice,
+  GP_CUDA(ctx, gp_memcpy(ctx, ctx->d_fxscal, fxscal, sizeof(double) * K, cudaMemcpyHostToDevice,
                                ctx->stream));
   GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   ctx->nweights = K;
@@ -641,7 +669,7 @@ extern "C" int gp_lsqproj(gp_ctx *ctx, int32_t numeigs, const int32_t *samples, 
   double *d_P = d_E + nE, *d_co = d_P + nP, *d_rr = d_co + nco, *d_work = d_rr + nrr;
   double *d_a = d_work + nwork, *d_b = d_a + nrr;
   int32_t *d_samp = (int32_t *)(d_b + nrr), *d_nobs = d_samp + nproj, *d_st = d_nobs + nproj;
-  GP_CUDA(ctx, cudaMemcpyAsync(d_samp, samples, sizeof(int32_t) * (size_t)nproj,
+  GP_CUDA(ctx, gp_memcpy(ctx, d_samp, samples, sizeof(int32_t) * (size_t)nproj,
                                cudaMemcpyHostToDevice, ctx->stream));
   if (nk) {
     int blocks = (nk + 127) / 128;
@@ -662,15 +690,15 @@ extern "C" int gp_lsqproj(gp_ctx *ctx, int32_t numeigs, const int32_t *samples, 
   GP_LAUNCH_CHECK(ctx, "k_lsq_solve");
   std::vector<int32_t> st((size_t)nproj);
   std::vector<double> ha(nrr);
-  GP_CUDA(ctx, cudaMemcpyAsync(ha.data(), d_a, sizeof(double) * nrr, cudaMemcpyDeviceToHost,
+  GP_CUDA(ctx, gp_memcpy(ctx, ha.data(), d_a, sizeof(double) * nrr, cudaMemcpyDeviceToHost,
                                ctx->stream));
-  GP_CUDA(ctx, cudaMemcpyAsync(st.data(), d_st, sizeof(int32_t) * (size_t)nproj,
+  GP_CUDA(ctx, gp_memcpy(ctx, st.data(), d_st, sizeof(int32_t) * (size_t)nproj,
                                cudaMemcpyDeviceToHost, ctx->stream));
   if (bcoeffs)
-    GP_CUDA(ctx, cudaMemcpyAsync(bcoeffs, d_b, sizeof(double) * nrr, cudaMemcpyDeviceToHost,
+    GP_CUDA(ctx, gp_memcpy(ctx, bcoeffs, d_b, sizeof(double) * nrr, cudaMemcpyDeviceToHost,
                                  ctx->stream));
   if (nobs)
-    GP_CUDA(ctx, cudaMemcpyAsync(nobs, d_nobs, sizeof(int32_t) * (size_t)nproj,
+    GP_CUDA(ctx, gp_memcpy(ctx, nobs, d_nobs, sizeof(int32_t) * (size_t)nproj,
                                  cudaMemcpyDeviceToHost, ctx->stream));
   GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   for (int32_t q = 0; q < nproj; ++q) {
@@ -679,5 +707,67 @@ extern "C" int gp_lsqproj(gp_ctx *ctx, int32_t numeigs, const int32_t *samples, 
     for (int32_t j = 0; j < K; ++j)
       acoeffs[(size_t)j * nproj + q] = ha[(size_t)j * nproj + q];
   }
+  return GP_OK;
+}
+
+/* ------------------------------------------------------------------------------------ */
+
+extern "C" int gp_timer_start(gp_ctx *ctx)
+{
+  if (!ctx) return GP_ERR_ARG;
+  GP_CUDA(ctx, cudaEventRecord(ctx->ev_t0, ctx->stream));
+  return GP_OK;
+}
+
+extern "C" int gp_timer_stop(gp_ctx *ctx, double *ms)
+{
+  if (!ctx || !ms) return GP_ERR_ARG;
+  GP_CUDA(ctx, cudaEventRecord(ctx->ev_t1, ctx->stream));
+  GP_CUDA(ctx, cudaEventSynchronize(ctx->ev_t1));
+  float f = 0.f;
+  GP_CUDA(ctx, cudaEventElapsedTime(&f, ctx->ev_t0, ctx->ev_t1));
+  *ms = f;
+  return GP_OK;
+}
+
+extern "C" int gp_last_gram_time(const gp_ctx *ctx, double *ms, int32_t *launches, double *flops)
+{
+  if (!ctx) return GP_ERR_ARG;
+  if (ms) *ms = ctx->gram_ms;
+  if (launches) *launches = ctx->gram_launches;
+  if (flops) *flops = ctx->gram_flops;
+  return GP_OK;
+}
+
+extern "C" int gp_host_register(void *ptr, size_t bytes)
+{
+  if (!ptr || !bytes) return GP_ERR_ARG;
+  cudaError_t e = cudaHostRegister(ptr, bytes, cudaHostRegisterDefault);
+  if (e != cudaSuccess) return gp_fail(NULL, GP_ERR_CUDA, "cudaHostRegister: %s", cudaGetErrorString(e));
+  return GP_OK;
+}
+
+extern "C" int gp_host_unregister(void *ptr)
+{
+  if (!ptr) return GP_ERR_ARG;
+  cudaError_t e = cudaHostUnregister(ptr);
+  if (e != cudaSuccess) return gp_fail(NULL, GP_ERR_CUDA, "cudaHostUnregister: %s", cudaGetErrorString(e));
+  return GP_OK;
+}
+
+extern "C" int gp_transfer_bytes(gp_ctx *ctx, int64_t *h2d, int64_t *d2h, int32_t reset)
+{
+  if (!ctx) return GP_ERR_ARG;
+  if (h2d) *h2d = ctx->h2d_bytes;
+  if (d2h) *d2h = ctx->d2h_bytes;
+  if (reset) ctx->h2d_bytes = ctx->d2h_bytes = 0;
+  return GP_OK;
+}
+
+extern "C" int gp_launch_count(gp_ctx *ctx, int64_t *n, int32_t reset)
+{
+  if (!ctx) return GP_ERR_ARG;
+  if (n) *n = ctx->launches;
+  if (reset) ctx->launches = 0;
   return GP_OK;
 }

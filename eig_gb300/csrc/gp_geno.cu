@@ -110,6 +110,7 @@ extern "C" int gp_load_genotypes(gp_ctx *ctx, const uint8_t *records, int64_t re
   ctx->rlen_dev = rlen_dev;
   ctx->nrows = ctx->ncols = 0;
   ctx->xtx_valid = ctx->eig_valid = ctx->weights_valid = 0;
+  ctx->h2d_bytes += used * nsnp;
   GP_CUDA(ctx, cudaMemcpy2DAsync(ctx->d_geno, (size_t)rlen_dev, records, (size_t)record_bytes,
                                  (size_t)used, (size_t)nsnp, cudaMemcpyHostToDevice,
                                  ctx->stream));
@@ -125,6 +126,14 @@ extern "C" int gp_load_genotypes(gp_ctx *ctx, const uint8_t *records, int64_t re
   return GP_OK;
 }
 
+extern "C" int gp_genotype_shape(const gp_ctx *ctx, int64_t *nsnp, int32_t *nind)
+{
+  if (!ctx) return GP_ERR_ARG;
+  if (nsnp) *nsnp = ctx->d_geno ? ctx->nsnp_all : 0;
+  if (nind) *nind = ctx->d_geno ? ctx->nind_all : 0;
+  return GP_OK;
+}
+
 extern "C" int gp_set_missing(gp_ctx *ctx, const int64_t *pairs, int64_t npairs)
 {
   if (!ctx) return GP_ERR_ARG;
@@ -134,7 +143,7 @@ extern "C" int gp_set_missing(gp_ctx *ctx, const int64_t *pairs, int64_t npairs)
   int64_t *d_pairs;
   int rc = gp_scratch(ctx, sizeof(int64_t) * 2 * (size_t)npairs, (void **)&d_pairs);
   if (rc) return rc;
-  GP_CUDA(ctx, cudaMemcpyAsync(d_pairs, pairs, sizeof(int64_t) * 2 * (size_t)npairs,
+  GP_CUDA(ctx, gp_memcpy(ctx, d_pairs, pairs, sizeof(int64_t) * 2 * (size_t)npairs,
                                cudaMemcpyHostToDevice, ctx->stream));
   k_set_missing<<<grid_for(ctx, npairs, 256), 256, 0, ctx->stream>>>(
       ctx->d_geno, ctx->rlen_dev, d_pairs, npairs, ctx->nsnp_all, ctx->nind_all);
@@ -188,7 +197,7 @@ extern "C" int gp_set_samples(gp_ctx *ctx, const int32_t *xindex, int32_t nrows)
   int64_t nwords = ctx->rlen_dev / 4;
   rc = gp_realloc(ctx, (void **)&ctx->d_rowmask, sizeof(uint32_t) * (size_t)nwords);
   if (rc) return rc;
-  GP_CUDA(ctx, cudaMemcpyAsync(ctx->d_rows, xindex, sizeof(int32_t) * (size_t)nrows,
+  GP_CUDA(ctx, gp_memcpy(ctx, ctx->d_rows, xindex, sizeof(int32_t) * (size_t)nrows,
                                cudaMemcpyHostToDevice, ctx->stream));
   GP_CUDA(ctx, cudaMemsetAsync(ctx->d_rowmask, 0, sizeof(uint32_t) * (size_t)nwords,
                                ctx->stream));
@@ -218,7 +227,7 @@ extern "C" int gp_set_snps(gp_ctx *ctx, const int32_t *snp_index, int32_t ncols)
   if (!rc) rc = gp_realloc(ctx, (void **)&ctx->d_xfancy, sizeof(double) * (size_t)ncols);
   if (!rc) rc = gp_realloc(ctx, (void **)&ctx->d_kept, sizeof(int32_t) * (size_t)ncols);
   if (rc) return rc;
-  GP_CUDA(ctx, cudaMemcpyAsync(ctx->d_cols, snp_index, sizeof(int32_t) * (size_t)ncols,
+  GP_CUDA(ctx, gp_memcpy(ctx, ctx->d_cols, snp_index, sizeof(int32_t) * (size_t)ncols,
                                cudaMemcpyHostToDevice, ctx->stream));
   ctx->ncols = ncols;
   ctx->xtx_valid = ctx->eig_valid = ctx->weights_valid = 0;
@@ -303,10 +312,10 @@ extern "C" int gp_valid_counts(gp_ctx *ctx, const uint8_t *sample_use, const uin
   uint8_t *d_su = (uint8_t *)(d_mask + nwords);
   uint8_t *d_pu = d_su + nsnp;
   if (snp_use)
-    GP_CUDA(ctx, cudaMemcpyAsync(d_su, snp_use, (size_t)nsnp, cudaMemcpyHostToDevice,
+    GP_CUDA(ctx, gp_memcpy(ctx, d_su, snp_use, (size_t)nsnp, cudaMemcpyHostToDevice,
                                  ctx->stream));
   if (sample_use) {
-    GP_CUDA(ctx, cudaMemcpyAsync(d_pu, sample_use, (size_t)ctx->nind_all,
+    GP_CUDA(ctx, gp_memcpy(ctx, d_pu, sample_use, (size_t)ctx->nind_all,
                                  cudaMemcpyHostToDevice, ctx->stream));
   } else {
     GP_CUDA(ctx, cudaMemsetAsync(d_pu, 1, (size_t)ctx->nind_all, ctx->stream));
@@ -318,7 +327,7 @@ extern "C" int gp_valid_counts(gp_ctx *ctx, const uint8_t *sample_use, const uin
     k_snp_valid<<<grid_for(ctx, nsnp * 32, 256), 256, 0, ctx->stream>>>(
         ctx->d_geno, ctx->rlen_dev, nsnp, d_mask, NULL, d_sv);
     GP_LAUNCH_CHECK(ctx, "k_snp_valid");
-    GP_CUDA(ctx, cudaMemcpyAsync(snp_valid, d_sv, sizeof(int32_t) * (size_t)nsnp,
+    GP_CUDA(ctx, gp_memcpy(ctx, snp_valid, d_sv, sizeof(int32_t) * (size_t)nsnp,
                                  cudaMemcpyDeviceToHost, ctx->stream));
   }
   if (sample_valid) {
@@ -329,7 +338,7 @@ extern "C" int gp_valid_counts(gp_ctx *ctx, const uint8_t *sample_use, const uin
                                                   snp_use ? d_su : NULL, ctx->nind_all, d_iv,
                                                   slice);
     GP_LAUNCH_CHECK(ctx, "k_sample_valid");
-    GP_CUDA(ctx, cudaMemcpyAsync(sample_valid, d_iv, sizeof(int32_t) * (size_t)ctx->nind_all,
+    GP_CUDA(ctx, gp_memcpy(ctx, sample_valid, d_iv, sizeof(int32_t) * (size_t)ctx->nind_all,
                                  cudaMemcpyDeviceToHost, ctx->stream));
   }
   GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));

@@ -187,6 +187,7 @@ int gp_gram_fp64(gp_ctx *ctx)
                                               ctx->d_cols, ctx->d_kept, ctx->nkept, ctx->d_vtab,
                                               kper, ctx->d_xtx, n, 0);
     GP_LAUNCH_CHECK(ctx, "k_gram_f64");
+    ctx->gram_launches = 1;
     return GP_OK;
   }
   double *part;
@@ -199,6 +200,7 @@ int gp_gram_fp64(gp_ctx *ctx)
                                             ctx->d_cols, ctx->d_kept, ctx->nkept, ctx->d_vtab, kper,
                                             part, n, stride);
   GP_LAUNCH_CHECK(ctx, "k_gram_f64");
+  ctx->gram_launches = 1;
   int blocks = (int)((stride + 255) / 256);
   if (blocks > ctx->num_sms * 16) blocks = ctx->num_sms * 16;
   k_reduce_splits<<<blocks, 256, 0, ctx->stream>>>(ctx->d_xtx, part, nsplit, stride, n, n);

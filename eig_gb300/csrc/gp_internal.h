@@ -57,6 +57,16 @@ struct gp_ctx {
   int weights_valid;
   int32_t nweights;
 
+  /* timing */
+  cudaEvent_t ev_t0, ev_t1, ev_g0, ev_g1;
+  double gram_ms;
+  int32_t gram_launches;
+  double gram_flops;
+
+  /* host<->device bytes copied by the handle (gp_transfer_bytes) */
+  int64_t h2d_bytes, d2h_bytes;
+  int64_t launches;   /* kernels of this library launched by the handle */
+
   /* scratch arena (grows on demand, freed at close) */
   void *d_scratch;
   size_t scratch_cap;
@@ -65,6 +75,9 @@ struct gp_ctx {
 };
 
 int gp_fail(gp_ctx *ctx, int code, const char *fmt, ...);
+/* cudaMemcpyAsync that also counts host<->device bytes on the handle */
+cudaError_t gp_memcpy(gp_ctx *ctx, void *dst, const void *src, size_t bytes, cudaMemcpyKind kind,
+                      cudaStream_t stream);
 int gp_cuda_fail(gp_ctx *ctx, cudaError_t e, const char *what);
 int gp_scratch(gp_ctx *ctx, size_t bytes, void **out);
 int gp_scratch2(gp_ctx *ctx, size_t bytes, void **out);
@@ -78,6 +91,7 @@ int gp_realloc(gp_ctx *ctx, void **ptr, size_t bytes);
 
 #define GP_LAUNCH_CHECK(ctx, what)                          \
   do {                                                       \
+    (ctx)->launches++;                                       \
     cudaError_t _e = cudaGetLastError();                     \
     if (_e != cudaSuccess) return gp_cuda_fail(ctx, _e, what); \
   } while (0)

@@ -84,7 +84,9 @@ int gp_smartpca_run(gp_ctx *ctx, const gp_smartpca_opts *o, const gp_panel *p,
   memset(r->t_phase, 0, sizeof r->t_phase);
   r->noutliers = 0;
   r->npasses = 0;
-  if (!ctx || !o || !p || !r || M < 1 || N < 1 || !p->records) return GP_ERR_ARG;
+  r->gram_flops = 0.0;
+  r->gram_ms = 0.0;
+  if (!ctx || !o || !p || !r || M < 1 || N < 1) return GP_ERR_ARG;
 
   snp_ign = (uint8_t *)calloc((size_t)M, 1);
   ind_ign = (uint8_t *)calloc((size_t)N, 1);
@@ -103,9 +105,19 @@ int gp_smartpca_run(gp_ctx *ctx, const gp_smartpca_opts *o, const gp_panel *p,
     FAIL(GP_ERR_NOMEM);
 
   /* ---- upload (inpack / getbedgenos) and the male-X-het rule -------------------------- */
-  rc = gp_load_genotypes(ctx, p->records, p->record_bytes, M, N, p->code);
-  if (rc) goto done;
-  if (!o->noxdata && p->ind_male && p->snp_chrom) {
+  if (p->records) {
+    rc = gp_load_genotypes(ctx, p->records, p->record_bytes, M, N, p->code);
+    if (rc) goto done;
+  } else {
+    /* resident panel: the records were uploaded by an earlier gp_load_genotypes */
+    int64_t rs = 0;
+    int32_t rn = 0;
+    gp_genotype_shape(ctx, &rs, &rn);
+    if (rs != M || rn != N)
+      FAIL(gp_fail_msg(ctx, GP_ERR_STATE, "resident panel is %lld x %d, run asks %lld x %d",
+                       (long long)rs, rn, (long long)M, N));
+  }
+  if (p->records && !o->noxdata && p->ind_male && p->snp_chrom) {
     /* checkxval: male het on chrom X -> missing (src/mcio.c:1606-1619, :2856-2863) */
     int64_t cap = 1024, np = 0;
     int64_t *pairs = (int64_t *)malloc(sizeof(int64_t) * 2 * (size_t)cap);
@@ -249,6 +261,12 @@ int gp_smartpca_run(gp_ctx *ctx, const gp_smartpca_opts *o, const gp_panel *p,
     int32_t nused;
     rc = gp_xtx(ctx, &xo, NULL, NULL, NULL, kill, NULL, NULL, NULL, &trace, &nused);
     if (rc) goto done;
+    {
+      double gms = 0.0, gfl = 0.0;
+      gp_last_gram_time(ctx, &gms, NULL, &gfl);
+      r->gram_ms += gms;
+      r->gram_flops += gfl;
+    }
     for (int32_t c = 0; c < ncols; ++c)
       if (kill[c]) {
         snp_ign[cols[c]] = 2; /* minallelecnt: ignored from now on */

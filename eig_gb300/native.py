@@ -26,7 +26,9 @@ EXPORTED = ["gp_version", "gp_last_error", "gp_open", "gp_close", "gp_device_byt
             "gp_load_genotypes", "gp_set_missing", "gp_valid_counts", "gp_set_samples",
             "gp_set_snps", "gp_xtx", "gp_eigvecs", "gp_ridoutlier", "gp_snp_weights",
             "gp_lsqproj", "gp_fastpca", "gp_smartpca_defaults", "gp_smartpca_run",
-            "gp_fail_msg"]
+            "gp_fail_msg", "gp_genotype_shape", "gp_timer_start", "gp_timer_stop",
+            "gp_last_gram_time", "gp_host_register", "gp_host_unregister",
+            "gp_transfer_bytes", "gp_launch_count"]
 
 i32p = C.POINTER(C.c_int32)
 i64p = C.POINTER(C.c_int64)
@@ -64,7 +66,8 @@ class RunResult(C.Structure):
                 ("outlier_iter", i32p), ("outlier_vec", i32p), ("outlier_score", f64p),
                 ("nrows", C.c_int32), ("ncols", C.c_int32), ("numeigs", C.c_int32),
                 ("noutliers", C.c_int32), ("npasses", C.c_int32),
-                ("t_phase", C.c_double * 8)]
+                ("t_phase", C.c_double * 8), ("gram_flops", C.c_double),
+                ("gram_ms", C.c_double)]
 
 
 _lib = None
@@ -100,6 +103,14 @@ def load_library():
         "gp_fastpca": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, f64p,
                                  C.c_int32, f64p, f64p]),
         "gp_smartpca_defaults": (None, [C.POINTER(SmartpcaOpts)]),
+        "gp_genotype_shape": (C.c_int, [vp, i64p, i32p]),
+        "gp_timer_start": (C.c_int, [vp]),
+        "gp_timer_stop": (C.c_int, [vp, f64p]),
+        "gp_last_gram_time": (C.c_int, [vp, f64p, i32p, f64p]),
+        "gp_host_register": (C.c_int, [vp, C.c_size_t]),
+        "gp_host_unregister": (C.c_int, [vp]),
+        "gp_transfer_bytes": (C.c_int, [vp, i64p, i64p, C.c_int32]),
+        "gp_launch_count": (C.c_int, [vp, i64p, C.c_int32]),
         "gp_smartpca_run": (C.c_int, [vp, C.POINTER(SmartpcaOpts), C.POINTER(Panel),
                                       C.POINTER(RunResult)]),
     }
@@ -258,6 +269,31 @@ class Handle:
                                        ptr(st, C.c_int32)), "gp_lsqproj")
         return a, b, nobs, st
 
+    def timer_start(self):
+        self.check(self.lib.gp_timer_start(self.h), "gp_timer_start")
+
+    def timer_stop(self):
+        ms = C.c_double()
+        self.check(self.lib.gp_timer_stop(self.h, C.byref(ms)), "gp_timer_stop")
+        return ms.value
+
+    def transfer_bytes(self, reset=False):
+        a, b = C.c_int64(), C.c_int64()
+        self.check(self.lib.gp_transfer_bytes(self.h, C.byref(a), C.byref(b), int(reset)),
+                   "gp_transfer_bytes")
+        return a.value, b.value
+
+    def launch_count(self, reset=False):
+        a = C.c_int64()
+        self.check(self.lib.gp_launch_count(self.h, C.byref(a), int(reset)), "gp_launch_count")
+        return a.value
+
+    def last_gram_time(self):
+        ms, n, fl = C.c_double(), C.c_int32(), C.c_double()
+        self.check(self.lib.gp_last_gram_time(self.h, C.byref(ms), C.byref(n), C.byref(fl)),
+                   "gp_last_gram_time")
+        return ms.value, n.value, fl.value
+
     def fastpca(self, K, L, I, seed=0, omega=None, precision=GP_PREC_FP64):
         n = self.nrows
         ev = np.zeros(K)
@@ -297,9 +333,13 @@ def smartpca_run(handle, records, nind, opts, code=GP_CODE_PACKED, snp_chrom=Non
                  snp_ignore=None, ind_ignore=None, ind_affstatus=None, ind_male=None):
     """Run the whole smartpca hot path (gp_smartpca_run) on in-memory records."""
     lib = handle.lib
-    rec = np.ascontiguousarray(records, dtype=np.uint8)
-    nsnp, rb = rec.shape
     keep = []
+    if isinstance(records, tuple):  # (nsnp, record_bytes): the panel resident on the handle
+        rec = None
+        nsnp, rb = records
+    else:
+        rec = np.ascontiguousarray(records, dtype=np.uint8)
+        nsnp, rb = rec.shape
 
     def arr(a, dt):
         if a is None:
@@ -335,7 +375,8 @@ def smartpca_run(handle, records, nind, opts, code=GP_CODE_PACKED, snp_chrom=Non
                outliers=[(int(out["outlier_idx"][i]), int(out["outlier_iter"][i]),
                           int(out["outlier_vec"][i]), float(out["outlier_score"][i]))
                          for i in range(min(r.noutliers, nind))],
-               t_phase={PHASES[i]: r.t_phase[i] for i in range(8)})
+               t_phase={PHASES[i]: r.t_phase[i] for i in range(8)},
+               gram_flops=r.gram_flops, gram_ms=r.gram_ms)
     return res
 
 
@@ -375,3 +416,15 @@ def synth_write_dataset(prefix, nsnp, pop_sizes, fst, miss=0.01, miss_hi=None, n
     rc = s.gp_synth_write_dataset(C.byref(spec), prefix.encode(), nthreads or os.cpu_count() or 1)
     if rc != 0:
         raise RuntimeError("gp_synth_write_dataset failed: %d" % rc)
+
+
+def host_register(a):
+    """page-lock a numpy buffer (cudaHostRegister) for fast uploads"""
+    lib = load_library()
+    rc = lib.gp_host_register(a.ctypes.data_as(vp), a.nbytes)
+    if rc != GP_OK:
+        raise GpuError("gp_host_register failed: %s" % lib.gp_last_error(None).decode())
+
+
+def host_unregister(a):
+    load_library().gp_host_unregister(a.ctypes.data_as(vp))

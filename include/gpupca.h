@@ -69,6 +69,9 @@ int gp_device_bytes(const gp_ctx *ctx, int64_t *bytes);
 int gp_load_genotypes(gp_ctx *ctx, const uint8_t *records, int64_t record_bytes,
                       int64_t nsnp, int32_t nind, int32_t code);
 
+/* Shape of the resident panel (0 when none is loaded). */
+int gp_genotype_shape(const gp_ctx *ctx, int64_t *nsnp, int32_t *nind);
+
 /*
  * Set a genotype to missing in the device panel (the male-X-het rule, checkxval
  * src/mcio.c:1606-1619, applied by putgtypes(cupt, k, -1) in inpack :2856-2863).
@@ -171,6 +174,28 @@ int gp_lsqproj(gp_ctx *ctx, int32_t numeigs, const int32_t *samples, int32_t npr
  */
 int gp_fastpca(gp_ctx *ctx, int32_t K, int32_t L, int32_t I, uint64_t seed,
                const double *omega, int32_t precision, double *evals, double *evecs);
+
+
+/* ---- measurement helpers (no counterpart in the reference) ---------------------------- */
+
+/* Device stopwatch on the handle's stream (CUDA events); stop synchronises the stream. */
+int gp_timer_start(gp_ctx *ctx);
+int gp_timer_stop(gp_ctx *ctx, double *ms);
+
+/* Device time of the Gram kernel launches of the last gp_xtx call (CUDA events around them
+ * on the handle's stream), the number of Gram-kernel launches, and the algorithmic flop
+ * count nrows*(nrows+1)*kept_snps of that call. */
+int gp_last_gram_time(const gp_ctx *ctx, double *ms, int32_t *launches, double *flops);
+
+/* Host->device and device->host bytes the handle has copied (optionally reset to 0). */
+int gp_transfer_bytes(gp_ctx *ctx, int64_t *h2d, int64_t *d2h, int32_t reset);
+
+/* Number of this library's own kernels the handle has launched (optionally reset). */
+int gp_launch_count(gp_ctx *ctx, int64_t *launches, int32_t reset);
+
+/* Page-lock a host buffer for fast uploads (cudaHostRegister) and release it. */
+int gp_host_register(void *ptr, size_t bytes);
+int gp_host_unregister(void *ptr);
 
 #ifdef __cplusplus
 }

@@ -38,7 +38,8 @@ typedef struct {
 } gp_smartpca_opts;
 
 typedef struct {
-  const uint8_t *records;      /* nsnp records, SNP-major, sorted SNP order */
+  const uint8_t *records;      /* nsnp records, SNP-major, sorted SNP order; NULL = use the
+                                  panel already resident on the handle (gp_load_genotypes) */
   int64_t record_bytes;
   int64_t nsnp;
   int32_t nind;
@@ -76,6 +77,8 @@ typedef struct {
   /* scalar results */
   int32_t nrows, ncols, numeigs, noutliers, npasses;
   double t_phase[8];       /* wall seconds per GP_PH_* phase */
+  double gram_flops;       /* algorithmic Gram flops, sum over passes of N_p (N_p+1) M_p */
+  double gram_ms;          /* device time of the Gram kernels, sum over passes */
 } gp_run_result;
 
 void gp_smartpca_defaults(gp_smartpca_opts *o);

@@ -1,12 +1,439 @@
-/* placeholder until the tcgen05 split-BF16 Gram lands */
+/*
+ * Split-BF16 Gram on the 5th-generation tensor cores (tcgen05), replacing the reference's
+ * XTX accumulation (domult_increment_lookup / block_increment_binary,
+ * src/eigensrc/smartpca.c:3361-3495) for GP_PREC_SPLIT_BF16.
+ *
+ * Each normalised value v (the FP64 table entry of its SNP and genotype code) is split into
+ * hi = bf16(v) and lo = bf16(v - hi).  XTX = Xhi Xhi^T + Xhi Xlo^T + Xlo Xhi^T (the lo*lo term
+ * is dropped): three BF16 MMAs with FP32 accumulation in TMEM within a SNP chunk, and FP64
+ * accumulation across chunks, also kept in TMEM.
+ *
+ * Data layout in HBM: Xhi and Xlo as row-major [Npad][Kc] bf16 (samples x kept SNPs of the
+ * current super-chunk), written by k_split_materialize from the packed records; the Gram
+ * kernel reads them with TMA as 128-row x 64-SNP boxes in the 128-byte swizzle.
+ *
+ * Kernel structure (persistent, one CTA per SM, 6 warps):
+ *   warp 0      TMA producer: per k-block of 64 SNPs four 16 KB boxes (A hi/lo, B hi/lo)
+ *               into a 3-stage shared-memory ring;
+ *   warp 1      allocates 512 TMEM columns; one thread issues 12 tcgen05.mma (128x128x16)
+ *               per k-block into FP32 accumulator buffer (chunk & 1), columns 0-255;
+ *   warps 2-5   epilogue: at the end of each chunk add the FP32 buffer into the FP64
+ *               running sum held in TMEM columns 256-511 (two 32-bit words per element),
+ *               release the buffer, and after the last chunk of a tile write the FP64 tile
+ *               to the Gram in global memory.
+ * Tiles are the 128x128 blocks of the lower triangle, distributed round-robin over CTAs.
+ */
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+
+#include <stdlib.h>
+
 #include "gp_internal.h"
+#include "gp_tc.cuh"
+
+#define BT 128          /* tile edge (rows of A and B) */
+#define BK 64           /* SNPs per k-block (128 bytes of bf16) */
+#define NSTAGE 3
+#define BOX_BYTES (BT * BK * 2)
+#define STAGE_BYTES (4 * BOX_BYTES)
+#define GRAM_THREADS 192
+#define GRAM_SMEM (NSTAGE * STAGE_BYTES + 1024 + 256)
+
+/* error codes recorded by the kernel */
+#define GP_KERR_TIMEOUT_FULL 1
+#define GP_KERR_TIMEOUT_EMPTY 2
+#define GP_KERR_TIMEOUT_ACCF 3
+#define GP_KERR_TIMEOUT_ACCE 4
+
+__device__ __forceinline__ void tri_tile(int32_t t, int32_t *bi, int32_t *bj)
+{
+  int32_t i = (int32_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+  while ((i + 1) * (i + 2) / 2 <= t) ++i;
+  while (i * (i + 1) / 2 > t) --i;
+  *bi = i;
+  *bj = t - i * (i + 1) / 2;
+}
+
+/*
+ * grams: XTX (n x n row-major FP64); accumulate != 0 adds to the values already there
+ * (super-chunks after the first).  nkb = k-blocks of this super-chunk; chunk_kb = k-blocks
+ * per FP32 accumulation chunk.
+ */
+__global__ void __launch_bounds__(GRAM_THREADS, 1)
+k_gram_split_bf16(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ CUtensorMap tm_lo,
+                  int32_t ntiles, int32_t nkb, int32_t chunk_kb, double *xtx, int32_t n,
+                  int32_t accumulate, int *err)
+{
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t *bars = (uint64_t *)(smem + NSTAGE * STAGE_BYTES);
+  uint64_t *full = bars;                 /* [NSTAGE] */
+  uint64_t *empty = bars + NSTAGE;       /* [NSTAGE] */
+  uint64_t *accf = bars + 2 * NSTAGE;    /* [2] */
+  uint64_t *acce = bars + 2 * NSTAGE + 2;/* [2] */
+  uint64_t *drain = bars + 2 * NSTAGE + 4; /* abort path: wait for issued MMAs */
+  uint32_t *tmem_slot = (uint32_t *)(bars + 2 * NSTAGE + 5);
+  volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NSTAGE; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&accf[b], 1);
+      mbar_init(&acce[b], 4);
+    }
+    mbar_init(drain, 1);
+    *abort_flag = 0;
+    fence_mbar_init();
+  }
+  if (warp == 0 && lane == 0) {
+    tma_prefetch_desc(&tm_hi);
+    tma_prefetch_desc(&tm_lo);
+  }
+  if (warp == 1) tmem_alloc(tmem_slot, 512);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  const int32_t nchunk = (nkb + chunk_kb - 1) / chunk_kb;
+
+  if (warp == 0) {
+    /* ---------------- TMA producer ---------------- */
+    if (lane == 0) {
+      uint32_t it = 0;
+      for (int32_t t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x) {
+        int32_t bi, bj;
+        tri_tile(t, &bi, &bj);
+        for (int32_t kb = 0; kb < nkb; ++kb, ++it) {
+          uint32_t s = it % NSTAGE, ph = (it / NSTAGE) & 1u;
+          if (!mbar_wait(&empty[s], ph ^ 1u, abort_flag, err, GP_KERR_TIMEOUT_EMPTY)) break;
+          uint8_t *st = smem + s * STAGE_BYTES;
+          mbar_arrive_expect_tx(&full[s], STAGE_BYTES);
+          tma_load_2d(st, &tm_hi, &full[s], kb * BK, bi * BT);
+          tma_load_2d(st + BOX_BYTES, &tm_lo, &full[s], kb * BK, bi * BT);
+          tma_load_2d(st + 2 * BOX_BYTES, &tm_hi, &full[s], kb * BK, bj * BT);
+          tma_load_2d(st + 3 * BOX_BYTES, &tm_lo, &full[s], kb * BK, bj * BT);
+        }
+      }
+      if (*abort_flag) {
+        /* copies already issued must land before the CTA exits (bounded) */
+        uint32_t last = it < NSTAGE ? it : NSTAGE;
+        for (uint32_t j = it - last; j < it; ++j) {
+          uint64_t t0 = globaltimer_ns();
+          while (!mbar_try_wait(&full[j % NSTAGE], (j / NSTAGE) & 1u) &&
+                 globaltimer_ns() - t0 < GP_WAIT_NS) {
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    /* ---------------- MMA issuer ---------------- */
+    if (lane == 0) {
+      const uint32_t idesc = idesc_bf16_f32(BT, BT);
+      uint32_t it = 0, chunk = 0;
+      bool ok = true;
+      for (int32_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        for (int32_t c = 0; c < nchunk && ok; ++c, ++chunk) {
+          uint32_t buf = chunk & 1u, use = chunk >> 1;
+          if (!mbar_wait(&acce[buf], (use & 1u) ^ 1u, abort_flag, err, GP_KERR_TIMEOUT_ACCE)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t d = tmem + buf * BT;
+          int32_t kb0 = c * chunk_kb, kb1 = kb0 + chunk_kb < nkb ? kb0 + chunk_kb : nkb;
+          for (int32_t kb = kb0; kb < kb1; ++kb, ++it) {
+            uint32_t s = it % NSTAGE, ph = (it / NSTAGE) & 1u;
+            if (!mbar_wait(&full[s], ph, abort_flag, err, GP_KERR_TIMEOUT_FULL)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            uint32_t base = smem_u32(smem + s * STAGE_BYTES);
+            uint64_t ahi = sdesc_k128(base), alo = sdesc_k128(base + BOX_BYTES);
+            uint64_t bhi = sdesc_k128(base + 2 * BOX_BYTES), blo = sdesc_k128(base + 3 * BOX_BYTES);
+#pragma unroll
+            for (int k = 0; k < BK / 16; ++k) {
+              /* +32 bytes along K per 16 bf16 = +2 in the 16-byte address field */
+              uint64_t o = (uint64_t)(2 * k);
+              uint32_t acc0 = (kb > kb0 || k > 0) ? 1u : 0u;
+              umma_bf16(d, ahi + o, bhi + o, idesc, acc0);
+              umma_bf16(d, ahi + o, blo + o, idesc, 1u);
+              umma_bf16(d, alo + o, bhi + o, idesc, 1u);
+            }
+            umma_commit(&empty[s]);
+          }
+          if (!ok) break;
+          umma_commit(&accf[buf]);
+        }
+      }
+    }
+  } else {
+    /* ---------------- epilogue (warps 2..5) ---------------- */
+    const int q = warp & 3;               /* TMEM lane quarter this warp may access */
+    const int row = q * 32 + lane;         /* row of the tile */
+    const uint32_t lane_addr = (uint32_t)(q * 32) << 16;
+    uint32_t chunk = 0;
+    bool ok = true;
+    for (int32_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+      int32_t bi, bj;
+      tri_tile(t, &bi, &bj);
+      const int32_t gi = bi * BT + row;
+      /* FP64 running sum in TMEM columns 256..511: start from 0 or from the Gram so far */
+      for (int j0 = 0; j0 < BT; j0 += 8) {
+        uint32_t w[16];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          double v = 0.0;
+          int32_t gj = bj * BT + j0 + u;
+          if (accumulate && gi < n && gj < n) v = xtx[(int64_t)gi * n + gj];
+          uint64_t b = (uint64_t)__double_as_longlong(v);
+          w[2 * u] = (uint32_t)b;
+          w[2 * u + 1] = (uint32_t)(b >> 32);
+        }
+        tmem_st16(tmem + lane_addr + 256 + 2 * j0, w);
+      }
+      tmem_wait_st();
+      for (int32_t c = 0; c < nchunk; ++c, ++chunk) {
+        uint32_t buf = chunk & 1u, use = chunk >> 1;
+        bool got = mbar_wait(&accf[buf], use & 1u, abort_flag, err, GP_KERR_TIMEOUT_ACCF);
+        if (!__all_sync(0xffffffffu, got)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        for (int j0 = 0; j0 < BT; j0 += 16) {
+          uint32_t f[16], w0[16], w1[16];
+          tmem_ld16(tmem + lane_addr + buf * BT + j0, f);
+          tmem_ld16(tmem + lane_addr + 256 + 2 * j0, w0);
+          tmem_ld16(tmem + lane_addr + 256 + 2 * j0 + 16, w1);
+          tmem_wait_ld();
+#pragma unroll
+          for (int u = 0; u < 16; ++u) {
+            uint32_t *w = u < 8 ? w0 : w1;
+            int v = u & 7;
+            uint64_t b = ((uint64_t)w[2 * v + 1] << 32) | w[2 * v];
+            double sum = __longlong_as_double((long long)b) + (double)__uint_as_float(f[u]);
+            b = (uint64_t)__double_as_longlong(sum);
+            w[2 * v] = (uint32_t)b;
+            w[2 * v + 1] = (uint32_t)(b >> 32);
+          }
+          tmem_st16(tmem + lane_addr + 256 + 2 * j0, w0);
+          tmem_st16(tmem + lane_addr + 256 + 2 * j0 + 16, w1);
+        }
+        tmem_wait_st();
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&acce[buf]);
+      }
+      if (!ok) break;
+      /* the FP64 tile -> Gram rows (every lane loads; rows past n store nothing) */
+      double *orow = xtx + (int64_t)gi * n;
+      for (int j0 = 0; j0 < BT; j0 += 8) {
+        uint32_t w[16];
+        tmem_ld16(tmem + lane_addr + 256 + 2 * j0, w);
+        tmem_wait_ld();
+        if (gi < n) {
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            int32_t gj = bj * BT + j0 + u;
+            if (gj < n) {
+              uint64_t b = ((uint64_t)w[2 * u + 1] << 32) | w[2 * u];
+              orow[gj] = __longlong_as_double((long long)b);
+            }
+          }
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 1) {
+    if (*abort_flag && lane == 0) {
+      /* let MMAs already issued finish before the columns are released */
+      umma_commit(drain);
+      uint64_t t0 = globaltimer_ns();
+      while (!mbar_try_wait(drain, 0) && globaltimer_ns() - t0 < GP_WAIT_NS) {
+      }
+    }
+    __syncwarp();
+    tmem_dealloc(tmem, 512);
+  }
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* split materialisation                                                                  */
+
+/* per kept column: (hi, lo) bf16 pairs for codes 0..3 packed as 4 x uint32 (lo<<16 | hi) */
+__global__ void k_split_tables(const int32_t *kept, int32_t nkept, const double *vtab,
+                               uint32_t *split)
+{
+  for (int32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nkept; k += gridDim.x * blockDim.x) {
+    int32_t c = kept[k];
+    for (int g = 0; g < 4; ++g) {
+      double v = vtab[4 * c + g];
+      __nv_bfloat16 hi = __double2bfloat16(v);
+      double r = v - (double)__bfloat162float(hi);
+      __nv_bfloat16 lo = __double2bfloat16(r);
+      uint32_t h = (uint32_t)__bfloat16_as_ushort(hi), l = (uint32_t)__bfloat16_as_ushort(lo);
+      split[4 * k + g] = h | (l << 16);
+    }
+  }
+}
+
+/*
+ * Xhi/Xlo [npad][kc] for kept columns [k0, k0 + kc): thread = (row, 8 consecutive SNPs) ->
+ * two 16-byte stores.  Rows >= nrows and columns >= nkept are zero.
+ */
+__global__ void k_split_materialize(const uint8_t *__restrict__ geno, int64_t rlen,
+                                    const int32_t *__restrict__ rows, int32_t nrows,
+                                    const int32_t *__restrict__ cols, const int32_t *__restrict__ kept,
+                                    int32_t nkept, const uint32_t *__restrict__ split, int32_t k0,
+                                    int32_t kc, int32_t npad, __nv_bfloat16 *xhi, __nv_bfloat16 *xlo)
+{
+  const int32_t groups = kc / 8;
+  int64_t total = (int64_t)npad * groups;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int32_t r = (int32_t)(idx / groups), gq = (int32_t)(idx - (int64_t)r * groups);
+    uint32_t hv[4] = {0, 0, 0, 0}, lv[4] = {0, 0, 0, 0};
+    if (r < nrows) {
+      int32_t sidx = rows[r];
+      int32_t byte = sidx >> 2, sh = (3 - (sidx & 3)) * 2;
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        int32_t k = k0 + gq * 8 + u;
+        uint32_t pair = 0;
+        if (k < nkept) {
+          int32_t c = kept[k];
+          uint32_t code = (__ldg(geno + (int64_t)cols[c] * rlen + byte) >> sh) & 3u;
+          pair = __ldg(split + 4 * k + code);
+        }
+        uint32_t h = pair & 0xFFFFu, l = pair >> 16;
+        hv[u >> 1] |= h << ((u & 1) * 16);
+        lv[u >> 1] |= l << ((u & 1) * 16);
+      }
+    }
+    int64_t off = (int64_t)r * kc + gq * 8;
+    *(uint4 *)(xhi + off) = make_uint4(hv[0], hv[1], hv[2], hv[3]);
+    *(uint4 *)(xlo + off) = make_uint4(lv[0], lv[1], lv[2], lv[3]);
+  }
+}
+
+/* ------------------------------------------------------------------------------------ */
+
+static PFN_cuTensorMapEncodeTiled_v12000 get_encode(gp_ctx *ctx)
+{
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = NULL;
+  if (fn) return fn;
+  cudaDriverEntryPointQueryResult q;
+  void *p = NULL;
+  cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                                   cudaEnableDefault, &q);
+  if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !p) {
+    gp_fail(ctx, GP_ERR_CUDA, "cuTensorMapEncodeTiled entry point not found");
+    return NULL;
+  }
+  fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+  return fn;
+}
+
+static int make_map(gp_ctx *ctx, CUtensorMap *m, void *base, int32_t rows, int32_t cols)
+{
+  PFN_cuTensorMapEncodeTiled_v12000 enc = get_encode(ctx);
+  if (!enc) return GP_ERR_CUDA;
+  cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)cols * 2};
+  cuuint32_t box[2] = {BK, BT};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return gp_fail(ctx, GP_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return GP_OK;
+}
+
+/* FP32 accumulation depth in SNPs (k-blocks of 64) before the FP64 add; split budget in bytes */
+#define GP_BF16_CHUNK_KB 32
+#define GP_BF16_BUDGET (24ll << 30)
+
 int gp_gram_split_bf16(gp_ctx *ctx)
 {
-  return gp_fail(ctx, GP_ERR_NOTBUILT, "split-BF16 Gram not built yet");
-}
-extern "C" int gp_fastpca(gp_ctx *ctx, int32_t K, int32_t L, int32_t I, uint64_t seed,
-                          const double *omega, int32_t precision, double *evals, double *evecs)
-{
-  (void)K; (void)L; (void)I; (void)seed; (void)omega; (void)precision; (void)evals; (void)evecs;
-  return gp_fail(ctx, GP_ERR_NOTBUILT, "fastmode not built yet");
+  const int32_t n = ctx->nrows, nk = ctx->nkept;
+  const int32_t npad = (n + BT - 1) / BT * BT;
+  const int32_t nt = npad / BT, ntiles = nt * (nt + 1) / 2;
+  GP_CUDA(ctx, cudaMemsetAsync(ctx->d_xtx, 0, sizeof(double) * (size_t)n * n, ctx->stream));
+  if (nk == 0) return GP_OK;
+  const int32_t kpad = (nk + BK - 1) / BK * BK;
+  /* super-chunk of kept SNPs so that Xhi + Xlo fit the budget; the budget and the FP32
+   * chunk depth can be overridden (GP_BF16_BUDGET_BYTES, GP_BF16_CHUNK_SNPS) for tests and
+   * accuracy sweeps */
+  int64_t budget = GP_BF16_BUDGET;
+  int32_t chunk_kb = GP_BF16_CHUNK_KB;
+  {
+    const char *e = getenv("GP_BF16_BUDGET_BYTES");
+    if (e && atoll(e) > 0) budget = atoll(e);
+    e = getenv("GP_BF16_CHUNK_SNPS");
+    if (e && atoi(e) >= BK) chunk_kb = atoi(e) / BK;
+  }
+  int64_t per_col = (int64_t)npad * 4;
+  int64_t kc_max = budget / per_col / BK * BK;
+  if (kc_max < BK) kc_max = BK;
+  int32_t kc = (int32_t)(kpad < kc_max ? kpad : kc_max);
+  size_t xbytes = (size_t)npad * kc * 2;
+  size_t tab_bytes = (size_t)nk * 16 + 256;
+  uint8_t *base;
+  int rc = gp_scratch2(ctx, 2 * xbytes + tab_bytes + 256, (void **)&base);
+  if (rc) return rc;
+  __nv_bfloat16 *xhi = (__nv_bfloat16 *)base;
+  __nv_bfloat16 *xlo = (__nv_bfloat16 *)(base + xbytes);
+  uint32_t *split = (uint32_t *)(base + 2 * xbytes);
+  int *d_err;
+  rc = gp_scratch(ctx, 256, (void **)&d_err);
+  if (rc) return rc;
+  GP_CUDA(ctx, cudaMemsetAsync(d_err, 0, sizeof(int), ctx->stream));
+  {
+    int blocks = (nk + 255) / 256;
+    if (blocks > ctx->num_sms * 8) blocks = ctx->num_sms * 8;
+    k_split_tables<<<blocks, 256, 0, ctx->stream>>>(ctx->d_kept, nk, ctx->d_vtab, split);
+    GP_LAUNCH_CHECK(ctx, "k_split_tables");
+  }
+  static int attr_set = 0;
+  if (!attr_set) {
+    GP_CUDA(ctx, cudaFuncSetAttribute(k_gram_split_bf16, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      GRAM_SMEM));
+    attr_set = 1;
+  }
+  CUtensorMap mhi, mlo;
+  rc = make_map(ctx, &mhi, xhi, npad, kc);
+  if (!rc) rc = make_map(ctx, &mlo, xlo, npad, kc);
+  if (rc) return rc;
+  int grid = ctx->num_sms < ntiles ? ctx->num_sms : ntiles;
+  for (int32_t k0 = 0; k0 < kpad; k0 += kc) {
+    int32_t kcur = kpad - k0 < kc ? kpad - k0 : kc;
+    int64_t work = (int64_t)npad * (kc / 8);
+    int blocks = (int)((work + 255) / 256);
+    if (blocks > ctx->num_sms * 32) blocks = ctx->num_sms * 32;
+    /* columns beyond kcur in this super-chunk are zero (k >= nkept guard covers the tail) */
+    k_split_materialize<<<blocks, 256, 0, ctx->stream>>>(ctx->d_geno, ctx->rlen_dev, ctx->d_rows, n,
+                                                         ctx->d_cols, ctx->d_kept, nk, split, k0, kc,
+                                                         npad, xhi, xlo);
+    GP_LAUNCH_CHECK(ctx, "k_split_materialize");
+    int32_t nkb = kcur / BK;
+    k_gram_split_bf16<<<grid, GRAM_THREADS, GRAM_SMEM, ctx->stream>>>(
+        mhi, mlo, ntiles, nkb, chunk_kb, ctx->d_xtx, n, k0 > 0 ? 1 : 0, d_err);
+    GP_LAUNCH_CHECK(ctx, "k_gram_split_bf16");
+    ctx->gram_launches++;
+  }
+  int herr = 0;
+  GP_CUDA(ctx, gp_memcpy(ctx, &herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (herr) return gp_fail(ctx, GP_ERR_TIMEOUT, "split-BF16 Gram kernel wait timed out (code %d)", herr);
+  return GP_OK;
 }

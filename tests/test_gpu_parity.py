@@ -180,3 +180,64 @@ def test_cli_dropin_matches_reference_text(case, tmp_path):
     assert np.max(np.abs(A - B * s)) <= 1.01e-4
     got_out = open(d / "out.outliers").read()
     assert got_out == open(d / "ref.outliers").read()
+
+
+def _gram_pair(gpu, rec, nind, rows, cols, precision):
+    gpu.load_genotypes(rec, nind)
+    gpu.set_samples(rows)
+    gpu.set_snps(cols)
+    return gpu.xtx(precision=precision)
+
+
+@pytest.mark.parametrize("shape", [(333, 3000), (128, 64), (1000, 5000)])
+def test_split_bf16_gram_vs_oracle(gpu, shape):
+    """split-BF16 Gram (tcgen05) against the FP64 oracle Gram: the hi+lo split keeps about
+    17 significant bits per value, so elementwise error <= 2e-5 of the largest entry."""
+    nind, nsnp = shape
+    rec, pop = synth(nsnp, [nind // 3, nind // 3, nind - 2 * (nind // 3)], [0.01, 0.03, 0.05],
+                     miss=0.02, seed=31)
+    rows = np.arange(nind, dtype=np.int32)
+    cols = np.arange(nsnp, dtype=np.int32)
+    r = _gram_pair(gpu, rec, nind, rows, cols, native.GP_PREC_SPLIT_BF16)
+    s = O.pass_columns(rec, cols, rows)
+    X = O.gram(s)
+    scale = np.max(np.abs(X))
+    err = np.max(np.abs(r["XTX"] - X)) / scale
+    assert err <= 2e-5, err
+    assert np.array_equal(r["killed"], s.killed)
+
+
+def test_split_bf16_multi_tile_chunks_and_superchunks(gpu, monkeypatch):
+    """2600 samples (21 tile rows, 231 tiles: several per CTA), 6000 SNPs in FP32 chunks of
+    1024 and super-chunks of 2048 SNPs (FP64 carried through the Gram between launches),
+    against the FP64 GPU Gram."""
+    nind, nsnp = 2600, 6000
+    rec, pop = synth(nsnp, [900, 900, 800], [0.01, 0.02, 0.04], miss=0.02, seed=32)
+    rows = np.arange(nind, dtype=np.int32)
+    cols = np.arange(nsnp, dtype=np.int32)
+    ref = _gram_pair(gpu, rec, nind, rows, cols, native.GP_PREC_FP64)["XTX"]
+    monkeypatch.setenv("GP_BF16_CHUNK_SNPS", "1024")
+    monkeypatch.setenv("GP_BF16_BUDGET_BYTES", str(2688 * 4 * 2048))
+    r = _gram_pair(gpu, rec, nind, rows, cols, native.GP_PREC_SPLIT_BF16)
+    err = np.max(np.abs(r["XTX"] - ref)) / np.max(np.abs(ref))
+    assert err <= 2e-5, err
+    w1 = np.linalg.eigvalsh(r["XTX"])[::-1][:20]
+    w0 = np.linalg.eigvalsh(ref)[::-1][:20]
+    assert np.max(np.abs(w1 - w0) / w0) <= 1e-6
+
+
+def test_split_bf16_subset_rows(gpu):
+    """row subsets (outlier removal) and killed columns through the split path"""
+    rec, pop = synth(4000, [200, 200, 150], [0.01, 0.02, 0.05], miss=0.05, seed=33)
+    nind = len(pop)
+    rng = np.random.default_rng(4)
+    rows = np.sort(rng.choice(nind, 401, replace=False)).astype(np.int32)
+    cols = np.sort(rng.choice(4000, 3333, replace=False)).astype(np.int32)
+    gpu.load_genotypes(rec, nind)
+    gpu.set_samples(rows)
+    gpu.set_snps(cols)
+    r = gpu.xtx(precision=native.GP_PREC_SPLIT_BF16, minallelecnt=20)
+    s = O.pass_columns(rec, cols, rows, minallelecnt=20)
+    X = O.gram(s)
+    assert (s.killed == 1).sum() > 0
+    assert np.max(np.abs(r["XTX"] - X)) / np.max(np.abs(X)) <= 2e-5

@@ -137,7 +137,7 @@ def run_gpu(args, cfg, world, rank, local, dist):
 
     from eig_gb300 import native
     torch.cuda.set_device(local)
-    prec = native.GP_PREC_SPLIT_BF16 if args.precision == "bf16" else native.GP_PREC_FP64
+    prec = native.PRECISIONS[args.precision]
     t0 = time.time()
     rec, pop = native.synth_records(cfg["nsnp"], cfg["pops"], cfg["fst"], miss=cfg["miss"],
                                     seed=cfg["seed"])
@@ -249,7 +249,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--precision", default="bf16", choices=["bf16", "fp64"])
+    ap.add_argument("--precision", default="fp16", choices=["fp64", "bf16", "bf16x4", "fp16"])
     ap.add_argument("--config", default="full", choices=list(CONFIGS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -288,7 +288,7 @@ def main():
     value = world * res["gram_flops"] / (res["step_ms"] * 1e-3) / 1e12
     e2e = world * res["gram_flops"] / (res["e2e_ms"] * 1e-3) / 1e12
     peaks = res["peaks"]
-    if args.precision == "bf16":
+    if args.precision != "fp64":
         achieved = res["gram_kernel_flops"] / (res["gram_ms"] * 1e-3) / 1e12
         peak = peaks.get("bf16_tflops", 1900.0)
         roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
@@ -302,7 +302,9 @@ def main():
     line = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["step_ms"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "bf16x3 split (fp32 in tile, fp64 across)" if args.precision == "bf16" else "f64",
+            "dtype": {"fp64": "f64", "bf16": "bf16 hi+lo x3 MMA (fp32 in chunk, fp64 across)",
+                      "bf16x4": "bf16 hi+lo x4 MMA (fp32 in chunk, fp64 across)",
+                      "fp16": "fp16 hi+lo x3 MMA (fp32 in chunk, fp64 across)"}[args.precision],
             "data": "synthetic (seeded Balding-Nichols)", "config": config,
             "pca_wall_s": res["step_ms"] / 1e3,
             "phases_s": {k: round(v, 4) for k, v in r["t_phase"].items()},

@@ -184,7 +184,7 @@ extern "C" int gp_xtx(gp_ctx *ctx, const gp_xtx_opts *opts, int32_t *n0, int32_t
   if (!ctx || !opts) return GP_ERR_ARG;
   if (!ctx->d_geno || ctx->nrows < 1 || ctx->ncols < 1)
     return gp_fail(ctx, GP_ERR_STATE, "gp_xtx: genotypes, samples and SNPs must be set first");
-  if (opts->precision != GP_PREC_FP64 && opts->precision != GP_PREC_SPLIT_BF16)
+  if (opts->precision < GP_PREC_FP64 || opts->precision > GP_PREC_SPLIT_FP16)
     return gp_fail(ctx, GP_ERR_ARG, "gp_xtx: unknown precision %d", opts->precision);
   GP_CUDA(ctx, cudaSetDevice(ctx->device));
   const int32_t n = ctx->nrows, nc = ctx->ncols;
@@ -220,7 +220,7 @@ extern "C" int gp_xtx(gp_ctx *ctx, const gp_xtx_opts *opts, int32_t *n0, int32_t
   if (opts->precision == GP_PREC_FP64)
     rc = gp_gram_fp64(ctx);
   else
-    rc = gp_gram_split_bf16(ctx);
+    rc = gp_gram_split(ctx, opts->precision);
   if (rc) return rc;
   GP_CUDA(ctx, cudaEventRecord(ctx->ev_g1, ctx->stream));
 

@@ -4,27 +4,34 @@
  * src/eigensrc/smartpca.c:3361-3495) for GP_PREC_SPLIT_BF16.
  *
  * Each normalised value v (the FP64 table entry of its SNP and genotype code) is split into
- * hi = bf16(v) and lo = bf16(v - hi).  XTX = Xhi Xhi^T + Xhi Xlo^T + Xlo Xhi^T (the lo*lo term
- * is dropped): three BF16 MMAs with FP32 accumulation in TMEM within a SNP chunk, and FP64
- * accumulation across chunks, also kept in TMEM.
+ * hi = r(v) and lo = r(v - hi) in a 16-bit format (bf16 or fp16).  XTX = Xhi Xhi^T +
+ * Xhi Xlo^T + Xlo Xhi^T (+ Xlo Xlo^T with 4 MMAs): tcgen05 MMAs with FP32 accumulation in
+ * TMEM over a short SNP chunk (128 SNPs by default: the tensor core's FP32 accumulation
+ * truncates, so its error grows with the chunk depth), chunk sums added in FP32 registers
+ * (round to nearest) for a few chunks, then folded into a per-element running sum held in
+ * TMEM as an FP32 (hi, lo) pair with TwoSum (~48 bits), which stands in for FP64
+ * accumulation at FP32 speed (GB300's FP64 rate is a small fraction of its FP32 rate); the
+ * tile is written out in FP64.
  *
  * Data layout in HBM: Xhi and Xlo as row-major [Npad][Kc] bf16 (samples x kept SNPs of the
  * current super-chunk), written by k_split_materialize from the packed records; the Gram
  * kernel reads them with TMA as 128-row x 64-SNP boxes in the 128-byte swizzle.
  *
- * Kernel structure (persistent, one CTA per SM, 6 warps):
+ * Kernel structure (persistent, one CTA per SM, 18 warps):
  *   warp 0      TMA producer: per k-block of 64 SNPs four 16 KB boxes (A hi/lo, B hi/lo)
  *               into a 3-stage shared-memory ring;
- *   warp 1      allocates 512 TMEM columns; one thread issues 12 tcgen05.mma (128x128x16)
- *               per k-block into FP32 accumulator buffer (chunk & 1), columns 0-255;
- *   warps 2-5   epilogue: at the end of each chunk add the FP32 buffer into the FP64
- *               running sum held in TMEM columns 256-511 (two 32-bit words per element),
- *               release the buffer, and after the last chunk of a tile write the FP64 tile
- *               to the Gram in global memory.
+ *   warp 1      allocates 512 TMEM columns; one thread issues 12 (or 16) tcgen05.mma
+ *               (128x128x16) per k-block into FP32 accumulator buffer (chunk & 1),
+ *               columns 0-255;
+ *   warps 2-17  epilogue: at the end of each chunk read the FP32 buffer (tcgen05.ld),
+ *               release it and add it into registers; every GP_FOLD chunks fold those into
+ *               the (hi, lo) running sums in TMEM columns 256-511; after the last chunk of a
+ *               tile write the tile to the Gram in FP64.
  * Tiles are the 128x128 blocks of the lower triangle, distributed round-robin over CTAs.
  */
 #include <cuda.h>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <cudaTypedefs.h>
 
@@ -38,7 +45,13 @@
 #define NSTAGE 3
 #define BOX_BYTES (BT * BK * 2)
 #define STAGE_BYTES (4 * BOX_BYTES)
-#define GRAM_THREADS 192
+#ifndef EPI_COLS
+#define EPI_COLS 32 /* tile columns per epilogue thread */
+#endif
+#ifndef GP_FOLD
+#define GP_FOLD 8   /* chunks summed in FP32 registers before the TwoSum fold */
+#endif
+#define GRAM_THREADS (64 + 32 * 4 * (128 / EPI_COLS)) /* producer + MMA + epilogue warps */
 #define GRAM_SMEM (NSTAGE * STAGE_BYTES + 1024 + 256)
 
 /* error codes recorded by the kernel */
@@ -61,8 +74,9 @@ __device__ __forceinline__ void tri_tile(int32_t t, int32_t *bi, int32_t *bj)
  * (super-chunks after the first).  nkb = k-blocks of this super-chunk; chunk_kb = k-blocks
  * per FP32 accumulation chunk.
  */
+template <int FP16, int NMMA>
 __global__ void __launch_bounds__(GRAM_THREADS, 1)
-k_gram_split_bf16(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ CUtensorMap tm_lo,
+k_gram_split(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ CUtensorMap tm_lo,
                   int32_t ntiles, int32_t nkb, int32_t chunk_kb, double *xtx, int32_t n,
                   int32_t accumulate, int *err)
 {
@@ -85,7 +99,7 @@ k_gram_split_bf16(const __grid_constant__ CUtensorMap tm_hi, const __grid_consta
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&accf[b], 1);
-      mbar_init(&acce[b], 4);
+      mbar_init(&acce[b], 4 * (128 / EPI_COLS));
     }
     mbar_init(drain, 1);
     *abort_flag = 0;
@@ -134,7 +148,7 @@ k_gram_split_bf16(const __grid_constant__ CUtensorMap tm_hi, const __grid_consta
   } else if (warp == 1) {
     /* ---------------- MMA issuer ---------------- */
     if (lane == 0) {
-      const uint32_t idesc = idesc_bf16_f32(BT, BT);
+      const uint32_t idesc = FP16 ? idesc_f16_f32(BT, BT) : idesc_bf16_f32(BT, BT);
       uint32_t it = 0, chunk = 0;
       bool ok = true;
       for (int32_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
@@ -165,6 +179,7 @@ k_gram_split_bf16(const __grid_constant__ CUtensorMap tm_hi, const __grid_consta
               umma_bf16(d, ahi + o, bhi + o, idesc, acc0);
               umma_bf16(d, ahi + o, blo + o, idesc, 1u);
               umma_bf16(d, alo + o, bhi + o, idesc, 1u);
+              if (NMMA == 4) umma_bf16(d, alo + o, blo + o, idesc, 1u);
             }
             umma_commit(&empty[s]);
           }
@@ -174,31 +189,40 @@ k_gram_split_bf16(const __grid_constant__ CUtensorMap tm_hi, const __grid_consta
       }
     }
   } else {
-    /* ---------------- epilogue (warps 2..5) ---------------- */
-    const int q = warp & 3;               /* TMEM lane quarter this warp may access */
-    const int row = q * 32 + lane;         /* row of the tile */
+    /* ---------------- epilogue (warps 2..17) ----------------
+     * Warp w reads TMEM lanes 32*(w%4)..+31 (its row quarter); the four warps of a quarter
+     * take EPI_COLS columns each.  Three levels of accumulation:
+     *   tensor core  FP32 over one chunk (chunk_kb k-blocks) in TMEM buffer (chunk & 1);
+     *   registers    FP32 (round-to-nearest) sum of GP_FOLD chunks, A[];
+     *   TMEM         running sum as an FP32 (hi, lo) pair updated with TwoSum (~48 bits),
+     *                columns 256+col (hi) and 384+col (lo), written out in FP64 per tile.
+     * No FP64 arithmetic on the per-chunk path (GB300's FP64 rate is low). */
+    const int q = warp & 3;
+    const int row = q * 32 + lane;
+    const int col0 = ((warp - 2) >> 2) * EPI_COLS;
     const uint32_t lane_addr = (uint32_t)(q * 32) << 16;
+    const uint32_t t_acc = tmem + lane_addr;
     uint32_t chunk = 0;
     bool ok = true;
     for (int32_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
       int32_t bi, bj;
       tri_tile(t, &bi, &bj);
       const int32_t gi = bi * BT + row;
-      /* FP64 running sum in TMEM columns 256..511: start from 0 or from the Gram so far */
-      for (int j0 = 0; j0 < BT; j0 += 8) {
-        uint32_t w[16];
+      const int32_t gj0 = bj * BT + col0;
+      float A[EPI_COLS];
+      {
+        uint32_t z[16];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          double v = 0.0;
-          int32_t gj = bj * BT + j0 + u;
-          if (accumulate && gi < n && gj < n) v = xtx[(int64_t)gi * n + gj];
-          uint64_t b = (uint64_t)__double_as_longlong(v);
-          w[2 * u] = (uint32_t)b;
-          w[2 * u + 1] = (uint32_t)(b >> 32);
+        for (int v = 0; v < 16; ++v) z[v] = 0u;
+#pragma unroll
+        for (int g = 0; g < EPI_COLS / 16; ++g) {
+          tmem_st16(t_acc + 256 + col0 + 16 * g, z);
+          tmem_st16(t_acc + 384 + col0 + 16 * g, z);
         }
-        tmem_st16(tmem + lane_addr + 256 + 2 * j0, w);
+        tmem_wait_st();
       }
-      tmem_wait_st();
+#pragma unroll
+      for (int u = 0; u < EPI_COLS; ++u) A[u] = 0.f;
       for (int32_t c = 0; c < nchunk; ++c, ++chunk) {
         uint32_t buf = chunk & 1u, use = chunk >> 1;
         bool got = mbar_wait(&accf[buf], use & 1u, abort_flag, err, GP_KERR_TIMEOUT_ACCF);
@@ -207,44 +231,56 @@ k_gram_split_bf16(const __grid_constant__ CUtensorMap tm_hi, const __grid_consta
           break;
         }
         tc_fence_after();
-        for (int j0 = 0; j0 < BT; j0 += 16) {
-          uint32_t f[16], w0[16], w1[16];
-          tmem_ld16(tmem + lane_addr + buf * BT + j0, f);
-          tmem_ld16(tmem + lane_addr + 256 + 2 * j0, w0);
-          tmem_ld16(tmem + lane_addr + 256 + 2 * j0 + 16, w1);
+#pragma unroll
+        for (int g = 0; g < EPI_COLS / 16; ++g) {
+          uint32_t f[16];
+          tmem_ld16(t_acc + buf * BT + col0 + 16 * g, f);
           tmem_wait_ld();
 #pragma unroll
-          for (int u = 0; u < 16; ++u) {
-            uint32_t *w = u < 8 ? w0 : w1;
-            int v = u & 7;
-            uint64_t b = ((uint64_t)w[2 * v + 1] << 32) | w[2 * v];
-            double sum = __longlong_as_double((long long)b) + (double)__uint_as_float(f[u]);
-            b = (uint64_t)__double_as_longlong(sum);
-            w[2 * v] = (uint32_t)b;
-            w[2 * v + 1] = (uint32_t)(b >> 32);
-          }
-          tmem_st16(tmem + lane_addr + 256 + 2 * j0, w0);
-          tmem_st16(tmem + lane_addr + 256 + 2 * j0 + 16, w1);
+          for (int v = 0; v < 16; ++v) A[16 * g + v] = __fadd_rn(A[16 * g + v], __uint_as_float(f[v]));
         }
-        tmem_wait_st();
         tc_fence_before();
         __syncwarp();
-        if (lane == 0) mbar_arrive(&acce[buf]);
+        if (lane == 0) mbar_arrive(&acce[buf]); /* buffer free: the MMA may reuse it */
+        if ((c + 1) % GP_FOLD == 0 || c + 1 == nchunk) {
+          /* fold A into the (hi, lo) running sum with TwoSum */
+#pragma unroll
+          for (int g = 0; g < EPI_COLS / 16; ++g) {
+            uint32_t hs[16], ls[16];
+            tmem_ld16(t_acc + 256 + col0 + 16 * g, hs);
+            tmem_ld16(t_acc + 384 + col0 + 16 * g, ls);
+            tmem_wait_ld();
+#pragma unroll
+            for (int v = 0; v < 16; ++v) {
+              float Sv = __uint_as_float(hs[v]), x = A[16 * g + v];
+              float s1 = __fadd_rn(Sv, x);
+              float bp = __fsub_rn(s1, Sv);
+              float e = __fadd_rn(__fsub_rn(Sv, __fsub_rn(s1, bp)), __fsub_rn(x, bp));
+              hs[v] = __float_as_uint(s1);
+              ls[v] = __float_as_uint(__fadd_rn(__uint_as_float(ls[v]), e));
+              A[16 * g + v] = 0.f;
+            }
+            tmem_st16(t_acc + 256 + col0 + 16 * g, hs);
+            tmem_st16(t_acc + 384 + col0 + 16 * g, ls);
+          }
+          tmem_wait_st();
+        }
       }
       if (!ok) break;
-      /* the FP64 tile -> Gram rows (every lane loads; rows past n store nothing) */
+      /* the tile -> Gram rows in FP64 (super-chunks after the first add to what is there) */
       double *orow = xtx + (int64_t)gi * n;
-      for (int j0 = 0; j0 < BT; j0 += 8) {
-        uint32_t w[16];
-        tmem_ld16(tmem + lane_addr + 256 + 2 * j0, w);
+#pragma unroll
+      for (int g = 0; g < EPI_COLS / 16; ++g) {
+        uint32_t hs[16], ls[16];
+        tmem_ld16(t_acc + 256 + col0 + 16 * g, hs);
+        tmem_ld16(t_acc + 384 + col0 + 16 * g, ls);
         tmem_wait_ld();
         if (gi < n) {
-#pragma unroll
-          for (int u = 0; u < 8; ++u) {
-            int32_t gj = bj * BT + j0 + u;
+          for (int v = 0; v < 16; ++v) {
+            int32_t gj = gj0 + 16 * g + v;
             if (gj < n) {
-              uint64_t b = ((uint64_t)w[2 * u + 1] << 32) | w[2 * u];
-              orow[gj] = __longlong_as_double((long long)b);
+              double x = (double)__uint_as_float(hs[v]) + (double)__uint_as_float(ls[v]);
+              orow[gj] = accumulate ? orow[gj] + x : x;
             }
           }
         }
@@ -270,7 +306,9 @@ k_gram_split_bf16(const __grid_constant__ CUtensorMap tm_hi, const __grid_consta
 /* ------------------------------------------------------------------------------------ */
 /* split materialisation                                                                  */
 
-/* per kept column: (hi, lo) bf16 pairs for codes 0..3 packed as 4 x uint32 (lo<<16 | hi) */
+/* per kept column: (hi, lo) 16-bit pairs (bf16 or fp16) for codes 0..3 packed as
+ * 4 x uint32 (lo << 16 | hi); hi = round(v), lo = round(v - hi) */
+template <int FP16>
 __global__ void k_split_tables(const int32_t *kept, int32_t nkept, const double *vtab,
                                uint32_t *split)
 {
@@ -278,10 +316,18 @@ __global__ void k_split_tables(const int32_t *kept, int32_t nkept, const double 
     int32_t c = kept[k];
     for (int g = 0; g < 4; ++g) {
       double v = vtab[4 * c + g];
-      __nv_bfloat16 hi = __double2bfloat16(v);
-      double r = v - (double)__bfloat162float(hi);
-      __nv_bfloat16 lo = __double2bfloat16(r);
-      uint32_t h = (uint32_t)__bfloat16_as_ushort(hi), l = (uint32_t)__bfloat16_as_ushort(lo);
+      uint32_t h, l;
+      if (FP16) {
+        __half hi = __double2half(v);
+        __half lo = __double2half(v - (double)__half2float(hi));
+        h = (uint32_t)__half_as_ushort(hi);
+        l = (uint32_t)__half_as_ushort(lo);
+      } else {
+        __nv_bfloat16 hi = __double2bfloat16(v);
+        __nv_bfloat16 lo = __double2bfloat16(v - (double)__bfloat162float(hi));
+        h = (uint32_t)__bfloat16_as_ushort(hi);
+        l = (uint32_t)__bfloat16_as_ushort(lo);
+      }
       split[4 * k + g] = h | (l << 16);
     }
   }
@@ -344,7 +390,8 @@ static PFN_cuTensorMapEncodeTiled_v12000 get_encode(gp_ctx *ctx)
   return fn;
 }
 
-static int make_map(gp_ctx *ctx, CUtensorMap *m, void *base, int32_t rows, int32_t cols)
+static int make_map(gp_ctx *ctx, CUtensorMap *m, void *base, int32_t rows, int32_t cols,
+                    CUtensorMapDataType dt)
 {
   PFN_cuTensorMapEncodeTiled_v12000 enc = get_encode(ctx);
   if (!enc) return GP_ERR_CUDA;
@@ -352,19 +399,21 @@ static int make_map(gp_ctx *ctx, CUtensorMap *m, void *base, int32_t rows, int32
   cuuint64_t strides[1] = {(cuuint64_t)cols * 2};
   cuuint32_t box[2] = {BK, BT};
   cuuint32_t estr[2] = {1, 1};
-  CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
+  CUresult r = enc(m, dt, 2, base, dims, strides, box, estr,
                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return gp_fail(ctx, GP_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
   return GP_OK;
 }
 
-/* FP32 accumulation depth in SNPs (k-blocks of 64) before the FP64 add; split budget in bytes */
-#define GP_BF16_CHUNK_KB 32
+/* FP32 accumulation depth in k-blocks of 64 SNPs before the (hi, lo) add; split budget in bytes */
+#define GP_BF16_CHUNK_KB 2
 #define GP_BF16_BUDGET (24ll << 30)
 
-int gp_gram_split_bf16(gp_ctx *ctx)
+int gp_gram_split(gp_ctx *ctx, int precision)
 {
+  const int fp16 = precision == GP_PREC_SPLIT_FP16;
+  const int nmma = precision == GP_PREC_SPLIT_BF16X4 ? 4 : 3;
   const int32_t n = ctx->nrows, nk = ctx->nkept;
   const int32_t npad = (n + BT - 1) / BT * BT;
   const int32_t nt = npad / BT, ntiles = nt * (nt + 1) / 2;
@@ -401,18 +450,20 @@ int gp_gram_split_bf16(gp_ctx *ctx)
   {
     int blocks = (nk + 255) / 256;
     if (blocks > ctx->num_sms * 8) blocks = ctx->num_sms * 8;
-    k_split_tables<<<blocks, 256, 0, ctx->stream>>>(ctx->d_kept, nk, ctx->d_vtab, split);
+    if (fp16)
+      k_split_tables<1><<<blocks, 256, 0, ctx->stream>>>(ctx->d_kept, nk, ctx->d_vtab, split);
+    else
+      k_split_tables<0><<<blocks, 256, 0, ctx->stream>>>(ctx->d_kept, nk, ctx->d_vtab, split);
     GP_LAUNCH_CHECK(ctx, "k_split_tables");
   }
-  static int attr_set = 0;
-  if (!attr_set) {
-    GP_CUDA(ctx, cudaFuncSetAttribute(k_gram_split_bf16, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      GRAM_SMEM));
-    attr_set = 1;
-  }
+  void (*kern)(const CUtensorMap, const CUtensorMap, int32_t, int32_t, int32_t, double *, int32_t,
+               int32_t, int *) =
+      fp16 ? k_gram_split<1, 3> : (nmma == 4 ? k_gram_split<0, 4> : k_gram_split<0, 3>);
+  GP_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, GRAM_SMEM));
   CUtensorMap mhi, mlo;
-  rc = make_map(ctx, &mhi, xhi, npad, kc);
-  if (!rc) rc = make_map(ctx, &mlo, xlo, npad, kc);
+  CUtensorMapDataType dt = fp16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+  rc = make_map(ctx, &mhi, xhi, npad, kc, dt);
+  if (!rc) rc = make_map(ctx, &mlo, xlo, npad, kc, dt);
   if (rc) return rc;
   int grid = ctx->num_sms < ntiles ? ctx->num_sms : ntiles;
   for (int32_t k0 = 0; k0 < kpad; k0 += kc) {
@@ -426,9 +477,9 @@ int gp_gram_split_bf16(gp_ctx *ctx)
                                                          npad, xhi, xlo);
     GP_LAUNCH_CHECK(ctx, "k_split_materialize");
     int32_t nkb = kcur / BK;
-    k_gram_split_bf16<<<grid, GRAM_THREADS, GRAM_SMEM, ctx->stream>>>(
+    kern<<<grid, GRAM_THREADS, GRAM_SMEM, ctx->stream>>>(
         mhi, mlo, ntiles, nkb, chunk_kb, ctx->d_xtx, n, k0 > 0 ? 1 : 0, d_err);
-    GP_LAUNCH_CHECK(ctx, "k_gram_split_bf16");
+    GP_LAUNCH_CHECK(ctx, "k_gram_split");
     ctx->gram_launches++;
   }
   int herr = 0;

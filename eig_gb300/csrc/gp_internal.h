@@ -101,7 +101,7 @@ int gp_launch_valid_counts(gp_ctx *ctx, const uint8_t *d_sample_use, const uint8
                            int32_t *d_snp_valid, int32_t *d_sample_valid);
 int gp_launch_snp_stats(gp_ctx *ctx, const gp_xtx_opts *o);
 int gp_gram_fp64(gp_ctx *ctx);
-int gp_gram_split_bf16(gp_ctx *ctx);
+int gp_gram_split(gp_ctx *ctx, int precision);
 int gp_launch_symmetrize_trace(gp_ctx *ctx, double *d_trace);
 int gp_launch_materialize_f64(gp_ctx *ctx, int32_t k0, int32_t kc, int32_t pitch, double *d_x,
                               double scale);

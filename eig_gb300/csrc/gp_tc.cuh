@@ -185,6 +185,13 @@ __host__ __device__ constexpr uint32_t idesc_bf16_f32(uint32_t M, uint32_t N)
   return (1u << 4) | (1u << 7) | (1u << 10) | ((N >> 3) << 17) | ((M >> 4) << 24);
 }
 
+/* instruction descriptor: kind::f16, A = B = F16, D = F32, both K-major, M x N */
+__host__ __device__ constexpr uint32_t idesc_f16_f32(uint32_t M, uint32_t N)
+{
+  return (1u << 4) | ((N >> 3) << 17) | ((M >> 4) << 24);
+}
+
+/* one tcgen05.mma kind::f16 (bf16 or f16 operands, as the instruction descriptor says) */
 __device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc,
                                           uint32_t idesc, uint32_t accumulate)
 {

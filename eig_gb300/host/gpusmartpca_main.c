@@ -9,8 +9,8 @@
  *                    printed sample "%20s " ID, K x "%10.4f  " (hiprecision "%12.6f  ") and
  *                    "%15s\n" population (:1570-1591); fastmode as printevecs (:3837-3871)
  *   outlieroutname   "REMOVED outlier %s iter %d evec %d sigmage %.3f pop: %s\n" (:1255-1257)
- * One extra key selects the Gram precision: gpuprecision: FP64 (default, the drop-in) or
- * SPLIT_BF16.  Keys of the reference's other analyses (Fst, ANOVA, shrinkage, LD regression,
+ * One extra key selects the Gram precision: gpuprecision: FP64 (default, the drop-in),
+ * SPLIT_BF16, SPLIT_BF16X4 or SPLIT_FP16 (include/gpupca.h).  Keys of the reference's other analyses (Fst, ANOVA, shrinkage, LD regression,
  * GRM dump) are accepted and ignored with a note.
  */
 #include <stdio.h>
@@ -109,7 +109,16 @@ int main(int argc, char **argv)
     fprintf(stderr, "ldregress is not supported by this path\n");
     return 1;
   }
-  if (prec && strcmp(prec, "SPLIT_BF16") == 0) o.precision = GP_PREC_SPLIT_BF16;
+  if (prec) {
+    if (strcmp(prec, "FP64") == 0) o.precision = GP_PREC_FP64;
+    else if (strcmp(prec, "SPLIT_BF16") == 0) o.precision = GP_PREC_SPLIT_BF16;
+    else if (strcmp(prec, "SPLIT_BF16X4") == 0) o.precision = GP_PREC_SPLIT_BF16X4;
+    else if (strcmp(prec, "SPLIT_FP16") == 0) o.precision = GP_PREC_SPLIT_FP16;
+    else {
+      fprintf(stderr, "gpuprecision: %s is not FP64, SPLIT_BF16, SPLIT_BF16X4 or SPLIT_FP16\n", prec);
+      return 1;
+    }
+  }
   if (o.fastmode) {
     if (o.fastiter < 0) o.fastiter = o.numeigs;
     if (o.fastdim < 0) o.fastdim = 2 * o.numeigs;

@@ -18,7 +18,8 @@ GP_ERR = {-1: "GP_ERR_ARG", -2: "GP_ERR_CUDA", -3: "GP_ERR_NOMEM", -4: "GP_ERR_S
           -5: "GP_ERR_SOLVER", -6: "GP_ERR_NODATA", -7: "GP_ERR_TIMEOUT", -8: "GP_ERR_FULL",
           -9: "GP_ERR_NOTBUILT"}
 GP_CODE_PACKED, GP_CODE_BED = 0, 1
-GP_PREC_FP64, GP_PREC_SPLIT_BF16 = 0, 1
+GP_PREC_FP64, GP_PREC_SPLIT_BF16, GP_PREC_SPLIT_BF16X4, GP_PREC_SPLIT_FP16 = 0, 1, 2, 3
+PRECISIONS = {"fp64": 0, "bf16": 1, "bf16x4": 2, "fp16": 3}
 PHASES = ["load", "filter", "gram", "eig", "outlier", "weights", "lsqproj", "total"]
 
 # every symbol the headers declare (checked by the CPU test suite)

@@ -42,8 +42,13 @@ extern "C" {
 #define GP_CODE_PACKED 0     /* packedancestrymap 2-bit, MSB first, 3 = missing */
 #define GP_CODE_BED 1        /* PLINK .bed, LSB first, 01 = missing */
 
-#define GP_PREC_FP64 0       /* plain FP64 Gram: the drop-in */
-#define GP_PREC_SPLIT_BF16 1 /* hi+lo BF16 tcgen05 MMAs, FP32 in a SNP tile, FP64 across */
+#define GP_PREC_FP64 0         /* plain FP64 Gram: the drop-in */
+/* Split precisions: each normalised value v = hi + lo in a 16-bit format, tcgen05 MMAs with
+ * FP32 accumulation inside a SNP chunk and FP64 accumulation across chunks. */
+#define GP_PREC_SPLIT_BF16 1   /* bf16 hi+lo, 3 MMAs (hi.hi + hi.lo + lo.hi): the dropped
+                                  lo.lo term biases eigenvalues low by ~2^-18 (~4e-6) */
+#define GP_PREC_SPLIT_BF16X4 2 /* bf16 hi+lo, 4 MMAs (adds lo.lo): no bias, 4/3 the MMAs */
+#define GP_PREC_SPLIT_FP16 3   /* fp16 hi+lo (11-bit halves), 3 MMAs: lo.lo ~2^-22 */
 
 typedef struct gp_ctx gp_ctx;
 

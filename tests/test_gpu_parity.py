@@ -18,6 +18,12 @@ from tests.goldens import CASES, Case, compare_coords, coords_by_id
 pytestmark = pytest.mark.gpu
 
 
+# split precisions: (elementwise tolerance of the Gram relative to its largest entry,
+# relative tolerance of the top-20 eigenvalues)
+SPLIT_TOL = {native.GP_PREC_SPLIT_BF16: (2e-5, 1e-5), native.GP_PREC_SPLIT_BF16X4: (2e-6, 1e-6),
+             native.GP_PREC_SPLIT_FP16: (2e-6, 1e-6)}
+
+
 def synth(nsnp, pops, fst, miss=0.02, seed=5, **kw):
     rec, pop = native.synth_records(nsnp, pops, fst, miss=miss, seed=seed, nthreads=4, **kw)
     return rec, pop
@@ -189,8 +195,9 @@ def _gram_pair(gpu, rec, nind, rows, cols, precision):
     return gpu.xtx(precision=precision)
 
 
+@pytest.mark.parametrize("prec", list(SPLIT_TOL))
 @pytest.mark.parametrize("shape", [(333, 3000), (128, 64), (1000, 5000)])
-def test_split_bf16_gram_vs_oracle(gpu, shape):
+def test_split_gram_vs_oracle(gpu, shape, prec):
     """split-BF16 Gram (tcgen05) against the FP64 oracle Gram: the hi+lo split keeps about
     17 significant bits per value, so elementwise error <= 2e-5 of the largest entry."""
     nind, nsnp = shape
@@ -198,35 +205,37 @@ def test_split_bf16_gram_vs_oracle(gpu, shape):
                      miss=0.02, seed=31)
     rows = np.arange(nind, dtype=np.int32)
     cols = np.arange(nsnp, dtype=np.int32)
-    r = _gram_pair(gpu, rec, nind, rows, cols, native.GP_PREC_SPLIT_BF16)
+    r = _gram_pair(gpu, rec, nind, rows, cols, prec)
     s = O.pass_columns(rec, cols, rows)
     X = O.gram(s)
     scale = np.max(np.abs(X))
     err = np.max(np.abs(r["XTX"] - X)) / scale
-    assert err <= 2e-5, err
+    assert err <= SPLIT_TOL[prec][0], err
     assert np.array_equal(r["killed"], s.killed)
 
 
-def test_split_bf16_multi_tile_chunks_and_superchunks(gpu, monkeypatch):
-    """2600 samples (21 tile rows, 231 tiles: several per CTA), 6000 SNPs in FP32 chunks of
-    1024 and super-chunks of 2048 SNPs (FP64 carried through the Gram between launches),
-    against the FP64 GPU Gram."""
+@pytest.mark.parametrize("prec", list(SPLIT_TOL))
+def test_split_multi_tile_chunks_and_superchunks(gpu, monkeypatch, prec):
+    """2600 samples (21 tile rows, 231 tiles: several per CTA), 6000 SNPs in super-chunks of
+    2048 SNPs (the sum carried through the Gram between launches), against the FP64 GPU
+    Gram."""
     nind, nsnp = 2600, 6000
     rec, pop = synth(nsnp, [900, 900, 800], [0.01, 0.02, 0.04], miss=0.02, seed=32)
     rows = np.arange(nind, dtype=np.int32)
     cols = np.arange(nsnp, dtype=np.int32)
     ref = _gram_pair(gpu, rec, nind, rows, cols, native.GP_PREC_FP64)["XTX"]
-    monkeypatch.setenv("GP_BF16_CHUNK_SNPS", "1024")
     monkeypatch.setenv("GP_BF16_BUDGET_BYTES", str(2688 * 4 * 2048))
-    r = _gram_pair(gpu, rec, nind, rows, cols, native.GP_PREC_SPLIT_BF16)
+    r = _gram_pair(gpu, rec, nind, rows, cols, prec)
+    etol, vtol = SPLIT_TOL[prec]
     err = np.max(np.abs(r["XTX"] - ref)) / np.max(np.abs(ref))
-    assert err <= 2e-5, err
+    assert err <= etol, err
     w1 = np.linalg.eigvalsh(r["XTX"])[::-1][:20]
     w0 = np.linalg.eigvalsh(ref)[::-1][:20]
-    assert np.max(np.abs(w1 - w0) / w0) <= 1e-6
+    assert np.max(np.abs(w1 - w0) / w0) <= vtol
 
 
-def test_split_bf16_subset_rows(gpu):
+@pytest.mark.parametrize("prec", list(SPLIT_TOL))
+def test_split_subset_rows(gpu, prec):
     """row subsets (outlier removal) and killed columns through the split path"""
     rec, pop = synth(4000, [200, 200, 150], [0.01, 0.02, 0.05], miss=0.05, seed=33)
     nind = len(pop)
@@ -236,8 +245,8 @@ def test_split_bf16_subset_rows(gpu):
     gpu.load_genotypes(rec, nind)
     gpu.set_samples(rows)
     gpu.set_snps(cols)
-    r = gpu.xtx(precision=native.GP_PREC_SPLIT_BF16, minallelecnt=20)
+    r = gpu.xtx(precision=prec, minallelecnt=20)
     s = O.pass_columns(rec, cols, rows, minallelecnt=20)
     X = O.gram(s)
     assert (s.killed == 1).sum() > 0
-    assert np.max(np.abs(r["XTX"] - X)) / np.max(np.abs(X)) <= 2e-5
+    assert np.max(np.abs(r["XTX"] - X)) / np.max(np.abs(X)) <= SPLIT_TOL[prec][0]

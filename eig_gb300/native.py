@@ -29,7 +29,8 @@ EXPORTED = ["gp_version", "gp_last_error", "gp_open", "gp_close", "gp_device_byt
             "gp_lsqproj", "gp_fastpca", "gp_smartpca_defaults", "gp_smartpca_run",
             "gp_fail_msg", "gp_genotype_shape", "gp_timer_start", "gp_timer_stop",
             "gp_last_gram_time", "gp_host_register", "gp_host_unregister",
-            "gp_transfer_bytes", "gp_launch_count"]
+            "gp_transfer_bytes", "gp_launch_count", "gp_gram_fp64_noalloc",
+            "gp_noalloc_last_error"]
 
 i32p = C.POINTER(C.c_int32)
 i64p = C.POINTER(C.c_int64)
@@ -112,6 +113,8 @@ def load_library():
         "gp_host_unregister": (C.c_int, [vp]),
         "gp_transfer_bytes": (C.c_int, [vp, i64p, i64p, C.c_int32]),
         "gp_launch_count": (C.c_int, [vp, i64p, C.c_int32]),
+        "gp_gram_fp64_noalloc": (C.c_int, [vp, C.c_int64, C.c_int32, C.c_int32, vp, vp, vp]),
+        "gp_noalloc_last_error": (C.c_char_p, []),
         "gp_smartpca_run": (C.c_int, [vp, C.POINTER(SmartpcaOpts), C.POINTER(Panel),
                                       C.POINTER(RunResult)]),
     }

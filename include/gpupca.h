@@ -202,6 +202,27 @@ int gp_launch_count(gp_ctx *ctx, int64_t *launches, int32_t reset);
 int gp_host_register(void *ptr, size_t bytes);
 int gp_host_unregister(void *ptr);
 
+/* ---- no-allocation entry point (no counterpart in the reference) ----------------------- */
+
+/*
+ * FP64 Gram XTX = sum over SNPs s of v_s v_s^T for a small panel, computed without any
+ * device allocation, for callers that cannot allocate: e.g. a process whose memory manager
+ * has reserved the whole device for its own pool, or a latency-critical loop that must not
+ * call cudaMalloc/cudaFree (they can synchronise the device).  All buffers are the caller's
+ * DEVICE memory: d_records = nsnp packed records of record_bytes bytes (2-bit
+ * packedancestrymap code, every sample and SNP used), d_vtab = [4*nsnp] value of codes
+ * 0,1,2,3 per SNP (as gp_xtx builds them; 3 = missing, normally 0), d_xtx = [nind*nind]
+ * output, full symmetric.  Work is queued on `stream` (a cudaStream_t; NULL = default).
+ * Limit: nind <= 1024 (larger panels return GP_ERR_ARG; use gp_xtx).  Scratch for the
+ * split-K partial sums is a fixed 16 MiB array inside the library that every GPU loading it
+ * holds until exit; the first call on a device looks its address up (make it before any
+ * stream capture); calls that overlap on the GPU race on that array.  gp_noalloc_last_error
+ * gives the text of the last failure.
+ */
+int gp_gram_fp64_noalloc(const uint8_t *d_records, int64_t record_bytes, int32_t nind,
+                         int32_t nsnp, const double *d_vtab, double *d_xtx, void *stream);
+const char *gp_noalloc_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "gp_geno_gemm.h"
+#include "gp_geno_tc.h"
 #include "gp_internal.h"
 
 #define GP_VERSION 10000
@@ -79,6 +80,13 @@ int gp_scratch(gp_ctx *ctx, size_t bytes, void **out)
   return rc;
 }
 
+int gp_scratch_aux(gp_ctx *ctx, size_t bytes, void **out)
+{
+  int rc = grow(ctx, &ctx->d_scratch3, &ctx->scratch3_cap, bytes);
+  *out = ctx->d_scratch3;
+  return rc;
+}
+
 int gp_scratch2(gp_ctx *ctx, size_t bytes, void **out)
 {
   int rc = grow(ctx, &ctx->d_scratch2, &ctx->scratch2_cap, bytes);
@@ -120,6 +128,7 @@ extern "C" int gp_open(int device, gp_ctx **out)
     free(ctx);
     return GP_ERR_CUDA;
   }
+  if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->d_err, 256);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_t0);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_t1);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_g0);
@@ -147,7 +156,7 @@ extern "C" void gp_close(gp_ctx *ctx)
   void *bufs[] = {ctx->d_geno,   ctx->d_rows,    ctx->d_rowmask, ctx->d_cols,    ctx->d_cnt,
                   ctx->d_killed, ctx->d_vtab,    ctx->d_xmean,   ctx->d_xfancy,  ctx->d_kept,
                   ctx->d_xtx,    ctx->d_evals,   ctx->d_evecs,   ctx->d_ffvecs,  ctx->d_fxscal,
-                  ctx->d_scratch, ctx->d_scratch2};
+                  ctx->d_scratch, ctx->d_scratch2, ctx->d_scratch3, ctx->d_err};
   for (size_t i = 0; i < sizeof(bufs) / sizeof(bufs[0]); ++i)
     if (bufs[i]) cudaFree(bufs[i]);
   if (ctx->solver) cusolverDnDestroy(ctx->solver);
@@ -163,7 +172,8 @@ extern "C" int gp_device_bytes(const gp_ctx *ctx, int64_t *bytes)
 {
   if (!ctx || !bytes) return GP_ERR_ARG;
   int64_t b = (int64_t)ctx->rlen_dev * ctx->nsnp_all + (int64_t)ctx->scratch_cap +
-              (int64_t)ctx->scratch2_cap + (int64_t)sizeof(double) * ctx->xtx_cap;
+              (int64_t)ctx->scratch2_cap + (int64_t)ctx->scratch3_cap +
+              (int64_t)sizeof(double) * ctx->xtx_cap;
   *bytes = b;
   return GP_OK;
 }
@@ -198,6 +208,7 @@ extern "C" int gp_xtx(gp_ctx *ctx, const gp_xtx_opts *opts, int32_t *n0, int32_t
     ctx->xtx_cap = need;
   }
   ctx->xtx_valid = ctx->eig_valid = ctx->weights_valid = 0;
+  ctx->precision = opts->precision;
   int rc = gp_launch_snp_stats(ctx, opts);
   if (rc) return rc;
 
@@ -441,6 +452,31 @@ __global__ void k_kept_tables(const int32_t *kept, int32_t nkept, const int32_t 
   }
 }
 
+/* ffvT[k][j] = fancy_c Yg[k][j] - xmean_c Yo[k][j], c = kept[k]  (X = G fancy - O xmean) */
+__global__ void k_combine_gx(double *ffvT, const double *yg, const double *yo, const int32_t *kept,
+                             const double *xfancy, const double *xmean, int32_t nk, int32_t K)
+{
+  int64_t total = (int64_t)nk * K;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int32_t c = kept[idx / K];
+    ffvT[idx] = xfancy[c] * yg[idx] - xmean[c] * yo[idx];
+  }
+}
+
+/* a[k][j] = fancy_c w[k][j], b[k][j] = xmean_c w[k][j], c = kept[k] */
+__global__ void k_scale_rows2(double *a, double *b, const double *w, const int32_t *kept,
+                              const double *xfancy, const double *xmean, int32_t nk, int32_t K)
+{
+  int64_t total = (int64_t)nk * K;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int32_t c = kept[idx / K];
+    a[idx] = xfancy[c] * w[idx];
+    b[idx] = xmean[c] * w[idx];
+  }
+}
+
 /* ffvecs[j*ncols + kept[k]] = ffvT[k*K + j] (killed columns stay 0) */
 __global__ void k_scatter_ffvecs(double *ffvecs, const double *ffvT, const int32_t *kept,
                                  int32_t nkept, int32_t ncols, int32_t K)
@@ -510,9 +546,29 @@ extern "C" int gp_snp_weights(gp_ctx *ctx, int32_t numeigs, double *ffvecs, doub
   if (blocks > ctx->num_sms * 16) blocks = ctx->num_sms * 16;
   k_fvecs_T<<<blocks, 256, 0, ctx->stream>>>(d_B, ctx->d_evecs, n, K);
   GP_LAUNCH_CHECK(ctx, "k_fvecs_T");
-  /* ffvecs^T[k][j] = sum_r v(r,k) * 10 evec_j[r] */
-  rc = gp_geno_gemm_f64(ctx, 0, ctx->d_rows, n, kt.snprec, kt.vt, nk, d_B, K, K, d_ffvT, K);
-  if (rc) return rc;
+  if (ctx->precision != GP_PREC_FP64 && nk > 0) {
+    /* tensor-core exact products: X = G fancy - O xmean, so
+     * ffvecs^T = fancy (G^T W) - xmean (O^T W) with W = 10 evecs^T over the rows */
+    double *tmp;
+    rc = gp_scratch_aux(ctx, sizeof(double) * 2 * (size_t)nk * K, (void **)&tmp);
+    if (rc) return rc;
+    double *d_yg = tmp, *d_yo = tmp + (size_t)nk * K;
+    gp_tc_panel pw = {d_B, K, 1.0, 1};
+    rc = gp_geno_panel_tc(ctx, 0, ctx->d_rows, n, kt.snprec, nk, 1, &pw, K, d_yg, K);
+    if (rc) return rc;
+    pw.count = 0;
+    rc = gp_geno_panel_tc(ctx, 0, ctx->d_rows, n, kt.snprec, nk, 1, &pw, K, d_yo, K);
+    if (rc) return rc;
+    int b3 = (int)(((int64_t)nk * K + 255) / 256);
+    if (b3 > ctx->num_sms * 16) b3 = ctx->num_sms * 16;
+    k_combine_gx<<<b3, 256, 0, ctx->stream>>>(d_ffvT, d_yg, d_yo, ctx->d_kept, ctx->d_xfancy,
+                                             ctx->d_xmean, nk, K);
+    GP_LAUNCH_CHECK(ctx, "k_combine_gx");
+  } else {
+    /* ffvecs^T[k][j] = sum_r v(r,k) * 10 evec_j[r] */
+    rc = gp_geno_gemm_f64(ctx, 0, ctx->d_rows, n, kt.snprec, kt.vt, nk, d_B, K, K, d_ffvT, K);
+    if (rc) return rc;
+  }
   GP_CUDA(ctx, cudaMemsetAsync(ctx->d_ffvecs, 0, sizeof(double) * (size_t)K * nc, ctx->stream));
   if (nk) {
     int b2 = (int)(((int64_t)nk * K + 255) / 256);
@@ -520,9 +576,23 @@ extern "C" int gp_snp_weights(gp_ctx *ctx, int32_t numeigs, double *ffvecs, doub
     k_scatter_ffvecs<<<b2, 256, 0, ctx->stream>>>(ctx->d_ffvecs, d_ffvT, ctx->d_kept, nk, nc, K);
     GP_LAUNCH_CHECK(ctx, "k_scatter_ffvecs");
   }
-  /* fxvecs^T[i][j] = xrow_i . ffvecs_j  (fixxrow values) */
-  rc = gp_geno_gemm_f64(ctx, 1, ctx->d_rows, n, kt.snprec, kt.rt, nk, d_ffvT, K, K, d_fxT, K);
-  if (rc) return rc;
+  /* fxvecs^T[i][j] = xrow_i . ffvecs_j  (fixxrow values g fancy - xmean) */
+  if (ctx->precision != GP_PREC_FP64 && nk > 0) {
+    double *tmp;
+    rc = gp_scratch_aux(ctx, sizeof(double) * 2 * (size_t)nk * K, (void **)&tmp);
+    if (rc) return rc;
+    int b3 = (int)(((int64_t)nk * K + 255) / 256);
+    if (b3 > ctx->num_sms * 16) b3 = ctx->num_sms * 16;
+    k_scale_rows2<<<b3, 256, 0, ctx->stream>>>(tmp, tmp + (size_t)nk * K, d_ffvT, ctx->d_kept,
+                                              ctx->d_xfancy, ctx->d_xmean, nk, K);
+    GP_LAUNCH_CHECK(ctx, "k_scale_rows2");
+    gp_tc_panel pr[2] = {{tmp, K, 1.0, 1}, {tmp + (size_t)nk * K, K, -1.0, 0}};
+    rc = gp_geno_panel_tc(ctx, 1, ctx->d_rows, n, kt.snprec, nk, 2, pr, K, d_fxT, K);
+    if (rc) return rc;
+  } else {
+    rc = gp_geno_gemm_f64(ctx, 1, ctx->d_rows, n, kt.snprec, kt.rt, nk, d_ffvT, K, K, d_fxT, K);
+    if (rc) return rc;
+  }
   std::vector<double> fx((size_t)n * K);
   GP_CUDA(ctx, gp_memcpy(ctx, fx.data(), d_fxT, sizeof(double) * fx.size(),
                                cudaMemcpyDeviceToHost, ctx->stream));
@@ -679,10 +749,27 @@ extern "C" int gp_lsqproj(gp_ctx *ctx, int32_t numeigs, const int32_t *samples, 
     GP_LAUNCH_CHECK(ctx, "k_build_EP");
   }
   /* masked normal equations: co = O P (pair sums + observed count), rr = R E */
-  rc = gp_geno_gemm_f64(ctx, 1, d_samp, nproj, kt.snprec, kt.ot, nk, d_P, ldp, ldp, d_co, ldp);
-  if (rc) return rc;
-  rc = gp_geno_gemm_f64(ctx, 1, d_samp, nproj, kt.snprec, kt.rt, nk, d_E, K, K, d_rr, K);
-  if (rc) return rc;
+  if (ctx->precision != GP_PREC_FP64 && nk > 0) {
+    gp_tc_panel pc = {d_P, ldp, 1.0, 0};
+    rc = gp_geno_panel_tc(ctx, 1, d_samp, nproj, kt.snprec, nk, 1, &pc, ldp, d_co, ldp);
+    if (rc) return rc;
+    double *tmp;
+    rc = gp_scratch_aux(ctx, sizeof(double) * 2 * (size_t)nk * K, (void **)&tmp);
+    if (rc) return rc;
+    int b3 = (int)(((int64_t)nk * K + 255) / 256);
+    if (b3 > ctx->num_sms * 16) b3 = ctx->num_sms * 16;
+    k_scale_rows2<<<b3, 256, 0, ctx->stream>>>(tmp, tmp + (size_t)nk * K, d_E, ctx->d_kept,
+                                              ctx->d_xfancy, ctx->d_xmean, nk, K);
+    GP_LAUNCH_CHECK(ctx, "k_scale_rows2");
+    gp_tc_panel pr[2] = {{tmp, K, 1.0, 1}, {tmp + (size_t)nk * K, K, -1.0, 0}};
+    rc = gp_geno_panel_tc(ctx, 1, d_samp, nproj, kt.snprec, nk, 2, pr, K, d_rr, K);
+    if (rc) return rc;
+  } else {
+    rc = gp_geno_gemm_f64(ctx, 1, d_samp, nproj, kt.snprec, kt.ot, nk, d_P, ldp, ldp, d_co, ldp);
+    if (rc) return rc;
+    rc = gp_geno_gemm_f64(ctx, 1, d_samp, nproj, kt.snprec, kt.rt, nk, d_E, K, K, d_rr, K);
+    if (rc) return rc;
+  }
   GP_CUDA(ctx, cudaMemsetAsync(d_a, 0, sizeof(double) * nrr, ctx->stream));
   int blocks = (nproj + 127) / 128;
   k_lsq_solve<<<blocks, 128, 0, ctx->stream>>>(d_co, ldp, d_rr, K, nproj, d_a, d_b, d_nobs, d_st,

@@ -1,0 +1,562 @@
+/*
+ * Exact genotype x FP64-panel products on the tensor cores.
+ *
+ *   Y[r][c] = sum_k A_r(k) P[k][c]
+ *
+ * A_r(k) is a small integer decoded from a 2-bit genotype code through a 4-entry table
+ * (observed mask {1,1,1,0} or allele count {0,1,2,0}); P is an FP64 panel.  Each column of
+ * P is scaled by a power of two 2^e_c >= max|P[.][c]| and cut into 4 fixed-point slices,
+ * x = P/2^e_c = sum_t q_t 1024^-(t+1) with |q_0| <= 1024 and |q_t| <= 512 (t > 0): integers
+ * that fp16 holds exactly.  A tensor-core MMA of {0,1,2} by such integers over at most 8,192
+ * k values sums to an integer below 2^24, which FP32 holds exactly, so the FP32 accumulation
+ * of the MMA loses nothing; chunk sums are added in int32 registers and flushed with FP64
+ * atomics of exact integers (order-independent, hence deterministic).  The only error left
+ * is the slicing, about 2^-41 of the column maximum.
+ *
+ * This is how the masked per-sample normal equations of lsqproject (regressit
+ * src/regsubs.c:19-26, lsqproj src/eigensrc/smartpca.c:4690-4712), the sample scores fxvecs
+ * and the SNP weights ffvecs (smartpca.c:1485-1525) reach FP64 accuracy at tensor-core
+ * speed.  Both orientations use the same kernel; only the operand layout differs:
+ *   sum over SNPs     rows = samples, k = kept SNPs (codes in sample-major order)
+ *   sum over samples  rows = kept SNPs, k = samples (codes in SNP-major order)
+ *
+ * Kernel structure (grid-stride over work items = row tile x column tile x k-split):
+ *   warp 0      TMA of the B tile (128 slice-columns x 64 k, fp16, 128-byte swizzle);
+ *   warp 1      one thread issues 4 tcgen05.mma (128x128x16, f16 -> f32) per k-block into
+ *               TMEM buffer (chunk & 1);
+ *   warps 2-5   decode the A tile: one thread per row reads 16 bytes of codes (64 k) and
+ *               writes 64 fp16 values into shared memory in the same swizzled layout, then
+ *               fence.proxy.async + mbarrier arrive;
+ *   warps 6-13  epilogue: per chunk tcgen05.ld the exact FP32 sums, add into int32
+ *               registers (64 columns per thread), flush with FP64 atomics per work item.
+ */
+#include <cuda.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+#include <math.h>
+
+#include "gp_geno_tc.h"
+#include "gp_tc.cuh"
+
+#define XT 128              /* rows / slice-columns per tile */
+#define XK 64               /* k per k-block */
+#define XSTAGES 4
+#define XA_BYTES (XT * XK * 2)
+#define XB_BYTES (XT * XK * 2)
+#define XSTAGE_BYTES (XA_BYTES + XB_BYTES)
+#define X_THREADS 448       /* 14 warps */
+#define X_SMEM (XSTAGES * XSTAGE_BYTES + 1024 + 256)
+#define X_CHUNK_KB 128      /* 8,192 k per exact FP32 chunk */
+
+#define XERR_FULL 11
+#define XERR_EMPTY 12
+#define XERR_ACCF 13
+#define XERR_ACCE 14
+
+/* fp16 bit patterns of the 4-entry decode tables */
+#define H0 0x0000ull
+#define H1 0x3C00ull
+#define H2 0x4000ull
+static const uint64_t LUT_MASK = H1 | (H1 << 16) | (H1 << 32);      /* {1,1,1,0} */
+static const uint64_t LUT_COUNT = H0 | (H1 << 16) | (H2 << 32);     /* {0,1,2,0} */
+
+__device__ __forceinline__ void fence_proxy_async_smem()
+{
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+/*
+ * codes: [nrows_pad][ldc] bytes (2-bit codes, MSB first, 3 = missing -> 0); k-block kb of row
+ * r is the 16 bytes at codes + r*ldc + (kb % kb_period)*16, decoded with lut_lo for
+ * kb < kb_switch and lut_hi otherwise (the concatenated-k form [G | O]).
+ * zout: [nrows][ldz] FP64, receives atomically the exact integer sums per slice-column.
+ */
+__global__ void __launch_bounds__(X_THREADS, 1)
+k_geno_panel_tc(const __grid_constant__ CUtensorMap tm_b, const uint8_t *__restrict__ codes,
+                int64_t ldc, int32_t nrows, int32_t ncols4, int32_t nkb, int32_t kb_period,
+                int32_t kb_switch, uint64_t lut_lo, uint64_t lut_hi, int32_t ksplit,
+                double *zout, int64_t ldz, int *err)
+{
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t *bars = (uint64_t *)(smem + XSTAGES * XSTAGE_BYTES);
+  uint64_t *full = bars, *empty = bars + XSTAGES, *accf = bars + 2 * XSTAGES,
+           *acce = bars + 2 * XSTAGES + 2, *drain = bars + 2 * XSTAGES + 4;
+  uint32_t *tmem_slot = (uint32_t *)(bars + 2 * XSTAGES + 5);
+  volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  const int32_t nrt = (nrows + XT - 1) / XT, nct = (ncols4 + XT - 1) / XT;
+  const int32_t nitems = nrt * nct * ksplit;
+  const int32_t kb_per = (nkb + ksplit - 1) / ksplit;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < XSTAGES; ++s) {
+      mbar_init(&full[s], 1 + XT);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&accf[b], 1);
+      mbar_init(&acce[b], 8);
+    }
+    mbar_init(drain, 1);
+    *abort_flag = 0;
+    fence_mbar_init();
+  }
+  if (warp == 0 && lane == 0) tma_prefetch_desc(&tm_b);
+  if (warp == 1) tmem_alloc(tmem_slot, 256);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    /* ---------------- B producer (TMA) ---------------- */
+    if (lane == 0) {
+      uint32_t it = 0;
+      bool ok = true;
+      for (int32_t w = blockIdx.x; w < nitems && ok; w += gridDim.x) {
+        int32_t ks = w % ksplit, ct = (w / ksplit) % nct;
+        int32_t kb0 = ks * kb_per, kb1 = kb0 + kb_per < nkb ? kb0 + kb_per : nkb;
+        for (int32_t kb = kb0; kb < kb1; ++kb, ++it) {
+          uint32_t s = it % XSTAGES, ph = (it / XSTAGES) & 1u;
+          if (!mbar_wait(&empty[s], ph ^ 1u, abort_flag, err, XERR_EMPTY)) {
+            ok = false;
+            break;
+          }
+          mbar_arrive_expect_tx(&full[s], XB_BYTES);
+          tma_load_2d(smem + s * XSTAGE_BYTES + XA_BYTES, &tm_b, &full[s], kb * XK, ct * XT);
+        }
+      }
+      if (*abort_flag) {
+        uint32_t last = it < XSTAGES ? it : XSTAGES;
+        for (uint32_t j = it - last; j < it; ++j) {
+          uint64_t t0 = globaltimer_ns();
+          while (!mbar_try_wait(&full[j % XSTAGES], (j / XSTAGES) & 1u) &&
+                 globaltimer_ns() - t0 < GP_WAIT_NS) {
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    /* ---------------- MMA issuer ---------------- */
+    if (lane == 0) {
+      const uint32_t idesc = idesc_f16_f32(XT, XT);
+      uint32_t it = 0, chunk = 0;
+      bool ok = true;
+      for (int32_t w = blockIdx.x; w < nitems && ok; w += gridDim.x) {
+        int32_t ks = w % ksplit;
+        int32_t kb0 = ks * kb_per, kb1 = kb0 + kb_per < nkb ? kb0 + kb_per : nkb;
+        for (int32_t c0 = kb0; c0 < kb1 && ok; c0 += X_CHUNK_KB, ++chunk) {
+          int32_t c1 = c0 + X_CHUNK_KB < kb1 ? c0 + X_CHUNK_KB : kb1;
+          uint32_t buf = chunk & 1u, use = chunk >> 1;
+          if (!mbar_wait(&acce[buf], (use & 1u) ^ 1u, abort_flag, err, XERR_ACCE)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t d = tmem + buf * XT;
+          for (int32_t kb = c0; kb < c1; ++kb, ++it) {
+            uint32_t s = it % XSTAGES, ph = (it / XSTAGES) & 1u;
+            if (!mbar_wait(&full[s], ph, abort_flag, err, XERR_FULL)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            uint32_t base = smem_u32(smem + s * XSTAGE_BYTES);
+            uint64_t ad = sdesc_k128(base), bd = sdesc_k128(base + XA_BYTES);
+#pragma unroll
+            for (int k = 0; k < XK / 16; ++k)
+              umma_bf16(d, ad + (uint64_t)(2 * k), bd + (uint64_t)(2 * k), idesc,
+                        (kb > c0 || k > 0) ? 1u : 0u);
+            umma_commit(&empty[s]);
+          }
+          if (!ok) break;
+          umma_commit(&accf[buf]);
+        }
+      }
+    }
+  } else if (warp < 6) {
+    /* ---------------- A decoders: one row of the tile per thread ---------------- */
+    const int r = (warp - 2) * 32 + lane;
+    uint32_t it = 0;
+    bool ok = true;
+    for (int32_t w = blockIdx.x; w < nitems && ok; w += gridDim.x) {
+      int32_t ks = w % ksplit, rt = w / (ksplit * nct);
+      int32_t kb0 = ks * kb_per, kb1 = kb0 + kb_per < nkb ? kb0 + kb_per : nkb;
+      const int32_t grow = rt * XT + r;
+      const uint8_t *crow = codes + (int64_t)grow * ldc;
+      for (int32_t kb = kb0; kb < kb1; ++kb, ++it) {
+        uint32_t s = it % XSTAGES, ph = (it / XSTAGES) & 1u;
+        bool got = mbar_wait(&empty[s], ph ^ 1u, abort_flag, err, XERR_EMPTY);
+        if (!got) {
+          ok = false;
+          break;
+        }
+        const uint64_t lut = kb < kb_switch ? lut_lo : lut_hi;
+        uint4 raw = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
+        if (grow < nrows) raw = __ldg((const uint4 *)(crow + (int64_t)(kb % kb_period) * 16));
+        uint8_t *row_base = smem + s * XSTAGE_BYTES + r * 128;
+        const uint32_t words[4] = {raw.x, raw.y, raw.z, raw.w};
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          /* codes 8j..8j+7: bytes 2j, 2j+1 of the 16 (little-endian words) */
+          uint32_t wv = words[j >> 1] >> ((j & 1) * 16);
+          uint32_t h[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            uint32_t b0 = (wv >> ((u >> 1) * 8)) & 0xFFu; /* byte holding codes 2u, 2u+1 */
+            uint32_t c0 = (b0 >> ((3 - ((2 * u) & 3)) * 2)) & 3u;
+            uint32_t c1 = (b0 >> ((3 - ((2 * u + 1) & 3)) * 2)) & 3u;
+            uint32_t v0 = (uint32_t)(lut >> (16 * c0)) & 0xFFFFu;
+            uint32_t v1 = (uint32_t)(lut >> (16 * c1)) & 0xFFFFu;
+            h[u] = v0 | (v1 << 16);
+          }
+          *(uint4 *)(row_base + ((j ^ (r & 7)) * 16)) = make_uint4(h[0], h[1], h[2], h[3]);
+        }
+        fence_proxy_async_smem();
+        mbar_arrive(&full[s]);
+      }
+    }
+  } else {
+    /* ---------------- epilogue: warps 6..13 ---------------- */
+    const int q = warp & 3, half = (warp - 6) >> 2;
+    const int row = q * 32 + lane;
+    const int col0 = half * 64;
+    const uint32_t t_acc = tmem + ((uint32_t)(q * 32) << 16);
+    uint32_t chunk = 0;
+    bool ok = true;
+    for (int32_t w = blockIdx.x; w < nitems && ok; w += gridDim.x) {
+      int32_t ks = w % ksplit, ct = (w / ksplit) % nct, rt = w / (ksplit * nct);
+      int32_t kb0 = ks * kb_per, kb1 = kb0 + kb_per < nkb ? kb0 + kb_per : nkb;
+      int32_t acc[64];
+#pragma unroll
+      for (int u = 0; u < 64; ++u) acc[u] = 0;
+      for (int32_t c0 = kb0; c0 < kb1; c0 += X_CHUNK_KB, ++chunk) {
+        uint32_t buf = chunk & 1u, use = chunk >> 1;
+        bool got = mbar_wait(&accf[buf], use & 1u, abort_flag, err, XERR_ACCF);
+        if (!__all_sync(0xffffffffu, got)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+#pragma unroll
+        for (int g = 0; g < 4; ++g) {
+          uint32_t f[16];
+          tmem_ld16(t_acc + buf * XT + col0 + 16 * g, f);
+          tmem_wait_ld();
+#pragma unroll
+          for (int v = 0; v < 16; ++v) acc[16 * g + v] += __float2int_rn(__uint_as_float(f[v]));
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&acce[buf]);
+      }
+      if (!ok) break;
+      const int32_t grow = rt * XT + row;
+      if (grow < nrows) {
+        double *zr = zout + (int64_t)grow * ldz;
+#pragma unroll
+        for (int u = 0; u < 64; ++u) {
+          int32_t gc = ct * XT + col0 + u;
+          if (gc < ncols4 && acc[u] != 0) atomicAdd(zr + gc, (double)acc[u]);
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 1) {
+    if (*abort_flag && lane == 0) {
+      umma_commit(drain);
+      uint64_t t0 = globaltimer_ns();
+      while (!mbar_try_wait(drain, 0) && globaltimer_ns() - t0 < GP_WAIT_NS) {
+      }
+    }
+    __syncwarp();
+    tmem_dealloc(tmem, 256);
+  }
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* operand preparation                                                                    */
+
+/*
+ * sum over SNPs: codes[r][k] = code of sample samp[r] at kept SNP k (record snprec[k]);
+ * row stride ldc bytes; pad k (>= nk) and pad rows are 3.  Thread = (row, 16-byte k group).
+ */
+__global__ void k_codes_by_sample(const uint8_t *__restrict__ geno, int64_t rlen,
+                                  const int32_t *__restrict__ samp, int32_t nsamp,
+                                  int32_t nrows_pad, const int32_t *__restrict__ snprec,
+                                  int32_t nk, int64_t ldc, uint8_t *codes)
+{
+  const int64_t groups = ldc / 16;
+  int64_t total = (int64_t)nrows_pad * groups;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int64_t r = idx % nrows_pad, gq = idx / nrows_pad; /* consecutive threads: consecutive rows */
+    uint32_t out[4] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
+    if (r < nsamp) {
+      int32_t sidx = samp[r];
+      int32_t byte = sidx >> 2, sh = (3 - (sidx & 3)) * 2;
+#pragma unroll 4
+      for (int j = 0; j < 64; ++j) {
+        int64_t k = gq * 64 + j;
+        uint32_t c = 3u;
+        if (k < nk) c = (__ldg(geno + (int64_t)snprec[k] * rlen + byte) >> sh) & 3u;
+        /* code j of the group: byte j>>2 (word j>>4), bits (3-(j&3))*2 within the byte */
+        uint32_t wpos = (uint32_t)((j >> 2) & 3) * 8u + (3u - (uint32_t)(j & 3)) * 2u;
+        out[j >> 4] = (out[j >> 4] & ~(3u << wpos)) | (c << wpos);
+      }
+    }
+    *(uint4 *)(codes + r * ldc + gq * 16) = make_uint4(out[0], out[1], out[2], out[3]);
+  }
+}
+
+/*
+ * sum over samples: codes[k][j] = code of sample samp[j] at kept SNP k; one row per kept
+ * SNP, j over the nsamp samples; pad j and pad rows are 3.
+ */
+__global__ void k_codes_by_snp(const uint8_t *__restrict__ geno, int64_t rlen,
+                               const int32_t *__restrict__ samp, int32_t nsamp,
+                               const int32_t *__restrict__ snprec, int32_t nk, int32_t nrows_pad,
+                               int64_t ldc, uint8_t *codes)
+{
+  const int64_t groups = ldc / 16;
+  int64_t total = (int64_t)nrows_pad * groups;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int64_t k = idx / groups, gq = idx % groups; /* consecutive threads: same SNP */
+    uint32_t out[4] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
+    if (k < nk) {
+      const uint8_t *rec = geno + (int64_t)snprec[k] * rlen;
+#pragma unroll 4
+      for (int j = 0; j < 64; ++j) {
+        int64_t q = gq * 64 + j;
+        uint32_t c = 3u;
+        if (q < nsamp) {
+          int32_t sidx = samp[q];
+          c = (__ldg(rec + (sidx >> 2)) >> ((3 - (sidx & 3)) * 2)) & 3u;
+        }
+        uint32_t wpos = (uint32_t)((j >> 2) & 3) * 8u + (3u - (uint32_t)(j & 3)) * 2u;
+        out[j >> 4] = (out[j >> 4] & ~(3u << wpos)) | (c << wpos);
+      }
+    }
+    *(uint4 *)(codes + k * ldc + gq * 16) = make_uint4(out[0], out[1], out[2], out[3]);
+  }
+}
+
+/* per column c of P [nk][ldp] (FP64): exponent e_c with max|P| < 2^e_c (ncols columns) */
+__global__ void k_panel_exponent(const double *P, int64_t ldp, int32_t nk, int32_t ncols,
+                                 int32_t *expo)
+{
+  __shared__ double red[256];
+  for (int32_t c = blockIdx.x; c < ncols; c += gridDim.x) {
+    double m = 0.0;
+    for (int32_t k = threadIdx.x; k < nk; k += blockDim.x) m = fmax(m, fabs(P[(int64_t)k * ldp + c]));
+    red[threadIdx.x] = m;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o; o >>= 1) {
+      if ((int)threadIdx.x < o) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + o]);
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      double mx = red[0];
+      int e = 0;
+      if (mx > 0.0) {
+        frexp(mx, &e); /* mx = f 2^e, f in [0.5, 1) -> mx < 2^e */
+      }
+      expo[c] = e;
+    }
+    __syncthreads();
+  }
+}
+
+/*
+ * B[(4c+t)][k] (fp16, row stride ldb elements) = slice t of P[k][c] / 2^e_c, for k < nk
+ * (pad k and pad rows zero are written by a memset before).  Rows of P beyond koff..: the
+ * panel block [koff, koff+nk) of a concatenated k range goes to columns koff + k of B.
+ */
+__global__ void k_panel_slices(const double *P, int64_t ldp, int32_t nk, int32_t ncols,
+                               const int32_t *expo, double sign, int64_t koff, __half *B,
+                               int64_t ldb)
+{
+  int64_t total = (int64_t)nk * ncols;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int64_t k = idx / ncols;
+    int32_t c = (int32_t)(idx - k * ncols);
+    double x = ldexp(sign * P[k * ldp + c], -expo[c]); /* |x| < 1 (exact scaling) */
+    double r = x * 1024.0;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      double qv = rint(r);
+      r = (r - qv) * 1024.0; /* exact: r - qv is the low part of r */
+      B[(int64_t)(4 * c + t) * ldb + koff + k] = __double2half(qv);
+    }
+  }
+}
+
+/* Y[r][c] = 2^e_c sum_t Z[r][4c+t] 1024^-(t+1) */
+__global__ void k_panel_combine(const double *Z, int64_t ldz, int32_t nrows, int32_t ncols,
+                                const int32_t *expo, double *Y, int64_t ldy)
+{
+  int64_t total = (int64_t)nrows * ncols;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int64_t r = idx / ncols;
+    int32_t c = (int32_t)(idx - r * ncols);
+    const double *z = Z + r * ldz + 4 * c;
+    double s = ((z[0] * 0x1p-10 + z[1] * 0x1p-20) + z[2] * 0x1p-30) + z[3] * 0x1p-40;
+    Y[r * ldy + c] = ldexp(s, expo[c]);
+  }
+}
+
+/* ------------------------------------------------------------------------------------ */
+
+static PFN_cuTensorMapEncodeTiled_v12000 tc_encode(gp_ctx *ctx)
+{
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = NULL;
+  if (fn) return fn;
+  cudaDriverEntryPointQueryResult q;
+  void *p = NULL;
+  cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                                   cudaEnableDefault, &q);
+  if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !p) {
+    gp_fail(ctx, GP_ERR_CUDA, "cuTensorMapEncodeTiled entry point not found");
+    return NULL;
+  }
+  fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+  return fn;
+}
+
+static int grid_cap(const gp_ctx *ctx, int64_t work, int per_block, int mult)
+{
+  int64_t g = (work + per_block - 1) / per_block;
+  int64_t cap = (int64_t)ctx->num_sms * mult;
+  if (g > cap) g = cap;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+static size_t align256(size_t b) { return (b + 255) / 256 * 256; }
+
+int gp_geno_panel_tc(gp_ctx *ctx, int sum_over_snps, const int32_t *d_samp, int32_t nsamp,
+                     const int32_t *d_snprec, int32_t nk, int npanels, const gp_tc_panel *pp,
+                     int32_t ncols, double *d_Y, int64_t ldy)
+{
+  if (npanels < 1 || npanels > 2 || ncols < 1 || ncols > 1024)
+    return gp_fail(ctx, GP_ERR_ARG, "gp_geno_panel_tc: bad panel shape");
+  const int32_t nrows = sum_over_snps ? nsamp : nk;   /* output rows */
+  const int32_t k0 = sum_over_snps ? nk : nsamp;      /* one panel's k extent */
+  if (nrows < 1 || k0 < 1) return GP_OK;
+  const int32_t nrows_pad = (nrows + XT - 1) / XT * XT;
+  const int32_t kb0 = (k0 + XK - 1) / XK;             /* k-blocks per panel */
+  const int32_t kpad0 = kb0 * XK;
+  const int32_t nkb = kb0 * npanels;
+  const int32_t ncols4 = 4 * ncols, ncols4_pad = (ncols4 + XT - 1) / XT * XT;
+  const int64_t ldc = kpad0 / 4;                      /* code bytes per row */
+  const int64_t ldb = (int64_t)kpad0 * npanels;       /* B row stride (elements) */
+  const int64_t ldz = ncols4_pad;
+  size_t b_codes = align256((size_t)nrows_pad * ldc);
+  size_t b_B = align256((size_t)ncols4_pad * ldb * 2);
+  size_t b_Z = align256((size_t)nrows * ldz * 8);
+  size_t b_e = align256((size_t)ncols * npanels * 4 + 4 * (size_t)ncols);
+  uint8_t *base;
+  int rc = gp_scratch2(ctx, b_codes + b_B + b_Z + b_e + 256, (void **)&base);
+  if (rc) return rc;
+  uint8_t *codes = base;
+  __half *B = (__half *)(base + b_codes);
+  double *Z = (double *)(base + b_codes + b_B);
+  int32_t *expo = (int32_t *)(base + b_codes + b_B + b_Z);
+  int32_t *expo_p = expo + ncols; /* per-panel exponents, then the joint one */
+  int *d_err = ctx->d_err;
+  GP_CUDA(ctx, cudaMemsetAsync(d_err, 0, sizeof(int), ctx->stream));
+
+  /* codes */
+  {
+    int64_t work = (int64_t)nrows_pad * (ldc / 16);
+    if (sum_over_snps)
+      k_codes_by_sample<<<grid_cap(ctx, work, 256, 32), 256, 0, ctx->stream>>>(
+          ctx->d_geno, ctx->rlen_dev, d_samp, nsamp, nrows_pad, d_snprec, nk, ldc, codes);
+    else
+      k_codes_by_snp<<<grid_cap(ctx, work, 256, 32), 256, 0, ctx->stream>>>(
+          ctx->d_geno, ctx->rlen_dev, d_samp, nsamp, d_snprec, nk, nrows_pad, ldc, codes);
+    GP_LAUNCH_CHECK(ctx, "k_codes");
+  }
+  /* joint column exponents over the panels, then the slices */
+  for (int p = 0; p < npanels; ++p) {
+    k_panel_exponent<<<ncols < 1024 ? ncols : 1024, 256, 0, ctx->stream>>>(
+        pp[p].P, pp[p].ldp, k0, ncols, expo_p + p * ncols);
+    GP_LAUNCH_CHECK(ctx, "k_panel_exponent");
+  }
+  if (npanels == 1) {
+    GP_CUDA(ctx, cudaMemcpyAsync(expo, expo_p, sizeof(int32_t) * ncols, cudaMemcpyDeviceToDevice,
+                                 ctx->stream));
+  } else {
+    std::vector<int32_t> he((size_t)ncols * npanels);
+    GP_CUDA(ctx, gp_memcpy(ctx, he.data(), expo_p, sizeof(int32_t) * he.size(),
+                           cudaMemcpyDeviceToHost, ctx->stream));
+    GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    std::vector<int32_t> j((size_t)ncols);
+    for (int32_t c = 0; c < ncols; ++c) {
+      int e = he[(size_t)c];
+      for (int p = 1; p < npanels; ++p) e = he[(size_t)p * ncols + c] > e ? he[(size_t)p * ncols + c] : e;
+      j[(size_t)c] = e;
+    }
+    GP_CUDA(ctx, gp_memcpy(ctx, expo, j.data(), sizeof(int32_t) * ncols, cudaMemcpyHostToDevice,
+                           ctx->stream));
+  }
+  GP_CUDA(ctx, cudaMemsetAsync(B, 0, (size_t)ncols4_pad * ldb * 2, ctx->stream));
+  for (int p = 0; p < npanels; ++p) {
+    int64_t work = (int64_t)k0 * ncols;
+    k_panel_slices<<<grid_cap(ctx, work, 256, 32), 256, 0, ctx->stream>>>(
+        pp[p].P, pp[p].ldp, k0, ncols, expo, pp[p].sign, (int64_t)p * kpad0, B, ldb);
+    GP_LAUNCH_CHECK(ctx, "k_panel_slices");
+  }
+  GP_CUDA(ctx, cudaMemsetAsync(Z, 0, (size_t)nrows * ldz * 8, ctx->stream));
+
+  /* the tensor-core kernel */
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tc_encode(ctx);
+  if (!enc) return GP_ERR_CUDA;
+  CUtensorMap tmb;
+  {
+    cuuint64_t dims[2] = {(cuuint64_t)ldb, (cuuint64_t)ncols4_pad};
+    cuuint64_t strides[1] = {(cuuint64_t)ldb * 2};
+    cuuint32_t box[2] = {XK, XT};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(&tmb, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, B, dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return gp_fail(ctx, GP_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  }
+  GP_CUDA(ctx, cudaFuncSetAttribute(k_geno_panel_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    X_SMEM));
+  const int32_t nrt = nrows_pad / XT, nct = ncols4_pad / XT;
+  int32_t tiles = nrt * nct;
+  int32_t ksplit = 1;
+  while (tiles * ksplit < 2 * ctx->num_sms && ksplit * 4 <= nkb) ksplit *= 2;
+  /* keep each work item's k range below 2^19 so that int32 sums stay exact */
+  while ((int64_t)((nkb + ksplit - 1) / ksplit) * XK > (1 << 19)) ksplit *= 2;
+  int32_t nitems = tiles * ksplit;
+  int grid = nitems < ctx->num_sms ? nitems : ctx->num_sms;
+  uint64_t lut_lo = pp[0].count ? LUT_COUNT : LUT_MASK;
+  uint64_t lut_hi = npanels > 1 ? (pp[1].count ? LUT_COUNT : LUT_MASK) : lut_lo;
+  k_geno_panel_tc<<<grid, X_THREADS, X_SMEM, ctx->stream>>>(tmb, codes, ldc, nrows, ncols4, nkb,
+                                                           kb0, kb0, lut_lo, lut_hi, ksplit, Z, ldz,
+                                                           d_err);
+  GP_LAUNCH_CHECK(ctx, "k_geno_panel_tc");
+  {
+    int64_t work = (int64_t)nrows * ncols;
+    k_panel_combine<<<grid_cap(ctx, work, 256, 32), 256, 0, ctx->stream>>>(Z, ldz, nrows, ncols,
+                                                                            expo, d_Y, ldy);
+    GP_LAUNCH_CHECK(ctx, "k_panel_combine");
+  }
+  int herr = 0;
+  GP_CUDA(ctx, gp_memcpy(ctx, &herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (herr) return gp_fail(ctx, GP_ERR_TIMEOUT, "tensor-core product wait timed out (code %d)", herr);
+  return GP_OK;
+}

@@ -443,9 +443,7 @@ int gp_gram_split(gp_ctx *ctx, int precision)
   __nv_bfloat16 *xhi = (__nv_bfloat16 *)base;
   __nv_bfloat16 *xlo = (__nv_bfloat16 *)(base + xbytes);
   uint32_t *split = (uint32_t *)(base + 2 * xbytes);
-  int *d_err;
-  rc = gp_scratch(ctx, 256, (void **)&d_err);
-  if (rc) return rc;
+  int *d_err = ctx->d_err;
   GP_CUDA(ctx, cudaMemsetAsync(d_err, 0, sizeof(int), ctx->stream));
   {
     int blocks = (nk + 255) / 256;

@@ -72,6 +72,11 @@ struct gp_ctx {
   size_t scratch_cap;
   void *d_scratch2;
   size_t scratch2_cap;
+  void *d_scratch3;    /* small panels built between the products of gp_geno_tc */
+  size_t scratch3_cap;
+  int *d_err;          /* error word written by the tensor-core kernels' bounded waits */
+  int precision;       /* precision of the last gp_xtx: split precisions use the tensor-core
+                          exact products for weights and lsqproject */
 };
 
 int gp_fail(gp_ctx *ctx, int code, const char *fmt, ...);
@@ -81,6 +86,7 @@ cudaError_t gp_memcpy(gp_ctx *ctx, void *dst, const void *src, size_t bytes, cud
 int gp_cuda_fail(gp_ctx *ctx, cudaError_t e, const char *what);
 int gp_scratch(gp_ctx *ctx, size_t bytes, void **out);
 int gp_scratch2(gp_ctx *ctx, size_t bytes, void **out);
+int gp_scratch_aux(gp_ctx *ctx, size_t bytes, void **out);
 int gp_realloc(gp_ctx *ctx, void **ptr, size_t bytes);
 
 #define GP_CUDA(ctx, call)                                   \

@@ -120,7 +120,10 @@ def test_ridoutlier_host_matches_oracle():
         assert np.array_equal(s1, s2)
 
 
-def test_weights_and_lsqproj_vs_oracle(gpu):
+@pytest.mark.parametrize("prec", [native.GP_PREC_FP64, native.GP_PREC_SPLIT_FP16])
+def test_weights_and_lsqproj_vs_oracle(gpu, prec):
+    """SNP weights, sample scores and lsqproject against the oracle on the same eigenvectors:
+    FP64 SIMT kernels (FP64 path) or the exact sliced tensor-core products (split paths)."""
     rec, pop = synth(3000, [80, 80, 60], [0.01, 0.03, 0.05], miss=0.05, seed=25, n_admixed=10)
     nind = len(pop)
     gpu.load_genotypes(rec, nind)
@@ -128,7 +131,7 @@ def test_weights_and_lsqproj_vs_oracle(gpu):
     cols = np.arange(3000, dtype=np.int32)
     gpu.set_samples(rows)
     gpu.set_snps(cols)
-    gpu.xtx(minallelecnt=3)
+    gpu.xtx(minallelecnt=3, precision=prec)
     ev, V = gpu.eigvecs(8)
     K = 6
     ff, fx, sc = gpu.snp_weights(K)
@@ -143,8 +146,9 @@ def test_weights_and_lsqproj_vs_oracle(gpu):
     assert np.array_equal(nobs, onobs)
     assert np.array_equal(st, ost)
     ok = st == 0
-    assert np.max(np.abs(a[:, ok] - oa[:, ok])) <= 1e-8
-    assert np.max(np.abs(b[:, ok] - ob[:, ok])) <= 1e-8 * max(1.0, np.max(np.abs(ob)))
+    # lsqproject coefficients (before eigscale, magnitudes up to ~1e4): 1e-11 relative
+    assert np.max(np.abs(a[:, ok] - oa[:, ok])) <= 1e-11 * max(1.0, np.max(np.abs(oa)))
+    assert np.max(np.abs(b[:, ok] - ob[:, ok])) <= 1e-11 * max(1.0, np.max(np.abs(ob)))
 
 
 @pytest.mark.parametrize("case", CASES)
@@ -250,3 +254,47 @@ def test_split_subset_rows(gpu, prec):
     X = O.gram(s)
     assert (s.killed == 1).sum() > 0
     assert np.max(np.abs(r["XTX"] - X)) / np.max(np.abs(X)) <= SPLIT_TOL[prec][0]
+
+
+def test_tc_products_large_k_and_projection_subset(gpu):
+    """exact tensor-core products over 20,000 SNPs (several 8,192-SNP chunks, k-splits) and a
+    projection set of samples outside the PCA rows, against the oracle"""
+    rec, pop = synth(20000, [150, 150, 100], [0.01, 0.02, 0.05], miss=0.1, seed=26, n_admixed=30)
+    nind = len(pop)
+    gpu.load_genotypes(rec, nind)
+    rows = np.arange(0, 300, dtype=np.int32)
+    cols = np.arange(20000, dtype=np.int32)
+    gpu.set_samples(rows)
+    gpu.set_snps(cols)
+    gpu.xtx(precision=native.GP_PREC_SPLIT_FP16)
+    ev, V = gpu.eigvecs(10)
+    K = 10
+    ff, fx, sc = gpu.snp_weights(K)
+    s = O.pass_columns(rec, cols, rows)
+    off, ofx, osc = O.weights(s, V, K)
+    assert np.max(np.abs(ff - off)) <= 1e-10 * np.max(np.abs(off))
+    assert np.max(np.abs(fx - ofx)) <= 1e-10 * np.max(np.abs(ofx))
+    proj = np.arange(250, nind, dtype=np.int32)
+    a, b, nobs, st = gpu.lsqproj(K, proj)
+    oa, ob, onobs, ost = O.lsqproj(s, off, osc, K, proj)
+    assert np.array_equal(nobs, onobs) and np.array_equal(st, ost)
+    ok = st == 0
+    # lsqproject coefficients (before eigscale, magnitudes up to ~1e4): 1e-11 relative
+    assert np.max(np.abs(a[:, ok] - oa[:, ok])) <= 1e-11 * max(1.0, np.max(np.abs(oa)))
+    assert np.max(np.abs(b[:, ok] - ob[:, ok])) <= 1e-11 * max(1.0, np.max(np.abs(ob)))
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_smartpca_run_split_fp16_vs_reference(gpu, case):
+    """split-fp16 Gram + tensor-core weights/lsqproject against the reference goldens:
+    eigenvalues within 1e-6 relative (of the largest), identical outliers and printed sets,
+    the top two coordinates (population structure) within 1e-4."""
+    c = Case(case)
+    opts = native.default_opts(precision=native.GP_PREC_SPLIT_FP16, **c.opts())
+    r = native.smartpca_run(gpu, c.records, c.nind, opts, code=c.code,
+                            ind_affstatus=c.affstatus)
+    assert r["nrows"] == len(c.ref_evals)
+    assert np.max(np.abs(r["evals"] - c.ref_evals)) <= 1e-6 * abs(c.ref_evals[0])
+    assert [c.ids[k] for k, *_ in r["outliers"]] == c.ref_outliers
+    mine = coords_by_id(c.ids, r["coords"], r["ind_out"])
+    compare_coords(c.ref_coords, mine, 2, 1e-4)

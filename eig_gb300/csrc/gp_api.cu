@@ -310,39 +310,54 @@ extern "C" int gp_eigvecs(gp_ctx *ctx, int32_t nvec, double *evals, double *evec
   int32_t keep = nvec > 0 ? nvec : 1;
   rc = gp_realloc(ctx, (void **)&ctx->d_evecs, sizeof(double) * (size_t)n * keep);
   if (rc) return rc;
-  int lwork = 0;
-  if (cusolverDnDsyevd_bufferSize(ctx->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
-                                  n, ctx->d_xtx, n, ctx->d_evals, &lwork) !=
-      CUSOLVER_STATUS_SUCCESS)
-    return gp_fail(ctx, GP_ERR_SOLVER, "cusolverDnDsyevd_bufferSize failed");
-  uint8_t *ws;
-  rc = gp_scratch(ctx, sizeof(double) * (size_t)lwork + 256, (void **)&ws);
-  if (rc) return rc;
-  int *d_info = (int *)(ws + sizeof(double) * (size_t)lwork);
-  if (cusolverDnDsyevd(ctx->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n,
-                       ctx->d_xtx, n, ctx->d_evals, (double *)ws, lwork,
-                       d_info) != CUSOLVER_STATUS_SUCCESS)
-    return gp_fail(ctx, GP_ERR_SOLVER, "cusolverDnDsyevd failed to launch");
-  int info = 0;
-  GP_CUDA(ctx, gp_memcpy(ctx, &info, d_info, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-  if (nvec > 0) {
-    int64_t tot = (int64_t)n * nvec;
-    int b2 = (int)((tot + 255) / 256);
-    if (b2 > ctx->num_sms * 16) b2 = ctx->num_sms * 16;
-    k_take_top<<<b2, 256, 0, ctx->stream>>>(ctx->d_evecs, ctx->d_xtx, n, nvec);
-    GP_LAUNCH_CHECK(ctx, "k_take_top");
-  }
-  std::vector<double> w((size_t)n);
-  GP_CUDA(ctx, gp_memcpy(ctx, w.data(), ctx->d_evals, sizeof(double) * (size_t)n,
-                               cudaMemcpyDeviceToHost, ctx->stream));
-  if (evecs && nvec > 0)
-    GP_CUDA(ctx, gp_memcpy(ctx, evecs, ctx->d_evecs, sizeof(double) * (size_t)n * nvec,
+  const char *alt = getenv("GP_EIG_SYEVD");
+  if (!(alt && alt[0] == '1')) {
+    /* tridiagonalisation + bisection + inverse iteration for the top vectors (gp_eig.cu) */
+    rc = gp_eig_tridiag(ctx, n, nvec, ctx->d_evals, ctx->d_evecs);
+    if (rc) return rc;
+    if (evals)
+      GP_CUDA(ctx, gp_memcpy(ctx, evals, ctx->d_evals, sizeof(double) * (size_t)n,
+                             cudaMemcpyDeviceToHost, ctx->stream));
+    if (evecs && nvec > 0)
+      GP_CUDA(ctx, gp_memcpy(ctx, evecs, ctx->d_evecs, sizeof(double) * (size_t)n * nvec,
+                             cudaMemcpyDeviceToHost, ctx->stream));
+    GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->xtx_valid = 0; /* sytrd overwrote the Gram */
+  } else {
+    int lwork = 0;
+    if (cusolverDnDsyevd_bufferSize(ctx->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
+                                    n, ctx->d_xtx, n, ctx->d_evals, &lwork) !=
+        CUSOLVER_STATUS_SUCCESS)
+      return gp_fail(ctx, GP_ERR_SOLVER, "cusolverDnDsyevd_bufferSize failed");
+    uint8_t *ws;
+    rc = gp_scratch(ctx, sizeof(double) * (size_t)lwork + 256, (void **)&ws);
+    if (rc) return rc;
+    int *d_info = (int *)(ws + sizeof(double) * (size_t)lwork);
+    if (cusolverDnDsyevd(ctx->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n,
+                         ctx->d_xtx, n, ctx->d_evals, (double *)ws, lwork,
+                         d_info) != CUSOLVER_STATUS_SUCCESS)
+      return gp_fail(ctx, GP_ERR_SOLVER, "cusolverDnDsyevd failed to launch");
+    int info = 0;
+    GP_CUDA(ctx, gp_memcpy(ctx, &info, d_info, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    if (nvec > 0) {
+      int64_t tot = (int64_t)n * nvec;
+      int b2 = (int)((tot + 255) / 256);
+      if (b2 > ctx->num_sms * 16) b2 = ctx->num_sms * 16;
+      k_take_top<<<b2, 256, 0, ctx->stream>>>(ctx->d_evecs, ctx->d_xtx, n, nvec);
+      GP_LAUNCH_CHECK(ctx, "k_take_top");
+    }
+    std::vector<double> w((size_t)n);
+    GP_CUDA(ctx, gp_memcpy(ctx, w.data(), ctx->d_evals, sizeof(double) * (size_t)n,
                                  cudaMemcpyDeviceToHost, ctx->stream));
-  GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  ctx->xtx_valid = 0; /* the solver overwrote the Gram with eigenvectors */
-  if (info != 0) return gp_fail(ctx, GP_ERR_SOLVER, "eigensolver info = %d", info);
-  if (evals)
-    for (int32_t i = 0; i < n; ++i) evals[i] = w[(size_t)(n - 1 - i)];
+    if (evecs && nvec > 0)
+      GP_CUDA(ctx, gp_memcpy(ctx, evecs, ctx->d_evecs, sizeof(double) * (size_t)n * nvec,
+                                   cudaMemcpyDeviceToHost, ctx->stream));
+    GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->xtx_valid = 0; /* the solver overwrote the Gram with eigenvectors */
+    if (info != 0) return gp_fail(ctx, GP_ERR_SOLVER, "eigensolver info = %d", info);
+    if (evals)
+      for (int32_t i = 0; i < n; ++i) evals[i] = w[(size_t)(n - 1 - i)];
+  }
   ctx->nvec = nvec;
   ctx->eig_valid = 1;
   ctx->weights_valid = 0;

@@ -1,0 +1,385 @@
+/*
+ * Dense symmetric FP64 eigensolve for the smartpca Gram, on the device: all N eigenvalues
+ * and the top nvec eigenvectors (the reference computes every eigenpair with LAPACK dspev,
+ * src/eigensrc/eigx.c:97-117, but prints all eigenvalues and uses only the top vectors).
+ *
+ *   1. Householder tridiagonalisation A = Q T Q^T (cuSOLVER sytrd, lower);
+ *   2. all eigenvalues of T by bisection on Sturm counts, one thread per eigenvalue index
+ *      (the published bisection method: the count of negative pivots of the LDL^T
+ *      factorisation of T - x I equals the number of eigenvalues below x): FP32 brackets
+ *      first, checked and finished in FP64 to a few ulps;
+ *   3. the top nvec eigenvectors of T by inverse iteration, one block per vector: LU with
+ *      partial pivoting of the tridiagonal T - lambda I (Gaussian elimination with row
+ *      interchanges) and three solves from a fixed pseudo-random start, then modified
+ *      Gram-Schmidt over the vectors in order (eigenvalues that are distinct to far more than
+ *      eps*||T|| make each iterate converge to its own eigenvector);
+ *   4. back-transformation of those nvec vectors only, V = Q Z (cuSOLVER ormtr).
+ */
+#include <cuda_runtime.h>
+#include <cusolverDn.h>
+#include <float.h>
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+
+#include "gp_internal.h"
+
+
+/*
+ * Number of eigenvalues of T (d, e2 = e^2) below x; pivmin guards tiny pivots.  Only the
+ * signs of the pivots matter, so e2/q uses a reciprocal from the FP32 approximation with
+ * one FP64 Newton step (relative error ~2^-46) instead of an IEEE FP64 division, whose
+ * instruction sequence is long on this GPU's narrow FP64 pipe.
+ */
+__device__ __forceinline__ int sturm_count(const double *d, const double *e2, int n, double x,
+                                           double pivmin)
+{
+  int cnt = 0;
+  double q = d[0] - x;
+  if (fabs(q) < pivmin) q = -pivmin;
+  if (q < 0.0) ++cnt;
+  for (int i = 1; i < n; ++i) {
+    double r = (double)__frcp_rn((float)q);
+    r = r * fma(-q, r, 2.0);
+    q = fma(-e2[i - 1], r, d[i] - x);
+    if (fabs(q) < pivmin) q = -pivmin;
+    if (q < 0.0) ++cnt;
+  }
+  return cnt;
+}
+
+/* the same count in FP32 (coarse brackets only; verified in FP64 afterwards) */
+__device__ __forceinline__ int sturm_count_f(const float *d, const float *e2, int n, float x,
+                                             float pivmin)
+{
+  int cnt = 0;
+  float q = d[0] - x;
+  if (fabsf(q) < pivmin) q = -pivmin;
+  if (q < 0.f) ++cnt;
+  for (int i = 1; i < n; ++i) {
+    q = (d[i] - x) - __fdividef(e2[i - 1], q);
+    if (fabsf(q) < pivmin) q = -pivmin;
+    if (q < 0.f) ++cnt;
+  }
+  return cnt;
+}
+
+/*
+ * w[k] = k-th smallest eigenvalue of T, one thread per k: bisection in FP32 to a bracket of
+ * about 1e-6 of ||T|| (FP32 division is cheap on this GPU, FP64 is not), widened by a safety
+ * margin and checked with two FP64 Sturm counts (back to the full Gershgorin bracket if the
+ * check fails), then FP64 bisection to a few ulps.  d, e2 (and FP32 copies) are staged in
+ * shared memory when they fit (dynamic smem = 24 n bytes), else read from global memory.
+ */
+__global__ void k_bisect_all(const double *gd, const double *ge2, int n, double gl, double gu,
+                             double tnorm, double pivmin, int use_smem, double *w)
+{
+  extern __shared__ double sm[];
+  const double *d = gd, *e2 = ge2;
+  const float *df = NULL, *e2f = NULL;
+  if (use_smem) {
+    double *sd = sm, *se2 = sm + n;
+    float *sdf = (float *)(sm + 2 * n), *se2f = sdf + n;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      sd[i] = gd[i];
+      sdf[i] = (float)gd[i];
+      if (i < n - 1) {
+        se2[i] = ge2[i];
+        se2f[i] = (float)ge2[i];
+      }
+    }
+    __syncthreads();
+    d = sd;
+    e2 = se2;
+    df = sdf;
+    e2f = se2f;
+  }
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  double lo = gl, hi = gu;
+  if (df) {
+    float flo = (float)gl, fhi = (float)gu;
+    const float fpiv = fmaxf((float)pivmin, 1e-30f) * 1e6f;
+    const float ftol = 4e-7f * (float)tnorm;
+    for (int it = 0; it < 40 && fhi - flo > ftol; ++it) {
+      float mid = 0.5f * (flo + fhi);
+      if (mid <= flo || mid >= fhi) break;
+      if (sturm_count_f(df, e2f, n, mid, fpiv) > k)
+        fhi = mid;
+      else
+        flo = mid;
+    }
+    const double margin = 64.0 * (double)FLT_EPSILON * tnorm;
+    lo = fmax(gl, (double)flo - margin);
+    hi = fmin(gu, (double)fhi + margin);
+    if (sturm_count(d, e2, n, lo, pivmin) > k || sturm_count(d, e2, n, hi, pivmin) <= k) {
+      lo = gl;
+      hi = gu;
+    }
+  }
+  for (int it = 0; it < 80; ++it) {
+    double mid = 0.5 * (lo + hi);
+    if (mid <= lo || mid >= hi) break;
+    if (sturm_count(d, e2, n, mid, pivmin) > k)
+      hi = mid;
+    else
+      lo = mid;
+  }
+  w[k] = 0.5 * (lo + hi);
+}
+
+/* deterministic start vector entry in (-1, 1) */
+__device__ __forceinline__ double start_entry(int j, int i)
+{
+  uint64_t z = ((uint64_t)(j + 1) << 32) ^ (uint64_t)(i + 1) ^ 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  return ((double)(z >> 11) * (1.0 / 9007199254740992.0)) * 2.0 - 1.0;
+}
+
+__device__ double block_sum(double v, double *red)
+{
+  red[threadIdx.x] = v;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o; o >>= 1) {
+    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  double r = red[0];
+  __syncthreads();
+  return r;
+}
+
+/*
+ * Inverse iteration, one block per top eigenvalue (vector j belongs to w[n-1-j]).
+ * The LU factorisation with partial pivoting of T - lam I and the solves are sequential
+ * recurrences run by thread 0 with the running values carried in registers (the arrays are
+ * only written, or read ahead of the dependency chain); the other threads normalise.
+ * work: per vector 6n doubles.  Z [nvec][n] (column-major N x nvec for ormtr).
+ */
+__global__ void k_inverse_iteration(const double *d, const double *e, int n, const double *w,
+                                    int nvec, double tnorm, double *Z, double *work)
+{
+  __shared__ double red[256];
+  const int j = blockIdx.x;
+  if (j >= nvec) return;
+  double *base = work + (int64_t)j * 6 * n;
+  double *Dinv = base, *DL = base + n, *DU = base + 2 * n, *DU2 = base + 3 * n;
+  double *x = Z + (int64_t)j * n;
+  int *piv = (int *)(base + 5 * n);
+  const double lam = w[n - 1 - j];
+  const double tiny = DBL_EPSILON * tnorm;
+  if (threadIdx.x == 0) {
+    /* dgttrf-style elimination; cur = running diagonal of row i, du = its superdiagonal */
+    double cur = d[0] - lam;
+    double du = n > 1 ? e[0] : 0.0;
+    for (int i = 0; i < n - 1; ++i) {
+      double ei = e[i];
+      double dn = d[i + 1] - lam;                    /* row i+1 diagonal */
+      double en = (i < n - 2) ? e[i + 1] : 0.0;      /* row i+1 superdiagonal */
+      if (fabs(cur) >= fabs(ei)) {
+        if (cur == 0.0) cur = tiny;
+        double f = ei / cur;
+        DL[i] = f;
+        DU[i] = du;
+        DU2[i] = 0.0;
+        Dinv[i] = 1.0 / cur;
+        piv[i] = 0;
+        cur = dn - f * du;
+        du = en;
+      } else {
+        double f = cur / ei;
+        DL[i] = f;
+        Dinv[i] = 1.0 / ei;
+        DU[i] = dn;
+        DU2[i] = en;
+        piv[i] = 1;
+        cur = du - f * dn;
+        du = -f * en;
+      }
+    }
+    if (cur == 0.0) cur = tiny;
+    Dinv[n - 1] = 1.0 / cur;
+  }
+  for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = start_entry(j, i);
+  __syncthreads();
+  for (int iter = 0; iter < 3; ++iter) {
+    double s2 = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s2 += x[i] * x[i];
+    s2 = block_sum(s2, red);
+    double inv = s2 > 0.0 ? 1.0 / sqrt(s2) : 1.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] *= inv;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      /* forward: apply the row interchanges and L; carry x[i+1] in a register */
+      double xi = x[0];
+      for (int i = 0; i < n - 1; ++i) {
+        double xn = x[i + 1];
+        if (piv[i] == 0) {
+          x[i] = xi;
+          xi = xn - DL[i] * xi;
+        } else {
+          x[i] = xn;
+          xi = xi - DL[i] * xn;
+        }
+      }
+      x[n - 1] = xi;
+      /* back substitution with U (diag, super, super-super) */
+      double x2 = 0.0, x1 = x[n - 1] * Dinv[n - 1];
+      x[n - 1] = x1;
+      for (int i = n - 2; i >= 0; --i) {
+        double v = (x[i] - DU[i] * x1 - DU2[i] * x2) * Dinv[i];
+        x[i] = v;
+        x2 = x1;
+        x1 = v;
+      }
+    }
+    __syncthreads();
+  }
+  double s2 = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s2 += x[i] * x[i];
+  s2 = block_sum(s2, red);
+  double inv = 1.0 / sqrt(s2);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] *= inv;
+}
+
+/* modified Gram-Schmidt over the nvec vectors, in order (one block) */
+__global__ void k_mgs(double *Z, int n, int nvec)
+{
+  __shared__ double red[256];
+  for (int j = 0; j < nvec; ++j) {
+    double *zj = Z + (int64_t)j * n;
+    for (int p = 0; p < j; ++p) {
+      const double *zp = Z + (int64_t)p * n;
+      double s = 0.0;
+      for (int i = threadIdx.x; i < n; i += blockDim.x) s += zp[i] * zj[i];
+      s = block_sum(s, red);
+      for (int i = threadIdx.x; i < n; i += blockDim.x) zj[i] -= s * zp[i];
+      __syncthreads();
+    }
+    double s2 = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s2 += zj[i] * zj[i];
+    s2 = block_sum(s2, red);
+    double inv = 1.0 / sqrt(s2);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) zj[i] *= inv;
+    __syncthreads();
+  }
+}
+
+/* evals_desc[i] = w[n-1-i] */
+__global__ void k_reverse(const double *w, double *out, int n)
+{
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    out[i] = w[n - 1 - i];
+}
+
+/*
+ * Eigenpairs of the symmetric n x n matrix in ctx->d_xtx (overwritten): d_evals_desc [n]
+ * all eigenvalues descending, d_vecs [nvec][n] top eigenvectors (descending).
+ */
+int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, double *d_vecs)
+{
+  cusolverDnHandle_t h = ctx->solver;
+  int lwork = 0, lwork2 = 0;
+  /* GP_EIG_TIMING=1 prints the device time of each stage to stderr */
+  const char *tenv = getenv("GP_EIG_TIMING");
+  const int timing = tenv && tenv[0] == '1';
+  cudaEvent_t ev[5];
+  if (timing)
+    for (int i = 0; i < 5; ++i) cudaEventCreate(&ev[i]);
+#define GP_EIG_MARK(i) \
+  if (timing) cudaEventRecord(ev[i], ctx->stream)
+  /* scratch: d, e, tau, e2, w, work(sytrd), inverse-iteration work, info */
+  if (cusolverDnDsytrd_bufferSize(h, CUBLAS_FILL_MODE_LOWER, n, ctx->d_xtx, n, NULL, NULL, NULL,
+                                  &lwork) != CUSOLVER_STATUS_SUCCESS)
+    return gp_fail(ctx, GP_ERR_SOLVER, "cusolverDnDsytrd_bufferSize failed");
+  int nv = nvec > 0 ? nvec : 1;
+  if (cusolverDnDormtr_bufferSize(h, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, n, nv,
+                                  ctx->d_xtx, n, NULL, d_vecs, n, &lwork2) != CUSOLVER_STATUS_SUCCESS)
+    return gp_fail(ctx, GP_ERR_SOLVER, "cusolverDnDormtr_bufferSize failed");
+  int lw = lwork > lwork2 ? lwork : lwork2;
+  size_t nd = (size_t)n;
+  size_t bytes = sizeof(double) * (5 * nd + (size_t)lw + 6 * nd * nv + 64) + sizeof(int) * 64;
+  double *base;
+  int rc = gp_scratch(ctx, bytes, (void **)&base);
+  if (rc) return rc;
+  double *d = base, *e = d + nd, *tau = e + nd, *e2 = tau + nd, *w = e2 + nd;
+  double *ws = w + nd, *iw = ws + lw;
+  int *d_info = (int *)(iw + 6 * nd * nv + 8);
+  GP_EIG_MARK(0);
+  if (cusolverDnDsytrd(h, CUBLAS_FILL_MODE_LOWER, n, ctx->d_xtx, n, d, e, tau, ws, lw, d_info) !=
+      CUSOLVER_STATUS_SUCCESS)
+    return gp_fail(ctx, GP_ERR_SOLVER, "cusolverDnDsytrd failed to launch");
+  GP_EIG_MARK(1);
+  int info = 0;
+  GP_CUDA(ctx, gp_memcpy(ctx, &info, d_info, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  /* Gershgorin bounds and the pivot guard need d, e on the host (2n doubles) */
+  std::vector<double> hd(nd), he(nd > 1 ? nd - 1 : 1);
+  GP_CUDA(ctx, gp_memcpy(ctx, hd.data(), d, sizeof(double) * nd, cudaMemcpyDeviceToHost, ctx->stream));
+  if (n > 1)
+    GP_CUDA(ctx, gp_memcpy(ctx, he.data(), e, sizeof(double) * (nd - 1), cudaMemcpyDeviceToHost,
+                           ctx->stream));
+  GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (info != 0) return gp_fail(ctx, GP_ERR_SOLVER, "sytrd info = %d", info);
+  double gl = hd[0], gu = hd[0], tnorm = 0.0, emax2 = 0.0;
+  std::vector<double> he2(nd > 1 ? nd - 1 : 1);
+  for (int i = 0; i < n; ++i) {
+    double r = (i > 0 ? fabs(he[(size_t)i - 1]) : 0.0) + (i < n - 1 ? fabs(he[(size_t)i]) : 0.0);
+    gl = fmin(gl, hd[(size_t)i] - r);
+    gu = fmax(gu, hd[(size_t)i] + r);
+    tnorm = fmax(tnorm, fabs(hd[(size_t)i]) + r);
+    if (i < n - 1) {
+      he2[(size_t)i] = he[(size_t)i] * he[(size_t)i];
+      emax2 = fmax(emax2, he2[(size_t)i]);
+    }
+  }
+  double span = gu - gl;
+  gl -= 2.0 * DBL_EPSILON * tnorm * n + DBL_MIN;
+  gu += 2.0 * DBL_EPSILON * tnorm * n + DBL_MIN;
+  (void)span;
+  /* the pivot guard stays inside FP32's exponent range (the reciprocal starts in FP32) */
+  double pivmin = fmax(DBL_MIN * fmax(1.0, emax2), 1e-30 * fmax(tnorm, 1e-300));
+  if (n > 1)
+    GP_CUDA(ctx, gp_memcpy(ctx, e2, he2.data(), sizeof(double) * (nd - 1), cudaMemcpyHostToDevice,
+                           ctx->stream));
+  GP_EIG_MARK(2);
+  {
+    size_t smem = (size_t)24 * (size_t)n;
+    int use_smem = smem <= 200 * 1024;
+    if (use_smem)
+      GP_CUDA(ctx, cudaFuncSetAttribute(k_bisect_all, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem));
+    int threads = 64;
+    k_bisect_all<<<(n + threads - 1) / threads, threads, use_smem ? smem : 0, ctx->stream>>>(
+        d, e2, n, gl, gu, tnorm, pivmin, use_smem, w);
+    GP_LAUNCH_CHECK(ctx, "k_bisect_all");
+  }
+  k_reverse<<<(n + 255) / 256, 256, 0, ctx->stream>>>(w, d_evals_desc, n);
+  GP_LAUNCH_CHECK(ctx, "k_reverse");
+  GP_EIG_MARK(3);
+  if (nvec > 0) {
+    k_inverse_iteration<<<nvec, 256, 0, ctx->stream>>>(d, e, n, w, nvec, tnorm, d_vecs, iw);
+    GP_LAUNCH_CHECK(ctx, "k_inverse_iteration");
+    k_mgs<<<1, 256, 0, ctx->stream>>>(d_vecs, n, nvec);
+    GP_LAUNCH_CHECK(ctx, "k_mgs");
+    if (cusolverDnDormtr(h, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, n, nvec,
+                         ctx->d_xtx, n, tau, d_vecs, n, ws, lw, d_info) != CUSOLVER_STATUS_SUCCESS)
+      return gp_fail(ctx, GP_ERR_SOLVER, "cusolverDnDormtr failed to launch");
+    GP_CUDA(ctx, gp_memcpy(ctx, &info, d_info, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (info != 0) return gp_fail(ctx, GP_ERR_SOLVER, "ormtr info = %d", info);
+  }
+  if (timing) {
+    GP_EIG_MARK(4);
+    cudaEventSynchronize(ev[4]);
+    float t01 = 0, t23 = 0, t34 = 0;
+    cudaEventElapsedTime(&t01, ev[0], ev[1]);
+    cudaEventElapsedTime(&t23, ev[2], ev[3]);
+    cudaEventElapsedTime(&t34, ev[3], ev[4]);
+    fprintf(stderr, "eig n=%d: sytrd %.1f ms, eigenvalues %.1f ms, vectors+ormtr %.1f ms\n", n,
+            t01, t23, t34);
+    for (int i = 0; i < 5; ++i) cudaEventDestroy(ev[i]);
+  }
+  return GP_OK;
+}

@@ -7,6 +7,7 @@
 #include <stdint.h>
 #include <stdio.h>
 #include <string.h>
+#include <vector>
 
 #include "../../include/gpupca.h"
 
@@ -109,6 +110,7 @@ int gp_launch_snp_stats(gp_ctx *ctx, const gp_xtx_opts *o);
 int gp_gram_fp64(gp_ctx *ctx);
 int gp_gram_split(gp_ctx *ctx, int precision);
 int gp_launch_symmetrize_trace(gp_ctx *ctx, double *d_trace);
+int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, double *d_vecs);
 int gp_launch_materialize_f64(gp_ctx *ctx, int32_t k0, int32_t kc, int32_t pitch, double *d_x,
                               double scale);
 

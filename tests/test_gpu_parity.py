@@ -188,8 +188,14 @@ def test_cli_dropin_matches_reference_text(case, tmp_path):
     assert [l.split()[0] for l in mine[1:]] == [l.split()[0] for l in want[1:]]
     s = np.sign(np.sum(A * B, axis=0))
     assert np.max(np.abs(A - B * s)) <= 1.01e-4
-    got_out = open(d / "out.outliers").read()
-    assert got_out == open(d / "ref.outliers").read()
+    # outlier lines: identical except the sign of the z-score, which follows the (arbitrary)
+    # sign of the eigenvector, as the reference's does with its LAPACK build
+    got = [l.split() for l in open(d / "out.outliers").read().splitlines()]
+    exp = [l.split() for l in open(d / "ref.outliers").read().splitlines()]
+    assert len(got) == len(exp)
+    for g, x in zip(got, exp):
+        assert g[:8] == x[:8] and g[9:] == x[9:]
+        assert g[8].lstrip("-") == x[8].lstrip("-")
 
 
 def _gram_pair(gpu, rec, nind, rows, cols, precision):
@@ -298,3 +304,30 @@ def test_smartpca_run_split_fp16_vs_reference(gpu, case):
     assert [c.ids[k] for k, *_ in r["outliers"]] == c.ref_outliers
     mine = coords_by_id(c.ids, r["coords"], r["ind_out"])
     compare_coords(c.ref_coords, mine, 2, 1e-4)
+
+
+def test_eig_tridiag_all_values_top_vectors(gpu):
+    """sytrd + bisection + inverse iteration + ormtr: every eigenvalue within 1e-12 of the
+    largest against LAPACK (numpy eigh), 24 top eigenvectors with small residuals, orthonormal,
+    and equal (up to sign) to LAPACK's where the eigenvalues are separated"""
+    rec, pop = synth(6000, [500, 400, 300], [0.01, 0.02, 0.04], miss=0.02, seed=27)
+    nind = len(pop)
+    gpu.load_genotypes(rec, nind)
+    rows = np.arange(nind, dtype=np.int32)
+    cols = np.arange(6000, dtype=np.int32)
+    gpu.set_samples(rows)
+    gpu.set_snps(cols)
+    X = gpu.xtx()["XTX"]
+    ev, V = gpu.eigvecs(24)
+    Xs = X * ((nind - 1) / np.trace(X))
+    w, U = np.linalg.eigh(Xs)
+    w = w[::-1]
+    U = U[:, ::-1].T
+    assert np.max(np.abs(ev - w)) <= 1e-12 * w[0]
+    R = V @ Xs - ev[:24, None] * V
+    assert np.max(np.linalg.norm(R, axis=1)) <= 1e-9 * w[0]
+    assert np.max(np.abs(V @ V.T - np.eye(24))) <= 1e-10
+    gaps = np.minimum(np.abs(np.diff(w[:25]))[:-1], np.abs(np.diff(w[:25]))[1:])
+    sep = np.concatenate([[w[0] - w[1]], gaps])[:24] > 1e-3 * w[0]
+    cos = np.abs(np.sum(V * U[:24], axis=1))
+    assert np.all(cos[sep] > 1 - 1e-9)

@@ -67,14 +67,16 @@ __device__ __forceinline__ void fence_proxy_async_smem()
 }
 
 /*
- * codes: [nrows_pad][ldc] bytes (2-bit codes, MSB first, 3 = missing -> 0); k-block kb of row
- * r is the 16 bytes at codes + r*ldc + (kb % kb_period)*16, decoded with lut_lo for
- * kb < kb_switch and lut_hi otherwise (the concatenated-k form [G | O]).
+ * codes: rows of ldc bytes (2-bit codes, MSB first, 3 = missing -> 0); output row r reads
+ * code row row_map[r] (r itself when row_map is NULL); its k-block kb is the 16 bytes at
+ * (kb % kb_period)*16, decoded with lut_lo for kb < kb_switch and lut_hi otherwise (the
+ * concatenated-k form [G | O]).
  * zout: [nrows][ldz] FP64, receives atomically the exact integer sums per slice-column.
  */
 __global__ void __launch_bounds__(X_THREADS, 1)
 k_geno_panel_tc(const __grid_constant__ CUtensorMap tm_b, const uint8_t *__restrict__ codes,
-                int64_t ldc, int32_t nrows, int32_t ncols4, int32_t nkb, int32_t kb_period,
+                int64_t ldc, const int32_t *__restrict__ row_map, int32_t nrows, int32_t ncols4,
+                int32_t nkb, int32_t kb_period,
                 int32_t kb_switch, uint64_t lut_lo, uint64_t lut_hi, int32_t ksplit,
                 double *zout, int64_t ldz, int *err)
 {
@@ -186,7 +188,8 @@ k_geno_panel_tc(const __grid_constant__ CUtensorMap tm_b, const uint8_t *__restr
       int32_t ks = w % ksplit, rt = w / (ksplit * nct);
       int32_t kb0 = ks * kb_per, kb1 = kb0 + kb_per < nkb ? kb0 + kb_per : nkb;
       const int32_t grow = rt * XT + r;
-      const uint8_t *crow = codes + (int64_t)grow * ldc;
+      const int64_t crow_idx = grow < nrows ? (row_map ? (int64_t)row_map[grow] : (int64_t)grow) : 0;
+      const uint8_t *crow = codes + crow_idx * ldc;
       for (int32_t kb = kb0; kb < kb1; ++kb, ++it) {
         uint32_t s = it % XSTAGES, ph = (it / XSTAGES) & 1u;
         bool got = mbar_wait(&empty[s], ph ^ 1u, abort_flag, err, XERR_EMPTY);
@@ -443,49 +446,64 @@ static int grid_cap(const gp_ctx *ctx, int64_t work, int per_block, int mult)
 
 static size_t align256(size_t b) { return (b + 255) / 256 * 256; }
 
-int gp_geno_panel_tc(gp_ctx *ctx, int sum_over_snps, const int32_t *d_samp, int32_t nsamp,
-                     const int32_t *d_snprec, int32_t nk, int npanels, const gp_tc_panel *pp,
-                     int32_t ncols, double *d_Y, int64_t ldy)
+int gp_tc_code_bytes(int sum_over_snps, int32_t nsamp, int32_t nk, int64_t *ldc, int32_t *rows_pad)
+{
+  const int32_t nrows = sum_over_snps ? nsamp : nk;
+  const int32_t k0 = sum_over_snps ? nk : nsamp;
+  *rows_pad = (nrows + XT - 1) / XT * XT;
+  *ldc = (int64_t)((k0 + XK - 1) / XK) * XK / 4;
+  return GP_OK;
+}
+
+int gp_tc_build_codes(gp_ctx *ctx, int sum_over_snps, const int32_t *d_samp, int32_t nsamp,
+                      const int32_t *d_snprec, int32_t nk, uint8_t *codes, gp_tc_codes *out)
+{
+  int64_t ldc;
+  int32_t nrows_pad;
+  gp_tc_code_bytes(sum_over_snps, nsamp, nk, &ldc, &nrows_pad);
+  int64_t work = (int64_t)nrows_pad * (ldc / 16);
+  if (sum_over_snps)
+    k_codes_by_sample<<<grid_cap(ctx, work, 256, 32), 256, 0, ctx->stream>>>(
+        ctx->d_geno, ctx->rlen_dev, d_samp, nsamp, nrows_pad, d_snprec, nk, ldc, codes);
+  else
+    k_codes_by_snp<<<grid_cap(ctx, work, 256, 32), 256, 0, ctx->stream>>>(
+        ctx->d_geno, ctx->rlen_dev, d_samp, nsamp, d_snprec, nk, nrows_pad, ldc, codes);
+  GP_LAUNCH_CHECK(ctx, "k_codes");
+  out->codes = codes;
+  out->ldc = ldc;
+  out->row_map = NULL;
+  out->nrows = sum_over_snps ? nsamp : nk;
+  out->k0 = sum_over_snps ? nk : nsamp;
+  return GP_OK;
+}
+
+int gp_geno_panel_tc_codes(gp_ctx *ctx, const gp_tc_codes *A, int npanels, const gp_tc_panel *pp,
+                           int32_t ncols, double *d_Y, int64_t ldy)
 {
   if (npanels < 1 || npanels > 2 || ncols < 1 || ncols > 1024)
     return gp_fail(ctx, GP_ERR_ARG, "gp_geno_panel_tc: bad panel shape");
-  const int32_t nrows = sum_over_snps ? nsamp : nk;   /* output rows */
-  const int32_t k0 = sum_over_snps ? nk : nsamp;      /* one panel's k extent */
+  const int32_t nrows = A->nrows, k0 = A->k0;
   if (nrows < 1 || k0 < 1) return GP_OK;
-  const int32_t nrows_pad = (nrows + XT - 1) / XT * XT;
   const int32_t kb0 = (k0 + XK - 1) / XK;             /* k-blocks per panel */
   const int32_t kpad0 = kb0 * XK;
+  if (A->ldc < (int64_t)kpad0 / 4)
+    return gp_fail(ctx, GP_ERR_ARG, "gp_geno_panel_tc: code rows too short");
   const int32_t nkb = kb0 * npanels;
   const int32_t ncols4 = 4 * ncols, ncols4_pad = (ncols4 + XT - 1) / XT * XT;
-  const int64_t ldc = kpad0 / 4;                      /* code bytes per row */
   const int64_t ldb = (int64_t)kpad0 * npanels;       /* B row stride (elements) */
   const int64_t ldz = ncols4_pad;
-  size_t b_codes = align256((size_t)nrows_pad * ldc);
   size_t b_B = align256((size_t)ncols4_pad * ldb * 2);
   size_t b_Z = align256((size_t)nrows * ldz * 8);
   size_t b_e = align256((size_t)ncols * npanels * 4 + 4 * (size_t)ncols);
   uint8_t *base;
-  int rc = gp_scratch2(ctx, b_codes + b_B + b_Z + b_e + 256, (void **)&base);
+  int rc = gp_scratch2(ctx, b_B + b_Z + b_e + 256, (void **)&base);
   if (rc) return rc;
-  uint8_t *codes = base;
-  __half *B = (__half *)(base + b_codes);
-  double *Z = (double *)(base + b_codes + b_B);
-  int32_t *expo = (int32_t *)(base + b_codes + b_B + b_Z);
+  __half *B = (__half *)base;
+  double *Z = (double *)(base + b_B);
+  int32_t *expo = (int32_t *)(base + b_B + b_Z);
   int32_t *expo_p = expo + ncols; /* per-panel exponents, then the joint one */
   int *d_err = ctx->d_err;
   GP_CUDA(ctx, cudaMemsetAsync(d_err, 0, sizeof(int), ctx->stream));
-
-  /* codes */
-  {
-    int64_t work = (int64_t)nrows_pad * (ldc / 16);
-    if (sum_over_snps)
-      k_codes_by_sample<<<grid_cap(ctx, work, 256, 32), 256, 0, ctx->stream>>>(
-          ctx->d_geno, ctx->rlen_dev, d_samp, nsamp, nrows_pad, d_snprec, nk, ldc, codes);
-    else
-      k_codes_by_snp<<<grid_cap(ctx, work, 256, 32), 256, 0, ctx->stream>>>(
-          ctx->d_geno, ctx->rlen_dev, d_samp, nsamp, d_snprec, nk, nrows_pad, ldc, codes);
-    GP_LAUNCH_CHECK(ctx, "k_codes");
-  }
   /* joint column exponents over the panels, then the slices */
   for (int p = 0; p < npanels; ++p) {
     k_panel_exponent<<<ncols < 1024 ? ncols : 1024, 256, 0, ctx->stream>>>(
@@ -534,7 +552,7 @@ int gp_geno_panel_tc(gp_ctx *ctx, int sum_over_snps, const int32_t *d_samp, int3
   }
   GP_CUDA(ctx, cudaFuncSetAttribute(k_geno_panel_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     X_SMEM));
-  const int32_t nrt = nrows_pad / XT, nct = ncols4_pad / XT;
+  const int32_t nrt = (nrows + XT - 1) / XT, nct = ncols4_pad / XT;
   int32_t tiles = nrt * nct;
   int32_t ksplit = 1;
   while (tiles * ksplit < 2 * ctx->num_sms && ksplit * 4 <= nkb) ksplit *= 2;
@@ -544,9 +562,9 @@ int gp_geno_panel_tc(gp_ctx *ctx, int sum_over_snps, const int32_t *d_samp, int3
   int grid = nitems < ctx->num_sms ? nitems : ctx->num_sms;
   uint64_t lut_lo = pp[0].count ? LUT_COUNT : LUT_MASK;
   uint64_t lut_hi = npanels > 1 ? (pp[1].count ? LUT_COUNT : LUT_MASK) : lut_lo;
-  k_geno_panel_tc<<<grid, X_THREADS, X_SMEM, ctx->stream>>>(tmb, codes, ldc, nrows, ncols4, nkb,
-                                                           kb0, kb0, lut_lo, lut_hi, ksplit, Z, ldz,
-                                                           d_err);
+  k_geno_panel_tc<<<grid, X_THREADS, X_SMEM, ctx->stream>>>(tmb, A->codes, A->ldc, A->row_map,
+                                                           nrows, ncols4, nkb, kb0, kb0, lut_lo,
+                                                           lut_hi, ksplit, Z, ldz, d_err);
   GP_LAUNCH_CHECK(ctx, "k_geno_panel_tc");
   {
     int64_t work = (int64_t)nrows * ncols;
@@ -559,4 +577,21 @@ int gp_geno_panel_tc(gp_ctx *ctx, int sum_over_snps, const int32_t *d_samp, int3
   GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   if (herr) return gp_fail(ctx, GP_ERR_TIMEOUT, "tensor-core product wait timed out (code %d)", herr);
   return GP_OK;
+}
+
+int gp_geno_panel_tc(gp_ctx *ctx, int sum_over_snps, const int32_t *d_samp, int32_t nsamp,
+                     const int32_t *d_snprec, int32_t nk, int npanels, const gp_tc_panel *pp,
+                     int32_t ncols, double *d_Y, int64_t ldy)
+{
+  int64_t ldc;
+  int32_t rows_pad;
+  gp_tc_code_bytes(sum_over_snps, nsamp, nk, &ldc, &rows_pad);
+  if ((sum_over_snps ? nsamp : nk) < 1 || (sum_over_snps ? nk : nsamp) < 1) return GP_OK;
+  uint8_t *codes;
+  int rc = gp_scratch4(ctx, (size_t)rows_pad * ldc + 256, (void **)&codes);
+  if (rc) return rc;
+  gp_tc_codes A;
+  rc = gp_tc_build_codes(ctx, sum_over_snps, d_samp, nsamp, d_snprec, nk, codes, &A);
+  if (rc) return rc;
+  return gp_geno_panel_tc_codes(ctx, &A, npanels, pp, ncols, d_Y, ldy);
 }

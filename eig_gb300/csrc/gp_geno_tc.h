@@ -14,6 +14,24 @@ struct gp_tc_panel {
   int count;
 };
 
+/* A genotype code operand: rows of ldc bytes of 2-bit codes (MSB first, 3 -> 0); output
+ * row r reads code row row_map[r] (or r); k0 = the k extent of one panel. */
+struct gp_tc_codes {
+  const uint8_t *codes;
+  int64_t ldc;
+  const int32_t *row_map;
+  int32_t nrows;
+  int32_t k0;
+};
+
+/* bytes of the code operand built by gp_tc_build_codes: rows_pad * ldc */
+int gp_tc_code_bytes(int sum_over_snps, int32_t nsamp, int32_t nk, int64_t *ldc, int32_t *rows_pad);
+int gp_tc_build_codes(gp_ctx *ctx, int sum_over_snps, const int32_t *d_samp, int32_t nsamp,
+                      const int32_t *d_snprec, int32_t nk, uint8_t *codes, gp_tc_codes *out);
+/* Y[r][c] = sum_p sum_k A(r, k) sign_p P_p[k][c] with a prepared code operand */
+int gp_geno_panel_tc_codes(gp_ctx *ctx, const gp_tc_codes *A, int npanels, const gp_tc_panel *pp,
+                           int32_t ncols, double *d_Y, int64_t ldy);
+
 /*
  * sum_over_snps = 1: Y[q][c] = sum_p sum_{s < nk} A_p(samp[q], snprec[s]) sign_p P_p[s][c]
  * sum_over_snps = 0: Y[s][c] = sum_p sum_{q < nsamp} A_p(samp[q], snprec[s]) sign_p P_p[q][c]

@@ -3,6 +3,7 @@
 #define GP_INTERNAL_H
 
 #include <cuda_runtime.h>
+#include <cublas_v2.h>
 #include <cusolverDn.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -18,6 +19,7 @@ struct gp_ctx {
   int num_sms;
   cudaStream_t stream;
   cusolverDnHandle_t solver;
+  cublasHandle_t blas;  /* created on first use (fastmode) */
   char err[GP_ERRLEN];
 
   /* genotype panel: nsnp_all records of rlen_dev bytes (packed 2-bit, MSB first) */
@@ -75,6 +77,8 @@ struct gp_ctx {
   size_t scratch2_cap;
   void *d_scratch3;    /* small panels built between the products of gp_geno_tc */
   size_t scratch3_cap;
+  void *d_scratch4;    /* genotype code operands of gp_geno_tc */
+  size_t scratch4_cap;
   int *d_err;          /* error word written by the tensor-core kernels' bounded waits */
   int precision;       /* precision of the last gp_xtx: split precisions use the tensor-core
                           exact products for weights and lsqproject */
@@ -88,6 +92,7 @@ int gp_cuda_fail(gp_ctx *ctx, cudaError_t e, const char *what);
 int gp_scratch(gp_ctx *ctx, size_t bytes, void **out);
 int gp_scratch2(gp_ctx *ctx, size_t bytes, void **out);
 int gp_scratch_aux(gp_ctx *ctx, size_t bytes, void **out);
+int gp_scratch4(gp_ctx *ctx, size_t bytes, void **out);
 int gp_realloc(gp_ctx *ctx, void **ptr, size_t bytes);
 
 #define GP_CUDA(ctx, call)                                   \

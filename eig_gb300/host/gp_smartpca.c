@@ -198,7 +198,8 @@ int gp_smartpca_run(gp_ctx *ctx, const gp_smartpca_opts *o, const gp_panel *p,
     evals = (double *)calloc((size_t)K, sizeof(double));
     evecs = (double *)calloc((size_t)K * nrows, sizeof(double));
     if (!evals || !evecs) FAIL(GP_ERR_NOMEM);
-    rc = gp_fastpca(ctx, K, L, I, (uint64_t)o->seed, NULL, o->precision, evals, evecs);
+    gp_xtx_opts fo = {o->fancynorm, o->altnormstyle, 0, 0x7fffffff, o->precision};
+    rc = gp_fastpca(ctx, K, L, I, (uint64_t)o->seed, NULL, &fo, evals, evecs);
     if (rc) goto done;
     r->t_phase[GP_PH_GRAM] = now_s() - t;
     r->nrows = nrows;

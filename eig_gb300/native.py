@@ -103,7 +103,7 @@ def load_library():
         "gp_snp_weights": (C.c_int, [vp, C.c_int32, f64p, f64p, f64p]),
         "gp_lsqproj": (C.c_int, [vp, C.c_int32, i32p, C.c_int32, f64p, f64p, i32p, i32p]),
         "gp_fastpca": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, f64p,
-                                 C.c_int32, f64p, f64p]),
+                                 C.POINTER(XtxOpts), f64p, f64p]),
         "gp_smartpca_defaults": (None, [C.POINTER(SmartpcaOpts)]),
         "gp_genotype_shape": (C.c_int, [vp, i64p, i32p]),
         "gp_timer_start": (C.c_int, [vp]),
@@ -298,12 +298,14 @@ class Handle:
                    "gp_last_gram_time")
         return ms.value, n.value, fl.value
 
-    def fastpca(self, K, L, I, seed=0, omega=None, precision=GP_PREC_FP64):
+    def fastpca(self, K, L, I, seed=0, omega=None, precision=GP_PREC_FP64, fancynorm=1,
+                altnormstyle=1):
         n = self.nrows
         ev = np.zeros(K)
         V = np.zeros((K, n))
         om = None if omega is None else np.ascontiguousarray(omega, dtype=np.float64)
-        self.check(self.lib.gp_fastpca(self.h, K, L, I, seed, ptr(om, C.c_double), precision,
+        o = XtxOpts(fancynorm, altnormstyle, 0, 0x7fffffff, precision)
+        self.check(self.lib.gp_fastpca(self.h, K, L, I, seed, ptr(om, C.c_double), C.byref(o),
                                        ptr(ev, C.c_double), ptr(V, C.c_double)), "gp_fastpca")
         return ev, V
 

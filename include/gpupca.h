@@ -170,15 +170,17 @@ int gp_lsqproj(gp_ctx *ctx, int32_t numeigs, const int32_t *samples, int32_t npr
 
 /*
  * fastmode randomized block-Krylov PCA (kjg_fpca src/ksrc/kjg_fpca.c:24-102 with the data
- * table of setgval src/gval.c:31-87): X (ncols x nrows) holds ((g - mean) fancy)/sqrt(2),
- * missing 0; Omega (nrows x L) Gaussian from `seed` (or the caller's omega, row-major,
- * when not NULL); I power steps G <- X^T X G / M; Q = [X G_0 .. X G_I]; Q <- orthonormal
- * basis; B = X^T Q; SVD(B).  evals [K] = S^2/M, evecs [K*nrows] (vector j at [j*nrows]).
- * precision selects FP64 or split-BF16 products; orthogonalisation and Rayleigh-Ritz are
- * FP64.
+ * table of setgval src/gval.c:31-87) over the current rows and columns: X (ncols x nrows)
+ * holds ((g - mean) fancy)/sqrt(2), missing 0 (opts: fancynorm, altnormstyle and precision
+ * are used; no allele-count kill rule applies, as in the reference); Omega (nrows x L)
+ * Gaussian from `seed` (or the caller's omega, row-major, when not NULL); I power steps
+ * G <- X^T X G / M; Q = [X G_0 .. X G_I] (needs (I+1) L <= 1024); Q <- orthonormal basis;
+ * B = X^T Q; SVD(B).  evals [K] = S^2/M, evecs [K*nrows] (vector j at [j*nrows], unit norm,
+ * arbitrary sign).  The products with X are the exact tensor-core products for split
+ * precisions (FP64 SIMT for GP_PREC_FP64); orthogonalisation and Rayleigh-Ritz are FP64.
  */
 int gp_fastpca(gp_ctx *ctx, int32_t K, int32_t L, int32_t I, uint64_t seed,
-               const double *omega, int32_t precision, double *evals, double *evecs);
+               const double *omega, const gp_xtx_opts *opts, double *evals, double *evecs);
 
 
 /* ---- measurement helpers (no counterpart in the reference) ---------------------------- */

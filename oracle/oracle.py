@@ -259,3 +259,26 @@ def smartpca(records, nind, numeigs=10, numoutliter=5, numoutleigs=10, outlthres
         out = ~ind_ign
     return dict(evals=evals, evecs=evecs[:K], xindex=xindex, coords=coords, ind_out=out,
                 outliers=outliers, ncols=len(cols), nrows=n, numeigs=K, snp_state=snp_ign)
+
+
+def fastpca(records, cols, xindex, K, L, I, omega, fancynorm=1, altnormstyle=1):
+    """kjg_fpca (src/ksrc/kjg_fpca.c:24-102) on the setgval table (src/gval.c:31-87), in numpy
+    FP64 with the caller's Omega (nrows x L): returns evals [K] = S^2/M and evecs [K][nrows]."""
+    rec = np.ascontiguousarray(records, dtype=np.uint8)
+    s = pass_columns(rec, cols, xindex, fancynorm, altnormstyle, 0, 2 ** 31 - 1)
+    g = unpack(rec[np.asarray(cols)], rec.shape[1] * 4)[:, np.asarray(xindex)]
+    code = np.where(g < 0, 3, g)
+    tab = s.tab.reshape(-1, 4)
+    X = np.take_along_axis(tab, code, axis=1) / np.sqrt(2.0)  # m x n
+    m = X.shape[0]
+    G = np.asarray(omega, dtype=np.float64)
+    blocks = []
+    for _ in range(I):
+        Qi = X @ G
+        blocks.append(Qi)
+        G = X.T @ Qi / m
+    blocks.append(X @ G)
+    U, _, _ = np.linalg.svd(np.hstack(blocks), full_matrices=False)
+    B = X.T @ U
+    Ub, Sb, _ = np.linalg.svd(B, full_matrices=False)
+    return Sb[:K] ** 2 / m, np.ascontiguousarray(Ub[:, :K].T)

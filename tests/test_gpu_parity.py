@@ -331,3 +331,42 @@ def test_eig_tridiag_all_values_top_vectors(gpu):
     sep = np.concatenate([[w[0] - w[1]], gaps])[:24] > 1e-3 * w[0]
     cos = np.abs(np.sum(V * U[:24], axis=1))
     assert np.all(cos[sep] > 1 - 1e-9)
+
+
+@pytest.mark.parametrize("prec", [native.GP_PREC_FP64, native.GP_PREC_SPLIT_FP16])
+def test_fastpca_vs_oracle(gpu, prec):
+    """fastmode with the same Omega as the numpy restatement of kjg_fpca: eigenvalues within
+    1e-9 relative, eigenvectors equal up to sign (|cos| > 1 - 1e-8) for the separated ones;
+    row subset (every other sample) and all-sample paths"""
+    rec, pop = synth(5000, [120, 120, 80], [0.01, 0.03, 0.05], miss=0.02, seed=28, n_admixed=20)
+    nind = len(pop)
+    cols = np.arange(5000, dtype=np.int32)
+    K, L, I = 4, 8, 4
+    for rows in (np.arange(nind, dtype=np.int32), np.arange(0, nind, 2, dtype=np.int32)):
+        gpu.load_genotypes(rec, nind)
+        gpu.set_samples(rows)
+        gpu.set_snps(cols)
+        om = np.random.default_rng(5).standard_normal((len(rows), L))
+        ev, V = gpu.fastpca(K, L, I, omega=om, precision=prec)
+        oev, oV = O.fastpca(rec, cols, rows, K, L, I, om)
+        assert np.max(np.abs(ev - oev) / oev) <= 1e-9
+        cos = np.abs(np.sum(V * oV, axis=1))
+        sep = np.r_[oev[:-1] / oev[1:] > 1.01, True][:K]
+        assert np.all(cos[sep] > 1 - 1e-8), cos
+        assert np.allclose(np.linalg.norm(V, axis=1), 1.0)
+
+
+def test_fastpca_top_eigenvalues_match_exact(gpu):
+    """fastmode's top eigenvalues against the exact FP64 eigenvalues of X^T X / M (the
+    randomized method converges on the separated population-structure eigenvalues)"""
+    rec, pop = synth(8000, [150, 150, 100], [0.02, 0.04, 0.08], miss=0.01, seed=29)
+    nind = len(pop)
+    rows = np.arange(nind, dtype=np.int32)
+    cols = np.arange(8000, dtype=np.int32)
+    gpu.load_genotypes(rec, nind)
+    gpu.set_samples(rows)
+    gpu.set_snps(cols)
+    ev, V = gpu.fastpca(2, 8, 4, seed=3, precision=native.GP_PREC_SPLIT_FP16)
+    s = O.pass_columns(rec, cols, rows, minallelecnt=0, maxmissing=2 ** 31 - 1)
+    w = np.linalg.eigvalsh(O.gram(s))[::-1] / (2.0 * 8000)
+    assert np.max(np.abs(ev - w[:2]) / w[:2]) <= 1e-6

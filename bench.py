@@ -132,6 +132,148 @@ def max_over_ranks(dist, x):
     return float(t.item())
 
 
+def _subspace_angle_deg(A, B):
+    """largest principal angle between the row spaces of A and B (k x n)"""
+    qa, _ = np.linalg.qr(A.T)
+    qb, _ = np.linalg.qr(B.T)
+    sv = np.linalg.svd(qa.T @ qb, compute_uv=False)
+    return float(np.degrees(np.arccos(np.clip(sv.min(), -1.0, 1.0))))
+
+
+def accuracy_vs_fp64(h, resident, nind, cfg, r_split, step_ms):
+    """one plain FP64 GPU run of the same workload: wall time, eigenvalue error, subspace
+    angle and outlier decisions of the split run against it"""
+    from eig_gb300 import native
+    opts = native.default_opts(numeigs=cfg["K"], numoutliter=5, outlthresh=6.0,
+                               precision=native.GP_PREC_FP64)
+    h.timer_start()
+    r64 = native.smartpca_run(h, resident, nind, opts)
+    ms = h.timer_stop()
+    K = cfg["K"]
+    e64, e16 = r64["evals"][:K], r_split["evals"][:K]
+    same_rows = np.array_equal(r64["xindex"], r_split["xindex"])
+    out = {"fp64_pca_wall_s": ms / 1e3, "split_speedup": ms / step_ms,
+           "eval_max_rel_err": float(np.max(np.abs(e16 - e64) / np.abs(e64))),
+           "outliers_identical": [o[:3] for o in r64["outliers"]] ==
+                                 [o[:3] for o in r_split["outliers"]],
+           "kept_samples_identical": bool(same_rows)}
+    if same_rows:
+        out["subspace_angle_deg"] = _subspace_angle_deg(r64["evecs"][:K], r_split["evecs"][:K])
+    return out
+
+
+def _serve_load(srv, rows, sizes, offsets, arrivals):
+    """submit request i at arrivals[i] seconds; returns per-request latency (ms, from the
+    scheduled arrival to completion), the span (s) and the completed requests"""
+    n = len(sizes)
+    done_t = [0.0] * n
+    reqs = [None] * n
+    ready = threading.Semaphore(0)
+    errors = []
+
+    def waiter():
+        for i in range(n):
+            ready.acquire()
+            try:
+                reqs[i].wait(300.0)
+            except Exception as e:  # noqa: BLE001 - reported after the run
+                errors.append(str(e))
+            done_t[i] = time.perf_counter()
+
+    th = threading.Thread(target=waiter)
+    th.start()
+    t0 = time.perf_counter()
+    for i in range(n):
+        while True:
+            dt = t0 + arrivals[i] - time.perf_counter()
+            if dt <= 0:
+                break
+            time.sleep(min(dt, 0.001))
+        reqs[i] = srv.submit(rows[offsets[i]:offsets[i] + sizes[i]])
+        ready.release()
+    th.join()
+    if errors:
+        raise RuntimeError("serving request failed: %s" % errors[0])
+    lat = np.array([(done_t[i] - (t0 + arrivals[i])) * 1e3 for i in range(n)])
+    return lat, max(done_t) - t0, reqs
+
+
+def run_serving(h, cfg, nreq=400, seed=11):
+    """Projection serving on the panel left resident by the PCA run: capacity, Poisson
+    arrivals at 50% and 80% of it, the FP64 one-request-at-a-time baseline, and the
+    coordinate error of the tensor-core path against the FP64 one."""
+    from eig_gb300 import native
+    K = cfg["K"]
+    srv = native.Server(h, K, max_batch=4096, pool_samples=32768)
+    npool = 4096
+    npops = len(cfg["pops"])
+    per = (3 * npool // 4) // npops
+    t = time.time()
+    rows, _ = native.synth_sample_rows(cfg["nsnp"], [per] * npops, cfg["fst"], srv.snp_index,
+                                       srv.row_bytes, sample_seed=cfg["seed"] + 1000, miss=0.0,
+                                       miss_hi=0.95, n_admixed=npool - per * npops,
+                                       seed=cfg["seed"])
+    gen_s = time.time() - t
+    native.host_register(rows)
+    rng = np.random.default_rng(seed)
+
+    def draw(n):
+        sz = rng.integers(1, 2001, size=n)
+        off = np.array([rng.integers(0, npool - z + 1) for z in sz])
+        return sz, off
+
+    # warm-up and capacity: every request offered at t = 0
+    sz, off = draw(20)
+    _serve_load(srv, rows, sz, off, np.zeros(len(sz)))
+    sz, off = draw(nreq)
+    b0, s0, q0 = srv.stats()
+    lat, span, reqs = _serve_load(srv, rows, sz, off, np.zeros(nreq))
+    b1, s1, q1 = srv.stats()
+    cap_sps = float(sz.sum()) / span
+    cap_rps = nreq / span
+    out = {"panel": "K=%d over %d kept SNPs (%d bytes per sample row)" % (K, srv.nsnp,
+                                                                           srv.row_bytes),
+           "requests": "1-2000 new samples each (3/4 from the %d panel populations, 1/4 "
+                       "two-way admixed), per-sample missing ~U(0,0.95), rows in pinned host "
+                       "memory, H2D inside the latency" % npops,
+           "capacity": {"samples_per_s": cap_sps, "req_per_s": cap_rps, "n": nreq,
+                        "batches": b1 - b0, "packed_gbs": cap_sps * srv.row_bytes / 1e9},
+           "poisson": [], "request_gen_s": gen_s}
+    for frac in (0.5, 0.8):
+        rate = frac * cap_rps
+        sz, off = draw(nreq)
+        arr = np.cumsum(rng.exponential(1.0 / rate, size=nreq))
+        lat, span, reqs = _serve_load(srv, rows, sz, off, arr)
+        out["poisson"].append({"offered_req_per_s": rate, "load": frac, "n": nreq,
+                               "samples_per_s": float(sz.sum()) / span,
+                               "p50_ms": float(np.percentile(lat, 50)),
+                               "p99_ms": float(np.percentile(lat, 99))})
+    # coordinates of a few requests on the tensor-core server, kept for the comparison
+    sz_c, off_c = draw(4)
+    _, _, creqs = _serve_load(srv, rows, sz_c, off_c, np.zeros(4))
+    srv.close()
+    # FP64 baseline: one request at a time, FP64 SIMT products
+    s64 = native.Server(h, K, max_batch=2048, pool_samples=4096, fp64_serial=True)
+    lat64, span64, r64 = _serve_load(s64, rows, sz_c, off_c, np.zeros(4))
+    s64.close()
+    err_abs, err_rel = 0.0, 0.0
+    for a, b in zip(creqs, r64):
+        ok = (a.status == 0) & (b.status == 0)
+        assert np.array_equal(a.status, b.status)
+        d = np.abs(a.coords[ok] - b.coords[ok])
+        if d.size:
+            err_abs = max(err_abs, float(d.max()))
+            err_rel = max(err_rel, float(d.max() / np.abs(b.coords[ok]).max()))
+    sps64 = float(sz_c.sum()) / span64
+    out["fp64_serial"] = {"samples_per_s": sps64, "n": 4, "samples": int(sz_c.sum()),
+                          "ms_per_request": span64 / 4 * 1e3}
+    out["speedup_vs_fp64_serial"] = cap_sps / sps64
+    out["coord_max_abs_err_vs_fp64"] = err_abs
+    out["coord_max_rel_err_vs_fp64"] = err_rel
+    native.host_unregister(rows)
+    return out
+
+
 def run_gpu(args, cfg, world, rank, local, dist):
     import torch
 
@@ -202,12 +344,21 @@ def run_gpu(args, cfg, world, rank, local, dist):
     n_e2e = len(e2e_times)
     native.host_unregister(rec)
     e2e_ms = max_over_ranks(dist, float(np.mean(e2e_times)))
+    # the split run's results and timing against one plain FP64 GPU run
+    acc = None
+    if not args.no_fp64_check and args.precision != "fp64":
+        r_split = native.smartpca_run(h, resident, nind, opts)
+        acc = accuracy_vs_fp64(h, resident, nind, cfg, r_split, step_ms)
+    serving = None
+    if not args.no_serving:
+        r_split = native.smartpca_run(h, resident, nind, opts)  # leaves the K=20 panel resident
+        serving = run_serving(h, cfg)
     h.close()
     peaks, peak_kind = load_peaks()
     res = dict(step_ms=step_ms, gram_flops=total_flops, gram_ms=g_ms, gram_launches=g_launch,
                gram_kernel_flops=g_flops, clocks=clk, e2e_ms=e2e_ms, h2d=h2d / n_e2e,
                d2h=d2h / n_e2e, run=r, gen_s=gen_s, peaks=peaks, peak_kind=peak_kind,
-               nind=nind, launches=launches)
+               nind=nind, launches=launches, acc=acc, serving=serving)
     return res
 
 
@@ -252,6 +403,8 @@ def main():
     ap.add_argument("--precision", default="fp16", choices=["fp64", "bf16", "bf16x4", "fp16"])
     ap.add_argument("--config", default="full", choices=list(CONFIGS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64-check", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
     args = ap.parse_args()
     cfg = CONFIGS[args.config]
     world, rank, local, dist = dist_setup()
@@ -313,6 +466,7 @@ def main():
             "roofline": roof, "clocks": res["clocks"],
             "e2e": {"value": e2e, "unit": "TFLOP/s", "h2d_bytes_per_step": int(res["h2d"]),
                     "d2h_bytes_per_step": int(res["d2h"]), "wall_s": res["e2e_ms"] / 1e3},
+            "accuracy_vs_fp64": res["acc"], "serving": res["serving"],
             "gpu_launches": res["launches"],
             "gpu_launches_note": "own kernels per timed step (cuSOLVER eigensolver launches not counted)"}
     if rank == 0 and not args.no_cpu_baseline:

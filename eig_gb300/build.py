@@ -27,7 +27,7 @@ NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
                      "-I" + os.path.join(ROOT, "include")]
 CUDA_SOURCES = ["gp_api.cu", "gp_geno.cu", "gp_gram_f64.cu", "gp_geno_gemm_f64.cu",
                 "gp_gram_bf16.cu", "gp_fast.cu",
-                "gp_noalloc.cu", "gp_geno_tc.cu", "gp_eig.cu"]
+                "gp_noalloc.cu", "gp_geno_tc.cu", "gp_eig.cu", "gp_serve.cu"]
 HOST_LIB_SOURCES = ["gp_smartpca.c"]
 CFLAGS = ["-O2", "-fPIC", "-std=gnu11", "-Wall", "-Wno-unused-result",
           "-I" + os.path.join(ROOT, "include")]
@@ -83,7 +83,7 @@ def build(verbose=False, force=False):
     lib = os.path.join(LIB, "libgpupca.so")
     if force or _newer(lib, objs):
         _run([nvcc] + ARCH + ["-shared", "-o", lib] + objs +
-             ["-lcusolver", "-lcublas", "-lcudart"])
+             ["-lcusolver", "-lcublas", "-lcudart", "-lpthread"])
     synth = os.path.join(LIB, "libgpsynth.so")
     ss = os.path.join(HOST, "gp_synth.c")
     if force or _newer(synth, [ss] + hdrs):

@@ -94,6 +94,13 @@ int gp_scratch4(gp_ctx *ctx, size_t bytes, void **out)
   return rc;
 }
 
+int gp_scratch5(gp_ctx *ctx, size_t bytes, void **out)
+{
+  int rc = grow(ctx, &ctx->d_scratch5, &ctx->scratch5_cap, bytes);
+  *out = ctx->d_scratch5;
+  return rc;
+}
+
 int gp_scratch2(gp_ctx *ctx, size_t bytes, void **out)
 {
   int rc = grow(ctx, &ctx->d_scratch2, &ctx->scratch2_cap, bytes);
@@ -163,7 +170,8 @@ extern "C" void gp_close(gp_ctx *ctx)
   void *bufs[] = {ctx->d_geno,   ctx->d_rows,    ctx->d_rowmask, ctx->d_cols,    ctx->d_cnt,
                   ctx->d_killed, ctx->d_vtab,    ctx->d_xmean,   ctx->d_xfancy,  ctx->d_kept,
                   ctx->d_xtx,    ctx->d_evals,   ctx->d_evecs,   ctx->d_ffvecs,  ctx->d_fxscal,
-                  ctx->d_scratch, ctx->d_scratch2, ctx->d_scratch3, ctx->d_scratch4, ctx->d_err};
+                  ctx->d_scratch, ctx->d_scratch2, ctx->d_scratch3, ctx->d_scratch4, ctx->d_scratch5,
+                  ctx->d_err};
   for (size_t i = 0; i < sizeof(bufs) / sizeof(bufs[0]); ++i)
     if (bufs[i]) cudaFree(bufs[i]);
   if (ctx->solver) cusolverDnDestroy(ctx->solver);
@@ -181,7 +189,7 @@ extern "C" int gp_device_bytes(const gp_ctx *ctx, int64_t *bytes)
   if (!ctx || !bytes) return GP_ERR_ARG;
   int64_t b = (int64_t)ctx->rlen_dev * ctx->nsnp_all + (int64_t)ctx->scratch_cap +
               (int64_t)ctx->scratch2_cap + (int64_t)ctx->scratch3_cap +
-              (int64_t)ctx->scratch4_cap +
+              (int64_t)ctx->scratch4_cap + (int64_t)ctx->scratch5_cap +
               (int64_t)sizeof(double) * ctx->xtx_cap;
   *bytes = b;
   return GP_OK;

@@ -477,34 +477,26 @@ int gp_tc_build_codes(gp_ctx *ctx, int sum_over_snps, const int32_t *d_samp, int
   return GP_OK;
 }
 
-int gp_geno_panel_tc_codes(gp_ctx *ctx, const gp_tc_codes *A, int npanels, const gp_tc_panel *pp,
-                           int32_t ncols, double *d_Y, int64_t ldy)
+size_t gp_tc_prepared_bytes(int npanels, int32_t ncols, int32_t k0)
 {
-  if (npanels < 1 || npanels > 2 || ncols < 1 || ncols > 1024)
-    return gp_fail(ctx, GP_ERR_ARG, "gp_geno_panel_tc: bad panel shape");
-  const int32_t nrows = A->nrows, k0 = A->k0;
-  if (nrows < 1 || k0 < 1) return GP_OK;
-  const int32_t kb0 = (k0 + XK - 1) / XK;             /* k-blocks per panel */
-  const int32_t kpad0 = kb0 * XK;
-  if (A->ldc < (int64_t)kpad0 / 4)
-    return gp_fail(ctx, GP_ERR_ARG, "gp_geno_panel_tc: code rows too short");
-  const int32_t nkb = kb0 * npanels;
+  const int32_t kpad0 = (k0 + XK - 1) / XK * XK;
+  const int32_t ncols4_pad = (4 * ncols + XT - 1) / XT * XT;
+  return align256((size_t)ncols4_pad * kpad0 * npanels * 2) +
+         align256((size_t)ncols * npanels * 4 + 4 * (size_t)ncols) + 256;
+}
+
+int gp_tc_prepare(gp_ctx *ctx, int npanels, const gp_tc_panel *pp, int32_t ncols, int32_t k0,
+                  void *storage, gp_tc_prepared *out)
+{
+  if (npanels < 1 || npanels > 2 || ncols < 1 || ncols > 1024 || k0 < 1)
+    return gp_fail(ctx, GP_ERR_ARG, "gp_tc_prepare: bad panel shape");
+  const int32_t kb0 = (k0 + XK - 1) / XK, kpad0 = kb0 * XK;
   const int32_t ncols4 = 4 * ncols, ncols4_pad = (ncols4 + XT - 1) / XT * XT;
-  const int64_t ldb = (int64_t)kpad0 * npanels;       /* B row stride (elements) */
-  const int64_t ldz = ncols4_pad;
-  size_t b_B = align256((size_t)ncols4_pad * ldb * 2);
-  size_t b_Z = align256((size_t)nrows * ldz * 8);
-  size_t b_e = align256((size_t)ncols * npanels * 4 + 4 * (size_t)ncols);
-  uint8_t *base;
-  int rc = gp_scratch2(ctx, b_B + b_Z + b_e + 256, (void **)&base);
-  if (rc) return rc;
+  const int64_t ldb = (int64_t)kpad0 * npanels;
+  uint8_t *base = (uint8_t *)storage;
   __half *B = (__half *)base;
-  double *Z = (double *)(base + b_B);
-  int32_t *expo = (int32_t *)(base + b_B + b_Z);
+  int32_t *expo = (int32_t *)(base + align256((size_t)ncols4_pad * ldb * 2));
   int32_t *expo_p = expo + ncols; /* per-panel exponents, then the joint one */
-  int *d_err = ctx->d_err;
-  GP_CUDA(ctx, cudaMemsetAsync(d_err, 0, sizeof(int), ctx->stream));
-  /* joint column exponents over the panels, then the slices */
   for (int p = 0; p < npanels; ++p) {
     k_panel_exponent<<<ncols < 1024 ? ncols : 1024, 256, 0, ctx->stream>>>(
         pp[p].P, pp[p].ldp, k0, ncols, expo_p + p * ncols);
@@ -534,25 +526,50 @@ int gp_geno_panel_tc_codes(gp_ctx *ctx, const gp_tc_codes *A, int npanels, const
         pp[p].P, pp[p].ldp, k0, ncols, expo, pp[p].sign, (int64_t)p * kpad0, B, ldb);
     GP_LAUNCH_CHECK(ctx, "k_panel_slices");
   }
-  GP_CUDA(ctx, cudaMemsetAsync(Z, 0, (size_t)nrows * ldz * 8, ctx->stream));
-
-  /* the tensor-core kernel */
   PFN_cuTensorMapEncodeTiled_v12000 enc = tc_encode(ctx);
   if (!enc) return GP_ERR_CUDA;
-  CUtensorMap tmb;
   {
     cuuint64_t dims[2] = {(cuuint64_t)ldb, (cuuint64_t)ncols4_pad};
     cuuint64_t strides[1] = {(cuuint64_t)ldb * 2};
     cuuint32_t box[2] = {XK, XT};
     cuuint32_t estr[2] = {1, 1};
-    CUresult r = enc(&tmb, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, B, dims, strides, box, estr,
+    CUresult r = enc(&out->tmb, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, B, dims, strides, box, estr,
                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return gp_fail(ctx, GP_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
   }
+  out->B = B;
+  out->expo = expo;
+  out->ncols = ncols;
+  out->ncols4 = ncols4;
+  out->ncols4_pad = ncols4_pad;
+  out->npanels = npanels;
+  out->kb0 = kb0;
+  out->k0 = k0;
+  out->ldb = ldb;
+  out->lut_lo = pp[0].count ? LUT_COUNT : LUT_MASK;
+  out->lut_hi = npanels > 1 ? (pp[1].count ? LUT_COUNT : LUT_MASK) : out->lut_lo;
+  return GP_OK;
+}
+
+int gp_tc_apply(gp_ctx *ctx, const gp_tc_codes *A, const gp_tc_prepared *P, double *d_Y,
+                int64_t ldy, int sync)
+{
+  const int32_t nrows = A->nrows;
+  if (nrows < 1) return GP_OK;
+  if (A->k0 != P->k0 || A->ldc < (int64_t)P->kb0 * XK / 4)
+    return gp_fail(ctx, GP_ERR_ARG, "gp_tc_apply: code operand and panel disagree");
+  const int64_t ldz = P->ncols4_pad;
+  double *Z;
+  int rc = gp_scratch5(ctx, (size_t)nrows * ldz * 8 + 256, (void **)&Z);
+  if (rc) return rc;
+  int *d_err = ctx->d_err;
+  if (sync) GP_CUDA(ctx, cudaMemsetAsync(d_err, 0, sizeof(int), ctx->stream));
+  GP_CUDA(ctx, cudaMemsetAsync(Z, 0, (size_t)nrows * ldz * 8, ctx->stream));
   GP_CUDA(ctx, cudaFuncSetAttribute(k_geno_panel_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     X_SMEM));
-  const int32_t nrt = (nrows + XT - 1) / XT, nct = ncols4_pad / XT;
+  const int32_t nkb = P->kb0 * P->npanels;
+  const int32_t nrt = (nrows + XT - 1) / XT, nct = P->ncols4_pad / XT;
   int32_t tiles = nrt * nct;
   int32_t ksplit = 1;
   while (tiles * ksplit < 2 * ctx->num_sms && ksplit * 4 <= nkb) ksplit *= 2;
@@ -560,23 +577,36 @@ int gp_geno_panel_tc_codes(gp_ctx *ctx, const gp_tc_codes *A, int npanels, const
   while ((int64_t)((nkb + ksplit - 1) / ksplit) * XK > (1 << 19)) ksplit *= 2;
   int32_t nitems = tiles * ksplit;
   int grid = nitems < ctx->num_sms ? nitems : ctx->num_sms;
-  uint64_t lut_lo = pp[0].count ? LUT_COUNT : LUT_MASK;
-  uint64_t lut_hi = npanels > 1 ? (pp[1].count ? LUT_COUNT : LUT_MASK) : lut_lo;
-  k_geno_panel_tc<<<grid, X_THREADS, X_SMEM, ctx->stream>>>(tmb, A->codes, A->ldc, A->row_map,
-                                                           nrows, ncols4, nkb, kb0, kb0, lut_lo,
-                                                           lut_hi, ksplit, Z, ldz, d_err);
+  k_geno_panel_tc<<<grid, X_THREADS, X_SMEM, ctx->stream>>>(P->tmb, A->codes, A->ldc, A->row_map,
+                                                           nrows, P->ncols4, nkb, P->kb0, P->kb0,
+                                                           P->lut_lo, P->lut_hi, ksplit, Z, ldz,
+                                                           d_err);
   GP_LAUNCH_CHECK(ctx, "k_geno_panel_tc");
   {
-    int64_t work = (int64_t)nrows * ncols;
-    k_panel_combine<<<grid_cap(ctx, work, 256, 32), 256, 0, ctx->stream>>>(Z, ldz, nrows, ncols,
-                                                                            expo, d_Y, ldy);
+    int64_t work = (int64_t)nrows * P->ncols;
+    k_panel_combine<<<grid_cap(ctx, work, 256, 32), 256, 0, ctx->stream>>>(Z, ldz, nrows, P->ncols,
+                                                                            P->expo, d_Y, ldy);
     GP_LAUNCH_CHECK(ctx, "k_panel_combine");
   }
+  if (!sync) return GP_OK;
   int herr = 0;
   GP_CUDA(ctx, gp_memcpy(ctx, &herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   if (herr) return gp_fail(ctx, GP_ERR_TIMEOUT, "tensor-core product wait timed out (code %d)", herr);
   return GP_OK;
+}
+
+int gp_geno_panel_tc_codes(gp_ctx *ctx, const gp_tc_codes *A, int npanels, const gp_tc_panel *pp,
+                           int32_t ncols, double *d_Y, int64_t ldy)
+{
+  if (A->nrows < 1 || A->k0 < 1) return GP_OK;
+  uint8_t *storage;
+  int rc = gp_scratch2(ctx, gp_tc_prepared_bytes(npanels, ncols, A->k0), (void **)&storage);
+  if (rc) return rc;
+  gp_tc_prepared P;
+  rc = gp_tc_prepare(ctx, npanels, pp, ncols, A->k0, storage, &P);
+  if (rc) return rc;
+  return gp_tc_apply(ctx, A, &P, d_Y, ldy, 1);
 }
 
 int gp_geno_panel_tc(gp_ctx *ctx, int sum_over_snps, const int32_t *d_samp, int32_t nsamp,

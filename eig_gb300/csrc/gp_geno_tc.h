@@ -1,6 +1,8 @@
 /* Exact genotype x FP64-panel products on the tensor cores (gp_geno_tc.cu). */
 #ifndef GP_GENO_TC_H
 #define GP_GENO_TC_H
+#include <cuda.h>
+#include <cuda_fp16.h>
 #include <vector>
 
 #include "gp_internal.h"
@@ -28,6 +30,24 @@ struct gp_tc_codes {
 int gp_tc_code_bytes(int sum_over_snps, int32_t nsamp, int32_t nk, int64_t *ldc, int32_t *rows_pad);
 int gp_tc_build_codes(gp_ctx *ctx, int sum_over_snps, const int32_t *d_samp, int32_t nsamp,
                       const int32_t *d_snprec, int32_t nk, uint8_t *codes, gp_tc_codes *out);
+/* a panel cut into fp16 slices once (B operand + column exponents + its tensor map) */
+struct gp_tc_prepared {
+  __half *B;
+  int32_t *expo;
+  int32_t ncols, ncols4, ncols4_pad, npanels, kb0, k0;
+  int64_t ldb;
+  uint64_t lut_lo, lut_hi;
+  CUtensorMap tmb;
+};
+size_t gp_tc_prepared_bytes(int npanels, int32_t ncols, int32_t k0);
+/* slice the panels into caller storage of gp_tc_prepared_bytes bytes (device) */
+int gp_tc_prepare(gp_ctx *ctx, int npanels, const gp_tc_panel *pp, int32_t ncols, int32_t k0,
+                  void *storage, gp_tc_prepared *out);
+/* Y[r][c] = products of the code operand with a prepared panel; sync = 0 leaves the work
+ * queued on ctx->stream and neither clears nor reads ctx->d_err (the caller does both) */
+int gp_tc_apply(gp_ctx *ctx, const gp_tc_codes *A, const gp_tc_prepared *P, double *d_Y,
+                int64_t ldy, int sync);
+
 /* Y[r][c] = sum_p sum_k A(r, k) sign_p P_p[k][c] with a prepared code operand */
 int gp_geno_panel_tc_codes(gp_ctx *ctx, const gp_tc_codes *A, int npanels, const gp_tc_panel *pp,
                            int32_t ncols, double *d_Y, int64_t ldy);

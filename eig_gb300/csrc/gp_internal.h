@@ -79,6 +79,8 @@ struct gp_ctx {
   size_t scratch3_cap;
   void *d_scratch4;    /* genotype code operands of gp_geno_tc */
   size_t scratch4_cap;
+  void *d_scratch5;    /* exact integer partial sums of gp_geno_tc */
+  size_t scratch5_cap;
   int *d_err;          /* error word written by the tensor-core kernels' bounded waits */
   int precision;       /* precision of the last gp_xtx: split precisions use the tensor-core
                           exact products for weights and lsqproject */
@@ -93,6 +95,7 @@ int gp_scratch(gp_ctx *ctx, size_t bytes, void **out);
 int gp_scratch2(gp_ctx *ctx, size_t bytes, void **out);
 int gp_scratch_aux(gp_ctx *ctx, size_t bytes, void **out);
 int gp_scratch4(gp_ctx *ctx, size_t bytes, void **out);
+int gp_scratch5(gp_ctx *ctx, size_t bytes, void **out);
 int gp_realloc(gp_ctx *ctx, void **ptr, size_t bytes);
 
 #define GP_CUDA(ctx, call)                                   \
@@ -116,6 +119,11 @@ int gp_gram_fp64(gp_ctx *ctx);
 int gp_gram_split(gp_ctx *ctx, int precision);
 int gp_launch_symmetrize_trace(gp_ctx *ctx, double *d_trace);
 int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, double *d_vecs);
+/* per-sample masked normal equations solve of lsqproj (gp_api.cu); co rows hold the K(K+1)/2
+ * pair sums then the observed count, rr rows the K right-hand sides; acoef/bcoef are [K][nproj] */
+__global__ void k_lsq_solve(const double *co, int32_t ldco, const double *rr, int32_t K,
+                            int32_t nproj, double *acoef, double *bcoef, int32_t *nobs,
+                            int32_t *status, double *work);
 int gp_launch_materialize_f64(gp_ctx *ctx, int32_t k0, int32_t kc, int32_t pitch, double *d_x,
                               double scale);
 

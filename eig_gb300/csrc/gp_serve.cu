@@ -1,0 +1,652 @@
+/*
+ * Projection serving on a resident panel (include/gpupca_serve.h): admission by device
+ * memory, continuous batching with two batches in flight, exact tensor-core masked normal
+ * equations and per-sample FP64 Cholesky solves (the lsqproj/regressit arithmetic of
+ * src/eigensrc/smartpca.c:4690-4712 and src/regsubs.c:8-72 restated for a batch).
+ */
+#include <cuda_runtime.h>
+#include <errno.h>
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+#include <deque>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/gpupca_serve.h"
+#include "gp_geno_tc.h"
+#include "gp_internal.h"
+
+struct gp_req {
+  int64_t id;
+  int32_t nsamp;
+  const uint8_t *codes;
+  double *coords;
+  int32_t *status;
+  int64_t row_start;  /* ring position of the first row */
+  int64_t skip;       /* ring rows skipped before it (wrap) */
+  cudaEvent_t copied;
+  int done;
+  int error;
+};
+/* tickets are released by the gp_serve_test / gp_serve_wait call that sees them complete */
+
+struct gp_batch {
+  std::vector<gp_req *> reqs;
+  int64_t row_start;
+  int32_t nrows;
+  int slot;
+  int failed; /* launch error: its finished event was never recorded */
+  cudaEvent_t finished;
+};
+
+struct gp_server {
+  gp_ctx *ctx;
+  int32_t K, npair, ldp, nk;
+  std::vector<int32_t> snp_index; /* panel SNP k -> genotype SNP record */
+  int64_t row_bytes;
+  int32_t max_batch;
+  int64_t pool_cap;
+  int fp64_serial;
+  std::vector<double> eigscale;
+  /* resident panel */
+  double *d_E, *d_P, *d_fE, *d_mE;
+  double *d_otab, *d_rtab;
+  void *stor_co, *stor_rr;
+  gp_tc_prepared Pco, Prr;
+  /* pool and per-slot batch buffers */
+  uint8_t *d_pool;
+  int64_t head, tail;
+  cudaStream_t copy_stream;
+  double *d_co[2], *d_rr[2], *d_a[2], *d_b[2], *d_work[2], *d_part[2];
+  int32_t *d_nobs[2], *d_status[2];
+  int *d_errw[2];
+  double *h_a[2];
+  int32_t *h_status[2];
+  int *h_err[2];
+  /* queues */
+  pthread_mutex_t mu;
+  pthread_cond_t cv;
+  std::deque<gp_req *> waiting, admitted;
+  std::deque<gp_batch *> inflight;
+  std::unordered_map<int64_t, gp_req *> all;
+  int64_t next_id;
+  pthread_t thread;
+  int stop, thread_started, paused;
+  int64_t n_batches, n_samples, n_requests;
+  char err[GP_ERRLEN];
+};
+
+/* FP64 products for the serial baseline: Y[q][c] = sum_s T_s[code(q,s)] P[s][c], codes
+ * sample-major (row q at codes + q*ldc); split over s into part[split][q][c] */
+#define ST 64
+#define SK 16
+__global__ void __launch_bounds__(256)
+k_codes_gemm_f64(const uint8_t *__restrict__ codes, int64_t ldc, int32_t nrows,
+                 const double *__restrict__ tab, int32_t nk, const double *__restrict__ P,
+                 int64_t ldp, int32_t ncols, int32_t kper, double *part)
+{
+  __shared__ double As[SK][ST + 1];
+  __shared__ double Bs[SK][ST + 1];
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const int32_t q0 = (int32_t)blockIdx.y * ST, c0 = (int32_t)blockIdx.x * ST;
+  const int32_t kb = (int32_t)blockIdx.z * kper, ke = kb + kper < nk ? kb + kper : nk;
+  const int lk = tid & 15, lr = tid >> 4;
+  double acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) acc[a][b] = 0.0;
+  for (int32_t k0 = kb; k0 < ke; k0 += SK) {
+    int32_t s = k0 + lk;
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+      int32_t q = q0 + lr + 16 * p;
+      double v = 0.0;
+      if (s < ke && q < nrows) {
+        uint32_t c = (codes[(int64_t)q * ldc + (s >> 2)] >> ((3 - (s & 3)) * 2)) & 3u;
+        v = tab[4 * s + c];
+      }
+      As[lk][lr + 16 * p] = v;
+    }
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+      int e = tid + 256 * p;
+      int r = e >> 6, c = e & 63;
+      int32_t ss = k0 + r, cc = c0 + c;
+      Bs[r][c] = (ss < ke && cc < ncols) ? P[(int64_t)ss * ldp + cc] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < SK; ++k) {
+      double a[4], b[4];
+#pragma unroll
+      for (int p = 0; p < 4; ++p) {
+        a[p] = As[k][ty + 16 * p];
+        b[p] = Bs[k][tx + 16 * p];
+      }
+#pragma unroll
+      for (int p = 0; p < 4; ++p)
+#pragma unroll
+        for (int r = 0; r < 4; ++r) acc[p][r] = fma(a[p], b[r], acc[p][r]);
+    }
+    __syncthreads();
+  }
+  double *o = part + (int64_t)blockIdx.z * nrows * ncols;
+#pragma unroll
+  for (int p = 0; p < 4; ++p) {
+    int32_t q = q0 + ty + 16 * p;
+    if (q >= nrows) continue;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      int32_t c = c0 + tx + 16 * r;
+      if (c < ncols) o[(int64_t)q * ncols + c] = acc[p][r];
+    }
+  }
+}
+
+__global__ void k_parts_sum(double *Y, int64_t ldy, const double *part, int32_t nsplit,
+                            int32_t nrows, int32_t ncols)
+{
+  int64_t total = (int64_t)nrows * ncols;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int64_t q = idx / ncols, c = idx - q * ncols;
+    double s = 0.0;
+    for (int32_t t = 0; t < nsplit; ++t) s += part[t * total + idx];
+    Y[q * ldy + c] = s;
+  }
+}
+
+/* panel arrays of the server from the source handle (kept columns in kept order) */
+__global__ void k_serve_panel(const double *ffvecs, const double *fxscal, const int32_t *kept,
+                              const double *xfancy, const double *xmean, int32_t nk, int32_t ncols,
+                              int32_t K, double *E, double *P, int32_t ldp, double *fE, double *mE,
+                              double *otab, double *rtab)
+{
+  for (int32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nk; k += gridDim.x * blockDim.x) {
+    int32_t c = kept[k];
+    double f = xfancy[c], m = xmean[c];
+    double e[64];
+    for (int j = 0; j < K; ++j) {
+      e[j] = fxscal[j] * ffvecs[(int64_t)j * ncols + c];
+      E[(int64_t)k * K + j] = e[j];
+      fE[(int64_t)k * K + j] = f * e[j];
+      mE[(int64_t)k * K + j] = m * e[j];
+    }
+    double *p = P + (int64_t)k * ldp;
+    int t = 0;
+    for (int a = 0; a < K; ++a)
+      for (int b = a; b < K; ++b) p[t++] = e[a] * e[b];
+    p[t] = 1.0;
+    otab[4 * k] = otab[4 * k + 1] = otab[4 * k + 2] = 1.0;
+    otab[4 * k + 3] = 0.0;
+    for (int g = 0; g < 3; ++g) {
+      double x = __dmul_rn((double)g, f);
+      rtab[4 * k + g] = (x < -0.001) ? 0.0 : __dsub_rn(x, m);
+    }
+    rtab[4 * k + 3] = 0.0;
+  }
+}
+
+static int srv_fail(gp_server *s, int code, const char *msg)
+{
+  snprintf(s->err, sizeof s->err, "%s", msg);
+  return code;
+}
+
+/* admission by pool memory, in FIFO order; called with the lock held */
+static void admit_waiting(gp_server *s)
+{
+  while (!s->waiting.empty()) {
+    gp_req *r = s->waiting.front();
+    int64_t used = s->head - s->tail;
+    if (used == 0) s->head = s->tail = 0; /* an empty ring restarts at row 0 */
+    int64_t pos = s->head % s->pool_cap;
+    int64_t skip = (pos + r->nsamp > s->pool_cap) ? s->pool_cap - pos : 0;
+    if (used + skip + r->nsamp > s->pool_cap) break; /* waits until memory frees up */
+    s->head += skip;
+    r->skip = skip;
+    r->row_start = s->head % s->pool_cap;
+    s->head += r->nsamp;
+    cudaError_t e = cudaMemcpyAsync(s->d_pool + r->row_start * s->row_bytes, r->codes,
+                                    (size_t)r->nsamp * s->row_bytes, cudaMemcpyHostToDevice,
+                                    s->copy_stream);
+    if (e == cudaSuccess) e = cudaEventRecord(r->copied, s->copy_stream);
+    if (e != cudaSuccess) r->error = GP_ERR_CUDA;
+    s->waiting.pop_front();
+    s->admitted.push_back(r);
+  }
+}
+
+/* queue the batch's work on the compute stream; called without the lock */
+static int launch_batch(gp_server *s, gp_batch *b)
+{
+  gp_ctx *ctx = s->ctx;
+  const int sl = b->slot;
+  for (gp_req *r : b->reqs) GP_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, r->copied, 0));
+  GP_CUDA(ctx, cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
+  gp_tc_codes A;
+  A.codes = s->d_pool + b->row_start * s->row_bytes;
+  A.ldc = s->row_bytes;
+  A.row_map = NULL;
+  A.nrows = b->nrows;
+  A.k0 = s->nk;
+  int rc;
+  if (!s->fp64_serial) {
+    rc = gp_tc_apply(ctx, &A, &s->Pco, s->d_co[sl], s->ldp, 0);
+    if (!rc) rc = gp_tc_apply(ctx, &A, &s->Prr, s->d_rr[sl], s->K, 0);
+    if (rc) return rc;
+  } else {
+    const int32_t n = b->nrows;
+    for (int which = 0; which < 2; ++which) {
+      const double *P = which ? s->d_E : s->d_P;
+      const double *tab = which ? s->d_rtab : s->d_otab;
+      int32_t nc = which ? s->K : s->ldp;
+      double *Y = which ? s->d_rr[sl] : s->d_co[sl];
+      int64_t tiles = (int64_t)((n + ST - 1) / ST) * ((nc + ST - 1) / ST);
+      int32_t nsplit = (int32_t)((2 * ctx->num_sms + tiles - 1) / tiles);
+      if (nsplit > 16) nsplit = 16;
+      if (nsplit < 1) nsplit = 1;
+      int32_t kper = ((s->nk + nsplit - 1) / nsplit + SK - 1) / SK * SK;
+      nsplit = (s->nk + kper - 1) / kper;
+      dim3 grid((unsigned)((nc + ST - 1) / ST), (unsigned)((n + ST - 1) / ST), (unsigned)nsplit);
+      k_codes_gemm_f64<<<grid, 256, 0, ctx->stream>>>(A.codes, A.ldc, n, tab, s->nk, P, nc, nc,
+                                                       kper, s->d_part[sl]);
+      GP_LAUNCH_CHECK(ctx, "k_codes_gemm_f64");
+      int64_t tot = (int64_t)n * nc;
+      int blocks = (int)((tot + 255) / 256);
+      if (blocks > ctx->num_sms * 8) blocks = ctx->num_sms * 8;
+      k_parts_sum<<<blocks, 256, 0, ctx->stream>>>(Y, nc, s->d_part[sl], nsplit, n, nc);
+      GP_LAUNCH_CHECK(ctx, "k_parts_sum");
+    }
+  }
+  k_lsq_solve<<<(b->nrows + 127) / 128, 128, 0, ctx->stream>>>(
+      s->d_co[sl], s->ldp, s->d_rr[sl], s->K, b->nrows, s->d_a[sl], s->d_b[sl], s->d_nobs[sl],
+      s->d_status[sl], s->d_work[sl]);
+  GP_LAUNCH_CHECK(ctx, "k_lsq_solve");
+  GP_CUDA(ctx, cudaMemcpyAsync(s->h_a[sl], s->d_a[sl], sizeof(double) * (size_t)s->K * b->nrows,
+                               cudaMemcpyDeviceToHost, ctx->stream));
+  GP_CUDA(ctx, cudaMemcpyAsync(s->h_status[sl], s->d_status[sl], sizeof(int32_t) * b->nrows,
+                               cudaMemcpyDeviceToHost, ctx->stream));
+  GP_CUDA(ctx, cudaMemcpyAsync(s->h_err[sl], ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost,
+                               ctx->stream));
+  GP_CUDA(ctx, cudaEventRecord(b->finished, ctx->stream));
+  return GP_OK;
+}
+
+/* results of a finished batch into the requests; called with the lock held */
+static void complete_batch(gp_server *s, gp_batch *b, int rc)
+{
+  const int sl = b->slot;
+  const int32_t K = s->K, n = b->nrows;
+  int err = rc ? rc : (*s->h_err[sl] ? GP_ERR_TIMEOUT : GP_OK);
+  int32_t off = 0;
+  for (gp_req *r : b->reqs) {
+    if (!err && !r->error) {
+      for (int32_t q = 0; q < r->nsamp; ++q) {
+        int32_t st = s->h_status[sl][off + q];
+        r->status[q] = st;
+        for (int32_t j = 0; j < K; ++j)
+          r->coords[(size_t)q * K + j] =
+              st == 0 ? s->h_a[sl][(size_t)j * n + off + q] * s->eigscale[(size_t)j] : 0.0;
+      }
+    } else if (!r->error) {
+      r->error = err;
+    }
+    off += r->nsamp;
+    s->tail += r->skip + r->nsamp;
+    cudaEventDestroy(r->copied);
+    r->copied = NULL;
+    r->done = 1;
+    s->n_requests++;
+  }
+  s->n_batches++;
+  s->n_samples += n;
+}
+
+static void *scheduler(void *arg)
+{
+  gp_server *s = (gp_server *)arg;
+  cudaSetDevice(s->ctx->device);
+  int next_slot = 0;
+  pthread_mutex_lock(&s->mu);
+  while (!s->stop || !s->admitted.empty() || !s->inflight.empty() || !s->waiting.empty()) {
+    admit_waiting(s);
+    if (!s->paused && s->inflight.size() < 2 && !s->admitted.empty()) {
+      /* the next batch: admitted requests, contiguous in the pool, up to max_batch rows */
+      gp_batch *b = new gp_batch;
+      b->slot = next_slot;
+      next_slot ^= 1;
+      b->row_start = s->admitted.front()->row_start;
+      b->nrows = 0;
+      while (!s->admitted.empty()) {
+        gp_req *r = s->admitted.front();
+        if (!b->reqs.empty() && (s->fp64_serial || r->skip != 0 ||
+                                 r->row_start != b->row_start + b->nrows ||
+                                 b->nrows + r->nsamp > s->max_batch))
+          break;
+        b->reqs.push_back(r);
+        b->nrows += r->nsamp;
+        s->admitted.pop_front();
+        if (s->fp64_serial) break;
+      }
+      b->failed = 0;
+      cudaEventCreateWithFlags(&b->finished, cudaEventDisableTiming);
+      s->inflight.push_back(b);
+      pthread_mutex_unlock(&s->mu);
+      int rc = launch_batch(s, b);
+      if (rc) {
+        /* completes in order behind the batches before it, once the stream has drained */
+        cudaStreamSynchronize(s->ctx->stream);
+        b->failed = rc;
+      }
+      pthread_mutex_lock(&s->mu);
+      continue;
+    }
+    if (!s->inflight.empty()) {
+      gp_batch *b = s->inflight.front();
+      pthread_mutex_unlock(&s->mu);
+      cudaError_t e = b->failed ? cudaSuccess : cudaEventSynchronize(b->finished);
+      pthread_mutex_lock(&s->mu);
+      s->inflight.pop_front();
+      complete_batch(s, b, b->failed ? b->failed : (e == cudaSuccess ? GP_OK : GP_ERR_CUDA));
+      cudaEventDestroy(b->finished);
+      delete b;
+      pthread_cond_broadcast(&s->cv);
+      continue;
+    }
+    if (s->stop) break;
+    struct timespec ts;
+    clock_gettime(CLOCK_REALTIME, &ts);
+    ts.tv_nsec += 50 * 1000 * 1000;
+    if (ts.tv_nsec >= 1000000000L) {
+      ts.tv_sec += 1;
+      ts.tv_nsec -= 1000000000L;
+    }
+    pthread_cond_timedwait(&s->cv, &s->mu, &ts);
+  }
+  pthread_mutex_unlock(&s->mu);
+  return NULL;
+}
+
+/* ------------------------------------------------------------------------------------ */
+
+extern "C" const char *gp_serve_last_error(const gp_server *srv) { return srv ? srv->err : ""; }
+
+extern "C" void gp_serve_close(gp_server *s)
+{
+  if (!s) return;
+  if (s->thread_started) {
+    pthread_mutex_lock(&s->mu);
+    s->stop = 1;
+    s->paused = 0;
+    pthread_cond_broadcast(&s->cv);
+    pthread_mutex_unlock(&s->mu);
+    pthread_join(s->thread, NULL);
+  }
+  if (s->ctx) cudaSetDevice(s->ctx->device);
+  void *dev[] = {s->d_E,     s->d_P,      s->d_fE,     s->d_mE,     s->d_otab,   s->d_rtab,
+                 s->stor_co, s->stor_rr,  s->d_pool,   s->d_co[0],  s->d_co[1],  s->d_rr[0],
+                 s->d_rr[1], s->d_a[0],   s->d_a[1],   s->d_b[0],   s->d_b[1],   s->d_work[0],
+                 s->d_work[1], s->d_part[0], s->d_part[1], s->d_nobs[0], s->d_nobs[1],
+                 s->d_status[0], s->d_status[1]};
+  for (size_t i = 0; i < sizeof(dev) / sizeof(dev[0]); ++i)
+    if (dev[i]) cudaFree(dev[i]);
+  for (int i = 0; i < 2; ++i) {
+    if (s->h_a[i]) cudaFreeHost(s->h_a[i]);
+    if (s->h_status[i]) cudaFreeHost(s->h_status[i]);
+    if (s->h_err[i]) cudaFreeHost(s->h_err[i]);
+  }
+  for (auto &kv : s->all) {
+    if (kv.second->copied) cudaEventDestroy(kv.second->copied);
+    delete kv.second;
+  }
+  if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
+  if (s->ctx) gp_close(s->ctx);
+  pthread_mutex_destroy(&s->mu);
+  pthread_cond_destroy(&s->cv);
+  delete s;
+}
+
+extern "C" int gp_serve_open(gp_ctx *src, const gp_serve_opts *o, gp_server **out)
+{
+  if (!src || !o || !out) return GP_ERR_ARG;
+  *out = NULL;
+  if (!src->weights_valid)
+    return gp_fail(src, GP_ERR_STATE, "gp_serve_open: the source handle has no SNP weights");
+  const int32_t K = o->numeigs;
+  if (K < 1 || K > src->nweights || K > 64)
+    return gp_fail(src, GP_ERR_ARG, "gp_serve_open: numeigs %d out of range", K);
+  if (src->nkept < 1) return gp_fail(src, GP_ERR_NODATA, "gp_serve_open: the panel has no SNP");
+  gp_server *s = new gp_server();
+  pthread_mutex_init(&s->mu, NULL);
+  pthread_cond_init(&s->cv, NULL);
+  s->K = K;
+  s->npair = K * (K + 1) / 2;
+  s->ldp = s->npair + 1;
+  s->nk = src->nkept;
+  s->row_bytes = (int64_t)((s->nk + 63) / 64) * 16;
+  s->max_batch = o->max_batch > 0 ? o->max_batch : 4096;
+  s->pool_cap = o->pool_samples > 0 ? o->pool_samples : 32768;
+  if (s->pool_cap < s->max_batch) s->pool_cap = s->max_batch;
+  s->fp64_serial = o->fp64_serial;
+  s->eigscale.assign((size_t)K, 1.0);
+  if (o->eigscale)
+    for (int32_t j = 0; j < K; ++j) s->eigscale[(size_t)j] = o->eigscale[j];
+  int rc = gp_open(src->device, &s->ctx);
+  if (rc) {
+    snprintf(src->err, GP_ERRLEN, "gp_serve_open: %s", gp_last_error(NULL));
+    delete s;
+    return rc;
+  }
+  gp_ctx *ctx = s->ctx;
+  const size_t nk = (size_t)s->nk;
+  cudaError_t e = cudaSuccess;
+#define SALLOC(p, bytes)                                   \
+  if (e == cudaSuccess) e = cudaMalloc((void **)&(p), (bytes) < 256 ? 256 : (bytes))
+  SALLOC(s->d_E, sizeof(double) * nk * K);
+  SALLOC(s->d_P, sizeof(double) * nk * s->ldp);
+  SALLOC(s->d_fE, sizeof(double) * nk * K);
+  SALLOC(s->d_mE, sizeof(double) * nk * K);
+  SALLOC(s->d_otab, sizeof(double) * nk * 4);
+  SALLOC(s->d_rtab, sizeof(double) * nk * 4);
+  SALLOC(s->d_pool, (size_t)s->pool_cap * s->row_bytes);
+  for (int i = 0; i < 2; ++i) {
+    SALLOC(s->d_co[i], sizeof(double) * (size_t)s->max_batch * s->ldp);
+    SALLOC(s->d_rr[i], sizeof(double) * (size_t)s->max_batch * K);
+    SALLOC(s->d_a[i], sizeof(double) * (size_t)s->max_batch * K);
+    SALLOC(s->d_b[i], sizeof(double) * (size_t)s->max_batch * K);
+    SALLOC(s->d_work[i], sizeof(double) * (size_t)s->max_batch * (K * K + 2 * K));
+    SALLOC(s->d_nobs[i], sizeof(int32_t) * (size_t)s->max_batch);
+    SALLOC(s->d_status[i], sizeof(int32_t) * (size_t)s->max_batch);
+    if (s->fp64_serial) SALLOC(s->d_part[i], sizeof(double) * 16 * (size_t)s->max_batch * s->ldp);
+    if (e == cudaSuccess) e = cudaHostAlloc((void **)&s->h_a[i], sizeof(double) * (size_t)s->max_batch * K, 0);
+    if (e == cudaSuccess) e = cudaHostAlloc((void **)&s->h_status[i], sizeof(int32_t) * (size_t)s->max_batch, 0);
+    if (e == cudaSuccess) e = cudaHostAlloc((void **)&s->h_err[i], sizeof(int) * 4, 0);
+  }
+  if (!s->fp64_serial) {
+    size_t b1 = gp_tc_prepared_bytes(1, s->ldp, s->nk), b2 = gp_tc_prepared_bytes(2, K, s->nk);
+    SALLOC(s->stor_co, b1);
+    SALLOC(s->stor_rr, b2);
+  }
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) {
+    /* panel SNP records, host side, for callers that build request rows */
+    std::vector<int32_t> kept(nk), cols((size_t)src->ncols);
+    cudaSetDevice(src->device);
+    e = cudaMemcpy(kept.data(), src->d_kept, sizeof(int32_t) * nk, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(cols.data(), src->d_cols, sizeof(int32_t) * cols.size(), cudaMemcpyDeviceToHost);
+    s->snp_index.resize(nk);
+    for (size_t k = 0; k < nk && e == cudaSuccess; ++k) s->snp_index[k] = cols[(size_t)kept[k]];
+  }
+  if (e != cudaSuccess) {
+    gp_fail(src, GP_ERR_NOMEM, "gp_serve_open: allocation failed: %s", cudaGetErrorString(e));
+    gp_serve_close(s);
+    return GP_ERR_NOMEM;
+  }
+  /* the panel: from the source handle's resident weights (its own stream, then wait) */
+  GP_CUDA(src, cudaSetDevice(src->device));
+  if (s->nk > 0) {
+    int blocks = (int)((nk + 127) / 128);
+    if (blocks > src->num_sms * 8) blocks = src->num_sms * 8;
+    k_serve_panel<<<blocks, 128, 0, src->stream>>>(src->d_ffvecs, src->d_fxscal, src->d_kept,
+                                                   src->d_xfancy, src->d_xmean, s->nk, src->ncols,
+                                                   K, s->d_E, s->d_P, s->ldp, s->d_fE, s->d_mE,
+                                                   s->d_otab, s->d_rtab);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(src->stream);
+    if (e != cudaSuccess) {
+      gp_cuda_fail(src, e, "k_serve_panel");
+      gp_serve_close(s);
+      return GP_ERR_CUDA;
+    }
+  }
+  if (!s->fp64_serial && s->nk > 0) {
+    gp_tc_panel pc = {s->d_P, s->ldp, 1.0, 0};
+    rc = gp_tc_prepare(ctx, 1, &pc, s->ldp, s->nk, s->stor_co, &s->Pco);
+    gp_tc_panel pr[2] = {{s->d_fE, K, 1.0, 1}, {s->d_mE, K, -1.0, 0}};
+    if (!rc) rc = gp_tc_prepare(ctx, 2, pr, K, s->nk, s->stor_rr, &s->Prr);
+    /* the products' slice-column buffer, sized once for the largest batch */
+    void *z;
+    if (!rc) rc = gp_scratch5(ctx, (size_t)s->max_batch * s->Pco.ncols4_pad * 8 + 256, &z);
+    if (!rc) {
+      e = cudaStreamSynchronize(ctx->stream);
+      if (e != cudaSuccess) rc = gp_cuda_fail(ctx, e, "gp_serve_open prepare");
+    }
+    if (rc) {
+      snprintf(src->err, GP_ERRLEN, "gp_serve_open: %s", gp_last_error(ctx));
+      gp_serve_close(s);
+      return rc;
+    }
+  }
+  if (pthread_create(&s->thread, NULL, scheduler, s) != 0) {
+    gp_fail(src, GP_ERR_STATE, "gp_serve_open: could not start the scheduler thread");
+    gp_serve_close(s);
+    return GP_ERR_STATE;
+  }
+  s->thread_started = 1;
+  *out = s;
+  return GP_OK;
+}
+
+extern "C" int gp_serve_layout(const gp_server *s, int64_t *nsnp, int64_t *row_bytes)
+{
+  if (!s) return GP_ERR_ARG;
+  if (nsnp) *nsnp = s->nk;
+  if (row_bytes) *row_bytes = s->row_bytes;
+  return GP_OK;
+}
+
+extern "C" int gp_serve_panel_snps(const gp_server *s, int32_t *snp_index)
+{
+  if (!s || !snp_index) return GP_ERR_ARG;
+  memcpy(snp_index, s->snp_index.data(), sizeof(int32_t) * s->snp_index.size());
+  return GP_OK;
+}
+
+extern "C" int gp_serve_submit(gp_server *s, const uint8_t *codes, int32_t nsamp, double *coords,
+                               int32_t *status, int64_t *ticket)
+{
+  if (!s || !codes || !coords || !status || !ticket || nsamp < 1) return GP_ERR_ARG;
+  if (nsamp > s->max_batch || nsamp > s->pool_cap)
+    return srv_fail(s, GP_ERR_FULL, "request larger than the batch or the device pool");
+  gp_req *r = new gp_req();
+  r->nsamp = nsamp;
+  r->codes = codes;
+  r->coords = coords;
+  r->status = status;
+  if (cudaEventCreateWithFlags(&r->copied, cudaEventDisableTiming) != cudaSuccess) {
+    delete r;
+    return srv_fail(s, GP_ERR_CUDA, "cudaEventCreate failed");
+  }
+  pthread_mutex_lock(&s->mu);
+  r->id = s->next_id++;
+  s->all[r->id] = r;
+  s->waiting.push_back(r);
+  admit_waiting(s);
+  pthread_cond_broadcast(&s->cv);
+  pthread_mutex_unlock(&s->mu);
+  *ticket = r->id;
+  return GP_OK;
+}
+
+extern "C" int gp_serve_test(gp_server *s, int64_t ticket)
+{
+  if (!s) return GP_ERR_ARG;
+  pthread_mutex_lock(&s->mu);
+  auto it = s->all.find(ticket);
+  int rc;
+  if (it == s->all.end()) {
+    rc = GP_ERR_ARG;
+  } else if (!it->second->done) {
+    rc = 0;
+  } else {
+    rc = it->second->error ? it->second->error : 1;
+    delete it->second;
+    s->all.erase(it);
+  }
+  pthread_mutex_unlock(&s->mu);
+  return rc;
+}
+
+extern "C" int gp_serve_wait(gp_server *s, int64_t ticket, double timeout_s)
+{
+  if (!s) return GP_ERR_ARG;
+  struct timespec dl;
+  clock_gettime(CLOCK_REALTIME, &dl);
+  double t = (double)dl.tv_sec + 1e-9 * dl.tv_nsec + (timeout_s > 0 ? timeout_s : 0.0);
+  dl.tv_sec = (time_t)t;
+  dl.tv_nsec = (long)((t - (double)dl.tv_sec) * 1e9);
+  pthread_mutex_lock(&s->mu);
+  auto it = s->all.find(ticket);
+  if (it == s->all.end()) {
+    pthread_mutex_unlock(&s->mu);
+    return srv_fail(s, GP_ERR_ARG, "unknown ticket");
+  }
+  gp_req *r = it->second;
+  int rc = GP_OK;
+  while (!r->done) {
+    int w = pthread_cond_timedwait(&s->cv, &s->mu, &dl);
+    if (w == ETIMEDOUT && !r->done) {
+      rc = GP_ERR_TIMEOUT;
+      snprintf(s->err, sizeof s->err, "request %lld still pending after %.3f s",
+               (long long)ticket, timeout_s);
+      break;
+    }
+  }
+  if (r->done) {
+    if (r->error) rc = r->error;
+    s->all.erase(ticket); /* by key: inserts meanwhile may have rehashed the map */
+    delete r;
+  }
+  pthread_mutex_unlock(&s->mu);
+  return rc;
+}
+
+extern "C" int gp_serve_pause(gp_server *s, int32_t paused)
+{
+  if (!s) return GP_ERR_ARG;
+  pthread_mutex_lock(&s->mu);
+  s->paused = paused ? 1 : 0;
+  pthread_cond_broadcast(&s->cv);
+  pthread_mutex_unlock(&s->mu);
+  return GP_OK;
+}
+
+extern "C" int gp_serve_stats(const gp_server *s, int64_t *batches, int64_t *samples,
+                              int64_t *requests)
+{
+  if (!s) return GP_ERR_ARG;
+  gp_server *m = (gp_server *)s;
+  pthread_mutex_lock(&m->mu);
+  if (batches) *batches = s->n_batches;
+  if (samples) *samples = s->n_samples;
+  if (requests) *requests = s->n_requests;
+  pthread_mutex_unlock(&m->mu);
+  return GP_OK;
+}

@@ -147,6 +147,16 @@ static void snp_freqs(const gp_synth_spec *sp, int64_t s, double *pk)
   }
 }
 
+/* genotype code of sample n at SNP s given its allele frequency p and missing rate */
+static inline int draw_code(uint64_t seed, int64_t s, int64_t n, double p, double miss)
+{
+  uint64_t h1 = key3(seed, (uint64_t)s, (uint64_t)n, 2);
+  uint64_t h2 = mix64(h1 ^ 0x5851F42D4C957F2Dull);
+  int g = (u01(h1) < p) + (u01(h2) < p);
+  uint64_t h3 = mix64(h2 + 0x14057B7EF767814Full);
+  return u01(h3) < miss ? 3 : g;
+}
+
 static void *synth_worker(void *arg)
 {
   synth_job *job = (synth_job *)arg;
@@ -159,15 +169,105 @@ static void *synth_worker(void *arg)
     for (int32_t n = 0; n < sp->nind; ++n) {
       double p = pk[job->pop_a[n]];
       if (job->pop_b[n] >= 0) p = job->mix[n] * p + (1.0 - job->mix[n]) * pk[job->pop_b[n]];
-      uint64_t h1 = key3(sp->seed, (uint64_t)s, (uint64_t)n, 2);
-      uint64_t h2 = mix64(h1 ^ 0x5851F42D4C957F2Dull);
-      int g = (u01(h1) < p) + (u01(h2) < p);
-      uint64_t h3 = mix64(h2 + 0x14057B7EF767814Full);
-      if (u01(h3) < job->miss[n]) g = 3;
+      int g = draw_code(sp->seed, s, n, p, job->miss[n]);
       rec[n >> 2] |= (uint8_t)(g << ((3 - (n & 3)) * 2));
     }
   }
   return NULL;
+}
+
+/* ---- new samples of the same populations, in request-row layout ----------------------- */
+
+typedef struct {
+  const gp_synth_spec *sp;
+  uint64_t sample_seed;
+  const int64_t *snp_index;
+  int64_t nk, row_bytes;
+  double *pk;               /* [nk][npops] */
+  int32_t *pop_a, *pop_b;
+  double *mix, *miss;
+  uint8_t *rows;
+  int64_t lo, hi;           /* SNP range (phase 0) or sample range (phase 1) */
+  int phase;
+} rows_job;
+
+static void *rows_worker(void *arg)
+{
+  rows_job *j = (rows_job *)arg;
+  const gp_synth_spec *sp = j->sp;
+  if (j->phase == 0) {
+    for (int64_t k = j->lo; k < j->hi; ++k) snp_freqs(sp, j->snp_index[k], j->pk + k * sp->npops);
+    return NULL;
+  }
+  for (int64_t n = j->lo; n < j->hi; ++n) {
+    uint8_t *row = j->rows + n * j->row_bytes;
+    memset(row, 0xFF, (size_t)j->row_bytes); /* pad codes 3 */
+    for (int64_t k = 0; k < j->nk; ++k) {
+      const double *pk = j->pk + k * sp->npops;
+      double p = pk[j->pop_a[n]];
+      if (j->pop_b[n] >= 0) p = j->mix[n] * p + (1.0 - j->mix[n]) * pk[j->pop_b[n]];
+      int g = draw_code(j->sample_seed, j->snp_index[k], n, p, j->miss[n]);
+      int sh = (3 - (int)(k & 3)) * 2;
+      row[k >> 2] = (uint8_t)((row[k >> 2] & ~(3u << sh)) | ((unsigned)g << sh));
+    }
+  }
+  return NULL;
+}
+
+static void run_rows_jobs(rows_job *base, int64_t total, int nthreads, int phase)
+{
+  pthread_t th[256];
+  rows_job jobs[256];
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > 256) nthreads = 256;
+  int64_t per = (total + nthreads - 1) / nthreads;
+  int started[256] = {0};
+  for (int t = 0; t < nthreads; ++t) {
+    jobs[t] = *base;
+    jobs[t].phase = phase;
+    jobs[t].lo = per * t < total ? per * t : total;
+    jobs[t].hi = per * (t + 1) < total ? per * (t + 1) : total;
+    if (t > 0 && pthread_create(&th[t], NULL, rows_worker, &jobs[t]) == 0) started[t] = 1;
+    else if (t > 0) rows_worker(&jobs[t]);
+  }
+  rows_worker(&jobs[0]);
+  for (int t = 1; t < nthreads; ++t)
+    if (started[t]) pthread_join(th[t], NULL);
+}
+
+int gp_synth_sample_rows(const gp_synth_spec *sp, uint64_t sample_seed, const int64_t *snp_index,
+                         int64_t nk, int64_t row_bytes, uint8_t *rows, int32_t *pop_of_sample,
+                         int nthreads)
+{
+  if (row_bytes * 4 < nk || nk < 0) return -1;
+  gp_synth_spec rs = *sp;
+  rs.seed = sample_seed; /* assignment, admixture and missingness of the new samples */
+  int32_t *pa = (int32_t *)malloc(sizeof(int32_t) * (size_t)sp->nind);
+  int32_t *pb = (int32_t *)malloc(sizeof(int32_t) * (size_t)sp->nind);
+  double *mx = (double *)malloc(sizeof(double) * (size_t)sp->nind);
+  double *ms = (double *)malloc(sizeof(double) * (size_t)sp->nind);
+  double *pk = (double *)malloc(sizeof(double) * (size_t)(nk > 0 ? nk : 1) * sp->npops);
+  int rc = 0;
+  if (!pa || !pb || !mx || !ms || !pk) {
+    rc = -3;
+    goto done;
+  }
+  rc = gp_synth_assign(&rs, pa, pb, mx, ms);
+  if (rc) goto done;
+  if (pop_of_sample)
+    for (int32_t n = 0; n < sp->nind; ++n) pop_of_sample[n] = (pb[n] >= 0) ? sp->npops : pa[n];
+  {
+    rows_job b = {sp, sample_seed, snp_index, nk, row_bytes, pk, pa, pb, mx, ms, rows, 0, 0, 0};
+    run_rows_jobs(&b, nk, nthreads, 0);          /* population frequencies of the panel SNPs */
+    run_rows_jobs(&b, sp->nind, nthreads, 1);    /* the samples' rows */
+  }
+done:
+  free(pa);
+  free(pb);
+  free(mx);
+  free(ms);
+  free(pk);
+  return rc;
 }
 
 int gp_synth_assign(const gp_synth_spec *sp, int32_t *pop_a, int32_t *pop_b, double *mix,

@@ -33,6 +33,14 @@ int gp_synth_assign(const gp_synth_spec *sp, int32_t *pop_a, int32_t *pop_b, dou
 int gp_synth_records(const gp_synth_spec *sp, uint8_t *records, int64_t rlen,
                      int32_t *pop_of_sample, int nthreads);
 
+/* New samples of the spec's populations (the same per-SNP population frequencies as
+ * gp_synth_records with sp->seed; assignment, admixture, missingness and genotypes drawn
+ * with sample_seed): sp->nind rows of row_bytes bytes, sample n's code at panel SNP k
+ * (record snp_index[k]) in byte k>>2, bits (3-(k&3))*2, padded with code 3. */
+int gp_synth_sample_rows(const gp_synth_spec *sp, uint64_t sample_seed, const int64_t *snp_index,
+                         int64_t nk, int64_t row_bytes, uint8_t *rows, int32_t *pop_of_sample,
+                         int nthreads);
+
 /* Write prefix.geno (packed, with header hashes), prefix.snp and prefix.ind. */
 int gp_synth_write_dataset(const gp_synth_spec *sp, const char *prefix, int nthreads);
 

@@ -17,6 +17,7 @@ GP_OK = 0
 GP_ERR = {-1: "GP_ERR_ARG", -2: "GP_ERR_CUDA", -3: "GP_ERR_NOMEM", -4: "GP_ERR_STATE",
           -5: "GP_ERR_SOLVER", -6: "GP_ERR_NODATA", -7: "GP_ERR_TIMEOUT", -8: "GP_ERR_FULL",
           -9: "GP_ERR_NOTBUILT"}
+GP_ERR_TIMEOUT = -7
 GP_CODE_PACKED, GP_CODE_BED = 0, 1
 GP_PREC_FP64, GP_PREC_SPLIT_BF16, GP_PREC_SPLIT_BF16X4, GP_PREC_SPLIT_FP16 = 0, 1, 2, 3
 PRECISIONS = {"fp64": 0, "bf16": 1, "bf16x4": 2, "fp16": 3}
@@ -30,7 +31,9 @@ EXPORTED = ["gp_version", "gp_last_error", "gp_open", "gp_close", "gp_device_byt
             "gp_fail_msg", "gp_genotype_shape", "gp_timer_start", "gp_timer_stop",
             "gp_last_gram_time", "gp_host_register", "gp_host_unregister",
             "gp_transfer_bytes", "gp_launch_count", "gp_gram_fp64_noalloc",
-            "gp_noalloc_last_error"]
+            "gp_noalloc_last_error", "gp_serve_open", "gp_serve_layout",
+            "gp_serve_panel_snps", "gp_serve_submit", "gp_serve_test", "gp_serve_wait",
+            "gp_serve_stats", "gp_serve_last_error", "gp_serve_close", "gp_serve_pause"]
 
 i32p = C.POINTER(C.c_int32)
 i64p = C.POINTER(C.c_int64)
@@ -60,6 +63,11 @@ class Panel(C.Structure):
                 ("nind", C.c_int32), ("code", C.c_int32), ("snp_chrom", i32p),
                 ("snp_ignore", u8p), ("ind_ignore", u8p), ("ind_affstatus", u8p),
                 ("ind_male", u8p)]
+
+
+class ServeOpts(C.Structure):
+    _fields_ = [("numeigs", C.c_int32), ("max_batch", C.c_int32), ("pool_samples", C.c_int64),
+                ("fp64_serial", C.c_int32), ("eigscale", f64p)]
 
 
 class RunResult(C.Structure):
@@ -115,6 +123,16 @@ def load_library():
         "gp_launch_count": (C.c_int, [vp, i64p, C.c_int32]),
         "gp_gram_fp64_noalloc": (C.c_int, [vp, C.c_int64, C.c_int32, C.c_int32, vp, vp, vp]),
         "gp_noalloc_last_error": (C.c_char_p, []),
+        "gp_serve_open": (C.c_int, [vp, C.POINTER(ServeOpts), C.POINTER(vp)]),
+        "gp_serve_layout": (C.c_int, [vp, i64p, i64p]),
+        "gp_serve_panel_snps": (C.c_int, [vp, i32p]),
+        "gp_serve_submit": (C.c_int, [vp, u8p, C.c_int32, f64p, i32p, i64p]),
+        "gp_serve_test": (C.c_int, [vp, C.c_int64]),
+        "gp_serve_wait": (C.c_int, [vp, C.c_int64, C.c_double]),
+        "gp_serve_stats": (C.c_int, [vp, i64p, i64p, i64p]),
+        "gp_serve_pause": (C.c_int, [vp, C.c_int32]),
+        "gp_serve_last_error": (C.c_char_p, [vp]),
+        "gp_serve_close": (None, [vp]),
         "gp_smartpca_run": (C.c_int, [vp, C.POINTER(SmartpcaOpts), C.POINTER(Panel),
                                       C.POINTER(RunResult)]),
     }
@@ -139,6 +157,9 @@ def load_synth():
     s.gp_synth_records.argtypes = [vp, u8p, C.c_int64, i32p, C.c_int]
     s.gp_synth_write_dataset.restype = C.c_int
     s.gp_synth_write_dataset.argtypes = [vp, C.c_char_p, C.c_int]
+    s.gp_synth_sample_rows.restype = C.c_int
+    s.gp_synth_sample_rows.argtypes = [vp, C.c_uint64, i64p, C.c_int64, C.c_int64, u8p, i32p,
+                                       C.c_int]
     s.gp_hash_string.restype = C.c_int32
     s.gp_hash_string.argtypes = [C.c_char_p]
     _synth = s
@@ -310,6 +331,117 @@ class Handle:
         return ev, V
 
 
+class ServeRequest:
+    """One submitted request: keeps its code rows and output buffers alive until done."""
+
+    def __init__(self, server, ticket, codes, coords, status):
+        self.server, self.ticket = server, ticket
+        self.codes, self.coords, self.status = codes, coords, status
+        self.done = False
+
+    def test(self):
+        if self.done:
+            return True
+        rc = self.server.lib.gp_serve_test(self.server.s, self.ticket)
+        if rc == 0:
+            return False
+        self.done = True
+        self.server.check(rc, "gp_serve_test")
+        return True
+
+    def wait(self, timeout=60.0):
+        """Block until done; returns (coords [nsamp, K], status [nsamp])."""
+        if not self.done:
+            rc = self.server.lib.gp_serve_wait(self.server.s, self.ticket, timeout)
+            if rc != GP_ERR_TIMEOUT:
+                self.done = True
+            self.server.check(rc, "gp_serve_wait")
+        return self.coords, self.status
+
+
+class Server:
+    """Projection server on the panel (SNP weights) resident in `handle` (gpupca_serve.h)."""
+
+    def __init__(self, handle, numeigs, max_batch=0, pool_samples=0, fp64_serial=False,
+                 eigscale=None):
+        self.lib = load_library()
+        self.K = numeigs
+        self._scale = None if eigscale is None else np.ascontiguousarray(eigscale, np.float64)
+        o = ServeOpts(numeigs, max_batch, pool_samples, int(fp64_serial),
+                      ptr(self._scale, C.c_double))
+        s = vp()
+        handle.check(self.lib.gp_serve_open(handle.h, C.byref(o), C.byref(s)), "gp_serve_open")
+        self.s = s
+        n, rb = C.c_int64(), C.c_int64()
+        self.check(self.lib.gp_serve_layout(self.s, C.byref(n), C.byref(rb)), "gp_serve_layout")
+        self.nsnp, self.row_bytes = n.value, rb.value
+        self.snp_index = np.zeros(self.nsnp, np.int32)
+        self.check(self.lib.gp_serve_panel_snps(self.s, ptr(self.snp_index, C.c_int32)),
+                   "gp_serve_panel_snps")
+
+    def check(self, rc, what):
+        if rc < 0:
+            msg = self.lib.gp_serve_last_error(self.s).decode(errors="replace")
+            raise GpuError("%s: %s: %s" % (what, GP_ERR.get(rc, rc), msg))
+        return rc
+
+    def submit(self, codes, coords=None, status=None):
+        """codes: uint8 [nsamp, row_bytes] request rows (see request_rows)."""
+        codes = np.ascontiguousarray(codes, dtype=np.uint8)
+        q = codes.shape[0]
+        assert codes.shape[1] == self.row_bytes
+        if coords is None:
+            coords = np.zeros((q, self.K))
+        if status is None:
+            status = np.zeros(q, np.int32)
+        t = C.c_int64()
+        self.check(self.lib.gp_serve_submit(self.s, ptr(codes, C.c_uint8), q,
+                                            ptr(coords, C.c_double), ptr(status, C.c_int32),
+                                            C.byref(t)), "gp_serve_submit")
+        return ServeRequest(self, t.value, codes, coords, status)
+
+    def pause(self, paused=True):
+        self.check(self.lib.gp_serve_pause(self.s, int(paused)), "gp_serve_pause")
+
+    def stats(self):
+        a, b, c = C.c_int64(), C.c_int64(), C.c_int64()
+        self.check(self.lib.gp_serve_stats(self.s, C.byref(a), C.byref(b), C.byref(c)),
+                   "gp_serve_stats")
+        return a.value, b.value, c.value
+
+    def close(self):
+        if self.s:
+            self.lib.gp_serve_close(self.s)
+            self.s = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def request_rows(records, nind, samples, snp_index, row_bytes):
+    """Request rows for `samples` from SNP-major packed records (packedancestrymap layout:
+    sample i of a record at byte i>>2, bits (3-(i&3))*2): one row per sample over the panel
+    SNPs snp_index, MSB first, padded with code 3."""
+    rec = np.asarray(records, dtype=np.uint8)[np.asarray(snp_index)]
+    samples = np.asarray(samples, dtype=np.int64)
+    g = (rec[:, samples >> 2] >> ((3 - (samples & 3)) * 2).astype(np.uint8)) & 3  # [nk, q]
+    q, nk = len(samples), len(snp_index)
+    codes = np.full((q, row_bytes * 4), 3, np.uint8)
+    codes[:, :nk] = g.T
+    c4 = codes.reshape(q, row_bytes, 4)
+    return ((c4[:, :, 0] << 6) | (c4[:, :, 1] << 4) | (c4[:, :, 2] << 2) | c4[:, :, 3]).astype(
+        np.uint8)
+
+
 def ridoutlier(evecs, neigs, thresh=6.0, mode=0):
     lib = load_library()
     E = np.ascontiguousarray(evecs, dtype=np.float64)
@@ -409,6 +541,27 @@ def synth_records(nsnp, pop_sizes, fst, miss=0.01, miss_hi=None, n_admixed=0, se
     if rc != 0:
         raise RuntimeError("gp_synth_records failed: %d" % rc)
     return rec, pop
+
+
+def synth_sample_rows(nsnp, pop_sizes, fst, snp_index, row_bytes, sample_seed, miss=0.01,
+                      miss_hi=None, n_admixed=0, seed=1, p_lo=0.05, p_hi=0.95, nthreads=None):
+    """New samples of the populations of synth_records(nsnp, pop_sizes, fst, seed=seed) as
+    request rows over the panel SNPs snp_index (uint8 [nind, row_bytes]) and their labels."""
+    s = load_synth()
+    ps = np.ascontiguousarray(pop_sizes, dtype=np.int32)
+    fs = np.ascontiguousarray(fst, dtype=np.float64)
+    nind = int(ps.sum()) + int(n_admixed)
+    spec = SynthSpec(nsnp, nind, len(ps), ptr(ps, C.c_int32), ptr(fs, C.c_double), p_lo, p_hi,
+                     miss, miss if miss_hi is None else miss_hi, seed)
+    idx = np.ascontiguousarray(snp_index, dtype=np.int64)
+    rows = np.empty((nind, row_bytes), np.uint8)
+    pop = np.zeros(nind, np.int32)
+    rc = s.gp_synth_sample_rows(C.byref(spec), sample_seed, ptr(idx, C.c_int64), len(idx),
+                                row_bytes, ptr(rows, C.c_uint8), ptr(pop, C.c_int32),
+                                nthreads or os.cpu_count() or 1)
+    if rc != 0:
+        raise RuntimeError("gp_synth_sample_rows failed: %d" % rc)
+    return rows, pop
 
 
 def synth_write_dataset(prefix, nsnp, pop_sizes, fst, miss=0.01, miss_hi=None, n_admixed=0,

@@ -23,13 +23,15 @@ ORACLE = os.path.join(ROOT, "oracle")
 ORACLE_BIN = os.path.join(ORACLE, "_bin")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
+NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
                      "-I" + os.path.join(ROOT, "include")]
 CUDA_SOURCES = ["gp_api.cu", "gp_geno.cu", "gp_gram_f64.cu", "gp_geno_gemm_f64.cu",
                 "gp_gram_bf16.cu", "gp_fast.cu",
                 "gp_noalloc.cu", "gp_geno_tc.cu", "gp_eig.cu", "gp_serve.cu"]
 HOST_LIB_SOURCES = ["gp_smartpca.c"]
-CFLAGS = ["-O2", "-fPIC", "-std=gnu11", "-Wall", "-Wno-unused-result",
+# no FMA contraction in host code: the reference's host arithmetic is plain multiply-add
+# (aarch64 would otherwise fuse it)
+CFLAGS = ["-O2", "-fPIC", "-std=gnu11", "-Wall", "-Wno-unused-result", "-ffp-contract=off",
           "-I" + os.path.join(ROOT, "include")]
 
 

@@ -4,10 +4,10 @@
  * src/eigensrc/eigx.c:97-117, but prints all eigenvalues and uses only the top vectors).
  *
  *   1. Householder tridiagonalisation A = Q T Q^T (cuSOLVER sytrd, lower);
- *   2. all eigenvalues of T by bisection on Sturm counts, one thread per eigenvalue index
- *      (the published bisection method: the count of negative pivots of the LDL^T
- *      factorisation of T - x I equals the number of eigenvalues below x): FP32 brackets
- *      first, checked and finished in FP64 to a few ulps;
+ *   2. all eigenvalues of T by multisection on Sturm counts (the published bisection method:
+ *      the count of negative pivots of the LDL^T factorisation of T - x I equals the number
+ *      of eigenvalues below x), several lanes per eigenvalue index: FP32 brackets first,
+ *      checked and finished in FP64 to 1e-13 ||T||;
  *   3. the top nvec eigenvectors of T by inverse iteration, one block per vector: LU with
  *      partial pivoting of the tridiagonal T - lambda I (Gaussian elimination with row
  *      interchanges) and three solves from a fixed pseudo-random start, then modified
@@ -24,29 +24,6 @@
 
 #include "gp_internal.h"
 
-
-/*
- * Number of eigenvalues of T (d, e2 = e^2) below x; pivmin guards tiny pivots.  Only the
- * signs of the pivots matter, so e2/q uses a reciprocal from the FP32 approximation with
- * one FP64 Newton step (relative error ~2^-46) instead of an IEEE FP64 division, whose
- * instruction sequence is long on this GPU's narrow FP64 pipe.
- */
-__device__ __forceinline__ int sturm_count(const double *d, const double *e2, int n, double x,
-                                           double pivmin)
-{
-  int cnt = 0;
-  double q = d[0] - x;
-  if (fabs(q) < pivmin) q = -pivmin;
-  if (q < 0.0) ++cnt;
-  for (int i = 1; i < n; ++i) {
-    double r = (double)__frcp_rn((float)q);
-    r = r * fma(-q, r, 2.0);
-    q = fma(-e2[i - 1], r, d[i] - x);
-    if (fabs(q) < pivmin) q = -pivmin;
-    if (q < 0.0) ++cnt;
-  }
-  return cnt;
-}
 
 /* the same count in FP32 (coarse brackets only; verified in FP64 afterwards) */
 __device__ __forceinline__ int sturm_count_f(const float *d, const float *e2, int n, float x,
@@ -65,14 +42,72 @@ __device__ __forceinline__ int sturm_count_f(const float *d, const float *e2, in
 }
 
 /*
- * w[k] = k-th smallest eigenvalue of T, one thread per k: bisection in FP32 to a bracket of
- * about 1e-6 of ||T|| (FP32 division is cheap on this GPU, FP64 is not), widened by a safety
- * margin and checked with two FP64 Sturm counts (back to the full Gershgorin bracket if the
- * check fails), then FP64 bisection to a few ulps.  d, e2 (and FP32 copies) are staged in
- * shared memory when they fit (dynamic smem = 24 n bytes), else read from global memory.
+ * 1/q to ~2^-44 relative with four integer-built pieces and two FP64 FMAs: the mantissa of q
+ * (truncated to 23 bits) is inverted by the FP32 approximate reciprocal, the exponent is
+ * negated in integer arithmetic, and one Newton step r = r0 + r0 (1 - q r0) refines it.
+ * Valid for normal q with |exponent| < 1000 (the Sturm pivots are clamped away from 0).
+ * GB300's FP64 pipe is narrow, so this keeps conversions and divisions off it.
  */
-__global__ void k_bisect_all(const double *gd, const double *ge2, int n, double gl, double gu,
-                             double tnorm, double pivmin, int use_smem, double *w)
+__device__ __forceinline__ double rcp_newton(double q)
+{
+  const unsigned long long qb = (unsigned long long)__double_as_longlong(q);
+  const unsigned hi = (unsigned)(qb >> 32);
+  const int e = (int)((hi >> 20) & 0x7FFu) - 1023;
+  const float f = __uint_as_float(0x3F800000u | (unsigned)((qb >> 29) & 0x7FFFFFull));
+  float rf;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(f));
+  const unsigned rb = __float_as_uint(rf);
+  const unsigned er = (unsigned)((int)(rb >> 23) - 127 - e + 1023);
+  const unsigned long long r0b =
+      ((unsigned long long)((hi & 0x80000000u) | (er << 20) | ((rb & 0x7FFFFFu) >> 3)) << 32) |
+      ((unsigned long long)(rb & 7u) << 29);
+  const double r0 = __longlong_as_double((long long)r0b);
+  return fma(r0, fma(-q, r0, 1.0), r0);
+}
+
+/*
+ * Sturm count with 4 FP64-pipe operations per step (d - x and three FMAs); the pivot clamp
+ * and the sign test work on the bit patterns.
+ */
+__device__ __forceinline__ int sturm_count_bits(const double *d, const double *e2, int n, double x,
+                                                double pivmin)
+{
+  const unsigned long long piv_bits = (unsigned long long)__double_as_longlong(pivmin);
+  const double negpiv = -pivmin;
+  int cnt = 0;
+  double q = d[0] - x;
+  unsigned long long qb = (unsigned long long)__double_as_longlong(q);
+  if ((qb & 0x7FFFFFFFFFFFFFFFull) < piv_bits) {
+    q = negpiv;
+    qb = (unsigned long long)__double_as_longlong(negpiv);
+  }
+  cnt += (int)(qb >> 63);
+  for (int i = 1; i < n; ++i) {
+    const double r = rcp_newton(q);
+    q = fma(-e2[i - 1], r, d[i] - x);
+    qb = (unsigned long long)__double_as_longlong(q);
+    if ((qb & 0x7FFFFFFFFFFFFFFFull) < piv_bits) {
+      q = negpiv;
+      qb = (unsigned long long)__double_as_longlong(negpiv);
+    }
+    cnt += (int)(qb >> 63);
+  }
+  return cnt;
+}
+
+/*
+ * All eigenvalues by multisection: a warp owns epw consecutive eigenvalue indices and each
+ * index gets P = 32/epw lanes (P >= 1), so every warp slot of the GPU has work whatever N is.
+ * A step evaluates P interior points of the bracket at once (one Sturm count per lane) and
+ * keeps the sub-interval where the count crosses k: log2(P+1) bits per step.  FP32 counts
+ * narrow the bracket to ~4e-7 ||T||, it is widened by 64 eps_32 ||T|| and checked with two
+ * FP64 counts (back to the Gershgorin bracket if the check fails), then FP64 counts narrow it
+ * to tol.  Grid: one CTA of 4 warps per SM; d, e2 and FP32 copies in shared memory
+ * (24 N bytes) when they fit.
+ */
+__global__ void __launch_bounds__(128)
+k_multisect(const double *gd, const double *ge2, int n, double gl, double gu, double tnorm,
+            double pivmin, double tol, int use_smem, int epw, int P, double *w)
 {
   extern __shared__ double sm[];
   const double *d = gd, *e2 = ge2;
@@ -94,38 +129,60 @@ __global__ void k_bisect_all(const double *gd, const double *ge2, int n, double 
     df = sdf;
     e2f = se2f;
   }
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int gwarp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int slot = lane / P, sub = lane - slot * P;
+  if (slot >= epw) return;
+  const int k = gwarp * epw + slot;
   if (k >= n) return;
+  const unsigned gmask = ((P == 32) ? 0xFFFFFFFFu : ((1u << P) - 1u)) << (slot * P);
+  const int gshift = slot * P;
+  const unsigned gbits = (P == 32) ? 0xFFFFFFFFu : ((1u << P) - 1u);
   double lo = gl, hi = gu;
   if (df) {
     float flo = (float)gl, fhi = (float)gu;
     const float fpiv = fmaxf((float)pivmin, 1e-30f) * 1e6f;
     const float ftol = 4e-7f * (float)tnorm;
-    for (int it = 0; it < 40 && fhi - flo > ftol; ++it) {
-      float mid = 0.5f * (flo + fhi);
-      if (mid <= flo || mid >= fhi) break;
-      if (sturm_count_f(df, e2f, n, mid, fpiv) > k)
-        fhi = mid;
-      else
-        flo = mid;
+    for (int it = 0; it < 64 && fhi - flo > ftol; ++it) {
+      const float wdt = fhi - flo;
+      const float x = flo + wdt * (float)(sub + 1) / (float)(P + 1);
+      const int flag = (x > flo && x < fhi) ? (sturm_count_f(df, e2f, n, x, fpiv) > k) : (x >= fhi);
+      const unsigned b = (__ballot_sync(gmask, flag) >> gshift) & gbits;
+      const int first = b ? __ffs(b) - 1 : P;
+      const float nlo = first == 0 ? flo : flo + wdt * (float)first / (float)(P + 1);
+      const float nhi = first == P ? fhi : flo + wdt * (float)(first + 1) / (float)(P + 1);
+      if (!(nhi - nlo < wdt)) break;
+      flo = nlo;
+      fhi = nhi;
     }
     const double margin = 64.0 * (double)FLT_EPSILON * tnorm;
     lo = fmax(gl, (double)flo - margin);
     hi = fmin(gu, (double)fhi + margin);
-    if (sturm_count(d, e2, n, lo, pivmin) > k || sturm_count(d, e2, n, hi, pivmin) <= k) {
+    int ok = 1;
+    if (sub < 2) {
+      const double x = sub == 0 ? lo : hi;
+      const int c = sturm_count_bits(d, e2, n, x, pivmin);
+      ok = sub == 0 ? (c <= k) : (c > k);
+    }
+    const unsigned bad = (__ballot_sync(gmask, !ok) >> gshift) & gbits;
+    if (bad) {
       lo = gl;
       hi = gu;
     }
   }
-  for (int it = 0; it < 80; ++it) {
-    double mid = 0.5 * (lo + hi);
-    if (mid <= lo || mid >= hi) break;
-    if (sturm_count(d, e2, n, mid, pivmin) > k)
-      hi = mid;
-    else
-      lo = mid;
+  for (int it = 0; it < 200 && hi - lo > tol; ++it) {
+    const double wdt = hi - lo;
+    const double x = lo + wdt * (double)(sub + 1) / (double)(P + 1);
+    const int flag = (x > lo && x < hi) ? (sturm_count_bits(d, e2, n, x, pivmin) > k) : (x >= hi);
+    const unsigned b = (__ballot_sync(gmask, flag) >> gshift) & gbits;
+    const int first = b ? __ffs(b) - 1 : P;
+    const double nlo = first == 0 ? lo : lo + wdt * (double)first / (double)(P + 1);
+    const double nhi = first == P ? hi : lo + wdt * (double)(first + 1) / (double)(P + 1);
+    if (!(nhi - nlo < wdt)) break;
+    lo = nlo;
+    hi = nhi;
   }
-  w[k] = 0.5 * (lo + hi);
+  if (sub == 0) w[k] = 0.5 * (lo + hi);
 }
 
 /* deterministic start vector entry in (-1, 1) */
@@ -347,13 +404,20 @@ int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, d
   {
     size_t smem = (size_t)24 * (size_t)n;
     int use_smem = smem <= 200 * 1024;
+    const int warps = ctx->num_sms * 4;
+    int epw = (n + warps - 1) / warps;
+    if (epw > 32) epw = 32;
+    const int P = 32 / epw;
+    const int nwarps = (n + epw - 1) / epw;
+    const int blocks = (nwarps + 3) / 4;
+    /* FP64 brackets end at 1e-13 ||T||: the counts' own backward error is ~6e-14 ||T|| */
+    const double tol = 1e-13 * tnorm;
     if (use_smem)
-      GP_CUDA(ctx, cudaFuncSetAttribute(k_bisect_all, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      GP_CUDA(ctx, cudaFuncSetAttribute(k_multisect, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)smem));
-    int threads = 64;
-    k_bisect_all<<<(n + threads - 1) / threads, threads, use_smem ? smem : 0, ctx->stream>>>(
-        d, e2, n, gl, gu, tnorm, pivmin, use_smem, w);
-    GP_LAUNCH_CHECK(ctx, "k_bisect_all");
+    k_multisect<<<blocks, 128, use_smem ? smem : 0, ctx->stream>>>(d, e2, n, gl, gu, tnorm, pivmin,
+                                                                   tol, use_smem, epw, P, w);
+    GP_LAUNCH_CHECK(ctx, "k_multisect");
   }
   k_reverse<<<(n + 255) / 256, 256, 0, ctx->stream>>>(w, d_evals_desc, n);
   GP_LAUNCH_CHECK(ctx, "k_reverse");

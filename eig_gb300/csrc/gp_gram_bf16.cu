@@ -14,7 +14,7 @@
  * tile is written out in FP64.
  *
  * Data layout in HBM: Xhi and Xlo as row-major [Npad][Kc] bf16 (samples x kept SNPs of the
- * current super-chunk), written by k_split_materialize from the packed records; the Gram
+ * current super-chunk), written by k_split_transpose from the packed records; the Gram
  * kernel reads them with TMA as 128-row x 64-SNP boxes in the 128-byte swizzle.
  *
  * Kernel structure (persistent, one CTA per SM, 18 warps):
@@ -334,39 +334,83 @@ __global__ void k_split_tables(const int32_t *kept, int32_t nkept, const double 
 }
 
 /*
- * Xhi/Xlo [npad][kc] for kept columns [k0, k0 + kc): thread = (row, 8 consecutive SNPs) ->
- * two 16-byte stores.  Rows >= nrows and columns >= nkept are zero.
+ * Xhi/Xlo [npad][kc] for kept columns [k0, k0 + kc), rows >= nrows and columns >= nkept zero,
+ * tile by tile through shared memory (a transpose of the SNP-major records):
+ * CTA (kt, rt) covers 64 kept SNPs x 256 output rows.  When the tile's samples span at most
+ * 256 record bytes (always when the rows are all samples or a subset with few gaps) the 64
+ * records' byte ranges are read once, coalesced, into shared memory; each thread then writes
+ * whole 16-byte groups so that a warp stores four 128-byte row segments.  Wider spans (sparse
+ * sample subsets) read the bytes from global memory per thread.
  */
-__global__ void k_split_materialize(const uint8_t *__restrict__ geno, int64_t rlen,
-                                    const int32_t *__restrict__ rows, int32_t nrows,
-                                    const int32_t *__restrict__ cols, const int32_t *__restrict__ kept,
-                                    int32_t nkept, const uint32_t *__restrict__ split, int32_t k0,
-                                    int32_t kc, int32_t npad, __nv_bfloat16 *xhi, __nv_bfloat16 *xlo)
+#define MT_SNP 64
+#define MT_ROWS 256
+#define MT_SPAN 256
+#define MT_PITCH_W (MT_SPAN / 4 + 1) /* 65 words: rows one bank apart */
+__global__ void __launch_bounds__(256)
+k_split_transpose(const uint8_t *__restrict__ geno, int64_t rlen, const int32_t *__restrict__ rows,
+                  int32_t nrows, const int32_t *__restrict__ cols, const int32_t *__restrict__ kept,
+                  int32_t nkept, const uint32_t *__restrict__ split, int32_t k0, int32_t kc,
+                  int32_t npad, __nv_bfloat16 *xhi, __nv_bfloat16 *xlo)
 {
-  const int32_t groups = kc / 8;
-  int64_t total = (int64_t)npad * groups;
-  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
-       idx += (int64_t)gridDim.x * blockDim.x) {
-    int32_t r = (int32_t)(idx / groups), gq = (int32_t)(idx - (int64_t)r * groups);
+  __shared__ uint32_t srec[MT_SNP][MT_PITCH_W];
+  __shared__ uint32_t stab[MT_SNP][4];
+  __shared__ int64_t srecoff[MT_SNP];
+  const int tid = threadIdx.x;
+  const int32_t kt = blockIdx.x, r0 = blockIdx.y * MT_ROWS;
+  const int32_t kbase = k0 + kt * MT_SNP;
+  int32_t base = 0, span = 0;
+  if (r0 < nrows) {
+    const int32_t rl = (r0 + MT_ROWS < nrows ? r0 + MT_ROWS : nrows) - 1;
+    base = (rows[r0] >> 2) & ~15;
+    span = (rows[rl] >> 2) - base + 1;
+  }
+  const bool fast = span <= MT_SPAN;
+  if (tid < MT_SNP) {
+    const int32_t k = kbase + tid;
+    srecoff[tid] = k < nkept ? (int64_t)cols[kept[k]] * rlen : -1;
+  }
+  {
+    const int u = tid >> 2, g = tid & 3;
+    const int32_t k = kbase + u;
+    stab[u][g] = k < nkept ? __ldg(split + 4 * k + g) : 0u;
+  }
+  __syncthreads();
+  if (fast && span > 0) {
+    const int nvec = (span + 15) >> 4;
+    for (int i = tid; i < MT_SNP * nvec; i += blockDim.x) {
+      const int u = i / nvec, v = i - u * nvec;
+      uint4 val = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
+      if (srecoff[u] >= 0) val = __ldg((const uint4 *)(geno + srecoff[u] + base + 16 * v));
+      srec[u][4 * v] = val.x;
+      srec[u][4 * v + 1] = val.y;
+      srec[u][4 * v + 2] = val.z;
+      srec[u][4 * v + 3] = val.w;
+    }
+  }
+  __syncthreads();
+  const int g8 = tid & 7, rsub = tid >> 3;
+#pragma unroll 1
+  for (int i = 0; i < MT_ROWS / 32; ++i) {
+    const int32_t r = r0 + rsub + 32 * i;
+    if (r >= npad) break;
     uint32_t hv[4] = {0, 0, 0, 0}, lv[4] = {0, 0, 0, 0};
     if (r < nrows) {
-      int32_t sidx = rows[r];
-      int32_t byte = sidx >> 2, sh = (3 - (sidx & 3)) * 2;
+      const int32_t sidx = rows[r];
+      const int32_t b = (sidx >> 2) - base, sh = (3 - (sidx & 3)) * 2;
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
-        int32_t k = k0 + gq * 8 + u;
-        uint32_t pair = 0;
-        if (k < nkept) {
-          int32_t c = kept[k];
-          uint32_t code = (__ldg(geno + (int64_t)cols[c] * rlen + byte) >> sh) & 3u;
-          pair = __ldg(split + 4 * k + code);
-        }
-        uint32_t h = pair & 0xFFFFu, l = pair >> 16;
-        hv[u >> 1] |= h << ((u & 1) * 16);
-        lv[u >> 1] |= l << ((u & 1) * 16);
+        const int uu = g8 * 8 + u;
+        uint32_t byte;
+        if (fast)
+          byte = (srec[uu][b >> 2] >> ((b & 3) * 8)) & 0xFFu;
+        else
+          byte = srecoff[uu] >= 0 ? __ldg(geno + srecoff[uu] + (sidx >> 2)) : 0xFFu;
+        const uint32_t pair = stab[uu][(byte >> sh) & 3u];
+        hv[u >> 1] |= (pair & 0xFFFFu) << ((u & 1) * 16);
+        lv[u >> 1] |= (pair >> 16) << ((u & 1) * 16);
       }
     }
-    int64_t off = (int64_t)r * kc + gq * 8;
+    const int64_t off = (int64_t)r * kc + (int64_t)kt * MT_SNP + g8 * 8;
     *(uint4 *)(xhi + off) = make_uint4(hv[0], hv[1], hv[2], hv[3]);
     *(uint4 *)(xlo + off) = make_uint4(lv[0], lv[1], lv[2], lv[3]);
   }
@@ -466,14 +510,12 @@ int gp_gram_split(gp_ctx *ctx, int precision)
   int grid = ctx->num_sms < ntiles ? ctx->num_sms : ntiles;
   for (int32_t k0 = 0; k0 < kpad; k0 += kc) {
     int32_t kcur = kpad - k0 < kc ? kpad - k0 : kc;
-    int64_t work = (int64_t)npad * (kc / 8);
-    int blocks = (int)((work + 255) / 256);
-    if (blocks > ctx->num_sms * 32) blocks = ctx->num_sms * 32;
     /* columns beyond kcur in this super-chunk are zero (k >= nkept guard covers the tail) */
-    k_split_materialize<<<blocks, 256, 0, ctx->stream>>>(ctx->d_geno, ctx->rlen_dev, ctx->d_rows, n,
-                                                         ctx->d_cols, ctx->d_kept, nk, split, k0, kc,
-                                                         npad, xhi, xlo);
-    GP_LAUNCH_CHECK(ctx, "k_split_materialize");
+    dim3 tgrid((unsigned)(kc / MT_SNP), (unsigned)((npad + MT_ROWS - 1) / MT_ROWS));
+    k_split_transpose<<<tgrid, 256, 0, ctx->stream>>>(ctx->d_geno, ctx->rlen_dev, ctx->d_rows, n,
+                                                      ctx->d_cols, ctx->d_kept, nk, split, k0, kc,
+                                                      npad, xhi, xlo);
+    GP_LAUNCH_CHECK(ctx, "k_split_transpose");
     int32_t nkb = kcur / BK;
     kern<<<grid, GRAM_THREADS, GRAM_SMEM, ctx->stream>>>(
         mhi, mlo, ntiles, nkb, chunk_kb, ctx->d_xtx, n, k0 > 0 ? 1 : 0, d_err);

@@ -467,3 +467,68 @@ int gp_read_genotypes(const char *path, const gp_snplist *s, const gp_indlist *i
   *rec_bytes = rlen;
   return 0;
 }
+
+/* ---- GRM dump ----------------------------------------------------------------------- */
+
+int gp_write_grm(const char *name, int binary, const double *xtx, int32_t n, int32_t numsnps,
+                 char (*ids)[GP_IDLEN], const int32_t *xindex, char *err, int errlen)
+{
+  char path[4096];
+  snprintf(path, sizeof path, "%s.id", name);
+  FILE *f = fopen(path, "w");
+  if (!f) {
+    snprintf(err, (size_t)errlen, "cannot write %s", path);
+    return -1;
+  }
+  for (int32_t a = 0; a < n; ++a) fprintf(f, "%s\t%s\n", "NA", ids[xindex[a]]);
+  fclose(f);
+  /* the PCA's scaling, with the reference's operation order: trace as a running sum of the
+   * diagonal, then XTX *= 1/y with y = trace/(n-1) */
+  double tr = 0.0;
+  for (int32_t a = 0; a < n; ++a) tr += xtx[(size_t)a * n + a];
+  const double ys = 1.0 / (tr / (double)(n - 1));
+  if (binary) {
+    snprintf(path, sizeof path, "%s.N.bin", name);
+    f = fopen(path, "wb");
+    if (!f) {
+      snprintf(err, (size_t)errlen, "cannot write %s", path);
+      return -1;
+    }
+    int32_t w = numsnps;
+    const int64_t nout = (int64_t)n * (n + 1) / 2;
+    for (int64_t i = 0; i < nout; ++i) fwrite(&w, 4, 1, f);
+    fclose(f);
+    double ts = 0.0;
+    for (int32_t a = 0; a < n; ++a) ts += xtx[(size_t)a * n + a] * ys;
+    const double ynorm = ts / (double)n;
+    snprintf(path, sizeof path, "%s.bin", name);
+    f = fopen(path, "wb");
+    if (!f) {
+      snprintf(err, (size_t)errlen, "cannot write %s", path);
+      return -1;
+    }
+    for (int32_t a = 0; a < n; ++a)
+      for (int32_t b = 0; b <= a; ++b) {
+        float y = (float)(xtx[(size_t)a * n + b] * ys / ynorm);
+        fwrite(&y, 4, 1, f);
+      }
+    fclose(f);
+    return 0;
+  }
+  double ds = 0.0;
+  for (int32_t a = 0; a < n; ++a) ds += xtx[(size_t)a * n + a] * ys;
+  const double recip = (double)n / ds;
+  f = fopen(name, "w");
+  if (!f) {
+    snprintf(err, (size_t)errlen, "cannot write %s", name);
+    return -1;
+  }
+  for (int32_t a = 0; a < n; ++a)
+    for (int32_t b = 0; b <= a; ++b) {
+      fprintf(f, "%d %d ", a + 1, b + 1);
+      fprintf(f, "%d ", numsnps);
+      fprintf(f, "%0.6f\n", xtx[(size_t)a * n + b] * ys * recip);
+    }
+  fclose(f);
+  return 0;
+}

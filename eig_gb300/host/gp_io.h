@@ -50,4 +50,14 @@ int gp_read_genotypes(const char *path, const gp_snplist *s, const gp_indlist *i
                       int hashcheck, uint8_t **out_records, int64_t *rec_bytes, int32_t *code,
                       char *err, int errlen);
 
+/*
+ * GRM dump of the last pass (dumpgrm/dumpgrmbin/dumpgrmid src/eigensrc/smartpca.c:3687-3808)
+ * from the unscaled XTX (n x n, row-major): the Gram is first scaled by (n-1)/trace as the
+ * PCA does (:1230-1236), then written as GCTA text "i j numsnps value" (lower triangle,
+ * value = XTX * n / sum(diag)) or, with binary = 1, as name.bin (float, XTX / (trace/n)) and
+ * name.N.bin (int32 numsnps, n(n+1)/2 times); name.id gets "NA\tID" per row.
+ */
+int gp_write_grm(const char *name, int binary, const double *xtx, int32_t n, int32_t numsnps,
+                 char (*ids)[GP_IDLEN], const int32_t *xindex, char *err, int errlen);
+
 #endif

@@ -86,6 +86,7 @@ int gp_smartpca_run(gp_ctx *ctx, const gp_smartpca_opts *o, const gp_panel *p,
   r->npasses = 0;
   r->gram_flops = 0.0;
   r->gram_ms = 0.0;
+  r->nused = 0;
   if (!ctx || !o || !p || !r || M < 1 || N < 1) return GP_ERR_ARG;
 
   snp_ign = (uint8_t *)calloc((size_t)M, 1);
@@ -260,8 +261,9 @@ int gp_smartpca_run(gp_ctx *ctx, const gp_smartpca_opts *o, const gp_panel *p,
     if (rc) goto done;
     double trace;
     int32_t nused;
-    rc = gp_xtx(ctx, &xo, NULL, NULL, NULL, kill, NULL, NULL, NULL, &trace, &nused);
+    rc = gp_xtx(ctx, &xo, NULL, NULL, NULL, kill, NULL, NULL, r->xtx, &trace, &nused);
     if (rc) goto done;
+    r->nused = nused;
     {
       double gms = 0.0, gfl = 0.0;
       gp_last_gram_time(ctx, &gms, NULL, &gfl);

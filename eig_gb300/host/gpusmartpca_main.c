@@ -55,8 +55,10 @@ int main(int argc, char **argv)
   gp_smartpca_opts o;
   gp_smartpca_defaults(&o);
   const char *genotypename = NULL, *snpname = NULL, *indivname = NULL, *evecout = NULL,
-             *evalout = NULL, *outlierout = NULL, *poplistname = NULL, *prec = NULL;
-  int32_t hiprec = 0, familynames = 1, hashcheck = 1, t = 0, xdata = -1, seed = 0;
+             *evalout = NULL, *outlierout = NULL, *poplistname = NULL, *prec = NULL,
+             *grmout = NULL;
+  int32_t hiprec = 0, familynames = 1, hashcheck = 1, t = 0, xdata = -1, seed = 0,
+          grmbinary = 0;
   gp_par_str(&pf, "genotypename:", &genotypename);
   gp_par_str(&pf, "snpname:", &snpname);
   gp_par_str(&pf, "indivname:", &indivname);
@@ -69,6 +71,8 @@ int main(int argc, char **argv)
   gp_par_str(&pf, "outliername:", &outlierout);
   gp_par_str(&pf, "outlieroutname:", &outlierout);
   gp_par_str(&pf, "gpuprecision:", &prec);
+  gp_par_str(&pf, "grmoutname:", &grmout);
+  gp_par_int(&pf, "grmbinary:", &grmbinary);
   gp_par_int(&pf, "numeigs:", &o.numeigs);
   gp_par_int(&pf, "numoutevec:", &o.numeigs);
   gp_par_int(&pf, "fancynorm:", &o.fancynorm);
@@ -193,6 +197,13 @@ int main(int argc, char **argv)
   r.outlier_iter = (int32_t *)calloc((size_t)N, sizeof(int32_t));
   r.outlier_vec = (int32_t *)calloc((size_t)N, sizeof(int32_t));
   r.outlier_score = (double *)calloc((size_t)N, sizeof(double));
+  if (grmout && !o.fastmode) {
+    r.xtx = (double *)malloc(sizeof(double) * (size_t)N * N);
+    if (!r.xtx) {
+      fprintf(stderr, "no memory for the GRM (%d samples)\n", N);
+      return 1;
+    }
+  }
 
   gp_ctx *ctx = NULL;
   int rc = gp_open(0, &ctx);
@@ -217,6 +228,16 @@ int main(int argc, char **argv)
             r.outlier_iter[i], r.outlier_vec[i], r.outlier_score[i], inds.pop[k]);
   }
   if (ol && ol != stdout) fclose(ol);
+
+  if (r.xtx) {
+    /* dumpgrm (smartpca.c:1297): the last pass's Gram in xindex order */
+    if (gp_write_grm(grmout, grmbinary, r.xtx, r.nrows, r.nused, inds.id, r.xindex, err,
+                     (int)sizeof err)) {
+      fprintf(stderr, "%s\n", err);
+      return 1;
+    }
+    printf("grm dumped\n");
+  }
 
   int32_t nK = r.numeigs;
   if (evalout && !o.fastmode) {

@@ -77,7 +77,7 @@ class RunResult(C.Structure):
                 ("nrows", C.c_int32), ("ncols", C.c_int32), ("numeigs", C.c_int32),
                 ("noutliers", C.c_int32), ("npasses", C.c_int32),
                 ("t_phase", C.c_double * 8), ("gram_flops", C.c_double),
-                ("gram_ms", C.c_double)]
+                ("gram_ms", C.c_double), ("xtx", f64p), ("nused", C.c_int32)]
 
 
 _lib = None
@@ -468,7 +468,8 @@ def default_opts(**kw):
 
 
 def smartpca_run(handle, records, nind, opts, code=GP_CODE_PACKED, snp_chrom=None,
-                 snp_ignore=None, ind_ignore=None, ind_affstatus=None, ind_male=None):
+                 snp_ignore=None, ind_ignore=None, ind_affstatus=None, ind_male=None,
+                 want_xtx=False):
     """Run the whole smartpca hot path (gp_smartpca_run) on in-memory records."""
     lib = handle.lib
     keep = []
@@ -501,6 +502,9 @@ def smartpca_run(handle, records, nind, opts, code=GP_CODE_PACKED, snp_chrom=Non
                   ptr(out["ind_out"], C.c_uint8), ptr(out["snp_state"], C.c_uint8),
                   ptr(out["outlier_idx"], C.c_int32), ptr(out["outlier_iter"], C.c_int32),
                   ptr(out["outlier_vec"], C.c_int32), ptr(out["outlier_score"], C.c_double))
+    if want_xtx:
+        out["xtx"] = np.zeros(nind * nind)
+        r.xtx = ptr(out["xtx"], C.c_double)
     handle.check(lib.gp_smartpca_run(handle.h, C.byref(opts), C.byref(p), C.byref(r)),
                  "gp_smartpca_run")
     n, k = r.nrows, r.numeigs
@@ -514,7 +518,9 @@ def smartpca_run(handle, records, nind, opts, code=GP_CODE_PACKED, snp_chrom=Non
                           int(out["outlier_vec"][i]), float(out["outlier_score"][i]))
                          for i in range(min(r.noutliers, nind))],
                t_phase={PHASES[i]: r.t_phase[i] for i in range(8)},
-               gram_flops=r.gram_flops, gram_ms=r.gram_ms)
+               gram_flops=r.gram_flops, gram_ms=r.gram_ms, nused=r.nused)
+    if want_xtx:
+        res["xtx"] = out["xtx"][: n * n].reshape(n, n).copy()
     return res
 
 

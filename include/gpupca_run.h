@@ -79,6 +79,10 @@ typedef struct {
   double t_phase[8];       /* wall seconds per GP_PH_* phase */
   double gram_flops;       /* algorithmic Gram flops, sum over passes of N_p (N_p+1) M_p */
   double gram_ms;          /* device time of the Gram kernels, sum over passes */
+  /* optional (zero-initialise the struct when unused) */
+  double *xtx;             /* [nind*nind] or NULL: the last pass's unscaled XTX, nrows x nrows
+                              row-major in xindex order (for the GRM dump, smartpca.c:1297) */
+  int32_t nused;           /* SNPs in the last pass's Gram (ynumsnps, smartpca.c:1172-1181) */
 } gp_run_result;
 
 void gp_smartpca_defaults(gp_smartpca_opts *o);

@@ -258,7 +258,36 @@ def smartpca(records, nind, numeigs=10, numoutliter=5, numoutleigs=10, outlthres
                 coords[j, proj] = scale * a[j]
         out = ~ind_ign
     return dict(evals=evals, evecs=evecs[:K], xindex=xindex, coords=coords, ind_out=out,
-                outliers=outliers, ncols=len(cols), nrows=n, numeigs=K, snp_state=snp_ign)
+                outliers=outliers, ncols=len(cols), nrows=n, numeigs=K, snp_state=snp_ign,
+                xtx=X, nused=int((s.killed == 0).sum()))
+
+
+def grm(X):
+    """The GRM dump of the last pass (dumpgrm / dumpgrmbin, src/eigensrc/smartpca.c:3770-3808,
+    :3705-3767) from the unscaled Gram X: the PCA scaling XTX *= 1/(trace/(n-1)) (:1230-1236),
+    then text values XTX * n/sum(diag) and binary float values XTX / (trace/n), lower
+    triangle row by row, with the reference's sequential sums.  Returns (text, binary)."""
+    n = X.shape[0]
+    tr = 0.0
+    for a in range(n):
+        tr += X[a, a]
+    ys = 1.0 / (tr / (n - 1))
+    Xs = X * ys
+    ds = 0.0
+    for a in range(n):
+        ds += Xs[a, a]
+    recip = n / ds
+    ynorm = ds / n
+    il = np.tril_indices(n)
+    return Xs[il] * recip, (Xs[il] / ynorm).astype(np.float32)
+
+
+def grm_text_lines(X, numsnps):
+    """dumpgrm text lines "a b numsnps %0.6f" (smartpca.c:3797-3804)"""
+    n = X.shape[0]
+    txt, _ = grm(X)
+    il = np.tril_indices(n)
+    return ["%d %d %d %0.6f" % (a + 1, b + 1, numsnps, v) for a, b, v in zip(il[0], il[1], txt)]
 
 
 def fastpca(records, cols, xindex, K, L, I, omega, fancynorm=1, altnormstyle=1):

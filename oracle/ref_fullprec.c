@@ -2,8 +2,9 @@
  * -Wl,--wrap=fprintf so every fprintf lands here.  By default the call is passed through
  * unchanged.  With EIG_REF_FULLPREC=1 the number formats of the .eval file
  * (src/eigensrc/smartpca.c:1428 "%12.6f\n"), the .evec header (:1435 "%9.3f ") and the
- * .evec coordinates (:1584-1585 "%10.4f  " / "%12.6f  ") are printed as %.17g, so that the
- * reference's own results can be compared at 1e-10 instead of at 6 printed decimals. */
+ * .evec coordinates (:1584-1585 "%10.4f  " / "%12.6f  ") and the GRM text values
+ * (:3803 "%0.6f\n") are printed as %.17g, so that the reference's own results can be
+ * compared at 1e-10 instead of at 6 printed decimals. */
 #include <stdarg.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -25,7 +26,7 @@ int __wrap_fprintf(FILE *f, const char *fmt, ...)
   va_list ap;
   int r;
   if (fullprec_mode()) {
-    if (strcmp(fmt, "%12.6f\n") == 0)
+    if (strcmp(fmt, "%12.6f\n") == 0 || strcmp(fmt, "%0.6f\n") == 0)
       use = "%.17g\n";
     else if (strcmp(fmt, "%10.4f  ") == 0 || strcmp(fmt, "%12.6f  ") == 0)
       use = "%.17g  ";

@@ -10,6 +10,7 @@ EIG_REF_FULLPREC=1 prints .eval/.evec numbers as %.17g).  Writes, per case:
   <case>/ref.eval.txt, ref.evec.txt       reference outputs in the shipped text formats
   <case>/ref.outliers                     the reference's outlier-removal lines
   <case>/ref.log                          the reference's log
+  <case>/ref.grm[.txt], ref.grm.id, ref.grm.bin, ref.grm.N.bin   GRM dumps (grm cases)
 
 and copies the reference's own example fixtures (CONVERTF/example.*,
 EIGENSTRAT/example.*) into ref_examples/.  Usage:
@@ -47,6 +48,11 @@ CASES = {
                        miss_hi=0.97, n_admixed=20, seed=13, fmt="packed",
                        par={"numoutevec": "5", "numoutlieriter": "0",
                             "poplistname": "poplist"}, poplist=["POP0", "POP1"]),
+    # GRM dump (grmoutname) of the last pass after outlier removal, text and binary
+    "bn_grm": dict(nsnp=2500, pops=[24, 24, 20, 1, 1], fst=[0.01, 0.02, 0.03, 0.3, 0.3],
+                   miss=0.02, seed=14, fmt="packed",
+                   par={"numoutevec": "4", "numoutlieriter": "3", "grmoutname": "out.grm"},
+                   grm=True),
 }
 
 
@@ -97,10 +103,23 @@ def make_case(name, spec):
     with open(os.path.join(d, "par"), "w") as f:
         for k, v in par.items():
             f.write("%s: %s\n" % (k, v))
-    run_reference(d)
+    run_reference(d, spec.get("grm", False))
+    if spec.get("grm"):
+        # the binary GRM from a second run of the same parfile with grmbinary: YES
+        with open(os.path.join(d, "par_bin"), "w") as f:
+            for k, v in par.items():
+                f.write("%s: %s\n" % (k, v))
+            f.write("grmbinary: YES\n")
+        with open(os.path.join(d, "ref_bin.log"), "w") as log:
+            subprocess.run([REF_BIN, "-p", "par_bin"], cwd=d, stdout=log,
+                           stderr=subprocess.STDOUT, check=True)
+        for ext in (".bin", ".N.bin"):
+            shutil.move(os.path.join(d, "out.grm" + ext), os.path.join(d, "ref.grm" + ext))
+        for n in ("out.eval", "out.evec", "out.outliers", "out.grm.id"):
+            os.remove(os.path.join(d, n))
 
 
-def run_reference(d):
+def run_reference(d, grm=False):
     env = dict(os.environ)
     for prec, suffix in ((False, ".txt"), (True, "")):
         env["EIG_REF_FULLPREC"] = "1" if prec else "0"
@@ -110,6 +129,9 @@ def run_reference(d):
         shutil.move(os.path.join(d, "out.eval"), os.path.join(d, "ref.eval" + suffix))
         shutil.move(os.path.join(d, "out.evec"), os.path.join(d, "ref.evec" + suffix))
         shutil.move(os.path.join(d, "out.outliers"), os.path.join(d, "ref.outliers"))
+        if grm:
+            shutil.move(os.path.join(d, "out.grm"), os.path.join(d, "ref.grm" + suffix))
+            shutil.move(os.path.join(d, "out.grm.id"), os.path.join(d, "ref.grm.id"))
 
 
 def copy_examples(ref_root):
@@ -131,6 +153,9 @@ if __name__ == "__main__":
     if not os.path.exists(REF_BIN):
         raise SystemExit("build the reference first: sh oracle/build_ref.sh")
     copy_examples(ref_root)
+    only = sys.argv[2:]  # optional case names
     for name, spec in CASES.items():
+        if only and name not in only:
+            continue
         make_case(name, spec)
         print("made", name)

@@ -4,7 +4,7 @@ import os
 import numpy as np
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = ["bn_outliers", "bn_bed_altnorm", "bn_project"]
+CASES = ["bn_outliers", "bn_bed_altnorm", "bn_project", "bn_grm"]
 
 
 def read_par(case):
@@ -99,3 +99,39 @@ def compare_coords(ref, mine, K, tol):
     err = np.max(np.abs(A - B * s))
     assert err < tol, "coordinate error %g" % err
     return err
+
+
+class Grm:
+    """The reference's GRM dump of a grm case: full-precision text values, the shipped text
+    lines, the binary floats and counts, the id lines."""
+
+    def __init__(self, case):
+        d = os.path.join(GOLDEN, case)
+        full = np.loadtxt(os.path.join(d, "ref.grm"))
+        self.ij = full[:, :2].astype(np.int64)
+        self.numsnps = full[:, 2].astype(np.int64)
+        self.values = full[:, 3]
+        self.text = open(os.path.join(d, "ref.grm.txt")).read().splitlines()
+        self.bin = np.fromfile(os.path.join(d, "ref.grm.bin"), np.float32)
+        self.nbin = np.fromfile(os.path.join(d, "ref.grm.N.bin"), np.int32)
+        self.ids = open(os.path.join(d, "ref.grm.id")).read().splitlines()
+
+
+def float_ulps(a, b):
+    """distance in float32 units in the last place"""
+    ia = np.asarray(a, np.float32).view(np.int32).astype(np.int64)
+    ib = np.asarray(b, np.float32).view(np.int32).astype(np.int64)
+    return np.abs(ia - ib)
+
+
+def compare_grm_text(lines, ref_lines, values, ref_values):
+    """same pairs and counts; values within 1e-10 of the reference; printed lines identical
+    except where a value sits on a rounding boundary of %0.6f"""
+    assert len(lines) == len(ref_lines)
+    diff = [i for i, (a, b) in enumerate(zip(lines, ref_lines)) if a != b]
+    for i in diff:
+        a, b = lines[i].split(), ref_lines[i].split()
+        assert a[:3] == b[:3]
+        assert abs(float(a[3]) - float(b[3])) <= 1.0000001e-6
+    assert len(diff) <= max(1, len(lines) // 10000)
+    assert np.max(np.abs(np.asarray(values) - ref_values)) <= 1e-10 * np.max(np.abs(ref_values))

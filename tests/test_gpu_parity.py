@@ -198,6 +198,47 @@ def test_cli_dropin_matches_reference_text(case, tmp_path):
         assert g[8].lstrip("-") == x[8].lstrip("-")
 
 
+@pytest.mark.parametrize("binary", [False, True])
+def test_cli_grm_dump_matches_reference(binary, tmp_path):
+    """grmoutname (and grmbinary): the last pass's GRM after outlier removal, as text
+    (values within 1e-10 at full precision, printed lines identical up to %0.6f rounding
+    boundaries) or float binary (within 1 ulp), with the reference's id and count files."""
+    import shutil
+
+    from tests.goldens import Grm, compare_grm_text, float_ulps
+    c = Case("bn_grm")
+    d = tmp_path / "bn_grm"
+    shutil.copytree(c.dir, d)
+    cli = os.path.join(native.LIB_DIR, "gpusmartpca")
+    out = subprocess.run([cli, "-p", "par_bin" if binary else "par"], cwd=d, capture_output=True,
+                         text=True)
+    assert out.returncode == 0, out.stderr + out.stdout
+    g = Grm("bn_grm")
+    assert open(d / "out.grm.id").read().splitlines() == g.ids
+    if binary:
+        assert np.array_equal(np.fromfile(d / "out.grm.N.bin", np.int32), g.nbin)
+        assert np.max(float_ulps(np.fromfile(d / "out.grm.bin", np.float32), g.bin)) <= 1
+    else:
+        lines = open(d / "out.grm").read().splitlines()
+        vals = [float(l.split()[3]) for l in lines]
+        # the printed values carry 6 decimals; the full-precision check is the run's XTX below
+        compare_grm_text(lines, g.text, g.values, g.values)
+        assert np.max(np.abs(np.array(vals) - g.values)) <= 5.0000001e-7
+
+
+def test_smartpca_run_grm_values_full_precision(gpu):
+    """the last pass's XTX returned by gp_smartpca_run gives the reference's GRM values
+    within 1e-10 (relative to the largest)"""
+    from tests.goldens import Grm
+    c = Case("bn_grm")
+    opts = native.default_opts(**c.opts())
+    r = native.smartpca_run(gpu, c.records, c.nind, opts, code=c.code, want_xtx=True)
+    g = Grm("bn_grm")
+    txt, binv = O.grm(r["xtx"])
+    assert r["nused"] == g.numsnps[0]
+    assert np.max(np.abs(txt - g.values)) <= 1e-10 * np.max(np.abs(g.values))
+
+
 def _gram_pair(gpu, rec, nind, rows, cols, precision):
     gpu.load_genotypes(rec, nind)
     gpu.set_samples(rows)
@@ -245,12 +286,21 @@ def test_split_multi_tile_chunks_and_superchunks(gpu, monkeypatch, prec):
 
 
 @pytest.mark.parametrize("prec", list(SPLIT_TOL))
-def test_split_subset_rows(gpu, prec):
-    """row subsets (outlier removal) and killed columns through the split path"""
-    rec, pop = synth(4000, [200, 200, 150], [0.01, 0.02, 0.05], miss=0.05, seed=33)
-    nind = len(pop)
-    rng = np.random.default_rng(4)
-    rows = np.sort(rng.choice(nind, 401, replace=False)).astype(np.int32)
+@pytest.mark.parametrize("density", ["dense", "sparse"])
+def test_split_subset_rows(gpu, prec, density):
+    """row subsets (outlier removal) and killed columns through the split path; the sparse
+    subset (every 6th sample) spans more record bytes per 256-row tile than the shared-memory
+    transpose stages, so it takes the per-thread path"""
+    if density == "dense":
+        rec, pop = synth(4000, [200, 200, 150], [0.01, 0.02, 0.05], miss=0.05, seed=33)
+        nind = len(pop)
+        rng = np.random.default_rng(4)
+        rows = np.sort(rng.choice(nind, 401, replace=False)).astype(np.int32)
+    else:
+        rec, pop = synth(4000, [1200, 1000, 800], [0.01, 0.02, 0.05], miss=0.05, seed=33)
+        nind = len(pop)
+        rng = np.random.default_rng(4)
+        rows = np.arange(1, nind, 6, dtype=np.int32)
     cols = np.sort(rng.choice(4000, 3333, replace=False)).astype(np.int32)
     gpu.load_genotypes(rec, nind)
     gpu.set_samples(rows)

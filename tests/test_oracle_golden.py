@@ -66,3 +66,19 @@ def test_lookup_gram_equals_plain(case):
     a = O.gram(s)
     b = O.gram(s, lookup=True, nthreads=3)
     assert np.max(np.abs(a - b)) <= 1e-12 * np.max(np.abs(a))
+
+
+def test_oracle_grm_matches_reference():
+    """GRM dump (dumpgrm/dumpgrmbin) of the oracle's last-pass Gram against the reference's
+    text, binary and id files"""
+    from tests.goldens import Grm, compare_grm_text, float_ulps
+    c = Case("bn_grm")
+    r = O.smartpca(c.packed_records(), c.nind, ind_affstatus=c.affstatus, **c.opts())
+    g = Grm("bn_grm")
+    txt, binv = O.grm(r["xtx"])
+    lines = O.grm_text_lines(r["xtx"], r["nused"])
+    assert np.all(g.numsnps == r["nused"]) and np.all(g.nbin == r["nused"])
+    assert len(g.nbin) == len(binv)
+    compare_grm_text(lines, g.text, txt, g.values)
+    assert np.max(float_ulps(binv, g.bin)) <= 1
+    assert g.ids == ["NA\t" + c.ids[k] for k in r["xindex"]]

@@ -41,6 +41,12 @@ CONFIGS = {
                      I=10, seed=3, fst_seed=3,
                      name="fastmode N=55000 (10 BN pops of 5000 + 5000 two-way admixed) x "
                           "M=500000, F~U(0.005,0.05), 1% missing, K=10, L=20, I=10, omega seed 3"),
+    "mixed": dict(nsnp=600_000, pops=[500, 700, 800, 900, 1000, 1100],
+                  fst=[0.005, 0.01, 0.02, 0.03, 0.04, 0.05], miss=0.02, K=20, seed=2,
+                  jobs=6, nproj=200, rate=40.0, pca_every=21, pca_K=10,
+                  name="mixed stream: projection requests on the N=5000 x M=600000 K=20 panel "
+                       "+ full-PCA jobs at 1:20 (N log-U 200-8000, M U 50k-600k, 2-8 pops, "
+                       "F~U(0.005,0.05), 1-5% missing, K=10), Poisson arrivals 40/s"),
     "small": dict(nsnp=60_000, pops=[100, 150, 200, 250, 150, 150],
                   fst=[0.005, 0.01, 0.02, 0.03, 0.04, 0.05], miss=0.02, K=20, seed=2,
                   name="smartpca N=1000 x M=60000 BN 6 pops (profiling case)"),
@@ -276,6 +282,175 @@ def run_serving(h, cfg, nreq=400, seed=11):
     out["coord_max_rel_err_vs_fp64"] = err_rel
     native.host_unregister(rows)
     return out
+
+
+def _serial_queue(arrivals, service):
+    """FIFO single-server queue: completion latency of each item given arrival times and
+    service times (s)"""
+    t, lat = 0.0, []
+    for a, d in zip(arrivals, service):
+        t = max(t, a) + d
+        lat.append(t - a)
+    return np.array(lat)
+
+
+def run_mixed(args, cfg, local):
+    """Config 5: projection requests and full-PCA jobs in one Poisson stream through the
+    server (jobs admitted by device footprint on worker handles), against the plain FP64
+    path run one item at a time (measured service times, FIFO queue on the same arrivals)."""
+    import torch
+
+    from eig_gb300 import native
+    torch.cuda.set_device(local)
+    prec = native.PRECISIONS[args.precision]
+    rng = np.random.default_rng(cfg["seed"] + 7)
+    t0 = time.time()
+    rec, pop = native.synth_records(cfg["nsnp"], cfg["pops"], cfg["fst"], miss=cfg["miss"],
+                                    seed=cfg["seed"])
+    nind = len(pop)
+    h = native.Handle(local)
+    opts = native.default_opts(numeigs=cfg["K"], numoutliter=5, outlthresh=6.0, precision=prec)
+    native.smartpca_run(h, rec, nind, opts)        # leaves the K=20 panel resident
+    # the full-PCA job datasets
+    jobs = []
+    for j in range(cfg["jobs"]):
+        n = int(round(np.exp(rng.uniform(np.log(200), np.log(8000)))))
+        m = int(rng.uniform(50_000, 600_000))
+        npop = int(rng.integers(2, 9))
+        sizes = [n // npop] * npop
+        sizes[0] += n - sum(sizes)
+        fst = list(rng.uniform(0.005, 0.05, size=npop))
+        miss = float(rng.uniform(0.01, 0.05))
+        jr, _ = native.synth_records(m, sizes, fst, miss=miss, seed=cfg["seed"] + 100 + j)
+        native.host_register(jr)
+        jobs.append(dict(rec=jr, n=n, m=m, npop=npop, miss=miss))
+    gen_s = time.time() - t0
+    K2 = cfg["pca_K"]
+    jopts = native.default_opts(numeigs=K2, numoutliter=5, outlthresh=6.0, precision=prec)
+    srv = native.Server(h, cfg["K"], max_batch=4096, pool_samples=32768, pca_workers=2,
+                        pca_budget_bytes=96 << 30)
+    npool = 4096
+    npops = len(cfg["pops"])
+    per = (3 * npool // 4) // npops
+    rows, _ = native.synth_sample_rows(cfg["nsnp"], [per] * npops, cfg["fst"], srv.snp_index,
+                                       srv.row_bytes, sample_seed=cfg["seed"] + 1000, miss=0.0,
+                                       miss_hi=0.95, n_admixed=npool - per * npops,
+                                       seed=cfg["seed"])
+    native.host_register(rows)
+    # warm-up: every dataset once through the server, a few projections
+    for jb in jobs:
+        srv.submit_pca(jb["rec"], jb["n"], jopts).wait(600.0)
+    for _ in range(5):
+        srv.submit(rows[:1000]).wait(60.0)
+    # the stream
+    nitems = cfg["nproj"] + cfg["nproj"] // (cfg["pca_every"] - 1)
+    arrivals = np.cumsum(rng.exponential(1.0 / cfg["rate"], size=nitems))
+    kinds, sizes, offs, jidx = [], [], [], []
+    for i in range(nitems):
+        if i % cfg["pca_every"] == cfg["pca_every"] - 1:
+            kinds.append(1)
+            jidx.append(i // cfg["pca_every"] % len(jobs))
+            sizes.append(0)
+            offs.append(0)
+        else:
+            kinds.append(0)
+            z = int(rng.integers(1, 2001))
+            sizes.append(z)
+            offs.append(int(rng.integers(0, npool - z + 1)))
+            jidx.append(-1)
+    done_t = [0.0] * nitems
+    reqs = [None] * nitems
+    ready = threading.Semaphore(0)
+    errors = []
+
+    def waiter():
+        for i in range(nitems):
+            ready.acquire()
+            try:
+                reqs[i].wait(900.0)
+            except Exception as e:  # noqa: BLE001 - reported after the run
+                errors.append(str(e))
+            done_t[i] = time.perf_counter()
+
+    th = threading.Thread(target=waiter)
+    th.start()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ts = time.perf_counter()
+    for i in range(nitems):
+        while True:
+            dt = ts + arrivals[i] - time.perf_counter()
+            if dt <= 0:
+                break
+            time.sleep(min(dt, 0.001))
+        if kinds[i]:
+            jb = jobs[jidx[i]]
+            reqs[i] = srv.submit_pca(jb["rec"], jb["n"], jopts)
+        else:
+            reqs[i] = srv.submit(rows[offs[i]:offs[i] + sizes[i]])
+        ready.release()
+    th.join()
+    clk = clocks.stop()
+    if errors:
+        raise RuntimeError("mixed stream item failed: %s" % errors[0])
+    span = max(done_t) - ts
+    lat = np.array([(done_t[i] - (ts + arrivals[i])) * 1e3 for i in range(nitems)])
+    kinds = np.array(kinds)
+    split_evals = {}
+    for i in range(nitems):
+        if kinds[i] and jidx[i] not in split_evals:
+            split_evals[jidx[i]] = reqs[i].args.collect()["evals"][:K2]
+    done, peak, _ = srv.pca_stats()
+    srv.close()
+    # plain FP64 one item at a time: service times measured on the same GPU
+    s64 = native.Server(h, cfg["K"], max_batch=2048, pool_samples=4096, fp64_serial=True)
+    tt = time.perf_counter()
+    z64 = 0
+    for z in (500, 1000, 2000):
+        s64.submit(rows[:z]).wait(600.0)
+        z64 += z
+    sps64 = z64 / (time.perf_counter() - tt)
+    s64.close()
+    o64 = native.default_opts(numeigs=K2, numoutliter=5, outlthresh=6.0,
+                              precision=native.GP_PREC_FP64)
+    t64, err = {}, {}
+    for j, jb in enumerate(jobs):
+        if j not in split_evals:
+            continue
+        h.timer_start()
+        r64 = native.smartpca_run(h, jb["rec"], jb["n"], o64)
+        t64[j] = h.timer_stop() / 1e3
+        e64 = r64["evals"][:K2]
+        err[j] = float(np.max(np.abs(split_evals[j] - e64) / np.abs(e64)))
+    service = [sizes[i] / sps64 if not kinds[i] else t64[jidx[i]] for i in range(nitems)]
+    lat64 = _serial_queue(arrivals, service) * 1e3
+    span64 = max(float(np.sum(service)), float(arrivals[-1]))
+    for jb in jobs:
+        native.host_unregister(jb["rec"])
+    native.host_unregister(rows)
+    h.close()
+    proj, pca = kinds == 0, kinds == 1
+    nsamp = int(np.sum(np.array(sizes)[proj]))
+    return {
+        "items": nitems, "projection_requests": int(proj.sum()), "pca_jobs": int(pca.sum()),
+        "span_s": span, "items_per_s": nitems / span, "samples_per_s": nsamp / span,
+        "pca_jobs_per_s": int(pca.sum()) / span,
+        "proj_p50_ms": float(np.percentile(lat[proj], 50)),
+        "proj_p99_ms": float(np.percentile(lat[proj], 99)),
+        "pca_p50_ms": float(np.percentile(lat[pca], 50)),
+        "pca_p99_ms": float(np.percentile(lat[pca], 99)),
+        "pca_peak_concurrent": peak,
+        "jobs": [{"n": jb["n"], "m": jb["m"], "pops": jb["npop"], "miss": round(jb["miss"], 4),
+                  "fp64_s": t64.get(j), "eval_max_rel_err_vs_fp64": err.get(j)}
+                 for j, jb in enumerate(jobs)],
+        "serial_fp64": {"span_s": span64, "items_per_s": nitems / span64,
+                        "proj_p50_ms": float(np.percentile(lat64[proj], 50)),
+                        "proj_p99_ms": float(np.percentile(lat64[proj], 99)),
+                        "pca_p50_ms": float(np.percentile(lat64[pca], 50)),
+                        "pca_p99_ms": float(np.percentile(lat64[pca], 99)),
+                        "proj_samples_per_s": sps64,
+                        "note": "measured FP64 service times, FIFO queue on the same arrivals"},
+        "clocks": clk, "gen_s": gen_s}
 
 
 def run_gpu(args, cfg, world, rank, local, dist):
@@ -528,6 +703,18 @@ def main():
         print(json.dumps(line))
         return
 
+    if args.config == "mixed":
+        res = run_mixed(args, cfg, local)
+        line = {"metric": "mixed serving: items/s and p50/p99 latency vs serial plain FP64",
+                "value": res["items_per_s"], "unit": "items/s", "n_gpus": world,
+                "steps": 1, "warmup": 1, "ms_per_step": res["span_s"] * 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "split fp16 Gram + exact tensor-core products, FP64 eigensolve",
+                "data": "synthetic (seeded Balding-Nichols)", "config": config,
+                "mixed": res, "clocks": res["clocks"]}
+        if rank == 0:
+            print(json.dumps(line))
+        return
     if args.config == "fastmode":
         res = run_fastmode(args, cfg, local)
         value = world * res["flops"] / (res["step_ms"] * 1e-3) / 1e12

@@ -184,6 +184,33 @@ extern "C" void gp_close(gp_ctx *ctx)
   free(ctx);
 }
 
+extern "C" int gp_release(gp_ctx *ctx)
+{
+  if (!ctx) return GP_ERR_ARG;
+  GP_CUDA(ctx, cudaSetDevice(ctx->device));
+  GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  void **bufs[] = {(void **)&ctx->d_geno,    (void **)&ctx->d_rows,     (void **)&ctx->d_rowmask,
+                   (void **)&ctx->d_cols,    (void **)&ctx->d_cnt,      (void **)&ctx->d_killed,
+                   (void **)&ctx->d_vtab,    (void **)&ctx->d_xmean,    (void **)&ctx->d_xfancy,
+                   (void **)&ctx->d_kept,    (void **)&ctx->d_xtx,      (void **)&ctx->d_evals,
+                   (void **)&ctx->d_evecs,   (void **)&ctx->d_ffvecs,   (void **)&ctx->d_fxscal,
+                   (void **)&ctx->d_scratch, (void **)&ctx->d_scratch2, (void **)&ctx->d_scratch3,
+                   (void **)&ctx->d_scratch4, (void **)&ctx->d_scratch5};
+  for (size_t i = 0; i < sizeof(bufs) / sizeof(bufs[0]); ++i) {
+    if (*bufs[i]) cudaFree(*bufs[i]);
+    *bufs[i] = NULL;
+  }
+  ctx->scratch_cap = ctx->scratch2_cap = ctx->scratch3_cap = ctx->scratch4_cap =
+      ctx->scratch5_cap = 0;
+  ctx->xtx_cap = 0;
+  ctx->nsnp_all = 0;
+  ctx->nind_all = 0;
+  ctx->rlen_dev = 0;
+  ctx->nrows = ctx->ncols = ctx->nkept = ctx->nvec = ctx->nweights = 0;
+  ctx->xtx_valid = ctx->eig_valid = ctx->weights_valid = 0;
+  return GP_OK;
+}
+
 extern "C" int gp_device_bytes(const gp_ctx *ctx, int64_t *bytes)
 {
   if (!ctx || !bytes) return GP_ERR_ARG;

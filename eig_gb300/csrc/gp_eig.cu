@@ -23,6 +23,7 @@
 #include <stdlib.h>
 
 #include "gp_internal.h"
+#include "gp_tc.cuh"
 
 
 /* the same count in FP32 (coarse brackets only; verified in FP64 afterwards) */
@@ -183,6 +184,269 @@ k_multisect(const double *gd, const double *ge2, int n, double gl, double gu, do
     hi = nhi;
   }
   if (sub == 0) w[k] = 0.5 * (lo + hi);
+}
+
+/* ---------------------------------------------------------------------------------- */
+/*
+ * Householder tridiagonalisation A = Q T Q^T of the symmetric n x n matrix (lower triangle,
+ * column-major: element (r, q), r >= q, at A[q*n + r]), the unblocked algorithm of LAPACK
+ * dsytd2 (lower) restated for one cooperative launch:
+ *   for c = 0 .. n-2:  x = A(c+1:n, c);  (beta, tau, v) = reflector of x (dlarfg: v(c+1) = 1,
+ *   beta = -sign(alpha) ||x||, tau = (beta - alpha)/beta, v = x/(alpha - beta) below);
+ *   y = A(c+1:n, c+1:n) v;  w = tau y - (tau^2/2)(y.v) v;  A(c+1:n, c+1:n) -= v w^T + w v^T.
+ * The rank-2 update of step c is not a pass of its own: it is applied while step c+1 reads the
+ * trailing matrix for its product (look-ahead), so each step reads and writes the lower
+ * triangle once and reads it once more.  Per step, with the blocks' row/column ranges
+ * balanced by element count:
+ *   A   column c gets the pending update; w of step c-1; v of step c-1 stored into A(:, c-1)
+ *       (LAPACK's reflector storage, e(c-1) on the subdiagonal); partial ||x||^2
+ *   --- grid barrier
+ *   B1  each block, per owned column r of the trailing matrix: pending update of A(r:n, r),
+ *       written back, and y(r) = A(r:n, r) . v (lower part incl. diagonal), warp per column
+ *   --- grid barrier
+ *   B2  each block, per owned row r: y(r) += A(r, c+1:r) . v (strictly lower part; lanes
+ *       over rows, so the loads stay coalesced in column-major), partial y.v
+ *   --- grid barrier
+ * Every sum has a fixed order (no atomics), so the result is deterministic.  The grid
+ * barriers are counter + generation words with a %globaltimer bound: on expiry the kernel
+ * records an error code and returns (the host reports GP_ERR_TIMEOUT).
+ * Outputs: d[n], e[n-1], tau[n-1] and the reflectors in A, as cusolverDnDormtr(lower) reads
+ * them.  Shared memory: v(step c-1), w(step c-1), v(step c) over the rows (24 n bytes).
+ */
+#define TR_THREADS 256
+#define TR_WARPS (TR_THREADS / 32)
+#define TR_ERR_BARRIER 11
+
+__device__ __forceinline__ bool tr_grid_sync(unsigned *count, unsigned *gen, int *err)
+{
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    volatile unsigned *vgen = gen;
+    volatile int *verr = err;
+    const unsigned g = *vgen;
+    __threadfence();
+    const unsigned arrived = atomicAdd(count, 1u);
+    if (arrived == gridDim.x - 1) {
+      atomicExch(count, 0u);
+      __threadfence();
+      atomicAdd(gen, 1u);
+    } else {
+      const uint64_t t0 = globaltimer_ns();
+      while (*vgen == g) {
+        if (*verr) {
+          ok = 0;
+          break;
+        }
+        if (globaltimer_ns() - t0 > GP_WAIT_NS) {
+          atomicExch(err, TR_ERR_BARRIER);
+          ok = 0;
+          break;
+        }
+      }
+    }
+    __threadfence();
+    if (*verr) ok = 0;
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+/* sum of the G block partials in a fixed order (warp 0), broadcast through shared memory */
+__device__ __forceinline__ double tr_sum_partials(const double *part, int G, double *slot)
+{
+  if (threadIdx.x < 32) {
+    double s = 0.0;
+    for (int g = threadIdx.x; g < G; g += 32) s += part[g];
+    for (int o = 16; o; o >>= 1) s += __shfl_down_sync(0xFFFFFFFFu, s, o);
+    if (threadIdx.x == 0) *slot = s;
+  }
+  __syncthreads();
+  const double r = *slot;
+  __syncthreads();
+  return r;
+}
+
+/* block sum of one value per thread (fixed order), result valid in thread 0 */
+__device__ __forceinline__ double tr_block_sum(double v, double *red)
+{
+  for (int o = 16; o; o >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < TR_WARPS; ++w) s += red[w];
+  __syncthreads();
+  return s;
+}
+
+/* start of block b's share of [0, m) when column u weighs (m - u) (B1) */
+__device__ __forceinline__ int tr_split_cols(int m, int b, int G)
+{
+  if (b <= 0) return 0;
+  if (b >= G) return m;
+  const double tot = 0.5 * (double)m * (double)(m + 1);
+  const double t = tot * (double)b / (double)G;
+  const double a = 2.0 * (double)m + 1.0;
+  double u = 0.5 * (a - sqrt(fmax(a * a - 8.0 * t, 0.0)));
+  int iu = (int)ceil(u - 1e-9);
+  return iu < 0 ? 0 : (iu > m ? m : iu);
+}
+
+/* start of block b's share of [0, m) when row u weighs u (B2) */
+__device__ __forceinline__ int tr_split_rows(int m, int b, int G)
+{
+  if (b <= 0) return 0;
+  if (b >= G) return m;
+  const double tot = 0.5 * (double)m * (double)(m - 1);
+  const double t = tot * (double)b / (double)G;
+  double u = 0.5 * (1.0 + sqrt(1.0 + 8.0 * t));
+  int iu = (int)ceil(u - 1e-9);
+  return iu < 0 ? 0 : (iu > m ? m : iu);
+}
+
+__global__ void __launch_bounds__(TR_THREADS, 1)
+k_tridiag(double *A, int n, double *d, double *e, double *tau, double *wbuf, double *ybuf,
+          double *part_norm, double *part_dot, unsigned *bar, int *err)
+{
+  extern __shared__ double sh[];
+  double *svp = sh, *swp = sh + n, *svc = sh + 2 * n;
+  __shared__ double red[TR_WARPS];
+  __shared__ double bred[TR_WARPS][32];
+  __shared__ double s_slot;
+  const int G = gridDim.x, b = blockIdx.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  unsigned *count = bar, *gen = bar + 1;
+  double tau_p = 0.0, scale_p = 0.0, e_p = 0.0;
+  bool have_p = false;
+  for (int c = 0; c < n - 1; ++c) {
+    /* ---- A: w and storage of step c-1, column c update, partial ||x||^2 ---- */
+    double alpha_p = 0.0, wpc = 0.0;
+    if (have_p) {
+      alpha_p = -0.5 * tau_p * tau_p * tr_sum_partials(part_dot, G, &s_slot);
+      wpc = tau_p * ybuf[c] + alpha_p; /* v_p(c) = 1 */
+    }
+    {
+      const int cnt = n - c, per = (cnt + G - 1) / G;
+      const int r0 = c + b * per, r1 = min(n, r0 + per);
+      double nrm = 0.0;
+      for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+        double a = A[(int64_t)c * n + r];
+        if (have_p) {
+          const double vpr = (r == c) ? 1.0 : A[(int64_t)(c - 1) * n + r] * scale_p;
+          const double wpr = tau_p * ybuf[r] + alpha_p * vpr;
+          wbuf[r] = wpr;
+          A[(int64_t)(c - 1) * n + r] = (r == c) ? e_p : vpr;
+          a = a - vpr * wpc - wpr;
+        }
+        A[(int64_t)c * n + r] = a;
+        if (r >= c + 2) nrm = fma(a, a, nrm);
+      }
+      nrm = tr_block_sum(nrm, red);
+      if (threadIdx.x == 0) part_norm[b] = nrm;
+    }
+    if (!tr_grid_sync(count, gen, err)) return;
+    /* ---- reflector of column c (every block, same arithmetic) ---- */
+    const double xn2 = tr_sum_partials(part_norm, G, &s_slot);
+    const double alpha = A[(int64_t)c * n + c + 1];
+    double beta, tau_c, scale_c;
+    if (xn2 == 0.0) {
+      beta = alpha;
+      tau_c = 0.0;
+      scale_c = 0.0;
+    } else {
+      const double xn = sqrt(xn2);
+      const double ax = fabs(alpha), big = fmax(ax, xn), sml = fmin(ax, xn);
+      const double r = sml / big;
+      const double nrm = big * sqrt(1.0 + r * r);
+      beta = alpha >= 0.0 ? -nrm : nrm;
+      tau_c = (beta - alpha) / beta;
+      scale_c = 1.0 / (alpha - beta);
+    }
+    if (b == 0 && threadIdx.x == 0) {
+      d[c] = A[(int64_t)c * n + c];
+      e[c] = beta;
+      tau[c] = tau_c;
+    }
+    /* ---- B1: pending update + lower product, warp per column ---- */
+    const int m = n - c - 1;
+    for (int q = c + 1 + threadIdx.x; q < n; q += blockDim.x) {
+      svp[q] = have_p ? A[(int64_t)(c - 1) * n + q] : 0.0;
+      swp[q] = have_p ? wbuf[q] : 0.0;
+      svc[q] = (q == c + 1) ? 1.0 : A[(int64_t)c * n + q] * scale_c;
+    }
+    __syncthreads();
+    {
+      const int u0 = tr_split_cols(m, b, G), u1 = tr_split_cols(m, b + 1, G);
+      for (int u = u0 + warp; u < u1; u += TR_WARPS) {
+        const int r = c + 1 + u;
+        const double vpr = svp[r], wpr = swp[r];
+        double *col = A + (int64_t)r * n;
+        double dot = 0.0;
+        if (have_p) {
+          for (int q = r + lane; q < n; q += 32) {
+            double a = col[q];
+            a = fma(-svp[q], wpr, a);
+            a = fma(-swp[q], vpr, a);
+            col[q] = a;
+            dot = fma(a, svc[q], dot);
+          }
+        } else {
+          for (int q = r + lane; q < n; q += 32) dot = fma(col[q], svc[q], dot);
+        }
+        for (int o = 16; o; o >>= 1) dot += __shfl_down_sync(0xFFFFFFFFu, dot, o);
+        if (lane == 0) ybuf[r] = dot;
+      }
+    }
+    if (!tr_grid_sync(count, gen, err)) return;
+    /* ---- B2: strictly lower part of the product, lanes over rows ---- */
+    {
+      const int u0 = tr_split_rows(m, b, G), u1 = tr_split_rows(m, b + 1, G);
+      double dpart = 0.0;
+      for (int ch = u0; ch < u1; ch += 32) {
+        const int u = ch + lane;
+        const int r = c + 1 + u;
+        const bool valid = u < u1;
+        const int qend = c + 1 + min(ch + 32, u1); /* columns below the chunk's last row */
+        double acc = 0.0;
+        for (int q = c + 1 + warp; q < qend; q += TR_WARPS)
+          if (valid && q < r) acc = fma(A[(int64_t)q * n + r], svc[q], acc);
+        bred[warp][lane] = acc;
+        __syncthreads();
+        if (warp == 0 && valid) {
+          double y1 = 0.0;
+          for (int w = 0; w < TR_WARPS; ++w) y1 += bred[w][lane];
+          const double y = ybuf[r] + y1;
+          ybuf[r] = y;
+          dpart = fma(y, svc[r], dpart);
+        }
+        __syncthreads();
+      }
+      dpart = tr_block_sum(dpart, red);
+      if (threadIdx.x == 0) part_dot[b] = dpart;
+    }
+    if (!tr_grid_sync(count, gen, err)) return;
+    tau_p = tau_c;
+    scale_p = scale_c;
+    e_p = beta;
+    have_p = true;
+  }
+  /* last diagonal entry and the storage of the last reflector */
+  if (b == 0) {
+    double alpha_p = 0.0;
+    if (have_p) alpha_p = -0.5 * tau_p * tau_p * tr_sum_partials(part_dot, G, &s_slot);
+    if (threadIdx.x == 0) {
+      double a = A[(int64_t)(n - 1) * n + n - 1];
+      if (have_p) {
+        const double wp = tau_p * ybuf[n - 1] + alpha_p;
+        a = a - wp - wp;
+        A[(int64_t)(n - 2) * n + n - 1] = e_p;
+      }
+      d[n - 1] = a;
+    }
+  }
 }
 
 /* deterministic start vector entry in (-1, 1) */

@@ -16,12 +16,20 @@
 #include <unordered_map>
 #include <vector>
 
+#include "../../include/gpupca_run.h"
 #include "../../include/gpupca_serve.h"
 #include "gp_geno_tc.h"
 #include "gp_internal.h"
 
 struct gp_req {
   int64_t id;
+  int kind;           /* 0 projection request, 1 full-PCA job */
+  /* full-PCA job */
+  const gp_panel *panel;
+  const gp_smartpca_opts *opts;
+  gp_run_result *result;
+  int64_t footprint;
+  /* projection request */
   int32_t nsamp;
   const uint8_t *codes;
   double *coords;
@@ -74,6 +82,13 @@ struct gp_server {
   std::deque<gp_batch *> inflight;
   std::unordered_map<int64_t, gp_req *> all;
   int64_t next_id;
+  /* full-PCA jobs: FIFO, admitted while their footprint fits the budget */
+  std::deque<gp_req *> pca_waiting;
+  std::vector<gp_ctx *> wctx;
+  std::vector<pthread_t> workers;
+  int64_t pca_budget, pca_used;
+  int32_t pca_running, pca_peak;
+  int64_t pca_done;
   pthread_t thread;
   int stop, thread_started, paused;
   int64_t n_batches, n_samples, n_requests;
@@ -373,6 +388,73 @@ static void *scheduler(void *arg)
   return NULL;
 }
 
+/* full-PCA worker: takes the front job when it fits the budget (or nothing else runs) */
+struct worker_arg {
+  gp_server *s;
+  int index;
+};
+
+static void *pca_worker(void *arg)
+{
+  worker_arg *wa = (worker_arg *)arg;
+  gp_server *s = wa->s;
+  gp_ctx *ctx = s->wctx[(size_t)wa->index];
+  delete wa;
+  cudaSetDevice(ctx->device);
+  pthread_mutex_lock(&s->mu);
+  for (;;) {
+    gp_req *j = NULL;
+    if (!s->pca_waiting.empty()) {
+      gp_req *f = s->pca_waiting.front();
+      if (s->pca_running == 0 || s->pca_used + f->footprint <= s->pca_budget) {
+        j = f;
+        s->pca_waiting.pop_front();
+      }
+    }
+    if (!j) {
+      if (s->stop && s->pca_waiting.empty()) break;
+      pthread_cond_wait(&s->cv, &s->mu);
+      continue;
+    }
+    s->pca_used += j->footprint;
+    s->pca_running++;
+    if (s->pca_running > s->pca_peak) s->pca_peak = s->pca_running;
+    pthread_mutex_unlock(&s->mu);
+    int rc = gp_smartpca_run(ctx, j->opts, j->panel, j->result);
+    if (rc) snprintf(s->err, sizeof s->err, "PCA job %lld: %s", (long long)j->id, gp_last_error(ctx));
+    gp_release(ctx);
+    pthread_mutex_lock(&s->mu);
+    s->pca_used -= j->footprint;
+    s->pca_running--;
+    s->pca_done++;
+    j->error = rc;
+    j->done = 1;
+    pthread_cond_broadcast(&s->cv);
+  }
+  pthread_mutex_unlock(&s->mu);
+  return NULL;
+}
+
+extern "C" int64_t gp_smartpca_footprint(int32_t nind, int64_t nsnp, int32_t precision,
+                                         int32_t numeigs)
+{
+  const int64_t n = nind, m = nsnp, npad = (n + 127) / 128 * 128;
+  const int64_t rec = m * ((n + 63) / 64 * 16);
+  const int64_t gram = 8 * n * n;
+  const int64_t k = numeigs > 0 ? numeigs : 1;
+  const int64_t eig = 8 * n * 64 + 48 * n * (k > 10 ? k : 10) + 8 * n * k;
+  int64_t work;
+  if (precision == GP_PREC_FP64) {
+    work = 8 * m * (k * (k + 1) / 2 + 1) + 8 * n * 256;
+  } else {
+    int64_t split = 4 * npad * m;
+    if (split > (int64_t)24 << 30) split = (int64_t)24 << 30;
+    const int64_t tc = n * (m / 4 + 16) + m * 1024 + n * 8 * 1024 + 8 * m * 256;
+    work = split > tc ? split : tc;
+  }
+  return rec + gram + eig + work + 100 * m + ((int64_t)256 << 20);
+}
+
 /* ------------------------------------------------------------------------------------ */
 
 extern "C" const char *gp_serve_last_error(const gp_server *srv) { return srv ? srv->err : ""; }
@@ -388,6 +470,14 @@ extern "C" void gp_serve_close(gp_server *s)
     pthread_mutex_unlock(&s->mu);
     pthread_join(s->thread, NULL);
   }
+  if (!s->workers.empty()) {
+    pthread_mutex_lock(&s->mu);
+    s->stop = 1;
+    pthread_cond_broadcast(&s->cv);
+    pthread_mutex_unlock(&s->mu);
+    for (pthread_t t : s->workers) pthread_join(t, NULL);
+  }
+  for (gp_ctx *w : s->wctx) gp_close(w);
   if (s->ctx) cudaSetDevice(s->ctx->device);
   void *dev[] = {s->d_E,     s->d_P,      s->d_fE,     s->d_mE,     s->d_otab,   s->d_rtab,
                  s->stor_co, s->stor_rr,  s->d_pool,   s->d_co[0],  s->d_co[1],  s->d_rr[0],
@@ -530,6 +620,26 @@ extern "C" int gp_serve_open(gp_ctx *src, const gp_serve_opts *o, gp_server **ou
     return GP_ERR_STATE;
   }
   s->thread_started = 1;
+  /* full-PCA workers, each with its own handle (stream, solver) */
+  s->pca_budget = o->pca_budget_bytes > 0 ? o->pca_budget_bytes : ((int64_t)64 << 30);
+  const int nw = o->pca_workers > 0 ? (o->pca_workers > 8 ? 8 : o->pca_workers) : 1;
+  for (int i = 0; i < nw; ++i) {
+    gp_ctx *w = NULL;
+    if (gp_open(src->device, &w) != GP_OK) break;
+    s->wctx.push_back(w);
+    worker_arg *wa = new worker_arg{s, i};
+    pthread_t t;
+    if (pthread_create(&t, NULL, pca_worker, wa) != 0) {
+      delete wa;
+      break;
+    }
+    s->workers.push_back(t);
+  }
+  if (s->workers.empty()) {
+    gp_fail(src, GP_ERR_STATE, "gp_serve_open: could not start a PCA worker");
+    gp_serve_close(s);
+    return GP_ERR_STATE;
+  }
   *out = s;
   return GP_OK;
 }
@@ -572,6 +682,40 @@ extern "C" int gp_serve_submit(gp_server *s, const uint8_t *codes, int32_t nsamp
   pthread_cond_broadcast(&s->cv);
   pthread_mutex_unlock(&s->mu);
   *ticket = r->id;
+  return GP_OK;
+}
+
+extern "C" int gp_serve_submit_pca(gp_server *s, const gp_panel *panel,
+                                   const gp_smartpca_opts *opts, gp_run_result *result,
+                                   int64_t *ticket)
+{
+  if (!s || !panel || !opts || !result || !ticket || !panel->records) return GP_ERR_ARG;
+  gp_req *r = new gp_req();
+  r->kind = 1;
+  r->panel = panel;
+  r->opts = opts;
+  r->result = result;
+  r->footprint = gp_smartpca_footprint(panel->nind, panel->nsnp, opts->precision, opts->numeigs);
+  pthread_mutex_lock(&s->mu);
+  r->id = s->next_id++;
+  s->all[r->id] = r;
+  s->pca_waiting.push_back(r);
+  pthread_cond_broadcast(&s->cv);
+  pthread_mutex_unlock(&s->mu);
+  *ticket = r->id;
+  return GP_OK;
+}
+
+extern "C" int gp_serve_pca_stats(const gp_server *s, int64_t *jobs_done, int32_t *peak_running,
+                                  int64_t *bytes_in_use)
+{
+  if (!s) return GP_ERR_ARG;
+  gp_server *m = (gp_server *)s;
+  pthread_mutex_lock(&m->mu);
+  if (jobs_done) *jobs_done = s->pca_done;
+  if (peak_running) *peak_running = s->pca_peak;
+  if (bytes_in_use) *bytes_in_use = s->pca_used;
+  pthread_mutex_unlock(&m->mu);
   return GP_OK;
 }
 

@@ -33,7 +33,8 @@ EXPORTED = ["gp_version", "gp_last_error", "gp_open", "gp_close", "gp_device_byt
             "gp_transfer_bytes", "gp_launch_count", "gp_gram_fp64_noalloc",
             "gp_noalloc_last_error", "gp_serve_open", "gp_serve_layout",
             "gp_serve_panel_snps", "gp_serve_submit", "gp_serve_test", "gp_serve_wait",
-            "gp_serve_stats", "gp_serve_last_error", "gp_serve_close", "gp_serve_pause"]
+            "gp_serve_stats", "gp_serve_last_error", "gp_serve_close", "gp_serve_pause",
+            "gp_serve_submit_pca", "gp_serve_pca_stats", "gp_smartpca_footprint", "gp_release"]
 
 i32p = C.POINTER(C.c_int32)
 i64p = C.POINTER(C.c_int64)
@@ -67,7 +68,8 @@ class Panel(C.Structure):
 
 class ServeOpts(C.Structure):
     _fields_ = [("numeigs", C.c_int32), ("max_batch", C.c_int32), ("pool_samples", C.c_int64),
-                ("fp64_serial", C.c_int32), ("eigscale", f64p)]
+                ("fp64_serial", C.c_int32), ("eigscale", f64p), ("pca_workers", C.c_int32),
+                ("pca_budget_bytes", C.c_int64)]
 
 
 class RunResult(C.Structure):
@@ -131,6 +133,11 @@ def load_library():
         "gp_serve_wait": (C.c_int, [vp, C.c_int64, C.c_double]),
         "gp_serve_stats": (C.c_int, [vp, i64p, i64p, i64p]),
         "gp_serve_pause": (C.c_int, [vp, C.c_int32]),
+        "gp_serve_submit_pca": (C.c_int, [vp, C.POINTER(Panel), C.POINTER(SmartpcaOpts),
+                                          C.POINTER(RunResult), i64p]),
+        "gp_serve_pca_stats": (C.c_int, [vp, i64p, i32p, i64p]),
+        "gp_smartpca_footprint": (C.c_int64, [C.c_int32, C.c_int64, C.c_int32, C.c_int32]),
+        "gp_release": (C.c_int, [vp]),
         "gp_serve_last_error": (C.c_char_p, [vp]),
         "gp_serve_close": (None, [vp]),
         "gp_smartpca_run": (C.c_int, [vp, C.POINTER(SmartpcaOpts), C.POINTER(Panel),
@@ -359,16 +366,28 @@ class ServeRequest:
         return self.coords, self.status
 
 
+class PcaJob(ServeRequest):
+    """A full-PCA job queued on a Server; wait() returns the smartpca_run result dict."""
+
+    def __init__(self, server, ticket, args):
+        super().__init__(server, ticket, None, None, None)
+        self.args = args
+
+    def wait(self, timeout=600.0):
+        super().wait(timeout)
+        return self.args.collect()
+
+
 class Server:
     """Projection server on the panel (SNP weights) resident in `handle` (gpupca_serve.h)."""
 
     def __init__(self, handle, numeigs, max_batch=0, pool_samples=0, fp64_serial=False,
-                 eigscale=None):
+                 eigscale=None, pca_workers=0, pca_budget_bytes=0):
         self.lib = load_library()
         self.K = numeigs
         self._scale = None if eigscale is None else np.ascontiguousarray(eigscale, np.float64)
         o = ServeOpts(numeigs, max_batch, pool_samples, int(fp64_serial),
-                      ptr(self._scale, C.c_double))
+                      ptr(self._scale, C.c_double), pca_workers, pca_budget_bytes)
         s = vp()
         handle.check(self.lib.gp_serve_open(handle.h, C.byref(o), C.byref(s)), "gp_serve_open")
         self.s = s
@@ -399,6 +418,22 @@ class Server:
                                             ptr(coords, C.c_double), ptr(status, C.c_int32),
                                             C.byref(t)), "gp_serve_submit")
         return ServeRequest(self, t.value, codes, coords, status)
+
+    def submit_pca(self, records, nind, opts, **panel):
+        """queue a full-PCA job (gp_serve_submit_pca); returns a request whose wait() gives
+        the smartpca_run result dict"""
+        a = _RunArgs(records, nind, opts, **panel)
+        t = C.c_int64()
+        self.check(self.lib.gp_serve_submit_pca(self.s, C.byref(a.panel), C.byref(opts),
+                                                C.byref(a.result), C.byref(t)),
+                   "gp_serve_submit_pca")
+        return PcaJob(self, t.value, a)
+
+    def pca_stats(self):
+        a, b, c = C.c_int64(), C.c_int32(), C.c_int64()
+        self.check(self.lib.gp_serve_pca_stats(self.s, C.byref(a), C.byref(b), C.byref(c)),
+                   "gp_serve_pca_stats")
+        return a.value, b.value, c.value
 
     def pause(self, paused=True):
         self.check(self.lib.gp_serve_pause(self.s, int(paused)), "gp_serve_pause")
@@ -467,61 +502,83 @@ def default_opts(**kw):
     return o
 
 
+class _RunArgs:
+    """ctypes panel + result of one gp_smartpca_run, with the arrays they point into"""
+
+    def __init__(self, records, nind, opts, code=GP_CODE_PACKED, snp_chrom=None,
+                 snp_ignore=None, ind_ignore=None, ind_affstatus=None, ind_male=None,
+                 want_xtx=False):
+        self.keep = []
+        if isinstance(records, tuple):  # (nsnp, record_bytes): the panel resident on the handle
+            rec = None
+            nsnp, rb = records
+        else:
+            rec = np.ascontiguousarray(records, dtype=np.uint8)
+            nsnp, rb = rec.shape
+            self.keep.append(rec)
+
+        def arr(a, dt):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, dtype=dt)
+            self.keep.append(a)
+            return a
+
+        self.nind, self.opts, self.want_xtx = nind, opts, want_xtx
+        chrom = arr(snp_chrom, np.int32)
+        self.panel = Panel(ptr(rec, C.c_uint8), rb, nsnp, nind, code, ptr(chrom, C.c_int32),
+                           ptr(arr(snp_ignore, np.uint8), C.c_uint8),
+                           ptr(arr(ind_ignore, np.uint8), C.c_uint8),
+                           ptr(arr(ind_affstatus, np.uint8), C.c_uint8),
+                           ptr(arr(ind_male, np.uint8), C.c_uint8))
+        K = max(opts.numeigs, 1)
+        out = dict(xindex=np.zeros(nind, np.int32), evals=np.zeros(nind),
+                   evecs=np.zeros(K * nind), coords=np.zeros(K * nind),
+                   ind_out=np.zeros(nind, np.uint8), snp_state=np.zeros(nsnp, np.uint8),
+                   outlier_idx=np.zeros(nind, np.int32), outlier_iter=np.zeros(nind, np.int32),
+                   outlier_vec=np.zeros(nind, np.int32), outlier_score=np.zeros(nind))
+        r = RunResult(ptr(out["xindex"], C.c_int32), ptr(out["evals"], C.c_double),
+                      ptr(out["evecs"], C.c_double), ptr(out["coords"], C.c_double),
+                      ptr(out["ind_out"], C.c_uint8), ptr(out["snp_state"], C.c_uint8),
+                      ptr(out["outlier_idx"], C.c_int32), ptr(out["outlier_iter"], C.c_int32),
+                      ptr(out["outlier_vec"], C.c_int32), ptr(out["outlier_score"], C.c_double))
+        if want_xtx:
+            out["xtx"] = np.zeros(nind * nind)
+            r.xtx = ptr(out["xtx"], C.c_double)
+        self.out, self.result = out, r
+
+    def collect(self):
+        r, out, nind, opts = self.result, self.out, self.nind, self.opts
+        n, k = r.nrows, r.numeigs
+        res = dict(nrows=n, ncols=r.ncols, numeigs=k, npasses=r.npasses,
+                   xindex=out["xindex"][:n].copy(),
+                   evals=out["evals"][: (k if opts.fastmode else n)].copy(),
+                   evecs=out["evecs"][: k * n].reshape(k, n).copy(),
+                   coords=out["coords"][: k * nind].reshape(k, nind).copy(),
+                   ind_out=out["ind_out"].astype(bool), snp_state=out["snp_state"],
+                   outliers=[(int(out["outlier_idx"][i]), int(out["outlier_iter"][i]),
+                              int(out["outlier_vec"][i]), float(out["outlier_score"][i]))
+                             for i in range(min(r.noutliers, nind))],
+                   t_phase={PHASES[i]: r.t_phase[i] for i in range(8)},
+                   gram_flops=r.gram_flops, gram_ms=r.gram_ms, nused=r.nused)
+        if self.want_xtx:
+            res["xtx"] = out["xtx"][: n * n].reshape(n, n).copy()
+        return res
+
+
 def smartpca_run(handle, records, nind, opts, code=GP_CODE_PACKED, snp_chrom=None,
                  snp_ignore=None, ind_ignore=None, ind_affstatus=None, ind_male=None,
                  want_xtx=False):
     """Run the whole smartpca hot path (gp_smartpca_run) on in-memory records."""
-    lib = handle.lib
-    keep = []
-    if isinstance(records, tuple):  # (nsnp, record_bytes): the panel resident on the handle
-        rec = None
-        nsnp, rb = records
-    else:
-        rec = np.ascontiguousarray(records, dtype=np.uint8)
-        nsnp, rb = rec.shape
+    a = _RunArgs(records, nind, opts, code, snp_chrom, snp_ignore, ind_ignore, ind_affstatus,
+                 ind_male, want_xtx)
+    handle.check(handle.lib.gp_smartpca_run(handle.h, C.byref(opts), C.byref(a.panel),
+                                            C.byref(a.result)), "gp_smartpca_run")
+    return a.collect()
 
-    def arr(a, dt):
-        if a is None:
-            return None
-        a = np.ascontiguousarray(a, dtype=dt)
-        keep.append(a)
-        return a
 
-    chrom = arr(snp_chrom, np.int32)
-    p = Panel(ptr(rec, C.c_uint8), rb, nsnp, nind, code, ptr(chrom, C.c_int32),
-              ptr(arr(snp_ignore, np.uint8), C.c_uint8), ptr(arr(ind_ignore, np.uint8), C.c_uint8),
-              ptr(arr(ind_affstatus, np.uint8), C.c_uint8), ptr(arr(ind_male, np.uint8), C.c_uint8))
-    K = max(opts.numeigs, 1)
-    out = dict(xindex=np.zeros(nind, np.int32), evals=np.zeros(nind), evecs=np.zeros(K * nind),
-               coords=np.zeros(K * nind), ind_out=np.zeros(nind, np.uint8),
-               snp_state=np.zeros(nsnp, np.uint8), outlier_idx=np.zeros(nind, np.int32),
-               outlier_iter=np.zeros(nind, np.int32), outlier_vec=np.zeros(nind, np.int32),
-               outlier_score=np.zeros(nind))
-    r = RunResult(ptr(out["xindex"], C.c_int32), ptr(out["evals"], C.c_double),
-                  ptr(out["evecs"], C.c_double), ptr(out["coords"], C.c_double),
-                  ptr(out["ind_out"], C.c_uint8), ptr(out["snp_state"], C.c_uint8),
-                  ptr(out["outlier_idx"], C.c_int32), ptr(out["outlier_iter"], C.c_int32),
-                  ptr(out["outlier_vec"], C.c_int32), ptr(out["outlier_score"], C.c_double))
-    if want_xtx:
-        out["xtx"] = np.zeros(nind * nind)
-        r.xtx = ptr(out["xtx"], C.c_double)
-    handle.check(lib.gp_smartpca_run(handle.h, C.byref(opts), C.byref(p), C.byref(r)),
-                 "gp_smartpca_run")
-    n, k = r.nrows, r.numeigs
-    res = dict(nrows=n, ncols=r.ncols, numeigs=k, npasses=r.npasses,
-               xindex=out["xindex"][:n].copy(),
-               evals=out["evals"][: (k if opts.fastmode else n)].copy(),
-               evecs=out["evecs"][: k * n].reshape(k, n).copy(),
-               coords=out["coords"][: k * nind].reshape(k, nind).copy(),
-               ind_out=out["ind_out"].astype(bool), snp_state=out["snp_state"],
-               outliers=[(int(out["outlier_idx"][i]), int(out["outlier_iter"][i]),
-                          int(out["outlier_vec"][i]), float(out["outlier_score"][i]))
-                         for i in range(min(r.noutliers, nind))],
-               t_phase={PHASES[i]: r.t_phase[i] for i in range(8)},
-               gram_flops=r.gram_flops, gram_ms=r.gram_ms, nused=r.nused)
-    if want_xtx:
-        res["xtx"] = out["xtx"][: n * n].reshape(n, n).copy()
-    return res
+def smartpca_footprint(nind, nsnp, precision, numeigs):
+    return load_library().gp_smartpca_footprint(nind, nsnp, precision, numeigs)
 
 
 class SynthSpec(C.Structure):

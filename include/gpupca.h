@@ -183,6 +183,11 @@ int gp_fastpca(gp_ctx *ctx, int32_t K, int32_t L, int32_t I, uint64_t seed,
                const double *omega, const gp_xtx_opts *opts, double *evals, double *evecs);
 
 
+/* Free every device buffer of the handle (panel, Gram, vectors, scratch); the handle, its
+ * stream and solver stay usable and the next gp_load_genotypes starts afresh.  No
+ * counterpart in the reference (a process ends instead). */
+int gp_release(gp_ctx *ctx);
+
 /* ---- measurement helpers (no counterpart in the reference) ---------------------------- */
 
 /* Device stopwatch on the handle's stream (CUDA events); stop synchronises the stream. */

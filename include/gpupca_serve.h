@@ -18,6 +18,9 @@
  * batch.  Products are exact integer sums, so a sample's coordinates do not depend on which
  * other requests share its batch.
  *
+ * Full-PCA jobs (gp_serve_submit_pca) share the server: they are admitted by estimated device
+ * footprint and run on worker handles beside the projection batches.
+ *
  * Outputs per sample: coords [nsamp*K] (sample q, eigenvector j at q*K + j), scaled by the
  * opts' eigscale; status 0 ok, 1 = at most K observed SNPs (dropped, coords 0), 2 = normal
  * equations not positive definite (coords 0).  The caller's code buffer must stay valid and
@@ -29,6 +32,7 @@
 #include <stdint.h>
 
 #include "gpupca.h"
+#include "gpupca_run.h"
 
 #ifdef __cplusplus
 extern "C" {
@@ -42,6 +46,8 @@ typedef struct {
   int64_t pool_samples;  /* device staging capacity in sample rows (default 32768 when 0) */
   int32_t fp64_serial;   /* 1: one request per batch, FP64 products (the plain baseline) */
   const double *eigscale;/* [K] multiplies coordinate j (seteigscale); NULL = 1 */
+  int32_t pca_workers;   /* full-PCA worker handles (default 1 when 0, at most 8) */
+  int64_t pca_budget_bytes; /* device bytes the running PCA jobs may hold (default 64 GiB) */
 } gp_serve_opts;
 
 int gp_serve_open(gp_ctx *src, const gp_serve_opts *opts, gp_server **out);
@@ -52,6 +58,22 @@ int gp_serve_panel_snps(const gp_server *srv, int32_t *snp_index);
 /* queue a request; *ticket identifies it.  GP_ERR_FULL if it can never fit the pool. */
 int gp_serve_submit(gp_server *srv, const uint8_t *codes, int32_t nsamp, double *coords,
                     int32_t *status, int64_t *ticket);
+/*
+ * Queue a full-PCA job (gp_smartpca_run of gpupca_run.h on panel->records, which must be host
+ * records).  Jobs are admitted in FIFO order while the sum of their estimated device
+ * footprints (gp_smartpca_footprint) fits pca_budget_bytes (a job is always admitted when no
+ * other runs), each on a worker handle with its own stream, so they overlap the projection
+ * batches; the worker frees its device memory after each job.  The panel, opts and result
+ * arrays must stay valid until the job completes; the ticket works with test/wait.
+ */
+int gp_serve_submit_pca(gp_server *srv, const gp_panel *panel, const gp_smartpca_opts *opts,
+                        gp_run_result *result, int64_t *ticket);
+/* device bytes one gp_smartpca_run on nind x nsnp holds at most (an upper estimate) */
+int64_t gp_smartpca_footprint(int32_t nind, int64_t nsnp, int32_t precision, int32_t numeigs);
+/* PCA jobs completed, the largest number that ran at once, bytes admitted now */
+int gp_serve_pca_stats(const gp_server *srv, int64_t *jobs_done, int32_t *peak_running,
+                       int64_t *bytes_in_use);
+
 /* 1 when the request has completed, 0 while pending, < 0 on error.  A call that reports
  * completion (1 or the request's error) releases the ticket; one waiter per ticket. */
 int gp_serve_test(gp_server *srv, int64_t ticket);

@@ -143,3 +143,52 @@ def test_serve_ticket_released_after_wait(gpu, panel):
         # the ticket was released by the completed wait
         assert srv.lib.gp_serve_wait(srv.s, r.ticket, 0.1) == -1
         assert srv.lib.gp_serve_test(srv.s, 10 ** 9) == -1
+
+
+def _pca_data(nsnp, pops, seed):
+    rec, pop = native.synth_records(nsnp, pops, [0.01, 0.03, 0.05][:len(pops)], miss=0.02,
+                                    seed=seed, nthreads=4)
+    return rec, len(pop)
+
+
+@pytest.mark.parametrize("prec", [native.GP_PREC_FP64, native.GP_PREC_SPLIT_FP16])
+def test_serve_pca_job_same_alone_and_in_the_mix(gpu, panel, prec):
+    """a full-PCA job run by the server beside projection batches gives exactly the result
+    of gp_smartpca_run on its own handle"""
+    rec, nind = _pca_data(6000, [120, 100, 80], 41)
+    opts = native.default_opts(numeigs=6, numoutliter=2, precision=prec)
+    with native.Handle(0) as h2:
+        alone = native.smartpca_run(h2, rec, nind, opts)
+    rng = np.random.default_rng(9)
+    with native.Server(gpu, K, max_batch=256, pca_workers=2) as srv:
+        reqs = [srv.submit(_rows(srv, panel, rng.choice(panel["nind"], 50, replace=False)))
+                for _ in range(10)]
+        job = srv.submit_pca(rec, nind, opts)
+        reqs += [srv.submit(_rows(srv, panel, rng.choice(panel["nind"], 50, replace=False)))
+                 for _ in range(10)]
+        mixed = job.wait(300.0)
+        for r in reqs:
+            r.wait(60.0)
+        done, peak, used = srv.pca_stats()
+        assert done == 1 and used == 0
+    for key in ("xindex", "evals", "evecs", "coords", "ind_out"):
+        assert np.array_equal(alone[key], mixed[key]), key
+    assert alone["outliers"] == mixed["outliers"]
+
+
+def test_serve_pca_admission_by_footprint(gpu, panel):
+    """with a budget below one job's footprint the jobs run one at a time (a job is admitted
+    alone when nothing else runs); all complete with their own results"""
+    data = [_pca_data(3000, [60, 60], s) for s in (51, 52, 53)]
+    opts = native.default_opts(numeigs=4, numoutliter=0, precision=native.GP_PREC_SPLIT_FP16)
+    fp = native.smartpca_footprint(data[0][1], 3000, native.GP_PREC_SPLIT_FP16, 4)
+    assert fp > 3000 * 32
+    with native.Server(gpu, K, pca_workers=3, pca_budget_bytes=fp // 2) as srv:
+        jobs = [srv.submit_pca(rec, n, opts) for rec, n in data]
+        res = [j.wait(300.0) for j in jobs]
+        done, peak, used = srv.pca_stats()
+    assert done == 3 and peak == 1
+    with native.Handle(0) as h2:
+        for (rec, n), r in zip(data, res):
+            want = native.smartpca_run(h2, rec, n, opts)
+            assert np.array_equal(want["evals"], r["evals"])

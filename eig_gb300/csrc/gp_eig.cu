@@ -3,7 +3,8 @@
  * and the top nvec eigenvectors (the reference computes every eigenpair with LAPACK dspev,
  * src/eigensrc/eigx.c:97-117, but prints all eigenvalues and uses only the top vectors).
  *
- *   1. Householder tridiagonalisation A = Q T Q^T (cuSOLVER sytrd, lower);
+ *   1. Householder tridiagonalisation A = Q T Q^T (k_tridiag below: one cooperative launch,
+ *      LAPACK dsytd2's reflectors and storage; cuSOLVER sytrd beyond 8,533 rows);
  *   2. all eigenvalues of T by multisection on Sturm counts (the published bisection method:
  *      the count of negative pivots of the LDL^T factorisation of T - x I equals the number
  *      of eigenvalues below x), several lanes per eigenvalue index: FP32 brackets first,
@@ -213,37 +214,33 @@ k_multisect(const double *gd, const double *ge2, int n, double gl, double gu, do
  * Outputs: d[n], e[n-1], tau[n-1] and the reflectors in A, as cusolverDnDormtr(lower) reads
  * them.  Shared memory: v(step c-1), w(step c-1), v(step c) over the rows (24 n bytes).
  */
-#define TR_THREADS 256
+#define TR_THREADS 512
 #define TR_WARPS (TR_THREADS / 32)
+#define TR_U 8 /* loads in flight per lane in the product loops */
 #define TR_ERR_BARRIER 11
 
-__device__ __forceinline__ bool tr_grid_sync(unsigned *count, unsigned *gen, int *err)
+/* grid barrier on a monotonic arrival counter: the k-th barrier of the launch waits until
+ * k * gridDim.x blocks have arrived (one atomic per block, no reset) */
+__device__ __forceinline__ bool tr_grid_sync(unsigned *count, unsigned target, int *err)
 {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
-    volatile unsigned *vgen = gen;
+    volatile unsigned *vcount = count;
     volatile int *verr = err;
-    const unsigned g = *vgen;
     __threadfence();
-    const unsigned arrived = atomicAdd(count, 1u);
-    if (arrived == gridDim.x - 1) {
-      atomicExch(count, 0u);
-      __threadfence();
-      atomicAdd(gen, 1u);
-    } else {
-      const uint64_t t0 = globaltimer_ns();
-      while (*vgen == g) {
-        if (*verr) {
-          ok = 0;
-          break;
-        }
-        if (globaltimer_ns() - t0 > GP_WAIT_NS) {
-          atomicExch(err, TR_ERR_BARRIER);
-          ok = 0;
-          break;
-        }
+    atomicAdd(count, 1u);
+    const uint64_t t0 = globaltimer_ns();
+    while (*vcount < target) {
+      if (*verr) {
+        ok = 0;
+        break;
+      }
+      if (globaltimer_ns() - t0 > GP_WAIT_NS) {
+        atomicExch(err, TR_ERR_BARRIER);
+        ok = 0;
+        break;
       }
     }
     __threadfence();
@@ -307,140 +304,315 @@ __device__ __forceinline__ int tr_split_rows(int m, int b, int G)
   return iu < 0 ? 0 : (iu > m ? m : iu);
 }
 
+/*
+ * Float-float arithmetic: a value is an unevaluated sum h + l of two FP32 numbers (about 46
+ * significant bits), built from the error-free transformations TwoSum (Knuth) and TwoProd
+ * with FMA (Dekker / Ogita-Rump-Oishi 2005).  GB300's FP64 pipe issues about 2 FMAs per clock
+ * per SM and its FP32 pipe 128, so the tridiagonalisation keeps its trailing matrix and
+ * vectors in this form; every operation below is explicitly rounded (no contraction).
+ */
+struct ff2 {
+  float h, l;
+};
+
+__device__ __forceinline__ ff2 ff_make(float h, float l)
+{
+  ff2 r;
+  r.h = h;
+  r.l = l;
+  return r;
+}
+__device__ __forceinline__ ff2 ff_from_double(double x)
+{
+  const float h = __double2float_rn(x);
+  return ff_make(h, __double2float_rn(x - (double)h));
+}
+__device__ __forceinline__ double ff_to_double(ff2 a) { return (double)a.h + (double)a.l; }
+__device__ __forceinline__ ff2 ff_neg(ff2 a) { return ff_make(-a.h, -a.l); }
+/* a + b */
+__device__ __forceinline__ ff2 ff_add(ff2 a, ff2 b)
+{
+  const float s = __fadd_rn(a.h, b.h);
+  const float bb = __fsub_rn(s, a.h);
+  float err = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(b.h, bb));
+  err = __fadd_rn(err, __fadd_rn(a.l, b.l));
+  const float h = __fadd_rn(s, err);
+  return ff_make(h, __fsub_rn(err, __fsub_rn(h, s)));
+}
+/* a * b */
+__device__ __forceinline__ ff2 ff_mul(ff2 a, ff2 b)
+{
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  const float h = __fadd_rn(p, e);
+  return ff_make(h, __fsub_rn(e, __fsub_rn(h, p)));
+}
+/* a * b + c */
+__device__ __forceinline__ ff2 ff_fma(ff2 a, ff2 b, ff2 c)
+{
+  const float p = __fmul_rn(a.h, b.h);
+  float pe = __fmaf_rn(a.h, b.h, -p);
+  pe = __fmaf_rn(a.h, b.l, pe);
+  pe = __fmaf_rn(a.l, b.h, pe);
+  const float s = __fadd_rn(c.h, p);
+  const float bb = __fsub_rn(s, c.h);
+  float err = __fadd_rn(__fsub_rn(c.h, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+  err = __fadd_rn(err, __fadd_rn(c.l, pe));
+  const float h = __fadd_rn(s, err);
+  return ff_make(h, __fsub_rn(err, __fsub_rn(h, s)));
+}
+__device__ __forceinline__ ff2 ff_shfl_xor(ff2 a, int o)
+{
+  return ff_make(__shfl_xor_sync(0xFFFFFFFFu, a.h, o), __shfl_xor_sync(0xFFFFFFFFu, a.l, o));
+}
+__device__ __forceinline__ ff2 ff_load(const double *p)
+{
+  const float2 v = *reinterpret_cast<const float2 *>(p);
+  return ff_make(v.x, v.y);
+}
+__device__ __forceinline__ void ff_store(double *p, ff2 a)
+{
+  *reinterpret_cast<float2 *>(p) = make_float2(a.h, a.l);
+}
+
+/* block sum of one float-float per thread (fixed order), as a double in thread 0 */
+__device__ __forceinline__ double ff_block_sum(ff2 v, ff2 *red)
+{
+  for (int o = 16; o; o >>= 1) v = ff_add(v, ff_shfl_xor(v, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0) {
+    ff2 t = red[0];
+    for (int w = 1; w < TR_WARPS; ++w) t = ff_add(t, red[w]);
+    s = ff_to_double(t);
+  }
+  __syncthreads();
+  return s;
+}
+
+/* lower triangle (r >= q) of the double matrix to float-float pairs, in place */
+__global__ void k_tri_to_ff(double *A, int n)
+{
+  const int64_t total = (int64_t)n * n;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t q = idx / n, r = idx - q * n;
+    if (r >= q) ff_store(A + idx, ff_from_double(A[idx]));
+  }
+}
+
+/* per-step scalars, computed once per block by thread 0 (GB300's FP64 pipe is narrow, so
+ * scalar square roots and divisions are not repeated by every thread) */
+struct tr_step {
+  double beta, tau_c, scale_c;
+  ff2 alpha_pf, wpc, scale_cf;
+  int b1_u0, b1_u1, b2_u0, b2_u1;
+};
+
+/*
+ * A holds the lower triangle as float-float pairs on entry (k_tri_to_ff); vbuf/wbuf/ybuf
+ * [n] float-float vectors (as doubles' storage).  On exit the reflectors are FP64 again in
+ * A(c+2:n, c) and e on the subdiagonal, as cusolverDnDormtr(lower) reads them.
+ */
 __global__ void __launch_bounds__(TR_THREADS, 1)
-k_tridiag(double *A, int n, double *d, double *e, double *tau, double *wbuf, double *ybuf,
-          double *part_norm, double *part_dot, unsigned *bar, int *err)
+k_tridiag(double *A, int n, double *d, double *e, double *tau, double *vbuf, double *wbuf,
+          double *ybuf, double *part_norm, double *part_dot, unsigned *bar, int *err)
 {
   extern __shared__ double sh[];
-  double *svp = sh, *swp = sh + n, *svc = sh + 2 * n;
-  __shared__ double red[TR_WARPS];
-  __shared__ double bred[TR_WARPS][32];
+  double *svp = sh, *swp = sh + n, *svc = sh + 2 * n; /* float-float pairs */
+  __shared__ ff2 red[TR_WARPS];
+  __shared__ ff2 bred[TR_WARPS][32];
   __shared__ double s_slot;
+  __shared__ tr_step st;
   const int G = gridDim.x, b = blockIdx.x;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  unsigned *count = bar, *gen = bar + 1;
-  double tau_p = 0.0, scale_p = 0.0, e_p = 0.0;
+  const ff2 ONE = ff_make(1.f, 0.f), ZERO = ff_make(0.f, 0.f);
+  unsigned *count = bar;
+  unsigned target = 0;
+  double tau_p = 0.0, e_p = 0.0;
+  ff2 tau_pf = ZERO, scale_pf = ZERO;
   bool have_p = false;
   for (int c = 0; c < n - 1; ++c) {
     /* ---- A: w and storage of step c-1, column c update, partial ||x||^2 ---- */
-    double alpha_p = 0.0, wpc = 0.0;
     if (have_p) {
-      alpha_p = -0.5 * tau_p * tau_p * tr_sum_partials(part_dot, G, &s_slot);
-      wpc = tau_p * ybuf[c] + alpha_p; /* v_p(c) = 1 */
-    }
-    {
-      const int cnt = n - c, per = (cnt + G - 1) / G;
-      const int r0 = c + b * per, r1 = min(n, r0 + per);
-      double nrm = 0.0;
-      for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
-        double a = A[(int64_t)c * n + r];
-        if (have_p) {
-          const double vpr = (r == c) ? 1.0 : A[(int64_t)(c - 1) * n + r] * scale_p;
-          const double wpr = tau_p * ybuf[r] + alpha_p * vpr;
-          wbuf[r] = wpr;
-          A[(int64_t)(c - 1) * n + r] = (r == c) ? e_p : vpr;
-          a = a - vpr * wpc - wpr;
-        }
-        A[(int64_t)c * n + r] = a;
-        if (r >= c + 2) nrm = fma(a, a, nrm);
+      const double dsum = tr_sum_partials(part_dot, G, &s_slot);
+      if (threadIdx.x == 0) {
+        const double alpha_p = -0.5 * tau_p * tau_p * dsum;
+        st.alpha_pf = ff_from_double(alpha_p);
+        st.wpc = ff_fma(tau_pf, ff_load(ybuf + c), st.alpha_pf); /* v_p(c) = 1 */
       }
-      nrm = tr_block_sum(nrm, red);
-      if (threadIdx.x == 0) part_norm[b] = nrm;
-    }
-    if (!tr_grid_sync(count, gen, err)) return;
-    /* ---- reflector of column c (every block, same arithmetic) ---- */
-    const double xn2 = tr_sum_partials(part_norm, G, &s_slot);
-    const double alpha = A[(int64_t)c * n + c + 1];
-    double beta, tau_c, scale_c;
-    if (xn2 == 0.0) {
-      beta = alpha;
-      tau_c = 0.0;
-      scale_c = 0.0;
-    } else {
-      const double xn = sqrt(xn2);
-      const double ax = fabs(alpha), big = fmax(ax, xn), sml = fmin(ax, xn);
-      const double r = sml / big;
-      const double nrm = big * sqrt(1.0 + r * r);
-      beta = alpha >= 0.0 ? -nrm : nrm;
-      tau_c = (beta - alpha) / beta;
-      scale_c = 1.0 / (alpha - beta);
-    }
-    if (b == 0 && threadIdx.x == 0) {
-      d[c] = A[(int64_t)c * n + c];
-      e[c] = beta;
-      tau[c] = tau_c;
-    }
-    /* ---- B1: pending update + lower product, warp per column ---- */
-    const int m = n - c - 1;
-    for (int q = c + 1 + threadIdx.x; q < n; q += blockDim.x) {
-      svp[q] = have_p ? A[(int64_t)(c - 1) * n + q] : 0.0;
-      swp[q] = have_p ? wbuf[q] : 0.0;
-      svc[q] = (q == c + 1) ? 1.0 : A[(int64_t)c * n + q] * scale_c;
     }
     __syncthreads();
     {
-      const int u0 = tr_split_cols(m, b, G), u1 = tr_split_cols(m, b + 1, G);
+      const ff2 alpha_pf = st.alpha_pf, wpc = st.wpc;
+      const int cnt = n - c, per = (cnt + G - 1) / G;
+      const int r0 = c + b * per, r1 = min(n, r0 + per);
+      ff2 nrm = ZERO;
+      for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+        ff2 x = ff_load(A + (int64_t)c * n + r);
+        if (have_p) {
+          const ff2 vpr = (r == c) ? ONE : ff_mul(ff_load(A + (int64_t)(c - 1) * n + r), scale_pf);
+          const ff2 wpr = ff_fma(tau_pf, ff_load(ybuf + r), ff_mul(alpha_pf, vpr));
+          ff_store(wbuf + r, wpr);
+          ff_store(vbuf + r, vpr);
+          A[(int64_t)(c - 1) * n + r] = (r == c) ? e_p : ff_to_double(vpr); /* FP64 again */
+          x = ff_fma(ff_neg(vpr), wpc, x);
+          x = ff_add(x, ff_neg(wpr));
+        }
+        ff_store(A + (int64_t)c * n + r, x);
+        if (r >= c + 2) nrm = ff_fma(x, x, nrm);
+      }
+      const double ns = ff_block_sum(nrm, red);
+      if (threadIdx.x == 0) part_norm[b] = ns;
+    }
+    target += G;
+    if (!tr_grid_sync(count, target, err)) return;
+    /* ---- reflector of column c and this step's partitions ---- */
+    const int m = n - c - 1;
+    {
+      if (threadIdx.x == 32) st.b1_u0 = tr_split_cols(m, b, G);
+      if (threadIdx.x == 33) st.b1_u1 = tr_split_cols(m, b + 1, G);
+      if (threadIdx.x == 34) st.b2_u0 = tr_split_rows(m, b, G);
+      if (threadIdx.x == 35) st.b2_u1 = tr_split_rows(m, b + 1, G);
+      const double xn2 = tr_sum_partials(part_norm, G, &s_slot);
+      if (threadIdx.x == 0) {
+        const double alpha = ff_to_double(ff_load(A + (int64_t)c * n + c + 1));
+        if (xn2 == 0.0) {
+          st.beta = alpha;
+          st.tau_c = 0.0;
+          st.scale_c = 0.0;
+        } else {
+          const double xn = sqrt(xn2);
+          const double ax = fabs(alpha), big = fmax(ax, xn), sml = fmin(ax, xn);
+          const double rr = sml / big;
+          const double nrm = big * sqrt(1.0 + rr * rr);
+          st.beta = alpha >= 0.0 ? -nrm : nrm;
+          st.tau_c = (st.beta - alpha) / st.beta;
+          st.scale_c = 1.0 / (alpha - st.beta);
+        }
+        st.scale_cf = ff_from_double(st.scale_c);
+        if (b == 0) {
+          d[c] = ff_to_double(ff_load(A + (int64_t)c * n + c));
+          e[c] = st.beta;
+          tau[c] = st.tau_c;
+        }
+      }
+      __syncthreads();
+    }
+    const double beta = st.beta, tau_c = st.tau_c;
+    const ff2 scale_cf = st.scale_cf;
+    /* ---- B1: pending update + lower product, warp per column ---- */
+#pragma unroll 4
+    for (int q = c + 1 + threadIdx.x; q < n; q += blockDim.x) {
+      ff_store(svp + q, have_p ? ff_load(vbuf + q) : ZERO);
+      ff_store(swp + q, have_p ? ff_load(wbuf + q) : ZERO);
+      ff_store(svc + q, (q == c + 1) ? ONE : ff_mul(ff_load(A + (int64_t)c * n + q), scale_cf));
+    }
+    __syncthreads();
+    {
+      const int u0 = st.b1_u0, u1 = st.b1_u1;
       for (int u = u0 + warp; u < u1; u += TR_WARPS) {
         const int r = c + 1 + u;
-        const double vpr = svp[r], wpr = swp[r];
+        const ff2 vpr = ff_neg(ff_load(svp + r)), wpr = ff_neg(ff_load(swp + r));
         double *col = A + (int64_t)r * n;
-        double dot = 0.0;
-        if (have_p) {
-          for (int q = r + lane; q < n; q += 32) {
-            double a = col[q];
-            a = fma(-svp[q], wpr, a);
-            a = fma(-swp[q], vpr, a);
-            col[q] = a;
-            dot = fma(a, svc[q], dot);
+        ff2 dot = ZERO;
+        int q = r + lane;
+        /* TR_U independent loads per lane before the arithmetic (memory-level parallelism) */
+        for (; q + 32 * (TR_U - 1) < n; q += 32 * TR_U) {
+          ff2 a[TR_U];
+#pragma unroll
+          for (int k = 0; k < TR_U; ++k) a[k] = ff_load(col + q + 32 * k);
+#pragma unroll
+          for (int k = 0; k < TR_U; ++k) {
+            const int qq = q + 32 * k;
+            if (have_p) {
+              a[k] = ff_fma(ff_load(svp + qq), wpr, a[k]);
+              a[k] = ff_fma(ff_load(swp + qq), vpr, a[k]);
+              ff_store(col + qq, a[k]);
+            }
+            dot = ff_fma(a[k], ff_load(svc + qq), dot);
           }
-        } else {
-          for (int q = r + lane; q < n; q += 32) dot = fma(col[q], svc[q], dot);
         }
-        for (int o = 16; o; o >>= 1) dot += __shfl_down_sync(0xFFFFFFFFu, dot, o);
-        if (lane == 0) ybuf[r] = dot;
+        for (; q < n; q += 32) {
+          ff2 a = ff_load(col + q);
+          if (have_p) {
+            a = ff_fma(ff_load(svp + q), wpr, a);
+            a = ff_fma(ff_load(swp + q), vpr, a);
+            ff_store(col + q, a);
+          }
+          dot = ff_fma(a, ff_load(svc + q), dot);
+        }
+        for (int o = 16; o; o >>= 1) dot = ff_add(dot, ff_shfl_xor(dot, o));
+        if (lane == 0) ff_store(ybuf + r, dot);
       }
     }
-    if (!tr_grid_sync(count, gen, err)) return;
-    /* ---- B2: strictly lower part of the product, lanes over rows ---- */
+    target += G;
+    if (!tr_grid_sync(count, target, err)) return;
+    /* ---- B2: strictly lower part of the product.  A warp instruction covers RPP rows x
+     * (32/RPP) columns (RPP = 8, 16 or 32 from the block's row count) so that short row
+     * ranges keep every lane busy; loads stay coalesced along the rows of a column. ---- */
     {
-      const int u0 = tr_split_rows(m, b, G), u1 = tr_split_rows(m, b + 1, G);
-      double dpart = 0.0;
-      for (int ch = u0; ch < u1; ch += 32) {
-        const int u = ch + lane;
+      const int u0 = st.b2_u0, u1 = st.b2_u1;
+      const int nr = u1 - u0;
+      const int rpp = nr >= 32 ? 32 : (nr > 8 ? 16 : 8);
+      const int cpi = 32 / rpp;
+      const int lr = lane & (rpp - 1), lc = lane / rpp;
+      ff2 dpart = ZERO;
+      for (int ch = u0; ch < u1; ch += rpp) {
+        const int u = ch + lr;
         const int r = c + 1 + u;
         const bool valid = u < u1;
-        const int qend = c + 1 + min(ch + 32, u1); /* columns below the chunk's last row */
-        double acc = 0.0;
-        for (int q = c + 1 + warp; q < qend; q += TR_WARPS)
-          if (valid && q < r) acc = fma(A[(int64_t)q * n + r], svc[q], acc);
-        bred[warp][lane] = acc;
+        const int qend = c + 1 + min(ch + rpp, u1); /* columns below the chunk's last row */
+        const int qstep = TR_WARPS * cpi;
+        ff2 acc = ZERO;
+        for (int q0 = c + 1 + warp * cpi + lc; q0 < qend; q0 += qstep * TR_U) {
+          ff2 a[TR_U];
+#pragma unroll
+          for (int k = 0; k < TR_U; ++k) {
+            const int q = q0 + qstep * k;
+            a[k] = (valid && q < qend && q < r) ? ff_load(A + (int64_t)q * n + r) : ZERO;
+          }
+#pragma unroll
+          for (int k = 0; k < TR_U; ++k) {
+            const int q = q0 + qstep * k;
+            if (q < qend) acc = ff_fma(a[k], ff_load(svc + q), acc);
+          }
+        }
+        for (int o = rpp; o < 32; o <<= 1) acc = ff_add(acc, ff_shfl_xor(acc, o));
+        if (lc == 0) bred[warp][lr] = acc;
         __syncthreads();
-        if (warp == 0 && valid) {
-          double y1 = 0.0;
-          for (int w = 0; w < TR_WARPS; ++w) y1 += bred[w][lane];
-          const double y = ybuf[r] + y1;
-          ybuf[r] = y;
-          dpart = fma(y, svc[r], dpart);
+        if (warp == 0 && lane < rpp && valid) {
+          ff2 y1 = bred[0][lane];
+          for (int w = 1; w < TR_WARPS; ++w) y1 = ff_add(y1, bred[w][lane]);
+          const ff2 y = ff_add(ff_load(ybuf + r), y1);
+          ff_store(ybuf + r, y);
+          dpart = ff_fma(y, ff_load(svc + r), dpart);
         }
         __syncthreads();
       }
-      dpart = tr_block_sum(dpart, red);
-      if (threadIdx.x == 0) part_dot[b] = dpart;
+      const double ds = ff_block_sum(dpart, red);
+      if (threadIdx.x == 0) part_dot[b] = ds;
     }
-    if (!tr_grid_sync(count, gen, err)) return;
+    target += G;
+    if (!tr_grid_sync(count, target, err)) return;
     tau_p = tau_c;
-    scale_p = scale_c;
+    tau_pf = ff_from_double(tau_c);
+    scale_pf = scale_cf;
     e_p = beta;
     have_p = true;
   }
   /* last diagonal entry and the storage of the last reflector */
   if (b == 0) {
-    double alpha_p = 0.0;
-    if (have_p) alpha_p = -0.5 * tau_p * tau_p * tr_sum_partials(part_dot, G, &s_slot);
+    double dsum = 0.0;
+    if (have_p) dsum = tr_sum_partials(part_dot, G, &s_slot);
     if (threadIdx.x == 0) {
-      double a = A[(int64_t)(n - 1) * n + n - 1];
+      double a = ff_to_double(ff_load(A + (int64_t)(n - 1) * n + n - 1));
       if (have_p) {
-        const double wp = tau_p * ybuf[n - 1] + alpha_p;
+        const double alpha_p = -0.5 * tau_p * tau_p * dsum;
+        const double wp = tau_p * ff_to_double(ff_load(ybuf + n - 1)) + alpha_p;
         a = a - wp - wp;
         A[(int64_t)(n - 2) * n + n - 1] = e_p;
       }
@@ -621,20 +793,60 @@ int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, d
     return gp_fail(ctx, GP_ERR_SOLVER, "cusolverDnDormtr_bufferSize failed");
   int lw = lwork > lwork2 ? lwork : lwork2;
   size_t nd = (size_t)n;
-  size_t bytes = sizeof(double) * (5 * nd + (size_t)lw + 6 * nd * nv + 64) + sizeof(int) * 64;
+  const size_t G = (size_t)ctx->num_sms;
+  size_t bytes = sizeof(double) * (8 * nd + 2 * G + (size_t)lw + 6 * nd * nv + 72) +
+                 sizeof(int) * 64;
   double *base;
   int rc = gp_scratch(ctx, bytes, (void **)&base);
   if (rc) return rc;
   double *d = base, *e = d + nd, *tau = e + nd, *e2 = tau + nd, *w = e2 + nd;
-  double *ws = w + nd, *iw = ws + lw;
+  double *wbuf = w + nd, *ybuf = wbuf + nd, *vbuf = ybuf + nd, *parts = vbuf + nd;
+  unsigned *bar = (unsigned *)(parts + 2 * G);
+  double *ws = parts + 2 * G + 8, *iw = ws + lw;
   int *d_info = (int *)(iw + 6 * nd * nv + 8);
+  /* the cooperative tridiagonalisation (k_tridiag) unless GP_EIG_CUSOLVER_SYTRD=1, the
+   * vectors do not fit shared memory or the device cannot co-schedule one block per SM */
+  const char *senv = getenv("GP_EIG_CUSOLVER_SYTRD");
+  const size_t tr_smem = 24 * nd;
+  int coop = !(senv && senv[0] == '1') && n >= 2 && tr_smem <= 200 * 1024;
+  if (coop) {
+    int dev_coop = 0, per_sm = 0;
+    cudaDeviceGetAttribute(&dev_coop, cudaDevAttrCooperativeLaunch, ctx->device);
+    GP_CUDA(ctx, cudaFuncSetAttribute(k_tridiag, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)tr_smem));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tridiag, TR_THREADS, tr_smem);
+    coop = dev_coop && per_sm >= 1;
+  }
   GP_EIG_MARK(0);
-  if (cusolverDnDsytrd(h, CUBLAS_FILL_MODE_LOWER, n, ctx->d_xtx, n, d, e, tau, ws, lw, d_info) !=
-      CUSOLVER_STATUS_SUCCESS)
-    return gp_fail(ctx, GP_ERR_SOLVER, "cusolverDnDsytrd failed to launch");
-  GP_EIG_MARK(1);
   int info = 0;
-  GP_CUDA(ctx, gp_memcpy(ctx, &info, d_info, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  if (coop) {
+    int *d_err = ctx->d_err;
+    GP_CUDA(ctx, cudaMemsetAsync(d_err, 0, sizeof(int), ctx->stream));
+    GP_CUDA(ctx, cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), ctx->stream));
+    double *A = ctx->d_xtx, *pn = parts, *pd = parts + G;
+    int nn = n;
+    {
+      int64_t tot = (int64_t)n * n;
+      int blocks = (int)((tot + 255) / 256);
+      if (blocks > ctx->num_sms * 16) blocks = ctx->num_sms * 16;
+      k_tri_to_ff<<<blocks, 256, 0, ctx->stream>>>(A, n);
+      GP_LAUNCH_CHECK(ctx, "k_tri_to_ff");
+    }
+    void *args[] = {&A, &nn, &d, &e, &tau, &vbuf, &wbuf, &ybuf, &pn, &pd, &bar, &d_err};
+    GP_CUDA(ctx, cudaLaunchCooperativeKernel((const void *)k_tridiag, dim3((unsigned)G),
+                                             dim3(TR_THREADS), args, tr_smem, ctx->stream));
+    ctx->launches++;
+    int herr = 0;
+    GP_CUDA(ctx, gp_memcpy(ctx, &herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (herr) return gp_fail(ctx, GP_ERR_TIMEOUT, "tridiagonalisation grid barrier timed out");
+  } else {
+    if (cusolverDnDsytrd(h, CUBLAS_FILL_MODE_LOWER, n, ctx->d_xtx, n, d, e, tau, ws, lw,
+                         d_info) != CUSOLVER_STATUS_SUCCESS)
+      return gp_fail(ctx, GP_ERR_SOLVER, "cusolverDnDsytrd failed to launch");
+    GP_CUDA(ctx, gp_memcpy(ctx, &info, d_info, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  GP_EIG_MARK(1);
   /* Gershgorin bounds and the pivot guard need d, e on the host (2n doubles) */
   std::vector<double> hd(nd), he(nd > 1 ? nd - 1 : 1);
   GP_CUDA(ctx, gp_memcpy(ctx, hd.data(), d, sizeof(double) * nd, cudaMemcpyDeviceToHost, ctx->stream));

@@ -612,11 +612,14 @@ extern "C" int gp_snp_weights(gp_ctx *ctx, int32_t numeigs, double *ffvecs, doub
     rc = gp_scratch_aux(ctx, sizeof(double) * 2 * (size_t)nk * K, (void **)&tmp);
     if (rc) return rc;
     double *d_yg = tmp, *d_yo = tmp + (size_t)nk * K;
+    gp_tc_codes A;
+    rc = gp_tc_codes_for(ctx, 0, ctx->d_rows, n, kt.snprec, nk, &A);
+    if (rc) return rc;
     gp_tc_panel pw = {d_B, K, 1.0, 1};
-    rc = gp_geno_panel_tc(ctx, 0, ctx->d_rows, n, kt.snprec, nk, 1, &pw, K, d_yg, K);
+    rc = gp_geno_panel_tc_codes(ctx, &A, 1, &pw, K, d_yg, K);
     if (rc) return rc;
     pw.count = 0;
-    rc = gp_geno_panel_tc(ctx, 0, ctx->d_rows, n, kt.snprec, nk, 1, &pw, K, d_yo, K);
+    rc = gp_geno_panel_tc_codes(ctx, &A, 1, &pw, K, d_yo, K);
     if (rc) return rc;
     int b3 = (int)(((int64_t)nk * K + 255) / 256);
     if (b3 > ctx->num_sms * 16) b3 = ctx->num_sms * 16;
@@ -809,8 +812,11 @@ extern "C" int gp_lsqproj(gp_ctx *ctx, int32_t numeigs, const int32_t *samples, 
   }
   /* masked normal equations: co = O P (pair sums + observed count), rr = R E */
   if (ctx->precision != GP_PREC_FP64 && nk > 0) {
+    gp_tc_codes A;
+    rc = gp_tc_codes_for(ctx, 1, d_samp, nproj, kt.snprec, nk, &A);
+    if (rc) return rc;
     gp_tc_panel pc = {d_P, ldp, 1.0, 0};
-    rc = gp_geno_panel_tc(ctx, 1, d_samp, nproj, kt.snprec, nk, 1, &pc, ldp, d_co, ldp);
+    rc = gp_geno_panel_tc_codes(ctx, &A, 1, &pc, ldp, d_co, ldp);
     if (rc) return rc;
     double *tmp;
     rc = gp_scratch_aux(ctx, sizeof(double) * 2 * (size_t)nk * K, (void **)&tmp);
@@ -821,7 +827,7 @@ extern "C" int gp_lsqproj(gp_ctx *ctx, int32_t numeigs, const int32_t *samples, 
                                               ctx->d_xfancy, ctx->d_xmean, nk, K);
     GP_LAUNCH_CHECK(ctx, "k_scale_rows2");
     gp_tc_panel pr[2] = {{tmp, K, 1.0, 1}, {tmp + (size_t)nk * K, K, -1.0, 0}};
-    rc = gp_geno_panel_tc(ctx, 1, d_samp, nproj, kt.snprec, nk, 2, pr, K, d_rr, K);
+    rc = gp_geno_panel_tc_codes(ctx, &A, 2, pr, K, d_rr, K);
     if (rc) return rc;
   } else {
     rc = gp_geno_gemm_f64(ctx, 1, d_samp, nproj, kt.snprec, kt.ot, nk, d_P, ldp, ldp, d_co, ldp);

@@ -232,15 +232,17 @@ __device__ __forceinline__ bool tr_grid_sync(unsigned *count, unsigned target, i
     __threadfence();
     atomicAdd(count, 1u);
     const uint64_t t0 = globaltimer_ns();
-    while (*vcount < target) {
-      if (*verr) {
-        ok = 0;
-        break;
-      }
-      if (globaltimer_ns() - t0 > GP_WAIT_NS) {
-        atomicExch(err, TR_ERR_BARRIER);
-        ok = 0;
-        break;
+    for (unsigned it = 1; *vcount < target; ++it) {
+      if ((it & 63u) == 0) {
+        if (*verr) {
+          ok = 0;
+          break;
+        }
+        if (globaltimer_ns() - t0 > GP_WAIT_NS) {
+          atomicExch(err, TR_ERR_BARRIER);
+          ok = 0;
+          break;
+        }
       }
     }
     __threadfence();
@@ -438,11 +440,12 @@ k_tridiag(double *A, int n, double *d, double *e, double *tau, double *vbuf, dou
   for (int c = 0; c < n - 1; ++c) {
     /* ---- A: w and storage of step c-1, column c update, partial ||x||^2 ---- */
     if (have_p) {
+      const ff2 yc = ff_load(ybuf + c); /* issued before the reduction */
       const double dsum = tr_sum_partials(part_dot, G, &s_slot);
       if (threadIdx.x == 0) {
         const double alpha_p = -0.5 * tau_p * tau_p * dsum;
         st.alpha_pf = ff_from_double(alpha_p);
-        st.wpc = ff_fma(tau_pf, ff_load(ybuf + c), st.alpha_pf); /* v_p(c) = 1 */
+        st.wpc = ff_fma(tau_pf, yc, st.alpha_pf); /* v_p(c) = 1 */
       }
     }
     __syncthreads();
@@ -473,13 +476,21 @@ k_tridiag(double *A, int n, double *d, double *e, double *tau, double *vbuf, dou
     /* ---- reflector of column c and this step's partitions ---- */
     const int m = n - c - 1;
     {
+      /* v, w of step c-1 and the raw column x into shared memory while the norm is summed */
+#pragma unroll 4
+      for (int q = c + 1 + threadIdx.x; q < n; q += blockDim.x) {
+        ff_store(svp + q, have_p ? ff_load(vbuf + q) : ZERO);
+        ff_store(swp + q, have_p ? ff_load(wbuf + q) : ZERO);
+        ff_store(svc + q, ff_load(A + (int64_t)c * n + q));
+      }
       if (threadIdx.x == 32) st.b1_u0 = tr_split_cols(m, b, G);
       if (threadIdx.x == 33) st.b1_u1 = tr_split_cols(m, b + 1, G);
       if (threadIdx.x == 34) st.b2_u0 = tr_split_rows(m, b, G);
       if (threadIdx.x == 35) st.b2_u1 = tr_split_rows(m, b + 1, G);
+      const ff2 xa = ff_load(A + (int64_t)c * n + c + 1), xd = ff_load(A + (int64_t)c * n + c);
       const double xn2 = tr_sum_partials(part_norm, G, &s_slot);
       if (threadIdx.x == 0) {
-        const double alpha = ff_to_double(ff_load(A + (int64_t)c * n + c + 1));
+        const double alpha = ff_to_double(xa);
         if (xn2 == 0.0) {
           st.beta = alpha;
           st.tau_c = 0.0;
@@ -495,7 +506,7 @@ k_tridiag(double *A, int n, double *d, double *e, double *tau, double *vbuf, dou
         }
         st.scale_cf = ff_from_double(st.scale_c);
         if (b == 0) {
-          d[c] = ff_to_double(ff_load(A + (int64_t)c * n + c));
+          d[c] = ff_to_double(xd);
           e[c] = st.beta;
           tau[c] = st.tau_c;
         }
@@ -505,12 +516,8 @@ k_tridiag(double *A, int n, double *d, double *e, double *tau, double *vbuf, dou
     const double beta = st.beta, tau_c = st.tau_c;
     const ff2 scale_cf = st.scale_cf;
     /* ---- B1: pending update + lower product, warp per column ---- */
-#pragma unroll 4
-    for (int q = c + 1 + threadIdx.x; q < n; q += blockDim.x) {
-      ff_store(svp + q, have_p ? ff_load(vbuf + q) : ZERO);
-      ff_store(swp + q, have_p ? ff_load(wbuf + q) : ZERO);
-      ff_store(svc + q, (q == c + 1) ? ONE : ff_mul(ff_load(A + (int64_t)c * n + q), scale_cf));
-    }
+    for (int q = c + 1 + threadIdx.x; q < n; q += blockDim.x)
+      ff_store(svc + q, (q == c + 1) ? ONE : ff_mul(ff_load(svc + q), scale_cf));
     __syncthreads();
     {
       const int u0 = st.b1_u0, u1 = st.b1_u1;
@@ -556,12 +563,12 @@ k_tridiag(double *A, int n, double *d, double *e, double *tau, double *vbuf, dou
      * ranges keep every lane busy; loads stay coalesced along the rows of a column. ---- */
     {
       const int u0 = st.b2_u0, u1 = st.b2_u1;
-      const int nr = u1 - u0;
-      const int rpp = nr >= 32 ? 32 : (nr > 8 ? 16 : 8);
-      const int cpi = 32 / rpp;
-      const int lr = lane & (rpp - 1), lc = lane / rpp;
       ff2 dpart = ZERO;
-      for (int ch = u0; ch < u1; ch += rpp) {
+      for (int ch = u0, rpp = 32; ch < u1; ch += rpp) {
+        const int rem = u1 - ch;
+        rpp = rem >= 32 ? 32 : (rem > 8 ? 16 : 8);
+        const int cpi = 32 / rpp;
+        const int lr = lane & (rpp - 1), lc = lane / rpp;
         const int u = ch + lr;
         const int r = c + 1 + u;
         const bool valid = u < u1;

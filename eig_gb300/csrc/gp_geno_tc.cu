@@ -288,117 +288,201 @@ k_geno_panel_tc(const __grid_constant__ CUtensorMap tm_b, const uint8_t *__restr
 
 /*
  * sum over SNPs: codes[r][k] = code of sample samp[r] at kept SNP k (record snprec[k]);
- * row stride ldc bytes; pad k (>= nk) and pad rows are 3.  Thread = (row, 16-byte k group).
+ * row stride ldc bytes; pad k (>= nk) and pad rows are 3.  A transpose through shared
+ * memory: CTA (kt, rt) covers 128 kept SNPs x 128 rows; when the rows' samples span at most
+ * CB_SPAN record bytes, the 128 records' byte ranges are read once (coalesced), and two
+ * threads build each row's 32 output bytes; wider spans read per thread.
  */
-__global__ void k_codes_by_sample(const uint8_t *__restrict__ geno, int64_t rlen,
-                                  const int32_t *__restrict__ samp, int32_t nsamp,
-                                  int32_t nrows_pad, const int32_t *__restrict__ snprec,
-                                  int32_t nk, int64_t ldc, uint8_t *codes)
+#define CB_SNP 128
+#define CB_ROWS 128
+#define CB_SPAN 64
+#define CB_PITCH_W (CB_SPAN / 4 + 1)
+__global__ void __launch_bounds__(256)
+k_codes_by_sample(const uint8_t *__restrict__ geno, int64_t rlen, const int32_t *__restrict__ samp,
+                  int32_t nsamp, int32_t nrows_pad, const int32_t *__restrict__ snprec, int32_t nk,
+                  int64_t ldc, uint8_t *codes)
 {
-  const int64_t groups = ldc / 16;
-  int64_t total = (int64_t)nrows_pad * groups;
-  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
-       idx += (int64_t)gridDim.x * blockDim.x) {
-    int64_t r = idx % nrows_pad, gq = idx / nrows_pad; /* consecutive threads: consecutive rows */
-    uint32_t out[4] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
-    if (r < nsamp) {
-      int32_t sidx = samp[r];
-      int32_t byte = sidx >> 2, sh = (3 - (sidx & 3)) * 2;
-#pragma unroll 4
-      for (int j = 0; j < 64; ++j) {
-        int64_t k = gq * 64 + j;
-        uint32_t c = 3u;
-        if (k < nk) c = (__ldg(geno + (int64_t)snprec[k] * rlen + byte) >> sh) & 3u;
-        /* code j of the group: byte j>>2 (word j>>4), bits (3-(j&3))*2 within the byte */
-        uint32_t wpos = (uint32_t)((j >> 2) & 3) * 8u + (3u - (uint32_t)(j & 3)) * 2u;
-        out[j >> 4] = (out[j >> 4] & ~(3u << wpos)) | (c << wpos);
-      }
-    }
-    *(uint4 *)(codes + r * ldc + gq * 16) = make_uint4(out[0], out[1], out[2], out[3]);
+  __shared__ uint32_t srec[CB_SNP][CB_PITCH_W];
+  __shared__ int64_t soff[CB_SNP];
+  const int tid = threadIdx.x;
+  const int32_t k0 = blockIdx.x * CB_SNP, r0 = blockIdx.y * CB_ROWS;
+  int32_t base = 0, span = 0;
+  if (r0 < nsamp) {
+    const int32_t rl = (r0 + CB_ROWS < nsamp ? r0 + CB_ROWS : nsamp) - 1;
+    base = (samp[r0] >> 2) & ~15;
+    span = (samp[rl] >> 2) - base + 1;
   }
+  const bool fast = span <= CB_SPAN;
+  if (tid < CB_SNP) soff[tid] = (k0 + tid < nk) ? (int64_t)snprec[k0 + tid] * rlen : -1;
+  __syncthreads();
+  if (fast && span > 0) {
+    const int nvec = (span + 15) >> 4;
+    for (int i = tid; i < CB_SNP * nvec; i += blockDim.x) {
+      const int u = i / nvec, v = i - u * nvec;
+      uint4 val = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
+      if (soff[u] >= 0) val = __ldg((const uint4 *)(geno + soff[u] + base + 16 * v));
+      srec[u][4 * v] = val.x;
+      srec[u][4 * v + 1] = val.y;
+      srec[u][4 * v + 2] = val.z;
+      srec[u][4 * v + 3] = val.w;
+    }
+  }
+  __syncthreads();
+  const int rl = tid >> 1, half = tid & 1;
+  const int32_t r = r0 + rl;
+  if (r >= nrows_pad || (int64_t)k0 + 64 * half >= ldc * 4) return;
+  uint32_t out[4] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
+  if (r < nsamp) {
+    const int32_t sidx = samp[r];
+    const int32_t bb = (sidx >> 2) - base, sh = (3 - (sidx & 3)) * 2;
+#pragma unroll 8
+    for (int j = 0; j < 64; ++j) {
+      const int u = 64 * half + j;
+      uint32_t byte = 0xFFu;
+      if (soff[u] >= 0)
+        byte = fast ? (srec[u][bb >> 2] >> ((bb & 3) * 8)) & 0xFFu : __ldg(geno + soff[u] + (sidx >> 2));
+      const uint32_t c = (byte >> sh) & 3u;
+      /* code j of the group: byte j>>2 (word j>>4), bits (3-(j&3))*2 within the byte */
+      const uint32_t wpos = (uint32_t)((j >> 2) & 3) * 8u + (3u - (uint32_t)(j & 3)) * 2u;
+      out[j >> 4] = (out[j >> 4] & ~(3u << wpos)) | (c << wpos);
+    }
+  }
+  *(uint4 *)(codes + (int64_t)r * ldc + (k0 >> 2) + 16 * half) = make_uint4(out[0], out[1], out[2], out[3]);
 }
 
 /*
  * sum over samples: codes[k][j] = code of sample samp[j] at kept SNP k; one row per kept
- * SNP, j over the nsamp samples; pad j and pad rows are 3.
+ * SNP, j over the nsamp samples; pad j and pad rows are 3.  One warp per SNP row: the
+ * record is staged in shared memory (coalesced), then each lane gathers its 64-sample
+ * groups from it.  Dynamic shared memory: warps x rlen bytes.
  */
-__global__ void k_codes_by_snp(const uint8_t *__restrict__ geno, int64_t rlen,
-                               const int32_t *__restrict__ samp, int32_t nsamp,
-                               const int32_t *__restrict__ snprec, int32_t nk, int32_t nrows_pad,
-                               int64_t ldc, uint8_t *codes)
+__global__ void __launch_bounds__(256)
+k_codes_by_snp(const uint8_t *__restrict__ geno, int64_t rlen, const int32_t *__restrict__ samp,
+               int32_t nsamp, const int32_t *__restrict__ snprec, int32_t nk, int32_t nrows_pad,
+               int64_t ldc, uint8_t *codes)
 {
+  extern __shared__ uint4 srec4[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  uint8_t *rec_s = (uint8_t *)(srec4 + (int64_t)warp * (rlen / 16));
   const int64_t groups = ldc / 16;
-  int64_t total = (int64_t)nrows_pad * groups;
-  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
-       idx += (int64_t)gridDim.x * blockDim.x) {
-    int64_t k = idx / groups, gq = idx % groups; /* consecutive threads: same SNP */
-    uint32_t out[4] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
+  for (int64_t k = (int64_t)blockIdx.x * nw + warp; k < nrows_pad; k += (int64_t)gridDim.x * nw) {
     if (k < nk) {
-      const uint8_t *rec = geno + (int64_t)snprec[k] * rlen;
-#pragma unroll 4
-      for (int j = 0; j < 64; ++j) {
-        int64_t q = gq * 64 + j;
-        uint32_t c = 3u;
-        if (q < nsamp) {
-          int32_t sidx = samp[q];
-          c = (__ldg(rec + (sidx >> 2)) >> ((3 - (sidx & 3)) * 2)) & 3u;
+      const uint4 *src = (const uint4 *)(geno + (int64_t)snprec[k] * rlen);
+      for (int64_t v = lane; v < rlen / 16; v += 32) ((uint4 *)rec_s)[v] = __ldg(src + v);
+    }
+    __syncwarp();
+    for (int64_t gq = lane; gq < groups; gq += 32) {
+      uint32_t out[4] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
+      if (k < nk) {
+#pragma unroll 8
+        for (int j = 0; j < 64; ++j) {
+          const int64_t q = gq * 64 + j;
+          uint32_t c = 3u;
+          if (q < nsamp) {
+            const int32_t sidx = samp[q];
+            c = (rec_s[sidx >> 2] >> ((3 - (sidx & 3)) * 2)) & 3u;
+          }
+          const uint32_t wpos = (uint32_t)((j >> 2) & 3) * 8u + (3u - (uint32_t)(j & 3)) * 2u;
+          out[j >> 4] = (out[j >> 4] & ~(3u << wpos)) | (c << wpos);
         }
-        uint32_t wpos = (uint32_t)((j >> 2) & 3) * 8u + (3u - (uint32_t)(j & 3)) * 2u;
-        out[j >> 4] = (out[j >> 4] & ~(3u << wpos)) | (c << wpos);
       }
+      *(uint4 *)(codes + k * ldc + gq * 16) = make_uint4(out[0], out[1], out[2], out[3]);
     }
-    *(uint4 *)(codes + k * ldc + gq * 16) = make_uint4(out[0], out[1], out[2], out[3]);
-  }
-}
-
-/* per column c of P [nk][ldp] (FP64): exponent e_c with max|P| < 2^e_c (ncols columns) */
-__global__ void k_panel_exponent(const double *P, int64_t ldp, int32_t nk, int32_t ncols,
-                                 int32_t *expo)
-{
-  __shared__ double red[256];
-  for (int32_t c = blockIdx.x; c < ncols; c += gridDim.x) {
-    double m = 0.0;
-    for (int32_t k = threadIdx.x; k < nk; k += blockDim.x) m = fmax(m, fabs(P[(int64_t)k * ldp + c]));
-    red[threadIdx.x] = m;
-    __syncthreads();
-    for (int o = blockDim.x / 2; o; o >>= 1) {
-      if ((int)threadIdx.x < o) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + o]);
-      __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-      double mx = red[0];
-      int e = 0;
-      if (mx > 0.0) {
-        frexp(mx, &e); /* mx = f 2^e, f in [0.5, 1) -> mx < 2^e */
-      }
-      expo[c] = e;
-    }
-    __syncthreads();
+    __syncwarp();
   }
 }
 
 /*
- * B[(4c+t)][k] (fp16, row stride ldb elements) = slice t of P[k][c] / 2^e_c, for k < nk
- * (pad k and pad rows zero are written by a memset before).  Rows of P beyond koff..: the
- * panel block [koff, koff+nk) of a concatenated k range goes to columns koff + k of B.
+ * per column c of P [nk][ldp] (FP64): running max of |P[k][c]| as its bit pattern (the
+ * order of non-negative doubles), folded into mx[c] with atomicMax; threads keep a fixed
+ * column so that a warp reads rows of P contiguously.  Several panels may fold into the
+ * same mx (their joint exponent).
  */
-__global__ void k_panel_slices(const double *P, int64_t ldp, int32_t nk, int32_t ncols,
-                               const int32_t *expo, double sign, int64_t koff, __half *B,
-                               int64_t ldb)
+__global__ void k_panel_absmax(const double *__restrict__ P, int64_t ldp, int32_t nk,
+                               int32_t ncols, unsigned long long *mx)
 {
-  int64_t total = (int64_t)nk * ncols;
-  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
-       idx += (int64_t)gridDim.x * blockDim.x) {
-    int64_t k = idx / ncols;
-    int32_t c = (int32_t)(idx - k * ncols);
-    double x = ldexp(sign * P[k * ldp + c], -expo[c]); /* |x| < 1 (exact scaling) */
-    double r = x * 1024.0;
+  __shared__ unsigned long long smx[1024];
+  for (int c = threadIdx.x; c < ncols; c += blockDim.x) smx[c] = 0ull;
+  __syncthreads();
+  const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
+  const int64_t step = nthreads / ncols * ncols;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < step) {
+    const int32_t c = (int32_t)(t % ncols);
+    unsigned long long m = 0ull;
+    const int64_t total = (int64_t)nk * ncols;
+    for (int64_t idx = t; idx < total; idx += step) {
+      const int64_t k = idx / ncols;
+      const unsigned long long bits =
+          (unsigned long long)__double_as_longlong(P[k * ldp + c]) & 0x7FFFFFFFFFFFFFFFull;
+      m = bits > m ? bits : m;
+    }
+    if (m) atomicMax(smx + c, m);
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < ncols; c += blockDim.x)
+    if (smx[c]) atomicMax(mx + c, smx[c]);
+}
+
+/* exponent e_c with max|P| < 2^e_c (frexp), 0 for an all-zero column */
+__global__ void k_panel_expo(const unsigned long long *mx, int32_t ncols, int32_t *expo)
+{
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncols; c += gridDim.x * blockDim.x) {
+    const double v = __longlong_as_double((long long)mx[c]);
+    int e = 0;
+    if (v > 0.0) frexp(v, &e); /* v = f 2^e, f in [0.5, 1) -> v < 2^e */
+    expo[c] = e;
+  }
+}
+
+/*
+ * B[(4c+t)][koff + k] (fp16, row stride ldb elements) = slice t of sign P[k][c] / 2^e_c for
+ * k < nk (pad k and pad rows are zero from a memset before): x = sign P / 2^e_c (|x| < 1,
+ * exact) is cut into four balanced base-1024 digits, digit t = rint(x 1024^(t+1)) minus the
+ * digits before, so that x = sum_t d_t 1024^-(t+1) + O(2^-41).  A tile of 64 k x 32 columns
+ * is read row-wise (coalesced) into shared memory and written as 128-byte rows of B.
+ */
+#define SL_K 64
+#define SL_C 32
+__global__ void __launch_bounds__(256)
+k_panel_slices(const double *__restrict__ P, int64_t ldp, int32_t nk, int32_t ncols,
+               const int32_t *__restrict__ expo, double sign, int64_t koff, __half *B, int64_t ldb)
+{
+  __shared__ double sp[SL_K][SL_C + 1];
+  __shared__ __align__(16) __half ss[SL_C * 4][SL_K + 8];
+  __shared__ double sscale[SL_C];
+  const int tid = threadIdx.x;
+  const int32_t kt0 = blockIdx.x * SL_K, ct0 = blockIdx.y * SL_C;
+  if (tid < SL_C) {
+    const int32_t c = ct0 + tid;
+    sscale[tid] = c < ncols ? ldexp(sign, -expo[c]) : 0.0;
+  }
+  for (int i = tid; i < SL_K * SL_C; i += blockDim.x) {
+    const int kk = i / SL_C, cc = i - kk * SL_C;
+    const int32_t k = kt0 + kk, c = ct0 + cc;
+    sp[kk][cc] = (k < nk && c < ncols) ? P[(int64_t)k * ldp + c] : 0.0;
+  }
+  __syncthreads();
+  for (int i = tid; i < SL_K * SL_C; i += blockDim.x) {
+    const int cc = i / SL_K, kk = i - cc * SL_K;
+    double r = sp[kk][cc] * sscale[cc] * 1024.0; /* exact: powers of two */
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
-      double qv = rint(r);
+      const double qv = rint(r);
       r = (r - qv) * 1024.0; /* exact: r - qv is the low part of r */
-      B[(int64_t)(4 * c + t) * ldb + koff + k] = __double2half(qv);
+      ss[4 * cc + t][kk] = __double2half(qv);
     }
+  }
+  __syncthreads();
+  /* 128 output rows x 64 halves: 8 threads write one row's 128 bytes */
+  for (int i = tid; i < SL_C * 4 * 8; i += blockDim.x) {
+    const int o = i >> 3, seg = i & 7;
+    const int32_t c = ct0 + (o >> 2);
+    if (c >= ncols) continue;
+    const int32_t k = kt0 + seg * 8;
+    if (k >= nk) continue;
+    __half *dst = B + (int64_t)(4 * ct0 + o) * ldb + koff + k;
+    *(uint4 *)dst = *(const uint4 *)&ss[o][seg * 8];
   }
 }
 
@@ -461,13 +545,25 @@ int gp_tc_build_codes(gp_ctx *ctx, int sum_over_snps, const int32_t *d_samp, int
   int64_t ldc;
   int32_t nrows_pad;
   gp_tc_code_bytes(sum_over_snps, nsamp, nk, &ldc, &nrows_pad);
-  int64_t work = (int64_t)nrows_pad * (ldc / 16);
-  if (sum_over_snps)
-    k_codes_by_sample<<<grid_cap(ctx, work, 256, 32), 256, 0, ctx->stream>>>(
-        ctx->d_geno, ctx->rlen_dev, d_samp, nsamp, nrows_pad, d_snprec, nk, ldc, codes);
-  else
-    k_codes_by_snp<<<grid_cap(ctx, work, 256, 32), 256, 0, ctx->stream>>>(
-        ctx->d_geno, ctx->rlen_dev, d_samp, nsamp, d_snprec, nk, nrows_pad, ldc, codes);
+  if (sum_over_snps) {
+    dim3 grid((unsigned)((ldc * 4 + CB_SNP - 1) / CB_SNP), (unsigned)((nrows_pad + CB_ROWS - 1) / CB_ROWS));
+    k_codes_by_sample<<<grid, 256, 0, ctx->stream>>>(ctx->d_geno, ctx->rlen_dev, d_samp, nsamp,
+                                                     nrows_pad, d_snprec, nk, ldc, codes);
+  } else {
+    int warps = (int)((200 * 1024) / ctx->rlen_dev);
+    if (warps > 8) warps = 8;
+    if (warps < 1)
+      return gp_fail(ctx, GP_ERR_ARG, "gp_tc_build_codes: records of %lld bytes are too long",
+                     (long long)ctx->rlen_dev);
+    const size_t smem = (size_t)warps * ctx->rlen_dev;
+    GP_CUDA(ctx, cudaFuncSetAttribute(k_codes_by_snp, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+    int blocks = (int)((nrows_pad + warps - 1) / warps);
+    if (blocks > ctx->num_sms * 16) blocks = ctx->num_sms * 16;
+    k_codes_by_snp<<<blocks, 32 * warps, smem, ctx->stream>>>(ctx->d_geno, ctx->rlen_dev, d_samp,
+                                                              nsamp, d_snprec, nk, nrows_pad, ldc,
+                                                              codes);
+  }
   GP_LAUNCH_CHECK(ctx, "k_codes");
   out->codes = codes;
   out->ldc = ldc;
@@ -481,8 +577,7 @@ size_t gp_tc_prepared_bytes(int npanels, int32_t ncols, int32_t k0)
 {
   const int32_t kpad0 = (k0 + XK - 1) / XK * XK;
   const int32_t ncols4_pad = (4 * ncols + XT - 1) / XT * XT;
-  return align256((size_t)ncols4_pad * kpad0 * npanels * 2) +
-         align256((size_t)ncols * npanels * 4 + 4 * (size_t)ncols) + 256;
+  return align256((size_t)ncols4_pad * kpad0 * npanels * 2) + align256((size_t)ncols * 16) + 256;
 }
 
 int gp_tc_prepare(gp_ctx *ctx, int npanels, const gp_tc_panel *pp, int32_t ncols, int32_t k0,
@@ -495,35 +590,24 @@ int gp_tc_prepare(gp_ctx *ctx, int npanels, const gp_tc_panel *pp, int32_t ncols
   const int64_t ldb = (int64_t)kpad0 * npanels;
   uint8_t *base = (uint8_t *)storage;
   __half *B = (__half *)base;
-  int32_t *expo = (int32_t *)(base + align256((size_t)ncols4_pad * ldb * 2));
-  int32_t *expo_p = expo + ncols; /* per-panel exponents, then the joint one */
+  uint8_t *ebase = base + align256((size_t)ncols4_pad * ldb * 2);
+  unsigned long long *mx = (unsigned long long *)ebase; /* [ncols] joint max |P| bits */
+  int32_t *expo = (int32_t *)(ebase + 8 * (size_t)ncols);
+  GP_CUDA(ctx, cudaMemsetAsync(mx, 0, 8 * (size_t)ncols, ctx->stream));
   for (int p = 0; p < npanels; ++p) {
-    k_panel_exponent<<<ncols < 1024 ? ncols : 1024, 256, 0, ctx->stream>>>(
-        pp[p].P, pp[p].ldp, k0, ncols, expo_p + p * ncols);
-    GP_LAUNCH_CHECK(ctx, "k_panel_exponent");
+    int blocks = grid_cap(ctx, (int64_t)k0 * ncols, 256 * 16, 8);
+    const int need = (ncols + 255) / 256;
+    if (blocks < need) blocks = need;
+    k_panel_absmax<<<blocks, 256, 0, ctx->stream>>>(pp[p].P, pp[p].ldp, k0, ncols, mx);
+    GP_LAUNCH_CHECK(ctx, "k_panel_absmax");
   }
-  if (npanels == 1) {
-    GP_CUDA(ctx, cudaMemcpyAsync(expo, expo_p, sizeof(int32_t) * ncols, cudaMemcpyDeviceToDevice,
-                                 ctx->stream));
-  } else {
-    std::vector<int32_t> he((size_t)ncols * npanels);
-    GP_CUDA(ctx, gp_memcpy(ctx, he.data(), expo_p, sizeof(int32_t) * he.size(),
-                           cudaMemcpyDeviceToHost, ctx->stream));
-    GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    std::vector<int32_t> j((size_t)ncols);
-    for (int32_t c = 0; c < ncols; ++c) {
-      int e = he[(size_t)c];
-      for (int p = 1; p < npanels; ++p) e = he[(size_t)p * ncols + c] > e ? he[(size_t)p * ncols + c] : e;
-      j[(size_t)c] = e;
-    }
-    GP_CUDA(ctx, gp_memcpy(ctx, expo, j.data(), sizeof(int32_t) * ncols, cudaMemcpyHostToDevice,
-                           ctx->stream));
-  }
+  k_panel_expo<<<(ncols + 255) / 256, 256, 0, ctx->stream>>>(mx, ncols, expo);
+  GP_LAUNCH_CHECK(ctx, "k_panel_expo");
   GP_CUDA(ctx, cudaMemsetAsync(B, 0, (size_t)ncols4_pad * ldb * 2, ctx->stream));
   for (int p = 0; p < npanels; ++p) {
-    int64_t work = (int64_t)k0 * ncols;
-    k_panel_slices<<<grid_cap(ctx, work, 256, 32), 256, 0, ctx->stream>>>(
-        pp[p].P, pp[p].ldp, k0, ncols, expo, pp[p].sign, (int64_t)p * kpad0, B, ldb);
+    dim3 sgrid((unsigned)((k0 + SL_K - 1) / SL_K), (unsigned)((ncols + SL_C - 1) / SL_C));
+    k_panel_slices<<<sgrid, 256, 0, ctx->stream>>>(pp[p].P, pp[p].ldp, k0, ncols, expo,
+                                                   pp[p].sign, (int64_t)p * kpad0, B, ldb);
     GP_LAUNCH_CHECK(ctx, "k_panel_slices");
   }
   PFN_cuTensorMapEncodeTiled_v12000 enc = tc_encode(ctx);
@@ -607,6 +691,27 @@ int gp_geno_panel_tc_codes(gp_ctx *ctx, const gp_tc_codes *A, int npanels, const
   rc = gp_tc_prepare(ctx, npanels, pp, ncols, A->k0, storage, &P);
   if (rc) return rc;
   return gp_tc_apply(ctx, A, &P, d_Y, ldy, 1);
+}
+
+int gp_tc_codes_for(gp_ctx *ctx, int sum_over_snps, const int32_t *d_samp, int32_t nsamp,
+                    const int32_t *d_snprec, int32_t nk, gp_tc_codes *out)
+{
+  if (!sum_over_snps && nsamp == ctx->nind_all) {
+    /* every sample in order: the resident records are the SNP-major operand */
+    out->codes = ctx->d_geno;
+    out->ldc = ctx->rlen_dev;
+    out->row_map = d_snprec;
+    out->nrows = nk;
+    out->k0 = nsamp;
+    return GP_OK;
+  }
+  int64_t ldc;
+  int32_t rows_pad;
+  gp_tc_code_bytes(sum_over_snps, nsamp, nk, &ldc, &rows_pad);
+  uint8_t *codes;
+  int rc = gp_scratch4(ctx, (size_t)rows_pad * ldc + 256, (void **)&codes);
+  if (rc) return rc;
+  return gp_tc_build_codes(ctx, sum_over_snps, d_samp, nsamp, d_snprec, nk, codes, out);
 }
 
 int gp_geno_panel_tc(gp_ctx *ctx, int sum_over_snps, const int32_t *d_samp, int32_t nsamp,

@@ -48,6 +48,10 @@ int gp_tc_prepare(gp_ctx *ctx, int npanels, const gp_tc_panel *pp, int32_t ncols
 int gp_tc_apply(gp_ctx *ctx, const gp_tc_codes *A, const gp_tc_prepared *P, double *d_Y,
                 int64_t ldy, int sync);
 
+/* the code operand of gp_geno_panel_tc (built into scratch4, or the resident records when a
+ * SNP-major operand covers every sample in order) */
+int gp_tc_codes_for(gp_ctx *ctx, int sum_over_snps, const int32_t *d_samp, int32_t nsamp,
+                    const int32_t *d_snprec, int32_t nk, gp_tc_codes *out);
 /* Y[r][c] = sum_p sum_k A(r, k) sign_p P_p[k][c] with a prepared code operand */
 int gp_geno_panel_tc_codes(gp_ctx *ctx, const gp_tc_codes *A, int npanels, const gp_tc_panel *pp,
                            int32_t ncols, double *d_Y, int64_t ldy);

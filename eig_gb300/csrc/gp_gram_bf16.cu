@@ -59,14 +59,48 @@
 #define GP_KERR_TIMEOUT_EMPTY 2
 #define GP_KERR_TIMEOUT_ACCF 3
 #define GP_KERR_TIMEOUT_ACCE 4
+#define GP_KERR_TIMEOUT_SYNC 5
+#define GRAM_SYNC_KB 64 /* k-blocks between the producers' lockstep points */
 
-__device__ __forceinline__ void tri_tile(int32_t t, int32_t *bi, int32_t *bj)
+__device__ __forceinline__ int32_t tri_root(int32_t t)
 {
   int32_t i = (int32_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
   while ((i + 1) * (i + 2) / 2 <= t) ++i;
   while (i * (i + 1) / 2 > t) --i;
-  *bi = i;
-  *bj = t - i * (i + 1) / 2;
+  return i;
+}
+
+/*
+ * Tile t of the lower triangle of nt x nt tiles, in groups: the tile grid is cut into
+ * GRAM_GROUP x GRAM_GROUP blocks (lower triangle of blocks, row by row), tiles row by row
+ * inside a block.  The CTAs that run at the same time then hold tiles of a few row blocks
+ * and walk the SNPs at the same pace, so the operand boxes they load are shared in L2
+ * instead of being read from HBM once per tile.
+ */
+#define GRAM_GROUP 12
+__device__ __forceinline__ void tri_tile(int32_t t, int32_t nt, int32_t *bi, int32_t *bj)
+{
+  const int32_t ng = (nt + GRAM_GROUP - 1) / GRAM_GROUP;
+  for (int32_t gi = 0; gi < ng; ++gi) {
+    const int32_t r0 = gi * GRAM_GROUP, nr = min(nt, r0 + GRAM_GROUP) - r0;
+    for (int32_t gj = 0; gj <= gi; ++gj) {
+      const int32_t c0 = gj * GRAM_GROUP, nc = min(nt, c0 + GRAM_GROUP) - c0;
+      const int32_t cnt = gi == gj ? nr * (nr + 1) / 2 : nr * nc;
+      if (t < cnt) {
+        if (gi == gj) {
+          const int32_t i = tri_root(t);
+          *bi = r0 + i;
+          *bj = c0 + t - i * (i + 1) / 2;
+        } else {
+          *bi = r0 + t / nc;
+          *bj = c0 + t % nc;
+        }
+        return;
+      }
+      t -= cnt;
+    }
+  }
+  *bi = *bj = 0; /* not reached for t < ntiles */
 }
 
 /*
@@ -78,7 +112,7 @@ template <int FP16, int NMMA>
 __global__ void __launch_bounds__(GRAM_THREADS, 1)
 k_gram_split(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ CUtensorMap tm_lo,
                   int32_t ntiles, int32_t nkb, int32_t chunk_kb, double *xtx, int32_t n,
-                  int32_t accumulate, int *err)
+                  int32_t accumulate, unsigned *sync_ctr, int *err)
 {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -90,6 +124,7 @@ k_gram_split(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ 
   uint64_t *drain = bars + 2 * NSTAGE + 4; /* abort path: wait for issued MMAs */
   uint32_t *tmem_slot = (uint32_t *)(bars + 2 * NSTAGE + 5);
   volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
+  const int32_t nt_rows = tri_root(ntiles - 1) + 1; /* tile rows of the lower triangle */
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
@@ -120,10 +155,35 @@ k_gram_split(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ 
     /* ---------------- TMA producer ---------------- */
     if (lane == 0) {
       uint32_t it = 0;
+      const int32_t nsync = (nkb + GRAM_SYNC_KB - 1) / GRAM_SYNC_KB;
       for (int32_t t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x) {
         int32_t bi, bj;
-        tri_tile(t, &bi, &bj);
+        tri_tile(t, nt_rows, &bi, &bj);
+        /* the CTAs of one wave (tiles t / gridDim) meet every GRAM_SYNC_KB k-blocks, so that
+         * the boxes one of them loads are still in L2 when the others need them */
+        const int32_t wave = t / (int32_t)gridDim.x;
+        const unsigned wave_n = (unsigned)min((int32_t)gridDim.x, ntiles - wave * (int32_t)gridDim.x);
         for (int32_t kb = 0; kb < nkb; ++kb, ++it) {
+          if (kb > 0 && kb % GRAM_SYNC_KB == 0) {
+            unsigned *ctr = sync_ctr + (int64_t)wave * nsync + kb / GRAM_SYNC_KB;
+            atomicAdd(ctr, 1u);
+            volatile unsigned *vc = ctr;
+            const uint64_t t0 = globaltimer_ns();
+            bool ok = true;
+            while (*vc < wave_n) {
+              if (*abort_flag) {
+                ok = false;
+                break;
+              }
+              if (globaltimer_ns() - t0 > GP_WAIT_NS) {
+                atomicExch(err, GP_KERR_TIMEOUT_SYNC);
+                *abort_flag = 1;
+                ok = false;
+                break;
+              }
+            }
+            if (!ok) break;
+          }
           uint32_t s = it % NSTAGE, ph = (it / NSTAGE) & 1u;
           if (!mbar_wait(&empty[s], ph ^ 1u, abort_flag, err, GP_KERR_TIMEOUT_EMPTY)) break;
           uint8_t *st = smem + s * STAGE_BYTES;
@@ -206,7 +266,7 @@ k_gram_split(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ 
     bool ok = true;
     for (int32_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
       int32_t bi, bj;
-      tri_tile(t, &bi, &bj);
+      tri_tile(t, nt_rows, &bi, &bj);
       const int32_t gi = bi * BT + row;
       const int32_t gj0 = bj * BT + col0;
       float A[EPI_COLS];
@@ -481,12 +541,16 @@ int gp_gram_split(gp_ctx *ctx, int precision)
   int32_t kc = (int32_t)(kpad < kc_max ? kpad : kc_max);
   size_t xbytes = (size_t)npad * kc * 2;
   size_t tab_bytes = (size_t)nk * 16 + 256;
+  const int grid0 = ctx->num_sms < ntiles ? ctx->num_sms : ntiles;
+  const size_t nsync = (size_t)((kc / BK + GRAM_SYNC_KB - 1) / GRAM_SYNC_KB);
+  const size_t sync_bytes = sizeof(unsigned) * nsync * (size_t)((ntiles + grid0 - 1) / grid0);
   uint8_t *base;
-  int rc = gp_scratch2(ctx, 2 * xbytes + tab_bytes + 256, (void **)&base);
+  int rc = gp_scratch2(ctx, 2 * xbytes + tab_bytes + sync_bytes + 512, (void **)&base);
   if (rc) return rc;
   __nv_bfloat16 *xhi = (__nv_bfloat16 *)base;
   __nv_bfloat16 *xlo = (__nv_bfloat16 *)(base + xbytes);
   uint32_t *split = (uint32_t *)(base + 2 * xbytes);
+  unsigned *sync_ctr = (unsigned *)(base + ((2 * xbytes + tab_bytes + 255) / 256) * 256);
   int *d_err = ctx->d_err;
   GP_CUDA(ctx, cudaMemsetAsync(d_err, 0, sizeof(int), ctx->stream));
   {
@@ -499,7 +563,7 @@ int gp_gram_split(gp_ctx *ctx, int precision)
     GP_LAUNCH_CHECK(ctx, "k_split_tables");
   }
   void (*kern)(const CUtensorMap, const CUtensorMap, int32_t, int32_t, int32_t, double *, int32_t,
-               int32_t, int *) =
+               int32_t, unsigned *, int *) =
       fp16 ? k_gram_split<1, 3> : (nmma == 4 ? k_gram_split<0, 4> : k_gram_split<0, 3>);
   GP_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, GRAM_SMEM));
   CUtensorMap mhi, mlo;
@@ -507,7 +571,7 @@ int gp_gram_split(gp_ctx *ctx, int precision)
   rc = make_map(ctx, &mhi, xhi, npad, kc, dt);
   if (!rc) rc = make_map(ctx, &mlo, xlo, npad, kc, dt);
   if (rc) return rc;
-  int grid = ctx->num_sms < ntiles ? ctx->num_sms : ntiles;
+  int grid = grid0;
   for (int32_t k0 = 0; k0 < kpad; k0 += kc) {
     int32_t kcur = kpad - k0 < kc ? kpad - k0 : kc;
     /* columns beyond kcur in this super-chunk are zero (k >= nkept guard covers the tail) */
@@ -517,9 +581,14 @@ int gp_gram_split(gp_ctx *ctx, int precision)
                                                       npad, xhi, xlo);
     GP_LAUNCH_CHECK(ctx, "k_split_transpose");
     int32_t nkb = kcur / BK;
-    kern<<<grid, GRAM_THREADS, GRAM_SMEM, ctx->stream>>>(
-        mhi, mlo, ntiles, nkb, chunk_kb, ctx->d_xtx, n, k0 > 0 ? 1 : 0, d_err);
-    GP_LAUNCH_CHECK(ctx, "k_gram_split");
+    GP_CUDA(ctx, cudaMemsetAsync(sync_ctr, 0, sync_bytes, ctx->stream));
+    /* cooperative launch: the producers' lockstep points need every CTA resident */
+    int32_t a_nt = ntiles, a_nkb = nkb, a_ck = chunk_kb, a_n = n, a_acc = k0 > 0 ? 1 : 0;
+    double *a_xtx = ctx->d_xtx;
+    void *args[] = {&mhi, &mlo, &a_nt, &a_nkb, &a_ck, &a_xtx, &a_n, &a_acc, &sync_ctr, &d_err};
+    GP_CUDA(ctx, cudaLaunchCooperativeKernel((const void *)kern, dim3(grid), dim3(GRAM_THREADS),
+                                             args, GRAM_SMEM, ctx->stream));
+    ctx->launches++;
     ctx->gram_launches++;
   }
   int herr = 0;

@@ -660,6 +660,21 @@ def cpu_reference_sample(cfg, seconds_target=12.0, nthreads=None):
     return flops / dt / 1e12, nthreads, dt, m2, nind
 
 
+def gram_traffic(args):
+    """DRAM bytes per launch of the split Gram kernel from the committed ncu summary of the
+    full workload (profiles/gram_split_fp16_full_dram.md), or None for other workloads"""
+    if args.config != "full" or args.precision != "fp16":
+        return None
+    p = os.path.join(ROOT, "profiles", "gram_split_fp16_full_dram.md")
+    try:
+        for line in open(p):
+            if line.strip().startswith("traffic_bytes_per_launch:"):
+                return int(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -743,8 +758,10 @@ def main():
         achieved = res["gram_kernel_flops"] / (res["gram_ms"] * 1e-3) / 1e12
         peak = peaks.get("bf16_tflops", 1900.0)
         roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak, "traffic": None,
-                "peak_kind": "bf16 burst, %s" % res["peak_kind"]}
+                "frac": achieved / peak, "traffic": gram_traffic(args),
+                "peak_kind": "bf16 burst, %s" % res["peak_kind"],
+                "kernels": "k_split_transpose + k_gram_split (algorithmic N(N+1)M flop; the "
+                           "split scheme issues 3 MMAs per algorithmic FMA)"}
     else:
         achieved = res["gram_kernel_flops"] / (res["gram_ms"] * 1e-3) / 1e12
         roof = {"bound": "fp64", "achieved": achieved, "peak": 1.25, "unit": "TFLOP/s",

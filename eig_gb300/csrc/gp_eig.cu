@@ -199,15 +199,18 @@ k_multisect(const double *gd, const double *ge2, int n, double gl, double gu, do
  * trailing matrix for its product (look-ahead), so each step reads and writes the lower
  * triangle once and reads it once more.  Per step, with the blocks' row/column ranges
  * balanced by element count:
- *   A   column c gets the pending update; w of step c-1; v of step c-1 stored into A(:, c-1)
- *       (LAPACK's reflector storage, e(c-1) on the subdiagonal); partial ||x||^2
- *   --- grid barrier
+ *   A   every block rebuilds, from y and x of step c-1 and column c, the vectors v and w of
+ *       step c-1, the pending update of column c, its norm and the reflector (O(n) work done
+ *       redundantly instead of a grid-wide reduction); each block writes its share of the
+ *       reflector storage of step c-1 (LAPACK's, e(c-1) on the subdiagonal) and of x_c
  *   B1  each block, per owned column r of the trailing matrix: pending update of A(r:n, r),
  *       written back, and y(r) = A(r:n, r) . v (lower part incl. diagonal), warp per column
  *   --- grid barrier
  *   B2  each block, per owned row r: y(r) += A(r, c+1:r) . v (strictly lower part; lanes
- *       over rows, so the loads stay coalesced in column-major), partial y.v
+ *       over (row, column) pairs, loads coalesced in column-major), partial y.v
  *   --- grid barrier
+ * x and y are double-buffered across steps, so phase A of one step never reads a vector
+ * that a faster block is already writing in the next.
  * Every sum has a fixed order (no atomics), so the result is deterministic.  The grid
  * barriers are counter + generation words with a %globaltimer bound: on expiry the kernel
  * records an error code and returns (the host reports GP_ERR_TIMEOUT).
@@ -415,9 +418,10 @@ struct tr_step {
 };
 
 /*
- * A holds the lower triangle as float-float pairs on entry (k_tri_to_ff); vbuf/wbuf/ybuf
- * [n] float-float vectors (as doubles' storage).  On exit the reflectors are FP64 again in
- * A(c+2:n, c) and e on the subdiagonal, as cusolverDnDormtr(lower) reads them.
+ * A holds the lower triangle as float-float pairs on entry (k_tri_to_ff); vbuf/wbuf hold the
+ * updated column x of alternate steps and ybuf [2n] the product y of alternate steps, as
+ * float-float pairs in doubles' storage.  On exit the reflectors are FP64 again in A(c+2:n, c) and e on the
+ * subdiagonal, as cusolverDnDormtr(lower) reads them.
  */
 __global__ void __launch_bounds__(TR_THREADS, 1)
 k_tridiag(double *A, int n, double *d, double *e, double *tau, double *vbuf, double *wbuf,
@@ -438,59 +442,58 @@ k_tridiag(double *A, int n, double *d, double *e, double *tau, double *vbuf, dou
   ff2 tau_pf = ZERO, scale_pf = ZERO;
   bool have_p = false;
   for (int c = 0; c < n - 1; ++c) {
-    /* ---- A: w and storage of step c-1, column c update, partial ||x||^2 ---- */
+    /* ---- A (every block, no grid barrier): v and w of step c-1, the pending update of
+     * column c and its norm, rebuilt from y, the stored x of step c-1 and column c; each
+     * block also writes its share of the reflector storage and of x_c (double buffer) ---- */
+    const int m = n - c - 1;
+    double *xcur = (c & 1) ? wbuf : vbuf, *xprev = (c & 1) ? vbuf : wbuf;
+    /* y of step c and of step c-1 (double buffer: phase A reads one while B1 writes the other) */
+    double *ycur = ybuf + (int64_t)(c & 1) * n, *yprev = ybuf + (int64_t)((c + 1) & 1) * n;
+    if (threadIdx.x == 32) st.b1_u0 = tr_split_cols(m, b, G);
+    if (threadIdx.x == 33) st.b1_u1 = tr_split_cols(m, b + 1, G);
+    if (threadIdx.x == 34) st.b2_u0 = tr_split_rows(m, b, G);
+    if (threadIdx.x == 35) st.b2_u1 = tr_split_rows(m, b + 1, G);
     if (have_p) {
-      const ff2 yc = ff_load(ybuf + c); /* issued before the reduction */
       const double dsum = tr_sum_partials(part_dot, G, &s_slot);
-      if (threadIdx.x == 0) {
-        const double alpha_p = -0.5 * tau_p * tau_p * dsum;
-        st.alpha_pf = ff_from_double(alpha_p);
-        st.wpc = ff_fma(tau_pf, yc, st.alpha_pf); /* v_p(c) = 1 */
+      if (threadIdx.x == 0) st.alpha_pf = ff_from_double(-0.5 * tau_p * tau_p * dsum);
+    }
+    __syncthreads();
+    {
+      const ff2 alpha_pf = st.alpha_pf;
+#pragma unroll 4
+      for (int q = c + threadIdx.x; q < n; q += blockDim.x) {
+        ff2 vp = ZERO, wp = ZERO;
+        if (have_p) {
+          vp = (q == c) ? ONE : ff_mul(ff_load(xprev + q), scale_pf);
+          wp = ff_fma(tau_pf, ff_load(yprev + q), ff_mul(alpha_pf, vp));
+        }
+        ff_store(svp + q, vp);
+        ff_store(swp + q, wp);
+        ff_store(svc + q, ff_load(A + (int64_t)c * n + q));
       }
     }
     __syncthreads();
     {
-      const ff2 alpha_pf = st.alpha_pf, wpc = st.wpc;
+      const ff2 wpc = ff_load(swp + c); /* w_p(c); v_p(c) = 1 */
       const int cnt = n - c, per = (cnt + G - 1) / G;
       const int r0 = c + b * per, r1 = min(n, r0 + per);
       ff2 nrm = ZERO;
-      for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
-        ff2 x = ff_load(A + (int64_t)c * n + r);
+      for (int q = c + threadIdx.x; q < n; q += blockDim.x) {
+        ff2 x = ff_load(svc + q);
+        const bool mine = q >= r0 && q < r1;
         if (have_p) {
-          const ff2 vpr = (r == c) ? ONE : ff_mul(ff_load(A + (int64_t)(c - 1) * n + r), scale_pf);
-          const ff2 wpr = ff_fma(tau_pf, ff_load(ybuf + r), ff_mul(alpha_pf, vpr));
-          ff_store(wbuf + r, wpr);
-          ff_store(vbuf + r, vpr);
-          A[(int64_t)(c - 1) * n + r] = (r == c) ? e_p : ff_to_double(vpr); /* FP64 again */
-          x = ff_fma(ff_neg(vpr), wpc, x);
-          x = ff_add(x, ff_neg(wpr));
+          const ff2 vp = ff_load(svp + q);
+          x = ff_fma(ff_neg(vp), wpc, x);
+          x = ff_add(x, ff_neg(ff_load(swp + q)));
+          if (mine) A[(int64_t)(c - 1) * n + q] = (q == c) ? e_p : ff_to_double(vp); /* FP64 */
         }
-        ff_store(A + (int64_t)c * n + r, x);
-        if (r >= c + 2) nrm = ff_fma(x, x, nrm);
+        ff_store(svc + q, x);
+        if (mine) ff_store(xcur + q, x);
+        if (q >= c + 2) nrm = ff_fma(x, x, nrm);
       }
-      const double ns = ff_block_sum(nrm, red);
-      if (threadIdx.x == 0) part_norm[b] = ns;
-    }
-    target += G;
-    if (!tr_grid_sync(count, target, err)) return;
-    /* ---- reflector of column c and this step's partitions ---- */
-    const int m = n - c - 1;
-    {
-      /* v, w of step c-1 and the raw column x into shared memory while the norm is summed */
-#pragma unroll 4
-      for (int q = c + 1 + threadIdx.x; q < n; q += blockDim.x) {
-        ff_store(svp + q, have_p ? ff_load(vbuf + q) : ZERO);
-        ff_store(swp + q, have_p ? ff_load(wbuf + q) : ZERO);
-        ff_store(svc + q, ff_load(A + (int64_t)c * n + q));
-      }
-      if (threadIdx.x == 32) st.b1_u0 = tr_split_cols(m, b, G);
-      if (threadIdx.x == 33) st.b1_u1 = tr_split_cols(m, b + 1, G);
-      if (threadIdx.x == 34) st.b2_u0 = tr_split_rows(m, b, G);
-      if (threadIdx.x == 35) st.b2_u1 = tr_split_rows(m, b + 1, G);
-      const ff2 xa = ff_load(A + (int64_t)c * n + c + 1), xd = ff_load(A + (int64_t)c * n + c);
-      const double xn2 = tr_sum_partials(part_norm, G, &s_slot);
+      const double xn2 = ff_block_sum(nrm, red); /* thread 0; the sum's barriers publish svc */
       if (threadIdx.x == 0) {
-        const double alpha = ff_to_double(xa);
+        const double alpha = ff_to_double(ff_load(svc + c + 1));
         if (xn2 == 0.0) {
           st.beta = alpha;
           st.tau_c = 0.0;
@@ -499,14 +502,14 @@ k_tridiag(double *A, int n, double *d, double *e, double *tau, double *vbuf, dou
           const double xn = sqrt(xn2);
           const double ax = fabs(alpha), big = fmax(ax, xn), sml = fmin(ax, xn);
           const double rr = sml / big;
-          const double nrm = big * sqrt(1.0 + rr * rr);
-          st.beta = alpha >= 0.0 ? -nrm : nrm;
+          const double nrm2 = big * sqrt(1.0 + rr * rr);
+          st.beta = alpha >= 0.0 ? -nrm2 : nrm2;
           st.tau_c = (st.beta - alpha) / st.beta;
           st.scale_c = 1.0 / (alpha - st.beta);
         }
         st.scale_cf = ff_from_double(st.scale_c);
         if (b == 0) {
-          d[c] = ff_to_double(xd);
+          d[c] = ff_to_double(ff_load(svc + c));
           e[c] = st.beta;
           tau[c] = st.tau_c;
         }
@@ -553,7 +556,7 @@ k_tridiag(double *A, int n, double *d, double *e, double *tau, double *vbuf, dou
           dot = ff_fma(a, ff_load(svc + q), dot);
         }
         for (int o = 16; o; o >>= 1) dot = ff_add(dot, ff_shfl_xor(dot, o));
-        if (lane == 0) ff_store(ybuf + r, dot);
+        if (lane == 0) ff_store(ycur + r, dot);
       }
     }
     target += G;
@@ -594,8 +597,8 @@ k_tridiag(double *A, int n, double *d, double *e, double *tau, double *vbuf, dou
         if (warp == 0 && lane < rpp && valid) {
           ff2 y1 = bred[0][lane];
           for (int w = 1; w < TR_WARPS; ++w) y1 = ff_add(y1, bred[w][lane]);
-          const ff2 y = ff_add(ff_load(ybuf + r), y1);
-          ff_store(ybuf + r, y);
+          const ff2 y = ff_add(ff_load(ycur + r), y1);
+          ff_store(ycur + r, y);
           dpart = ff_fma(y, ff_load(svc + r), dpart);
         }
         __syncthreads();
@@ -619,7 +622,8 @@ k_tridiag(double *A, int n, double *d, double *e, double *tau, double *vbuf, dou
       double a = ff_to_double(ff_load(A + (int64_t)(n - 1) * n + n - 1));
       if (have_p) {
         const double alpha_p = -0.5 * tau_p * tau_p * dsum;
-        const double wp = tau_p * ff_to_double(ff_load(ybuf + n - 1)) + alpha_p;
+        const double wp =
+            tau_p * ff_to_double(ff_load(ybuf + (int64_t)((n - 2) & 1) * n + n - 1)) + alpha_p;
         a = a - wp - wp;
         A[(int64_t)(n - 2) * n + n - 1] = e_p;
       }
@@ -801,13 +805,13 @@ int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, d
   int lw = lwork > lwork2 ? lwork : lwork2;
   size_t nd = (size_t)n;
   const size_t G = (size_t)ctx->num_sms;
-  size_t bytes = sizeof(double) * (8 * nd + 2 * G + (size_t)lw + 6 * nd * nv + 72) +
+  size_t bytes = sizeof(double) * (9 * nd + 2 * G + (size_t)lw + 6 * nd * nv + 72) +
                  sizeof(int) * 64;
   double *base;
   int rc = gp_scratch(ctx, bytes, (void **)&base);
   if (rc) return rc;
   double *d = base, *e = d + nd, *tau = e + nd, *e2 = tau + nd, *w = e2 + nd;
-  double *wbuf = w + nd, *ybuf = wbuf + nd, *vbuf = ybuf + nd, *parts = vbuf + nd;
+  double *wbuf = w + nd, *ybuf = wbuf + nd, *vbuf = ybuf + 2 * nd, *parts = vbuf + nd;
   unsigned *bar = (unsigned *)(parts + 2 * G);
   double *ws = parts + 2 * G + 8, *iw = ws + lw;
   int *d_info = (int *)(iw + 6 * nd * nv + 8);

@@ -284,27 +284,34 @@ __device__ __forceinline__ double tr_block_sum(double v, double *red)
   return s;
 }
 
-/* start of block b's share of [0, m) when column u weighs (m - u) (B1) */
+/* start of block b's share of [0, m) when column u weighs (m - u) + TR_COL_COST, its elements
+ * plus a fixed cost per column (warp reduction, loop setup) (B1) */
+#define TR_COL_COST 256
+#define TR_ROW_COST 64
 __device__ __forceinline__ int tr_split_cols(int m, int b, int G)
 {
   if (b <= 0) return 0;
   if (b >= G) return m;
-  const double tot = 0.5 * (double)m * (double)(m + 1);
+  const double mc = (double)m + TR_COL_COST;
+  const double tot = (double)m * mc - 0.5 * (double)m * (double)(m - 1);
   const double t = tot * (double)b / (double)G;
-  const double a = 2.0 * (double)m + 1.0;
+  const double a = 2.0 * mc + 1.0;
   double u = 0.5 * (a - sqrt(fmax(a * a - 8.0 * t, 0.0)));
   int iu = (int)ceil(u - 1e-9);
   return iu < 0 ? 0 : (iu > m ? m : iu);
 }
 
-/* start of block b's share of [0, m) when row u weighs u (B2) */
+/* start of block b's share of [0, m) when row u weighs u + TR_ROW_COST (B2) */
 __device__ __forceinline__ int tr_split_rows(int m, int b, int G)
 {
   if (b <= 0) return 0;
   if (b >= G) return m;
-  const double tot = 0.5 * (double)m * (double)(m - 1);
+  const double c0 = TR_ROW_COST;
+  const double tot = 0.5 * (double)m * (double)(m - 1) + c0 * (double)m;
   const double t = tot * (double)b / (double)G;
-  double u = 0.5 * (1.0 + sqrt(1.0 + 8.0 * t));
+  /* u (u - 1) / 2 + c0 u = t */
+  const double bq = c0 - 0.5;
+  double u = -bq + sqrt(bq * bq + 2.0 * t);
   int iu = (int)ceil(u - 1e-9);
   return iu < 0 ? 0 : (iu > m ? m : iu);
 }
@@ -382,6 +389,52 @@ __device__ __forceinline__ void ff_store(double *p, ff2 a)
   *reinterpret_cast<float2 *>(p) = make_float2(a.h, a.l);
 }
 
+/* sqrt(a) for a > 0: FP32 root plus one correction, (a - s^2) / 2s */
+__device__ __forceinline__ ff2 ff_sqrt(ff2 a)
+{
+  const float s = sqrtf(a.h);
+  const ff2 r = ff_fma(ff_make(-s, 0.f), ff_make(s, 0.f), a);
+  return ff_add(ff_make(s, 0.f), ff_make(__fdiv_rn(r.h, 2.f * s), 0.f));
+}
+/* a / b: FP32 quotient plus one correction from the float-float remainder */
+__device__ __forceinline__ ff2 ff_div(ff2 a, ff2 b)
+{
+  const float q1 = __fdiv_rn(a.h, b.h);
+  const ff2 r = ff_fma(ff_neg(b), ff_make(q1, 0.f), a);
+  return ff_add(ff_make(q1, 0.f), ff_make(__fdiv_rn(r.h, b.h), 0.f));
+}
+__device__ __forceinline__ ff2 ff_scale(ff2 a, float s) { return ff_make(a.h * s, a.l * s); }
+
+/* sum of the G float-float block partials in a fixed order (warp 0), broadcast */
+__device__ __forceinline__ ff2 ff_sum_partials(const double *part, int G, ff2 *slot)
+{
+  if (threadIdx.x < 32) {
+    ff2 s = ff_make(0.f, 0.f);
+    for (int g = threadIdx.x; g < G; g += 32) s = ff_add(s, ff_load(part + g));
+    for (int o = 16; o; o >>= 1) s = ff_add(s, ff_shfl_xor(s, o));
+    if (threadIdx.x == 0) *slot = s;
+  }
+  __syncthreads();
+  const ff2 r = *slot;
+  __syncthreads();
+  return r;
+}
+
+/* block sum of one float-float per thread (fixed order), as float-float in thread 0 */
+__device__ __forceinline__ ff2 ff_block_sum2(ff2 v, ff2 *red)
+{
+  for (int o = 16; o; o >>= 1) v = ff_add(v, ff_shfl_xor(v, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  ff2 t = ff_make(0.f, 0.f);
+  if (threadIdx.x == 0) {
+    t = red[0];
+    for (int w = 1; w < TR_WARPS; ++w) t = ff_add(t, red[w]);
+  }
+  __syncthreads();
+  return t;
+}
+
 /* block sum of one float-float per thread (fixed order), as a double in thread 0 */
 __device__ __forceinline__ double ff_block_sum(ff2 v, ff2 *red)
 {
@@ -412,8 +465,7 @@ __global__ void k_tri_to_ff(double *A, int n)
 /* per-step scalars, computed once per block by thread 0 (GB300's FP64 pipe is narrow, so
  * scalar square roots and divisions are not repeated by every thread) */
 struct tr_step {
-  double beta, tau_c, scale_c;
-  ff2 alpha_pf, wpc, scale_cf;
+  ff2 alpha_pf, beta, tau_c, scale_c;
   int b1_u0, b1_u1, b2_u0, b2_u1;
 };
 
@@ -425,22 +477,31 @@ struct tr_step {
  */
 __global__ void __launch_bounds__(TR_THREADS, 1)
 k_tridiag(double *A, int n, double *d, double *e, double *tau, double *vbuf, double *wbuf,
-          double *ybuf, double *part_norm, double *part_dot, unsigned *bar, int *err)
+          double *ybuf, double *part_norm, double *part_dot, unsigned *bar, int *err,
+          unsigned long long *phase_ns)
 {
   extern __shared__ double sh[];
   double *svp = sh, *swp = sh + n, *svc = sh + 2 * n; /* float-float pairs */
   __shared__ ff2 red[TR_WARPS];
   __shared__ ff2 bred[TR_WARPS][32];
-  __shared__ double s_slot;
   __shared__ tr_step st;
   const int G = gridDim.x, b = blockIdx.x;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const ff2 ONE = ff_make(1.f, 0.f), ZERO = ff_make(0.f, 0.f);
   unsigned *count = bar;
   unsigned target = 0;
-  double tau_p = 0.0, e_p = 0.0;
-  ff2 tau_pf = ZERO, scale_pf = ZERO;
+  ff2 tau_pf = ZERO, scale_pf = ZERO, e_pf = ZERO;
+  __shared__ ff2 s_slotf;
   bool have_p = false;
+  /* phase_ns (optional, block 0): time in A, B1, barrier 1, B2, barrier 2 */
+  const bool stamp = phase_ns != NULL && b == 0 && threadIdx.x == 0;
+  unsigned long long t_prev = stamp ? globaltimer_ns() : 0ull, ph[5] = {0, 0, 0, 0, 0};
+#define TR_STAMP(i)                                  \
+  if (stamp) {                                       \
+    const unsigned long long t_now = globaltimer_ns(); \
+    ph[i] += t_now - t_prev;                         \
+    t_prev = t_now;                                  \
+  }
   for (int c = 0; c < n - 1; ++c) {
     /* ---- A (every block, no grid barrier): v and w of step c-1, the pending update of
      * column c and its norm, rebuilt from y, the stored x of step c-1 and column c; each
@@ -454,8 +515,8 @@ k_tridiag(double *A, int n, double *d, double *e, double *tau, double *vbuf, dou
     if (threadIdx.x == 34) st.b2_u0 = tr_split_rows(m, b, G);
     if (threadIdx.x == 35) st.b2_u1 = tr_split_rows(m, b + 1, G);
     if (have_p) {
-      const double dsum = tr_sum_partials(part_dot, G, &s_slot);
-      if (threadIdx.x == 0) st.alpha_pf = ff_from_double(-0.5 * tau_p * tau_p * dsum);
+      const ff2 dsum = ff_sum_partials(part_dot, G, &s_slotf);
+      if (threadIdx.x == 0) st.alpha_pf = ff_scale(ff_mul(ff_mul(tau_pf, tau_pf), dsum), -0.5f);
     }
     __syncthreads();
     {
@@ -485,39 +546,40 @@ k_tridiag(double *A, int n, double *d, double *e, double *tau, double *vbuf, dou
           const ff2 vp = ff_load(svp + q);
           x = ff_fma(ff_neg(vp), wpc, x);
           x = ff_add(x, ff_neg(ff_load(swp + q)));
-          if (mine) A[(int64_t)(c - 1) * n + q] = (q == c) ? e_p : ff_to_double(vp); /* FP64 */
+          if (mine) A[(int64_t)(c - 1) * n + q] = ff_to_double(q == c ? e_pf : vp); /* FP64 */
         }
         ff_store(svc + q, x);
         if (mine) ff_store(xcur + q, x);
         if (q >= c + 2) nrm = ff_fma(x, x, nrm);
       }
-      const double xn2 = ff_block_sum(nrm, red); /* thread 0; the sum's barriers publish svc */
+      const ff2 xn2 = ff_block_sum2(nrm, red); /* thread 0; the sum's barriers publish svc */
       if (threadIdx.x == 0) {
-        const double alpha = ff_to_double(ff_load(svc + c + 1));
-        if (xn2 == 0.0) {
+        /* the reflector (dlarfg) in float-float: beta = -sign(alpha) sqrt(alpha^2 + |x|^2),
+         * tau = (beta - alpha) / beta, scale = 1 / (alpha - beta) */
+        const ff2 alpha = ff_load(svc + c + 1);
+        if (xn2.h == 0.f) {
           st.beta = alpha;
-          st.tau_c = 0.0;
-          st.scale_c = 0.0;
+          st.tau_c = ZERO;
+          st.scale_c = ZERO;
         } else {
-          const double xn = sqrt(xn2);
-          const double ax = fabs(alpha), big = fmax(ax, xn), sml = fmin(ax, xn);
-          const double rr = sml / big;
-          const double nrm2 = big * sqrt(1.0 + rr * rr);
-          st.beta = alpha >= 0.0 ? -nrm2 : nrm2;
-          st.tau_c = (st.beta - alpha) / st.beta;
-          st.scale_c = 1.0 / (alpha - st.beta);
-        }
-        st.scale_cf = ff_from_double(st.scale_c);
-        if (b == 0) {
-          d[c] = ff_to_double(ff_load(svc + c));
-          e[c] = st.beta;
-          tau[c] = st.tau_c;
+          const ff2 nrm2 = ff_sqrt(ff_fma(alpha, alpha, xn2));
+          const ff2 beta = alpha.h >= 0.f ? ff_neg(nrm2) : nrm2;
+          const ff2 am = ff_add(alpha, ff_neg(beta));
+          st.beta = beta;
+          st.tau_c = ff_div(ff_neg(am), beta);
+          st.scale_c = ff_div(ONE, am);
         }
       }
       __syncthreads();
+      if (b == 0 && threadIdx.x == 32) {
+        d[c] = ff_to_double(ff_load(svc + c));
+        e[c] = ff_to_double(st.beta);
+        tau[c] = ff_to_double(st.tau_c);
+      }
     }
-    const double beta = st.beta, tau_c = st.tau_c;
-    const ff2 scale_cf = st.scale_cf;
+    const ff2 beta = st.beta, tau_c = st.tau_c;
+    const ff2 scale_cf = st.scale_c;
+    TR_STAMP(0)
     /* ---- B1: pending update + lower product, warp per column ---- */
     for (int q = c + 1 + threadIdx.x; q < n; q += blockDim.x)
       ff_store(svc + q, (q == c + 1) ? ONE : ff_mul(ff_load(svc + q), scale_cf));
@@ -559,75 +621,95 @@ k_tridiag(double *A, int n, double *d, double *e, double *tau, double *vbuf, dou
         if (lane == 0) ff_store(ycur + r, dot);
       }
     }
+    TR_STAMP(1)
     target += G;
     if (!tr_grid_sync(count, target, err)) return;
-    /* ---- B2: strictly lower part of the product.  A warp instruction covers RPP rows x
-     * (32/RPP) columns (RPP = 8, 16 or 32 from the block's row count) so that short row
-     * ranges keep every lane busy; loads stay coalesced along the rows of a column. ---- */
+    TR_STAMP(2)
+    /* ---- B2: strictly lower part of the product.  The block's rows come in 32-row chunks;
+     * F = min(chunks, 16) (a power of two) chunks are in flight at once, each with 16/F warps
+     * splitting its columns, lanes over rows (loads coalesced in column-major).  A single
+     * chunk of few rows uses RPP = 8 or 16 rows x 32/RPP columns per warp instruction so that
+     * every lane stays busy. ---- */
     {
       const int u0 = st.b2_u0, u1 = st.b2_u1;
+      const int nch = (u1 - u0 + 31) / 32;
+      int F = 1;
+      while (F * 2 <= nch && F * 2 <= TR_WARPS) F *= 2;
+      const int wpc = TR_WARPS / F, grp = warp / wpc, wg = warp - grp * wpc;
       ff2 dpart = ZERO;
-      for (int ch = u0, rpp = 32; ch < u1; ch += rpp) {
+      /* F > 1: round rb runs chunks rb .. rb+F-1 (32 rows each); F == 1: one group walks the
+       * rows in chunks of rpp (the last chunk may be 16 or 8 rows) */
+      for (int rb = 0, ch0 = u0; F > 1 ? rb < nch : ch0 < u1;) {
+        const int ch = F > 1 ? u0 + 32 * (rb + grp) : ch0;
         const int rem = u1 - ch;
-        rpp = rem >= 32 ? 32 : (rem > 8 ? 16 : 8);
+        const int rpp = F > 1 ? 32 : (rem >= 32 ? 32 : (rem > 8 ? 16 : 8));
         const int cpi = 32 / rpp;
         const int lr = lane & (rpp - 1), lc = lane / rpp;
         const int u = ch + lr;
         const int r = c + 1 + u;
-        const bool valid = u < u1;
+        const bool valid = (F == 1 || rb + grp < nch) && u < u1;
         const int qend = c + 1 + min(ch + rpp, u1); /* columns below the chunk's last row */
-        const int qstep = TR_WARPS * cpi;
+        const int qstep = wpc * cpi;
         ff2 acc = ZERO;
-        for (int q0 = c + 1 + warp * cpi + lc; q0 < qend; q0 += qstep * TR_U) {
-          ff2 a[TR_U];
+        if (F == 1 || rb + grp < nch) {
+          for (int q0 = c + 1 + wg * cpi + lc; q0 < qend; q0 += qstep * TR_U) {
+            ff2 a[TR_U];
 #pragma unroll
-          for (int k = 0; k < TR_U; ++k) {
-            const int q = q0 + qstep * k;
-            a[k] = (valid && q < qend && q < r) ? ff_load(A + (int64_t)q * n + r) : ZERO;
-          }
+            for (int k = 0; k < TR_U; ++k) {
+              const int q = q0 + qstep * k;
+              a[k] = (valid && q < qend && q < r) ? ff_load(A + (int64_t)q * n + r) : ZERO;
+            }
 #pragma unroll
-          for (int k = 0; k < TR_U; ++k) {
-            const int q = q0 + qstep * k;
-            if (q < qend) acc = ff_fma(a[k], ff_load(svc + q), acc);
+            for (int k = 0; k < TR_U; ++k) {
+              const int q = q0 + qstep * k;
+              if (q < qend) acc = ff_fma(a[k], ff_load(svc + q), acc);
+            }
           }
         }
         for (int o = rpp; o < 32; o <<= 1) acc = ff_add(acc, ff_shfl_xor(acc, o));
         if (lc == 0) bred[warp][lr] = acc;
         __syncthreads();
-        if (warp == 0 && lane < rpp && valid) {
-          ff2 y1 = bred[0][lane];
-          for (int w = 1; w < TR_WARPS; ++w) y1 = ff_add(y1, bred[w][lane]);
+        if (wg == 0 && lane < rpp && valid) {
+          ff2 y1 = bred[warp][lane];
+          for (int w = 1; w < wpc; ++w) y1 = ff_add(y1, bred[warp + w][lane]);
           const ff2 y = ff_add(ff_load(ycur + r), y1);
           ff_store(ycur + r, y);
           dpart = ff_fma(y, ff_load(svc + r), dpart);
         }
         __syncthreads();
+        rb += F;
+        ch0 += rpp;
       }
-      const double ds = ff_block_sum(dpart, red);
-      if (threadIdx.x == 0) part_dot[b] = ds;
+      const ff2 ds = ff_block_sum2(dpart, red);
+      if (threadIdx.x == 0) ff_store(part_dot + b, ds);
     }
+    TR_STAMP(3)
     target += G;
     if (!tr_grid_sync(count, target, err)) return;
-    tau_p = tau_c;
-    tau_pf = ff_from_double(tau_c);
+    TR_STAMP(4)
+    tau_pf = tau_c;
     scale_pf = scale_cf;
-    e_p = beta;
+    e_pf = beta;
     have_p = true;
   }
+  if (stamp)
+    for (int i = 0; i < 5; ++i) phase_ns[i] = ph[i];
+#undef TR_STAMP
   /* last diagonal entry and the storage of the last reflector */
   if (b == 0) {
-    double dsum = 0.0;
-    if (have_p) dsum = tr_sum_partials(part_dot, G, &s_slot);
+    ff2 dsum = ZERO;
+    if (have_p) dsum = ff_sum_partials(part_dot, G, &s_slotf);
     if (threadIdx.x == 0) {
-      double a = ff_to_double(ff_load(A + (int64_t)(n - 1) * n + n - 1));
+      ff2 a = ff_load(A + (int64_t)(n - 1) * n + n - 1);
       if (have_p) {
-        const double alpha_p = -0.5 * tau_p * tau_p * dsum;
-        const double wp =
-            tau_p * ff_to_double(ff_load(ybuf + (int64_t)((n - 2) & 1) * n + n - 1)) + alpha_p;
-        a = a - wp - wp;
-        A[(int64_t)(n - 2) * n + n - 1] = e_p;
+        const ff2 alpha_p = ff_scale(ff_mul(ff_mul(tau_pf, tau_pf), dsum), -0.5f);
+        const ff2 wp =
+            ff_fma(tau_pf, ff_load(ybuf + (int64_t)((n - 2) & 1) * n + n - 1), alpha_p);
+        a = ff_add(a, ff_neg(wp));
+        a = ff_add(a, ff_neg(wp));
+        A[(int64_t)(n - 2) * n + n - 1] = ff_to_double(e_pf);
       }
-      d[n - 1] = a;
+      d[n - 1] = ff_to_double(a);
     }
   }
 }
@@ -805,7 +887,7 @@ int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, d
   int lw = lwork > lwork2 ? lwork : lwork2;
   size_t nd = (size_t)n;
   const size_t G = (size_t)ctx->num_sms;
-  size_t bytes = sizeof(double) * (9 * nd + 2 * G + (size_t)lw + 6 * nd * nv + 72) +
+  size_t bytes = sizeof(double) * (9 * nd + 2 * G + (size_t)lw + 6 * nd * nv + 80) +
                  sizeof(int) * 64;
   double *base;
   int rc = gp_scratch(ctx, bytes, (void **)&base);
@@ -813,7 +895,7 @@ int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, d
   double *d = base, *e = d + nd, *tau = e + nd, *e2 = tau + nd, *w = e2 + nd;
   double *wbuf = w + nd, *ybuf = wbuf + nd, *vbuf = ybuf + 2 * nd, *parts = vbuf + nd;
   unsigned *bar = (unsigned *)(parts + 2 * G);
-  double *ws = parts + 2 * G + 8, *iw = ws + lw;
+  double *ws = parts + 2 * G + 16, *iw = ws + lw; /* 16 doubles: barrier words + phase timers */
   int *d_info = (int *)(iw + 6 * nd * nv + 8);
   /* the cooperative tridiagonalisation (k_tridiag) unless GP_EIG_CUSOLVER_SYTRD=1, the
    * vectors do not fit shared memory or the device cannot co-schedule one block per SM */
@@ -843,7 +925,12 @@ int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, d
       k_tri_to_ff<<<blocks, 256, 0, ctx->stream>>>(A, n);
       GP_LAUNCH_CHECK(ctx, "k_tri_to_ff");
     }
-    void *args[] = {&A, &nn, &d, &e, &tau, &vbuf, &wbuf, &ybuf, &pn, &pd, &bar, &d_err};
+    unsigned long long *phase = NULL;
+    if (timing) {
+      phase = (unsigned long long *)(bar + 8);
+      GP_CUDA(ctx, cudaMemsetAsync(phase, 0, 5 * sizeof(unsigned long long), ctx->stream));
+    }
+    void *args[] = {&A, &nn, &d, &e, &tau, &vbuf, &wbuf, &ybuf, &pn, &pd, &bar, &d_err, &phase};
     GP_CUDA(ctx, cudaLaunchCooperativeKernel((const void *)k_tridiag, dim3((unsigned)G),
                                              dim3(TR_THREADS), args, tr_smem, ctx->stream));
     ctx->launches++;
@@ -851,6 +938,12 @@ int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, d
     GP_CUDA(ctx, gp_memcpy(ctx, &herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (herr) return gp_fail(ctx, GP_ERR_TIMEOUT, "tridiagonalisation grid barrier timed out");
+    if (timing) {
+      unsigned long long hp[5];
+      cudaMemcpy(hp, phase, sizeof hp, cudaMemcpyDeviceToHost);
+      fprintf(stderr, "k_tridiag n=%d (block 0): A %.1f ms, B1 %.1f, barrier1 %.1f, B2 %.1f, barrier2 %.1f\n",
+              n, hp[0] * 1e-6, hp[1] * 1e-6, hp[2] * 1e-6, hp[3] * 1e-6, hp[4] * 1e-6);
+    }
   } else {
     if (cusolverDnDsytrd(h, CUBLAS_FILL_MODE_LOWER, n, ctx->d_xtx, n, d, e, tau, ws, lw,
                          d_info) != CUSOLVER_STATUS_SUCCESS)

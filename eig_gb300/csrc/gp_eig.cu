@@ -220,6 +220,7 @@ k_multisect(const double *gd, const double *ge2, int n, double gl, double gu, do
 #define TR_THREADS 512
 #define TR_WARPS (TR_THREADS / 32)
 #define TR_U 8 /* loads in flight per lane in the product loops */
+#define TR_B1_SLOTS 256 /* segment dots of one block in the column pass */
 #define TR_ERR_BARRIER 11
 
 /* grid barrier on a monotonic arrival counter: the k-th barrier of the launch waits until
@@ -465,7 +466,7 @@ __global__ void k_tri_to_ff(double *A, int n)
 /* per-step scalars, computed once per block by thread 0 (GB300's FP64 pipe is narrow, so
  * scalar square roots and divisions are not repeated by every thread) */
 struct tr_step {
-  ff2 alpha_pf, beta, tau_c, scale_c;
+  ff2 alpha_pf, wpc, beta, tau_c, scale_c;
   int b1_u0, b1_u1, b2_u0, b2_u1;
 };
 
@@ -484,6 +485,7 @@ k_tridiag(double *A, int n, double *d, double *e, double *tau, double *vbuf, dou
   double *svp = sh, *swp = sh + n, *svc = sh + 2 * n; /* float-float pairs */
   __shared__ ff2 red[TR_WARPS];
   __shared__ ff2 bred[TR_WARPS][32];
+  __shared__ ff2 sdotp[TR_B1_SLOTS];
   __shared__ tr_step st;
   const int G = gridDim.x, b = blockIdx.x;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -514,28 +516,31 @@ k_tridiag(double *A, int n, double *d, double *e, double *tau, double *vbuf, dou
     if (threadIdx.x == 33) st.b1_u1 = tr_split_cols(m, b + 1, G);
     if (threadIdx.x == 34) st.b2_u0 = tr_split_rows(m, b, G);
     if (threadIdx.x == 35) st.b2_u1 = tr_split_rows(m, b + 1, G);
-    if (have_p) {
-      const ff2 dsum = ff_sum_partials(part_dot, G, &s_slotf);
-      if (threadIdx.x == 0) st.alpha_pf = ff_scale(ff_mul(ff_mul(tau_pf, tau_pf), dsum), -0.5f);
-    }
-    __syncthreads();
-    {
-      const ff2 alpha_pf = st.alpha_pf;
+    /* loads first (v_p needs only step c-1's scale; y is kept raw in swp for now), so that
+     * they overlap the reduction of the previous step's partial dots */
 #pragma unroll 4
-      for (int q = c + threadIdx.x; q < n; q += blockDim.x) {
-        ff2 vp = ZERO, wp = ZERO;
-        if (have_p) {
-          vp = (q == c) ? ONE : ff_mul(ff_load(xprev + q), scale_pf);
-          wp = ff_fma(tau_pf, ff_load(yprev + q), ff_mul(alpha_pf, vp));
-        }
-        ff_store(svp + q, vp);
-        ff_store(swp + q, wp);
-        ff_store(svc + q, ff_load(A + (int64_t)c * n + q));
+    for (int q = c + threadIdx.x; q < n; q += blockDim.x) {
+      ff2 vp = ZERO, yq = ZERO;
+      if (have_p) {
+        vp = (q == c) ? ONE : ff_mul(ff_load(xprev + q), scale_pf);
+        yq = ff_load(yprev + q);
       }
+      ff_store(svp + q, vp);
+      ff_store(swp + q, yq);
+      ff_store(svc + q, ff_load(A + (int64_t)c * n + q));
+    }
+    if (have_p) {
+      const ff2 dsum = ff_sum_partials(part_dot, G, &s_slotf); /* its barriers publish svp/swp */
+      if (threadIdx.x == 0) {
+        st.alpha_pf = ff_scale(ff_mul(ff_mul(tau_pf, tau_pf), dsum), -0.5f);
+        st.wpc = ff_fma(tau_pf, ff_load(swp + c), st.alpha_pf); /* w_p(c); v_p(c) = 1 */
+      }
+    } else if (threadIdx.x == 0) {
+      st.wpc = ZERO;
     }
     __syncthreads();
     {
-      const ff2 wpc = ff_load(swp + c); /* w_p(c); v_p(c) = 1 */
+      const ff2 wpc = st.wpc, alpha_pf = st.alpha_pf;
       const int cnt = n - c, per = (cnt + G - 1) / G;
       const int r0 = c + b * per, r1 = min(n, r0 + per);
       ff2 nrm = ZERO;
@@ -544,8 +549,10 @@ k_tridiag(double *A, int n, double *d, double *e, double *tau, double *vbuf, dou
         const bool mine = q >= r0 && q < r1;
         if (have_p) {
           const ff2 vp = ff_load(svp + q);
+          const ff2 wp = ff_fma(tau_pf, ff_load(swp + q), ff_mul(alpha_pf, vp));
+          ff_store(swp + q, wp);
           x = ff_fma(ff_neg(vp), wpc, x);
-          x = ff_add(x, ff_neg(ff_load(swp + q)));
+          x = ff_add(x, ff_neg(wp));
           if (mine) A[(int64_t)(c - 1) * n + q] = ff_to_double(q == c ? e_pf : vp); /* FP64 */
         }
         ff_store(svc + q, x);
@@ -585,15 +592,22 @@ k_tridiag(double *A, int n, double *d, double *e, double *tau, double *vbuf, dou
       ff_store(svc + q, (q == c + 1) ? ONE : ff_mul(ff_load(svc + q), scale_cf));
     __syncthreads();
     {
-      const int u0 = st.b1_u0, u1 = st.b1_u1;
-      for (int u = u0 + warp; u < u1; u += TR_WARPS) {
-        const int r = c + 1 + u;
+      /* work items (column, segment): a block with fewer columns than warps splits each into
+       * S segments so that every warp works; segment dots are summed in order */
+      const int u0 = st.b1_u0, u1 = st.b1_u1, ncol = u1 - u0;
+      int S = (ncol > 0 && ncol < TR_WARPS) ? (TR_WARPS + ncol - 1) / ncol : 1;
+      const int nitem = ncol * S;
+      for (int it = warp; it < nitem; it += TR_WARPS) {
+        const int j = it / S, sg = it - j * S;
+        const int r = c + 1 + u0 + j;
+        const int seg = ((n - r + S - 1) / S + 31) & ~31;
+        const int qs = r + sg * seg, qe = min(n, qs + seg);
         const ff2 vpr = ff_neg(ff_load(svp + r)), wpr = ff_neg(ff_load(swp + r));
         double *col = A + (int64_t)r * n;
         ff2 dot = ZERO;
-        int q = r + lane;
+        int q = qs + lane;
         /* TR_U independent loads per lane before the arithmetic (memory-level parallelism) */
-        for (; q + 32 * (TR_U - 1) < n; q += 32 * TR_U) {
+        for (; q + 32 * (TR_U - 1) < qe; q += 32 * TR_U) {
           ff2 a[TR_U];
 #pragma unroll
           for (int k = 0; k < TR_U; ++k) a[k] = ff_load(col + q + 32 * k);
@@ -608,7 +622,7 @@ k_tridiag(double *A, int n, double *d, double *e, double *tau, double *vbuf, dou
             dot = ff_fma(a[k], ff_load(svc + qq), dot);
           }
         }
-        for (; q < n; q += 32) {
+        for (; q < qe; q += 32) {
           ff2 a = ff_load(col + q);
           if (have_p) {
             a = ff_fma(ff_load(svp + q), wpr, a);
@@ -618,7 +632,20 @@ k_tridiag(double *A, int n, double *d, double *e, double *tau, double *vbuf, dou
           dot = ff_fma(a, ff_load(svc + q), dot);
         }
         for (int o = 16; o; o >>= 1) dot = ff_add(dot, ff_shfl_xor(dot, o));
-        if (lane == 0) ff_store(ycur + r, dot);
+        if (lane == 0) {
+          if (S == 1)
+            ff_store(ycur + r, dot);
+          else
+            sdotp[it] = dot;
+        }
+      }
+      if (S > 1) {
+        __syncthreads();
+        for (int j = threadIdx.x; j < ncol; j += blockDim.x) {
+          ff2 t = sdotp[j * S];
+          for (int sg = 1; sg < S; ++sg) t = ff_add(t, sdotp[j * S + sg]);
+          ff_store(ycur + c + 1 + u0 + j, t);
+        }
       }
     }
     TR_STAMP(1)

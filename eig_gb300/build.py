@@ -5,6 +5,7 @@ Outputs (git-ignored):
   eig_gb300/_lib/libgpupca.so   C ABI of the hot path (include/gpupca.h, gpupca_run.h)
   eig_gb300/_lib/libgpsynth.so  seeded Balding-Nichols generator (eig_gb300/host/gp_synth.h)
   eig_gb300/_lib/gpusmartpca    drop-in CLI: smartpca -p parfile
+  eig_gb300/_lib/gpusmartrel    drop-in CLI: smartrel -p parfile
   oracle/_bin/liboracle.so      the CPU oracle (test infrastructure)
 """
 import concurrent.futures as cf
@@ -95,6 +96,12 @@ def build(verbose=False, force=False):
                os.path.join(HOST, "gp_synth.c")]
     if all(os.path.exists(s) for s in cli_src) and (force or _newer(cli, cli_src + hdrs + [lib])):
         _run(["gcc"] + CFLAGS + ["-o", cli] + cli_src +
+             ["-L" + LIB, "-lgpupca", "-Wl,-rpath,$ORIGIN", "-lm", "-lpthread"])
+    rel = os.path.join(LIB, "gpusmartrel")
+    rel_src = [os.path.join(HOST, "gpusmartrel_main.c"), os.path.join(HOST, "gp_io.c"),
+               os.path.join(HOST, "gp_synth.c")]
+    if all(os.path.exists(s) for s in rel_src) and (force or _newer(rel, rel_src + hdrs + [lib])):
+        _run(["gcc"] + CFLAGS + ["-o", rel] + rel_src +
              ["-L" + LIB, "-lgpupca", "-Wl,-rpath,$ORIGIN", "-lm", "-lpthread"])
     orc = os.path.join(ORACLE_BIN, "liboracle.so")
     osrc = os.path.join(ORACLE, "smartpca_oracle.c")

@@ -8,6 +8,7 @@
 #include <math.h>
 #include <stdarg.h>
 #include <stdlib.h>
+#include <algorithm>
 #include <vector>
 
 #include "gp_geno_gemm.h"
@@ -171,7 +172,7 @@ extern "C" void gp_close(gp_ctx *ctx)
                   ctx->d_killed, ctx->d_vtab,    ctx->d_xmean,   ctx->d_xfancy,  ctx->d_kept,
                   ctx->d_xtx,    ctx->d_evals,   ctx->d_evecs,   ctx->d_ffvecs,  ctx->d_fxscal,
                   ctx->d_scratch, ctx->d_scratch2, ctx->d_scratch3, ctx->d_scratch4, ctx->d_scratch5,
-                  ctx->d_err};
+                  ctx->d_err,   ctx->d_xtx_keep};
   for (size_t i = 0; i < sizeof(bufs) / sizeof(bufs[0]); ++i)
     if (bufs[i]) cudaFree(bufs[i]);
   if (ctx->solver) cusolverDnDestroy(ctx->solver);
@@ -195,7 +196,7 @@ extern "C" int gp_release(gp_ctx *ctx)
                    (void **)&ctx->d_kept,    (void **)&ctx->d_xtx,      (void **)&ctx->d_evals,
                    (void **)&ctx->d_evecs,   (void **)&ctx->d_ffvecs,   (void **)&ctx->d_fxscal,
                    (void **)&ctx->d_scratch, (void **)&ctx->d_scratch2, (void **)&ctx->d_scratch3,
-                   (void **)&ctx->d_scratch4, (void **)&ctx->d_scratch5};
+                   (void **)&ctx->d_scratch4, (void **)&ctx->d_scratch5, (void **)&ctx->d_xtx_keep};
   for (size_t i = 0; i < sizeof(bufs) / sizeof(bufs[0]); ++i) {
     if (*bufs[i]) cudaFree(*bufs[i]);
     *bufs[i] = NULL;
@@ -203,6 +204,8 @@ extern "C" int gp_release(gp_ctx *ctx)
   ctx->scratch_cap = ctx->scratch2_cap = ctx->scratch3_cap = ctx->scratch4_cap =
       ctx->scratch5_cap = 0;
   ctx->xtx_cap = 0;
+  ctx->keep_cap = 0;
+  ctx->keep_valid = 0;
   ctx->nsnp_all = 0;
   ctx->nind_all = 0;
   ctx->rlen_dev = 0;
@@ -348,6 +351,20 @@ extern "C" int gp_eigvecs(gp_ctx *ctx, int32_t nvec, double *evals, double *evec
   if (blocks > ctx->num_sms * 16) blocks = ctx->num_sms * 16;
   k_scale<<<blocks, 256, 0, ctx->stream>>>(ctx->d_xtx, nn, 1.0 / y);
   GP_LAUNCH_CHECK(ctx, "k_scale");
+  ctx->keep_valid = 0;
+  if (ctx->keep_gram) {
+    /* the scaled Gram for the relatedness scan (the eigensolve overwrites d_xtx) */
+    if (ctx->keep_cap < nn) {
+      if (ctx->d_xtx_keep) cudaFree(ctx->d_xtx_keep);
+      ctx->d_xtx_keep = NULL;
+      ctx->keep_cap = 0;
+      GP_CUDA(ctx, cudaMalloc((void **)&ctx->d_xtx_keep, sizeof(double) * (size_t)nn));
+      ctx->keep_cap = nn;
+    }
+    GP_CUDA(ctx, cudaMemcpyAsync(ctx->d_xtx_keep, ctx->d_xtx, sizeof(double) * (size_t)nn,
+                                 cudaMemcpyDeviceToDevice, ctx->stream));
+    ctx->keep_valid = 1;
+  }
 
   int rc = gp_realloc(ctx, (void **)&ctx->d_evals, sizeof(double) * (size_t)n);
   if (rc) return rc;
@@ -401,10 +418,116 @@ extern "C" int gp_eigvecs(gp_ctx *ctx, int32_t nvec, double *evals, double *evec
     if (info != 0) return gp_fail(ctx, GP_ERR_SOLVER, "eigensolver info = %d", info);
     if (evals)
       for (int32_t i = 0; i < n; ++i) evals[i] = w[(size_t)(n - 1 - i)];
+    /* the resident eigenvalues descending, as the tridiagonal path leaves them */
+    for (int32_t i = 0; i < n / 2; ++i) std::swap(w[(size_t)i], w[(size_t)(n - 1 - i)]);
+    GP_CUDA(ctx, gp_memcpy(ctx, ctx->d_evals, w.data(), sizeof(double) * (size_t)n,
+                           cudaMemcpyHostToDevice, ctx->stream));
   }
   ctx->nvec = nvec;
   ctx->eig_valid = 1;
   ctx->weights_valid = 0;
+  return GP_OK;
+}
+
+/* ------------------------------------------------------------------------------------ */
+/*
+ * Relatedness of smartrel (src/eigensrc/smartrel.c:578-615): from the scaled Gram of the last
+ * pass, R = XTX - sum_{i < K} w_i w_i^T with w_i = sqrt(lambda_i) v_i (subouter, in order),
+ * then for rows a < b: y = R_ab / sqrt(R_aa R_bb) + 1/(n-1); pairs with y >= relthresh.
+ * Same operation order as the reference, every product and sum rounded on its own.
+ */
+__global__ void k_rel_weights(const double *evals, const double *evecs, int32_t n, int32_t K,
+                              double *w)
+{
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < (int64_t)K * n;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t i = (int32_t)(idx / n);
+    w[idx] = __dmul_rn(evecs[idx], __dsqrt_rn(evals[i]));
+  }
+}
+
+__device__ __forceinline__ double rel_entry(const double *X, const double *w, int32_t n, int32_t K,
+                                            int32_t a, int32_t b)
+{
+  double r = X[(int64_t)a * n + b];
+  for (int32_t i = 0; i < K; ++i)
+    r = __dsub_rn(r, __dmul_rn(w[(int64_t)i * n + a], w[(int64_t)i * n + b]));
+  return r;
+}
+
+__global__ void k_rel_scan(const double *X, const double *w, int32_t n, int32_t K,
+                           double relthresh, int64_t max_pairs, int32_t *pa, int32_t *pb,
+                           double *ps, unsigned long long *count)
+{
+  const int64_t total = (int64_t)n * (n - 1) / 2;
+  const double add = 1.0 / (double)(n - 1);
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    /* t -> (a, b), a < b, row by row of the strict upper triangle */
+    int32_t a = (int32_t)floor(((2.0 * n - 1.0) - sqrt((2.0 * n - 1.0) * (2.0 * n - 1.0) - 8.0 * (double)t)) * 0.5);
+    while (a > 0 && (int64_t)a * (2 * (int64_t)n - a - 1) / 2 > t) --a;
+    while ((int64_t)(a + 1) * (2 * (int64_t)n - a - 2) / 2 <= t) ++a;
+    const int32_t b = (int32_t)(t - (int64_t)a * (2 * (int64_t)n - a - 1) / 2) + a + 1;
+    const double y1 = rel_entry(X, w, n, K, a, a), y2 = rel_entry(X, w, n, K, b, b);
+    const double y = __dadd_rn(__ddiv_rn(rel_entry(X, w, n, K, a, b), __dsqrt_rn(__dmul_rn(y1, y2))), add);
+    if (y < relthresh) continue;
+    const unsigned long long slot = atomicAdd(count, 1ull);
+    if ((int64_t)slot < max_pairs) {
+      pa[slot] = a;
+      pb[slot] = b;
+      ps[slot] = y;
+    }
+  }
+}
+
+extern "C" int gp_keep_gram(gp_ctx *ctx, int32_t keep)
+{
+  if (!ctx) return GP_ERR_ARG;
+  ctx->keep_gram = keep ? 1 : 0;
+  return GP_OK;
+}
+
+extern "C" int gp_relate(gp_ctx *ctx, int32_t numeigs, double relthresh, int64_t max_pairs,
+                         int32_t *pair_a, int32_t *pair_b, double *score, int64_t *npairs)
+{
+  if (!ctx || !npairs || max_pairs < 0 || (max_pairs > 0 && (!pair_a || !pair_b || !score)))
+    return GP_ERR_ARG;
+  if (!ctx->keep_valid || !ctx->eig_valid)
+    return gp_fail(ctx, GP_ERR_STATE, "gp_relate: no kept Gram (gp_keep_gram before gp_eigvecs)");
+  const int32_t n = ctx->nrows, K = numeigs;
+  if (K < 0 || K > ctx->nvec) return gp_fail(ctx, GP_ERR_ARG, "gp_relate: numeigs %d > %d", K, ctx->nvec);
+  GP_CUDA(ctx, cudaSetDevice(ctx->device));
+  const size_t nw = (size_t)K * n;
+  size_t bytes = sizeof(double) * (nw + (size_t)max_pairs) + sizeof(int32_t) * 2 * (size_t)max_pairs + 1024;
+  uint8_t *base;
+  int rc = gp_scratch(ctx, bytes, (void **)&base);
+  if (rc) return rc;
+  double *d_w = (double *)base, *d_s = d_w + nw;
+  int32_t *d_a = (int32_t *)(d_s + max_pairs), *d_b = d_a + max_pairs;
+  unsigned long long *d_cnt = (unsigned long long *)(((uintptr_t)(d_b + max_pairs) + 15) & ~(uintptr_t)15);
+  GP_CUDA(ctx, cudaMemsetAsync(d_cnt, 0, sizeof(unsigned long long), ctx->stream));
+  if (nw) {
+    int blocks = (int)((nw + 255) / 256);
+    if (blocks > ctx->num_sms * 8) blocks = ctx->num_sms * 8;
+    k_rel_weights<<<blocks, 256, 0, ctx->stream>>>(ctx->d_evals, ctx->d_evecs, n, K, d_w);
+    GP_LAUNCH_CHECK(ctx, "k_rel_weights");
+  }
+  if (n > 1) {
+    k_rel_scan<<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(ctx->d_xtx_keep, d_w, n, K, relthresh,
+                                                          max_pairs, d_a, d_b, d_s, d_cnt);
+    GP_LAUNCH_CHECK(ctx, "k_rel_scan");
+  }
+  unsigned long long cnt = 0;
+  GP_CUDA(ctx, gp_memcpy(ctx, &cnt, d_cnt, sizeof cnt, cudaMemcpyDeviceToHost, ctx->stream));
+  GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  *npairs = (int64_t)cnt;
+  const int64_t got = (int64_t)cnt < max_pairs ? (int64_t)cnt : max_pairs;
+  if (got > 0) {
+    GP_CUDA(ctx, gp_memcpy(ctx, pair_a, d_a, sizeof(int32_t) * (size_t)got, cudaMemcpyDeviceToHost, ctx->stream));
+    GP_CUDA(ctx, gp_memcpy(ctx, pair_b, d_b, sizeof(int32_t) * (size_t)got, cudaMemcpyDeviceToHost, ctx->stream));
+    GP_CUDA(ctx, gp_memcpy(ctx, score, d_s, sizeof(double) * (size_t)got, cudaMemcpyDeviceToHost, ctx->stream));
+    GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  }
   return GP_OK;
 }
 

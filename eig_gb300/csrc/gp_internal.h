@@ -51,6 +51,10 @@ struct gp_ctx {
   int64_t xtx_cap;
   double *d_evals;       /* [nrows] */
   double *d_evecs;       /* [nvec*nrows] top vectors, descending */
+  int keep_gram;         /* gp_keep_gram: copy the scaled Gram before the eigensolve */
+  double *d_xtx_keep;    /* [nrows*nrows] that copy (the relatedness scan reads it) */
+  int64_t keep_cap;
+  int keep_valid;
   int32_t nvec;
   int eig_valid;
 

@@ -34,7 +34,8 @@ EXPORTED = ["gp_version", "gp_last_error", "gp_open", "gp_close", "gp_device_byt
             "gp_noalloc_last_error", "gp_serve_open", "gp_serve_layout",
             "gp_serve_panel_snps", "gp_serve_submit", "gp_serve_test", "gp_serve_wait",
             "gp_serve_stats", "gp_serve_last_error", "gp_serve_close", "gp_serve_pause",
-            "gp_serve_submit_pca", "gp_serve_pca_stats", "gp_smartpca_footprint", "gp_release"]
+            "gp_serve_submit_pca", "gp_serve_pca_stats", "gp_smartpca_footprint", "gp_release",
+            "gp_keep_gram", "gp_relate"]
 
 i32p = C.POINTER(C.c_int32)
 i64p = C.POINTER(C.c_int64)
@@ -138,6 +139,8 @@ def load_library():
         "gp_serve_pca_stats": (C.c_int, [vp, i64p, i32p, i64p]),
         "gp_smartpca_footprint": (C.c_int64, [C.c_int32, C.c_int64, C.c_int32, C.c_int32]),
         "gp_release": (C.c_int, [vp]),
+        "gp_keep_gram": (C.c_int, [vp, C.c_int32]),
+        "gp_relate": (C.c_int, [vp, C.c_int32, C.c_double, C.c_int64, i32p, i32p, f64p, i64p]),
         "gp_serve_last_error": (C.c_char_p, [vp]),
         "gp_serve_close": (None, [vp]),
         "gp_smartpca_run": (C.c_int, [vp, C.POINTER(SmartpcaOpts), C.POINTER(Panel),
@@ -325,6 +328,28 @@ class Handle:
         self.check(self.lib.gp_last_gram_time(self.h, C.byref(ms), C.byref(n), C.byref(fl)),
                    "gp_last_gram_time")
         return ms.value, n.value, fl.value
+
+    def keep_gram(self, keep=True):
+        """keep a copy of the next eigensolve's scaled Gram for relate()"""
+        self.check(self.lib.gp_keep_gram(self.h, 1 if keep else 0), "gp_keep_gram")
+
+    def relate(self, numeigs, relthresh=0.05, max_pairs=1 << 16):
+        """smartrel's pair scan on the kept Gram: [(a, b, y)] in rows of the pass, highest y
+        first (ties by a, then b)"""
+        while True:
+            a = np.zeros(max_pairs, np.int32)
+            b = np.zeros(max_pairs, np.int32)
+            y = np.zeros(max_pairs)
+            n = C.c_int64()
+            self.check(self.lib.gp_relate(self.h, numeigs, relthresh, max_pairs,
+                                          ptr(a, C.c_int32), ptr(b, C.c_int32),
+                                          ptr(y, C.c_double), C.byref(n)), "gp_relate")
+            if n.value <= max_pairs:
+                break
+            max_pairs = n.value
+        a, b, y = a[:n.value], b[:n.value], y[:n.value]
+        order = np.lexsort((b, a, -y))
+        return [(int(a[k]), int(b[k]), float(y[k])) for k in order]
 
     def fastpca(self, K, L, I, seed=0, omega=None, precision=GP_PREC_FP64, fancynorm=1,
                 altnormstyle=1):
@@ -575,6 +600,25 @@ def smartpca_run(handle, records, nind, opts, code=GP_CODE_PACKED, snp_chrom=Non
     handle.check(handle.lib.gp_smartpca_run(handle.h, C.byref(opts), C.byref(a.panel),
                                             C.byref(a.result)), "gp_smartpca_run")
     return a.collect()
+
+
+def smartrel_run(handle, records, nind, numeigs=10, relthresh=0.05, minallelecnt=1,
+                 code=GP_CODE_PACKED, **kw):
+    """smartrel on in-memory records: the smartpca outlier loop with smartrel's SNP rule
+    (dropped when min(n0, n1) <= minallelecnt, no missingness limit, no projection), then the
+    relatedness scan.  Returns (pairs [(sample a, sample b, y)] highest first, run result)."""
+    panel_keys = ("snp_chrom", "snp_ignore", "ind_ignore", "ind_affstatus", "ind_male")
+    panel = {k: kw.pop(k) for k in panel_keys if k in kw}
+    opts = default_opts(numeigs=numeigs, minallelecnt=minallelecnt + 1, maxmissing=0x7fffffff,
+                        lsqproject=0, fastmode=0, **kw)
+    handle.keep_gram(True)
+    try:
+        r = smartpca_run(handle, records, nind, opts, code=code, **panel)
+        pairs = handle.relate(r["numeigs"], relthresh)
+    finally:
+        handle.keep_gram(False)
+    xi = r["xindex"]
+    return [(int(xi[a]), int(xi[b]), y) for a, b, y in pairs], r
 
 
 def smartpca_footprint(nind, nsnp, precision, numeigs):

@@ -183,6 +183,18 @@ int gp_fastpca(gp_ctx *ctx, int32_t K, int32_t L, int32_t I, uint64_t seed,
                const double *omega, const gp_xtx_opts *opts, double *evals, double *evecs);
 
 
+/*
+ * Relatedness (smartrel, src/eigensrc/smartrel.c:578-615).  gp_keep_gram(ctx, 1) makes
+ * gp_eigvecs keep a device copy of the scaled Gram; gp_relate then removes the top numeigs
+ * components, R = XTX - sum_i lambda_i v_i v_i^T (subouter, in order), and returns the row
+ * pairs a < b (indices into the PCA rows) with y = R_ab / sqrt(R_aa R_bb) + 1/(nrows-1) >=
+ * relthresh, in no particular order (the caller sorts by y, as the reference prints them).
+ * *npairs is the number found; at most max_pairs are copied.
+ */
+int gp_keep_gram(gp_ctx *ctx, int32_t keep);
+int gp_relate(gp_ctx *ctx, int32_t numeigs, double relthresh, int64_t max_pairs,
+              int32_t *pair_a, int32_t *pair_b, double *score, int64_t *npairs);
+
 /* Free every device buffer of the handle (panel, Gram, vectors, scratch); the handle, its
  * stream and solver stay usable and the next gp_load_genotypes starts afresh.  No
  * counterpart in the reference (a process ends instead). */

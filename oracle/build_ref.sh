@@ -1,5 +1,5 @@
 #!/bin/sh
-# Test infrastructure only: builds the UNMODIFIED reference `smartpca` (EIGENSOFT 8.0.0,
+# Test infrastructure only: builds the UNMODIFIED reference `smartpca` and `smartrel` (EIGENSOFT 8.0.0,
 # DReichLab/EIG) from its own C sources where they lie, into oracle/_ref/ (git-ignored).
 # The result is used to pin the oracle restatement and to generate the golden fixtures
 # under tests/golden/.  Nothing of the product links or runs it.
@@ -11,7 +11,7 @@
 #   * fastmode (src/ksrc, needs GSL) is replaced by a stub that exits with an error.
 #   * fprintf is wrapped (-Wl,--wrap=fprintf, ref_fullprec.c): unchanged output unless
 #     EIG_REF_FULLPREC=1, in which case the .eval/.evec number formats print %.17g so that
-#     1e-10 parity can be checked.  No reference source is modified or copied.
+#     1e-10 parity can be checked; smartrel also wraps printf (its relatedness scores).  No reference source is modified or copied.
 set -eu
 HERE=$(cd "$(dirname "$0")" && pwd)
 REF=${EIG_REFERENCE_DIR:-/root/reference}
@@ -56,3 +56,17 @@ gcc -o "$OUT/smartpca" $OBJS "$OUT/obj/ref_lapack_shim.o" "$OUT/obj/ref_fullprec
     "$OUT/obj/ref_fastmode_stub.o" -Wl,--wrap=fprintf \
     "$OPENBLAS" -Wl,-rpath,"$(dirname "$OPENBLAS")" -lm -lpthread
 echo "built $OUT/smartpca"
+# smartrel (src/Makefile: smartrel.o twsubs mcio qpsubs admutils egsubs regsubs eigsubs eigx
+# smartsubs + libnick) from the same objects
+gcc $CFLAGS -fno-builtin-printf -c "$REF/src/eigensrc/smartrel.c" -o "$OUT/obj/eigensrc_smartrel.o"
+RELOBJS=""
+for o in $OBJS; do
+  case "$o" in
+    *eigensrc_smartpca.o|*eigensrc_exclude.o|*_gval.o) ;;
+    *) RELOBJS="$RELOBJS $o" ;;
+  esac
+done
+gcc -o "$OUT/smartrel" "$OUT/obj/eigensrc_smartrel.o" $RELOBJS "$OUT/obj/ref_lapack_shim.o" \
+    "$OUT/obj/ref_fullprec.o" -Wl,--wrap=fprintf -Wl,--wrap=printf \
+    "$OPENBLAS" -Wl,-rpath,"$(dirname "$OPENBLAS")" -lm -lpthread
+echo "built $OUT/smartrel"

@@ -290,6 +290,46 @@ def grm_text_lines(X, numsnps):
     return ["%d %d %d %0.6f" % (a + 1, b + 1, numsnps, v) for a, b, v in zip(il[0], il[1], txt)]
 
 
+def relate(X, evals, evecs, numeigs, relthresh=0.05):
+    """The relatedness scan of smartrel (src/eigensrc/smartrel.c:578-618) on the unscaled Gram
+    X of the last pass: XTX scaled by 1/(trace/(n-1)) (:547-554), the top numeigs components
+    removed one by one (subouter of sqrt(lambda_i) v_i, :581-585, src/nicksrc/vsubs.c:2135),
+    then y = R_ab / sqrt(R_aa R_bb) + 1/(n-1) for a < b (:589-600).  Returns the pairs with
+    y >= relthresh as (a, b, y), rows of the pass, highest y first (the sort of -y, :606)."""
+    n = X.shape[0]
+    tr = 0.0
+    for a in range(n):
+        tr += X[a, a]
+    R = X * (1.0 / (tr / (n - 1)))
+    for i in range(numeigs):
+        w = evecs[i] * np.sqrt(evals[i])
+        R -= np.outer(w, w)
+    d = np.diag(R).copy()
+    ia, ib = np.triu_indices(n, 1)
+    y = R[ia, ib] / np.sqrt(d[ia] * d[ib]) + 1.0 / (n - 1)
+    keep = y >= relthresh
+    ia, ib, y = ia[keep], ib[keep], y[keep]
+    order = np.lexsort((ib, ia, -y))
+    return [(int(ia[k]), int(ib[k]), float(y[k])) for k in order]
+
+
+def smartrel(records, nind, numeigs=10, relthresh=0.05, numoutliter=5, numoutleigs=10,
+             outlthresh=6.0, minallelecnt=1, fancynorm=1, altnormstyle=1, snp_chrom=None,
+             noxdata=1, numchrom=22, ind_ignore=None, ind_affstatus=None):
+    """smartrel main() (src/eigensrc/smartrel.c:230-624): the smartpca outlier loop with a SNP
+    dropped when min(n0, n1) <= minallelecnt (:477-480) and no missingness limit, then
+    relate() on the last pass.  Returns (pairs with sample indices, the smartpca result)."""
+    r = smartpca(records, nind, numeigs=numeigs, numoutliter=numoutliter,
+                 numoutleigs=numoutleigs, outlthresh=outlthresh, fancynorm=fancynorm,
+                 altnormstyle=altnormstyle, minallelecnt=minallelecnt + 1,
+                 maxmissing=2 ** 31 - 1, lsqproject=0, snp_chrom=snp_chrom, noxdata=noxdata,
+                 numchrom=numchrom, ind_ignore=ind_ignore, ind_affstatus=ind_affstatus)
+    K = min(numeigs, r["numeigs"])
+    pairs = relate(r["xtx"], r["evals"], r["evecs"], K, relthresh)
+    xi = r["xindex"]
+    return [(int(xi[a]), int(xi[b]), y) for a, b, y in pairs], r
+
+
 def fastpca(records, cols, xindex, K, L, I, omega, fancynorm=1, altnormstyle=1):
     """kjg_fpca (src/ksrc/kjg_fpca.c:24-102) on the setgval table (src/gval.c:31-87), in numpy
     FP64 with the caller's Omega (nrows x L): returns evals [K] = S^2/M and evecs [K][nrows]."""

@@ -4,7 +4,9 @@
  * (src/eigensrc/smartpca.c:1428 "%12.6f\n"), the .evec header (:1435 "%9.3f ") and the
  * .evec coordinates (:1584-1585 "%10.4f  " / "%12.6f  ") and the GRM text values
  * (:3803 "%0.6f\n") are printed as %.17g, so that the reference's own results can be
- * compared at 1e-10 instead of at 6 printed decimals. */
+ * compared at 1e-10 instead of at 6 printed decimals.  The smartrel binary is also linked
+ * with -Wl,--wrap=printf: its relatedness score (src/eigensrc/smartrel.c:614 " %9.3f")
+ * prints as %.17g in the same mode. */
 #include <stdarg.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -35,6 +37,18 @@ int __wrap_fprintf(FILE *f, const char *fmt, ...)
   }
   va_start(ap, fmt);
   r = vfprintf(f, use, ap);
+  va_end(ap);
+  return r;
+}
+
+int __wrap_printf(const char *fmt, ...)
+{
+  const char *use = fmt;
+  va_list ap;
+  int r;
+  if (fullprec_mode() && strcmp(fmt, " %9.3f") == 0) use = " %.17g";
+  va_start(ap, fmt);
+  r = vprintf(use, ap);
   va_end(ap);
   return r;
 }

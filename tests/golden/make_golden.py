@@ -11,6 +11,9 @@ EIG_REF_FULLPREC=1 prints .eval/.evec numbers as %.17g).  Writes, per case:
   <case>/ref.outliers                     the reference's outlier-removal lines
   <case>/ref.log                          the reference's log
   <case>/ref.grm[.txt], ref.grm.id, ref.grm.bin, ref.grm.N.bin   GRM dumps (grm cases)
+  <case>/ref.rel, ref.rel.txt             smartrel "rel:" lines (tool == "smartrel": the case
+                                          runs oracle/_ref/smartrel; relatives are planted by
+                                          copying a share of one sample's genotypes to another)
 
 and copies the reference's own example fixtures (CONVERTF/example.*,
 EIGENSTRAT/example.*) into ref_examples/.  Usage:
@@ -31,6 +34,7 @@ from eig_gb300 import native  # noqa: E402  (the synthetic generator)
 from oracle import oracle as O  # noqa: E402
 
 REF_BIN = os.path.join(ROOT, "oracle", "_ref", "smartpca")
+REF_REL = os.path.join(ROOT, "oracle", "_ref", "smartrel")
 
 CASES = {
     # default options, 3 populations + 4 planted divergent samples -> outlier removal
@@ -53,7 +57,30 @@ CASES = {
                    miss=0.02, seed=14, fmt="packed",
                    par={"numoutevec": "4", "numoutlieriter": "3", "grmoutname": "out.grm"},
                    grm=True),
+    # smartrel: planted relatives (b copies a's genotype at a share of the SNPs), default
+    # relthresh 0.05 / outlier removal (numoutlierevec 10), 3 components removed, minallelecnt 2
+    "bn_rel": dict(nsnp=3000, pops=[40, 40, 30], fst=[0.01, 0.02, 0.03], miss=0.02, seed=15,
+                   fmt="packed", tool="smartrel",
+                   relatives=[(3, 4, 0.5), (10, 60, 0.5), (20, 21, 0.25), (45, 46, 0.9),
+                              (90, 91, 0.5), (100, 101, 0.125)],
+                   par={"minallelecnt": "2", "numoutevec": "3"}),
 }
+
+
+def plant_relatives(prefix, nsnp, nind, pairs, seed):
+    """copy sample a's genotype to sample b at a seeded share of the SNPs (GENO records)"""
+    raw = bytearray(open(prefix + ".geno", "rb").read())
+    rlen = max((nind + 3) // 4, 48)
+    rec = np.frombuffer(bytes(raw[rlen:]), np.uint8).reshape(nsnp, rlen)
+    g = O.unpack(rec, nind)
+    rng = np.random.default_rng(seed)
+    for a, b, frac in pairs:
+        m = rng.random(nsnp) < frac
+        g[m, b] = g[m, a]
+    out = O.pack(g)
+    raw[rlen:] = np.ascontiguousarray(out[:, :rlen]).tobytes()
+    with open(prefix + ".geno", "wb") as f:
+        f.write(bytes(raw))
 
 
 def write_bed_case(d, rec, nind, nsnp, pops):
@@ -83,6 +110,9 @@ def make_case(name, spec):
                                miss=spec["miss"], miss_hi=spec.get("miss_hi"),
                                n_admixed=spec.get("n_admixed", 0), seed=spec["seed"], nthreads=4)
     par = {}
+    if "relatives" in spec:
+        plant_relatives(prefix, spec["nsnp"], sum(spec["pops"]), spec["relatives"],
+                        spec["seed"] + 1000)
     if spec["fmt"] == "bed":
         nind = sum(spec["pops"])
         raw = open(prefix + ".geno", "rb").read()
@@ -95,7 +125,11 @@ def make_case(name, spec):
         par.update(genotypename="data.bed", snpname="data.bim", indivname="data.fam")
     else:
         par.update(genotypename="data.geno", snpname="data.snp", indivname="data.ind")
-    par.update(evecoutname="out.evec", evaloutname="out.eval", outlieroutname="out.outliers")
+    if spec.get("tool") == "smartrel":
+        par.update(outliername="out.outliers")
+    else:
+        par.update(evecoutname="out.evec", evaloutname="out.eval",
+                   outlieroutname="out.outliers")
     par.update(spec["par"])
     if "poplist" in spec:
         with open(os.path.join(d, "poplist"), "w") as f:
@@ -103,6 +137,9 @@ def make_case(name, spec):
     with open(os.path.join(d, "par"), "w") as f:
         for k, v in par.items():
             f.write("%s: %s\n" % (k, v))
+    if spec.get("tool") == "smartrel":
+        run_smartrel(d)
+        return
     run_reference(d, spec.get("grm", False))
     if spec.get("grm"):
         # the binary GRM from a second run of the same parfile with grmbinary: YES
@@ -132,6 +169,19 @@ def run_reference(d, grm=False):
         if grm:
             shutil.move(os.path.join(d, "out.grm"), os.path.join(d, "ref.grm" + suffix))
             shutil.move(os.path.join(d, "out.grm.id"), os.path.join(d, "ref.grm.id"))
+
+
+def run_smartrel(d):
+    env = dict(os.environ)
+    for prec, suffix in ((False, ".txt"), (True, "")):
+        env["EIG_REF_FULLPREC"] = "1" if prec else "0"
+        with open(os.path.join(d, "ref.log"), "w") as log:
+            subprocess.run([REF_REL, "-p", "par"], cwd=d, env=env, stdout=log,
+                           stderr=subprocess.STDOUT, check=True)
+        lines = [ln for ln in open(os.path.join(d, "ref.log")) if ln.startswith("rel:")]
+        with open(os.path.join(d, "ref.rel" + suffix), "w") as f:
+            f.writelines(lines)
+        shutil.move(os.path.join(d, "out.outliers"), os.path.join(d, "ref.outliers"))
 
 
 def copy_examples(ref_root):

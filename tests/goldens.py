@@ -5,6 +5,7 @@ import numpy as np
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 CASES = ["bn_outliers", "bn_bed_altnorm", "bn_project", "bn_grm"]
+REL_CASES = ["bn_rel"]
 
 
 def read_par(case):
@@ -52,14 +53,22 @@ class Case:
         if "poplistname" in p:
             keep = {l.strip() for l in open(os.path.join(d, p["poplistname"])) if l.strip()}
             self.affstatus = np.array([pp in keep for pp in self.pops], np.uint8)
-        self.ref_evals = np.loadtxt(os.path.join(d, "ref.eval"))
-        lines = open(os.path.join(d, "ref.evec")).read().splitlines()
-        self.ref_header = [float(x) for x in lines[0].split()[1:]]
-        self.ref_coords = {}
-        for l in lines[1:]:
-            t = l.split()
-            if t:
-                self.ref_coords[t[0]] = np.array([float(x) for x in t[1:-1]])
+        if os.path.exists(os.path.join(d, "ref.eval")):
+            self.ref_evals = np.loadtxt(os.path.join(d, "ref.eval"))
+            lines = open(os.path.join(d, "ref.evec")).read().splitlines()
+            self.ref_header = [float(x) for x in lines[0].split()[1:]]
+            self.ref_coords = {}
+            for l in lines[1:]:
+                t = l.split()
+                if t:
+                    self.ref_coords[t[0]] = np.array([float(x) for x in t[1:-1]])
+        if os.path.exists(os.path.join(d, "ref.rel")):
+            # smartrel "rel: ID ID y" lines, highest y first: full precision and as shipped
+            self.ref_rel = [(t[1], t[2], float(t[3])) for t in
+                            (l.split() for l in open(os.path.join(d, "ref.rel")))]
+            self.ref_rel_text = open(os.path.join(d, "ref.rel.txt")).read().splitlines()
+        self.ref_outlier_lines = [l.rstrip("\n") for l in open(os.path.join(d, "ref.outliers"))
+                                  if l.startswith("REMOVED")]
         self.ref_outliers = [l.split()[2] for l in open(os.path.join(d, "ref.outliers"))
                              if l.startswith("REMOVED")]
 
@@ -74,6 +83,20 @@ class Case:
             kw["altnormstyle"] = yesno(p["altnormstyle"])
         if "maxmissing" in p:
             kw["maxmissing"] = int(p["maxmissing"])
+        return kw
+
+    def rel_opts(self):
+        """smartrel keyword arguments of this case's parfile"""
+        p = self.par
+        kw = {}
+        if "numoutevec" in p:
+            kw["numeigs"] = int(p["numoutevec"])
+        if "relthresh" in p:
+            kw["relthresh"] = float(p["relthresh"])
+        if "minallelecnt" in p:
+            kw["minallelecnt"] = int(p["minallelecnt"])
+        if "numoutlieriter" in p:
+            kw["numoutliter"] = int(p["numoutlieriter"])
         return kw
 
     def packed_records(self):
@@ -135,3 +158,24 @@ def compare_grm_text(lines, ref_lines, values, ref_values):
         assert abs(float(a[3]) - float(b[3])) <= 1.0000001e-6
     assert len(diff) <= max(1, len(lines) // 10000)
     assert np.max(np.abs(np.asarray(values) - ref_values)) <= 1e-10 * np.max(np.abs(ref_values))
+
+
+def rel_lines(ids, pairs):
+    """the "rel:" lines smartrel prints (src/eigensrc/smartrel.c:611-615)"""
+    return ["rel: %20s %20s  %9.3f" % (ids[a], ids[b], y) for a, b, y in pairs]
+
+
+def compare_rel(pairs, ids, case, tol=1e-10):
+    """same pairs in the same order as the reference, scores within tol; printed lines equal
+    except where a score sits on a rounding boundary of %9.3f"""
+    got = [(ids[a], ids[b]) for a, b, _ in pairs]
+    want = [(a, b) for a, b, _ in case.ref_rel]
+    assert got == want
+    err = max([abs(y - r[2]) for (_, _, y), r in zip(pairs, case.ref_rel)] + [0.0])
+    assert err <= tol, "relatedness score error %g" % err
+    lines = rel_lines(ids, pairs)
+    diff = [i for i, (a, b) in enumerate(zip(lines, case.ref_rel_text)) if a != b]
+    for i in diff:
+        assert abs(float(lines[i].split()[3]) - float(case.ref_rel_text[i].split()[3])) <= 1.0000001e-3
+    assert len(diff) <= 1
+    return err

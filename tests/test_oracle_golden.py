@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle as O
-from tests.goldens import CASES, GOLDEN, Case, compare_coords, coords_by_id
+from tests.goldens import CASES, GOLDEN, REL_CASES, Case, compare_coords, coords_by_id
 
 EX = os.path.join(GOLDEN, "ref_examples")
 
@@ -82,3 +82,19 @@ def test_oracle_grm_matches_reference():
     compare_grm_text(lines, g.text, txt, g.values)
     assert np.max(float_ulps(binv, g.bin)) <= 1
     assert g.ids == ["NA\t" + c.ids[k] for k in r["xindex"]]
+
+
+@pytest.mark.parametrize("case", REL_CASES)
+def test_oracle_smartrel_matches_reference(case):
+    """smartrel: the oracle's outliers, pair list, order and scores against the reference"""
+    from tests.goldens import compare_rel, rel_lines
+    c = Case(case)
+    pairs, r = O.smartrel(c.packed_records(), c.nind, **c.rel_opts())
+    assert [c.ids[k] for k, *_ in r["outliers"]] == c.ref_outliers
+    # the sign of an eigenvector (and so of its z score) is the eigensolver's choice
+    assert ["REMOVED outlier %s iter %d evec %d sigmage %.3f" % (c.ids[k], it, v, abs(z))
+            for k, it, v, z in r["outliers"]] == [l.replace("sigmage -", "sigmage ")
+                                                   for l in c.ref_outlier_lines]
+    assert len(pairs) == len(c.ref_rel) > 20
+    compare_rel(pairs, c.ids, c, tol=1e-10)
+    assert rel_lines(c.ids, pairs)[0] == c.ref_rel_text[0]

@@ -455,9 +455,16 @@ __device__ __forceinline__ double rel_entry(const double *X, const double *w, in
   return r;
 }
 
-__global__ void k_rel_scan(const double *X, const double *w, int32_t n, int32_t K,
-                           double relthresh, int64_t max_pairs, int32_t *pa, int32_t *pb,
-                           double *ps, unsigned long long *count)
+/* R_aa for every row, once (the scan reads it for both ends of each pair) */
+__global__ void k_rel_diag(const double *X, const double *w, int32_t n, int32_t K, double *d)
+{
+  for (int32_t a = blockIdx.x * blockDim.x + threadIdx.x; a < n; a += gridDim.x * blockDim.x)
+    d[a] = rel_entry(X, w, n, K, a, a);
+}
+
+__global__ void k_rel_scan(const double *X, const double *w, const double *d, int32_t n,
+                           int32_t K, double relthresh, int64_t max_pairs, int32_t *pa,
+                           int32_t *pb, double *ps, unsigned long long *count)
 {
   const int64_t total = (int64_t)n * (n - 1) / 2;
   const double add = 1.0 / (double)(n - 1);
@@ -468,7 +475,7 @@ __global__ void k_rel_scan(const double *X, const double *w, int32_t n, int32_t 
     while (a > 0 && (int64_t)a * (2 * (int64_t)n - a - 1) / 2 > t) --a;
     while ((int64_t)(a + 1) * (2 * (int64_t)n - a - 2) / 2 <= t) ++a;
     const int32_t b = (int32_t)(t - (int64_t)a * (2 * (int64_t)n - a - 1) / 2) + a + 1;
-    const double y1 = rel_entry(X, w, n, K, a, a), y2 = rel_entry(X, w, n, K, b, b);
+    const double y1 = d[a], y2 = d[b];
     const double y = __dadd_rn(__ddiv_rn(rel_entry(X, w, n, K, a, b), __dsqrt_rn(__dmul_rn(y1, y2))), add);
     if (y < relthresh) continue;
     const unsigned long long slot = atomicAdd(count, 1ull);
@@ -498,11 +505,12 @@ extern "C" int gp_relate(gp_ctx *ctx, int32_t numeigs, double relthresh, int64_t
   if (K < 0 || K > ctx->nvec) return gp_fail(ctx, GP_ERR_ARG, "gp_relate: numeigs %d > %d", K, ctx->nvec);
   GP_CUDA(ctx, cudaSetDevice(ctx->device));
   const size_t nw = (size_t)K * n;
-  size_t bytes = sizeof(double) * (nw + (size_t)max_pairs) + sizeof(int32_t) * 2 * (size_t)max_pairs + 1024;
+  size_t bytes = sizeof(double) * (nw + (size_t)n + (size_t)max_pairs) +
+                 sizeof(int32_t) * 2 * (size_t)max_pairs + 1024;
   uint8_t *base;
   int rc = gp_scratch(ctx, bytes, (void **)&base);
   if (rc) return rc;
-  double *d_w = (double *)base, *d_s = d_w + nw;
+  double *d_w = (double *)base, *d_d = d_w + nw, *d_s = d_d + n;
   int32_t *d_a = (int32_t *)(d_s + max_pairs), *d_b = d_a + max_pairs;
   unsigned long long *d_cnt = (unsigned long long *)(((uintptr_t)(d_b + max_pairs) + 15) & ~(uintptr_t)15);
   GP_CUDA(ctx, cudaMemsetAsync(d_cnt, 0, sizeof(unsigned long long), ctx->stream));
@@ -513,8 +521,11 @@ extern "C" int gp_relate(gp_ctx *ctx, int32_t numeigs, double relthresh, int64_t
     GP_LAUNCH_CHECK(ctx, "k_rel_weights");
   }
   if (n > 1) {
-    k_rel_scan<<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(ctx->d_xtx_keep, d_w, n, K, relthresh,
-                                                          max_pairs, d_a, d_b, d_s, d_cnt);
+    k_rel_diag<<<(n + 255) / 256, 256, 0, ctx->stream>>>(ctx->d_xtx_keep, d_w, n, K, d_d);
+    GP_LAUNCH_CHECK(ctx, "k_rel_diag");
+    k_rel_scan<<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(ctx->d_xtx_keep, d_w, d_d, n, K,
+                                                          relthresh, max_pairs, d_a, d_b, d_s,
+                                                          d_cnt);
     GP_LAUNCH_CHECK(ctx, "k_rel_scan");
   }
   unsigned long long cnt = 0;

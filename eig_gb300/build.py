@@ -6,6 +6,7 @@ Outputs (git-ignored):
   eig_gb300/_lib/libgpsynth.so  seeded Balding-Nichols generator (eig_gb300/host/gp_synth.h)
   eig_gb300/_lib/gpusmartpca    drop-in CLI: smartpca -p parfile
   eig_gb300/_lib/gpusmartrel    drop-in CLI: smartrel -p parfile
+  eig_gb300/_lib/gpuconvertf    drop-in CLI: convertf -p parfile (packed/bed/EIGENSTRAT writers)
   oracle/_bin/liboracle.so      the CPU oracle (test infrastructure)
 """
 import concurrent.futures as cf
@@ -28,7 +29,7 @@ NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-ffp
                      "-I" + os.path.join(ROOT, "include")]
 CUDA_SOURCES = ["gp_api.cu", "gp_geno.cu", "gp_gram_f64.cu", "gp_geno_gemm_f64.cu",
                 "gp_gram_bf16.cu", "gp_fast.cu",
-                "gp_noalloc.cu", "gp_geno_tc.cu", "gp_eig.cu", "gp_serve.cu"]
+                "gp_noalloc.cu", "gp_geno_tc.cu", "gp_eig.cu", "gp_serve.cu", "gp_convert.cu"]
 HOST_LIB_SOURCES = ["gp_smartpca.c"]
 # no FMA contraction in host code: the reference's host arithmetic is plain multiply-add
 # (aarch64 would otherwise fuse it)
@@ -102,6 +103,12 @@ def build(verbose=False, force=False):
                os.path.join(HOST, "gp_synth.c")]
     if all(os.path.exists(s) for s in rel_src) and (force or _newer(rel, rel_src + hdrs + [lib])):
         _run(["gcc"] + CFLAGS + ["-o", rel] + rel_src +
+             ["-L" + LIB, "-lgpupca", "-Wl,-rpath,$ORIGIN", "-lm", "-lpthread"])
+    cvt = os.path.join(LIB, "gpuconvertf")
+    cvt_src = [os.path.join(HOST, "gpuconvertf_main.c"), os.path.join(HOST, "gp_io.c"),
+               os.path.join(HOST, "gp_synth.c")]
+    if all(os.path.exists(s) for s in cvt_src) and (force or _newer(cvt, cvt_src + hdrs + [lib])):
+        _run(["gcc"] + CFLAGS + ["-o", cvt] + cvt_src +
              ["-L" + LIB, "-lgpupca", "-Wl,-rpath,$ORIGIN", "-lm", "-lpthread"])
     orc = os.path.join(ORACLE_BIN, "liboracle.so")
     osrc = os.path.join(ORACLE, "smartpca_oracle.c")

@@ -240,6 +240,7 @@ int gp_read_snps(const char *path, int numchrom, gp_snplist *s, char *err, int e
   s->chrom = malloc(sizeof(int32_t) * cap);
   s->gpos = malloc(sizeof(double) * cap);
   s->ppos = malloc(sizeof(double) * cap);
+  s->alleles = malloc(sizeof(*s->alleles) * cap);
   char line[4096], *tok[16];
   while (fgets(line, sizeof line, f)) {
     int nt = split(line, tok, 16);
@@ -255,6 +256,7 @@ int gp_read_snps(const char *path, int numchrom, gp_snplist *s, char *err, int e
       s->chrom = realloc(s->chrom, sizeof(int32_t) * cap);
       s->gpos = realloc(s->gpos, sizeof(double) * cap);
       s->ppos = realloc(s->ppos, sizeof(double) * cap);
+      s->alleles = realloc(s->alleles, sizeof(*s->alleles) * cap);
     }
     const char *id = plink ? tok[1] : tok[0];
     const char *ch = plink ? tok[0] : tok[1];
@@ -262,9 +264,36 @@ int gp_read_snps(const char *path, int numchrom, gp_snplist *s, char *err, int e
     s->chrom[s->n] = chrom_of(ch, numchrom);
     s->gpos[s->n] = atof(tok[2]);
     s->ppos[s->n] = atof(tok[3]);
+    /* alleles: upper-cased first characters of columns 5 and 6 (readsnpdata,
+     * src/mcio.c:509-514); in a PLINK map as they are, '0' read as 'X' (readsnpmapdata
+     * :571-585) */
+    s->alleles[s->n][0] = s->alleles[s->n][1] = 0;
+    if (nt >= 6) {
+      for (int a = 0; a < 2; ++a) {
+        char c = tok[4 + a][0];
+        if (plink)
+          c = c == '0' ? 'X' : c;
+        else
+          c = (char)toupper((unsigned char)c);
+        s->alleles[s->n][a] = c;
+      }
+    }
     s->n++;
   }
   fclose(f);
+  /* genetic positions (src/mcio.c:517-535): all zero -> 1e-8 * physical position; else, if
+   * any exceeds 100, they are centimorgans and become morgans */
+  double maxg = -9999.0;
+  int usecm = 0;
+  for (int64_t i = 0; i < s->n; ++i) {
+    if (s->gpos[i] > maxg) maxg = s->gpos[i];
+    if (s->gpos[i] > 100) usecm = 1;
+  }
+  if (s->n > 0 && maxg <= 0.00001) {
+    for (int64_t i = 0; i < s->n; ++i) s->gpos[i] = 1.0e-8 * s->ppos[i];
+  } else if (usecm) {
+    for (int64_t i = 0; i < s->n; ++i) s->gpos[i] /= 100.0;
+  }
   s->order = malloc(sizeof(int64_t) * (s->n ? s->n : 1));
   for (int64_t i = 0; i < s->n; ++i) s->order[i] = i;
   g_sort_snps = s;
@@ -278,6 +307,7 @@ void gp_free_snps(gp_snplist *s)
   free(s->chrom);
   free(s->gpos);
   free(s->ppos);
+  free(s->alleles);
   free(s->order);
   memset(s, 0, sizeof *s);
 }

@@ -25,6 +25,7 @@ typedef struct {
   int32_t *chrom;
   double *gpos;
   double *ppos;
+  char (*alleles)[2]; /* first (reference) and second allele; 0 when the file has none */
   int64_t *order;   /* sorted position -> input row */
 } gp_snplist;
 

@@ -19,6 +19,7 @@ GP_ERR = {-1: "GP_ERR_ARG", -2: "GP_ERR_CUDA", -3: "GP_ERR_NOMEM", -4: "GP_ERR_S
           -9: "GP_ERR_NOTBUILT"}
 GP_ERR_TIMEOUT = -7
 GP_CODE_PACKED, GP_CODE_BED = 0, 1
+GP_OUT_PACKEDANCESTRYMAP, GP_OUT_PACKEDPED, GP_OUT_EIGENSTRAT = 0, 1, 2
 GP_PREC_FP64, GP_PREC_SPLIT_BF16, GP_PREC_SPLIT_BF16X4, GP_PREC_SPLIT_FP16 = 0, 1, 2, 3
 PRECISIONS = {"fp64": 0, "bf16": 1, "bf16x4": 2, "fp16": 3}
 PHASES = ["load", "filter", "gram", "eig", "outlier", "weights", "lsqproj", "total"]
@@ -35,7 +36,7 @@ EXPORTED = ["gp_version", "gp_last_error", "gp_open", "gp_close", "gp_device_byt
             "gp_serve_panel_snps", "gp_serve_submit", "gp_serve_test", "gp_serve_wait",
             "gp_serve_stats", "gp_serve_last_error", "gp_serve_close", "gp_serve_pause",
             "gp_serve_submit_pca", "gp_serve_pca_stats", "gp_smartpca_footprint", "gp_release",
-            "gp_keep_gram", "gp_relate"]
+            "gp_keep_gram", "gp_relate", "gp_record_bytes", "gp_encode_records"]
 
 i32p = C.POINTER(C.c_int32)
 i64p = C.POINTER(C.c_int64)
@@ -141,6 +142,9 @@ def load_library():
         "gp_release": (C.c_int, [vp]),
         "gp_keep_gram": (C.c_int, [vp, C.c_int32]),
         "gp_relate": (C.c_int, [vp, C.c_int32, C.c_double, C.c_int64, i32p, i32p, f64p, i64p]),
+        "gp_record_bytes": (C.c_int64, [C.c_int32, C.c_int32]),
+        "gp_encode_records": (C.c_int, [vp, C.c_int32, i32p, C.c_int32, i64p, u8p, C.c_int64,
+                                        vp, C.c_int32]),
         "gp_serve_last_error": (C.c_char_p, [vp]),
         "gp_serve_close": (None, [vp]),
         "gp_smartpca_run": (C.c_int, [vp, C.POINTER(SmartpcaOpts), C.POINTER(Panel),
@@ -328,6 +332,27 @@ class Handle:
         self.check(self.lib.gp_last_gram_time(self.h, C.byref(ms), C.byref(n), C.byref(fl)),
                    "gp_last_gram_time")
         return ms.value, n.value, fl.value
+
+    def encode_records(self, fmt, snps, samples=None, flip=None, nsamples=None, out=None):
+        """convertf's genotype records (gp_encode_records) of the resident panel: SNP list,
+        ordered sample list (None: the first nsamples samples), per-SNP flips.  Returns a
+        uint8 array [len(snps)][record bytes]; out may be a device pointer (int) instead."""
+        snp = np.ascontiguousarray(snps, dtype=np.int64)
+        smp = None if samples is None else np.ascontiguousarray(samples, dtype=np.int32)
+        n = len(smp) if smp is not None else int(nsamples)
+        fl = None if flip is None else np.ascontiguousarray(flip, dtype=np.uint8)
+        rb = self.lib.gp_record_bytes(fmt, n)
+        if out is None:
+            buf = np.zeros((len(snp), max(rb, 0)), np.uint8)
+            self.check(self.lib.gp_encode_records(self.h, fmt, ptr(smp, C.c_int32), n,
+                                                  ptr(snp, C.c_int64), ptr(fl, C.c_uint8),
+                                                  len(snp), buf.ctypes.data, 0),
+                       "gp_encode_records")
+            return buf
+        self.check(self.lib.gp_encode_records(self.h, fmt, ptr(smp, C.c_int32), n,
+                                              ptr(snp, C.c_int64), ptr(fl, C.c_uint8), len(snp),
+                                              out, 1), "gp_encode_records")
+        return None
 
     def keep_gram(self, keep=True):
         """keep a copy of the next eigensolve's scaled Gram for relate()"""

@@ -195,6 +195,27 @@ int gp_keep_gram(gp_ctx *ctx, int32_t keep);
 int gp_relate(gp_ctx *ctx, int32_t numeigs, double relthresh, int64_t max_pairs,
               int32_t *pair_a, int32_t *pair_b, double *score, int64_t *npairs);
 
+/*
+ * Genotype record writers of convertf (outputformat:) from the resident panel.
+ * gp_record_bytes: bytes of one output record for nsamples samples (-1 for a bad format):
+ *   GP_OUT_PACKEDANCESTRYMAP  max(ceil(n/4), 48)  outpack        src/mcio.c:2343-2457
+ *   GP_OUT_PACKEDPED          ceil(n/4)           outpackped     src/mcio.c:3619-3741
+ *   GP_OUT_EIGENSTRAT         n + 1 ('0'-'2', '9' missing, '\n') outeigenstrat src/mcio.c:3262
+ * gp_encode_records writes nsnps records (SNP snp_index[i] of the panel, samples
+ * sample_index[0..nsamples) in that order, or samples 0..nsamples-1 when sample_index is
+ * NULL; flip[i] != 0 replaces each observed g by 2 - g as flip1 does,
+ * src/convertf.c:1017-1026) to out (host memory, or device memory when out_on_device), one
+ * record after another.  The file headers (the "GENO" record, the bed magic) are the
+ * caller's.
+ */
+#define GP_OUT_PACKEDANCESTRYMAP 0
+#define GP_OUT_PACKEDPED 1
+#define GP_OUT_EIGENSTRAT 2
+int64_t gp_record_bytes(int32_t format, int32_t nsamples);
+int gp_encode_records(gp_ctx *ctx, int32_t format, const int32_t *sample_index,
+                      int32_t nsamples, const int64_t *snp_index, const uint8_t *flip,
+                      int64_t nsnps, uint8_t *out, int32_t out_on_device);
+
 /* Free every device buffer of the handle (panel, Gram, vectors, scratch); the handle, its
  * stream and solver stay usable and the next gp_load_genotypes starts afresh.  No
  * counterpart in the reference (a process ends instead). */

@@ -1,5 +1,5 @@
 #!/bin/sh
-# Test infrastructure only: builds the UNMODIFIED reference `smartpca` and `smartrel` (EIGENSOFT 8.0.0,
+# Test infrastructure only: builds the UNMODIFIED reference `smartpca`, `smartrel` and `convertf` (EIGENSOFT 8.0.0,
 # DReichLab/EIG) from its own C sources where they lie, into oracle/_ref/ (git-ignored).
 # The result is used to pin the oracle restatement and to generate the golden fixtures
 # under tests/golden/.  Nothing of the product links or runs it.
@@ -70,3 +70,15 @@ gcc -o "$OUT/smartrel" "$OUT/obj/eigensrc_smartrel.o" $RELOBJS "$OUT/obj/ref_lap
     "$OUT/obj/ref_fullprec.o" -Wl,--wrap=fprintf -Wl,--wrap=printf \
     "$OPENBLAS" -Wl,-rpath,"$(dirname "$OPENBLAS")" -lm -lpthread
 echo "built $OUT/smartrel"
+# convertf (src/Makefile: convertf.o mcio egsubs admutils h2d eigensrc/exclude + libnick)
+gcc $CFLAGS -c "$REF/src/convertf.c" -o "$OUT/obj/convertf.o"
+gcc $CFLAGS -c "$REF/src/h2d.c" -o "$OUT/obj/h2d.o"
+CVOBJS=""
+for o in $OBJS; do
+  case "$o" in
+    *nicksrc_*|*_mcio.o|*_egsubs.o|*_admutils.o|*eigensrc_exclude.o) CVOBJS="$CVOBJS $o" ;;
+  esac
+done
+gcc -o "$OUT/convertf" "$OUT/obj/convertf.o" "$OUT/obj/h2d.o" $CVOBJS "$OUT/obj/ref_lapack_shim.o" \
+    "$OPENBLAS" -Wl,-rpath,"$(dirname "$OPENBLAS")" -lm -lpthread
+echo "built $OUT/convertf"

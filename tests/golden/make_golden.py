@@ -184,6 +184,114 @@ def run_smartrel(d):
         shutil.move(os.path.join(d, "out.outliers"), os.path.join(d, "ref.outliers"))
 
 
+REF_CONVERTF = os.path.join(ROOT, "oracle", "_ref", "convertf")
+
+# convertf: input panels with the reference's edge cases, and the runs made on them
+CONVERT_CASES = {
+    "cv_edge": dict(nsnp=400, pops=[60, 50, 40], fst=[0.01, 0.02, 0.04], miss=0.03, seed=21,
+                    runs={"pk2pk": ("packed", "PACKEDANCESTRYMAP", False),
+                          "pk2bed": ("packed", "PACKEDPED", False),
+                          "pk2es": ("packed", "EIGENSTRAT", True),
+                          "bed2pk": ("bed", "PACKEDANCESTRYMAP", True),
+                          "bed2es": ("bed", "EIGENSTRAT", False)}),
+}
+
+
+def make_convert_case(name, spec):
+    """A seeded panel written as packedancestrymap (.geno/.snp/.ind) and PLINK (.bed/.bim/
+    .fam) with: chromosome 0 SNPs (dropped), chromosome X SNPs, duplicate positions (IDs of
+    equal and of different lengths), unknown first alleles (X, 0: flipped) and unknown
+    second ones, all-zero genetic positions (.snp: set from the physical position) and
+    centimorgans (.bim), an "Ignore" sample, a sample without data and samples of unknown
+    sex.  The reference convertf runs each entry of spec["runs"]:
+    (input, outputformat, with poplistname) -> out_<run>.{geno,snp,ind}."""
+    from oracle import convertf as CV
+    d = os.path.join(HERE, name)
+    os.makedirs(d, exist_ok=True)
+    rng = np.random.default_rng(spec["seed"])
+    rec, pop = native.synth_records(spec["nsnp"], spec["pops"], spec["fst"], miss=spec["miss"],
+                                    seed=spec["seed"], nthreads=4)
+    nind = len(pop)
+    M = spec["nsnp"]
+    g = O.unpack(rec, nind)
+    g[:, 7] = -1                                  # a sample without data
+    ids = ["S%07d" % k for k in range(nind)]
+    pops = ["POP%d" % p for p in pop]
+    pops[11] = "Ignore"
+    sexes = ["M" if k % 3 == 0 else "F" if k % 3 == 1 else "U" for k in range(nind)]
+    # SNP table in sorted order: 3 on chromosome 0, then 1, 2 and 23 (X)
+    chrom = np.concatenate([np.zeros(3, int), np.ones(197, int), np.full(180, 2),
+                            np.full(M - 380, 23)])
+    ppos = np.zeros(M, int)
+    for c in np.unique(chrom):
+        k = np.nonzero(chrom == c)[0]
+        ppos[k] = 1000 + np.cumsum(rng.integers(50, 5000, len(k)))
+    snp_id = ["rs%d" % (1000000 + i) for i in range(M)]
+    for i in range(20, M - 1, 37):                # duplicate positions
+        ppos[i + 1] = ppos[i]
+        if (i // 37) % 2:
+            snp_id[i + 1] = "AFFX-%07d" % i       # longer ID: the rs ID stays
+        else:
+            snp_id[i + 1] = "rs%d" % (2000000 + i)  # equal lengths: the larger ID stays
+    a0 = np.array(list("ACGT"))[rng.integers(0, 4, M)]
+    a1 = np.array(list("ACGT"))[rng.integers(0, 4, M)]
+    a0[5::23] = "X"                               # flipped
+    a0[9::31] = "0"                               # flipped ('0' in .snp and .bim)
+    a1[13::29] = "X"                              # not flipped
+    gen = np.zeros(M)                             # .snp: all zero -> 1e-8 * ppos
+    # packedancestrymap input
+    with open(os.path.join(d, "data.snp"), "w") as f:
+        for i in range(M):
+            f.write("%20s %4d %12.6f %12d %s %s\n" % (snp_id[i], chrom[i], gen[i], ppos[i],
+                                                     a0[i], a1[i]))
+    with open(os.path.join(d, "data.ind"), "w") as f:
+        for k in range(nind):
+            f.write("%20s %s %12s\n" % (ids[k], sexes[k], pops[k]))
+    with open(os.path.join(d, "data.geno"), "wb") as f:
+        f.write(CV.encode(g, "PACKEDANCESTRYMAP", ids=ids, snp_ids=snp_id))
+    # PLINK input: genetic positions in cM (> 100 somewhere -> converted)
+    cm = np.round(ppos * 1e-3, 6)
+    with open(os.path.join(d, "data.bim"), "w") as f:
+        for i in range(M):
+            f.write("%d\t%s\t%.6f\t%d\t%s\t%s\n" % (chrom[i], snp_id[i], cm[i], ppos[i], a0[i],
+                                                   a1[i]))
+    with open(os.path.join(d, "data.fam"), "w") as f:
+        for k in range(nind):
+            sx = {"M": 1, "F": 2, "U": 0}[sexes[k]]
+            f.write("F%d %s 0 0 %d %s\n" % (k, ids[k], sx, "-9" if k == 11 else pops[k]))
+    with open(os.path.join(d, "data.bed"), "wb") as f:
+        f.write(_bed_bytes(g))
+    with open(os.path.join(d, "poplist"), "w") as f:
+        f.write("POP2\nPOP0\n")
+    for run, (src, fmt, use_pl) in spec["runs"].items():
+        par = {"genotypename": "data.geno" if src == "packed" else "data.bed",
+               "snpname": "data.snp" if src == "packed" else "data.bim",
+               "indivname": "data.ind" if src == "packed" else "data.fam",
+               "outputformat": fmt, "genotypeoutname": "out_%s.geno" % run,
+               "snpoutname": "out_%s.snp" % run, "indivoutname": "out_%s.ind" % run}
+        if src == "bed":
+            par["familynames"] = "NO"
+        if use_pl:
+            par["poplistname"] = "poplist"
+        with open(os.path.join(d, "par_" + run), "w") as f:
+            for k, v in par.items():
+                f.write("%s: %s\n" % (k, v))
+        with open(os.path.join(d, "log_" + run), "w") as log:
+            subprocess.run([REF_CONVERTF, "-p", "par_" + run], cwd=d, stdout=log,
+                           stderr=subprocess.STDOUT, check=True)
+
+
+def _bed_bytes(g):
+    """PLINK .bed of a genotype matrix (count of the first allele, -1 missing)"""
+    nsnp, nind = g.shape
+    bedcode = np.where(g < 0, 1, np.where(g == 2, 0, np.where(g == 1, 2, 3))).astype(np.uint8)
+    blen = (nind + 3) // 4
+    pad = np.zeros((nsnp, blen * 4 - nind), np.uint8)
+    c = np.concatenate([bedcode, pad], axis=1).reshape(nsnp, blen, 4)
+    by = c[:, :, 0] | (c[:, :, 1] << 2) | (c[:, :, 2] << 4) | (c[:, :, 3] << 6)
+    return bytes([0x6C, 0x1B, 0x01]) + by.astype(np.uint8).tobytes()
+
+
 def copy_examples(ref_root):
     out = os.path.join(HERE, "ref_examples")
     os.makedirs(out, exist_ok=True)
@@ -208,4 +316,9 @@ if __name__ == "__main__":
         if only and name not in only:
             continue
         make_case(name, spec)
+        print("made", name)
+    for name, spec in CONVERT_CASES.items():
+        if only and name not in only:
+            continue
+        make_convert_case(name, spec)
         print("made", name)

@@ -98,3 +98,38 @@ def test_oracle_smartrel_matches_reference(case):
     assert len(pairs) == len(c.ref_rel) > 20
     compare_rel(pairs, c.ids, c, tol=1e-10)
     assert rel_lines(c.ids, pairs)[0] == c.ref_rel_text[0]
+
+
+CV_RUNS = ["pk2pk", "pk2bed", "pk2es", "bed2pk", "bed2es"]
+
+
+@pytest.mark.parametrize("run", CV_RUNS)
+def test_oracle_convertf_matches_reference(run):
+    """convertf's default path and packed writers restated (oracle/convertf.py): the three
+    output files byte-identical to the reference convertf's on a panel with chromosome 0,
+    duplicate positions, unknown alleles (flips), an Ignore sample and a sample without data"""
+    from oracle import convertf as CV
+    d = os.path.join(GOLDEN, "cv_edge")
+    par = {}
+    for line in open(os.path.join(d, "par_" + run)):
+        k, v = line.split(None, 1)
+        par[k.rstrip(":")] = v.strip()
+    o = CV.run_par(d, par)
+    assert o["geno"] == open(os.path.join(d, "out_%s.geno" % run), "rb").read()
+    assert o["snp"] == open(os.path.join(d, "out_%s.snp" % run)).read()
+    assert o["ind"] == open(os.path.join(d, "out_%s.ind" % run)).read()
+
+
+def test_convertf_edge_case_is_exercised():
+    """the fixture holds what it claims: dropped chromosome-0 and duplicate SNPs, flipped
+    SNPs (alleles swapped, genotypes 2-g), the Ignore sample and the sample without data"""
+    from oracle import convertf as CV
+    d = os.path.join(GOLDEN, "cv_edge")
+    snps, order = CV.read_snps(os.path.join(d, "data.snp"))
+    out = [l.split() for l in open(os.path.join(d, "out_pk2pk.snp"))]
+    assert len(out) < len(snps) - 3
+    ids = {s[0]: s for s in snps}
+    flipped = [o for o in out if ids[o[0]][4][0] in "X0" and ids[o[0]][4][1] not in "X0"]
+    assert len(flipped) >= 10 and all(o[4] == ids[o[0]][4][1] for o in flipped)
+    inds = [l.split()[0] for l in open(os.path.join(d, "out_pk2pk.ind"))]
+    assert "S0000011" not in inds and "S0000007" not in inds and len(inds) == 148

@@ -47,6 +47,10 @@ CONFIGS = {
                   name="mixed stream: projection requests on the N=5000 x M=600000 K=20 panel "
                        "+ full-PCA jobs at 1:20 (N log-U 200-8000, M U 50k-600k, 2-8 pops, "
                        "F~U(0.005,0.05), 1-5% missing, K=10), Poisson arrivals 40/s"),
+    "convertf": dict(nsnp=600_000, pops=[500, 700, 800, 900, 1000, 1100],
+                     fst=[0.005, 0.01, 0.02, 0.03, 0.04, 0.05], miss=0.02, K=0, seed=2,
+                     name="convertf packedancestrymap -> PLINK bed of the N=5000 x M=600000 "
+                          "panel (all samples, all SNPs)"),
     "small": dict(nsnp=60_000, pops=[100, 150, 200, 250, 150, 150],
                   fst=[0.005, 0.01, 0.02, 0.03, 0.04, 0.05], miss=0.02, K=20, seed=2,
                   name="smartpca N=1000 x M=60000 BN 6 pops (profiling case)"),
@@ -628,6 +632,72 @@ def run_fastmode(args, cfg, local):
                 d2h=d2h / n_e2e, acc=acc, gen_s=gen_s, nind=nind, launches=launches, evals=ev)
 
 
+def run_convertf(args, cfg, local):
+    """convertf's record writer (gp_encode_records, packed -> bed) on the resident panel:
+    device output timed by the kernel's CUDA events; e2e = pinned host records in, upload,
+    encode, bed records back in pinned host memory"""
+    import torch
+
+    from eig_gb300 import native
+    from oracle import convertf as CV
+    from oracle import oracle as O
+    torch.cuda.set_device(local)
+    rec, pop = native.synth_records(cfg["nsnp"], cfg["pops"], cfg["fst"], miss=cfg["miss"],
+                                    seed=cfg["seed"])
+    nind = len(pop)
+    M = cfg["nsnp"]
+    fmt = native.GP_OUT_PACKEDPED
+    rb = native.load_library().gp_record_bytes(fmt, nind)
+    h = native.Handle(local)
+    h.load_genotypes(rec, nind)
+    snps = np.arange(M, dtype=np.int64)
+    dev = torch.empty(M * rb, dtype=torch.uint8, device="cuda")
+    for _ in range(args.warmup):
+        h.encode_records(fmt, snps, None, None, nsamples=nind, out=dev.data_ptr())
+    clocks = ClockSampler(local)
+    clocks.start()
+    kern, wall = [], []
+    h.launch_count(reset=True)
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        h.timer_start()
+        h.encode_records(fmt, snps, None, None, nsamples=nind, out=dev.data_ptr())
+        wall.append(h.timer_stop())
+        kern.append(h.last_encode_time())
+    clk = clocks.stop()
+    launches = h.launch_count(reset=True) / max(1, args.steps)
+    alg = float(M) * (rec.shape[1] + rb)  # one read of each input record, one write of each output
+    # e2e through the C ABI: pinned host records -> device -> bed records in pinned host memory
+    out = np.empty((M, rb), np.uint8)
+    native.host_register(rec)
+    native.host_register(out)
+    h.transfer_bytes(reset=True)
+    e2e = []
+    for _ in range(max(1, min(args.steps, args.e2e_steps))):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        h.load_genotypes(rec, nind)
+        native.load_library().gp_encode_records(h.h, fmt, None, nind,
+                                                snps.ctypes.data_as(native.i64p), None, M,
+                                                out.ctypes.data, 0)
+        e2e.append(time.perf_counter() - t)
+    h2d, d2h = h.transfer_bytes(reset=True)
+    native.host_unregister(out)
+    native.host_unregister(rec)
+    ok = bool(np.array_equal(out.reshape(-1), dev.cpu().numpy()))
+    # CPU: the oracle's writer (unpack + outpackped restated in numpy, 1 thread) on a sample
+    ms = 20000
+    t = time.perf_counter()
+    CV.encode(O.unpack(rec[:ms], nind), "PACKEDPED", header=False)
+    cpu_dt = time.perf_counter() - t
+    cpu_val = ms * (rec.shape[1] + rb) / cpu_dt / 1e9
+    h.close()
+    n_e2e = len(e2e)
+    return dict(kern_ms=float(np.mean(kern)), wall_ms=float(np.mean(wall)), alg=alg,
+                e2e_s=float(np.mean(e2e)), h2d=h2d / n_e2e, d2h=d2h / n_e2e, clocks=clk,
+                launches=launches, nind=nind, ok=ok, cpu=(cpu_val, ms, cpu_dt))
+
+
 def cpu_reference_sample(cfg, seconds_target=12.0, nthreads=None):
     """The reference's partial-sum lookup Gram on the host cores over a SNP sample of the
     workload: returns (TFLOP/s in algorithmic N(N+1)M units, cores, sample description)."""
@@ -727,6 +797,36 @@ def main():
                 "dtype": "split fp16 Gram + exact tensor-core products, FP64 eigensolve",
                 "data": "synthetic (seeded Balding-Nichols)", "config": config,
                 "mixed": res, "clocks": res["clocks"]}
+        if rank == 0:
+            print(json.dumps(line))
+        return
+    if args.config == "convertf":
+        res = run_convertf(args, cfg, local)
+        peaks, kind = load_peaks()
+        achieved = res["alg"] / (res["kern_ms"] * 1e-3) / 1e9
+        line = {"metric": "convertf record conversion GB/s (input + output records)",
+                "value": world * achieved, "unit": "GB/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["kern_ms"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "u8", "data": "synthetic (seeded Balding-Nichols)",
+                "config": dict(config, numeigs=None, output="PACKEDPED"),
+                "call_ms": res["wall_ms"], "matches_host_path": res["ok"],
+                "roofline": {"bound": "hbm", "achieved": achieved,
+                             "peak": peaks.get("hbm_gbs", 6800.0), "unit": "GB/s",
+                             "frac": achieved / peaks.get("hbm_gbs", 6800.0), "traffic": None,
+                             "peak_kind": "HBM copy, %s" % kind,
+                             "kernels": "k_encode<PACKEDPED> (algorithmic M x (rlen_in + "
+                                        "rlen_out) bytes)"},
+                "clocks": res["clocks"],
+                "e2e": {"value": world * res["alg"] / res["e2e_s"] / 1e9, "unit": "GB/s",
+                        "h2d_bytes_per_step": int(res["h2d"]),
+                        "d2h_bytes_per_step": int(res["d2h"]), "wall_s": res["e2e_s"]},
+                "cpu_baseline": {"value": res["cpu"][0], "unit": "GB/s", "cores": 1,
+                                 "kind": "port",
+                                 "sample": "numpy restatement of outpackped (unpack + encode), "
+                                           "%d SNPs x %d samples, %.2f s" % (
+                                               res["cpu"][1], res["nind"], res["cpu"][2])},
+                "gpu_launches": res["launches"]}
         if rank == 0:
             print(json.dumps(line))
         return

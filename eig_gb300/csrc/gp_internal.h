@@ -69,6 +69,7 @@ struct gp_ctx {
   double gram_ms;
   int32_t gram_launches;
   double gram_flops;
+  double encode_ms;      /* k_encode time of the last device-output gp_encode_records */
 
   /* host<->device bytes copied by the handle (gp_transfer_bytes) */
   int64_t h2d_bytes, d2h_bytes;

@@ -36,7 +36,8 @@ EXPORTED = ["gp_version", "gp_last_error", "gp_open", "gp_close", "gp_device_byt
             "gp_serve_panel_snps", "gp_serve_submit", "gp_serve_test", "gp_serve_wait",
             "gp_serve_stats", "gp_serve_last_error", "gp_serve_close", "gp_serve_pause",
             "gp_serve_submit_pca", "gp_serve_pca_stats", "gp_smartpca_footprint", "gp_release",
-            "gp_keep_gram", "gp_relate", "gp_record_bytes", "gp_encode_records"]
+            "gp_keep_gram", "gp_relate", "gp_record_bytes", "gp_encode_records",
+            "gp_last_encode_time"]
 
 i32p = C.POINTER(C.c_int32)
 i64p = C.POINTER(C.c_int64)
@@ -143,6 +144,7 @@ def load_library():
         "gp_keep_gram": (C.c_int, [vp, C.c_int32]),
         "gp_relate": (C.c_int, [vp, C.c_int32, C.c_double, C.c_int64, i32p, i32p, f64p, i64p]),
         "gp_record_bytes": (C.c_int64, [C.c_int32, C.c_int32]),
+        "gp_last_encode_time": (C.c_int, [vp, f64p]),
         "gp_encode_records": (C.c_int, [vp, C.c_int32, i32p, C.c_int32, i64p, u8p, C.c_int64,
                                         vp, C.c_int32]),
         "gp_serve_last_error": (C.c_char_p, [vp]),
@@ -353,6 +355,11 @@ class Handle:
                                               ptr(snp, C.c_int64), ptr(fl, C.c_uint8), len(snp),
                                               out, 1), "gp_encode_records")
         return None
+
+    def last_encode_time(self):
+        ms = C.c_double()
+        self.check(self.lib.gp_last_encode_time(self.h, C.byref(ms)), "gp_last_encode_time")
+        return ms.value
 
     def keep_gram(self, keep=True):
         """keep a copy of the next eigensolve's scaled Gram for relate()"""

@@ -232,6 +232,10 @@ int gp_timer_stop(gp_ctx *ctx, double *ms);
  * count nrows*(nrows+1)*kept_snps of that call. */
 int gp_last_gram_time(const gp_ctx *ctx, double *ms, int32_t *launches, double *flops);
 
+/* Device time of the k_encode launch of the last gp_encode_records call that wrote to
+ * device memory (CUDA events around it on the handle's stream). */
+int gp_last_encode_time(const gp_ctx *ctx, double *ms);
+
 /* Host->device and device->host bytes the handle has copied (optionally reset to 0). */
 int gp_transfer_bytes(gp_ctx *ctx, int64_t *h2d, int64_t *d2h, int32_t reset);
 

@@ -88,3 +88,19 @@ def test_encode_rejects_out_of_range(gpu):
         gpu.encode_records(native.GP_OUT_PACKEDPED, [0], [0, 20])
     with pytest.raises(native.GpuError):
         gpu.encode_records(7, [0], None, None, nsamples=20)
+
+
+def test_encode_wide_records_direct_kernel(gpu):
+    """EIGENSTRAT records wider than shared memory (210,001 bytes) take the per-warp kernel"""
+    rng = np.random.default_rng(5)
+    nind, nsnp = 210_000, 6
+    g = rng.integers(0, 3, (nsnp, nind)).astype(np.int16)
+    g[rng.random((nsnp, nind)) < 0.2] = -1
+    gpu.load_genotypes(O.pack(g), nind)
+    flip = np.array([0, 1, 0, 1, 1, 0], np.uint8)
+    got = gpu.encode_records(native.GP_OUT_EIGENSTRAT, np.arange(nsnp), None, flip,
+                             nsamples=nind)
+    sub = g.copy()
+    f = flip.astype(bool)
+    sub[f] = np.where(sub[f] < 0, -1, 2 - sub[f])
+    assert got.tobytes() == CV.encode(sub, "EIGENSTRAT", header=False)

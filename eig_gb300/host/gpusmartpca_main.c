@@ -13,6 +13,7 @@
  * SPLIT_BF16, SPLIT_BF16X4 or SPLIT_FP16 (include/gpupca.h).  Keys of the reference's other analyses (Fst, ANOVA, shrinkage, LD regression,
  * GRM dump) are accepted and ignored with a note.
  */
+#include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -23,6 +24,224 @@
 #include "gp_io.h"
 
 static void usage(void) { fprintf(stderr, "usage: gpusmartpca -p parfile\n"); }
+
+/* get3 (src/admutils.c:1224-1237): the first character of a name and a blank */
+static const char *get3(const char *s)
+{
+  static char x[4];
+  x[0] = s[0] ? s[0] : ' ';
+  x[1] = ' ';
+  x[2] = 0;
+  return x;
+}
+
+/* printmatz5 / printmatz10 (src/admutils.c:1185-1221): lrint(scale * value) per entry */
+static void printmatz(const double *w, char **eg, int n, int wide)
+{
+  const double scale = wide ? 1000000.0 : 1000.0;
+  printf(" %5s", "   ");
+  for (int i = 0; i < n; ++i) printf(wide ? " %10s" : " %5s", get3(eg[i]));
+  printf("\n");
+  for (int i = 0; i < n; ++i) {
+    printf("%5s", get3(eg[i]));
+    for (int j = 0; j < n; ++j) printf(wide ? " %10d" : " %5d", (int)lrint(scale * w[i * n + j]));
+    printf("\n");
+  }
+}
+
+static double clipd(double x, double lo, double hi) { return x < lo ? lo : (x > hi ? hi : x); }
+
+/*
+ * The population summary and Fst section of smartpca's log after the PCA
+ * (src/eigensrc/smartpca.c:1784-1961): population sizes over the rows of the last pass, the
+ * block count, the Fst matrix and its jackknife standard errors (gp_fst), and the optional
+ * phylip / mega / fstdetails files.
+ */
+static int fst_tail(gp_ctx *ctx, const gp_parfile *pf, const gp_snplist *snps,
+                    const gp_indlist *inds, const gp_run_result *r, const char *poplistname,
+                    int64_t M, int32_t N)
+{
+  const char *phylipname = NULL, *fstdetailsname = NULL, *megaoutname = NULL;
+  int32_t fstverbose = 0, fsthiprec = 0, fstz = 0, t = 0;
+  double blgsize = 0.05;
+  gp_par_str(pf, "phylipname:", &phylipname);
+  gp_par_str(pf, "phylipoutname:", &phylipname);
+  gp_par_str(pf, "fstdetailsname:", &fstdetailsname);
+  gp_par_str(pf, "megaoutname:", &megaoutname);
+  gp_par_int(pf, "fstverbose:", &fstverbose);
+  gp_par_int(pf, "fsthiprecision:", &fsthiprec);
+  gp_par_int(pf, "fstz:", &fstz);
+  gp_par_dbl(pf, "blgsize:", &blgsize);
+  if (gp_par_int(pf, "inbreed:", &t) && t) {
+    printf("inbreed: YES is not supported by this path; no Fst section\n");
+    return 0;
+  }
+  /* eglist: the poplist order, else the order of first appearance (makeeglist) */
+  char **eg = (char **)malloc(sizeof(char *) * (size_t)(N + 4096));
+  int numeg = 0;
+  if (poplistname) {
+    FILE *pl = fopen(poplistname, "r");
+    char line[1024];
+    while (pl && fgets(line, sizeof line, pl)) {
+      char w[256];
+      if (sscanf(line, "%255s", w) != 1 || w[0] == '#') continue;
+      eg[numeg++] = strdup(w);
+    }
+    if (pl) fclose(pl);
+  } else {
+    for (int32_t k = 0; k < N; ++k) {
+      if (inds->ignore[k]) continue;
+      int found = 0;
+      for (int e = 0; e < numeg && !found; ++e) found = strcmp(eg[e], inds->pop[k]) == 0;
+      if (!found) eg[numeg++] = strdup(inds->pop[k]);
+    }
+  }
+  if (numeg < 1) return 0;
+  int32_t *xt = (int32_t *)malloc(sizeof(int32_t) * (size_t)r->nrows);
+  int32_t *psize = (int32_t *)calloc((size_t)numeg, sizeof(int32_t));
+  for (int32_t i = 0; i < r->nrows; ++i) {
+    xt[i] = -1;
+    for (int e = 0; e < numeg; ++e)
+      if (strcmp(eg[e], inds->pop[r->xindex[i]]) == 0) {
+        xt[i] = e;
+        break;
+      }
+    if (xt[i] >= 0) ++psize[xt[i]];
+  }
+  for (int e = 0; e < numeg; ++e) {
+    printf("population: %3d %20s %4d", e, eg[e], psize[e]);
+    if (psize[e] == 0) printf(" ***");
+    printf("\n");
+  }
+  /* jackknife blocks over the SNPs still in use (numblocks / setblocks) */
+  int32_t *chrom = (int32_t *)malloc(sizeof(int32_t) * (size_t)M);
+  double *gpos = (double *)malloc(sizeof(double) * (size_t)M);
+  uint8_t *ign = (uint8_t *)malloc((size_t)M);
+  int32_t *tag = (int32_t *)malloc(sizeof(int32_t) * (size_t)M);
+  for (int64_t i = 0; i < M; ++i) {
+    chrom[i] = snps->chrom[snps->order[i]];
+    gpos[i] = snps->gpos[snps->order[i]];
+    ign[i] = r->snp_state[i] != 0;
+  }
+  const int32_t nblocks = gp_set_blocks(chrom, gpos, ign, M, blgsize, tag);
+  printf("number of blocks for block jackknife: %d\n", nblocks);
+  if (nblocks == 1) printf("number of blocks 1: no standard error\n");
+  const size_t EE = (size_t)numeg * numeg;
+  double *fmean = (double *)calloc(EE, sizeof(double)), *fans = (double *)calloc(EE, sizeof(double));
+  double *fsd = (double *)calloc(EE, sizeof(double));
+  int32_t *fnum = (int32_t *)calloc(EE, sizeof(int32_t));
+  if (nblocks >= 1) {
+    int rc = gp_fst(ctx, xt, numeg, tag, nblocks, fmean, fans, fsd, fnum);
+    if (rc) return rc;
+  }
+  if (megaoutname) {
+    /* printmega (smartpca.c:4785-4812) */
+    FILE *f = fopen(megaoutname, "w");
+    if (f) {
+      fprintf(f, "#mega\n");
+      fprintf(f, "!TITLE distance for %d samples ;", numeg);
+      fprintf(f, "\n\n");
+      for (int i = 0; i < numeg; i++) fprintf(f, "#%s\n", eg[i]);
+      fprintf(f, "\n\n");
+      for (int i = 0; i < numeg; i++) {
+        for (int j = 0; j < i; j++) {
+          double y = fans[i * numeg + j];
+          fprintf(f, "  %9.6f", y > 0 ? y : 0);
+        }
+        fprintf(f, "\n");
+      }
+      fclose(f);
+    }
+  }
+  if ((phylipname == NULL && numeg > 10) || fstverbose) {
+    printf("## Fst statistics between populations:         fst       std error      Z\n");
+    for (int k1 = 0; k1 < numeg; ++k1) {
+      for (int k2 = k1 + 1; k2 < numeg; ++k2) {
+        const double z = fans[k1 * numeg + k2] / (fsd[k1 * numeg + k2] + 1.0e-10);
+        if (!fsthiprec)
+          printf(" %20s %20s %9.3f %10.4f", eg[k1], eg[k2], fans[k1 * numeg + k2],
+                 fsd[k1 * numeg + k2]);
+        else
+          printf(" %20s %20s %12.6f %12.6f", eg[k1], eg[k2], fans[k1 * numeg + k2],
+                 fsd[k1 * numeg + k2]);
+        printf("  %9.3f ", z);
+        printf(" %12d", fnum[k1 * numeg + k2]);
+        printf("\n");
+      }
+    }
+    printf("\n");
+  }
+  printf("## end of Fst statistics between populations\n");
+  if (fstdetailsname) {
+    FILE *f = fopen(fstdetailsname, "w");
+    if (f) {
+      fprintf(f, "## Fst statistics between populations:     fst     fstjack       std error      Z    snpnumber\n");
+      for (int k1 = 0; k1 < numeg; ++k1)
+        for (int k2 = k1 + 1; k2 < numeg; ++k2) {
+          const int k = k1 * numeg + k2;
+          if (!fsthiprec)
+            fprintf(f, "F_st %20s %20s %12.6f %12.6f %12.6f", eg[k1], eg[k2], fmean[k], fans[k],
+                    fsd[k]);
+          else
+            fprintf(f, "F_st %20s %20s %15.9f %15.9f %15.9f", eg[k1], eg[k2], fmean[k], fans[k],
+                    fsd[k]);
+          fprintf(f, " %9.3f", fans[k] / (fsd[k] + 1.0e-10));
+          fprintf(f, " %6d", fnum[k]);
+          fprintf(f, "\n");
+        }
+      fclose(f);
+    }
+  }
+  if (fstz) {
+    double *zz = (double *)malloc(sizeof(double) * EE);
+    memcpy(zz, fans, sizeof(double) * EE);
+    for (int k1 = 0; k1 < numeg; ++k1)
+      for (int k2 = k1 + 1; k2 < numeg; ++k2)
+        zz[k2 * numeg + k1] =
+            clipd(fans[k1 * numeg + k2] / (fsd[k1 * numeg + k2] + 1.0e-10), -9.999999, 9.999999);
+    printf("\n");
+    printf(fsthiprec ? "Fst: Z/F *1000000 [clipped to -10,10]\n" : "Fst: Z/F *1000 [clipped to -10,10]\n");
+    printmatz(zz, eg, numeg, fsthiprec);
+    free(zz);
+  }
+  printf("\n");
+  if (phylipname) {
+    FILE *f = fopen(phylipname, "w");
+    if (f) {
+      fprintf(f, "%6d\n", numeg);
+      for (int k1 = 0; k1 < numeg; ++k1) {
+        char sss[11];
+        snprintf(sss, sizeof sss, "%.10s", eg[k1]);
+        fprintf(f, "%10s", sss);
+        for (int k2 = 0; k2 < numeg; ++k2)
+          fprintf(f, "%6.3f", 0.5 * (fans[k1 * numeg + k2] + fans[k2 * numeg + k1]));
+        fprintf(f, "\n");
+      }
+      fclose(f);
+    }
+  }
+  if (numeg <= 10) {
+    printf(fsthiprec ? "fst *1000000:" : "fst *1000:");
+    printf("\n");
+    printmatz(fans, eg, numeg, fsthiprec);
+    printf("\n");
+  }
+  printf("std. err.  * 1000000:\n");
+  for (size_t i = 0; i < EE; ++i) fsd[i] *= 1000.0;
+  printmatz(fsd, eg, numeg, 0);
+  printf("\n");
+  free(fmean);
+  free(fans);
+  free(fsd);
+  free(fnum);
+  free(chrom);
+  free(gpos);
+  free(ign);
+  free(tag);
+  free(xt);
+  free(psize);
+  return 0;
+}
 
 static int in_list(const char *pop, char **list, int n)
 {
@@ -271,6 +490,14 @@ int main(int argc, char **argv)
     }
   }
   if (ef != stdout) fclose(ef);
+  if (!o.fastmode && nK > 0) {
+    rc = fst_tail(ctx, &pf, &snps, &inds, &r, poplistname, M, N);
+    if (rc) {
+      fprintf(stderr, "fatalx:\n%s (code %d)\n", gp_last_error(ctx), rc);
+      gp_close(ctx);
+      return 1;
+    }
+  }
   printf("## phase seconds: load %.3f filter %.3f gram %.3f eig %.3f outlier %.3f weights %.3f "
          "lsqproj %.3f total %.3f\n",
          r.t_phase[0], r.t_phase[1], r.t_phase[2], r.t_phase[3], r.t_phase[4], r.t_phase[5],

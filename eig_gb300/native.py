@@ -37,7 +37,7 @@ EXPORTED = ["gp_version", "gp_last_error", "gp_open", "gp_close", "gp_device_byt
             "gp_serve_stats", "gp_serve_last_error", "gp_serve_close", "gp_serve_pause",
             "gp_serve_submit_pca", "gp_serve_pca_stats", "gp_smartpca_footprint", "gp_release",
             "gp_keep_gram", "gp_relate", "gp_record_bytes", "gp_encode_records",
-            "gp_last_encode_time"]
+            "gp_last_encode_time", "gp_fst", "gp_set_blocks"]
 
 i32p = C.POINTER(C.c_int32)
 i64p = C.POINTER(C.c_int64)
@@ -145,6 +145,8 @@ def load_library():
         "gp_relate": (C.c_int, [vp, C.c_int32, C.c_double, C.c_int64, i32p, i32p, f64p, i64p]),
         "gp_record_bytes": (C.c_int64, [C.c_int32, C.c_int32]),
         "gp_last_encode_time": (C.c_int, [vp, f64p]),
+        "gp_fst": (C.c_int, [vp, i32p, C.c_int32, i32p, C.c_int32, f64p, f64p, f64p, i32p]),
+        "gp_set_blocks": (C.c_int32, [i32p, f64p, u8p, C.c_int64, C.c_double, i32p]),
         "gp_encode_records": (C.c_int, [vp, C.c_int32, i32p, C.c_int32, i64p, u8p, C.c_int64,
                                         vp, C.c_int32]),
         "gp_serve_last_error": (C.c_char_p, [vp]),
@@ -360,6 +362,16 @@ class Handle:
         ms = C.c_double()
         self.check(self.lib.gp_last_encode_time(self.h, C.byref(ms)), "gp_last_encode_time")
         return ms.value
+
+    def fst(self, xtypes, numeg, snp_block, nblocks):
+        """Fst of the last pass (gp_fst): (fstmean, fstans, fstsd, fstnum) [numeg, numeg]"""
+        xt = np.ascontiguousarray(xtypes, dtype=np.int32)
+        sb = np.ascontiguousarray(snp_block, dtype=np.int32)
+        out = [np.zeros((numeg, numeg)) for _ in range(3)] + [np.zeros((numeg, numeg), np.int32)]
+        self.check(self.lib.gp_fst(self.h, ptr(xt, C.c_int32), numeg, ptr(sb, C.c_int32),
+                                   nblocks, *[ptr(a, C.c_double) for a in out[:3]],
+                                   ptr(out[3], C.c_int32)), "gp_fst")
+        return tuple(out)
 
     def keep_gram(self, keep=True):
         """keep a copy of the next eigensolve's scaled Gram for relate()"""
@@ -651,6 +663,18 @@ def smartrel_run(handle, records, nind, numeigs=10, relthresh=0.05, minallelecnt
         handle.keep_gram(False)
     xi = r["xindex"]
     return [(int(xi[a]), int(xi[b]), y) for a, b, y in pairs], r
+
+
+def set_blocks(chrom, gpos, ignore, blocklen=0.05):
+    """setblocks: (number of blocks, tag per SNP)"""
+    ch = np.ascontiguousarray(chrom, dtype=np.int32)
+    gp = np.ascontiguousarray(gpos, dtype=np.float64)
+    ig = None if ignore is None else np.ascontiguousarray(ignore, dtype=np.uint8)
+    tag = np.zeros(len(ch), np.int32)
+    nb = load_library().gp_set_blocks(ptr(ch, C.c_int32), ptr(gp, C.c_double),
+                                      ptr(ig, C.c_uint8), len(ch), blocklen,
+                                      ptr(tag, C.c_int32))
+    return nb, tag
 
 
 def smartpca_footprint(nind, nsnp, precision, numeigs):

@@ -216,6 +216,27 @@ int gp_encode_records(gp_ctx *ctx, int32_t format, const int32_t *sample_index,
                       int32_t nsamples, const int64_t *snp_index, const uint8_t *flip,
                       int64_t nsnps, uint8_t *out, int32_t out_on_device);
 
+/*
+ * Fst between populations over the columns of the last gp_xtx pass that were not killed and
+ * the current rows (dofstxx src/eigensrc/smartpca.c:2830-2878, dofstnumx src/qpsubs.c:2488-2720,
+ * fstcolyy :1205-1345): xtypes[r] is the population (0..numeg-1; other values: none) of row r,
+ * snp_block[s] the jackknife block of panel SNP s (-1: none; gp_set_blocks), nblocks the
+ * number of blocks (numblocks :1631).  Per population pair a < b: fstnum = SNPs with an
+ * estimate, fstmean = sum N / (sum D + 1e-10), fstans and fstsd the weighted block-jackknife
+ * estimate and standard error (wjackest :2793-2858; fstmean and 0 with one block); all four
+ * [numeg*numeg] symmetric with a zero diagonal (fstmean: upper triangle).  Any output may be NULL.
+ * Populations are counted on the device; the estimator and jackknife run on the host in the
+ * reference's operation order.
+ */
+int gp_fst(gp_ctx *ctx, const int32_t *xtypes, int32_t numeg, const int32_t *snp_block,
+           int32_t nblocks, double *fstmean, double *fstans, double *fstsd, int32_t *fstnum);
+
+/* setblocks (src/qpsubs.c:1578-1627), a host function: block tags for n SNPs in sorted order
+ * (a new block at a chromosome change or blocklen morgans after the block's first SNP; SNPs
+ * with ignore[i] set get -1; tag may be NULL).  Returns the number of blocks. */
+int32_t gp_set_blocks(const int32_t *chrom, const double *gpos, const uint8_t *ignore, int64_t n,
+                      double blocklen, int32_t *tag);
+
 /* Free every device buffer of the handle (panel, Gram, vectors, scratch); the handle, its
  * stream and solver stay usable and the next gp_load_genotypes starts afresh.  No
  * counterpart in the reference (a process ends instead). */

@@ -330,6 +330,114 @@ def smartrel(records, nind, numeigs=10, relthresh=0.05, numoutliter=5, numoutlei
     return [(int(xi[a]), int(xi[b]), y) for a, b, y in pairs], r
 
 
+def set_blocks(chrom, gpos, ignore, blocklen=0.05):
+    """setblocks (src/qpsubs.c:1578-1627): (number of blocks, tag per SNP, -1 if ignored)"""
+    n, lchrom, xsize, fpos = 0, -1, 0, -1.0e20
+    tag = np.full(len(chrom), -1, np.int32)
+    for i in range(len(chrom)):
+        if ignore[i]:
+            continue
+        if chrom[i] != lchrom or gpos[i] - fpos >= blocklen:
+            if xsize > 0:
+                n += 1
+            lchrom, fpos, xsize = chrom[i], gpos[i], 0
+        tag[i] = n
+        xsize += 1
+    return n + (1 if xsize > 0 else 0), tag
+
+
+def _wjack(mean, jmean, jwt):
+    """wjackest / wjackestx (src/qpsubs.c:2793-2858), sequential sums"""
+    keep = [k for k in range(len(jwt)) if jwt[k] >= 1.0e-6]
+    jm = [jmean[k] for k in keep]
+    jw = [jwt[k] for k in keep]
+    g = len(jw)
+    if g <= 1:
+        return mean, 0.0
+    yn = 0.0
+    for w in jw:
+        yn += w
+    sd = 0.0
+    for m in jm:
+        sd += -(m + -mean)
+    dot = 0.0
+    for w, m in zip(jw, jm):
+        dot += w * m
+    jack = sd + dot / yn
+    var = 0.0
+    for w, m in zip(jw, jm):
+        hh = yn / w
+        w1 = hh + -1.0
+        xt = (hh * mean - w1 * m) + -jack
+        var += (xt * xt) / w1
+    return jack, float(np.sqrt(var / g))
+
+
+def fst(records, nind, xindex, xtypes, numeg, cols, tags, nblocks):
+    """dofstnumx (src/qpsubs.c:2488-2720) with fstcolyy (:1205-1345) over the columns cols
+    (SNP indices, none killed) and rows xindex with populations xtypes: (fstmean, fstans,
+    fstsd, fstnum), each numeg x numeg"""
+    g = unpack(np.ascontiguousarray(records)[np.asarray(cols)], nind)[:, np.asarray(xindex)]
+    xt = np.asarray(xtypes)
+    E = numeg
+    cnt = np.zeros((len(cols), E, 2), np.int64)
+    obs = g >= 0
+    for p in range(E):
+        m = (xt == p)[None, :] & obs
+        c0 = np.where(m, g, 0).sum(axis=1)
+        cnt[:, p, 0] = c0
+        cnt[:, p, 1] = 2 * m.sum(axis=1) - c0
+    top = np.zeros((nblocks, E, E))
+    bot = np.zeros((nblocks, E, E))
+    wj = np.zeros(nblocks)
+    num = np.zeros((E, E), np.int64)
+    for c, s in enumerate(cols):
+        b = tags[s]
+        if b < 0:
+            continue
+        wj[b] += 1.0
+        for a in range(E):
+            ya, yb = float(cnt[c, a, 0]), float(cnt[c, a, 1])
+            for bb in range(a + 1, E):
+                yaa, ybb = float(cnt[c, bb, 0]), float(cnt[c, bb, 1])
+                zz, z = yaa + ybb, ya + yb
+                if z < 1.5 or zz < 1.5:
+                    continue
+                yt = ya + yb
+                p1 = ya / yt
+                h1 = ya * yb / (yt * (yt - 1.0))
+                yt = yaa + ybb
+                p2 = yaa / yt
+                h2 = yaa * ybb / (yt * (yt - 1.0))
+                en = (p1 - p2) * (p1 - p2)
+                en -= h1 / z
+                en -= h2 / zz
+                ed = en + h1
+                ed += h2
+                num[a, bb] += 1
+                top[b, a, bb] += en
+                bot[b, a, bb] += ed
+    gtop = np.zeros((E, E))
+    gbot = np.zeros((E, E))
+    for k in range(nblocks):
+        gtop += top[k]
+        gbot += bot[k]
+    djk = (gtop[None] - top) / ((gbot[None] - bot) + 1.0e-10)
+    fmean = gtop / (gbot + 1.0e-10)
+    fans = np.zeros((E, E))
+    fsd = np.zeros((E, E))
+    fnum = np.zeros((E, E), np.int64)
+    for i in range(E):
+        for j in range(i + 1, E):
+            est, sig = fmean[i, j], 0.0
+            if nblocks > 1:
+                est, sig = _wjack(fmean[i, j], djk[:, i, j], wj)
+            fans[i, j] = fans[j, i] = est
+            fsd[i, j] = fsd[j, i] = sig
+            fnum[i, j] = fnum[j, i] = num[i, j]
+    return fmean, fans, fsd, fnum
+
+
 def fastpca(records, cols, xindex, K, L, I, omega, fancynorm=1, altnormstyle=1):
     """kjg_fpca (src/ksrc/kjg_fpca.c:24-102) on the setgval table (src/gval.c:31-87), in numpy
     FP64 with the caller's Omega (nrows x L): returns evals [K] = S^2/M and evecs [K][nrows]."""

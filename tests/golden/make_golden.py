@@ -11,6 +11,8 @@ EIG_REF_FULLPREC=1 prints .eval/.evec numbers as %.17g).  Writes, per case:
   <case>/ref.outliers                     the reference's outlier-removal lines
   <case>/ref.log                          the reference's log
   <case>/ref.grm[.txt], ref.grm.id, ref.grm.bin, ref.grm.N.bin   GRM dumps (grm cases)
+  <case>/ref.fstdetails[.txt], ref.mega   Fst files (bn_fst; ref_par_pl.log, ref.phylip and
+                                          ref_pl.fstdetails from its second parfile par_pl)
   <case>/ref.rel, ref.rel.txt             smartrel "rel:" lines (tool == "smartrel": the case
                                           runs oracle/_ref/smartrel; relatives are planted by
                                           copying a share of one sample's genotypes to another)
@@ -57,6 +59,18 @@ CASES = {
                    miss=0.02, seed=14, fmt="packed",
                    par={"numoutevec": "4", "numoutlieriter": "3", "grmoutname": "out.grm"},
                    grm=True),
+    # Fst tail: 12 populations on two chromosomes spanning ~24 jackknife blocks (numeg > 10:
+    # the per-pair Fst lines), fstdetails and mega files; a second run on 6 listed populations
+    # with phylip output, fsthiprecision and fstz
+    "bn_fst": dict(nsnp=3000, pops=[16, 18, 20, 15, 17, 19, 16, 18, 20, 15, 17, 19],
+                   fst=[0.005, 0.01, 0.02, 0.03, 0.04, 0.05, 0.005, 0.01, 0.02, 0.03, 0.04, 0.05],
+                   miss=0.02, seed=16, fmt="packed", relocate=(2, 4e-4),
+                   par={"numoutevec": "4", "fstdetailsname": "out.fstdetails",
+                        "megaoutname": "out.mega"},
+                   runs2={"par_pl": {"poplistname": "poplist", "phylipname": "out.phylip",
+                                     "fsthiprecision": "YES", "fstz": "YES",
+                                     "fstdetailsname": "out_pl.fstdetails"}},
+                   poplist=["POP5", "POP1", "POP3", "POP0", "POP9", "POP11"]),
     # smartrel: planted relatives (b copies a's genotype at a share of the SNPs), default
     # relthresh 0.05 / outlier removal (numoutlierevec 10), 3 components removed, minallelecnt 2
     "bn_rel": dict(nsnp=3000, pops=[40, 40, 30], fst=[0.01, 0.02, 0.03], miss=0.02, seed=15,
@@ -65,6 +79,18 @@ CASES = {
                               (90, 91, 0.5), (100, 101, 0.125)],
                    par={"minallelecnt": "2", "numoutevec": "3"}),
 }
+
+
+def relocate_snps(prefix, nchrom, step):
+    """spread the SNPs over nchrom chromosomes in equal runs, genetic positions step morgans
+    apart (physical 1e8 x genetic); the IDs, and so the GENO header hash, stay"""
+    lines = [l.split() for l in open(prefix + ".snp") if l.strip()]
+    per = (len(lines) + nchrom - 1) // nchrom
+    with open(prefix + ".snp", "w") as f:
+        for i, t in enumerate(lines):
+            c, j = 1 + i // per, i % per
+            f.write("%20s %4d %12.6f %12d %s %s\n" % (t[0], c, (j + 1) * step,
+                                                     int(round((j + 1) * step * 1e8)), t[4], t[5]))
 
 
 def plant_relatives(prefix, nsnp, nind, pairs, seed):
@@ -110,6 +136,8 @@ def make_case(name, spec):
                                miss=spec["miss"], miss_hi=spec.get("miss_hi"),
                                n_admixed=spec.get("n_admixed", 0), seed=spec["seed"], nthreads=4)
     par = {}
+    if "relocate" in spec:
+        relocate_snps(prefix, *spec["relocate"])
     if "relatives" in spec:
         plant_relatives(prefix, spec["nsnp"], sum(spec["pops"]), spec["relatives"],
                         spec["seed"] + 1000)
@@ -140,7 +168,22 @@ def make_case(name, spec):
     if spec.get("tool") == "smartrel":
         run_smartrel(d)
         return
-    run_reference(d, spec.get("grm", False))
+    run_reference(d, spec.get("grm", False), extra=("fstdetails",) if "fstdetailsname" in par else ())
+    for rname, extra_par in spec.get("runs2", {}).items():
+        with open(os.path.join(d, rname), "w") as f:
+            for k, v in par.items():
+                if k not in extra_par and k not in ("fstdetailsname", "megaoutname"):
+                    f.write("%s: %s\n" % (k, v))
+            for k, v in extra_par.items():
+                f.write("%s: %s\n" % (k, v))
+        env = dict(os.environ, EIG_REF_FULLPREC="0")
+        with open(os.path.join(d, "ref_%s.log" % rname), "w") as log:
+            subprocess.run([REF_BIN, "-p", rname], cwd=d, env=env, stdout=log,
+                           stderr=subprocess.STDOUT, check=True)
+        for n in ("out.eval", "out.evec", "out.outliers"):
+            os.remove(os.path.join(d, n))
+        shutil.move(os.path.join(d, "out.phylip"), os.path.join(d, "ref.phylip"))
+        shutil.move(os.path.join(d, "out_pl.fstdetails"), os.path.join(d, "ref_pl.fstdetails"))
     if spec.get("grm"):
         # the binary GRM from a second run of the same parfile with grmbinary: YES
         with open(os.path.join(d, "par_bin"), "w") as f:
@@ -156,7 +199,7 @@ def make_case(name, spec):
             os.remove(os.path.join(d, n))
 
 
-def run_reference(d, grm=False):
+def run_reference(d, grm=False, extra=()):
     env = dict(os.environ)
     for prec, suffix in ((False, ".txt"), (True, "")):
         env["EIG_REF_FULLPREC"] = "1" if prec else "0"
@@ -169,6 +212,10 @@ def run_reference(d, grm=False):
         if grm:
             shutil.move(os.path.join(d, "out.grm"), os.path.join(d, "ref.grm" + suffix))
             shutil.move(os.path.join(d, "out.grm.id"), os.path.join(d, "ref.grm.id"))
+        for ext in extra:
+            shutil.move(os.path.join(d, "out." + ext), os.path.join(d, "ref.%s%s" % (ext, suffix)))
+        if os.path.exists(os.path.join(d, "out.mega")):
+            shutil.move(os.path.join(d, "out.mega"), os.path.join(d, "ref.mega"))
 
 
 def run_smartrel(d):

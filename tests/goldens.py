@@ -179,3 +179,51 @@ def compare_rel(pairs, ids, case, tol=1e-10):
         assert abs(float(lines[i].split()[3]) - float(case.ref_rel_text[i].split()[3])) <= 1.0000001e-3
     assert len(diff) <= 1
     return err
+
+
+def snp_table(case):
+    """(chrom, gpos in morgans) per SNP of a case's .snp file, in file order (sorted)"""
+    c = Case(case)
+    rows = [l.split() for l in open(os.path.join(c.dir, c.par["snpname"])) if l.strip()]
+    chrom = np.array([int(r[1]) for r in rows], np.int32)
+    gpos = np.array([float(r[2]) for r in rows])
+    if gpos.max() <= 0.00001:
+        gpos = 1e-8 * np.array([float(r[3]) for r in rows])
+    elif gpos.max() > 100:
+        gpos = gpos / 100.0
+    return chrom, gpos
+
+
+def eglist(case, par=None):
+    """populations in the reference's order: the poplist, else first appearance"""
+    c = Case(case)
+    p = par or c.par
+    if "poplistname" in p:
+        return [l.split()[0] for l in open(os.path.join(c.dir, p["poplistname"])) if l.strip()]
+    out = []
+    for pop in c.pops:
+        if pop != "Ignore" and pop not in out:
+            out.append(pop)
+    return out
+
+
+def read_fstdetails(path):
+    """{(pop1, pop2): (fst, fstjack, stderr, z, snpnumber)}"""
+    out = {}
+    for line in open(path):
+        t = line.split()
+        if t and t[0] == "F_st":
+            out[(t[1], t[2])] = tuple(float(x) for x in t[3:7]) + (int(t[7]),)
+    return out
+
+
+def log_section(text):
+    """the population summary and Fst section of a smartpca log: from the first
+    "population:" line through the "std. err." matrix"""
+    lines = text.splitlines()
+    i0 = next(i for i, l in enumerate(lines) if l.startswith("population:"))
+    i1 = next(i for i, l in enumerate(lines) if l.startswith("std. err."))
+    j = i1 + 1
+    while j < len(lines) and lines[j].strip():
+        j += 1
+    return lines[i0:j]

@@ -133,3 +133,37 @@ def test_convertf_edge_case_is_exercised():
     assert len(flipped) >= 10 and all(o[4] == ids[o[0]][4][1] for o in flipped)
     inds = [l.split()[0] for l in open(os.path.join(d, "out_pk2pk.ind"))]
     assert "S0000011" not in inds and "S0000007" not in inds and len(inds) == 148
+
+
+@pytest.mark.parametrize("par_name,details,tol", [("par", "ref.fstdetails", 1e-12),
+                                                   ("par_pl", "ref_pl.fstdetails", 6e-10)])
+def test_oracle_fst_matches_reference(par_name, details, tol):
+    """Fst tail (fstcolyy + block jackknife) of the oracle on the last pass against the
+    reference's fstdetails file: 24 blocks over two chromosomes, 12 or 6 populations"""
+    from tests.goldens import eglist, read_fstdetails, snp_table
+    c = Case("bn_fst")
+    par = {}
+    for line in open(os.path.join(c.dir, par_name)):
+        k, v = line.split(None, 1)
+        par[k.rstrip(":")] = v.strip()
+    chrom, gpos = snp_table("bn_fst")
+    eg = eglist("bn_fst", par)
+    aff = None
+    if "poplistname" in par:
+        aff = np.array([p in eg for p in c.pops], np.uint8)
+    r = O.smartpca(c.packed_records(), c.nind, numeigs=int(par["numoutevec"]), snp_chrom=chrom,
+                   ind_affstatus=aff)
+    xt = [eg.index(c.pops[k]) if c.pops[k] in eg else -1 for k in r["xindex"]]
+    nb, tag = O.set_blocks(chrom, gpos, r["snp_state"] != 0)
+    assert nb == 24
+    cols = np.nonzero(r["snp_state"] == 0)[0]
+    fmean, fans, fsd, fnum = O.fst(c.packed_records(), c.nind, r["xindex"], xt, len(eg), cols,
+                                   tag, nb)
+    ref = read_fstdetails(os.path.join(c.dir, details))
+    assert len(ref) == len(eg) * (len(eg) - 1) // 2
+    for (p1, p2), (fm, fj, sd, z, n) in ref.items():
+        a, b = eg.index(p1), eg.index(p2)
+        assert abs(fmean[a, b] - fm) <= tol * max(1.0, abs(fm))
+        assert abs(fans[a, b] - fj) <= tol * max(1.0, abs(fj))
+        assert abs(fsd[a, b] - sd) <= tol * max(1.0, abs(sd))
+        assert fnum[a, b] == n

@@ -3,7 +3,8 @@ generator and the C oracle.  Plain nvcc/gcc invocations, compiled in parallel, n
 
 Outputs (git-ignored):
   eig_gb300/_lib/libgpupca.so   C ABI of the hot path (include/gpupca.h, gpupca_run.h)
-  eig_gb300/_lib/libgpsynth.so  seeded Balding-Nichols generator (eig_gb300/host/gp_synth.h)
+  eig_gb300/_lib/libgpsynth.so  host helpers: seeded Balding-Nichols generator (gp_synth.h) and
+                                the ANOVA tail probabilities (gp_stats.h)
   eig_gb300/_lib/gpusmartpca    drop-in CLI: smartpca -p parfile
   eig_gb300/_lib/gpusmartrel    drop-in CLI: smartrel -p parfile
   eig_gb300/_lib/gpuconvertf    drop-in CLI: convertf -p parfile (packed/bed/EIGENSTRAT writers)
@@ -90,12 +91,12 @@ def build(verbose=False, force=False):
         _run([nvcc] + ARCH + ["-shared", "-o", lib] + objs +
              ["-lcusolver", "-lcublas", "-lcudart", "-lpthread"])
     synth = os.path.join(LIB, "libgpsynth.so")
-    ss = os.path.join(HOST, "gp_synth.c")
-    if force or _newer(synth, [ss] + hdrs):
-        _run(["gcc"] + CFLAGS + ["-shared", "-o", synth, ss, "-lm", "-lpthread"])
+    ss = [os.path.join(HOST, "gp_synth.c"), os.path.join(HOST, "gp_stats.c")]
+    if force or _newer(synth, ss + hdrs):
+        _run(["gcc"] + CFLAGS + ["-shared", "-o", synth] + ss + ["-lm", "-lpthread"])
     cli = os.path.join(LIB, "gpusmartpca")
     cli_src = [os.path.join(HOST, "gpusmartpca_main.c"), os.path.join(HOST, "gp_io.c"),
-               os.path.join(HOST, "gp_synth.c")]
+               os.path.join(HOST, "gp_synth.c"), os.path.join(HOST, "gp_stats.c")]
     if all(os.path.exists(s) for s in cli_src) and (force or _newer(cli, cli_src + hdrs + [lib])):
         _run(["gcc"] + CFLAGS + ["-o", cli] + cli_src +
              ["-L" + LIB, "-lgpupca", "-Wl,-rpath,$ORIGIN", "-lm", "-lpthread"])

@@ -22,6 +22,7 @@
 #include "../../include/gpupca.h"
 #include "../../include/gpupca_run.h"
 #include "gp_io.h"
+#include "gp_stats.h"
 
 static void usage(void) { fprintf(stderr, "usage: gpusmartpca -p parfile\n"); }
 
@@ -50,6 +51,178 @@ static void printmatz(const double *w, char **eg, int n, int wide)
 }
 
 static double clipd(double x, double lo, double hi) { return x < lo ? lo : (x > hi ? hi : x); }
+
+/* centred values and population means (calcmean src/qpsubs.c:430-458): w0 = vec - mean,
+ * wmean[k] = sum of w0 over population k / (size + 1e-12); returns the sizes + 1e-12 */
+static void pop_means(const double *vec, int len, const int32_t *xt, int numeg, double *w0,
+                      double *wmean, double *psz)
+{
+  double s = 0.0;
+  for (int i = 0; i < len; ++i) s += vec[i];
+  const double y1 = s / (double)len;
+  for (int i = 0; i < len; ++i) w0[i] = vec[i] + -y1;
+  for (int k = 0; k < numeg; ++k) wmean[k] = psz[k] = 0.0;
+  for (int i = 0; i < len; ++i) {
+    psz[xt[i]] += 1.0;
+    wmean[xt[i]] += w0[i];
+  }
+  for (int k = 0; k < numeg; ++k) {
+    psz[k] = psz[k] + 1.0e-12;
+    wmean[k] = wmean[k] / psz[k];
+  }
+}
+
+/* anova (smartpca.c:2419-2476): F test of the population means, its upper tail */
+static double anova_f(const double *vec, int len, const int32_t *xt, int numeg, double *w0,
+                      double *wm, double *psz)
+{
+  if (numeg >= len) {
+    printf("*** warning: bad anova popsizes too small\n");
+    return 0.0;
+  }
+  pop_means(vec, len, xt, numeg, w0, wm, psz);
+  double top = 0.0, bot = 0.0;
+  for (int k = 0; k < numeg; ++k) top += (wm[k] * wm[k]) * psz[k];
+  for (int i = 0; i < len; ++i) {
+    const double d = w0[i] - wm[xt[i]];
+    bot += d * d;
+  }
+  bot = bot / (double)(len - numeg);
+  bot *= (double)(numeg - 1);
+  return gp_ftail(numeg - 1, len - numeg, top / bot);
+}
+
+/* anova1 (smartpca.c:2479-2515): log likelihood ratio 0.5 n log(var0 / var1) */
+static double anova_ll(const double *vec, int len, const int32_t *xt, int numeg, double *w0,
+                       double *wm, double *psz)
+{
+  pop_means(vec, len, xt, numeg, w0, wm, psz);
+  double y1 = 0.0, y2 = 0.0;
+  for (int i = 0; i < len; ++i) y1 += w0[i] * w0[i];
+  for (int i = 0; i < len; ++i) {
+    const double d = w0[i] - wm[xt[i]];
+    y2 += d * d;
+  }
+  y1 = y1 / (double)len;
+  y2 = y2 / (double)len;
+  return 0.5 * ((double)len) * log(y1 / y2);
+}
+
+/* publishit (smartpca.c:2518-2571) without chisqmode: name with blanks as underscores, the
+ * p-value, *** below 0.001 and +++ below 1e-6 */
+static void publish(const char *sss, double tail, int *ncall)
+{
+  char ss2[512];
+  snprintf(ss2, sizeof ss2, "%s", sss);
+  for (char *q = ss2; *q; ++q)
+    if (*q == ' ') *q = '_';
+  if ((*ncall)++ == 0) {
+    printf("## Anova statistics for population differences along each eigenvector:\n");
+    printf("%40s %12s\n", "", "p-value");
+  }
+  printf("%40s ", ss2);
+  printf(" %12.6g", tail);
+  printf(" %s", tail < 1.0e-6 ? "+++" : (tail < 0.001 ? "***" : ""));
+  printf("\n");
+}
+
+/*
+ * The ANOVA tail of smartpca's log (dottest smartpca.c:2316-2417 per eigenvector, then the
+ * popdifference table :1977-1993): population means of each eigenvector (sorted), the F-test
+ * p-value overall and per population pair, and per pair the chi-square of the summed
+ * likelihood ratios over the eigenvectors with its upper tail.  Eigenvector signs are the
+ * eigensolver's, so the means (and minv/maxv) may come out negated against the reference.
+ */
+static void anova_tail(const gp_run_result *r, char **eg, int numeg, const int32_t *xt,
+                       const int32_t *psize)
+{
+  const int n = r->nrows, K = r->numeigs;
+  double *w0 = (double *)malloc(sizeof(double) * (size_t)(n + numeg + 2));
+  double *wv = (double *)malloc(sizeof(double) * (size_t)(n + 2));
+  int32_t *xt2 = (int32_t *)malloc(sizeof(int32_t) * (size_t)(n + 2));
+  double *wm = (double *)malloc(sizeof(double) * (size_t)numeg), *psz = (double *)malloc(sizeof(double) * (size_t)numeg);
+  double *chitot = (double *)calloc((size_t)numeg * numeg, sizeof(double));
+  int *ord = (int *)malloc(sizeof(int) * (size_t)numeg);
+  int ncall = 0;
+  for (int j = 0; j < K; ++j) {
+    const double *vec = r->evecs + (size_t)j * n;
+    char sss[64];
+    snprintf(sss, sizeof sss, "eigenvector %d", j + 1);
+    pop_means(vec, n, xt, numeg, w0, wm, psz);
+    /* sortit: ascending, ties in index order */
+    for (int k = 0; k < numeg; ++k) ord[k] = k;
+    for (int a = 1; a < numeg; ++a) {
+      const int v = ord[a];
+      int b = a - 1;
+      while (b >= 0 && wm[ord[b]] > wm[v]) {
+        ord[b + 1] = ord[b];
+        --b;
+      }
+      ord[b + 1] = v;
+    }
+    printf("%s:means\n", sss);
+    for (int i = 0; i < numeg; ++i) {
+      printf("%20s ", eg[ord[i]]);
+      printf(" %9.3f\n", wm[ord[i]]);
+    }
+    int imax = 0, imin = 0;
+    for (int k = 1; k < numeg; ++k) {
+      if (wm[k] > wm[imax]) imax = k;
+      if (wm[k] < wm[imin]) imin = k;
+    }
+    const double wmin = wm[imin], wmax = wm[imax];
+    const double ans = anova_f(vec, n, xt, numeg, w0, wm, psz);
+    if (numeg > 2) {
+      char s2[128];
+      snprintf(s2, sizeof s2, "%s %s ", sss, "overall");
+      publish(s2, ans, &ncall);
+      printf(" %20s minv: %9.3f %20s maxv: %9.3f\n", eg[imin], wmin, eg[imax], wmax);
+    }
+    for (int k1 = 0; k1 < numeg; ++k1) {
+      for (int k2 = k1 + 1; k2 < numeg; ++k2) {
+        int m = 0, x1 = 0, x2 = 0;
+        for (int i = 0; i < n; ++i) {
+          if (xt[i] == k1) {
+            wv[m] = vec[i];
+            xt2[m++] = 0;
+            ++x1;
+          }
+          if (xt[i] == k2) {
+            wv[m] = vec[i];
+            xt2[m++] = 1;
+            ++x2;
+          }
+        }
+        if (x1 <= 1 || x2 <= 1) continue;
+        chitot[k1 * numeg + k2] += 2.0 * anova_ll(wv, m, xt2, 2, w0, wm, psz);
+        const double ansx = anova_f(wv, m, xt2, 2, w0, wm, psz);
+        char s2[256];
+        snprintf(s2, sizeof s2, "%s %s %s ", sss, eg[k1], eg[k2]);
+        publish(s2, ansx, &ncall);
+      }
+    }
+  }
+  printf("\n## Statistical significance of differences beween populations:\n");
+  printf("                                pop1                  pop2      chisq          p-value   |pop1|   |pop2|\n");
+  for (int k1 = 0; k1 < numeg; ++k1) {
+    for (int k2 = k1 + 1; k2 < numeg; ++k2) {
+      const double ychi = chitot[k1 * numeg + k2];
+      printf("popdifference:  %20s  %20s  %12.3f  %12.6g", eg[k1], eg[k2], ychi,
+             gp_chitail(K, ychi));
+      printf("   %5d", psize[k1]);
+      printf("   %5d", psize[k2]);
+      printf("\n");
+    }
+  }
+  printf("\n");
+  free(w0);
+  free(wv);
+  free(xt2);
+  free(wm);
+  free(psz);
+  free(chitot);
+  free(ord);
+}
 
 /*
  * The population summary and Fst section of smartpca's log after the PCA
@@ -230,6 +403,7 @@ static int fst_tail(gp_ctx *ctx, const gp_parfile *pf, const gp_snplist *snps,
   for (size_t i = 0; i < EE; ++i) fsd[i] *= 1000.0;
   printmatz(fsd, eg, numeg, 0);
   printf("\n");
+  anova_tail(r, eg, numeg, xt, psize);
   free(fmean);
   free(fans);
   free(fsd);

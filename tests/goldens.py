@@ -227,3 +227,50 @@ def log_section(text):
     while j < len(lines) and lines[j].strip():
         j += 1
     return lines[i0:j]
+
+
+def anova_section(text):
+    """the ANOVA tail of a smartpca log: {"means": {j: [(pop, mean)]}, "p": {name: p},
+    "minmax": {j: (minpop, minv, maxpop, maxv)}, "popdiff": [(p1, p2, chisq, p, n1, n2)]}"""
+    out = {"means": {}, "p": {}, "minmax": {}, "popdiff": []}
+    lines = text.splitlines()
+    j = None
+    mode = None
+    for line in lines:
+        t = line.split()
+        if line.startswith("eigenvector ") and line.endswith(":means"):
+            j = int(t[1].split(":")[0])
+            out["means"][j] = []
+            mode = "means"
+            continue
+        if mode == "means" and len(t) == 2 and not t[0].startswith("eigenvector_"):
+            out["means"][j].append((t[0], float(t[1])))
+            continue
+        mode = None
+        if t and t[0].startswith("eigenvector_") and len(t) >= 2:
+            out["p"][t[0]] = float(t[1])
+        elif len(t) == 6 and t[1] == "minv:" and t[4] == "maxv:":
+            out["minmax"][j] = (t[0], float(t[2]), t[3], float(t[5]))
+        elif t and t[0] == "popdifference:":
+            out["popdiff"].append((t[1], t[2], float(t[3]), float(t[4]), int(t[5]), int(t[6])))
+    return out
+
+
+def compare_anova(mine, ref):
+    """means and min/max up to each eigenvector's sign; p-values and chi-squares numerically"""
+    assert set(mine["means"]) == set(ref["means"]) and mine["means"]
+    for j, want in ref["means"].items():
+        got = mine["means"][j]
+        same = sorted(got) == sorted(want)
+        flip = sorted((p, -m if m != 0 else 0.0) for p, m in got) == \
+            sorted((p, m if m != 0 else 0.0) for p, m in want)
+        assert same or flip, (j, got, want)
+    assert set(mine["p"]) == set(ref["p"])
+    for k, b in ref["p"].items():
+        a = mine["p"][k]
+        assert abs(a - b) <= 2e-5 * abs(b) + 1e-15, (k, a, b)
+    assert len(mine["popdiff"]) == len(ref["popdiff"])
+    for a, b in zip(mine["popdiff"], ref["popdiff"]):
+        assert a[:2] == b[:2] and a[4:] == b[4:]
+        assert abs(a[2] - b[2]) <= 1.5e-3 * max(1.0, abs(b[2]) * 1e-6)
+        assert abs(a[3] - b[3]) <= 2e-5 * abs(b[3]) + 1e-15, (a, b)

@@ -66,3 +66,14 @@ def test_gp_fst_equals_oracle(gpu):
     for (p1, p2), (fm, fj, sd, z, n) in ref.items():
         a, b = eg.index(p1), eg.index(p2)
         assert abs(fans[a, b] - fj) <= 1e-12 and abs(fsd[a, b] - sd) <= 1e-12
+
+
+@pytest.mark.parametrize("case,par_name,ref_log", [(c, "par", "ref.log") for c in CASES] +
+                         [("bn_fst", "par", "ref.log"), ("bn_fst", "par_pl", "ref_par_pl.log")])
+def test_cli_anova_section_matches_reference(case, par_name, ref_log, tmp_path):
+    """per-eigenvector population means (up to the eigenvector's sign), ANOVA p-values and
+    the popdifference chi-squares against the reference's log"""
+    from tests.goldens import anova_section, compare_anova
+    d, stdout = _run_cli(case, par_name, tmp_path)
+    ref = anova_section(open(os.path.join(Case(case).dir, ref_log)).read())
+    compare_anova(anova_section(stdout), ref)

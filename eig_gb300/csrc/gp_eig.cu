@@ -880,6 +880,132 @@ __global__ void k_mgs(double *Z, int n, int nvec)
   }
 }
 
+/*
+ * Back-transformation Z := Q Z of the nvec eigenvectors of T (dormtr, side L, lower, no
+ * transpose), Q = H(0) H(1) ... H(n-2) with H(i) = I - tau_i v_i v_i^T, v_i(i+1) = 1 and
+ * v_i(i+2:n) stored in A(i+2:n, i).  The reflectors are taken WY_B at a time in the compact
+ * WY form H(i0)...H(i0+b-1) = I - V T V^T (T upper triangular, LAPACK dlarft's forward
+ * recurrence T(j,j) = tau_j, T(0:j,j) = -tau_j T(0:j,0:j) V(:,0:j)^T v_j), last block first,
+ * Z := Z - V (T (V^T Z)).  One cooperative launch, one CTA per SM with a fixed slab of rows:
+ * per block of reflectors each CTA forms its rows' share of V^T [V | Z] (partials), a grid
+ * barrier, the partials are summed in fixed order (entries spread over the CTAs), a second
+ * barrier, then every CTA builds T and W = T V^T Z from the sums and updates its own rows.
+ * Float-float arithmetic (about 46 bits) from the FP64 inputs to the FP64 output; bounded grid
+ * barriers report through err.
+ */
+#define WY_B 32
+#define WY_THREADS 256
+__global__ void __launch_bounds__(WY_THREADS, 1)
+k_apply_q(const double *__restrict__ A, int n, const double *__restrict__ tau, double *Z, int nvec,
+          double *part, double *S, unsigned *bar, int *err)
+{
+  /* all products in float-float on the FP32 pipe (GB300's FP64 pipe issues ~2 FMAs per
+   * clock per SM); part and S hold float-float pairs in doubles' storage */
+  extern __shared__ double wsm[];
+  const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x;
+  const int rpb = (n + G - 1) / G;
+  const int R0 = b * rpb < n ? b * rpb : n, R1 = R0 + rpb < n ? R0 + rpb : n;
+  const int ncolS = WY_B + nvec, nent = WY_B * ncolS;
+  ff2 *Vs = reinterpret_cast<ff2 *>(wsm);    /* [rpb][WY_B]  the CTA's rows of V */
+  ff2 *Zs = Vs + (size_t)rpb * WY_B;         /* [rpb][nvec]  its rows of Z */
+  ff2 *Ss = Zs + (size_t)rpb * nvec;         /* [WY_B][ncolS] V^T [V | Z] */
+  ff2 *Tm = Ss + (size_t)nent;               /* [WY_B][WY_B] */
+  ff2 *Wm = Tm + WY_B * WY_B;                /* [WY_B][nvec] */
+  const ff2 ZERO = ff_make(0.f, 0.f);
+  unsigned target = 0;
+  const int nr = R1 - R0;
+  for (int idx = tid; idx < nr * nvec; idx += WY_THREADS) {
+    const int c = idx / nr, r = idx - c * nr;
+    Zs[r * nvec + c] = ff_from_double(Z[(size_t)c * n + R0 + r]);
+  }
+  const int nref = n - 1;
+  const int nblk = (nref + WY_B - 1) / WY_B;
+  for (int blk = nblk - 1; blk >= 0; --blk) {
+    const int i0 = blk * WY_B, nb = nref - i0 < WY_B ? nref - i0 : WY_B;
+    const int r0 = R0 > i0 + 1 ? R0 : i0 + 1;  /* V is zero above row i0+1 */
+    const int m = r0 < R1 ? R1 - r0 : 0;
+    __syncthreads();
+    for (int idx = tid; idx < m * WY_B; idx += WY_THREADS) {
+      const int k = idx / m, rr = r0 + (idx - k * m);
+      const int i = i0 + k;
+      double v = 0.0;
+      if (k < nb) v = rr == i + 1 ? 1.0 : (rr > i + 1 ? A[(size_t)i * n + rr] : 0.0);
+      Vs[(rr - R0) * WY_B + k] = ff_from_double(v);
+    }
+    __syncthreads();
+    /* partial V^T [V | Z] over the CTA's rows (V^T V: upper triangle only) */
+    for (int e = tid; e < nent; e += WY_THREADS) {
+      const int k = e / ncolS, c = e - k * ncolS;
+      ff2 acc = ZERO;
+      if (c < WY_B) {
+        if (c >= k)
+          for (int rr = r0 - R0; rr < R1 - R0; ++rr)
+            acc = ff_fma(Vs[rr * WY_B + k], Vs[rr * WY_B + c], acc);
+      } else {
+        for (int rr = r0 - R0; rr < R1 - R0; ++rr)
+          acc = ff_fma(Vs[rr * WY_B + k], Zs[rr * nvec + (c - WY_B)], acc);
+      }
+      ff_store(part + (size_t)b * nent + e, acc);
+    }
+    target += G;
+    if (!tr_grid_sync(bar, target, err)) return;
+    /* one warp per entry: lanes sum every 32nd partial, then a fixed shuffle tree */
+    {
+      const int lane = tid & 31, gw = b * (WY_THREADS / 32) + (tid >> 5);
+      for (int e = gw; e < nent; e += G * (WY_THREADS / 32)) {
+        ff2 acc = ZERO;
+        for (int g = lane; g < G; g += 32) acc = ff_add(acc, ff_load(part + (size_t)g * nent + e));
+        for (int o = 16; o; o >>= 1) acc = ff_add(acc, ff_shfl_xor(acc, o));
+        if (lane == 0) ff_store(S + e, acc);
+      }
+    }
+    target += G;
+    if (!tr_grid_sync(bar, target, err)) return;
+    if (m == 0) continue;
+    for (int e = tid; e < nent; e += WY_THREADS) Ss[e] = ff_load(S + e);
+    __syncthreads();
+    /* T (dlarft forward, columnwise): one warp, column j after column j-1 */
+    if (tid < 32) {
+      for (int j = 0; j < WY_B; ++j) {
+        const ff2 tj = j < nb ? ff_from_double(tau[i0 + j]) : ZERO;
+        ff2 t = ZERO;
+        if (tid < j) t = ff_neg(ff_mul(tj, Ss[tid * ncolS + j]));
+        /* T(0:j, j) = T(0:j, 0:j) t: row tid of the upper triangle */
+        ff2 acc = ZERO;
+        for (int l = 0; l < j; ++l) {
+          const ff2 tl = ff_make(__shfl_sync(0xFFFFFFFFu, t.h, l), __shfl_sync(0xFFFFFFFFu, t.l, l));
+          if (tid <= l) acc = ff_fma(Tm[tid * WY_B + l], tl, acc);
+        }
+        if (tid < j) Tm[tid * WY_B + j] = acc;
+        if (tid == j) Tm[j * WY_B + j] = tj;
+        if (tid > j) Tm[tid * WY_B + j] = ZERO;
+        __syncwarp();
+      }
+    }
+    __syncthreads();
+    /* W = T (V^T Z) */
+    for (int e = tid; e < WY_B * nvec; e += WY_THREADS) {
+      const int k = e / nvec, c = e - k * nvec;
+      ff2 acc = ZERO;
+      for (int l = k; l < WY_B; ++l) acc = ff_fma(Tm[k * WY_B + l], Ss[l * ncolS + WY_B + c], acc);
+      Wm[e] = acc;
+    }
+    __syncthreads();
+    /* Z(rows) -= V(rows) W */
+    for (int idx = tid; idx < m * nvec; idx += WY_THREADS) {
+      const int rr = (r0 - R0) + idx / nvec, c = idx % nvec;
+      ff2 acc = ZERO;
+      for (int k = 0; k < WY_B; ++k) acc = ff_fma(Vs[rr * WY_B + k], Wm[k * nvec + c], acc);
+      Zs[rr * nvec + c] = ff_add(Zs[rr * nvec + c], ff_neg(acc));
+    }
+  }
+  __syncthreads();
+  for (int idx = tid; idx < nr * nvec; idx += WY_THREADS) {
+    const int c = idx / nr, r = idx - c * nr;
+    Z[(size_t)c * n + R0 + r] = ff_to_double(Zs[r * nvec + c]);
+  }
+}
+
 /* evals_desc[i] = w[n-1-i] */
 __global__ void k_reverse(const double *w, double *out, int n)
 {
@@ -898,9 +1024,9 @@ int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, d
   /* GP_EIG_TIMING=1 prints the device time of each stage to stderr */
   const char *tenv = getenv("GP_EIG_TIMING");
   const int timing = tenv && tenv[0] == '1';
-  cudaEvent_t ev[5];
+  cudaEvent_t ev[7];
   if (timing)
-    for (int i = 0; i < 5; ++i) cudaEventCreate(&ev[i]);
+    for (int i = 0; i < 7; ++i) cudaEventCreate(&ev[i]);
 #define GP_EIG_MARK(i) \
   if (timing) cudaEventRecord(ev[i], ctx->stream)
   /* scratch: d, e, tau, e2, w, work(sytrd), inverse-iteration work, info */
@@ -914,7 +1040,8 @@ int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, d
   int lw = lwork > lwork2 ? lwork : lwork2;
   size_t nd = (size_t)n;
   const size_t G = (size_t)ctx->num_sms;
-  size_t bytes = sizeof(double) * (9 * nd + 2 * G + (size_t)lw + 6 * nd * nv + 80) +
+  const size_t qpart_n = (G + 1) * (size_t)WY_B * (WY_B + nv); /* partials + sums of k_apply_q */
+  size_t bytes = sizeof(double) * (9 * nd + 2 * G + (size_t)lw + 6 * nd * nv + 80 + qpart_n) +
                  sizeof(int) * 64;
   double *base;
   int rc = gp_scratch(ctx, bytes, (void **)&base);
@@ -924,6 +1051,7 @@ int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, d
   unsigned *bar = (unsigned *)(parts + 2 * G);
   double *ws = parts + 2 * G + 16, *iw = ws + lw; /* 16 doubles: barrier words + phase timers */
   int *d_info = (int *)(iw + 6 * nd * nv + 8);
+  double *qpart = iw + 6 * nd * nv + 16; /* after d_info's 8 doubles (64 ints) */
   /* the cooperative tridiagonalisation (k_tridiag) unless GP_EIG_CUSOLVER_SYTRD=1, the
    * vectors do not fit shared memory or the device cannot co-schedule one block per SM */
   const char *senv = getenv("GP_EIG_CUSOLVER_SYTRD");
@@ -1032,25 +1160,66 @@ int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, d
   if (nvec > 0) {
     k_inverse_iteration<<<nvec, 256, 0, ctx->stream>>>(d, e, n, w, nvec, tnorm, d_vecs, iw);
     GP_LAUNCH_CHECK(ctx, "k_inverse_iteration");
+    GP_EIG_MARK(5);
     k_mgs<<<1, 256, 0, ctx->stream>>>(d_vecs, n, nvec);
     GP_LAUNCH_CHECK(ctx, "k_mgs");
-    if (cusolverDnDormtr(h, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, n, nvec,
-                         ctx->d_xtx, n, tau, d_vecs, n, ws, lw, d_info) != CUSOLVER_STATUS_SUCCESS)
-      return gp_fail(ctx, GP_ERR_SOLVER, "cusolverDnDormtr failed to launch");
-    GP_CUDA(ctx, gp_memcpy(ctx, &info, d_info, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-    GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    if (info != 0) return gp_fail(ctx, GP_ERR_SOLVER, "ormtr info = %d", info);
+    GP_EIG_MARK(6);
+    /* Z := Q Z: the cooperative WY kernel when its row slab fits shared memory, else
+     * cusolverDnDormtr (GP_EIG_CUSOLVER_ORMTR=1 forces the latter) */
+    const char *oenv = getenv("GP_EIG_CUSOLVER_ORMTR");
+    const int Gq = ctx->num_sms;
+    const size_t rpb = ((size_t)n + Gq - 1) / Gq;
+    const size_t nent = (size_t)WY_B * (WY_B + nvec);
+    const size_t q_smem = sizeof(double) * (rpb * (WY_B + nvec) + nent + WY_B * WY_B + (size_t)WY_B * nvec);
+    int qcoop = !(oenv && oenv[0] == '1') && n >= 2 && q_smem <= 200 * 1024 &&
+                qpart != NULL;
+    if (qcoop) {
+      int dev_coop = 0, per_sm = 0;
+      cudaDeviceGetAttribute(&dev_coop, cudaDevAttrCooperativeLaunch, ctx->device);
+      GP_CUDA(ctx, cudaFuncSetAttribute(k_apply_q, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)q_smem));
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_apply_q, WY_THREADS, q_smem);
+      qcoop = dev_coop && per_sm >= 1;
+    }
+    if (qcoop) {
+      unsigned *qbar = bar + 4;
+      int *d_err = ctx->d_err;
+      GP_CUDA(ctx, cudaMemsetAsync(d_err, 0, sizeof(int), ctx->stream));
+      GP_CUDA(ctx, cudaMemsetAsync(qbar, 0, sizeof(unsigned), ctx->stream));
+      const double *Aq = ctx->d_xtx;
+      double *Sq = qpart + (size_t)Gq * nent;
+      int nn = n, nv2 = nvec;
+      void *qargs[] = {(void *)&Aq, &nn, &tau, &d_vecs, &nv2, &qpart, &Sq, &qbar, &d_err};
+      GP_CUDA(ctx, cudaLaunchCooperativeKernel((const void *)k_apply_q, dim3((unsigned)Gq),
+                                               dim3(WY_THREADS), qargs, q_smem, ctx->stream));
+      ctx->launches++;
+      int herr = 0;
+      GP_CUDA(ctx, gp_memcpy(ctx, &herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+      GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+      if (herr) return gp_fail(ctx, GP_ERR_TIMEOUT, "back-transformation grid barrier timed out");
+    } else {
+      if (cusolverDnDormtr(h, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, n, nvec,
+                           ctx->d_xtx, n, tau, d_vecs, n, ws, lw, d_info) != CUSOLVER_STATUS_SUCCESS)
+        return gp_fail(ctx, GP_ERR_SOLVER, "cusolverDnDormtr failed to launch");
+      GP_CUDA(ctx, gp_memcpy(ctx, &info, d_info, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+      GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+      if (info != 0) return gp_fail(ctx, GP_ERR_SOLVER, "ormtr info = %d", info);
+    }
   }
   if (timing) {
     GP_EIG_MARK(4);
     cudaEventSynchronize(ev[4]);
-    float t01 = 0, t23 = 0, t34 = 0;
+    float t01 = 0, t23 = 0, t34 = 0, t35 = 0, t56 = 0;
     cudaEventElapsedTime(&t01, ev[0], ev[1]);
     cudaEventElapsedTime(&t23, ev[2], ev[3]);
     cudaEventElapsedTime(&t34, ev[3], ev[4]);
-    fprintf(stderr, "eig n=%d: sytrd %.1f ms, eigenvalues %.1f ms, vectors+ormtr %.1f ms\n", n,
-            t01, t23, t34);
-    for (int i = 0; i < 5; ++i) cudaEventDestroy(ev[i]);
+    if (nvec > 0) {
+      cudaEventElapsedTime(&t35, ev[3], ev[5]);
+      cudaEventElapsedTime(&t56, ev[5], ev[6]);
+    }
+    fprintf(stderr, "eig n=%d: sytrd %.1f ms, eigenvalues %.1f ms, vectors+ormtr %.1f ms "
+            "(inverse iteration %.1f, mgs %.1f)\n", n, t01, t23, t34, t35, t56);
+    for (int i = 0; i < 7; ++i) cudaEventDestroy(ev[i]);
   }
   return GP_OK;
 }

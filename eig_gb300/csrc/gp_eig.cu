@@ -217,7 +217,7 @@ k_multisect(const double *gd, const double *ge2, int n, double gl, double gu, do
  * dormtr (lower) reads them.  Shared memory: v(step c-1), w(step c-1), v(step c) over the
  * rows (24 n bytes).
  */
-#define TR_THREADS 512
+#define TR_THREADS 1024
 #define TR_WARPS (TR_THREADS / 32)
 #define TR_U 8 /* loads in flight per lane in the product loops */
 #define TR_B1_SLOTS 256 /* segment dots of one block in the column pass */

@@ -106,6 +106,17 @@ k_geno_panel_tc(const __grid_constant__ CUtensorMap tm_b, const uint8_t *__restr
     *abort_flag = 0;
     fence_mbar_init();
   }
+  /* byte -> four fp16 decode tables (one per 4-entry table): entry b holds the values of
+   * the codes b>>6, (b>>4)&3, (b>>2)&3, b&3 in that order */
+  __shared__ uint2 s_lut[2][256];
+  for (int idx = threadIdx.x; idx < 512; idx += blockDim.x) {
+    const uint64_t lt = (idx >> 8) ? lut_hi : lut_lo;
+    const uint32_t bb = (uint32_t)idx & 255u;
+    uint32_t hv[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) hv[u] = (uint32_t)(lt >> (16 * ((bb >> (6 - 2 * u)) & 3u))) & 0xFFFFu;
+    s_lut[idx >> 8][bb] = make_uint2(hv[0] | (hv[1] << 16), hv[2] | (hv[3] << 16));
+  }
   if (warp == 0 && lane == 0) tma_prefetch_desc(&tm_b);
   if (warp == 1) tmem_alloc(tmem_slot, 256);
   tc_fence_before();
@@ -197,26 +208,18 @@ k_geno_panel_tc(const __grid_constant__ CUtensorMap tm_b, const uint8_t *__restr
           ok = false;
           break;
         }
-        const uint64_t lut = kb < kb_switch ? lut_lo : lut_hi;
+        const uint2 *lut = s_lut[kb < kb_switch ? 0 : 1];
         uint4 raw = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
         if (grow < nrows) raw = __ldg((const uint4 *)(crow + (int64_t)(kb % kb_period) * 16));
         uint8_t *row_base = smem + s * XSTAGE_BYTES + r * 128;
         const uint32_t words[4] = {raw.x, raw.y, raw.z, raw.w};
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
-          /* codes 8j..8j+7: bytes 2j, 2j+1 of the 16 (little-endian words) */
-          uint32_t wv = words[j >> 1] >> ((j & 1) * 16);
-          uint32_t h[4];
-#pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            uint32_t b0 = (wv >> ((u >> 1) * 8)) & 0xFFu; /* byte holding codes 2u, 2u+1 */
-            uint32_t c0 = (b0 >> ((3 - ((2 * u) & 3)) * 2)) & 3u;
-            uint32_t c1 = (b0 >> ((3 - ((2 * u + 1) & 3)) * 2)) & 3u;
-            uint32_t v0 = (uint32_t)(lut >> (16 * c0)) & 0xFFFFu;
-            uint32_t v1 = (uint32_t)(lut >> (16 * c1)) & 0xFFFFu;
-            h[u] = v0 | (v1 << 16);
-          }
-          *(uint4 *)(row_base + ((j ^ (r & 7)) * 16)) = make_uint4(h[0], h[1], h[2], h[3]);
+          /* codes 8j..8j+7: bytes 2j, 2j+1 of the 16 (little-endian words), four codes per
+           * table entry */
+          const uint32_t wv = words[j >> 1] >> ((j & 1) * 16);
+          const uint2 lo = lut[wv & 0xFFu], hi = lut[(wv >> 8) & 0xFFu];
+          *(uint4 *)(row_base + ((j ^ (r & 7)) * 16)) = make_uint4(lo.x, lo.y, hi.x, hi.y);
         }
         fence_proxy_async_smem();
         mbar_arrive(&full[s]);

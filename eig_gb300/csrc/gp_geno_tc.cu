@@ -201,7 +201,21 @@ k_geno_panel_tc(const __grid_constant__ CUtensorMap tm_b, const uint8_t *__restr
       const int32_t grow = rt * XT + r;
       const int64_t crow_idx = grow < nrows ? (row_map ? (int64_t)row_map[grow] : (int64_t)grow) : 0;
       const uint8_t *crow = codes + crow_idx * ldc;
+      /* the row's codes of the next four k-blocks are loaded ahead of the stage waits (the
+       * k-block index wraps at kb_period, so loads past kb1 stay inside the row) */
+      const bool live = grow < nrows;
+      auto ld_codes = [&](int32_t kbx) {
+        return live ? __ldg((const uint4 *)(crow + (int64_t)(kbx % kb_period) * 16))
+                    : make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
+      };
+      uint4 pf0 = ld_codes(kb0), pf1 = ld_codes(kb0 + 1), pf2 = ld_codes(kb0 + 2),
+            pf3 = ld_codes(kb0 + 3);
       for (int32_t kb = kb0; kb < kb1; ++kb, ++it) {
+        const uint4 raw = pf0;
+        pf0 = pf1;
+        pf1 = pf2;
+        pf2 = pf3;
+        pf3 = ld_codes(kb + 4);
         uint32_t s = it % XSTAGES, ph = (it / XSTAGES) & 1u;
         bool got = mbar_wait(&empty[s], ph ^ 1u, abort_flag, err, XERR_EMPTY);
         if (!got) {
@@ -209,8 +223,6 @@ k_geno_panel_tc(const __grid_constant__ CUtensorMap tm_b, const uint8_t *__restr
           break;
         }
         const uint2 *lut = s_lut[kb < kb_switch ? 0 : 1];
-        uint4 raw = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
-        if (grow < nrows) raw = __ldg((const uint4 *)(crow + (int64_t)(kb % kb_period) * 16));
         uint8_t *row_base = smem + s * XSTAGE_BYTES + r * 128;
         const uint32_t words[4] = {raw.x, raw.y, raw.z, raw.w};
 #pragma unroll

@@ -686,15 +686,18 @@ __device__ double block_sum(double v, double *red)
  * work: per vector 6n doubles.  Z [nvec][n] (column-major N x nvec for ormtr).
  */
 __global__ void k_inverse_iteration(const double *d, const double *e, int n, const double *w,
-                                    int nvec, double tnorm, double *Z, double *work)
+                                    int nvec, double tnorm, double *Z, double *work, int in_smem)
 {
   __shared__ double red[256];
+  extern __shared__ double ii_sm[];
   const int j = blockIdx.x;
   if (j >= nvec) return;
-  double *base = work + (int64_t)j * 6 * n;
+  /* the factors in shared memory when they fit (in_smem), so that the sequential recurrences
+   * of thread 0 wait on shared-memory rather than L2 latency */
+  double *base = in_smem ? ii_sm : work + (int64_t)j * 6 * n;
   double *Dinv = base, *DL = base + n, *DU = base + 2 * n, *DU2 = base + 3 * n;
   double *x = Z + (int64_t)j * n;
-  int *piv = (int *)(base + 5 * n);
+  int *piv = (int *)(base + 4 * n);
   const double lam = w[n - 1 - j];
   const double tiny = DBL_EPSILON * tnorm;
   if (threadIdx.x == 0) {
@@ -1072,7 +1075,13 @@ int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, d
   GP_LAUNCH_CHECK(ctx, "k_reverse");
   GP_EIG_MARK(3);
   if (nvec > 0) {
-    k_inverse_iteration<<<nvec, 256, 0, ctx->stream>>>(d, e, n, w, nvec, tnorm, d_vecs, iw);
+    const size_t ii_smem = (size_t)n * (4 * sizeof(double) + sizeof(int)) + 16;
+    const int ii_in_smem = ii_smem <= 200 * 1024;
+    if (ii_in_smem)
+      GP_CUDA(ctx, cudaFuncSetAttribute(k_inverse_iteration,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ii_smem));
+    k_inverse_iteration<<<nvec, 256, ii_in_smem ? ii_smem : 0, ctx->stream>>>(
+        d, e, n, w, nvec, tnorm, d_vecs, iw, ii_in_smem);
     GP_LAUNCH_CHECK(ctx, "k_inverse_iteration");
     GP_EIG_MARK(5);
     k_mgs<<<1, 256, 0, ctx->stream>>>(d_vecs, n, nvec);

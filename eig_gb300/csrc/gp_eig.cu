@@ -14,7 +14,8 @@
  *      interchanges) and three solves from a fixed pseudo-random start, then modified
  *      Gram-Schmidt over the vectors in order (eigenvalues that are distinct to far more than
  *      eps*||T|| make each iterate converge to its own eigenvector);
- *   4. back-transformation of those nvec vectors only, V = Q Z (cuSOLVER ormtr).
+ *   4. back-transformation of those nvec vectors only, V = Q Z (k_apply_q: compact WY blocks
+ *      of 32 reflectors in float-float; cuSOLVER ormtr when its row slab does not fit).
  */
 #include <cuda_runtime.h>
 #include <cusolverDn.h>
@@ -683,7 +684,7 @@ __device__ double block_sum(double v, double *red)
  * The LU factorisation with partial pivoting of T - lam I and the solves are sequential
  * recurrences run by thread 0 with the running values carried in registers (the arrays are
  * only written, or read ahead of the dependency chain); the other threads normalise.
- * work: per vector 6n doubles.  Z [nvec][n] (column-major N x nvec for ormtr).
+ * work: per vector 6n doubles.  Z [nvec][n] (column-major N x nvec).
  */
 __global__ void k_inverse_iteration(const double *d, const double *e, int n, const double *w,
                                     int nvec, double tnorm, double *Z, double *work, int in_smem)
@@ -1140,7 +1141,7 @@ int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, d
       cudaEventElapsedTime(&t35, ev[3], ev[5]);
       cudaEventElapsedTime(&t56, ev[5], ev[6]);
     }
-    fprintf(stderr, "eig n=%d: sytrd %.1f ms, eigenvalues %.1f ms, vectors+ormtr %.1f ms "
+    fprintf(stderr, "eig n=%d: tridiagonal %.1f ms, eigenvalues %.1f ms, vectors %.1f ms "
             "(inverse iteration %.1f, mgs %.1f)\n", n, t01, t23, t34, t35, t56);
     for (int i = 0; i < 7; ++i) cudaEventDestroy(ev[i]);
   }

@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
+#include <stdlib.h>
 
 #include <vector>
 
@@ -116,7 +117,14 @@ extern "C" int gp_fst(gp_ctx *ctx, const int32_t *xtypes, int32_t numeg, const i
   const int64_t words = ctx->rlen_dev / 4;
   const size_t mask_bytes = sizeof(uint32_t) * (size_t)words * (size_t)E;
   const size_t xt_bytes = (sizeof(int32_t) * (size_t)n + 255) & ~(size_t)255;
-  const size_t cnt_bytes = sizeof(int32_t) * 2 * (size_t)E * (size_t)nc;
+  /* columns in chunks so that the counts of a chunk stay within 64 MB whatever numeg is
+   * (GP_FST_CHUNK_COLS sets a smaller chunk) */
+  int64_t chunk = ((int64_t)64 << 20) / ((int64_t)8 * E);
+  const char *cenv = getenv("GP_FST_CHUNK_COLS");
+  if (cenv && atoll(cenv) > 0 && atoll(cenv) < chunk) chunk = atoll(cenv);
+  if (chunk < 1) chunk = 1;
+  if (chunk > nc) chunk = nc > 0 ? nc : 1;
+  const size_t cnt_bytes = sizeof(int32_t) * 2 * (size_t)E * (size_t)chunk;
   uint8_t *base;
   int rc = gp_scratch(ctx, ((mask_bytes + 255) & ~(size_t)255) + xt_bytes + cnt_bytes + 256,
                       (void **)&base);
@@ -134,17 +142,8 @@ extern "C" int gp_fst(gp_ctx *ctx, const int32_t *xtypes, int32_t numeg, const i
                                                                   n, E);
     GP_LAUNCH_CHECK(ctx, "k_pop_masks");
   }
-  {
-    int64_t blocks = ((int64_t)nc * 32 + 255) / 256;
-    if (blocks > (int64_t)ctx->num_sms * 16) blocks = (int64_t)ctx->num_sms * 16;
-    if (blocks < 1) blocks = 1;
-    k_pop_counts<<<(unsigned)blocks, 256, 0, ctx->stream>>>(ctx->d_geno, ctx->rlen_dev, d_masks,
-                                                            ctx->d_cols, nc, E, d_cnt);
-    GP_LAUNCH_CHECK(ctx, "k_pop_counts");
-  }
-  std::vector<int32_t> cnt((size_t)2 * E * nc), cols((size_t)nc);
+  std::vector<int32_t> cnt((size_t)2 * E * (size_t)chunk), cols((size_t)nc);
   std::vector<uint8_t> killed((size_t)nc);
-  GP_CUDA(ctx, gp_memcpy(ctx, cnt.data(), d_cnt, cnt_bytes, cudaMemcpyDeviceToHost, ctx->stream));
   GP_CUDA(ctx, gp_memcpy(ctx, cols.data(), ctx->d_cols, sizeof(int32_t) * (size_t)nc,
                          cudaMemcpyDeviceToHost, ctx->stream));
   GP_CUDA(ctx, gp_memcpy(ctx, killed.data(), ctx->d_killed, (size_t)nc, cudaMemcpyDeviceToHost,
@@ -156,37 +155,49 @@ extern "C" int gp_fst(gp_ctx *ctx, const int32_t *xtypes, int32_t numeg, const i
   std::vector<double> btop((size_t)nblocks * EE, 0.0), bbot((size_t)nblocks * EE, 0.0);
   std::vector<double> wj((size_t)nblocks, 0.0);
   std::vector<int32_t> num(EE, 0);
-  for (int32_t c = 0; c < nc; ++c) {
-    if (killed[(size_t)c]) continue;
-    const int32_t bnum = snp_block[cols[(size_t)c]];
-    if (bnum < 0) continue;
-    if (bnum >= nblocks) return gp_fail(ctx, GP_ERR_ARG, "gp_fst: block %d >= %d", bnum, nblocks);
-    wj[(size_t)bnum] += 1.0;
-    double *top = &btop[(size_t)bnum * EE], *bot = &bbot[(size_t)bnum * EE];
-    const int32_t *cc = &cnt[(size_t)c * E * 2];
-    for (int32_t a = 0; a < E; ++a) {
-      for (int32_t b = a + 1; b < E; ++b) {
-        /* fstcolyy (:1301-1337) */
-        const double ya = cc[2 * a], yb = cc[2 * a + 1], yaa = cc[2 * b], ybb = cc[2 * b + 1];
-        const double zz = yaa + ybb, z = ya + yb;
-        if ((z < 1.5) || (zz < 1.5)) continue;
-        double yt = ya + yb;
-        const double p1 = ya / yt;
-        const double h1 = ya * yb / (yt * (yt - 1.0));
-        yt = yaa + ybb;
-        const double p2 = yaa / yt;
-        const double h2 = yaa * ybb / (yt * (yt - 1.0));
-        double en = (p1 - p2) * (p1 - p2);
-        en -= h1 / z;
-        en -= h2 / zz;
-        double ed = en;
-        ed += h1;
-        ed += h2;
-        if (ed < 0.0) continue;
-        const size_t k = (size_t)a * E + b;
-        ++num[k];
-        top[k] += en;
-        bot[k] += ed;
+  for (int32_t c0 = 0; c0 < nc; c0 += (int32_t)chunk) {
+    const int32_t ncc = nc - c0 < chunk ? nc - c0 : (int32_t)chunk;
+    int64_t blocks = ((int64_t)ncc * 32 + 255) / 256;
+    if (blocks > (int64_t)ctx->num_sms * 16) blocks = (int64_t)ctx->num_sms * 16;
+    if (blocks < 1) blocks = 1;
+    k_pop_counts<<<(unsigned)blocks, 256, 0, ctx->stream>>>(ctx->d_geno, ctx->rlen_dev, d_masks,
+                                                            ctx->d_cols + c0, ncc, E, d_cnt);
+    GP_LAUNCH_CHECK(ctx, "k_pop_counts");
+    GP_CUDA(ctx, gp_memcpy(ctx, cnt.data(), d_cnt, sizeof(int32_t) * 2 * (size_t)E * ncc,
+                           cudaMemcpyDeviceToHost, ctx->stream));
+    GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int32_t c = c0; c < c0 + ncc; ++c) {
+      if (killed[(size_t)c]) continue;
+      const int32_t bnum = snp_block[cols[(size_t)c]];
+      if (bnum < 0) continue;
+      if (bnum >= nblocks) return gp_fail(ctx, GP_ERR_ARG, "gp_fst: block %d >= %d", bnum, nblocks);
+      wj[(size_t)bnum] += 1.0;
+      double *top = &btop[(size_t)bnum * EE], *bot = &bbot[(size_t)bnum * EE];
+      const int32_t *cc = &cnt[(size_t)(c - c0) * E * 2];
+      for (int32_t a = 0; a < E; ++a) {
+        for (int32_t b = a + 1; b < E; ++b) {
+          /* fstcolyy (:1301-1337) */
+          const double ya = cc[2 * a], yb = cc[2 * a + 1], yaa = cc[2 * b], ybb = cc[2 * b + 1];
+          const double zz = yaa + ybb, z = ya + yb;
+          if ((z < 1.5) || (zz < 1.5)) continue;
+          double yt = ya + yb;
+          const double p1 = ya / yt;
+          const double h1 = ya * yb / (yt * (yt - 1.0));
+          yt = yaa + ybb;
+          const double p2 = yaa / yt;
+          const double h2 = yaa * ybb / (yt * (yt - 1.0));
+          double en = (p1 - p2) * (p1 - p2);
+          en -= h1 / z;
+          en -= h2 / zz;
+          double ed = en;
+          ed += h1;
+          ed += h2;
+          if (ed < 0.0) continue;
+          const size_t k = (size_t)a * E + b;
+          ++num[k];
+          top[k] += en;
+          bot[k] += ed;
+        }
       }
     }
   }

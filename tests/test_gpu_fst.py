@@ -77,3 +77,19 @@ def test_cli_anova_section_matches_reference(case, par_name, ref_log, tmp_path):
     d, stdout = _run_cli(case, par_name, tmp_path)
     ref = anova_section(open(os.path.join(Case(case).dir, ref_log)).read())
     compare_anova(anova_section(stdout), ref)
+
+
+def test_gp_fst_column_chunks_give_the_same_result(gpu, monkeypatch):
+    """the counts taken in chunks of 999 columns give the one-chunk result bit for bit"""
+    c = Case("bn_fst")
+    chrom, gpos = snp_table("bn_fst")
+    eg = eglist("bn_fst")
+    r = native.smartpca_run(gpu, c.records, c.nind, native.default_opts(numeigs=4), code=c.code,
+                            snp_chrom=chrom)
+    xt = np.array([eg.index(c.pops[k]) for k in r["xindex"]], np.int32)
+    nb, tag = native.set_blocks(chrom, gpos, r["snp_state"] != 0)
+    whole = gpu.fst(xt, len(eg), tag, nb)
+    monkeypatch.setenv("GP_FST_CHUNK_COLS", "999")
+    parts = gpu.fst(xt, len(eg), tag, nb)
+    for a, b in zip(whole, parts):
+        assert np.array_equal(a, b)

@@ -27,7 +27,12 @@
  *               release it and add it into registers; every GP_FOLD chunks fold those into
  *               the (hi, lo) running sums in TMEM columns 256-511; after the last chunk of a
  *               tile write the tile to the Gram in FP64.
- * Tiles are the 128x128 blocks of the lower triangle, distributed round-robin over CTAs.
+ * Tiles are the 128x128 blocks of the lower triangle, distributed round-robin over CTAs, or
+ * over clusters: four CTAs on a 2 x 2 block of tiles (each loads one box of its tile row and
+ * one of its tile column and multicasts it to the two CTAs that share it: half the boxes of
+ * the one-CTA kernel) or two CTAs on two tiles of a row (the row's boxes multicast: three
+ * quarters).  A stage is then released when every CTA of the cluster has read it
+ * (tcgen05.commit multicast to each CTA's empty barrier).
  */
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -78,6 +83,33 @@ __device__ __forceinline__ int32_t tri_root(int32_t t)
  * instead of being read from HBM once per tile.
  */
 #define GRAM_GROUP 12
+/* element t of the lower triangle of an nt x nt grid walked in gs x gs groups */
+__device__ __forceinline__ void tri_tile_group(int32_t t, int32_t nt, int32_t gs, int32_t *bi,
+                                               int32_t *bj)
+{
+  const int32_t ng = (nt + gs - 1) / gs;
+  for (int32_t gi = 0; gi < ng; ++gi) {
+    const int32_t r0 = gi * gs, nr = min(nt, r0 + gs) - r0;
+    for (int32_t gj = 0; gj <= gi; ++gj) {
+      const int32_t c0 = gj * gs, nc = min(nt, c0 + gs) - c0;
+      const int32_t cnt = gi == gj ? nr * (nr + 1) / 2 : nr * nc;
+      if (t < cnt) {
+        if (gi == gj) {
+          const int32_t i = tri_root(t);
+          *bi = r0 + i;
+          *bj = c0 + t - i * (i + 1) / 2;
+        } else {
+          *bi = r0 + t / nc;
+          *bj = c0 + t % nc;
+        }
+        return;
+      }
+      t -= cnt;
+    }
+  }
+  *bi = *bj = 0; /* not reached for t < nt (nt + 1) / 2 */
+}
+
 __device__ __forceinline__ void tri_tile(int32_t t, int32_t nt, int32_t *bi, int32_t *bj)
 {
   const int32_t ng = (nt + GRAM_GROUP - 1) / GRAM_GROUP;
@@ -104,16 +136,95 @@ __device__ __forceinline__ void tri_tile(int32_t t, int32_t nt, int32_t *bi, int
 }
 
 /*
+ * Pair p of tiles for a cluster of two CTAs: the tiles of one tile row are taken two at a time
+ * (columns 2q, 2q+1 of the row inside its group block), so the pair shares the row block bi
+ * (the A operand).  bj1 = -1 when the row has an odd count and p is its last pair.
+ */
+__device__ __forceinline__ void tri_pair(int32_t p, int32_t nt, int32_t *bi, int32_t *bj0,
+                                         int32_t *bj1)
+{
+  const int32_t ng = (nt + GRAM_GROUP - 1) / GRAM_GROUP;
+  for (int32_t gi = 0; gi < ng; ++gi) {
+    const int32_t r0 = gi * GRAM_GROUP, nr = min(nt, r0 + GRAM_GROUP) - r0;
+    for (int32_t gj = 0; gj <= gi; ++gj) {
+      const int32_t c0 = gj * GRAM_GROUP, nc = min(nt, c0 + GRAM_GROUP) - c0;
+      for (int32_t lr = 0; lr < nr; ++lr) {
+        const int32_t len = gi == gj ? lr + 1 : nc;
+        const int32_t np = (len + 1) / 2;
+        if (p < np) {
+          *bi = r0 + lr;
+          *bj0 = c0 + 2 * p;
+          *bj1 = 2 * p + 1 < len ? c0 + 2 * p + 1 : -1;
+          return;
+        }
+        p -= np;
+      }
+    }
+  }
+  *bi = *bj0 = 0; /* not reached for p < npairs */
+  *bj1 = -1;
+}
+
+/*
+ * Quad w: a 2 x 2 block of tiles (tile rows 2I, 2I+1, tile columns 2J, 2J+1, J <= I) for a
+ * cluster of four CTAs, quads in GRAM_GROUP/2-square groups (lower triangle of groups, row by
+ * row inside a group) like the tiles of tri_tile.
+ */
+__device__ __forceinline__ void tri_quad(int32_t w, int32_t nq, int32_t *qi, int32_t *qj)
+{
+  tri_tile_group(w, nq, GRAM_GROUP / 2, qi, qj);
+}
+
+/*
+ * The tile of work item w for this CTA (cluster rank `rank`): CL = 1 a tile; CL = 2 the
+ * rank's tile of pair w (the second CTA of an odd pair computes the first tile again); CL = 4
+ * tile (2I + rank/2, 2J + rank%2) of quad w.  *write is false for a stand-in tile (a second
+ * tile the pair does not have, or a quad position outside the lower triangle or the matrix);
+ * *arow / *bcol are the tile row and column whose boxes the CTA loads (in the matrix always).
+ */
+template <int CL>
+__device__ __forceinline__ void gram_work(int32_t w, int32_t nt, uint32_t rank, int32_t *bi,
+                                          int32_t *bj, bool *write)
+{
+  if (CL == 1) {
+    tri_tile(w, nt, bi, bj);
+    *write = true;
+  } else if (CL == 2) {
+    int32_t j0, j1;
+    tri_pair(w, nt, bi, &j0, &j1);
+    *bj = (rank == 0 || j1 < 0) ? j0 : j1;
+    *write = rank == 0 || j1 >= 0;
+  } else {
+    int32_t qi, qj;
+    tri_quad(w, (nt + 1) / 2, &qi, &qj);
+    const int32_t ti = 2 * qi + (int32_t)(rank >> 1), tj = 2 * qj + (int32_t)(rank & 1);
+    *write = ti < nt && tj < nt && tj <= ti;
+    *bi = ti < nt ? ti : 2 * qi;
+    *bj = tj < nt ? tj : 2 * qj;
+  }
+}
+
+/*
  * grams: XTX (n x n row-major FP64); accumulate != 0 adds to the values already there
  * (super-chunks after the first).  nkb = k-blocks of this super-chunk; chunk_kb = k-blocks
  * per FP32 accumulation chunk.
  */
-template <int FP16, int NMMA>
+template <int FP16, int NMMA, int CL>
 __global__ void __launch_bounds__(GRAM_THREADS, 1)
 k_gram_split(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ CUtensorMap tm_lo,
-                  int32_t ntiles, int32_t nkb, int32_t chunk_kb, double *xtx, int32_t n,
-                  int32_t accumulate, unsigned *sync_ctr, int *err)
+                  int32_t nwork, int32_t nt_rows, int32_t nkb, int32_t chunk_kb, double *xtx,
+                  int32_t n, int32_t accumulate, unsigned *sync_ctr, int *err)
 {
+  /* CL = 2: clusters of two CTAs computing two tiles of one tile row; the row block's boxes
+   * (A hi and lo) are multicast to both, one box by each CTA.  CL = 4: clusters of four CTAs
+   * computing a 2 x 2 block of tiles; each CTA loads one of the two boxes of its tile row
+   * (multicast to the row's two CTAs) and one of the two boxes of its tile column
+   * (multicast to the column's two CTAs).  A stage is released when every CTA's MMAs of the
+   * cluster have read it. */
+  const uint32_t rank = CL > 1 ? cluster_ctarank() : 0u;
+  const int32_t w0 = CL > 1 ? (int32_t)cluster_id_x() : (int32_t)blockIdx.x;
+  const int32_t wstride = CL > 1 ? (int32_t)cluster_count_x() : (int32_t)gridDim.x;
+  const uint16_t all_mask = (uint16_t)((1u << CL) - 1u);
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t *bars = (uint64_t *)(smem + NSTAGE * STAGE_BYTES);
@@ -124,13 +235,12 @@ k_gram_split(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ 
   uint64_t *drain = bars + 2 * NSTAGE + 4; /* abort path: wait for issued MMAs */
   uint32_t *tmem_slot = (uint32_t *)(bars + 2 * NSTAGE + 5);
   volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
-  const int32_t nt_rows = tri_root(ntiles - 1) + 1; /* tile rows of the lower triangle */
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
     for (int s = 0; s < NSTAGE; ++s) {
       mbar_init(&full[s], 1);
-      mbar_init(&empty[s], 1);
+      mbar_init(&empty[s], CL);
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&accf[b], 1);
@@ -147,6 +257,7 @@ k_gram_split(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ 
   if (warp == 1) tmem_alloc(tmem_slot, 512);
   tc_fence_before();
   __syncthreads();
+  if (CL > 1) cluster_sync_all(); /* the peers' barriers are initialised before any multicast */
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
   const int32_t nchunk = (nkb + chunk_kb - 1) / chunk_kb;
@@ -156,13 +267,14 @@ k_gram_split(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ 
     if (lane == 0) {
       uint32_t it = 0;
       const int32_t nsync = (nkb + GRAM_SYNC_KB - 1) / GRAM_SYNC_KB;
-      for (int32_t t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x) {
+      for (int32_t t = w0; t < nwork && !*abort_flag; t += wstride) {
         int32_t bi, bj;
-        tri_tile(t, nt_rows, &bi, &bj);
-        /* the CTAs of one wave (tiles t / gridDim) meet every GRAM_SYNC_KB k-blocks, so that
-         * the boxes one of them loads are still in L2 when the others need them */
-        const int32_t wave = t / (int32_t)gridDim.x;
-        const unsigned wave_n = (unsigned)min((int32_t)gridDim.x, ntiles - wave * (int32_t)gridDim.x);
+        bool wr;
+        gram_work<CL>(t, nt_rows, rank, &bi, &bj, &wr);
+        /* the CTAs of one wave (work items t / wstride) meet every GRAM_SYNC_KB k-blocks, so
+         * that the boxes one of them loads are still in L2 when the others need them */
+        const int32_t wave = t / wstride;
+        const unsigned wave_n = (unsigned)(min(wstride, nwork - wave * wstride) * CL);
         for (int32_t kb = 0; kb < nkb; ++kb, ++it) {
           if (kb > 0 && kb % GRAM_SYNC_KB == 0) {
             unsigned *ctr = sync_ctr + (int64_t)wave * nsync + kb / GRAM_SYNC_KB;
@@ -188,10 +300,29 @@ k_gram_split(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ 
           if (!mbar_wait(&empty[s], ph ^ 1u, abort_flag, err, GP_KERR_TIMEOUT_EMPTY)) break;
           uint8_t *st = smem + s * STAGE_BYTES;
           mbar_arrive_expect_tx(&full[s], STAGE_BYTES);
-          tma_load_2d(st, &tm_hi, &full[s], kb * BK, bi * BT);
-          tma_load_2d(st + BOX_BYTES, &tm_lo, &full[s], kb * BK, bi * BT);
-          tma_load_2d(st + 2 * BOX_BYTES, &tm_hi, &full[s], kb * BK, bj * BT);
-          tma_load_2d(st + 3 * BOX_BYTES, &tm_lo, &full[s], kb * BK, bj * BT);
+          if (CL == 4) {
+            /* rank = 2 a + b: row a's box (hi for b = 0, lo for b = 1) to ranks 2a, 2a+1;
+             * column b's box (hi for a = 0, lo for a = 1) to ranks b, b+2 */
+            const uint32_t a = rank >> 1, b = rank & 1u;
+            const uint16_t rmask = (uint16_t)(3u << (2 * a)), cmask = (uint16_t)(5u << b);
+            tma_load_2d_mc(st + b * BOX_BYTES, b ? &tm_lo : &tm_hi, &full[s], kb * BK, bi * BT,
+                           rmask);
+            tma_load_2d_mc(st + (2 + a) * BOX_BYTES, a ? &tm_lo : &tm_hi, &full[s], kb * BK,
+                           bj * BT, cmask);
+          } else {
+            if (CL == 2) {
+              /* A hi from rank 0 and A lo from rank 1, each into both CTAs */
+              if (rank == 0)
+                tma_load_2d_mc(st, &tm_hi, &full[s], kb * BK, bi * BT, (uint16_t)3);
+              else
+                tma_load_2d_mc(st + BOX_BYTES, &tm_lo, &full[s], kb * BK, bi * BT, (uint16_t)3);
+            } else {
+              tma_load_2d(st, &tm_hi, &full[s], kb * BK, bi * BT);
+              tma_load_2d(st + BOX_BYTES, &tm_lo, &full[s], kb * BK, bi * BT);
+            }
+            tma_load_2d(st + 2 * BOX_BYTES, &tm_hi, &full[s], kb * BK, bj * BT);
+            tma_load_2d(st + 3 * BOX_BYTES, &tm_lo, &full[s], kb * BK, bj * BT);
+          }
         }
       }
       if (*abort_flag) {
@@ -211,7 +342,7 @@ k_gram_split(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ 
       const uint32_t idesc = FP16 ? idesc_f16_f32(BT, BT) : idesc_bf16_f32(BT, BT);
       uint32_t it = 0, chunk = 0;
       bool ok = true;
-      for (int32_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+      for (int32_t t = w0; t < nwork && ok; t += wstride) {
         for (int32_t c = 0; c < nchunk && ok; ++c, ++chunk) {
           uint32_t buf = chunk & 1u, use = chunk >> 1;
           if (!mbar_wait(&acce[buf], (use & 1u) ^ 1u, abort_flag, err, GP_KERR_TIMEOUT_ACCE)) {
@@ -241,7 +372,10 @@ k_gram_split(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ 
               umma_bf16(d, alo + o, bhi + o, idesc, 1u);
               if (NMMA == 4) umma_bf16(d, alo + o, blo + o, idesc, 1u);
             }
-            umma_commit(&empty[s]);
+            if (CL > 1)
+              umma_commit_mc(&empty[s], all_mask); /* this CTA has read the stage */
+            else
+              umma_commit(&empty[s]);
           }
           if (!ok) break;
           umma_commit(&accf[buf]);
@@ -264,9 +398,10 @@ k_gram_split(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ 
     const uint32_t t_acc = tmem + lane_addr;
     uint32_t chunk = 0;
     bool ok = true;
-    for (int32_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+    for (int32_t t = w0; t < nwork && ok; t += wstride) {
       int32_t bi, bj;
-      tri_tile(t, nt_rows, &bi, &bj);
+      bool wr;
+      gram_work<CL>(t, nt_rows, rank, &bi, &bj, &wr);
       const int32_t gi = bi * BT + row;
       const int32_t gj0 = bj * BT + col0;
       float A[EPI_COLS];
@@ -335,7 +470,7 @@ k_gram_split(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ 
         tmem_ld16(t_acc + 256 + col0 + 16 * g, hs);
         tmem_ld16(t_acc + 384 + col0 + 16 * g, ls);
         tmem_wait_ld();
-        if (gi < n) {
+        if (wr && gi < n) {
           for (int v = 0; v < 16; ++v) {
             int32_t gj = gj0 + 16 * g + v;
             if (gj < n) {
@@ -350,14 +485,17 @@ k_gram_split(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ 
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  if (warp == 1) {
-    if (*abort_flag && lane == 0) {
-      /* let MMAs already issued finish before the columns are released */
-      umma_commit(drain);
-      uint64_t t0 = globaltimer_ns();
-      while (!mbar_try_wait(drain, 0) && globaltimer_ns() - t0 < GP_WAIT_NS) {
-      }
+  if (warp == 1 && lane == 0 && (CL > 1 || *abort_flag)) {
+    /* let MMAs already issued finish (and, in a pair, their arrivals on the peer's
+     * barriers land) before the columns are released and the CTA leaves */
+    umma_commit(drain);
+    uint64_t t0 = globaltimer_ns();
+    while (!mbar_try_wait(drain, 0) && globaltimer_ns() - t0 < GP_WAIT_NS) {
     }
+  }
+  __syncthreads();
+  if (CL > 1) cluster_sync_all(); /* no multicast or remote arrive targets a CTA that has left */
+  if (warp == 1) {
     __syncwarp();
     tmem_dealloc(tmem, 512);
   }
@@ -494,6 +632,21 @@ static PFN_cuTensorMapEncodeTiled_v12000 get_encode(gp_ctx *ctx)
   return fn;
 }
 
+/* number of tile pairs of tri_pair for nt tile rows */
+static int32_t gram_npairs(int32_t nt)
+{
+  const int32_t ng = (nt + GRAM_GROUP - 1) / GRAM_GROUP;
+  int32_t total = 0;
+  for (int32_t gi = 0; gi < ng; ++gi) {
+    const int32_t r0 = gi * GRAM_GROUP, nr = (nt < r0 + GRAM_GROUP ? nt : r0 + GRAM_GROUP) - r0;
+    for (int32_t gj = 0; gj <= gi; ++gj) {
+      const int32_t c0 = gj * GRAM_GROUP, nc = (nt < c0 + GRAM_GROUP ? nt : c0 + GRAM_GROUP) - c0;
+      for (int32_t lr = 0; lr < nr; ++lr) total += ((gi == gj ? lr + 1 : nc) + 1) / 2;
+    }
+  }
+  return total;
+}
+
 static int make_map(gp_ctx *ctx, CUtensorMap *m, void *base, int32_t rows, int32_t cols,
                     CUtensorMapDataType dt)
 {
@@ -543,7 +696,11 @@ int gp_gram_split(gp_ctx *ctx, int precision)
   size_t tab_bytes = (size_t)nk * 16 + 256;
   const int grid0 = ctx->num_sms < ntiles ? ctx->num_sms : ntiles;
   const size_t nsync = (size_t)((kc / BK + GRAM_SYNC_KB - 1) / GRAM_SYNC_KB);
-  const size_t sync_bytes = sizeof(unsigned) * nsync * (size_t)((ntiles + grid0 - 1) / grid0);
+  /* lockstep counters for the waves of either kernel (at least one cluster of two) */
+  const size_t waves = (size_t)((ntiles + grid0 - 1) / grid0) > (size_t)gram_npairs(nt)
+                           ? (size_t)((ntiles + grid0 - 1) / grid0)
+                           : (size_t)gram_npairs(nt);
+  const size_t sync_bytes = sizeof(unsigned) * nsync * waves;
   uint8_t *base;
   int rc = gp_scratch2(ctx, 2 * xbytes + tab_bytes + sync_bytes + 512, (void **)&base);
   if (rc) return rc;
@@ -562,9 +719,49 @@ int gp_gram_split(gp_ctx *ctx, int precision)
       k_split_tables<0><<<blocks, 256, 0, ctx->stream>>>(ctx->d_kept, nk, ctx->d_vtab, split);
     GP_LAUNCH_CHECK(ctx, "k_split_tables");
   }
-  void (*kern)(const CUtensorMap, const CUtensorMap, int32_t, int32_t, int32_t, double *, int32_t,
-               int32_t, unsigned *, int *) =
-      fp16 ? k_gram_split<1, 3> : (nmma == 4 ? k_gram_split<0, 4> : k_gram_split<0, 3>);
+  typedef void (*gram_kern_t)(const CUtensorMap, const CUtensorMap, int32_t, int32_t, int32_t,
+                              int32_t, double *, int32_t, int32_t, unsigned *, int *);
+  gram_kern_t kern = fp16 ? k_gram_split<1, 3, 1>
+                          : (nmma == 4 ? k_gram_split<0, 4, 1> : k_gram_split<0, 3, 1>);
+  gram_kern_t kern2 = fp16 ? k_gram_split<1, 3, 2>
+                           : (nmma == 4 ? k_gram_split<0, 4, 2> : k_gram_split<0, 3, 2>);
+  gram_kern_t kern4 = fp16 ? k_gram_split<1, 3, 4>
+                           : (nmma == 4 ? k_gram_split<0, 4, 4> : k_gram_split<0, 3, 4>);
+  /* clusters of four CTAs (2 x 2 tiles sharing row and column boxes), else two (two tiles of
+   * a row sharing its boxes), else one CTA per tile; GP_GRAM_CLUSTER=1|2|4 caps the size.
+   * The next smaller size is used when the cluster launch is refused. */
+  int cl = 4;
+  {
+    const char *ce = getenv("GP_GRAM_CLUSTER");
+    if (ce && atoi(ce) >= 1) cl = atoi(ce) >= 4 ? 4 : (atoi(ce) >= 2 ? 2 : 1);
+  }
+  const int32_t nq = (nt + 1) / 2;
+  const int32_t nwork_cl[5] = {0, ntiles, gram_npairs(nt), 0, nq * (nq + 1) / 2};
+  int32_t ncl = 0;
+  for (; cl > 1; cl /= 2) {
+    gram_kern_t kc = cl == 4 ? kern4 : kern2;
+    GP_CUDA(ctx, cudaFuncSetAttribute(kc, cudaFuncAttributeMaxDynamicSharedMemorySize, GRAM_SMEM));
+    cudaLaunchConfig_t qc = {};
+    qc.gridDim = dim3((unsigned)((ctx->num_sms / cl) * cl));
+    qc.blockDim = dim3(GRAM_THREADS);
+    qc.dynamicSmemBytes = GRAM_SMEM;
+    cudaLaunchAttribute qa[1];
+    qa[0].id = cudaLaunchAttributeClusterDimension;
+    qa[0].val.clusterDim.x = (unsigned)cl;
+    qa[0].val.clusterDim.y = 1;
+    qa[0].val.clusterDim.z = 1;
+    qc.attrs = qa;
+    qc.numAttrs = 1;
+    int maxcl = 0;
+    if (cudaOccupancyMaxActiveClusters(&maxcl, (const void *)kc, &qc) != cudaSuccess) {
+      cudaGetLastError();
+      maxcl = 0;
+    }
+    ncl = maxcl < ctx->num_sms / cl ? maxcl : ctx->num_sms / cl;
+    if (ncl > nwork_cl[cl]) ncl = nwork_cl[cl];
+    if (ncl >= 1) break;
+  }
+  if (cl < 2) ncl = 0;
   GP_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, GRAM_SMEM));
   CUtensorMap mhi, mlo;
   CUtensorMapDataType dt = fp16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
@@ -583,11 +780,42 @@ int gp_gram_split(gp_ctx *ctx, int precision)
     int32_t nkb = kcur / BK;
     GP_CUDA(ctx, cudaMemsetAsync(sync_ctr, 0, sync_bytes, ctx->stream));
     /* cooperative launch: the producers' lockstep points need every CTA resident */
-    int32_t a_nt = ntiles, a_nkb = nkb, a_ck = chunk_kb, a_n = n, a_acc = k0 > 0 ? 1 : 0;
+    int32_t a_nt = ntiles, a_rows = nt, a_nkb = nkb, a_ck = chunk_kb, a_n = n,
+            a_acc = k0 > 0 ? 1 : 0;
     double *a_xtx = ctx->d_xtx;
-    void *args[] = {&mhi, &mlo, &a_nt, &a_nkb, &a_ck, &a_xtx, &a_n, &a_acc, &sync_ctr, &d_err};
-    GP_CUDA(ctx, cudaLaunchCooperativeKernel((const void *)kern, dim3(grid), dim3(GRAM_THREADS),
-                                             args, GRAM_SMEM, ctx->stream));
+    bool launched = false;
+    while (!launched && ncl > 0) {
+      cudaLaunchConfig_t lc = {};
+      lc.gridDim = dim3((unsigned)(cl * ncl));
+      lc.blockDim = dim3(GRAM_THREADS);
+      lc.dynamicSmemBytes = GRAM_SMEM;
+      lc.stream = ctx->stream;
+      cudaLaunchAttribute la[2];
+      la[0].id = cudaLaunchAttributeClusterDimension;
+      la[0].val.clusterDim.x = (unsigned)cl;
+      la[0].val.clusterDim.y = 1;
+      la[0].val.clusterDim.z = 1;
+      la[1].id = cudaLaunchAttributeCooperative;
+      la[1].val.cooperative = 1;
+      lc.attrs = la;
+      lc.numAttrs = 2;
+      cudaError_t le = cudaLaunchKernelEx(&lc, cl == 4 ? kern4 : kern2, mhi, mlo, nwork_cl[cl],
+                                          a_rows, a_nkb, a_ck, a_xtx, a_n, a_acc, sync_ctr, d_err);
+      if (le == cudaSuccess) {
+        launched = true;
+      } else {
+        cudaGetLastError();
+        /* refused: the next smaller cluster (same count of SMs), finally one CTA per tile */
+        cl /= 2;
+        ncl = cl > 1 ? ((ctx->num_sms / cl) < nwork_cl[cl] ? ctx->num_sms / cl : nwork_cl[cl]) : 0;
+      }
+    }
+    if (!launched) {
+      void *args[] = {&mhi, &mlo, &a_nt, &a_rows, &a_nkb, &a_ck, &a_xtx, &a_n, &a_acc, &sync_ctr,
+                      &d_err};
+      GP_CUDA(ctx, cudaLaunchCooperativeKernel((const void *)kern, dim3(grid), dim3(GRAM_THREADS),
+                                               args, GRAM_SMEM, ctx->stream));
+    }
     ctx->launches++;
     ctx->gram_launches++;
   }

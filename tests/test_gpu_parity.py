@@ -420,3 +420,19 @@ def test_fastpca_top_eigenvalues_match_exact(gpu):
     s = O.pass_columns(rec, cols, rows, minallelecnt=0, maxmissing=2 ** 31 - 1)
     w = np.linalg.eigvalsh(O.gram(s))[::-1] / (2.0 * 8000)
     assert np.max(np.abs(ev - w[:2]) / w[:2]) <= 1e-6
+
+
+@pytest.mark.parametrize("nind", [1000, 1700])
+def test_split_gram_clusters_equal_single_ctas(gpu, monkeypatch, nind):
+    """the cluster kernels (four CTAs on a 2 x 2 block of tiles, two CTAs on two tiles of a
+    row, boxes multicast) give the Gram of the one-CTA kernel bit for bit, odd tile counts
+    (stand-in tiles) included"""
+    rec, pop = synth(3000, [nind // 2, nind - nind // 2], [0.01, 0.03], miss=0.02, seed=37)
+    rows = np.arange(nind, dtype=np.int32)
+    cols = np.arange(3000, dtype=np.int32)
+    grams = {}
+    for cl in ("4", "2", "1"):
+        monkeypatch.setenv("GP_GRAM_CLUSTER", cl)
+        grams[cl] = _gram_pair(gpu, rec, nind, rows, cols, native.GP_PREC_SPLIT_FP16)["XTX"]
+    assert np.array_equal(grams["4"], grams["1"])
+    assert np.array_equal(grams["2"], grams["1"])

@@ -771,8 +771,12 @@ def cpu_reference_sample(cfg, seconds_target=12.0, nthreads=None):
 
 def gram_traffic(args):
     """DRAM bytes per launch of the split Gram kernel from the committed ncu summary of the
-    full workload (profiles/gram_split_fp16_full_dram.md), or None for other workloads"""
+    full workload (profiles/gram_split_fp16_full_dram.md, one-CTA schedule), or None for other
+    workloads and for the cluster schedule (not captured: profiler replay of the cluster launch
+    is not used)"""
     if args.config != "full" or args.precision != "fp16":
+        return None
+    if os.environ.get("GP_GRAM_CLUSTER", "4") != "1":
         return None
     p = os.path.join(ROOT, "profiles", "gram_split_fp16_full_dram.md")
     try:
@@ -915,7 +919,10 @@ def main():
                 "frac": achieved / peak, "traffic": gram_traffic(args),
                 "peak_kind": "bf16 burst, %s" % res["peak_kind"],
                 "kernels": "k_split_transpose + k_gram_split (algorithmic N(N+1)M flop; the "
-                           "split scheme issues 3 MMAs per algorithmic FMA)"}
+                           "split scheme issues 3 MMAs per algorithmic FMA)",
+                "traffic_note": "DRAM bytes of the one-CTA schedule from "
+                                "profiles/gram_split_fp16_full_dram.md when GP_GRAM_CLUSTER=1; "
+                                "not captured for the cluster schedule"}
     else:
         achieved = res["gram_kernel_flops"] / (res["gram_ms"] * 1e-3) / 1e12
         roof = {"bound": "fp64", "achieved": achieved, "peak": 1.25, "unit": "TFLOP/s",

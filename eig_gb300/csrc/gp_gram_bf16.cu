@@ -65,6 +65,7 @@
 #define GP_KERR_TIMEOUT_ACCF 3
 #define GP_KERR_TIMEOUT_ACCE 4
 #define GP_KERR_TIMEOUT_SYNC 5
+#define GP_KERR_CLUSTER 6 /* launched without clusters of the kernel's size */
 #define GRAM_SYNC_KB 64 /* k-blocks between the producers' lockstep points */
 
 __device__ __forceinline__ int32_t tri_root(int32_t t)
@@ -221,6 +222,12 @@ k_gram_split(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ 
    * (multicast to the row's two CTAs) and one of the two boxes of its tile column
    * (multicast to the column's two CTAs).  A stage is released when every CTA's MMAs of the
    * cluster have read it. */
+  /* a cluster kernel run without clusters of its size (for instance a launch that lost the
+   * cluster attribute) would multicast to CTAs that do not exist: it refuses to run */
+  if (CL > 1 && cluster_nctarank() != (uint32_t)CL) {
+    if (threadIdx.x == 0) atomicExch(err, GP_KERR_CLUSTER);
+    return;
+  }
   const uint32_t rank = CL > 1 ? cluster_ctarank() : 0u;
   const int32_t w0 = CL > 1 ? (int32_t)cluster_id_x() : (int32_t)blockIdx.x;
   const int32_t wstride = CL > 1 ? (int32_t)cluster_count_x() : (int32_t)gridDim.x;
@@ -822,6 +829,8 @@ int gp_gram_split(gp_ctx *ctx, int precision)
   int herr = 0;
   GP_CUDA(ctx, gp_memcpy(ctx, &herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (herr == GP_KERR_CLUSTER)
+    return gp_fail(ctx, GP_ERR_CUDA, "split Gram: the cluster launch was not honoured");
   if (herr) return gp_fail(ctx, GP_ERR_TIMEOUT, "split-BF16 Gram kernel wait timed out (code %d)", herr);
   return GP_OK;
 }

@@ -124,6 +124,12 @@ __device__ __forceinline__ uint32_t cluster_id_x()
   asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
   return r;
 }
+__device__ __forceinline__ uint32_t cluster_nctarank()
+{
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+  return r;
+}
 __device__ __forceinline__ uint32_t cluster_count_x()
 {
   uint32_t r;

@@ -90,6 +90,7 @@ int gp_scratch_aux(gp_ctx *ctx, size_t bytes, void **out)
 
 int gp_scratch4(gp_ctx *ctx, size_t bytes, void **out)
 {
+  ctx->codes4_rows = 0; /* the caller overwrites the codes */
   int rc = grow(ctx, &ctx->d_scratch4, &ctx->scratch4_cap, bytes);
   *out = ctx->d_scratch4;
   return rc;
@@ -182,6 +183,7 @@ extern "C" void gp_close(gp_ctx *ctx)
   if (ctx->ev_g0) cudaEventDestroy(ctx->ev_g0);
   if (ctx->ev_g1) cudaEventDestroy(ctx->ev_g1);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  free(ctx->h_rows);
   free(ctx);
 }
 
@@ -204,6 +206,7 @@ extern "C" int gp_release(gp_ctx *ctx)
   ctx->scratch_cap = ctx->scratch2_cap = ctx->scratch3_cap = ctx->scratch4_cap =
       ctx->scratch5_cap = 0;
   ctx->xtx_cap = 0;
+  ctx->codes4_rows = 0;
   ctx->keep_cap = 0;
   ctx->keep_valid = 0;
   ctx->nsnp_all = 0;
@@ -269,6 +272,7 @@ extern "C" int gp_xtx(gp_ctx *ctx, const gp_xtx_opts *opts, int32_t *n0, int32_t
   for (int32_t c = 0; c < nc; ++c)
     if (!hk[(size_t)c]) kept.push_back(c);
   ctx->nkept = (int32_t)kept.size();
+  ctx->codes4_rows = 0;
   if (ctx->nkept)
     GP_CUDA(ctx, gp_memcpy(ctx, ctx->d_kept, kept.data(), sizeof(int32_t) * kept.size(),
                                  cudaMemcpyHostToDevice, ctx->stream));
@@ -947,7 +951,12 @@ extern "C" int gp_lsqproj(gp_ctx *ctx, int32_t numeigs, const int32_t *samples, 
   /* masked normal equations: co = O P (pair sums + observed count), rr = R E */
   if (ctx->precision != GP_PREC_FP64 && nk > 0) {
     gp_tc_codes A;
-    rc = gp_tc_codes_for(ctx, 1, d_samp, nproj, kt.snprec, nk, &A);
+    /* projecting exactly the analysis rows: the product can reuse their codes */
+    const int32_t *d_list = d_samp;
+    if (nproj == ctx->nrows && ctx->h_rows &&
+        memcmp(samples, ctx->h_rows, sizeof(int32_t) * (size_t)nproj) == 0)
+      d_list = ctx->d_rows;
+    rc = gp_tc_codes_for(ctx, 1, d_list, nproj, kt.snprec, nk, &A);
     if (rc) return rc;
     gp_tc_panel pc = {d_P, ldp, 1.0, 0};
     rc = gp_geno_panel_tc_codes(ctx, &A, 1, &pc, ldp, d_co, ldp);

@@ -462,7 +462,8 @@ k_tridiag(double *A, int n, double *d, double *e, double *tau, double *vbuf, dou
   ff2 tau_pf = ZERO, scale_pf = ZERO, e_pf = ZERO;
   __shared__ ff2 s_slotf;
   bool have_p = false;
-  /* phase_ns (optional, block 0): time in A, B and the barrier (entries 0, 1, 4) */
+  /* phase_ns (optional, block 0): time in A, B (entry 1; entry 2 for the first 30% of the
+   * steps) and the barrier (entry 4) */
   const bool stamp = phase_ns != NULL && b == 0 && threadIdx.x == 0;
   unsigned long long t_prev = stamp ? globaltimer_ns() : 0ull, ph[5] = {0, 0, 0, 0, 0};
 #define TR_STAMP(i)                                  \
@@ -471,6 +472,7 @@ k_tridiag(double *A, int n, double *d, double *e, double *tau, double *vbuf, dou
     ph[i] += t_now - t_prev;                         \
     t_prev = t_now;                                  \
   }
+  const int early = (int)((3LL * n) / 10);
   for (int c = 0; c < n - 1; ++c) {
     /* ---- A (every block, no grid barrier): v and w of step c-1, the pending update of
      * column c and its norm, rebuilt from y, the stored x of step c-1 and column c; each
@@ -560,49 +562,50 @@ k_tridiag(double *A, int n, double *d, double *e, double *tau, double *vbuf, dou
       ff_store(svc + q, (q == c + 1) ? ONE : ff_mul(ff_load(svc + q), scale_cf));
     __syncthreads();
     {
-      /* work items (column, segment): a block with fewer columns than warps splits each into
-       * S segments so that every warp works; segment dots are summed in order */
       const int u0 = st.b1_u0, u1 = st.b1_u1, ncol = u1 - u0;
-      int S = (ncol > 0 && ncol < TR_WARPS) ? (TR_WARPS + ncol - 1) / ncol : 1;
+      /* one piece [qs, qe) of column r: pending update, store and dot with v; the last
+       * partial batch is one predicated round of loads, so no piece ends in a chain of
+       * dependent single loads */
+      auto piece = [&](int r, int qs, int qe) -> ff2 {
+        const ff2 vpr = ff_neg(ff_load(svp + r)), wpr = ff_neg(ff_load(swp + r));
+        double *col = A + (int64_t)r * n;
+        ff2 dot = ZERO;
+        for (int qb = qs; qb < qe; qb += 32 * TR_U) {
+          ff2 a[TR_U];
+#pragma unroll
+          for (int u = 0; u < TR_U; ++u) {
+            const int qq = qb + lane + 32 * u;
+            a[u] = qq < qe ? ff_load(col + qq) : ZERO;
+          }
+#pragma unroll
+          for (int u = 0; u < TR_U; ++u) {
+            const int qq = qb + lane + 32 * u;
+            if (qq < qe) {
+              if (have_p) {
+                a[u] = ff_fma(ff_load(svp + qq), wpr, a[u]);
+                a[u] = ff_fma(ff_load(swp + qq), vpr, a[u]);
+                ff_store(col + qq, a[u]);
+              }
+              dot = ff_fma(a[u], ff_load(svc + qq), dot);
+            }
+          }
+        }
+        for (int o = 16; o; o >>= 1) dot = ff_add(dot, ff_shfl_xor(dot, o));
+        return dot;
+      };
+      /* work items (column, segment): a block with fewer columns than warps splits each into
+       * S segments so that every warp works; segment dots are summed in order.  (Equal
+       * flattened element ranges per warp measured slower than this split.) */
+      const int S = (ncol > 0 && ncol < TR_WARPS) ? (TR_WARPS + ncol - 1) / ncol : 1;
       const int nitem = ncol * S;
       const int seg = ((m + S - 1) / S + 31) & ~31;
       for (int it = warp; it < nitem; it += TR_WARPS) {
         const int j = it / S, sg = it - j * S;
-        const int r = c + 1 + u0 + j;
         const int qs = c + 1 + sg * seg, qe = min(n, qs + seg);
-        const ff2 vpr = ff_neg(ff_load(svp + r)), wpr = ff_neg(ff_load(swp + r));
-        double *col = A + (int64_t)r * n;
-        ff2 dot = ZERO;
-        int q = qs + lane;
-        /* TR_U independent loads per lane before the arithmetic (memory-level parallelism) */
-        for (; q + 32 * (TR_U - 1) < qe; q += 32 * TR_U) {
-          ff2 a[TR_U];
-#pragma unroll
-          for (int k = 0; k < TR_U; ++k) a[k] = ff_load(col + q + 32 * k);
-#pragma unroll
-          for (int k = 0; k < TR_U; ++k) {
-            const int qq = q + 32 * k;
-            if (have_p) {
-              a[k] = ff_fma(ff_load(svp + qq), wpr, a[k]);
-              a[k] = ff_fma(ff_load(swp + qq), vpr, a[k]);
-              ff_store(col + qq, a[k]);
-            }
-            dot = ff_fma(a[k], ff_load(svc + qq), dot);
-          }
-        }
-        for (; q < qe; q += 32) {
-          ff2 a = ff_load(col + q);
-          if (have_p) {
-            a = ff_fma(ff_load(svp + q), wpr, a);
-            a = ff_fma(ff_load(swp + q), vpr, a);
-            ff_store(col + q, a);
-          }
-          dot = ff_fma(a, ff_load(svc + q), dot);
-        }
-        for (int o = 16; o; o >>= 1) dot = ff_add(dot, ff_shfl_xor(dot, o));
+        const ff2 dot = piece(c + 1 + u0 + j, qs, qe);
         if (lane == 0) {
           if (S == 1)
-            ff_store(ycur + r, dot);
+            ff_store(ycur + c + 1 + u0 + j, dot);
           else
             sdotp[it] = dot;
         }
@@ -625,7 +628,7 @@ k_tridiag(double *A, int n, double *d, double *e, double *tau, double *vbuf, dou
       const ff2 ds = ff_block_sum2(dpart, red);
       if (threadIdx.x == 0) ff_store(part_dot2 + (size_t)(c & 1) * G + b, ds);
     }
-    TR_STAMP(1)
+    TR_STAMP(c < early ? 2 : 1)
     target += G;
     if (!tr_grid_sync(count, target, err)) return;
     TR_STAMP(4)
@@ -804,17 +807,106 @@ __global__ void k_mgs(double *Z, int n, int nvec)
  * v_i(i+2:n) stored in A(i+2:n, i).  The reflectors are taken WY_B at a time in the compact
  * WY form H(i0)...H(i0+b-1) = I - V T V^T (T upper triangular, LAPACK dlarft's forward
  * recurrence T(j,j) = tau_j, T(0:j,j) = -tau_j T(0:j,0:j) V(:,0:j)^T v_j), last block first,
- * Z := Z - V (T (V^T Z)).  One cooperative launch, one CTA per SM with a fixed slab of rows:
- * per block of reflectors each CTA forms its rows' share of V^T [V | Z] (partials), a grid
- * barrier, the partials are summed in fixed order (entries spread over the CTAs), a second
- * barrier, then every CTA builds T and W = T V^T Z from the sums and updates its own rows.
- * Float-float arithmetic (about 46 bits) from the FP64 inputs to the FP64 output; bounded grid
- * barriers report through err.
+ * Z := Z - V (T (V^T Z)).  T depends on the reflectors only, so k_wy_tmat builds every
+ * block's T at once (one CTA per block) before k_apply_q runs the blocks in order.
+ * Float-float arithmetic (about 46 bits) from the FP64 inputs to the FP64 output.
  */
 #define WY_B 32
-#define WY_THREADS 256
+#define WY_THREADS 512
+#define WT_THREADS 256
+#define WT_ROWS 64
+
+/* entry e of the upper triangle (row-major, k <= c) of a WY_B x WY_B matrix */
+__device__ __forceinline__ void wy_upper_entry(int e, int *k, int *c)
+{
+  int r = 0;
+  while (e >= WY_B - r) {
+    e -= WY_B - r;
+    ++r;
+  }
+  *k = r;
+  *c = r + e;
+}
+
+/* Tg [nblk][WY_B][WY_B] (float-float pairs in doubles' storage): block blk's T, from
+ * S = V^T V summed over the reflector rows in order (rows staged WT_ROWS at a time) */
+__global__ void __launch_bounds__(WT_THREADS)
+k_wy_tmat(const double *__restrict__ A, int n, const double *__restrict__ tau, double *Tg)
+{
+  __shared__ ff2 Vc[WT_ROWS][WY_B + 1];
+  __shared__ ff2 Ss[WY_B][WY_B + 1];
+  __shared__ ff2 Tm[WY_B][WY_B + 1];
+  constexpr int NUP = WY_B * (WY_B + 1) / 2;
+  constexpr int SLOTS = (NUP + WT_THREADS - 1) / WT_THREADS;
+  const int blk = blockIdx.x, tid = threadIdx.x;
+  const int nref = n - 1, i0 = blk * WY_B;
+  if (i0 >= nref) return;
+  const int nb = nref - i0 < WY_B ? nref - i0 : WY_B;
+  const ff2 ZERO = ff_make(0.f, 0.f);
+  int ek[SLOTS], ec[SLOTS];
+  ff2 acc[SLOTS];
+#pragma unroll
+  for (int sl = 0; sl < SLOTS; ++sl) {
+    const int e = tid + sl * WT_THREADS;
+    ek[sl] = ec[sl] = -1;
+    if (e < NUP) wy_upper_entry(e, &ek[sl], &ec[sl]);
+    acc[sl] = ZERO;
+  }
+  for (int r0 = i0 + 1; r0 < n; r0 += WT_ROWS) {
+    const int nr = n - r0 < WT_ROWS ? n - r0 : WT_ROWS;
+    __syncthreads();
+    for (int idx = tid; idx < WT_ROWS * WY_B; idx += WT_THREADS) {
+      const int k = idx / WT_ROWS, q = idx - k * WT_ROWS, rr = r0 + q, i = i0 + k;
+      double v = 0.0;
+      if (k < nb && q < nr) v = rr == i + 1 ? 1.0 : (rr > i + 1 ? A[(size_t)i * n + rr] : 0.0);
+      Vc[q][k] = ff_from_double(v);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int sl = 0; sl < SLOTS; ++sl) {
+      if (ek[sl] < 0) continue;
+      ff2 t = acc[sl];
+      for (int q = 0; q < nr; ++q) t = ff_fma(Vc[q][ek[sl]], Vc[q][ec[sl]], t);
+      acc[sl] = t;
+    }
+  }
+#pragma unroll
+  for (int sl = 0; sl < SLOTS; ++sl)
+    if (ek[sl] >= 0) Ss[ek[sl]][ec[sl]] = acc[sl];
+  __syncthreads();
+  /* T (dlarft forward, columnwise): one warp, column j after column j-1 */
+  if (tid < 32) {
+    for (int j = 0; j < WY_B; ++j) {
+      const ff2 tj = j < nb ? ff_from_double(tau[i0 + j]) : ZERO;
+      ff2 t = ZERO;
+      if (tid < j) t = ff_neg(ff_mul(tj, Ss[tid][j]));
+      /* T(0:j, j) = T(0:j, 0:j) t: row tid of the upper triangle */
+      ff2 a = ZERO;
+      for (int l = 0; l < j; ++l) {
+        const ff2 tl = ff_make(__shfl_sync(0xFFFFFFFFu, t.h, l), __shfl_sync(0xFFFFFFFFu, t.l, l));
+        if (tid <= l) a = ff_fma(Tm[tid][l], tl, a);
+      }
+      if (tid < j) Tm[tid][j] = a;
+      if (tid == j) Tm[j][j] = tj;
+      if (tid > j) Tm[tid][j] = ZERO;
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  double *T = Tg + (size_t)blk * WY_B * WY_B;
+  for (int idx = tid; idx < WY_B * WY_B; idx += WT_THREADS)
+    ff_store(T + idx, Tm[idx / WY_B][idx % WY_B]);
+}
+
+/*
+ * One cooperative launch, one CTA per SM with a fixed slab of rows: per block of reflectors
+ * each CTA forms its rows' share of V^T Z (partials), a grid barrier, the partials are summed
+ * in fixed order (entries spread over the CTAs), a second barrier, then every CTA forms
+ * W = T (V^T Z) with the block's T from k_wy_tmat and updates its own rows.  Bounded grid
+ * barriers report through err.
+ */
 __global__ void __launch_bounds__(WY_THREADS, 1)
-k_apply_q(const double *__restrict__ A, int n, const double *__restrict__ tau, double *Z, int nvec,
+k_apply_q(const double *__restrict__ A, int n, const double *__restrict__ Tg, double *Z, int nvec,
           double *part, double *S, unsigned *bar, int *err)
 {
   /* all products in float-float on the FP32 pipe (GB300's FP64 pipe issues ~2 FMAs per
@@ -823,10 +915,10 @@ k_apply_q(const double *__restrict__ A, int n, const double *__restrict__ tau, d
   const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x;
   const int rpb = (n + G - 1) / G;
   const int R0 = b * rpb < n ? b * rpb : n, R1 = R0 + rpb < n ? R0 + rpb : n;
-  const int ncolS = WY_B + nvec, nent = WY_B * ncolS;
+  const int nent = WY_B * nvec;
   ff2 *Vs = reinterpret_cast<ff2 *>(wsm);    /* [rpb][WY_B]  the CTA's rows of V */
   ff2 *Zs = Vs + (size_t)rpb * WY_B;         /* [rpb][nvec]  its rows of Z */
-  ff2 *Ss = Zs + (size_t)rpb * nvec;         /* [WY_B][ncolS] V^T [V | Z] */
+  ff2 *Ss = Zs + (size_t)rpb * nvec;         /* [WY_B][nvec] V^T Z */
   ff2 *Tm = Ss + (size_t)nent;               /* [WY_B][WY_B] */
   ff2 *Wm = Tm + WY_B * WY_B;                /* [WY_B][nvec] */
   const ff2 ZERO = ff_make(0.f, 0.f);
@@ -851,18 +943,12 @@ k_apply_q(const double *__restrict__ A, int n, const double *__restrict__ tau, d
       Vs[(rr - R0) * WY_B + k] = ff_from_double(v);
     }
     __syncthreads();
-    /* partial V^T [V | Z] over the CTA's rows (V^T V: upper triangle only) */
+    /* partial V^T Z over the CTA's rows */
     for (int e = tid; e < nent; e += WY_THREADS) {
-      const int k = e / ncolS, c = e - k * ncolS;
+      const int k = e / nvec, c = e - k * nvec;
       ff2 acc = ZERO;
-      if (c < WY_B) {
-        if (c >= k)
-          for (int rr = r0 - R0; rr < R1 - R0; ++rr)
-            acc = ff_fma(Vs[rr * WY_B + k], Vs[rr * WY_B + c], acc);
-      } else {
-        for (int rr = r0 - R0; rr < R1 - R0; ++rr)
-          acc = ff_fma(Vs[rr * WY_B + k], Zs[rr * nvec + (c - WY_B)], acc);
-      }
+      for (int rr = r0 - R0; rr < R1 - R0; ++rr)
+        acc = ff_fma(Vs[rr * WY_B + k], Zs[rr * nvec + c], acc);
       ff_store(part + (size_t)b * nent + e, acc);
     }
     target += G;
@@ -881,31 +967,14 @@ k_apply_q(const double *__restrict__ A, int n, const double *__restrict__ tau, d
     if (!tr_grid_sync(bar, target, err)) return;
     if (m == 0) continue;
     for (int e = tid; e < nent; e += WY_THREADS) Ss[e] = ff_load(S + e);
-    __syncthreads();
-    /* T (dlarft forward, columnwise): one warp, column j after column j-1 */
-    if (tid < 32) {
-      for (int j = 0; j < WY_B; ++j) {
-        const ff2 tj = j < nb ? ff_from_double(tau[i0 + j]) : ZERO;
-        ff2 t = ZERO;
-        if (tid < j) t = ff_neg(ff_mul(tj, Ss[tid * ncolS + j]));
-        /* T(0:j, j) = T(0:j, 0:j) t: row tid of the upper triangle */
-        ff2 acc = ZERO;
-        for (int l = 0; l < j; ++l) {
-          const ff2 tl = ff_make(__shfl_sync(0xFFFFFFFFu, t.h, l), __shfl_sync(0xFFFFFFFFu, t.l, l));
-          if (tid <= l) acc = ff_fma(Tm[tid * WY_B + l], tl, acc);
-        }
-        if (tid < j) Tm[tid * WY_B + j] = acc;
-        if (tid == j) Tm[j * WY_B + j] = tj;
-        if (tid > j) Tm[tid * WY_B + j] = ZERO;
-        __syncwarp();
-      }
-    }
+    for (int e = tid; e < WY_B * WY_B; e += WY_THREADS)
+      Tm[e] = ff_load(Tg + (size_t)blk * WY_B * WY_B + e);
     __syncthreads();
     /* W = T (V^T Z) */
     for (int e = tid; e < WY_B * nvec; e += WY_THREADS) {
       const int k = e / nvec, c = e - k * nvec;
       ff2 acc = ZERO;
-      for (int l = k; l < WY_B; ++l) acc = ff_fma(Tm[k * WY_B + l], Ss[l * ncolS + WY_B + c], acc);
+      for (int l = k; l < WY_B; ++l) acc = ff_fma(Tm[k * WY_B + l], Ss[l * nvec + c], acc);
       Wm[e] = acc;
     }
     __syncthreads();
@@ -958,7 +1027,9 @@ int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, d
   int lw = lwork > lwork2 ? lwork : lwork2;
   size_t nd = (size_t)n;
   const size_t G = (size_t)ctx->num_sms;
-  const size_t qpart_n = (G + 1) * (size_t)WY_B * (WY_B + nv); /* partials + sums of k_apply_q */
+  const size_t nwy = (nd + WY_B - 1) / WY_B;
+  /* partials + sums of k_apply_q, then the blocks' T from k_wy_tmat */
+  const size_t qpart_n = (G + 1) * (size_t)WY_B * nv + nwy * WY_B * WY_B;
   size_t bytes = sizeof(double) * (9 * nd + 2 * G + (size_t)lw + 6 * nd * nv + 80 + qpart_n) +
                  sizeof(int) * 64;
   double *base;
@@ -1014,8 +1085,10 @@ int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, d
     if (timing) {
       unsigned long long hp[5];
       cudaMemcpy(hp, phase, sizeof hp, cudaMemcpyDeviceToHost);
-      fprintf(stderr, "k_tridiag n=%d (block 0): A %.1f ms, B %.1f, barrier %.1f\n", n,
-              hp[0] * 1e-6, hp[1] * 1e-6, hp[4] * 1e-6);
+      fprintf(stderr,
+              "k_tridiag n=%d (block 0): A %.1f ms, B %.1f (first 30%% of steps %.1f), "
+              "barrier %.1f\n",
+              n, hp[0] * 1e-6, (hp[1] + hp[2]) * 1e-6, hp[2] * 1e-6, hp[4] * 1e-6);
     }
   } else {
     if (cusolverDnDsytrd(h, CUBLAS_FILL_MODE_LOWER, n, ctx->d_xtx, n, d, e, tau, ws, lw,
@@ -1093,7 +1166,7 @@ int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, d
     const char *oenv = getenv("GP_EIG_CUSOLVER_ORMTR");
     const int Gq = ctx->num_sms;
     const size_t rpb = ((size_t)n + Gq - 1) / Gq;
-    const size_t nent = (size_t)WY_B * (WY_B + nvec);
+    const size_t nent = (size_t)WY_B * nvec;
     const size_t q_smem = sizeof(double) * (rpb * (WY_B + nvec) + nent + WY_B * WY_B + (size_t)WY_B * nvec);
     int qcoop = !(oenv && oenv[0] == '1') && n >= 2 && q_smem <= 200 * 1024 &&
                 qpart != NULL;
@@ -1112,8 +1185,13 @@ int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, d
       GP_CUDA(ctx, cudaMemsetAsync(qbar, 0, sizeof(unsigned), ctx->stream));
       const double *Aq = ctx->d_xtx;
       double *Sq = qpart + (size_t)Gq * nent;
+      double *Tg = qpart + (size_t)(Gq + 1) * nent;
+      const int nwyb = (n - 1 + WY_B - 1) / WY_B;
+      k_wy_tmat<<<nwyb, WT_THREADS, 0, ctx->stream>>>(Aq, n, tau, Tg);
+      GP_LAUNCH_CHECK(ctx, "k_wy_tmat");
+      const double *Tgc = Tg;
       int nn = n, nv2 = nvec;
-      void *qargs[] = {(void *)&Aq, &nn, &tau, &d_vecs, &nv2, &qpart, &Sq, &qbar, &d_err};
+      void *qargs[] = {(void *)&Aq, &nn, (void *)&Tgc, &d_vecs, &nv2, &qpart, &Sq, &qbar, &d_err};
       GP_CUDA(ctx, cudaLaunchCooperativeKernel((const void *)k_apply_q, dim3((unsigned)Gq),
                                                dim3(WY_THREADS), qargs, q_smem, ctx->stream));
       ctx->launches++;

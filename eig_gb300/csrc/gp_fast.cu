@@ -196,6 +196,7 @@ extern "C" int gp_fastpca(gp_ctx *ctx, int32_t K, int32_t L, int32_t I, uint64_t
     if (!hk[(size_t)c]) kept.push_back(c);
   const int32_t nk = (int32_t)kept.size();
   ctx->nkept = nk;
+  ctx->codes4_rows = 0;
   if (nk < 1) return gp_fail(ctx, GP_ERR_NODATA, "gp_fastpca: no polymorphic SNP");
   GP_CUDA(ctx, gp_memcpy(ctx, ctx->d_kept, kept.data(), sizeof(int32_t) * (size_t)nk,
                          cudaMemcpyHostToDevice, ctx->stream));

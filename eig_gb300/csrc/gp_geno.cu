@@ -11,6 +11,8 @@
  * gather.
  */
 #include <cuda_runtime.h>
+#include <stdlib.h>
+#include <string.h>
 
 #include "gp_internal.h"
 
@@ -109,6 +111,7 @@ extern "C" int gp_load_genotypes(gp_ctx *ctx, const uint8_t *records, int64_t re
   ctx->nind_all = nind;
   ctx->rlen_dev = rlen_dev;
   ctx->nrows = ctx->ncols = 0;
+  ctx->codes4_rows = 0;
   ctx->xtx_valid = ctx->eig_valid = ctx->weights_valid = 0;
   ctx->h2d_bytes += used * nsnp;
   GP_CUDA(ctx, cudaMemcpy2DAsync(ctx->d_geno, (size_t)rlen_dev, records, (size_t)record_bytes,
@@ -204,7 +207,12 @@ extern "C" int gp_set_samples(gp_ctx *ctx, const int32_t *xindex, int32_t nrows)
   k_rowmask_from_list<<<grid_for(ctx, nrows, 256), 256, 0, ctx->stream>>>(
       ctx->d_rowmask, nwords, ctx->d_rows, nrows);
   GP_LAUNCH_CHECK(ctx, "k_rowmask_from_list");
+  int32_t *hr = (int32_t *)realloc(ctx->h_rows, sizeof(int32_t) * (size_t)nrows);
+  if (!hr) return gp_fail(ctx, GP_ERR_NOMEM, "gp_set_samples: host row list");
+  memcpy(hr, xindex, sizeof(int32_t) * (size_t)nrows);
+  ctx->h_rows = hr;
   ctx->nrows = nrows;
+  ctx->codes4_rows = 0;
   ctx->xtx_valid = ctx->eig_valid = ctx->weights_valid = 0;
   GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return GP_OK;
@@ -230,6 +238,7 @@ extern "C" int gp_set_snps(gp_ctx *ctx, const int32_t *snp_index, int32_t ncols)
   GP_CUDA(ctx, gp_memcpy(ctx, ctx->d_cols, snp_index, sizeof(int32_t) * (size_t)ncols,
                                cudaMemcpyHostToDevice, ctx->stream));
   ctx->ncols = ncols;
+  ctx->codes4_rows = 0;
   ctx->xtx_valid = ctx->eig_valid = ctx->weights_valid = 0;
   GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return GP_OK;

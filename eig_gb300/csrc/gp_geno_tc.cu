@@ -451,11 +451,42 @@ __global__ void k_panel_expo(const unsigned long long *mx, int32_t ncols, int32_
 }
 
 /*
+ * The four slices of x = sign P / 2^e_c (|x| < 1) in integer arithmetic (GB300's FP64 pipe is
+ * narrow): N = rint(x 2^40) from the double's mantissa and exponent (round half to even),
+ * then balanced base-1024 digits from the bottom, d_3, d_2, d_1 in [-512, 511] and
+ * d_0 = the rest (|d_0| <= 1024 since |N| <= 2^40), so that x = sum_t d_t 1024^-(t+1) + O(2^-41).
+ */
+__device__ __forceinline__ void slice4(double v, int e, bool neg, int d[4])
+{
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+  const int E = (int)((bits >> 52) & 0x7FF);
+  unsigned long long M = bits & 0xFFFFFFFFFFFFFull;
+  /* |v| = M 2^(E' - 1075) with E' = max(E, 1); x 2^40 = M / 2^sh, sh >= 13 when |v| < 2^e */
+  if (E) M |= 1ull << 52;
+  const int sh = 1035 + e - (E ? E : 1);
+  long long N = 0;
+  if (M != 0 && sh < 64) {
+    const int s = sh < 1 ? 1 : sh;
+    unsigned long long q = M >> s;
+    const unsigned long long rem = M & ((1ull << s) - 1), half = 1ull << (s - 1);
+    if (rem > half || (rem == half && (q & 1ull))) ++q;
+    N = (long long)q;
+  }
+  if (neg != (bool)(bits >> 63)) N = -N;
+#pragma unroll
+  for (int t = 3; t >= 1; --t) {
+    int r = (int)(N & 1023);
+    if (r >= 512) r -= 1024;
+    d[t] = r;
+    N = (N - r) >> 10; /* exact: N - r is a multiple of 1024 */
+  }
+  d[0] = (int)N;
+}
+
+/*
  * B[(4c+t)][koff + k] (fp16, row stride ldb elements) = slice t of sign P[k][c] / 2^e_c for
- * k < nk (pad k and pad rows are zero from a memset before): x = sign P / 2^e_c (|x| < 1,
- * exact) is cut into four balanced base-1024 digits, digit t = rint(x 1024^(t+1)) minus the
- * digits before, so that x = sum_t d_t 1024^-(t+1) + O(2^-41).  A tile of 64 k x 32 columns
- * is read row-wise (coalesced) into shared memory and written as 128-byte rows of B.
+ * k < nk (pad k and pad rows are zero from a memset before).  A tile of 64 k x 32 columns is
+ * read row-wise (coalesced) into shared memory and written as 128-byte rows of B.
  */
 #define SL_K 64
 #define SL_C 32
@@ -465,12 +496,13 @@ k_panel_slices(const double *__restrict__ P, int64_t ldp, int32_t nk, int32_t nc
 {
   __shared__ double sp[SL_K][SL_C + 1];
   __shared__ __align__(16) __half ss[SL_C * 4][SL_K + 8];
-  __shared__ double sscale[SL_C];
+  __shared__ int sexp[SL_C];
   const int tid = threadIdx.x;
   const int32_t kt0 = blockIdx.x * SL_K, ct0 = blockIdx.y * SL_C;
+  const bool neg = sign < 0.0;
   if (tid < SL_C) {
     const int32_t c = ct0 + tid;
-    sscale[tid] = c < ncols ? ldexp(sign, -expo[c]) : 0.0;
+    sexp[tid] = c < ncols ? expo[c] : 0;
   }
   for (int i = tid; i < SL_K * SL_C; i += blockDim.x) {
     const int kk = i / SL_C, cc = i - kk * SL_C;
@@ -480,13 +512,10 @@ k_panel_slices(const double *__restrict__ P, int64_t ldp, int32_t nk, int32_t nc
   __syncthreads();
   for (int i = tid; i < SL_K * SL_C; i += blockDim.x) {
     const int cc = i / SL_K, kk = i - cc * SL_K;
-    double r = sp[kk][cc] * sscale[cc] * 1024.0; /* exact: powers of two */
+    int d[4];
+    slice4(sp[kk][cc], sexp[cc], neg, d);
 #pragma unroll
-    for (int t = 0; t < 4; ++t) {
-      const double qv = rint(r);
-      r = (r - qv) * 1024.0; /* exact: r - qv is the low part of r */
-      ss[4 * cc + t][kk] = __double2half(qv);
-    }
+    for (int t = 0; t < 4; ++t) ss[4 * cc + t][kk] = __int2half_rn(d[t]);
   }
   __syncthreads();
   /* 128 output rows x 64 halves: 8 threads write one row's 128 bytes */
@@ -711,6 +740,20 @@ int gp_geno_panel_tc_codes(gp_ctx *ctx, const gp_tc_codes *A, int npanels, const
 int gp_tc_codes_for(gp_ctx *ctx, int sum_over_snps, const int32_t *d_samp, int32_t nsamp,
                     const int32_t *d_snprec, int32_t nk, gp_tc_codes *out)
 {
+  const int current_rows = sum_over_snps && d_samp == ctx->d_rows && nsamp == ctx->nrows &&
+                           nk == ctx->nkept;
+  if (current_rows && ctx->codes4_rows) {
+    /* the sample-major codes of the current rows are still in place */
+    int64_t ldc;
+    int32_t rows_pad;
+    gp_tc_code_bytes(1, nsamp, nk, &ldc, &rows_pad);
+    out->codes = (uint8_t *)ctx->d_scratch4;
+    out->ldc = ldc;
+    out->row_map = NULL;
+    out->nrows = nsamp;
+    out->k0 = nk;
+    return GP_OK;
+  }
   if (!sum_over_snps && nsamp == ctx->nind_all) {
     /* every sample in order: the resident records are the SNP-major operand */
     out->codes = ctx->d_geno;
@@ -726,22 +769,18 @@ int gp_tc_codes_for(gp_ctx *ctx, int sum_over_snps, const int32_t *d_samp, int32
   uint8_t *codes;
   int rc = gp_scratch4(ctx, (size_t)rows_pad * ldc + 256, (void **)&codes);
   if (rc) return rc;
-  return gp_tc_build_codes(ctx, sum_over_snps, d_samp, nsamp, d_snprec, nk, codes, out);
+  rc = gp_tc_build_codes(ctx, sum_over_snps, d_samp, nsamp, d_snprec, nk, codes, out);
+  if (!rc && current_rows) ctx->codes4_rows = 1;
+  return rc;
 }
 
 int gp_geno_panel_tc(gp_ctx *ctx, int sum_over_snps, const int32_t *d_samp, int32_t nsamp,
                      const int32_t *d_snprec, int32_t nk, int npanels, const gp_tc_panel *pp,
                      int32_t ncols, double *d_Y, int64_t ldy)
 {
-  int64_t ldc;
-  int32_t rows_pad;
-  gp_tc_code_bytes(sum_over_snps, nsamp, nk, &ldc, &rows_pad);
   if ((sum_over_snps ? nsamp : nk) < 1 || (sum_over_snps ? nk : nsamp) < 1) return GP_OK;
-  uint8_t *codes;
-  int rc = gp_scratch4(ctx, (size_t)rows_pad * ldc + 256, (void **)&codes);
-  if (rc) return rc;
   gp_tc_codes A;
-  rc = gp_tc_build_codes(ctx, sum_over_snps, d_samp, nsamp, d_snprec, nk, codes, &A);
+  int rc = gp_tc_codes_for(ctx, sum_over_snps, d_samp, nsamp, d_snprec, nk, &A);
   if (rc) return rc;
   return gp_geno_panel_tc_codes(ctx, &A, npanels, pp, ncols, d_Y, ldy);
 }

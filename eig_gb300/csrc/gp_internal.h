@@ -84,6 +84,9 @@ struct gp_ctx {
   size_t scratch3_cap;
   void *d_scratch4;    /* genotype code operands of gp_geno_tc */
   size_t scratch4_cap;
+  int codes4_rows;     /* d_scratch4 holds the sample-major codes of the current rows over the
+                          kept columns of the last gp_xtx, for reuse by the next product */
+  int32_t *h_rows;     /* [nrows] host copy of d_rows */
   void *d_scratch5;    /* exact integer partial sums of gp_geno_tc */
   size_t scratch5_cap;
   int *d_err;          /* error word written by the tensor-core kernels' bounded waits */

@@ -8,7 +8,7 @@
  *   2. all eigenvalues of T by multisection on Sturm counts (the published bisection method:
  *      the count of negative pivots of the LDL^T factorisation of T - x I equals the number
  *      of eigenvalues below x), several lanes per eigenvalue index: FP32 brackets first,
- *      checked and finished in FP64 to 1e-13 ||T||;
+ *      then float-float, checked and finished in FP64 to 1e-13 ||T||;
  *   3. the top nvec eigenvectors of T by inverse iteration, one block per vector: LU with
  *      partial pivoting of the tridiagonal T - lambda I (Gaussian elimination with row
  *      interchanges) and three solves from a fixed pseudo-random start, then modified
@@ -27,6 +27,95 @@
 #include "gp_internal.h"
 #include "gp_tc.cuh"
 
+
+/*
+ * Float-float arithmetic: a value is an unevaluated sum h + l of two FP32 numbers (about 46
+ * significant bits), built from the error-free transformations TwoSum (Knuth) and TwoProd
+ * with FMA (Dekker / Ogita-Rump-Oishi 2005).  GB300's FP64 pipe issues about 2 FMAs per clock
+ * per SM and its FP32 pipe 128, so the tridiagonalisation keeps its trailing matrix and
+ * vectors in this form; every operation below is explicitly rounded (no contraction).
+ */
+struct ff2 {
+  float h, l;
+};
+
+__device__ __forceinline__ ff2 ff_make(float h, float l)
+{
+  ff2 r;
+  r.h = h;
+  r.l = l;
+  return r;
+}
+__device__ __forceinline__ ff2 ff_from_double(double x)
+{
+  const float h = __double2float_rn(x);
+  return ff_make(h, __double2float_rn(x - (double)h));
+}
+__device__ __forceinline__ double ff_to_double(ff2 a) { return (double)a.h + (double)a.l; }
+__device__ __forceinline__ ff2 ff_neg(ff2 a) { return ff_make(-a.h, -a.l); }
+/* a + b */
+__device__ __forceinline__ ff2 ff_add(ff2 a, ff2 b)
+{
+  const float s = __fadd_rn(a.h, b.h);
+  const float bb = __fsub_rn(s, a.h);
+  float err = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(b.h, bb));
+  err = __fadd_rn(err, __fadd_rn(a.l, b.l));
+  const float h = __fadd_rn(s, err);
+  return ff_make(h, __fsub_rn(err, __fsub_rn(h, s)));
+}
+/* a * b */
+__device__ __forceinline__ ff2 ff_mul(ff2 a, ff2 b)
+{
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  const float h = __fadd_rn(p, e);
+  return ff_make(h, __fsub_rn(e, __fsub_rn(h, p)));
+}
+/* a * b + c */
+__device__ __forceinline__ ff2 ff_fma(ff2 a, ff2 b, ff2 c)
+{
+  const float p = __fmul_rn(a.h, b.h);
+  float pe = __fmaf_rn(a.h, b.h, -p);
+  pe = __fmaf_rn(a.h, b.l, pe);
+  pe = __fmaf_rn(a.l, b.h, pe);
+  const float s = __fadd_rn(c.h, p);
+  const float bb = __fsub_rn(s, c.h);
+  float err = __fadd_rn(__fsub_rn(c.h, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+  err = __fadd_rn(err, __fadd_rn(c.l, pe));
+  const float h = __fadd_rn(s, err);
+  return ff_make(h, __fsub_rn(err, __fsub_rn(h, s)));
+}
+__device__ __forceinline__ ff2 ff_shfl_xor(ff2 a, int o)
+{
+  return ff_make(__shfl_xor_sync(0xFFFFFFFFu, a.h, o), __shfl_xor_sync(0xFFFFFFFFu, a.l, o));
+}
+__device__ __forceinline__ ff2 ff_load(const double *p)
+{
+  const float2 v = *reinterpret_cast<const float2 *>(p);
+  return ff_make(v.x, v.y);
+}
+__device__ __forceinline__ void ff_store(double *p, ff2 a)
+{
+  *reinterpret_cast<float2 *>(p) = make_float2(a.h, a.l);
+}
+
+/* sqrt(a) for a > 0: FP32 root plus one correction, (a - s^2) / 2s */
+__device__ __forceinline__ ff2 ff_sqrt(ff2 a)
+{
+  const float s = sqrtf(a.h);
+  const ff2 r = ff_fma(ff_make(-s, 0.f), ff_make(s, 0.f), a);
+  return ff_add(ff_make(s, 0.f), ff_make(__fdiv_rn(r.h, 2.f * s), 0.f));
+}
+/* a / b: FP32 quotient plus one correction from the float-float remainder */
+__device__ __forceinline__ ff2 ff_div(ff2 a, ff2 b)
+{
+  const float q1 = __fdiv_rn(a.h, b.h);
+  const ff2 r = ff_fma(ff_neg(b), ff_make(q1, 0.f), a);
+  return ff_add(ff_make(q1, 0.f), ff_make(__fdiv_rn(r.h, b.h), 0.f));
+}
+__device__ __forceinline__ ff2 ff_scale(ff2 a, float s) { return ff_make(a.h * s, a.l * s); }
 
 /* the same count in FP32 (coarse brackets only; verified in FP64 afterwards) */
 __device__ __forceinline__ int sturm_count_f(const float *d, const float *e2, int n, float x,
@@ -98,15 +187,47 @@ __device__ __forceinline__ int sturm_count_bits(const double *d, const double *e
   return cnt;
 }
 
+/* a / b in float-float from the FP32 approximate reciprocal and one remainder correction
+ * (relative error ~2^-44; the Sturm brackets below allow for it) */
+__device__ __forceinline__ ff2 ff_div_approx(ff2 a, ff2 b)
+{
+  float rb;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rb) : "f"(b.h));
+  const float q1 = __fmul_rn(a.h, rb);
+  const ff2 r = ff_fma(ff_neg(b), ff_make(q1, 0.f), a);
+  const float q2 = __fmul_rn(r.h, rb);
+  const float h = __fadd_rn(q1, q2);
+  return ff_make(h, __fsub_rn(q2, __fsub_rn(h, q1)));
+}
+
+/* the Sturm count in float-float (d and e2 as hi/lo FP32 pairs; verified in FP64 afterwards) */
+__device__ __forceinline__ int sturm_count_ff(const float *dh, const float *dl, const float *eh,
+                                              const float *el, int n, ff2 x, float pivmin)
+{
+  const ff2 nx = ff_neg(x), clamp = ff_make(-pivmin, 0.f);
+  ff2 q = ff_add(ff_make(dh[0], dl[0]), nx);
+  if (fabsf(q.h) < pivmin) q = clamp;
+  int cnt = q.h < 0.f;
+  for (int i = 1; i < n; ++i) {
+    const ff2 t = ff_add(ff_make(dh[i], dl[i]), nx);
+    q = ff_add(t, ff_neg(ff_div_approx(ff_make(eh[i - 1], el[i - 1]), q)));
+    if (fabsf(q.h) < pivmin) q = clamp;
+    cnt += q.h < 0.f;
+  }
+  return cnt;
+}
+
 /*
  * All eigenvalues by multisection: a warp owns epw consecutive eigenvalue indices and each
  * index gets P = 32/epw lanes (P >= 1), so every warp slot of the GPU has work whatever N is.
  * A step evaluates P interior points of the bracket at once (one Sturm count per lane) and
  * keeps the sub-interval where the count crosses k: log2(P+1) bits per step.  FP32 counts
- * narrow the bracket to ~4e-7 ||T||, it is widened by 64 eps_32 ||T|| and checked with two
- * FP64 counts (back to the Gershgorin bracket if the check fails), then FP64 counts narrow it
- * to tol.  Grid: one CTA of 4 warps per SM; d, e2 and FP32 copies in shared memory
- * (24 N bytes) when they fit.
+ * narrow the bracket to ~4e-7 ||T|| (widened by 64 eps_32 ||T||), float-float counts on the
+ * FP32 pipe narrow it to ~1e-12 ||T|| (widened by 64 2^-44 ||T||), two FP64 counts check it
+ * (back to the Gershgorin bracket if the check fails), then FP64 counts narrow it to tol.
+ * Grid: one CTA of 4 warps per SM; d, e2 and their FP32 hi/lo copies in shared memory
+ * (32 N bytes) when they fit (use_smem 2), d, e2 and FP32 copies without the float-float
+ * phase (24 N bytes, use_smem 1), else FP64 counts from global memory only.
  */
 __global__ void __launch_bounds__(128)
 k_multisect(const double *gd, const double *ge2, int n, double gl, double gu, double tnorm,
@@ -114,16 +235,19 @@ k_multisect(const double *gd, const double *ge2, int n, double gl, double gu, do
 {
   extern __shared__ double sm[];
   const double *d = gd, *e2 = ge2;
-  const float *df = NULL, *e2f = NULL;
+  const float *df = NULL, *e2f = NULL, *dl = NULL, *e2l = NULL;
   if (use_smem) {
     double *sd = sm, *se2 = sm + n;
     float *sdf = (float *)(sm + 2 * n), *se2f = sdf + n;
+    float *sdl = se2f + n, *se2l = sdl + n;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
       sd[i] = gd[i];
       sdf[i] = (float)gd[i];
+      if (use_smem > 1) sdl[i] = (float)(gd[i] - (double)sdf[i]);
       if (i < n - 1) {
         se2[i] = ge2[i];
         se2f[i] = (float)ge2[i];
+        if (use_smem > 1) se2l[i] = (float)(ge2[i] - (double)se2f[i]);
       }
     }
     __syncthreads();
@@ -131,6 +255,10 @@ k_multisect(const double *gd, const double *ge2, int n, double gl, double gu, do
     e2 = se2;
     df = sdf;
     e2f = se2f;
+    if (use_smem > 1) {
+      dl = sdl;
+      e2l = se2l;
+    }
   }
   const int lane = threadIdx.x & 31;
   const int gwarp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -161,11 +289,39 @@ k_multisect(const double *gd, const double *ge2, int n, double gl, double gu, do
     const double margin = 64.0 * (double)FLT_EPSILON * tnorm;
     lo = fmax(gl, (double)flo - margin);
     hi = fmin(gu, (double)fhi + margin);
+    if (dl) {
+      /* float-float phase: the same multisection with x_j = lo + (hi - lo) j / (P+1) formed
+       * identically for a point and for the bracket end it becomes */
+      ff2 glo = ff_from_double(lo), ghi = ff_from_double(hi);
+      const float fpiv = fmaxf((float)pivmin, 1e-30f);
+      const float ftol2 = (float)(1e-12 * tnorm);
+      for (int it = 0; it < 64; ++it) {
+        const ff2 wdt = ff_add(ghi, ff_neg(glo));
+        if (!(wdt.h > ftol2)) break;
+        const ff2 x = ff_fma(wdt, ff_make((float)(sub + 1) / (float)(P + 1), 0.f), glo);
+        const bool inside = ff_add(x, ff_neg(glo)).h > 0.f && ff_add(ghi, ff_neg(x)).h > 0.f;
+        const int flag = inside ? (sturm_count_ff(df, dl, e2f, e2l, n, x, fpiv) > k)
+                                : (ff_add(x, ff_neg(ghi)).h >= 0.f);
+        const unsigned b = (__ballot_sync(gmask, flag) >> gshift) & gbits;
+        const int first = b ? __ffs(b) - 1 : P;
+        const ff2 nlo =
+            first == 0 ? glo : ff_fma(wdt, ff_make((float)first / (float)(P + 1), 0.f), glo);
+        const ff2 nhi =
+            first == P ? ghi : ff_fma(wdt, ff_make((float)(first + 1) / (float)(P + 1), 0.f), glo);
+        if (!(ff_add(nhi, ff_neg(nlo)).h < wdt.h)) break;
+        glo = nlo;
+        ghi = nhi;
+      }
+      const double margin2 = 64.0 * 0x1p-44 * tnorm;
+      lo = fmax(gl, ff_to_double(glo) - margin2);
+      hi = fmin(gu, ff_to_double(ghi) + margin2);
+    }
     int ok = 1;
     if (sub < 2) {
       const double x = sub == 0 ? lo : hi;
       const int c = sturm_count_bits(d, e2, n, x, pivmin);
       ok = sub == 0 ? (c <= k) : (c > k);
+      if (P == 1) ok = ok && sturm_count_bits(d, e2, n, hi, pivmin) > k; /* one lane: both ends */
     }
     const unsigned bad = (__ballot_sync(gmask, !ok) >> gshift) & gbits;
     if (bad) {
@@ -285,95 +441,6 @@ __device__ __forceinline__ double tr_block_sum(double v, double *red)
   __syncthreads();
   return s;
 }
-
-/*
- * Float-float arithmetic: a value is an unevaluated sum h + l of two FP32 numbers (about 46
- * significant bits), built from the error-free transformations TwoSum (Knuth) and TwoProd
- * with FMA (Dekker / Ogita-Rump-Oishi 2005).  GB300's FP64 pipe issues about 2 FMAs per clock
- * per SM and its FP32 pipe 128, so the tridiagonalisation keeps its trailing matrix and
- * vectors in this form; every operation below is explicitly rounded (no contraction).
- */
-struct ff2 {
-  float h, l;
-};
-
-__device__ __forceinline__ ff2 ff_make(float h, float l)
-{
-  ff2 r;
-  r.h = h;
-  r.l = l;
-  return r;
-}
-__device__ __forceinline__ ff2 ff_from_double(double x)
-{
-  const float h = __double2float_rn(x);
-  return ff_make(h, __double2float_rn(x - (double)h));
-}
-__device__ __forceinline__ double ff_to_double(ff2 a) { return (double)a.h + (double)a.l; }
-__device__ __forceinline__ ff2 ff_neg(ff2 a) { return ff_make(-a.h, -a.l); }
-/* a + b */
-__device__ __forceinline__ ff2 ff_add(ff2 a, ff2 b)
-{
-  const float s = __fadd_rn(a.h, b.h);
-  const float bb = __fsub_rn(s, a.h);
-  float err = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(b.h, bb));
-  err = __fadd_rn(err, __fadd_rn(a.l, b.l));
-  const float h = __fadd_rn(s, err);
-  return ff_make(h, __fsub_rn(err, __fsub_rn(h, s)));
-}
-/* a * b */
-__device__ __forceinline__ ff2 ff_mul(ff2 a, ff2 b)
-{
-  const float p = __fmul_rn(a.h, b.h);
-  float e = __fmaf_rn(a.h, b.h, -p);
-  e = __fmaf_rn(a.h, b.l, e);
-  e = __fmaf_rn(a.l, b.h, e);
-  const float h = __fadd_rn(p, e);
-  return ff_make(h, __fsub_rn(e, __fsub_rn(h, p)));
-}
-/* a * b + c */
-__device__ __forceinline__ ff2 ff_fma(ff2 a, ff2 b, ff2 c)
-{
-  const float p = __fmul_rn(a.h, b.h);
-  float pe = __fmaf_rn(a.h, b.h, -p);
-  pe = __fmaf_rn(a.h, b.l, pe);
-  pe = __fmaf_rn(a.l, b.h, pe);
-  const float s = __fadd_rn(c.h, p);
-  const float bb = __fsub_rn(s, c.h);
-  float err = __fadd_rn(__fsub_rn(c.h, __fsub_rn(s, bb)), __fsub_rn(p, bb));
-  err = __fadd_rn(err, __fadd_rn(c.l, pe));
-  const float h = __fadd_rn(s, err);
-  return ff_make(h, __fsub_rn(err, __fsub_rn(h, s)));
-}
-__device__ __forceinline__ ff2 ff_shfl_xor(ff2 a, int o)
-{
-  return ff_make(__shfl_xor_sync(0xFFFFFFFFu, a.h, o), __shfl_xor_sync(0xFFFFFFFFu, a.l, o));
-}
-__device__ __forceinline__ ff2 ff_load(const double *p)
-{
-  const float2 v = *reinterpret_cast<const float2 *>(p);
-  return ff_make(v.x, v.y);
-}
-__device__ __forceinline__ void ff_store(double *p, ff2 a)
-{
-  *reinterpret_cast<float2 *>(p) = make_float2(a.h, a.l);
-}
-
-/* sqrt(a) for a > 0: FP32 root plus one correction, (a - s^2) / 2s */
-__device__ __forceinline__ ff2 ff_sqrt(ff2 a)
-{
-  const float s = sqrtf(a.h);
-  const ff2 r = ff_fma(ff_make(-s, 0.f), ff_make(s, 0.f), a);
-  return ff_add(ff_make(s, 0.f), ff_make(__fdiv_rn(r.h, 2.f * s), 0.f));
-}
-/* a / b: FP32 quotient plus one correction from the float-float remainder */
-__device__ __forceinline__ ff2 ff_div(ff2 a, ff2 b)
-{
-  const float q1 = __fdiv_rn(a.h, b.h);
-  const ff2 r = ff_fma(ff_neg(b), ff_make(q1, 0.f), a);
-  return ff_add(ff_make(q1, 0.f), ff_make(__fdiv_rn(r.h, b.h), 0.f));
-}
-__device__ __forceinline__ ff2 ff_scale(ff2 a, float s) { return ff_make(a.h * s, a.l * s); }
 
 /* sum of the G float-float block partials in a fixed order (warp 0), broadcast */
 __device__ __forceinline__ ff2 ff_sum_partials(const double *part, int G, ff2 *slot)
@@ -669,15 +736,21 @@ __device__ __forceinline__ double start_entry(int j, int i)
   return ((double)(z >> 11) * (1.0 / 9007199254740992.0)) * 2.0 - 1.0;
 }
 
+/* block sum (fixed order: warp shuffles, then warp 0 over the warps' sums), broadcast to
+ * every thread; red holds at least one double per warp */
 __device__ double block_sum(double v, double *red)
 {
-  red[threadIdx.x] = v;
+  for (int o = 16; o; o >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
   __syncthreads();
-  for (int o = blockDim.x / 2; o; o >>= 1) {
-    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
-    __syncthreads();
+  if (threadIdx.x < 32) {
+    const int nw = blockDim.x >> 5;
+    double t = (int)threadIdx.x < nw ? red[threadIdx.x] : 0.0;
+    for (int o = 16; o; o >>= 1) t += __shfl_down_sync(0xFFFFFFFFu, t, o);
+    if (threadIdx.x == 0) red[32] = t;
   }
-  double r = red[0];
+  __syncthreads();
+  const double r = red[32];
   __syncthreads();
   return r;
 }
@@ -1128,8 +1201,12 @@ int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, d
                            ctx->stream));
   GP_EIG_MARK(2);
   {
-    size_t smem = (size_t)24 * (size_t)n;
-    int use_smem = smem <= 200 * 1024;
+    size_t smem = (size_t)32 * (size_t)n;
+    int use_smem = 2;
+    if (smem > 200 * 1024) {
+      smem = (size_t)24 * (size_t)n;
+      use_smem = smem <= 200 * 1024 ? 1 : 0;
+    }
     const int warps = ctx->num_sms * 4;
     int epw = (n + warps - 1) / warps;
     if (epw > 32) epw = 32;
@@ -1158,7 +1235,7 @@ int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, d
         d, e, n, w, nvec, tnorm, d_vecs, iw, ii_in_smem);
     GP_LAUNCH_CHECK(ctx, "k_inverse_iteration");
     GP_EIG_MARK(5);
-    k_mgs<<<1, 256, 0, ctx->stream>>>(d_vecs, n, nvec);
+    k_mgs<<<1, 1024, 0, ctx->stream>>>(d_vecs, n, nvec);
     GP_LAUNCH_CHECK(ctx, "k_mgs");
     GP_EIG_MARK(6);
     /* Z := Q Z: the cooperative WY kernel when its row slab fits shared memory, else

@@ -760,31 +760,46 @@ __device__ double block_sum(double v, double *red)
  * The LU factorisation with partial pivoting of T - lam I and the solves are sequential
  * recurrences run by thread 0 with the running values carried in registers (the arrays are
  * only written, or read ahead of the dependency chain); the other threads normalise.
- * work: per vector 6n doubles.  Z [nvec][n] (column-major N x nvec).
+ * With in_smem, the factors, the iterate and (during the factorisation) d and e sit in shared
+ * memory, 41 n bytes, so that the recurrences wait on shared-memory rather than L2 latency:
+ * d is staged where the iterate goes later and e where the second superdiagonal of U is
+ * written, each e(i) being read before DU2(i) overwrites it.  Otherwise work holds the
+ * factors (per vector 6n doubles) and the iterate stays in Z.
+ * Z [nvec][n] (column-major N x nvec).
  */
-__global__ void k_inverse_iteration(const double *d, const double *e, int n, const double *w,
-                                    int nvec, double tnorm, double *Z, double *work, int in_smem)
+__global__ void k_inverse_iteration(const double *__restrict__ d, const double *__restrict__ e,
+                                    int n, const double *__restrict__ w, int nvec, double tnorm,
+                                    double *Z, double *work, int in_smem)
 {
   __shared__ double red[256];
   extern __shared__ double ii_sm[];
   const int j = blockIdx.x;
   if (j >= nvec) return;
-  /* the factors in shared memory when they fit (in_smem), so that the sequential recurrences
-   * of thread 0 wait on shared-memory rather than L2 latency */
   double *base = in_smem ? ii_sm : work + (int64_t)j * 6 * n;
   double *Dinv = base, *DL = base + n, *DU = base + 2 * n, *DU2 = base + 3 * n;
-  double *x = Z + (int64_t)j * n;
-  int *piv = (int *)(base + 4 * n);
+  double *xg = Z + (int64_t)j * n;
+  double *x = in_smem ? base + 4 * n : xg;
+  uint8_t *piv = (uint8_t *)(base + 5 * n);
+  const double *dd = d, *ee = e;
+  if (in_smem) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      x[i] = d[i];
+      if (i < n - 1) DU2[i] = e[i];
+    }
+    __syncthreads();
+    dd = x;
+    ee = DU2;
+  }
   const double lam = w[n - 1 - j];
   const double tiny = DBL_EPSILON * tnorm;
   if (threadIdx.x == 0) {
     /* dgttrf-style elimination; cur = running diagonal of row i, du = its superdiagonal */
-    double cur = d[0] - lam;
-    double du = n > 1 ? e[0] : 0.0;
+    double cur = dd[0] - lam;
+    double du = n > 1 ? ee[0] : 0.0;
     for (int i = 0; i < n - 1; ++i) {
-      double ei = e[i];
-      double dn = d[i + 1] - lam;                    /* row i+1 diagonal */
-      double en = (i < n - 2) ? e[i + 1] : 0.0;      /* row i+1 superdiagonal */
+      const double ei = ee[i];
+      const double dn = dd[i + 1] - lam;               /* row i+1 diagonal */
+      const double en = (i < n - 2) ? ee[i + 1] : 0.0; /* row i+1 superdiagonal */
       if (fabs(cur) >= fabs(ei)) {
         if (cur == 0.0) cur = tiny;
         double f = ei / cur;
@@ -809,6 +824,7 @@ __global__ void k_inverse_iteration(const double *d, const double *e, int n, con
     if (cur == 0.0) cur = tiny;
     Dinv[n - 1] = 1.0 / cur;
   }
+  __syncthreads();
   for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = start_entry(j, i);
   __syncthreads();
   for (int iter = 0; iter < 3; ++iter) {
@@ -848,7 +864,7 @@ __global__ void k_inverse_iteration(const double *d, const double *e, int n, con
   for (int i = threadIdx.x; i < n; i += blockDim.x) s2 += x[i] * x[i];
   s2 = block_sum(s2, red);
   double inv = 1.0 / sqrt(s2);
-  for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] *= inv;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) xg[i] = x[i] * inv;
 }
 
 /* modified Gram-Schmidt over the nvec vectors, in order (one block) */
@@ -1226,8 +1242,11 @@ int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, d
   GP_LAUNCH_CHECK(ctx, "k_reverse");
   GP_EIG_MARK(3);
   if (nvec > 0) {
-    const size_t ii_smem = (size_t)n * (4 * sizeof(double) + sizeof(int)) + 16;
-    const int ii_in_smem = ii_smem <= 200 * 1024;
+    /* factors, iterate and byte pivots: 41 n bytes */
+    const size_t ii_smem = (size_t)n * (5 * sizeof(double) + 1) + 16;
+    int smem_optin = 0;
+    cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
+    const int ii_in_smem = ii_smem + 2048 <= (size_t)smem_optin;
     if (ii_in_smem)
       GP_CUDA(ctx, cudaFuncSetAttribute(k_inverse_iteration,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ii_smem));

@@ -251,22 +251,28 @@ extern "C" int gp_set_snps(gp_ctx *ctx, const int32_t *snp_index, int32_t ncols)
 __global__ void k_snp_valid(const uint8_t *geno, int64_t rlen_dev, int64_t nsnp,
                             const uint32_t *mask, const uint8_t *snp_use, int32_t *out)
 {
+  /* 16-byte words (rlen_dev and the mask are 16-byte aligned) */
   int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   int64_t nw = (int64_t)gridDim.x * blockDim.x >> 5;
-  int64_t words = rlen_dev >> 2;
+  int64_t words4 = rlen_dev >> 4;
+  const uint4 *m4 = (const uint4 *)mask;
   for (int64_t s = warp; s < nsnp; s += nw) {
     if (snp_use && !snp_use[s]) {
       if (lane == 0) out[s] = 0;
       continue;
     }
-    const uint32_t *rec = (const uint32_t *)(geno + s * rlen_dev);
+    const uint4 *rec = (const uint4 *)(geno + s * rlen_dev);
     int32_t cnt = 0;
-    for (int64_t i = lane; i < words; i += 32) {
-      uint32_t w = __ldg(rec + i), m = __ldg(mask + i);
-      uint32_t sel = m & 0x55555555u;
-      uint32_t miss = (w >> 1) & w & 0x55555555u;
-      cnt += __popc(sel) - __popc(miss & sel);
+    for (int64_t i = lane; i < words4; i += 32) {
+      const uint4 w = __ldg(rec + i), m = __ldg(m4 + i);
+      const uint32_t wv[4] = {w.x, w.y, w.z, w.w}, mv[4] = {m.x, m.y, m.z, m.w};
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const uint32_t sel = mv[q] & 0x55555555u;
+        const uint32_t miss = (wv[q] >> 1) & wv[q] & 0x55555555u;
+        cnt += __popc(sel) - __popc(miss & sel);
+      }
     }
     for (int o = 16; o; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
     if (lane == 0) out[s] = cnt;
@@ -274,7 +280,10 @@ __global__ void k_snp_valid(const uint8_t *geno, int64_t rlen_dev, int64_t nsnp,
 }
 
 /* per sample: number of non-missing genotypes over the used SNPs.  Thread = one word of
- * 16 samples, looping over a slice of SNPs; partial counts are summed with atomics. */
+ * 16 samples, looping over a slice of SNPs eight records at a time (loads first; an unused
+ * SNP reads as all-missing); the observed bits are summed in 4-bit fields of two words
+ * (fields 0, 2, .. and 1, 3, ..), flushed into per-sample counts every 15 SNPs; partial
+ * counts are summed with atomics. */
 __global__ void k_sample_valid(const uint8_t *geno, int64_t rlen_dev, int64_t nsnp,
                                const uint8_t *snp_use, int32_t nind, int32_t *out,
                                int64_t snps_per_slice)
@@ -287,16 +296,37 @@ __global__ void k_sample_valid(const uint8_t *geno, int64_t rlen_dev, int64_t ns
   int32_t cnt[16];
 #pragma unroll
   for (int j = 0; j < 16; ++j) cnt[j] = 0;
-  for (int64_t s = s0; s < s1; ++s) {
-    if (snp_use && !snp_use[s]) continue;
-    uint32_t v = __ldg((const uint32_t *)(geno + s * rlen_dev) + w);
-    uint32_t ok = ~((v >> 1) & v) & 0x55555555u;
+  uint32_t acc_a = 0, acc_b = 0;
+  int pend = 0;
+  auto flush = [&]() {
 #pragma unroll
-    for (int j = 0; j < 16; ++j) {
-      /* sample j of the word: byte j>>2, bits (3-(j&3))*2 */
-      cnt[j] += (ok >> ((j >> 2) * 8 + (3 - (j & 3)) * 2)) & 1u;
+    for (int f = 0; f < 16; ++f) {
+      /* field f (bits 2f, 2f+1) is sample (f >> 2) * 4 + 3 - (f & 3) of the word */
+      const uint32_t v = ((f & 1) ? acc_b : acc_a) >> (4 * (f >> 1));
+      cnt[(f >> 2) * 4 + 3 - (f & 3)] += (int32_t)(v & 0xFu);
+    }
+    acc_a = acc_b = 0;
+    pend = 0;
+  };
+  const uint32_t *col = (const uint32_t *)geno + w;
+  const int64_t stride = rlen_dev >> 2;
+  for (int64_t s = s0; s < s1; s += 8) {
+    uint32_t v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int64_t su = s + u;
+      v[u] = su < s1 ? __ldg(col + su * stride) : 0xFFFFFFFFu;
+      if (snp_use && su < s1 && !snp_use[su]) v[u] = 0xFFFFFFFFu;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const uint32_t ok = ~((v[u] >> 1) & v[u]) & 0x55555555u;
+      acc_a += ok & 0x11111111u;
+      acc_b += (ok >> 2) & 0x11111111u;
+      if (++pend == 15) flush();
     }
   }
+  flush();
 #pragma unroll
   for (int j = 0; j < 16; ++j) {
     int64_t k = w * 16 + j;
@@ -315,10 +345,11 @@ extern "C" int gp_valid_counts(gp_ctx *ctx, const uint8_t *sample_use, const uin
   uint8_t *base;
   int rc = gp_scratch(ctx, need, (void **)&base);
   if (rc) return rc;
-  int32_t *d_sv = (int32_t *)base;
+  /* the mask first: 16-byte aligned for k_snp_valid's vector loads */
+  uint32_t *d_mask = (uint32_t *)base;
+  int32_t *d_sv = (int32_t *)(d_mask + nwords);
   int32_t *d_iv = d_sv + nsnp;
-  uint32_t *d_mask = (uint32_t *)(d_iv + ctx->nind_all);
-  uint8_t *d_su = (uint8_t *)(d_mask + nwords);
+  uint8_t *d_su = (uint8_t *)(d_iv + ctx->nind_all);
   uint8_t *d_pu = d_su + nsnp;
   if (snp_use)
     GP_CUDA(ctx, gp_memcpy(ctx, d_su, snp_use, (size_t)nsnp, cudaMemcpyHostToDevice,
@@ -372,17 +403,24 @@ __global__ void k_snp_stats(const uint8_t *__restrict__ geno, int64_t rlen_dev,
   int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  int64_t words = rlen_dev >> 2;
+  /* 16-byte words (rlen_dev and the row mask are 16-byte aligned) */
+  int64_t words4 = rlen_dev >> 4;
+  const uint4 *m4 = (const uint4 *)rowmask;
   for (int64_t c = warp; c < ncols; c += nw) {
-    const uint32_t *rec = (const uint32_t *)(geno + (int64_t)cols[c] * rlen_dev);
+    const uint4 *rec = (const uint4 *)(geno + (int64_t)cols[c] * rlen_dev);
     int32_t sumg = 0, nmiss = 0;
-    for (int64_t i = lane; i < words; i += 32) {
-      uint32_t w = __ldg(rec + i), sel = __ldg(rowmask + i) & 0x55555555u;
-      uint32_t hi = (w >> 1) & 0x55555555u, lo = w & 0x55555555u;
-      uint32_t miss = hi & lo & sel;
-      uint32_t obs = sel & ~miss;
-      sumg += 2 * __popc(hi & obs) + __popc(lo & obs);
-      nmiss += __popc(miss);
+    for (int64_t i = lane; i < words4; i += 32) {
+      const uint4 w4 = __ldg(rec + i), s4 = __ldg(m4 + i);
+      const uint32_t wv[4] = {w4.x, w4.y, w4.z, w4.w}, sv[4] = {s4.x, s4.y, s4.z, s4.w};
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const uint32_t w = wv[q], sel = sv[q] & 0x55555555u;
+        const uint32_t hi = (w >> 1) & 0x55555555u, lo = w & 0x55555555u;
+        const uint32_t miss = hi & lo & sel;
+        const uint32_t obs = sel & ~miss;
+        sumg += 2 * __popc(hi & obs) + __popc(lo & obs);
+        nmiss += __popc(miss);
+      }
     }
     for (int off = 16; off; off >>= 1) {
       sumg += __shfl_down_sync(0xffffffffu, sumg, off);

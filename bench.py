@@ -500,6 +500,8 @@ def run_gpu(args, cfg, world, rank, local, dist):
     clocks.start()
     times = []
     gram_ms = []
+    tri_ms = []
+    tri_n = 0
     total_flops = 0.0
     h.launch_count(reset=True)
     for _ in range(args.steps):
@@ -509,6 +511,8 @@ def run_gpu(args, cfg, world, rank, local, dist):
         times.append(ms)
         g_ms, g_launch, g_flops = h.last_gram_time()
         gram_ms.append(g_ms)
+        t_ms, tri_n = h.last_tridiag_time()
+        tri_ms.append(t_ms)
         total_flops = r["gram_flops"]
     clk = clocks.stop()
     launches = h.launch_count(reset=True) / max(1, args.steps)
@@ -543,6 +547,7 @@ def run_gpu(args, cfg, world, rank, local, dist):
     h.close()
     peaks, peak_kind = load_peaks()
     res = dict(step_ms=step_ms, gram_flops=total_flops, gram_ms=g_ms, gram_launches=g_launch,
+               tridiag_ms=float(np.mean(tri_ms)) if tri_ms else 0.0, tridiag_n=tri_n,
                gram_kernel_flops=g_flops, clocks=clk, e2e_ms=e2e_ms, h2d=h2d / n_e2e,
                d2h=d2h / n_e2e, run=r, gen_s=gen_s, peaks=peaks, peak_kind=peak_kind,
                nind=nind, launches=launches, acc=acc, serving=serving)
@@ -769,6 +774,37 @@ def cpu_reference_sample(cfg, seconds_target=12.0, nthreads=None):
     return flops / dt / 1e12, nthreads, dt, m2, nind
 
 
+def tridiag_traffic(n):
+    """DRAM bytes of one k_tridiag launch of order n from the committed ncu summary
+    (profiles/tridiag_ff_5000_dram.md), or None for other orders"""
+    path = os.path.join(ROOT, "profiles", "tridiag_ff_5000_dram.md")
+    if n != 5000 or not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.strip().startswith("traffic_bytes_per_launch:"):
+            return int(line.split(":")[1])
+    return None
+
+
+def tridiag_roofline(res, peaks, peak_kind):
+    """roofline of the step's dominant kernel, the float-float tridiagonalisation: HBM-bound;
+    algorithmic bytes = LAPACK dsytd2's fused symv + syr2 pass, which reads and writes the
+    trailing lower triangle once per column step (8-byte elements):
+    sum over m = 1 .. n-1 of 8 m (m + 1) = 8 (n-1) n (n+1) / 3 bytes per launch"""
+    n, ms = res.get("tridiag_n", 0), res.get("tridiag_ms", 0.0)
+    if not n or ms <= 0.0:
+        return None
+    alg = 8.0 * (n - 1) * n * (n + 1) / 3.0
+    achieved = alg / (ms * 1e-3) / 1e9
+    peak = peaks.get("hbm_gbs", 6800.0)
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": tridiag_traffic(n),
+            "kernel": "k_tridiag (float-float Householder tridiagonalisation, order %d, one "
+                      "cooperative launch; %.1f ms by CUDA events)" % (n, ms),
+            "algorithmic_bytes": alg,
+            "peak_kind": "HBM copy, %s" % peak_kind}
+
+
 def gram_traffic(args):
     """DRAM bytes per launch of the split Gram kernel from the committed ncu summary of the
     full workload (profiles/gram_split_fp16_full_dram.md, one-CTA schedule), or None for other
@@ -939,7 +975,8 @@ def main():
             "phases_s": {k: round(v, 4) for k, v in r["t_phase"].items()},
             "passes": r["npasses"], "outliers": len(r["outliers"]),
             "gram_kernel_ms": res["gram_ms"],
-            "roofline": roof, "clocks": res["clocks"],
+            "roofline": tridiag_roofline(res, peaks, res["peak_kind"]) or roof,
+            "roofline_gram": roof, "clocks": res["clocks"],
             "e2e": {"value": e2e, "unit": "TFLOP/s", "h2d_bytes_per_step": int(res["h2d"]),
                     "d2h_bytes_per_step": int(res["d2h"]), "wall_s": res["e2e_ms"] / 1e3},
             "accuracy_vs_fp64": res["acc"], "serving": res["serving"],

@@ -148,6 +148,8 @@ extern "C" int gp_open(int device, gp_ctx **out)
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_t0);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_t1);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_g0);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_tr0);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_tr1);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_g1);
   if (e != cudaSuccess) {
     gp_fail(NULL, GP_ERR_CUDA, "gp_open: %s", cudaGetErrorString(e));
@@ -181,6 +183,8 @@ extern "C" void gp_close(gp_ctx *ctx)
   if (ctx->ev_t0) cudaEventDestroy(ctx->ev_t0);
   if (ctx->ev_t1) cudaEventDestroy(ctx->ev_t1);
   if (ctx->ev_g0) cudaEventDestroy(ctx->ev_g0);
+  if (ctx->ev_tr0) cudaEventDestroy(ctx->ev_tr0);
+  if (ctx->ev_tr1) cudaEventDestroy(ctx->ev_tr1);
   if (ctx->ev_g1) cudaEventDestroy(ctx->ev_g1);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   free(ctx->h_rows);
@@ -1022,6 +1026,14 @@ extern "C" int gp_timer_stop(gp_ctx *ctx, double *ms)
   float f = 0.f;
   GP_CUDA(ctx, cudaEventElapsedTime(&f, ctx->ev_t0, ctx->ev_t1));
   *ms = f;
+  return GP_OK;
+}
+
+extern "C" int gp_last_tridiag_time(const gp_ctx *ctx, double *ms, int32_t *n)
+{
+  if (!ctx) return GP_ERR_ARG;
+  if (ms) *ms = ctx->tridiag_ms;
+  if (n) *n = ctx->tridiag_n;
   return GP_OK;
 }
 

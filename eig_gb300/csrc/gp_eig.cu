@@ -1164,13 +1164,19 @@ int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, d
       GP_CUDA(ctx, cudaMemsetAsync(phase, 0, 5 * sizeof(unsigned long long), ctx->stream));
     }
     void *args[] = {&A, &nn, &d, &e, &tau, &vbuf, &wbuf, &ybuf, &pd2, &bar, &d_err, &phase};
+    GP_CUDA(ctx, cudaEventRecord(ctx->ev_tr0, ctx->stream));
     GP_CUDA(ctx, cudaLaunchCooperativeKernel((const void *)k_tridiag, dim3((unsigned)G),
                                              dim3(TR_THREADS), args, tr_smem, ctx->stream));
+    GP_CUDA(ctx, cudaEventRecord(ctx->ev_tr1, ctx->stream));
     ctx->launches++;
     int herr = 0;
     GP_CUDA(ctx, gp_memcpy(ctx, &herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (herr) return gp_fail(ctx, GP_ERR_TIMEOUT, "tridiagonalisation grid barrier timed out");
+    float tms = 0.f;
+    GP_CUDA(ctx, cudaEventElapsedTime(&tms, ctx->ev_tr0, ctx->ev_tr1));
+    ctx->tridiag_ms = tms;
+    ctx->tridiag_n = n;
     if (timing) {
       unsigned long long hp[5];
       cudaMemcpy(hp, phase, sizeof hp, cudaMemcpyDeviceToHost);
@@ -1180,6 +1186,8 @@ int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, d
               n, hp[0] * 1e-6, (hp[1] + hp[2]) * 1e-6, hp[2] * 1e-6, hp[4] * 1e-6);
     }
   } else {
+    ctx->tridiag_ms = 0.0;
+    ctx->tridiag_n = n;
     if (cusolverDnDsytrd(h, CUBLAS_FILL_MODE_LOWER, n, ctx->d_xtx, n, d, e, tau, ws, lw,
                          d_info) != CUSOLVER_STATUS_SUCCESS)
       return gp_fail(ctx, GP_ERR_SOLVER, "cusolverDnDsytrd failed to launch");

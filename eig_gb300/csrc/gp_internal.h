@@ -70,6 +70,9 @@ struct gp_ctx {
   int32_t gram_launches;
   double gram_flops;
   double encode_ms;      /* k_encode time of the last device-output gp_encode_records */
+  cudaEvent_t ev_tr0, ev_tr1;
+  double tridiag_ms;     /* k_tridiag time of the last eigensolve (0: cuSOLVER sytrd ran) */
+  int32_t tridiag_n;     /* its order */
 
   /* host<->device bytes copied by the handle (gp_transfer_bytes) */
   int64_t h2d_bytes, d2h_bytes;

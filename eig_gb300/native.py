@@ -30,7 +30,8 @@ EXPORTED = ["gp_version", "gp_last_error", "gp_open", "gp_close", "gp_device_byt
             "gp_set_snps", "gp_xtx", "gp_eigvecs", "gp_ridoutlier", "gp_snp_weights",
             "gp_lsqproj", "gp_fastpca", "gp_smartpca_defaults", "gp_smartpca_run",
             "gp_fail_msg", "gp_genotype_shape", "gp_timer_start", "gp_timer_stop",
-            "gp_last_gram_time", "gp_host_register", "gp_host_unregister",
+            "gp_last_gram_time", "gp_last_tridiag_time", "gp_host_register",
+            "gp_host_unregister",
             "gp_transfer_bytes", "gp_launch_count", "gp_gram_fp64_noalloc",
             "gp_noalloc_last_error", "gp_serve_open", "gp_serve_layout",
             "gp_serve_panel_snps", "gp_serve_submit", "gp_serve_test", "gp_serve_wait",
@@ -122,6 +123,7 @@ def load_library():
         "gp_timer_start": (C.c_int, [vp]),
         "gp_timer_stop": (C.c_int, [vp, f64p]),
         "gp_last_gram_time": (C.c_int, [vp, f64p, i32p, f64p]),
+        "gp_last_tridiag_time": (C.c_int, [vp, f64p, i32p]),
         "gp_host_register": (C.c_int, [vp, C.c_size_t]),
         "gp_host_unregister": (C.c_int, [vp]),
         "gp_transfer_bytes": (C.c_int, [vp, i64p, i64p, C.c_int32]),
@@ -336,6 +338,13 @@ class Handle:
         self.check(self.lib.gp_last_gram_time(self.h, C.byref(ms), C.byref(n), C.byref(fl)),
                    "gp_last_gram_time")
         return ms.value, n.value, fl.value
+
+    def last_tridiag_time(self):
+        """(ms, n) of the last eigensolve's tridiagonalisation kernel (0 ms: cuSOLVER ran)"""
+        ms, n = C.c_double(), C.c_int32()
+        self.check(self.lib.gp_last_tridiag_time(self.h, C.byref(ms), C.byref(n)),
+                   "gp_last_tridiag_time")
+        return ms.value, n.value
 
     def encode_records(self, fmt, snps, samples=None, flip=None, nsamples=None, out=None):
         """convertf's genotype records (gp_encode_records) of the resident panel: SNP list,

@@ -253,6 +253,11 @@ int gp_timer_stop(gp_ctx *ctx, double *ms);
  * count nrows*(nrows+1)*kept_snps of that call. */
 int gp_last_gram_time(const gp_ctx *ctx, double *ms, int32_t *launches, double *flops);
 
+/* Device time of the tridiagonalisation kernel (k_tridiag) of the last eigensolve (CUDA events
+ * around its launch on the handle's stream) and the matrix order; 0 ms when that solve used
+ * cuSOLVER's sytrd instead. */
+int gp_last_tridiag_time(const gp_ctx *ctx, double *ms, int32_t *n);
+
 /* Device time of the k_encode launch of the last gp_encode_records call that wrote to
  * device memory (CUDA events around it on the handle's stream). */
 int gp_last_encode_time(const gp_ctx *ctx, double *ms);

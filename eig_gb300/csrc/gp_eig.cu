@@ -1225,9 +1225,11 @@ int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, d
                            ctx->stream));
   GP_EIG_MARK(2);
   {
+    /* GP_EIG_NO_FF=1 selects the path without the float-float phase (as for N > 6,400) */
+    const char *ffenv = getenv("GP_EIG_NO_FF");
     size_t smem = (size_t)32 * (size_t)n;
     int use_smem = 2;
-    if (smem > 200 * 1024) {
+    if (smem > 200 * 1024 || (ffenv && ffenv[0] == '1')) {
       smem = (size_t)24 * (size_t)n;
       use_smem = smem <= 200 * 1024 ? 1 : 0;
     }
@@ -1254,7 +1256,9 @@ int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, d
     const size_t ii_smem = (size_t)n * (5 * sizeof(double) + 1) + 16;
     int smem_optin = 0;
     cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
-    const int ii_in_smem = ii_smem + 2048 <= (size_t)smem_optin;
+    /* GP_EIG_II_GLOBAL=1 selects the global-memory path (as for N > 5,600) */
+    const char *iienv = getenv("GP_EIG_II_GLOBAL");
+    const int ii_in_smem = ii_smem + 2048 <= (size_t)smem_optin && !(iienv && iienv[0] == '1');
     if (ii_in_smem)
       GP_CUDA(ctx, cudaFuncSetAttribute(k_inverse_iteration,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ii_smem));

@@ -356,10 +356,15 @@ def test_smartpca_run_split_fp16_vs_reference(gpu, case):
     compare_coords(c.ref_coords, mine, 2, 1e-4)
 
 
-def test_eig_tridiag_all_values_top_vectors(gpu):
+@pytest.mark.parametrize("path", ["default", "GP_EIG_NO_FF", "GP_EIG_II_GLOBAL"])
+def test_eig_tridiag_all_values_top_vectors(gpu, monkeypatch, path):
     """sytrd + bisection + inverse iteration + ormtr: every eigenvalue within 1e-12 of the
     largest against LAPACK (numpy eigh), 24 top eigenvectors with small residuals, orthonormal,
-    and equal (up to sign) to LAPACK's where the eigenvalues are separated"""
+    and equal (up to sign) to LAPACK's where the eigenvalues are separated; also through the
+    multisection without its float-float phase and the inverse iteration with its factors in
+    global memory (the paths of larger N)"""
+    if path != "default":
+        monkeypatch.setenv(path, "1")
     rec, pop = synth(6000, [500, 400, 300], [0.01, 0.02, 0.04], miss=0.02, seed=27)
     nind = len(pop)
     gpu.load_genotypes(rec, nind)
@@ -436,3 +441,4 @@ def test_split_gram_clusters_equal_single_ctas(gpu, monkeypatch, nind):
         grams[cl] = _gram_pair(gpu, rec, nind, rows, cols, native.GP_PREC_SPLIT_FP16)["XTX"]
     assert np.array_equal(grams["4"], grams["1"])
     assert np.array_equal(grams["2"], grams["1"])
+

@@ -457,16 +457,18 @@ __device__ __forceinline__ ff2 ff_sum_partials(const double *part, int G, ff2 *s
   return r;
 }
 
-/* block sum of one float-float per thread (fixed order), as float-float in thread 0 */
+/* block sum of one float-float per thread (fixed order: warp shuffles, then warp 0's
+ * shuffle tree over the warps' sums), as float-float in thread 0 */
 __device__ __forceinline__ ff2 ff_block_sum2(ff2 v, ff2 *red)
 {
+  static_assert(TR_WARPS == 32, "one warp sums the warps' partials");
   for (int o = 16; o; o >>= 1) v = ff_add(v, ff_shfl_xor(v, o));
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
   __syncthreads();
   ff2 t = ff_make(0.f, 0.f);
-  if (threadIdx.x == 0) {
-    t = red[0];
-    for (int w = 1; w < TR_WARPS; ++w) t = ff_add(t, red[w]);
+  if (threadIdx.x < 32) {
+    t = red[threadIdx.x];
+    for (int o = 16; o; o >>= 1) t = ff_add(t, ff_shfl_xor(t, o));
   }
   __syncthreads();
   return t;
@@ -550,8 +552,16 @@ k_tridiag(double *A, int n, double *d, double *e, double *tau, double *vbuf, dou
     double *ycur = ybuf + (int64_t)(c & 1) * n, *yprev = ybuf + (int64_t)((c + 1) & 1) * n;
     if (threadIdx.x == 32) st.b1_u0 = (int)(((int64_t)m * b) / G);
     if (threadIdx.x == 33) st.b1_u1 = (int)(((int64_t)m * (b + 1)) / G);
-    /* loads first (v_p needs only step c-1's scale; y is kept raw in swp for now), so that
-     * they overlap the reduction of the previous step's partial dots */
+    /* the block partials of y.v of step c-1 (double buffer: blocks already in step c+1 write
+     * the other half), loaded by the last warp ahead of the vector loads so that the two
+     * latencies overlap; summed per lane in order, then by a fixed shuffle tree */
+    ff2 pacc = ZERO;
+    if (have_p && warp == TR_WARPS - 1) {
+      const double *pprev = part_dot2 + (size_t)((c + 1) & 1) * G;
+#pragma unroll 4
+      for (int g = lane; g < G; g += 32) pacc = ff_add(pacc, ff_load(pprev + g));
+    }
+    /* loads (v_p needs only step c-1's scale; y is kept raw in swp for now) */
 #pragma unroll 4
     for (int q = c + threadIdx.x; q < n; q += blockDim.x) {
       ff2 vp = ZERO, yq = ZERO;
@@ -564,9 +574,12 @@ k_tridiag(double *A, int n, double *d, double *e, double *tau, double *vbuf, dou
       ff_store(svc + q, ff_load(A + (int64_t)c * n + q));
     }
     if (have_p) {
-      /* the block partials of y.v of step c-1 (double buffer: blocks already in step c+1
-       * write the other half) */
-      const ff2 dsum = ff_sum_partials(part_dot2 + (size_t)((c + 1) & 1) * G, G, &s_slotf);
+      if (warp == TR_WARPS - 1) {
+        for (int o = 16; o; o >>= 1) pacc = ff_add(pacc, ff_shfl_xor(pacc, o));
+        if (lane == 0) s_slotf = pacc;
+      }
+      __syncthreads();
+      const ff2 dsum = s_slotf;
       if (threadIdx.x == 0) {
         st.alpha_pf = ff_scale(ff_mul(ff_mul(tau_pf, tau_pf), dsum), -0.5f);
         st.wpc = ff_fma(tau_pf, ff_load(swp + c), st.alpha_pf); /* w_p(c); v_p(c) = 1 */

@@ -151,6 +151,7 @@ extern "C" int gp_set_missing(gp_ctx *ctx, const int64_t *pairs, int64_t npairs)
   k_set_missing<<<grid_for(ctx, npairs, 256), 256, 0, ctx->stream>>>(
       ctx->d_geno, ctx->rlen_dev, d_pairs, npairs, ctx->nsnp_all, ctx->nind_all);
   GP_LAUNCH_CHECK(ctx, "k_set_missing");
+  ctx->codes4_rows = 0;
   ctx->xtx_valid = ctx->eig_valid = ctx->weights_valid = 0;
   GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return GP_OK;

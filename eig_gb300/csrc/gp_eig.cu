@@ -380,20 +380,32 @@ k_multisect(const double *gd, const double *ge2, int n, double gl, double gu, do
 #define TR_B1_SLOTS 256 /* segment dots of one block in the column pass */
 #define TR_ERR_BARRIER 11
 
+/* arrival with release semantics at GPU scope (the block's writes, ordered before it by the
+ * block barrier, become visible to a block that acquires the count) */
+__device__ __forceinline__ void red_release_gpu(unsigned *p, unsigned v)
+{
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned *p)
+{
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
 /* grid barrier on a monotonic arrival counter: the k-th barrier of the launch waits until
- * k * gridDim.x blocks have arrived (one atomic per block, no reset) */
+ * k * gridDim.x blocks have arrived (one release-add per block, acquire loads while
+ * waiting, no reset) */
 __device__ __forceinline__ bool tr_grid_sync(unsigned *count, unsigned target, int *err)
 {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
-    volatile unsigned *vcount = count;
     volatile int *verr = err;
-    __threadfence();
-    atomicAdd(count, 1u);
+    red_release_gpu(count, 1u);
     const uint64_t t0 = globaltimer_ns();
-    for (unsigned it = 1; *vcount < target; ++it) {
+    for (unsigned it = 1; ld_acquire_gpu(count) < target; ++it) {
       if ((it & 63u) == 0) {
         if (*verr) {
           ok = 0;
@@ -406,7 +418,6 @@ __device__ __forceinline__ bool tr_grid_sync(unsigned *count, unsigned target, i
         }
       }
     }
-    __threadfence();
     if (*verr) ok = 0;
     s_ok = ok;
   }
@@ -502,7 +513,7 @@ __global__ void k_tri_to_ff(double *A, int n)
 /* per-step scalars, computed once per block by thread 0 (GB300's FP64 pipe is narrow, so
  * scalar square roots and divisions are not repeated by every thread) */
 struct tr_step {
-  ff2 alpha_pf, wpc, beta, tau_c, scale_c;
+  ff2 beta, tau_c, scale_c;
   int b1_u0, b1_u1;
 };
 
@@ -573,23 +584,19 @@ k_tridiag(double *A, int n, double *d, double *e, double *tau, double *vbuf, dou
       ff_store(swp + q, yq);
       ff_store(svc + q, ff_load(A + (int64_t)c * n + q));
     }
-    if (have_p) {
-      if (warp == TR_WARPS - 1) {
-        for (int o = 16; o; o >>= 1) pacc = ff_add(pacc, ff_shfl_xor(pacc, o));
-        if (lane == 0) s_slotf = pacc;
-      }
-      __syncthreads();
-      const ff2 dsum = s_slotf;
-      if (threadIdx.x == 0) {
-        st.alpha_pf = ff_scale(ff_mul(ff_mul(tau_pf, tau_pf), dsum), -0.5f);
-        st.wpc = ff_fma(tau_pf, ff_load(swp + c), st.alpha_pf); /* w_p(c); v_p(c) = 1 */
-      }
-    } else if (threadIdx.x == 0) {
-      st.wpc = ZERO;
+    if (have_p && warp == TR_WARPS - 1) {
+      for (int o = 16; o; o >>= 1) pacc = ff_add(pacc, ff_shfl_xor(pacc, o));
+      if (lane == 0) s_slotf = pacc;
     }
-    __syncthreads();
+    __syncthreads(); /* publishes the partial sum and svp, swp, svc */
+    ff2 wpc = ZERO, alpha_pf = ZERO;
+    if (have_p) {
+      /* every thread forms alpha and w_p(c) of step c-1 from the same values */
+      const ff2 dsum = s_slotf;
+      alpha_pf = ff_scale(ff_mul(ff_mul(tau_pf, tau_pf), dsum), -0.5f);
+      wpc = ff_fma(tau_pf, ff_load(swp + c), alpha_pf); /* w_p(c); v_p(c) = 1 */
+    }
     {
-      const ff2 wpc = st.wpc, alpha_pf = st.alpha_pf;
       const int cnt = n - c, per = (cnt + G - 1) / G;
       const int r0 = c + b * per, r1 = min(n, r0 + per);
       ff2 nrm = ZERO;

@@ -210,6 +210,7 @@ extern "C" int gp_release(gp_ctx *ctx)
   ctx->scratch_cap = ctx->scratch2_cap = ctx->scratch3_cap = ctx->scratch4_cap =
       ctx->scratch5_cap = 0;
   ctx->xtx_cap = 0;
+  ctx->geno_cap = 0;
   ctx->codes4_rows = 0;
   ctx->keep_cap = 0;
   ctx->keep_valid = 0;

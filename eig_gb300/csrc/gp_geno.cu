@@ -44,6 +44,32 @@ __global__ void k_recode_bed(uint8_t *rec, int64_t nsnp, int64_t rlen_dev, int64
   }
 }
 
+/* records of src_pitch bytes (used of them genotype bytes) into the 16-byte device pitch,
+ * one 16-byte chunk per thread; bytes past used read as 0xFF (missing) */
+__global__ void k_repitch(const uint8_t *__restrict__ src, int64_t src_pitch, int64_t used,
+                          uint8_t *__restrict__ dst, int64_t rlen_dev, int64_t nsnp)
+{
+  const int64_t chunks = rlen_dev >> 4, total = nsnp * chunks;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s = i / chunks, j = i - s * chunks, b0 = 16 * j;
+    const uint8_t *p = src + s * src_pitch + b0;
+    uint32_t w[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      uint32_t v = 0;
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const int64_t b = b0 + 4 * q + t;
+        const uint32_t by = b < used ? (uint32_t)p[4 * q + t] : 0xFFu;
+        v |= by << (8 * t);
+      }
+      w[q] = v;
+    }
+    *(uint4 *)(dst + s * rlen_dev + b0) = make_uint4(w[0], w[1], w[2], w[3]);
+  }
+}
+
 /* set the bytes after the last sample of each record to 0xFF (missing) */
 __global__ void k_pad_records(uint8_t *rec, int64_t nsnp, int64_t rlen_dev, int32_t nind)
 {
@@ -97,15 +123,22 @@ extern "C" int gp_load_genotypes(gp_ctx *ctx, const uint8_t *records, int64_t re
                    (long long)record_bytes, (long long)used);
   int64_t rlen_dev = (used + 15) / 16 * 16;
   size_t bytes = (size_t)(rlen_dev * nsnp);
-  if (ctx->d_geno) {
+  /* the panel's allocation is kept while it is large enough (no cudaFree / cudaMalloc, and
+   * their synchronisation, when a handle reloads panels of the same size) */
+  if (ctx->d_geno && bytes > ctx->geno_cap) {
+    cudaStreamSynchronize(ctx->stream);
     cudaFree(ctx->d_geno);
     ctx->d_geno = NULL;
+    ctx->geno_cap = 0;
   }
-  cudaError_t e = cudaMalloc((void **)&ctx->d_geno, bytes);
-  if (e != cudaSuccess) {
-    ctx->d_geno = NULL;
-    return gp_fail(ctx, GP_ERR_NOMEM, "gp_load_genotypes: cudaMalloc %zu bytes: %s", bytes,
-                   cudaGetErrorString(e));
+  if (!ctx->d_geno) {
+    cudaError_t e = cudaMalloc((void **)&ctx->d_geno, bytes);
+    if (e != cudaSuccess) {
+      ctx->d_geno = NULL;
+      return gp_fail(ctx, GP_ERR_NOMEM, "gp_load_genotypes: cudaMalloc %zu bytes: %s", bytes,
+                     cudaGetErrorString(e));
+    }
+    ctx->geno_cap = bytes;
   }
   ctx->nsnp_all = nsnp;
   ctx->nind_all = nind;
@@ -113,10 +146,21 @@ extern "C" int gp_load_genotypes(gp_ctx *ctx, const uint8_t *records, int64_t re
   ctx->nrows = ctx->ncols = 0;
   ctx->codes4_rows = 0;
   ctx->xtx_valid = ctx->eig_valid = ctx->weights_valid = 0;
-  ctx->h2d_bytes += used * nsnp;
-  GP_CUDA(ctx, cudaMemcpy2DAsync(ctx->d_geno, (size_t)rlen_dev, records, (size_t)record_bytes,
-                                 (size_t)used, (size_t)nsnp, cudaMemcpyHostToDevice,
-                                 ctx->stream));
+  /* one contiguous host-to-device copy (a pitched copy of many short rows is slow), then
+   * the records are re-pitched on the device when the host pitch differs */
+  const size_t hbytes = (size_t)record_bytes * (size_t)nsnp;
+  if (record_bytes == rlen_dev) {
+    GP_CUDA(ctx, gp_memcpy(ctx, ctx->d_geno, records, hbytes, cudaMemcpyHostToDevice,
+                           ctx->stream));
+  } else {
+    uint8_t *stage;
+    int rc = gp_scratch2(ctx, hbytes + 16, (void **)&stage);
+    if (rc) return rc;
+    GP_CUDA(ctx, gp_memcpy(ctx, stage, records, hbytes, cudaMemcpyHostToDevice, ctx->stream));
+    k_repitch<<<grid_for(ctx, nsnp * (rlen_dev >> 4), 256), 256, 0, ctx->stream>>>(
+        stage, record_bytes, used, ctx->d_geno, rlen_dev, nsnp);
+    GP_LAUNCH_CHECK(ctx, "k_repitch");
+  }
   if (code == GP_CODE_BED) {
     k_recode_bed<<<grid_for(ctx, nsnp * used, 256), 256, 0, ctx->stream>>>(
         ctx->d_geno, nsnp, rlen_dev, used, nind);

@@ -24,6 +24,7 @@ struct gp_ctx {
 
   /* genotype panel: nsnp_all records of rlen_dev bytes (packed 2-bit, MSB first) */
   uint8_t *d_geno;
+  size_t geno_cap;   /* bytes allocated at d_geno */
   int64_t nsnp_all;
   int32_t nind_all;
   int64_t rlen_dev;  /* padded to a multiple of 16 bytes; pad bytes are 0xFF (missing) */

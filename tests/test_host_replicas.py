@@ -76,3 +76,22 @@ def test_reference_arm_non_zero_rank_exits_without_work():
                        text=True, timeout=120)
     assert r.returncode == 0, r.stderr
     assert r.stdout.strip() == ""
+
+
+def test_tridiag_roofline_figures():
+    """the dominant-kernel roofline: dsytd2's algorithmic bytes 8 (n-1) n (n+1) / 3, achieved
+    GB/s from the CUDA-event time, and the DRAM bytes of the committed ncu summary for the
+    order it was captured at (none for other orders)"""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    res = {"tridiag_n": 5000, "tridiag_ms": 150.0}
+    roof = bench.tridiag_roofline(res, {"hbm_gbs": 6000.0}, "measured")
+    alg = 8.0 * 4999 * 5000 * 5001 / 3.0
+    assert roof["bound"] == "hbm" and roof["unit"] == "GB/s"
+    assert abs(roof["algorithmic_bytes"] - alg) < 1.0
+    assert abs(roof["achieved"] - alg / 0.150 / 1e9) < 1e-6
+    assert abs(roof["frac"] - roof["achieved"] / 6000.0) < 1e-12
+    assert roof["traffic"] == bench.tridiag_traffic(5000) and roof["traffic"] > alg
+    assert bench.tridiag_traffic(4000) is None
+    assert bench.tridiag_roofline({"tridiag_n": 5000, "tridiag_ms": 0.0}, {}, "x") is None

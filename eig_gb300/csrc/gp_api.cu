@@ -826,22 +826,41 @@ extern "C" int gp_snp_weights(gp_ctx *ctx, int32_t numeigs, double *ffvecs, doub
 /* ------------------------------------------------------------------------------------ */
 
 /* E[k*K + j] = fxscal_j * ffvecs_j[kept k];  P[k*ldp + pair(a,b)] = E_a E_b (a<=b), then 1 */
-__global__ void k_build_EP(const double *ffvecs, const double *fxscal, const int32_t *kept,
-                           int32_t nkept, int32_t ncols, int32_t K, double *E, double *P,
-                           int32_t ldp)
+/* E[k][j] = fxscal_j ffvecs_j(kept k) and P[k] = (E_a E_b for a <= b in row order, 1):
+ * a warp per kept SNP, E of the SNP in shared memory, the pair products written as
+ * consecutive doubles (coalesced) from a pair-index table; K <= 64 */
+#define EP_THREADS 256
+__global__ void __launch_bounds__(EP_THREADS)
+k_build_EP(const double *ffvecs, const double *fxscal, const int32_t *kept, int32_t nkept,
+           int32_t ncols, int32_t K, double *E, double *P, int32_t ldp)
 {
-  for (int32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nkept; k += gridDim.x * blockDim.x) {
-    int32_t c = kept[k];
-    double e[64];
-    for (int j = 0; j < K; ++j) {
-      e[j] = fxscal[j] * ffvecs[(int64_t)j * ncols + c];
-      E[(int64_t)k * K + j] = e[j];
+  __shared__ uint8_t pa[64 * 65 / 2], pb[64 * 65 / 2];
+  __shared__ double se[EP_THREADS / 32][64];
+  const int npair = K * (K + 1) / 2;
+  for (int t = threadIdx.x; t < npair; t += blockDim.x) {
+    int a = 0, rem = t;
+    while (rem >= K - a) {
+      rem -= K - a;
+      ++a;
     }
-    double *p = P + (int64_t)k * ldp;
-    int t = 0;
-    for (int a = 0; a < K; ++a)
-      for (int b = a; b < K; ++b) p[t++] = e[a] * e[b];
-    p[t] = 1.0;
+    pa[t] = (uint8_t)a;
+    pb[t] = (uint8_t)(a + rem);
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t k = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp; k < nkept; k += nw) {
+    const int32_t c = kept[k];
+    for (int j = lane; j < K; j += 32) {
+      const double v = fxscal[j] * ffvecs[(int64_t)j * ncols + c];
+      se[warp][j] = v;
+      E[k * K + j] = v;
+    }
+    __syncwarp();
+    double *p = P + k * ldp;
+    for (int t = lane; t < npair; t += 32) p[t] = se[warp][pa[t]] * se[warp][pb[t]];
+    if (lane == 0) p[npair] = 1.0;
+    __syncwarp();
   }
 }
 
@@ -947,10 +966,10 @@ extern "C" int gp_lsqproj(gp_ctx *ctx, int32_t numeigs, const int32_t *samples, 
   GP_CUDA(ctx, gp_memcpy(ctx, d_samp, samples, sizeof(int32_t) * (size_t)nproj,
                                cudaMemcpyHostToDevice, ctx->stream));
   if (nk) {
-    int blocks = (nk + 127) / 128;
-    if (blocks > ctx->num_sms * 8) blocks = ctx->num_sms * 8;
-    k_build_EP<<<blocks, 128, 0, ctx->stream>>>(ctx->d_ffvecs, ctx->d_fxscal, ctx->d_kept, nk, nc,
-                                                K, d_E, d_P, ldp);
+    int blocks = (nk + EP_THREADS / 32 - 1) / (EP_THREADS / 32);
+    if (blocks > ctx->num_sms * 16) blocks = ctx->num_sms * 16;
+    k_build_EP<<<blocks, EP_THREADS, 0, ctx->stream>>>(ctx->d_ffvecs, ctx->d_fxscal, ctx->d_kept,
+                                                       nk, nc, K, d_E, d_P, ldp);
     GP_LAUNCH_CHECK(ctx, "k_build_EP");
   }
   /* masked normal equations: co = O P (pair sums + observed count), rr = R E */

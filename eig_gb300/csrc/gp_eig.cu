@@ -820,20 +820,23 @@ __global__ void k_inverse_iteration(const double *__restrict__ d, const double *
       const double ei = ee[i];
       const double dn = dd[i + 1] - lam;               /* row i+1 diagonal */
       const double en = (i < n - 2) ? ee[i + 1] : 0.0; /* row i+1 superdiagonal */
+      /* one division per step: the pivot's reciprocal, then the multiplier from it */
       if (fabs(cur) >= fabs(ei)) {
         if (cur == 0.0) cur = tiny;
-        double f = ei / cur;
+        const double rc = 1.0 / cur;
+        double f = ei * rc;
         DL[i] = f;
         DU[i] = du;
         DU2[i] = 0.0;
-        Dinv[i] = 1.0 / cur;
+        Dinv[i] = rc;
         piv[i] = 0;
         cur = dn - f * du;
         du = en;
       } else {
-        double f = cur / ei;
+        const double re = 1.0 / ei;
+        double f = cur * re;
         DL[i] = f;
-        Dinv[i] = 1.0 / ei;
+        Dinv[i] = re;
         DU[i] = dn;
         DU2[i] = en;
         piv[i] = 1;

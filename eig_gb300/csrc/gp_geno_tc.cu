@@ -320,7 +320,7 @@ k_codes_by_sample(const uint8_t *__restrict__ geno, int64_t rlen, const int32_t 
   __shared__ uint32_t srec[CB_SNP][CB_PITCH_W];
   __shared__ int64_t soff[CB_SNP];
   const int tid = threadIdx.x;
-  const int32_t k0 = blockIdx.x * CB_SNP, r0 = blockIdx.y * CB_ROWS;
+  const int32_t r0 = blockIdx.y * CB_ROWS;
   int32_t base = 0, span = 0;
   if (r0 < nsamp) {
     const int32_t rl = (r0 + CB_ROWS < nsamp ? r0 + CB_ROWS : nsamp) - 1;
@@ -328,41 +328,50 @@ k_codes_by_sample(const uint8_t *__restrict__ geno, int64_t rlen, const int32_t 
     span = (samp[rl] >> 2) - base + 1;
   }
   const bool fast = span <= CB_SPAN;
-  if (tid < CB_SNP) soff[tid] = (k0 + tid < nk) ? (int64_t)snprec[k0 + tid] * rlen : -1;
-  __syncthreads();
-  if (fast && span > 0) {
-    const int nvec = (span + 15) >> 4;
-    for (int i = tid; i < CB_SNP * nvec; i += blockDim.x) {
-      const int u = i / nvec, v = i - u * nvec;
-      uint4 val = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
-      if (soff[u] >= 0) val = __ldg((const uint4 *)(geno + soff[u] + base + 16 * v));
-      srec[u][4 * v] = val.x;
-      srec[u][4 * v + 1] = val.y;
-      srec[u][4 * v + 2] = val.z;
-      srec[u][4 * v + 3] = val.w;
-    }
-  }
-  __syncthreads();
   const int rl = tid >> 1, half = tid & 1;
   const int32_t r = r0 + rl;
-  if (r >= nrows_pad || (int64_t)k0 + 64 * half >= ldc * 4) return;
-  uint32_t out[4] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
-  if (r < nsamp) {
-    const int32_t sidx = samp[r];
-    const int32_t bb = (sidx >> 2) - base, sh = (3 - (sidx & 3)) * 2;
-#pragma unroll 8
-    for (int j = 0; j < 64; ++j) {
-      const int u = 64 * half + j;
-      uint32_t byte = 0xFFu;
-      if (soff[u] >= 0)
-        byte = fast ? (srec[u][bb >> 2] >> ((bb & 3) * 8)) & 0xFFu : __ldg(geno + soff[u] + (sidx >> 2));
-      const uint32_t c = (byte >> sh) & 3u;
-      /* code j of the group: byte j>>2 (word j>>4), bits (3-(j&3))*2 within the byte */
-      const uint32_t wpos = (uint32_t)((j >> 2) & 3) * 8u + (3u - (uint32_t)(j & 3)) * 2u;
-      out[j >> 4] = (out[j >> 4] & ~(3u << wpos)) | (c << wpos);
+  const int32_t sidx = r < nsamp ? samp[r] : 0;
+  /* the CTA walks the SNP tiles of its row block (grid-stride over x) */
+  const int32_t nkt = (int32_t)((ldc * 4 + CB_SNP - 1) / CB_SNP);
+  for (int32_t kt = blockIdx.x; kt < nkt; kt += gridDim.x) {
+    const int32_t k0 = kt * CB_SNP;
+    if (tid < CB_SNP) soff[tid] = (k0 + tid < nk) ? (int64_t)snprec[k0 + tid] * rlen : -1;
+    __syncthreads();
+    if (fast && span > 0) {
+      const int nvec = (span + 15) >> 4;
+      for (int i = tid; i < CB_SNP * nvec; i += blockDim.x) {
+        const int u = i / nvec, v = i - u * nvec;
+        uint4 val = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
+        if (soff[u] >= 0) val = __ldg((const uint4 *)(geno + soff[u] + base + 16 * v));
+        srec[u][4 * v] = val.x;
+        srec[u][4 * v + 1] = val.y;
+        srec[u][4 * v + 2] = val.z;
+        srec[u][4 * v + 3] = val.w;
+      }
     }
+    __syncthreads();
+    if (r < nrows_pad && (int64_t)k0 + 64 * half < ldc * 4) {
+      uint32_t out[4] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
+      if (r < nsamp) {
+        const int32_t bb = (sidx >> 2) - base, sh = (3 - (sidx & 3)) * 2;
+#pragma unroll 8
+        for (int j = 0; j < 64; ++j) {
+          const int u = 64 * half + j;
+          uint32_t byte = 0xFFu;
+          if (soff[u] >= 0)
+            byte = fast ? (srec[u][bb >> 2] >> ((bb & 3) * 8)) & 0xFFu
+                        : __ldg(geno + soff[u] + (sidx >> 2));
+          const uint32_t c = (byte >> sh) & 3u;
+          /* code j of the group: byte j>>2 (word j>>4), bits (3-(j&3))*2 within the byte */
+          const uint32_t wpos = (uint32_t)((j >> 2) & 3) * 8u + (3u - (uint32_t)(j & 3)) * 2u;
+          out[j >> 4] = (out[j >> 4] & ~(3u << wpos)) | (c << wpos);
+        }
+      }
+      *(uint4 *)(codes + (int64_t)r * ldc + (k0 >> 2) + 16 * half) =
+          make_uint4(out[0], out[1], out[2], out[3]);
+    }
+    __syncthreads(); /* srec and soff are rewritten by the next tile */
   }
-  *(uint4 *)(codes + (int64_t)r * ldc + (k0 >> 2) + 16 * half) = make_uint4(out[0], out[1], out[2], out[3]);
 }
 
 /*
@@ -590,7 +599,12 @@ int gp_tc_build_codes(gp_ctx *ctx, int sum_over_snps, const int32_t *d_samp, int
   int32_t nrows_pad;
   gp_tc_code_bytes(sum_over_snps, nsamp, nk, &ldc, &nrows_pad);
   if (sum_over_snps) {
-    dim3 grid((unsigned)((ldc * 4 + CB_SNP - 1) / CB_SNP), (unsigned)((nrows_pad + CB_ROWS - 1) / CB_ROWS));
+    /* about 16 CTAs per SM in all; each walks the SNP tiles of its row block */
+    const int64_t nkt = (ldc * 4 + CB_SNP - 1) / CB_SNP, nrb = (nrows_pad + CB_ROWS - 1) / CB_ROWS;
+    int64_t gx = ((int64_t)ctx->num_sms * 16 + nrb - 1) / nrb;
+    if (gx > nkt) gx = nkt;
+    if (gx < 1) gx = 1;
+    dim3 grid((unsigned)gx, (unsigned)nrb);
     k_codes_by_sample<<<grid, 256, 0, ctx->stream>>>(ctx->d_geno, ctx->rlen_dev, d_samp, nsamp,
                                                      nrows_pad, d_snprec, nk, ldc, codes);
   } else {

@@ -737,10 +737,10 @@ int gp_gram_split(gp_ctx *ctx, int precision)
   /* clusters of four CTAs (2 x 2 tiles sharing row and column boxes), else two (two tiles of
    * a row sharing its boxes), else one CTA per tile; GP_GRAM_CLUSTER=1|2|4 caps the size.
    * The next smaller size is used when the cluster launch is refused. */
-  int cl = 4;
+  int cl = ctx->gram_cluster_cap > 0 ? ctx->gram_cluster_cap : 4;
   {
     const char *ce = getenv("GP_GRAM_CLUSTER");
-    if (ce && atoi(ce) >= 1) cl = atoi(ce) >= 4 ? 4 : (atoi(ce) >= 2 ? 2 : 1);
+    if (ce && atoi(ce) >= 1 && atoi(ce) < cl) cl = atoi(ce) >= 4 ? 4 : (atoi(ce) >= 2 ? 2 : 1);
   }
   const int32_t nq = (nt + 1) / 2;
   const int32_t nwork_cl[5] = {0, ntiles, gram_npairs(nt), 0, nq * (nq + 1) / 2};
@@ -829,8 +829,15 @@ int gp_gram_split(gp_ctx *ctx, int precision)
   int herr = 0;
   GP_CUDA(ctx, gp_memcpy(ctx, &herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  if (herr == GP_KERR_CLUSTER)
-    return gp_fail(ctx, GP_ERR_CUDA, "split Gram: the cluster launch was not honoured");
+  if (herr == GP_KERR_CLUSTER) {
+    /* the launch ran without its clusters (every CTA refused before any load or MMA, so
+     * nothing was written): redo the whole Gram on the one-CTA schedule, which needs no
+     * cluster, and keep that schedule for this handle */
+    if (ctx->gram_cluster_cap == 1)
+      return gp_fail(ctx, GP_ERR_CUDA, "split Gram: the cluster launch was not honoured");
+    ctx->gram_cluster_cap = 1;
+    return gp_gram_split(ctx, precision);
+  }
   if (herr) return gp_fail(ctx, GP_ERR_TIMEOUT, "split-BF16 Gram kernel wait timed out (code %d)", herr);
   return GP_OK;
 }

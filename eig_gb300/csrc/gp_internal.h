@@ -69,6 +69,8 @@ struct gp_ctx {
   cudaEvent_t ev_t0, ev_t1, ev_g0, ev_g1;
   double gram_ms;
   int32_t gram_launches;
+  int gram_cluster_cap;  /* largest split-Gram cluster size to try (0: 4); set to 1 after a
+                            cluster launch was not honoured */
   double gram_flops;
   double encode_ms;      /* k_encode time of the last device-output gp_encode_records */
   cudaEvent_t ev_tr0, ev_tr1;

@@ -13,12 +13,21 @@
  * (16 MiB).  Every GPU that loads the library holds it until the process exits.  Host code
  * cannot use the array's name as a device address, so the first call on each device (with
  * that device current) looks the address up with cudaGetSymbolAddress and caches it; make
- * that first call before any stream capture begins.  All calls share the one array and it
- * keeps the last call's contents: each call clears the part it uses, and calls whose work
- * overlaps on the GPU (different streams, or different host threads on one stream without
- * ordering) race on it.
+ * that first call before any stream capture begins.  With CUDA's lazy module loading (the
+ * default since CUDA 12.2) the array itself is only allocated when this code is first used on
+ * a device, i.e. by that first call: a caller whose pool reserves the whole device must make
+ * the first call before the pool takes the memory.  The cached address is not refreshed after
+ * a cudaDeviceReset of that device (which frees the array): after a reset the entry point must
+ * not be used again in that process.  All calls share the one array and it keeps the last
+ * call's contents: each call overwrites every scratch entry it later reads, and calls whose
+ * work overlaps on the GPU (different streams, or different host threads on one stream
+ * without ordering) race on it.  The host side is thread-safe: the address lookup happens
+ * once per device under a lock, and the failure text is kept per host thread.
  */
 #include <cuda_runtime.h>
+
+#include <atomic>
+#include <mutex>
 
 #include "gp_internal.h"
 
@@ -30,9 +39,10 @@
 
 static __device__ __align__(256) double g_noalloc_scratch[GP_NOALLOC_SCRATCH_DOUBLES];
 
-static double *g_noalloc_addr[GP_NOALLOC_MAX_DEVICES];
+static std::atomic<double *> g_noalloc_addr[GP_NOALLOC_MAX_DEVICES];
+static std::mutex g_noalloc_lookup;
 
-static char g_noalloc_err[256];
+static thread_local char g_noalloc_err[256];
 
 /* partial[s][i][j] (j <= i) = sum over SNPs of split s of v_i v_j for one 64x64 tile */
 __global__ void __launch_bounds__(256)
@@ -136,15 +146,18 @@ extern "C" int gp_gram_fp64_noalloc(const uint8_t *d_records, int64_t record_byt
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess || dev < 0 || dev >= GP_NOALLOC_MAX_DEVICES)
     return noalloc_fail(GP_ERR_CUDA, "gp_gram_fp64_noalloc: no usable current device");
-  if (!g_noalloc_addr[dev]) {
+  double *part = g_noalloc_addr[dev].load(std::memory_order_acquire);
+  if (!part) {
     /* once per device, with that device current: the array's device address */
-    double *p = NULL;
-    e = cudaGetSymbolAddress((void **)&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p)
-      return noalloc_fail(GP_ERR_CUDA, "gp_gram_fp64_noalloc: cudaGetSymbolAddress failed");
-    g_noalloc_addr[dev] = p;
+    std::lock_guard<std::mutex> lock(g_noalloc_lookup);
+    part = g_noalloc_addr[dev].load(std::memory_order_acquire);
+    if (!part) {
+      e = cudaGetSymbolAddress((void **)&part, g_noalloc_scratch);
+      if (e != cudaSuccess || !part)
+        return noalloc_fail(GP_ERR_CUDA, "gp_gram_fp64_noalloc: cudaGetSymbolAddress failed");
+      g_noalloc_addr[dev].store(part, std::memory_order_release);
+    }
   }
-  double *part = g_noalloc_addr[dev];
   cudaStream_t st = (cudaStream_t)stream;
   const int64_t nn = (int64_t)nind * nind;
   const int32_t nt = (nind + NT - 1) / NT, ntiles = nt * (nt + 1) / 2;
@@ -156,8 +169,9 @@ extern "C" int gp_gram_fp64_noalloc(const uint8_t *d_records, int64_t record_byt
   int32_t kper = (nsnp + nsplit - 1) / nsplit;
   kper = (kper + NK - 1) / NK * NK;
   nsplit = (nsnp + kper - 1) / kper;
-  e = cudaMemsetAsync(part, 0, sizeof(double) * (size_t)nn * nsplit, st);
-  if (e != cudaSuccess) return noalloc_fail(GP_ERR_CUDA, cudaGetErrorString(e));
+  /* no clearing needed: every split has SNPs (nsplit = ceil(nsnp / kper)) and its tiles write
+   * every lower-triangle entry i < nind, j <= i of its slice, the only entries the reduction
+   * reads */
   dim3 grid((unsigned)ntiles, (unsigned)nsplit);
   k_gram_f64_noalloc<<<grid, 256, 0, st>>>(d_records, record_bytes, nind, nsnp, d_vtab, kper, part);
   e = cudaGetLastError();

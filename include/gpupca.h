@@ -286,8 +286,12 @@ int gp_host_unregister(void *ptr);
  * Limit: nind <= 1024 (larger panels return GP_ERR_ARG; use gp_xtx).  Scratch for the
  * split-K partial sums is a fixed 16 MiB array inside the library that every GPU loading it
  * holds until exit; the first call on a device looks its address up (make it before any
- * stream capture); calls that overlap on the GPU race on that array.  gp_noalloc_last_error
- * gives the text of the last failure.
+ * stream capture) and, as CUDA loads modules lazily by default, is also when the array is
+ * allocated on that device: make the first call before a pool reserves the whole device.
+ * Each call overwrites the scratch entries it reads; calls that overlap on the GPU race on
+ * that array.  The cached address is not refreshed after cudaDeviceReset (do not call the
+ * entry point again on a device that was reset).  The host side may be called from several
+ * threads; gp_noalloc_last_error gives the text of the calling thread's last failure.
  */
 int gp_gram_fp64_noalloc(const uint8_t *d_records, int64_t record_bytes, int32_t nind,
                          int32_t nsnp, const double *d_vtab, double *d_xtx, void *stream);

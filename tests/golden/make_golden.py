@@ -19,7 +19,9 @@ EIG_REF_FULLPREC=1 prints .eval/.evec numbers as %.17g).  Writes, per case:
 
 and copies the reference's own example fixtures (CONVERTF/example.*,
 EIGENSTRAT/example.*) into ref_examples/.  Usage:
-  python tests/golden/make_golden.py [reference_root]
+  python tests/golden/make_golden.py REFERENCE_ROOT [--scratch DIR] [case ...]
+(the benchmark-shaped cases of BIG_CASES run only when named, with --scratch for their
+genotype files)
 """
 import os
 import shutil
@@ -353,12 +355,108 @@ def copy_examples(ref_root):
             shutil.copy(os.path.join(ref_root, sub, n), os.path.join(out, sub + "_" + n))
 
 
+# Panels at the benchmark shapes.  Their genotypes are NOT committed: the tests regenerate them
+# from the seed with the same generator and check the records' SHA-256 first.  Committed per
+# case: spec.json (generator arguments, records hash, kept-SNP count, parfile), ref.eval (the
+# first `keep_evals` eigenvalues at %.17g, plus their total), ref.evec (header + every
+# `evec_stride`-th sample at %.17g), ref.outliers and the head of ref.log.
+BIG_CASES = {
+    # N=1,000 x M=50,000, 3 populations of ~333, F=0.01, 1% missing, seed 1, K=10, no outlier
+    # removal: plain smartpca
+    "cfg1_plain": dict(nsnp=50_000, pops=[334, 333, 333], fst=[0.01, 0.01, 0.01], miss=0.01,
+                       seed=1, keep_evals=1000, evec_stride=1,
+                       par={"numoutevec": "10", "numoutlieriter": "0"}),
+    # the same shape with 8 planted divergent samples (two populations of 4 at F=0.25) and the
+    # default outlier removal (5 iterations, 10 eigenvectors, sigma 6): real outlier decisions at
+    # N > 1,000
+    "cfg1_outliers": dict(nsnp=50_000, pops=[330, 330, 332, 4, 4],
+                          fst=[0.01, 0.01, 0.01, 0.25, 0.25], miss=0.01, seed=4,
+                          keep_evals=200, evec_stride=1,
+                          par={"numoutevec": "10", "numoutlieriter": "5"}),
+    # N=5,000 x M=600,000, 6 populations 500..1,100, F 0.005..0.05, 2% missing, K=20, 5 outlier
+    # iterations at sigma 6, lsqproject (the benchmark's full workload, generator seed 2)
+    "cfg2_full": dict(nsnp=600_000, pops=[500, 700, 800, 900, 1000, 1100],
+                      fst=[0.005, 0.01, 0.02, 0.03, 0.04, 0.05], miss=0.02, seed=2,
+                      keep_evals=200, evec_stride=25,
+                      par={"numoutevec": "20", "numoutlieriter": "5",
+                           "outliersigmathresh": "6.0"}),
+}
+
+
+def records_sha256(rec):
+    import hashlib
+    return hashlib.sha256(np.ascontiguousarray(rec).tobytes()).hexdigest()
+
+
+def make_big_case(name, spec, scratch):
+    """Run the reference on a benchmark-shaped panel written to `scratch` (not committed) and
+    keep the outputs named above under tests/golden/<name>/."""
+    import json
+    d = os.path.join(HERE, name)
+    os.makedirs(d, exist_ok=True)
+    w = os.path.join(scratch, name)
+    os.makedirs(w, exist_ok=True)
+    prefix = os.path.join(w, "data")
+    native.synth_write_dataset(prefix, spec["nsnp"], spec["pops"], spec["fst"],
+                               miss=spec["miss"], seed=spec["seed"])
+    nind = sum(spec["pops"])
+    rlen = max((nind + 3) // 4, 48)
+    raw = np.fromfile(prefix + ".geno", np.uint8)[rlen:].reshape(spec["nsnp"], rlen)
+    par = {"genotypename": "data.geno", "snpname": "data.snp", "indivname": "data.ind",
+           "evecoutname": "out.evec", "evaloutname": "out.eval",
+           "outlieroutname": "out.outliers", "numthreads": str(os.cpu_count() or 8)}
+    par.update(spec["par"])
+    with open(os.path.join(w, "par"), "w") as f:
+        for k, v in par.items():
+            f.write("%s: %s\n" % (k, v))
+    env = dict(os.environ, EIG_REF_FULLPREC="1")
+    with open(os.path.join(w, "ref.log"), "w") as log:
+        subprocess.run([REF_BIN, "-p", "par"], cwd=w, env=env, stdout=log,
+                       stderr=subprocess.STDOUT, check=True)
+    ev = [float(x) for x in open(os.path.join(w, "out.eval")).read().split()]
+    with open(os.path.join(d, "ref.eval"), "w") as f:
+        for x in ev[:spec["keep_evals"]]:
+            f.write("%.17g\n" % x)
+    lines = open(os.path.join(w, "out.evec")).read().splitlines()
+    with open(os.path.join(d, "ref.evec"), "w") as f:
+        f.write(lines[0] + "\n")
+        for i, ln in enumerate(lines[1:]):
+            if i % spec["evec_stride"] == 0:
+                f.write(ln + "\n")
+    shutil.copy(os.path.join(w, "out.outliers"), os.path.join(d, "ref.outliers"))
+    log = open(os.path.join(w, "ref.log")).read().splitlines()
+    used = [ln for ln in log if "number of snps killed in pass" in ln or
+            "number of samples used" in ln or "samples after outlier removal" in ln]
+    with open(os.path.join(d, "ref.log"), "w") as f:
+        f.write("\n".join(log[:80]) + "\n")
+    kept = [int(ln.split("used:")[1]) for ln in used if "killed in pass" in ln]
+    meta = {"nsnp": spec["nsnp"], "pops": spec["pops"], "fst": spec["fst"],
+            "miss": spec["miss"], "seed": spec["seed"], "nind": nind,
+            "records_sha256": records_sha256(raw), "par": spec["par"],
+            "eval_count": len(ev), "eval_sum": float(np.sum(ev)),
+            "kept_snps_per_pass": kept, "evec_stride": spec["evec_stride"],
+            "log_counts": used}
+    with open(os.path.join(d, "spec.json"), "w") as f:
+        json.dump(meta, f, indent=1)
+        f.write("\n")
+
+
 if __name__ == "__main__":
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    # usage: make_golden.py REFERENCE_ROOT [--scratch DIR] [case ...]
+    args = sys.argv[1:]
+    scratch = None
+    if "--scratch" in args:
+        i = args.index("--scratch")
+        scratch = args[i + 1]
+        del args[i:i + 2]
+    if not args:
+        raise SystemExit("usage: make_golden.py REFERENCE_ROOT [--scratch DIR] [case ...]")
+    ref_root = args[0]
     if not os.path.exists(REF_BIN):
-        raise SystemExit("build the reference first: sh oracle/build_ref.sh")
-    copy_examples(ref_root)
-    only = sys.argv[2:]  # optional case names
+        raise SystemExit("build the reference first: sh oracle/build_ref.sh REFERENCE_ROOT")
+    only = args[1:]  # optional case names
+    if not only:
+        copy_examples(ref_root)
     for name, spec in CASES.items():
         if only and name not in only:
             continue
@@ -368,4 +466,11 @@ if __name__ == "__main__":
         if only and name not in only:
             continue
         make_convert_case(name, spec)
+        print("made", name)
+    for name, spec in BIG_CASES.items():
+        if not only or name not in only:
+            continue  # benchmark-shaped cases only on request (minutes to hours of CPU)
+        if scratch is None:
+            raise SystemExit("%s needs --scratch DIR for its (uncommitted) genotype files" % name)
+        make_big_case(name, spec, scratch)
         print("made", name)

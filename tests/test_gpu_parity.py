@@ -442,3 +442,52 @@ def test_split_gram_clusters_equal_single_ctas(gpu, monkeypatch, nind):
     assert np.array_equal(grams["4"], grams["1"])
     assert np.array_equal(grams["2"], grams["1"])
 
+
+
+@pytest.mark.parametrize("prec", [native.GP_PREC_SPLIT_FP16, native.GP_PREC_SPLIT_BF16X4])
+def test_split_gram_rare_variants(gpu, prec):
+    """ancestral allele frequencies down to 1/(2N) (hundreds of kept SNPs with a single minor
+    allele copy): the common genotype's value -2 sqrt(p) is small, so its fp16 lo part can be
+    subnormal; the split Gram still holds the split tolerances against the FP64 GPU Gram"""
+    nind, nsnp = 2000, 20000
+    rec, pop = synth(nsnp, [700, 700, 600], [0.01, 0.02, 0.03], miss=0.02, seed=41,
+                     p_lo=1.0 / (2 * nind), p_hi=0.02)
+    rows = np.arange(nind, dtype=np.int32)
+    cols = np.arange(nsnp, dtype=np.int32)
+    r64 = _gram_pair(gpu, rec, nind, rows, cols, native.GP_PREC_FP64)
+    mac = np.minimum(r64["n0"], r64["n1"])
+    assert np.sum((mac == 1) & (r64["killed"] == 0)) > 100
+    ref = r64["XTX"]
+    r = _gram_pair(gpu, rec, nind, rows, cols, prec)
+    etol, vtol = SPLIT_TOL[prec]
+    err = np.max(np.abs(r["XTX"] - ref)) / np.max(np.abs(ref))
+    assert err <= etol, err
+    w1 = np.linalg.eigvalsh(r["XTX"])[::-1][:20]
+    w0 = np.linalg.eigvalsh(ref)[::-1][:20]
+    assert np.max(np.abs(w1 - w0) / w0) <= vtol
+
+
+def test_eig_n5000_vs_lapack(gpu):
+    """the eigensolver at the benchmark's order, N=5,000, where the float-float
+    tridiagonalisation first streams a trailing matrix larger than L2: every eigenvalue within
+    1e-12 of the largest against LAPACK (numpy eigh on the host), the top 20 eigenvectors with
+    small residuals, orthonormal and equal (up to sign) to LAPACK's where separated"""
+    rec, pop = synth(7000, [1800, 1700, 1500], [0.01, 0.02, 0.04], miss=0.02, seed=43)
+    nind = len(pop)
+    gpu.load_genotypes(rec, nind)
+    gpu.set_samples(np.arange(nind, dtype=np.int32))
+    gpu.set_snps(np.arange(7000, dtype=np.int32))
+    X = gpu.xtx()["XTX"]
+    ev, V = gpu.eigvecs(20)
+    Xs = X * ((nind - 1) / np.trace(X))
+    w, U = np.linalg.eigh(Xs)
+    w = w[::-1]
+    U = U[:, ::-1].T
+    assert np.max(np.abs(ev - w)) <= 1e-12 * w[0]
+    R = V @ Xs - ev[:20, None] * V
+    assert np.max(np.linalg.norm(R, axis=1)) <= 1e-9 * w[0]
+    assert np.max(np.abs(V @ V.T - np.eye(20))) <= 1e-10
+    gaps = np.minimum(np.abs(np.diff(w[:21]))[:-1], np.abs(np.diff(w[:21]))[1:])
+    sep = np.concatenate([[w[0] - w[1]], gaps])[:20] > 1e-3 * w[0]
+    cos = np.abs(np.sum(V * U[:20], axis=1))
+    assert np.all(cos[sep] > 1 - 1e-9)

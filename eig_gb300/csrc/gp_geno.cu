@@ -201,6 +201,48 @@ extern "C" int gp_set_missing(gp_ctx *ctx, const int64_t *pairs, int64_t npairs)
   return GP_OK;
 }
 
+/*
+ * missingmode: every genotype of a real sample becomes the indicator of being observed,
+ * 1 when its code is 0/1/2 and 0 when it is missing (setmiss src/qpsubs.c:462-483); the pad
+ * codes past the last sample stay missing.  One 32-bit word (16 codes) per thread.
+ */
+__global__ void k_missingmode(uint8_t *geno, int64_t rlen_dev, int64_t nsnp, int32_t nind)
+{
+  const int64_t wpr = rlen_dev >> 2, total = nsnp * wpr;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t w = i % wpr;
+    uint32_t *pw = (uint32_t *)geno + i;
+    const uint32_t x = *pw;
+    /* per 2-bit code (h, l): missing = h & l; observed -> 01, missing -> 00 */
+    const uint32_t miss = (x >> 1) & x & 0x55555555u;
+    uint32_t y = ~miss & 0x55555555u;
+    /* codes of sample k sit in byte k>>2 (little-endian word w holds samples 16w..16w+15) */
+    const int64_t k0 = w * 16;
+    if (k0 + 16 > nind) {
+      uint32_t keep = 0;
+      for (int j = 0; j < 16; ++j)
+        if (k0 + j < nind) keep |= 3u << ((uint32_t)(j >> 2) * 8u + (3u - (uint32_t)(j & 3)) * 2u);
+      y = (y & keep) | (x & ~keep);
+    }
+    *pw = y;
+  }
+}
+
+extern "C" int gp_set_missingmode(gp_ctx *ctx)
+{
+  if (!ctx) return GP_ERR_ARG;
+  if (!ctx->d_geno) return gp_fail(ctx, GP_ERR_STATE, "gp_set_missingmode: no genotypes loaded");
+  const int64_t words = ctx->nsnp_all * (ctx->rlen_dev >> 2);
+  k_missingmode<<<grid_for(ctx, words, 256), 256, 0, ctx->stream>>>(ctx->d_geno, ctx->rlen_dev,
+                                                                   ctx->nsnp_all, ctx->nind_all);
+  GP_LAUNCH_CHECK(ctx, "k_missingmode");
+  ctx->codes4_rows = 0;
+  ctx->xtx_valid = ctx->eig_valid = ctx->weights_valid = 0;
+  GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return GP_OK;
+}
+
 /* ------------------------------------------------------------------------------------ */
 /* selection masks                                                                        */
 

@@ -47,6 +47,7 @@ void gp_smartpca_defaults(gp_smartpca_opts *o)
   o->fastdim = -1;
   o->fastiter = -1;
   o->seed = 0;
+  o->missingmode = 0;
 }
 
 static int geno_at(const gp_panel *p, int64_t s, int32_t k)
@@ -177,6 +178,14 @@ int gp_smartpca_run(gp_ctx *ctx, const gp_smartpca_opts *o, const gp_panel *p,
   int32_t nrows = 0, ncols = 0;
   for (int32_t k = 0; k < N; ++k)
     if (!ind_ign[k] && aff[k]) xindex[nrows++] = k;
+  /* missingmode (smartpca.c:901-904): setmiss after the pre-filters, then no fancynorm */
+  gp_smartpca_opts om = *o;
+  if (o->missingmode) {
+    rc = gp_set_missingmode(ctx);
+    if (rc) goto done;
+    om.fancynorm = 0;
+  }
+  o = &om;
   /* loadsnpx: non-ignored SNPs with a valid genotype among non-ignored samples */
   for (int32_t k = 0; k < N; ++k) use[k] = (uint8_t)!ind_ign[k];
   rc = gp_valid_counts(ctx, use, NULL, valid_s, NULL);

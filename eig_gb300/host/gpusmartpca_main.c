@@ -17,6 +17,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 #include <unistd.h>
 
 #include "../../include/gpupca.h"
@@ -494,10 +495,7 @@ int main(int argc, char **argv)
   gp_par_dbl(&pf, "outliersigmathresh:", &o.outlthresh);
   gp_par_int(&pf, "outliermode:", &o.outliermode);
   gp_par_int(&pf, "numchrom:", &o.numchrom);
-  if (gp_par_int(&pf, "missingmode:", &t) && t) {
-    fprintf(stderr, "missingmode: YES is not supported by this path\n");
-    return 1;
-  }
+  gp_par_int(&pf, "missingmode:", &o.missingmode);
   if (gp_par_int(&pf, "usepopsformissing:", &t) && t) {
     fprintf(stderr, "usepopsformissing: YES is not supported by this path\n");
     return 1;
@@ -519,6 +517,11 @@ int main(int argc, char **argv)
   if (o.fastmode) {
     if (o.fastiter < 0) o.fastiter = o.numeigs;
     if (o.fastdim < 0) o.fastdim = 2 * o.numeigs;
+    /* rngmode (smartpca.c:679-684): seed 0 draws a seed from the process id, user id and
+     * clock, as seednum does, and the seed is logged */
+    if (o.seed == 0)
+      o.seed = (int64_t)(((long)getpid() + (long)getuid()) << 15) ^ (int64_t)time(NULL);
+    printf("seed: %ld\n", (long)o.seed);
   }
   if (!genotypename || !snpname || !indivname) {
     fprintf(stderr, "genotypename, snpname and indivname are required\n");

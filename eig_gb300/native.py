@@ -26,7 +26,8 @@ PHASES = ["load", "filter", "gram", "eig", "outlier", "weights", "lsqproj", "tot
 
 # every symbol the headers declare (checked by the CPU test suite)
 EXPORTED = ["gp_version", "gp_last_error", "gp_open", "gp_close", "gp_device_bytes",
-            "gp_load_genotypes", "gp_set_missing", "gp_valid_counts", "gp_set_samples",
+            "gp_load_genotypes", "gp_set_missing", "gp_set_missingmode", "gp_valid_counts",
+            "gp_set_samples",
             "gp_set_snps", "gp_xtx", "gp_eigvecs", "gp_ridoutlier", "gp_snp_weights",
             "gp_lsqproj", "gp_fastpca", "gp_smartpca_defaults", "gp_smartpca_run",
             "gp_fail_msg", "gp_genotype_shape", "gp_timer_start", "gp_timer_stop",
@@ -60,7 +61,7 @@ class SmartpcaOpts(C.Structure):
                 ("minallelecnt", C.c_int32), ("maxmissing", C.c_int32),
                 ("lsqproject", C.c_int32), ("noxdata", C.c_int32), ("numchrom", C.c_int32),
                 ("precision", C.c_int32), ("fastmode", C.c_int32), ("fastdim", C.c_int32),
-                ("fastiter", C.c_int32), ("seed", C.c_int64)]
+                ("fastiter", C.c_int32), ("seed", C.c_int64), ("missingmode", C.c_int32)]
 
 
 class Panel(C.Structure):
@@ -106,6 +107,7 @@ def load_library():
         "gp_device_bytes": (C.c_int, [vp, i64p]),
         "gp_load_genotypes": (C.c_int, [vp, u8p, C.c_int64, C.c_int64, C.c_int32, C.c_int32]),
         "gp_set_missing": (C.c_int, [vp, i64p, C.c_int64]),
+        "gp_set_missingmode": (C.c_int, [vp]),
         "gp_valid_counts": (C.c_int, [vp, u8p, u8p, i32p, i32p]),
         "gp_set_samples": (C.c_int, [vp, i32p, C.c_int32]),
         "gp_set_snps": (C.c_int, [vp, i32p, C.c_int32]),
@@ -244,6 +246,10 @@ class Handle:
         pairs = np.ascontiguousarray(pairs, dtype=np.int64).reshape(-1, 2)
         self.check(self.lib.gp_set_missing(self.h, ptr(pairs, C.c_int64), len(pairs)),
                    "gp_set_missing")
+
+    def set_missingmode(self):
+        """missingmode: genotypes become observed (1) / missing (0) indicators (setmiss)"""
+        self.check(self.lib.gp_set_missingmode(self.h), "gp_set_missingmode")
 
     def valid_counts(self, sample_use=None, snp_use=None):
         su = None if sample_use is None else np.ascontiguousarray(sample_use, dtype=np.uint8)

@@ -85,6 +85,14 @@ int gp_genotype_shape(const gp_ctx *ctx, int64_t *nsnp, int32_t *nind);
 int gp_set_missing(gp_ctx *ctx, const int64_t *pairs, int64_t npairs);
 
 /*
+ * missingmode: replace every genotype of the resident panel by the indicator of its being
+ * observed (1 for 0/1/2, 0 for missing), as setmiss does (src/qpsubs.c:462-483, called at
+ * src/eigensrc/smartpca.c:901-904 after the pre-filters; the caller then runs with
+ * fancynorm off).
+ */
+int gp_set_missingmode(gp_ctx *ctx);
+
+/*
  * Valid-genotype counts used by the reference's pre-filters: per SNP over the samples with
  * sample_use[k] != 0 (numvalidgtx src/admutils.c:1136, numvalidgt :1118), and per sample over
  * the SNPs with snp_use[s] != 0 (numvalidgtallind :1075).  Either output may be NULL.

@@ -35,6 +35,7 @@ typedef struct {
   int32_t fastdim;      /* fastdim (-1: 2*numeigs) */
   int32_t fastiter;     /* fastiter (-1: numeigs) */
   int64_t seed;         /* seed (fastmode Omega) */
+  int32_t missingmode;  /* missingmode (NO): PCA of the missingness indicators, no fancynorm */
 } gp_smartpca_opts;
 
 typedef struct {

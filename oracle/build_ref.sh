@@ -8,13 +8,17 @@
 #   * gcc -O2 -fcommon: globals are defined in headers (include/globals.h:4-5).
 #   * LAPACK symbols (dspev_, dpotrf_, ...) are forwarded to the scipy-bundled OpenBLAS,
 #     which exports them with a `scipy_` prefix (ref_lapack_shim.c).
-#   * fastmode (src/ksrc, needs GSL) is replaced by a stub that exits with an error.
+#   * fastmode (src/ksrc/kjg_fpca.c, kjg_gsl.c) is compiled against oracle/gsl_shim: the GSL
+#     API subset it uses (views, gsl_blas_dgemm over CBLAS, GSL's default mt19937) written
+#     from GSL's documentation, and LAPACKE from the same scipy-bundled OpenBLAS.
 #   * fprintf is wrapped (-Wl,--wrap=fprintf, ref_fullprec.c): unchanged output unless
 #     EIG_REF_FULLPREC=1, in which case the .eval/.evec number formats print %.17g so that
 #     1e-10 parity can be checked; smartrel also wraps printf (its relatedness scores).  No reference source is modified or copied.
 set -eu
 HERE=$(cd "$(dirname "$0")" && pwd)
-REF=${EIG_REFERENCE_DIR:-/root/reference}
+# the reference checkout: first argument, else $EIG_REFERENCE_DIR, else a sibling checkout
+# named "reference" next to this repository
+REF=${1:-${EIG_REFERENCE_DIR:-$HERE/../../reference}}
 OUT="$HERE/_ref"
 if [ ! -d "$REF/src" ]; then
   echo "build_ref.sh: reference sources not present ($REF); nothing to build" >&2
@@ -51,10 +55,14 @@ done
 for p in $pids; do wait "$p"; done
 gcc -O2 -c "$HERE/ref_lapack_shim.c" -o "$OUT/obj/ref_lapack_shim.o"
 gcc -O2 -c "$HERE/ref_fullprec.c" -o "$OUT/obj/ref_fullprec.o"
-gcc -O2 -c "$HERE/ref_fastmode_stub.c" -o "$OUT/obj/ref_fastmode_stub.o"
-gcc -o "$OUT/smartpca" $OBJS "$OUT/obj/ref_lapack_shim.o" "$OUT/obj/ref_fullprec.o" \
-    "$OUT/obj/ref_fastmode_stub.o" -Wl,--wrap=fprintf \
+gcc -O2 -I"$HERE/gsl_shim" -c "$HERE/gsl_shim/gsl_shim.c" -o "$OUT/obj/gsl_shim.o"
+for k in kjg_fpca kjg_gsl; do
+  gcc $CFLAGS -I"$HERE/gsl_shim" -c "$REF/src/ksrc/$k.c" -o "$OUT/obj/ksrc_$k.o"
+done
+gcc -o "$OUT/smartpca.new" $OBJS "$OUT/obj/ref_lapack_shim.o" "$OUT/obj/ref_fullprec.o" \
+    "$OUT/obj/ksrc_kjg_fpca.o" "$OUT/obj/ksrc_kjg_gsl.o" "$OUT/obj/gsl_shim.o" -Wl,--wrap=fprintf \
     "$OPENBLAS" -Wl,-rpath,"$(dirname "$OPENBLAS")" -lm -lpthread
+mv -f "$OUT/smartpca.new" "$OUT/smartpca"
 echo "built $OUT/smartpca"
 # smartrel (src/Makefile: smartrel.o twsubs mcio qpsubs admutils egsubs regsubs eigsubs eigx
 # smartsubs + libnick) from the same objects

@@ -181,7 +181,7 @@ def lsqproj(s, ffvecs, fxscal, K, samples):
 def smartpca(records, nind, numeigs=10, numoutliter=5, numoutleigs=10, outlthresh=6.0,
              outliermode=0, fancynorm=1, altnormstyle=1, minallelecnt=1, maxmissing=9999999,
              lsqproject=1, snp_chrom=None, noxdata=1, numchrom=22, ind_ignore=None,
-             ind_affstatus=None, gram_lookup=False, nthreads=1):
+             ind_affstatus=None, gram_lookup=False, nthreads=1, missingmode=0):
     """The hot path of smartpca main() on packed records (sorted SNP order).
 
     Returns evals (all, descending), evecs (top K over the rows), xindex, the per-sample
@@ -201,6 +201,14 @@ def smartpca(records, nind, numeigs=10, numoutliter=5, numoutleigs=10, outlthres
     snp_ign[(snp_ign == 0) & nodata] = 1
     per_ind = valid[snp_ign == 0].sum(axis=0)
     ind_ign |= per_ind == 0
+
+    if missingmode:
+        # setmiss (src/qpsubs.c:462-483) after the pre-filters, then no fancynorm
+        # (src/eigensrc/smartpca.c:901-904): genotypes become 1 = observed, 0 = missing
+        g = valid.astype(np.int8)
+        rec = pack(g)
+        valid = np.ones_like(valid)
+        fancynorm = 0
 
     def rows():
         return np.nonzero(~ind_ign & aff)[0].astype(np.int32)
@@ -459,3 +467,64 @@ def fastpca(records, cols, xindex, K, L, I, omega, fancynorm=1, altnormstyle=1):
     B = X.T @ U
     Ub, Sb, _ = np.linalg.svd(B, full_matrices=False)
     return Sb[:K] ** 2 / m, np.ascontiguousarray(Ub[:, :K].T)
+
+
+class GslMt19937:
+    """GSL's default generator as kjg_gsl_rng_init sets it up (src/ksrc/kjg_gsl.c:100-110):
+    MT19937 (Matsumoto & Nishimura 1998) with its 2002 initialisation, the seed 0 mapped to
+    GSL's default 4357; uniform_pos = the next 32-bit output / 2^32, zero skipped."""
+
+    def __init__(self, seed):
+        s = int(seed) & 0xFFFFFFFFFFFFFFFF
+        if s == 0:
+            s = 4357
+        mt = [s & 0xFFFFFFFF]
+        for i in range(1, 624):
+            mt.append((1812433253 * (mt[-1] ^ (mt[-1] >> 30)) + i) & 0xFFFFFFFF)
+        self.mt, self.i = mt, 624
+
+    def _twist(self):
+        mt = self.mt
+        for k in range(624):
+            y = (mt[k] & 0x80000000) | (mt[(k + 1) % 624] & 0x7FFFFFFF)
+            mt[k] = mt[(k + 397) % 624] ^ (y >> 1) ^ (0x9908B0DF if y & 1 else 0)
+        self.i = 0
+
+    def next32(self):
+        if self.i >= 624:
+            self._twist()
+        y = self.mt[self.i]
+        self.i += 1
+        y ^= y >> 11
+        y ^= (y << 7) & 0x9D2C5680
+        y ^= (y << 15) & 0xEFC60000
+        y ^= y >> 18
+        return y & 0xFFFFFFFF
+
+    def uniform_pos(self):
+        while True:
+            x = self.next32() / 4294967296.0
+            if x != 0.0:
+                return x
+
+
+def gsl_omega(seed, nrows, L):
+    """kjg_gsl_ran_ugaussian_matrix (src/ksrc/kjg_gsl.c:144-190) on a fresh generator: polar
+    Box-Muller pairs along each row, the last column of an odd L holding one uniform draw"""
+    r = GslMt19937(seed)
+    om = np.zeros((nrows, L))
+    for i in range(nrows):
+        j = 0
+        while j + 1 < L:
+            while True:
+                x = -1.0 + 2.0 * r.uniform_pos()
+                y = -1.0 + 2.0 * r.uniform_pos()
+                r2 = x * x + y * y
+                if not (r2 > 1.0 or r2 == 0.0):
+                    break
+            f = np.sqrt(-2.0 * np.log(r2) / r2)
+            om[i, j], om[i, j + 1] = x * f, y * f
+            j += 2
+        if L % 2:
+            om[i, L - 1] = r.uniform_pos()
+    return om

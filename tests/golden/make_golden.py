@@ -80,7 +80,49 @@ CASES = {
                    relatives=[(3, 4, 0.5), (10, 60, 0.5), (20, 21, 0.25), (45, 46, 0.9),
                               (90, 91, 0.5), (100, 101, 0.125)],
                    par={"minallelecnt": "2", "numoutevec": "3"}),
+    # missingmode: the PCA of the missingness indicators (setmiss, fancynorm off); per-sample
+    # missing rates ~U(0, 0.4) so that missingness has structure
+    "bn_missingmode": dict(nsnp=3000, pops=[70, 70, 60], fst=[0.01, 0.02, 0.03], miss=0.0,
+                           miss_hi=0.4, seed=18, fmt="packed",
+                           par={"numoutevec": "4", "missingmode": "YES"}),
 }
+
+# fastmode (kjg_fpca) through the reference built with oracle/gsl_shim: default L = 2K, I = K
+# with Omega from GSL's mt19937 seeded 3, and a second parfile with an odd L (fastdim 7, whose
+# last Omega column holds uniform draws) and fastiter 3
+FAST_CASES = {
+    "bn_fastmode": dict(nsnp=5000, pops=[100, 100, 80], fst=[0.01, 0.03, 0.05], miss=0.01,
+                        n_admixed=20, seed=17,
+                        par={"fastmode": "YES", "numoutevec": "4", "seed": "3"},
+                        runs2={"par_odd": {"fastdim": "7", "fastiter": "3", "numoutevec": "3",
+                                           "seed": "5"}}),
+}
+
+
+def make_fast_case(name, spec):
+    """fastmode writes only the .evec (smartpca.c:955-977): full precision and as shipped"""
+    d = os.path.join(HERE, name)
+    os.makedirs(d, exist_ok=True)
+    prefix = os.path.join(d, "data")
+    native.synth_write_dataset(prefix, spec["nsnp"], spec["pops"], spec["fst"],
+                               miss=spec["miss"], n_admixed=spec.get("n_admixed", 0),
+                               seed=spec["seed"], nthreads=4)
+    base = {"genotypename": "data.geno", "snpname": "data.snp", "indivname": "data.ind",
+            "evecoutname": "out.evec", "evaloutname": "out.eval"}
+    runs = {"par": dict(base, **spec["par"])}
+    for rname, extra in spec.get("runs2", {}).items():
+        runs[rname] = dict(base, **dict(spec["par"], **extra))
+    for rname, par in runs.items():
+        with open(os.path.join(d, rname), "w") as f:
+            for k, v in par.items():
+                f.write("%s: %s\n" % (k, v))
+        tag = "" if rname == "par" else "_" + rname.split("_", 1)[1]
+        for prec, suffix in ((False, ".txt"), (True, "")):
+            env = dict(os.environ, EIG_REF_FULLPREC="1" if prec else "0")
+            with open(os.path.join(d, "ref%s.log" % tag), "w") as log:
+                subprocess.run([REF_BIN, "-p", rname], cwd=d, env=env, stdout=log,
+                               stderr=subprocess.STDOUT, check=True)
+            shutil.move(os.path.join(d, "out.evec"), os.path.join(d, "ref%s.evec%s" % (tag, suffix)))
 
 
 def relocate_snps(prefix, nchrom, step):
@@ -466,6 +508,11 @@ if __name__ == "__main__":
         if only and name not in only:
             continue
         make_convert_case(name, spec)
+        print("made", name)
+    for name, spec in FAST_CASES.items():
+        if only and name not in only:
+            continue
+        make_fast_case(name, spec)
         print("made", name)
     for name, spec in BIG_CASES.items():
         if not only or name not in only:

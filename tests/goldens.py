@@ -4,7 +4,7 @@ import os
 import numpy as np
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = ["bn_outliers", "bn_bed_altnorm", "bn_project", "bn_grm"]
+CASES = ["bn_outliers", "bn_bed_altnorm", "bn_project", "bn_grm", "bn_missingmode"]
 REL_CASES = ["bn_rel"]
 
 
@@ -83,6 +83,8 @@ class Case:
             kw["altnormstyle"] = yesno(p["altnormstyle"])
         if "maxmissing" in p:
             kw["maxmissing"] = int(p["maxmissing"])
+        if "missingmode" in p:
+            kw["missingmode"] = yesno(p["missingmode"])
         return kw
 
     def rel_opts(self):
@@ -274,3 +276,30 @@ def compare_anova(mine, ref):
         assert a[:2] == b[:2] and a[4:] == b[4:]
         assert abs(a[2] - b[2]) <= 1.5e-3 * max(1.0, abs(b[2]) * 1e-6)
         assert abs(a[3] - b[3]) <= 2e-5 * abs(b[3]) + 1e-15, (a, b)
+
+
+class FastCase:
+    """The reference's fastmode runs on bn_fastmode (make_golden.py FAST_CASES): the panel,
+    and per parfile its (K, L, I, seed) and the printed .evec (eigenvalues of the header,
+    unit-norm vectors as rows), at full precision and as shipped."""
+
+    RUNS = {"par": ("", 4, 8, 4, 3), "par_odd": ("_odd", 3, 7, 3, 5)}
+
+    def __init__(self):
+        d = os.path.join(GOLDEN, "bn_fastmode")
+        self.dir = d
+        ind = [l.split() for l in open(os.path.join(d, "data.ind")) if l.strip()]
+        self.ids = [t[0] for t in ind]
+        self.nind = len(ind)
+        self.nsnp = sum(1 for l in open(os.path.join(d, "data.snp")) if l.strip())
+        rlen = max((self.nind + 3) // 4, 48)
+        raw = np.fromfile(os.path.join(d, "data.geno"), np.uint8)[rlen:]
+        self.records = raw.reshape(self.nsnp, rlen).copy()
+
+    def run(self, par):
+        tag, K, L, I, seed = self.RUNS[par]
+        lines = open(os.path.join(self.dir, "ref%s.evec" % tag)).read().splitlines()
+        ev = np.array([float(x) for x in lines[0].split()[1:]])
+        V = np.array([[float(x) for x in l.split()[1:-1]] for l in lines[1:]]).T
+        return dict(K=K, L=L, I=I, seed=seed, evals=ev, evecs=V,
+                    text=open(os.path.join(self.dir, "ref%s.evec.txt" % tag)).read().splitlines())

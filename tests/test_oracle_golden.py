@@ -167,3 +167,34 @@ def test_oracle_fst_matches_reference(par_name, details, tol):
         assert abs(fans[a, b] - fj) <= tol * max(1.0, abs(fj))
         assert abs(fsd[a, b] - sd) <= tol * max(1.0, abs(sd))
         assert fnum[a, b] == n
+
+
+@pytest.mark.parametrize("seed", [0, 3, 5489, 2 ** 32 + 7])
+def test_gsl_mt19937_stream(seed):
+    """the oracle's GSL mt19937 is the published generator: its 32-bit outputs equal numpy's
+    legacy RandomState (MT19937 with the same 2002 initialisation) for the seed GSL uses
+    (0 -> 4357, then the low 32 bits); seed 5489 starts with the published 3499211612"""
+    g = O.GslMt19937(seed)
+    mine = np.array([g.next32() for _ in range(3000)], np.uint64)
+    s = 4357 if seed == 0 else seed & 0xFFFFFFFF
+    ref = np.random.RandomState(s).randint(0, 2 ** 32, size=3000, dtype=np.uint64)
+    assert np.array_equal(mine, ref)
+    if seed == 5489:
+        assert mine[0] == 3499211612
+
+
+@pytest.mark.parametrize("par", ["par", "par_odd"])
+def test_oracle_fastmode_matches_reference(par):
+    """the reference's fastmode (kjg_fpca, built against the GSL shim) against the oracle's
+    numpy kjg_fpca with the same GSL Omega: eigenvalues and unit eigenvectors to 1e-12 (an
+    odd L puts uniform draws in Omega's last column)"""
+    from tests.goldens import FastCase
+    fc = FastCase()
+    r = fc.run(par)
+    om = O.gsl_omega(r["seed"], fc.nind, r["L"])
+    ev, V = O.fastpca(fc.records, np.arange(fc.nsnp, dtype=np.int32),
+                      np.arange(fc.nind, dtype=np.int32), r["K"], r["L"], r["I"], om)
+    assert np.max(np.abs(ev - r["evals"]) / r["evals"]) < 1e-12
+    Vn = V / np.linalg.norm(V, axis=1, keepdims=True)
+    cos = np.abs(np.sum(Vn * r["evecs"], axis=1)) / np.linalg.norm(r["evecs"], axis=1)
+    assert np.all(cos > 1 - 1e-12)

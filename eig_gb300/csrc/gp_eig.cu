@@ -1112,11 +1112,20 @@ __global__ void k_reverse(const double *w, double *out, int n)
     out[i] = w[n - 1 - i];
 }
 
-/*
- * Eigenpairs of the symmetric n x n matrix in ctx->d_xtx (overwritten): d_evals_desc [n]
- * all eigenvalues descending, d_vecs [nvec][n] top eigenvectors (descending).
- */
 int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, double *d_vecs)
+{
+  return gp_eig_sym(ctx, ctx->d_xtx, n, nvec, d_evals_desc, d_vecs);
+}
+
+/*
+ * Eigenpairs of the symmetric n x n device matrix A (overwritten): d_evals_desc [n] all
+ * eigenvalues descending, d_vecs [nvec][n] top eigenvectors (descending).  Only this
+ * library's kernels run unless the matrix is too large for the cooperative kernels' shared
+ * memory (order above 8,533, or a back-transformation slab that does not fit), where cuSOLVER's
+ * sytrd / ormtr take over.
+ */
+int gp_eig_sym(gp_ctx *ctx, double *A_in, int32_t n, int32_t nvec, double *d_evals_desc,
+               double *d_vecs)
 {
   cusolverDnHandle_t h = ctx->solver;
   int lwork = 0, lwork2 = 0;
@@ -1129,17 +1138,28 @@ int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, d
 #define GP_EIG_MARK(i) \
   if (timing) cudaEventRecord(ev[i], ctx->stream)
   /* scratch: d, e, tau, e2, w, work(sytrd), inverse-iteration work, info */
-  if (cusolverDnDsytrd_bufferSize(h, CUBLAS_FILL_MODE_LOWER, n, ctx->d_xtx, n, NULL, NULL, NULL,
-                                  &lwork) != CUSOLVER_STATUS_SUCCESS)
-    return gp_fail(ctx, GP_ERR_SOLVER, "cusolverDnDsytrd_bufferSize failed");
   int nv = nvec > 0 ? nvec : 1;
-  if (cusolverDnDormtr_bufferSize(h, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, n, nv,
-                                  ctx->d_xtx, n, NULL, d_vecs, n, &lwork2) != CUSOLVER_STATUS_SUCCESS)
-    return gp_fail(ctx, GP_ERR_SOLVER, "cusolverDnDormtr_bufferSize failed");
-  int lw = lwork > lwork2 ? lwork : lwork2;
   size_t nd = (size_t)n;
   const size_t G = (size_t)ctx->num_sms;
   const size_t nwy = (nd + WY_B - 1) / WY_B;
+  /* cuSOLVER workspaces only where its fallbacks can run: the tridiagonalisation above the
+   * cooperative kernel's shared memory, or a back-transformation slab that does not fit */
+  const size_t rpb0 = (nd + G - 1) / G;
+  const size_t q_smem0 = sizeof(double) * (rpb0 * (WY_B + (size_t)nv) + (size_t)WY_B * nv +
+                                           WY_B * WY_B + (size_t)WY_B * nv);
+  const char *sy_env = getenv("GP_EIG_CUSOLVER_SYTRD"), *or_env = getenv("GP_EIG_CUSOLVER_ORMTR");
+  const int may_fallback = n < 2 || 24 * nd > 200 * 1024 || (nvec > 0 && q_smem0 > 200 * 1024) ||
+                           (sy_env && sy_env[0] == '1') || (or_env && or_env[0] == '1');
+  if (may_fallback) {
+    if (cusolverDnDsytrd_bufferSize(h, CUBLAS_FILL_MODE_LOWER, n, A_in, n, NULL, NULL, NULL,
+                                    &lwork) != CUSOLVER_STATUS_SUCCESS)
+      return gp_fail(ctx, GP_ERR_SOLVER, "cusolverDnDsytrd_bufferSize failed");
+    if (cusolverDnDormtr_bufferSize(h, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, n,
+                                    nv, A_in, n, NULL, d_vecs, n, &lwork2) !=
+        CUSOLVER_STATUS_SUCCESS)
+      return gp_fail(ctx, GP_ERR_SOLVER, "cusolverDnDormtr_bufferSize failed");
+  }
+  int lw = lwork > lwork2 ? lwork : lwork2;
   /* partials + sums of k_apply_q, then the blocks' T from k_wy_tmat */
   const size_t qpart_n = (G + 1) * (size_t)WY_B * nv + nwy * WY_B * WY_B;
   size_t bytes = sizeof(double) * (9 * nd + 2 * G + (size_t)lw + 6 * nd * nv + 80 + qpart_n) +
@@ -1166,13 +1186,15 @@ int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, d
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tridiag, TR_THREADS, tr_smem);
     coop = dev_coop && per_sm >= 1;
   }
+  if (!coop && !may_fallback)
+    return gp_fail(ctx, GP_ERR_CUDA, "eigensolve: the cooperative tridiagonalisation cannot run");
   GP_EIG_MARK(0);
   int info = 0;
   if (coop) {
     int *d_err = ctx->d_err;
     GP_CUDA(ctx, cudaMemsetAsync(d_err, 0, sizeof(int), ctx->stream));
     GP_CUDA(ctx, cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), ctx->stream));
-    double *A = ctx->d_xtx, *pd2 = parts;
+    double *A = A_in, *pd2 = parts;
     int nn = n;
     {
       int64_t tot = (int64_t)n * n;
@@ -1198,8 +1220,10 @@ int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, d
     if (herr) return gp_fail(ctx, GP_ERR_TIMEOUT, "tridiagonalisation grid barrier timed out");
     float tms = 0.f;
     GP_CUDA(ctx, cudaEventElapsedTime(&tms, ctx->ev_tr0, ctx->ev_tr1));
-    ctx->tridiag_ms = tms;
-    ctx->tridiag_n = n;
+    if (A_in == ctx->d_xtx) { /* the Gram's eigensolve: its time is reported */
+      ctx->tridiag_ms = tms;
+      ctx->tridiag_n = n;
+    }
     if (timing) {
       unsigned long long hp[5];
       cudaMemcpy(hp, phase, sizeof hp, cudaMemcpyDeviceToHost);
@@ -1211,7 +1235,7 @@ int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, d
   } else {
     ctx->tridiag_ms = 0.0;
     ctx->tridiag_n = n;
-    if (cusolverDnDsytrd(h, CUBLAS_FILL_MODE_LOWER, n, ctx->d_xtx, n, d, e, tau, ws, lw,
+    if (cusolverDnDsytrd(h, CUBLAS_FILL_MODE_LOWER, n, A_in, n, d, e, tau, ws, lw,
                          d_info) != CUSOLVER_STATUS_SUCCESS)
       return gp_fail(ctx, GP_ERR_SOLVER, "cusolverDnDsytrd failed to launch");
     GP_CUDA(ctx, gp_memcpy(ctx, &info, d_info, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -1309,12 +1333,14 @@ int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, d
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_apply_q, WY_THREADS, q_smem);
       qcoop = dev_coop && per_sm >= 1;
     }
+    if (!qcoop && !may_fallback)
+      return gp_fail(ctx, GP_ERR_CUDA, "eigensolve: the cooperative back-transformation cannot run");
     if (qcoop) {
       unsigned *qbar = bar + 4;
       int *d_err = ctx->d_err;
       GP_CUDA(ctx, cudaMemsetAsync(d_err, 0, sizeof(int), ctx->stream));
       GP_CUDA(ctx, cudaMemsetAsync(qbar, 0, sizeof(unsigned), ctx->stream));
-      const double *Aq = ctx->d_xtx;
+      const double *Aq = A_in;
       double *Sq = qpart + (size_t)Gq * nent;
       double *Tg = qpart + (size_t)(Gq + 1) * nent;
       const int nwyb = (n - 1 + WY_B - 1) / WY_B;
@@ -1332,7 +1358,7 @@ int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, d
       if (herr) return gp_fail(ctx, GP_ERR_TIMEOUT, "back-transformation grid barrier timed out");
     } else {
       if (cusolverDnDormtr(h, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, n, nvec,
-                           ctx->d_xtx, n, tau, d_vecs, n, ws, lw, d_info) != CUSOLVER_STATUS_SUCCESS)
+                           A_in, n, tau, d_vecs, n, ws, lw, d_info) != CUSOLVER_STATUS_SUCCESS)
         return gp_fail(ctx, GP_ERR_SOLVER, "cusolverDnDormtr failed to launch");
       GP_CUDA(ctx, gp_memcpy(ctx, &info, d_info, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
       GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));

@@ -24,8 +24,10 @@
  *   warp 0      TMA of the B tile (128 slice-columns x 64 k, fp16, 128-byte swizzle);
  *   warp 1      one thread issues 4 tcgen05.mma (128x128x16, f16 -> f32) per k-block into
  *               TMEM buffer (chunk & 1);
- *   warps 2-5   decode the A tile: one thread per row reads 16 bytes of codes (64 k) and
- *               writes 64 fp16 values into shared memory in the same swizzled layout, then
+ *   warps 2-5   decode the A tile: one thread per row reads 16 bytes of codes (64 k; the
+ *               next eight k-blocks' loads in flight) and writes 64 fp16 values into shared
+ *               memory in the same swizzled layout, each code turned into its fp16 value by a
+ *               byte permute of the 4-entry table held in two registers; then
  *               fence.proxy.async + mbarrier arrive;
  *   warps 6-13  epilogue: per chunk tcgen05.ld the exact FP32 sums, add into int32
  *               registers (64 columns per thread), flush with FP64 atomics per work item.
@@ -48,6 +50,7 @@
 #define X_THREADS 448       /* 14 warps */
 #define X_SMEM (XSTAGES * XSTAGE_BYTES + 1024 + 256)
 #define X_CHUNK_KB 128      /* 8,192 k per exact FP32 chunk */
+#define XPF 8               /* k-blocks of codes a decoder thread loads ahead */
 
 #define XERR_FULL 11
 #define XERR_EMPTY 12
@@ -105,17 +108,6 @@ k_geno_panel_tc(const __grid_constant__ CUtensorMap tm_b, const uint8_t *__restr
     mbar_init(drain, 1);
     *abort_flag = 0;
     fence_mbar_init();
-  }
-  /* byte -> four fp16 decode tables (one per 4-entry table): entry b holds the values of
-   * the codes b>>6, (b>>4)&3, (b>>2)&3, b&3 in that order */
-  __shared__ uint2 s_lut[2][256];
-  for (int idx = threadIdx.x; idx < 512; idx += blockDim.x) {
-    const uint64_t lt = (idx >> 8) ? lut_hi : lut_lo;
-    const uint32_t bb = (uint32_t)idx & 255u;
-    uint32_t hv[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) hv[u] = (uint32_t)(lt >> (16 * ((bb >> (6 - 2 * u)) & 3u))) & 0xFFFFu;
-    s_lut[idx >> 8][bb] = make_uint2(hv[0] | (hv[1] << 16), hv[2] | (hv[3] << 16));
   }
   if (warp == 0 && lane == 0) tma_prefetch_desc(&tm_b);
   if (warp == 1) tmem_alloc(tmem_slot, 256);
@@ -193,6 +185,9 @@ k_geno_panel_tc(const __grid_constant__ CUtensorMap tm_b, const uint8_t *__restr
   } else if (warp < 6) {
     /* ---------------- A decoders: one row of the tile per thread ---------------- */
     const int r = (warp - 2) * 32 + lane;
+    /* the 4-entry fp16 tables as byte tables for prmt: code c is bytes 2c, 2c+1 */
+    const uint32_t tlo0 = (uint32_t)lut_lo, tlo1 = (uint32_t)(lut_lo >> 32);
+    const uint32_t thi0 = (uint32_t)lut_hi, thi1 = (uint32_t)(lut_hi >> 32);
     uint32_t it = 0;
     bool ok = true;
     for (int32_t w = blockIdx.x; w < nitems && ok; w += gridDim.x) {
@@ -201,40 +196,54 @@ k_geno_panel_tc(const __grid_constant__ CUtensorMap tm_b, const uint8_t *__restr
       const int32_t grow = rt * XT + r;
       const int64_t crow_idx = grow < nrows ? (row_map ? (int64_t)row_map[grow] : (int64_t)grow) : 0;
       const uint8_t *crow = codes + crow_idx * ldc;
-      /* the row's codes of the next four k-blocks are loaded ahead of the stage waits (the
+      /* the row's codes of the next XPF k-blocks are loaded ahead of the stage waits (the
        * k-block index wraps at kb_period, so loads past kb1 stay inside the row) */
       const bool live = grow < nrows;
       auto ld_codes = [&](int32_t kbx) {
         return live ? __ldg((const uint4 *)(crow + (int64_t)(kbx % kb_period) * 16))
                     : make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
       };
-      uint4 pf0 = ld_codes(kb0), pf1 = ld_codes(kb0 + 1), pf2 = ld_codes(kb0 + 2),
-            pf3 = ld_codes(kb0 + 3);
-      for (int32_t kb = kb0; kb < kb1; ++kb, ++it) {
-        const uint4 raw = pf0;
-        pf0 = pf1;
-        pf1 = pf2;
-        pf2 = pf3;
-        pf3 = ld_codes(kb + 4);
-        uint32_t s = it % XSTAGES, ph = (it / XSTAGES) & 1u;
-        bool got = mbar_wait(&empty[s], ph ^ 1u, abort_flag, err, XERR_EMPTY);
-        if (!got) {
-          ok = false;
-          break;
-        }
-        const uint2 *lut = s_lut[kb < kb_switch ? 0 : 1];
-        uint8_t *row_base = smem + s * XSTAGE_BYTES + r * 128;
-        const uint32_t words[4] = {raw.x, raw.y, raw.z, raw.w};
+      uint4 pf[XPF];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          /* codes 8j..8j+7: bytes 2j, 2j+1 of the 16 (little-endian words), four codes per
-           * table entry */
-          const uint32_t wv = words[j >> 1] >> ((j & 1) * 16);
-          const uint2 lo = lut[wv & 0xFFu], hi = lut[(wv >> 8) & 0xFFu];
-          *(uint4 *)(row_base + ((j ^ (r & 7)) * 16)) = make_uint4(lo.x, lo.y, hi.x, hi.y);
+      for (int u = 0; u < XPF; ++u) pf[u] = ld_codes(kb0 + u);
+      for (int32_t kbb = kb0; kbb < kb1 && ok; kbb += XPF) {
+#pragma unroll
+        for (int u = 0; u < XPF; ++u) {
+          const int32_t kb = kbb + u;
+          if (kb >= kb1) break;
+          const uint4 raw = pf[u];
+          pf[u] = ld_codes(kb + XPF);
+          uint32_t s = it % XSTAGES, ph = (it / XSTAGES) & 1u;
+          ++it;
+          bool got = mbar_wait(&empty[s], ph ^ 1u, abort_flag, err, XERR_EMPTY);
+          if (!got) {
+            ok = false;
+            break;
+          }
+          const bool hi_tab = kb >= kb_switch;
+          const uint32_t t0 = hi_tab ? thi0 : tlo0, t1 = hi_tab ? thi1 : tlo1;
+          uint8_t *row_base = smem + s * XSTAGE_BYTES + r * 128;
+          const uint32_t words[4] = {raw.x, raw.y, raw.z, raw.w};
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            /* codes 8j..8j+7: bytes 2j, 2j+1 of the 16 (little-endian words); a byte holds
+             * four codes, MSB first, and each code c selects bytes 2c, 2c+1 of the table */
+            const uint32_t wv = words[j >> 1] >> ((j & 1) * 16);
+            uint32_t outv[4];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+              const uint32_t b = (wv >> (8 * h)) & 0xFFu;
+              const uint32_t sel01 = ((b >> 6) & 3u) * 0x22u + ((b >> 4) & 3u) * 0x2200u + 0x1010u;
+              const uint32_t sel23 = ((b >> 2) & 3u) * 0x22u + (b & 3u) * 0x2200u + 0x1010u;
+              outv[2 * h] = __byte_perm(t0, t1, sel01);
+              outv[2 * h + 1] = __byte_perm(t0, t1, sel23);
+            }
+            *(uint4 *)(row_base + ((j ^ (r & 7)) * 16)) =
+                make_uint4(outv[0], outv[1], outv[2], outv[3]);
+          }
+          fence_proxy_async_smem();
+          mbar_arrive(&full[s]);
         }
-        fence_proxy_async_smem();
-        mbar_arrive(&full[s]);
       }
     }
   } else {

@@ -133,6 +133,8 @@ int gp_gram_fp64(gp_ctx *ctx);
 int gp_gram_split(gp_ctx *ctx, int precision);
 int gp_launch_symmetrize_trace(gp_ctx *ctx, double *d_trace);
 int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, double *d_vecs);
+int gp_eig_sym(gp_ctx *ctx, double *A, int32_t n, int32_t nvec, double *d_evals_desc,
+               double *d_vecs);
 /* per-sample masked normal equations solve of lsqproj (gp_api.cu); co rows hold the K(K+1)/2
  * pair sums then the observed count, rr rows the K right-hand sides; acoef/bcoef are [K][nproj] */
 __global__ void k_lsq_solve(const double *co, int32_t ldco, const double *rr, int32_t K,

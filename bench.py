@@ -207,7 +207,7 @@ def _serve_load(srv, rows, sizes, offsets, arrivals):
     return lat, max(done_t) - t0, reqs
 
 
-def run_serving(h, cfg, nreq=400, seed=11):
+def run_serving(h, cfg, nreq=400, seed=11, n64=100):
     """Projection serving on the panel left resident by the PCA run: capacity, Poisson
     arrivals at 50% and 80% of it, the FP64 one-request-at-a-time baseline, and the
     coordinate error of the tensor-core path against the FP64 one."""
@@ -257,13 +257,13 @@ def run_serving(h, cfg, nreq=400, seed=11):
                                "samples_per_s": float(sz.sum()) / span,
                                "p50_ms": float(np.percentile(lat, 50)),
                                "p99_ms": float(np.percentile(lat, 99))})
-    # coordinates of a few requests on the tensor-core server, kept for the comparison
-    sz_c, off_c = draw(4)
-    _, _, creqs = _serve_load(srv, rows, sz_c, off_c, np.zeros(4))
+    # the FP64 one-request-at-a-time baseline over n64 requests of the same distribution, and
+    # the tensor-core server's coordinates for the same requests
+    sz_c, off_c = draw(n64)
+    _, _, creqs = _serve_load(srv, rows, sz_c, off_c, np.zeros(n64))
     srv.close()
-    # FP64 baseline: one request at a time, FP64 SIMT products
     s64 = native.Server(h, K, max_batch=2048, pool_samples=4096, fp64_serial=True)
-    lat64, span64, r64 = _serve_load(s64, rows, sz_c, off_c, np.zeros(4))
+    lat64, span64, r64 = _serve_load(s64, rows, sz_c, off_c, np.zeros(n64))
     s64.close()
     err_abs, err_rel = 0.0, 0.0
     for a, b in zip(creqs, r64):
@@ -274,8 +274,8 @@ def run_serving(h, cfg, nreq=400, seed=11):
             err_abs = max(err_abs, float(d.max()))
             err_rel = max(err_rel, float(d.max() / np.abs(b.coords[ok]).max()))
     sps64 = float(sz_c.sum()) / span64
-    out["fp64_serial"] = {"samples_per_s": sps64, "n": 4, "samples": int(sz_c.sum()),
-                          "ms_per_request": span64 / 4 * 1e3}
+    out["fp64_serial"] = {"samples_per_s": sps64, "n": n64, "samples": int(sz_c.sum()),
+                          "ms_per_request": span64 / n64 * 1e3}
     out["speedup_vs_fp64_serial"] = cap_sps / sps64
     out["coord_max_abs_err_vs_fp64"] = err_abs
     out["coord_max_rel_err_vs_fp64"] = err_rel

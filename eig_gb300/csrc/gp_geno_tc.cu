@@ -43,7 +43,7 @@
 
 #define XT 128              /* rows / slice-columns per tile */
 #define XK 64               /* k per k-block */
-#define XSTAGES 4
+#define XSTAGES 6
 #define XA_BYTES (XT * XK * 2)
 #define XB_BYTES (XT * XK * 2)
 #define XSTAGE_BYTES (XA_BYTES + XB_BYTES)

@@ -277,6 +277,7 @@ def test_split_multi_tile_chunks_and_superchunks(gpu, monkeypatch, prec):
     ref = _gram_pair(gpu, rec, nind, rows, cols, native.GP_PREC_FP64)["XTX"]
     monkeypatch.setenv("GP_BF16_BUDGET_BYTES", str(2688 * 4 * 2048))
     r = _gram_pair(gpu, rec, nind, rows, cols, prec)
+    etol, vtol = SPLIT_TOL[prec]
     err = np.max(np.abs(r["XTX"] - ref)) / np.max(np.abs(ref))
     assert err <= etol, err
     w1 = np.linalg.eigvalsh(r["XTX"])[::-1][:20]

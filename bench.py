@@ -46,10 +46,11 @@ CONFIGS = {
                           "M=500000, F~U(0.005,0.05), 1% missing, K=10, L=20, I=10, omega seed 3"),
     "mixed": dict(nsnp=600_000, pops=[500, 700, 800, 900, 1000, 1100],
                   fst=[0.005, 0.01, 0.02, 0.03, 0.04, 0.05], miss=0.02, K=20, seed=2,
-                  jobs=6, nproj=200, rate=40.0, pca_every=21, pca_K=10,
+                  jobs=6, nproj=200, rate=40.0, pca_every=21, pca_K=10, pca_burst=3,
                   name="mixed stream: projection requests on the N=5000 x M=600000 K=20 panel "
                        "+ full-PCA jobs at 1:20 (N log-U 200-8000, M U 50k-600k, 2-8 pops, "
-                       "F~U(0.005,0.05), 1-5% missing, K=10), Poisson arrivals 40/s"),
+                       "F~U(0.005,0.05), 1-5% missing, K=10), Poisson arrivals 40/s after a "
+                       "burst of 3 PCA jobs"),
     "convertf": dict(nsnp=600_000, pops=[500, 700, 800, 900, 1000, 1100],
                      fst=[0.005, 0.01, 0.02, 0.03, 0.04, 0.05], miss=0.02, K=0, seed=2,
                      name="convertf packedancestrymap -> PLINK bed of the N=5000 x M=600000 "
@@ -168,6 +169,18 @@ def accuracy_vs_fp64(h, resident, nind, cfg, r_split, step_ms):
            "kept_samples_identical": bool(same_rows)}
     if same_rows:
         out["subspace_angle_deg"] = _subspace_angle_deg(r64["evecs"][:K], r_split["evecs"][:K])
+        # ridoutlier's z-scores (src/eigensrc/smartsubs.c:18-91) of the last pass's top 10
+        # vectors on both paths: the smallest margin ||z| - sigma| and the largest split-vs-FP64
+        # z difference (a decision could flip only where the latter reaches the former)
+        def z(E):
+            W = E - E.mean(axis=1, keepdims=True)
+            return W / np.sqrt(np.mean(W * W, axis=1, keepdims=True))
+        z64, z16 = z(r64["evecs"][:10]), z(r_split["evecs"][:10])
+        z16 = z16 * np.sign(np.sum(z64 * z16, axis=1, keepdims=True))
+        margin = np.abs(np.abs(z64) - 6.0)
+        out["outlier_margin"] = {"sigma": 6.0, "min_margin": float(margin.min()),
+                                 "max_abs_z": float(np.abs(z64).max()),
+                                 "max_z_diff_split_vs_fp64": float(np.abs(z16 - z64).max())}
     return out
 
 
@@ -357,6 +370,16 @@ def run_mixed(args, cfg, local):
             sizes.append(z)
             offs.append(int(rng.integers(0, npool - z + 1)))
             jidx.append(-1)
+    # a burst: the stream opens with pca_burst full-PCA jobs offered at once, so that jobs
+    # run side by side on the server's PCA workers while projections keep arriving
+    nb = cfg.get("pca_burst", 0)
+    if nb:
+        arrivals = np.concatenate([np.zeros(nb), arrivals])
+        kinds = [1] * nb + kinds
+        jidx = [j % len(jobs) for j in range(nb)] + jidx
+        sizes = [0] * nb + sizes
+        offs = [0] * nb + offs
+        nitems += nb
     done_t = [0.0] * nitems
     reqs = [None] * nitems
     ready = threading.Semaphore(0)

@@ -20,7 +20,9 @@
  *   sum over SNPs     rows = samples, k = kept SNPs (codes in sample-major order)
  *   sum over samples  rows = kept SNPs, k = samples (codes in SNP-major order)
  *
- * Kernel structure (grid-stride over work items = row tile x column tile x k-split):
+ * Kernel structure (grid-stride over work items = row tile x column tile x k-split, the row
+ * tile fastest, so that the CTAs running at one time share the B tile and k range they
+ * stream and B is read from DRAM about once per wave instead of once per row tile):
  *   warp 0      TMA of the B tile (128 slice-columns x 64 k, fp16, 128-byte swizzle);
  *   warp 1      one thread issues 4 tcgen05.mma (128x128x16, f16 -> f32) per k-block into
  *               TMEM buffer (chunk & 1);
@@ -43,7 +45,7 @@
 
 #define XT 128              /* rows / slice-columns per tile */
 #define XK 64               /* k per k-block */
-#define XSTAGES 6
+#define XSTAGES 4
 #define XA_BYTES (XT * XK * 2)
 #define XB_BYTES (XT * XK * 2)
 #define XSTAGE_BYTES (XA_BYTES + XB_BYTES)
@@ -122,7 +124,7 @@ k_geno_panel_tc(const __grid_constant__ CUtensorMap tm_b, const uint8_t *__restr
       uint32_t it = 0;
       bool ok = true;
       for (int32_t w = blockIdx.x; w < nitems && ok; w += gridDim.x) {
-        int32_t ks = w % ksplit, ct = (w / ksplit) % nct;
+        int32_t ks = (w / nrt) % ksplit, ct = w / (nrt * ksplit);
         int32_t kb0 = ks * kb_per, kb1 = kb0 + kb_per < nkb ? kb0 + kb_per : nkb;
         for (int32_t kb = kb0; kb < kb1; ++kb, ++it) {
           uint32_t s = it % XSTAGES, ph = (it / XSTAGES) & 1u;
@@ -151,7 +153,7 @@ k_geno_panel_tc(const __grid_constant__ CUtensorMap tm_b, const uint8_t *__restr
       uint32_t it = 0, chunk = 0;
       bool ok = true;
       for (int32_t w = blockIdx.x; w < nitems && ok; w += gridDim.x) {
-        int32_t ks = w % ksplit;
+        int32_t ks = (w / nrt) % ksplit;
         int32_t kb0 = ks * kb_per, kb1 = kb0 + kb_per < nkb ? kb0 + kb_per : nkb;
         for (int32_t c0 = kb0; c0 < kb1 && ok; c0 += X_CHUNK_KB, ++chunk) {
           int32_t c1 = c0 + X_CHUNK_KB < kb1 ? c0 + X_CHUNK_KB : kb1;
@@ -191,7 +193,7 @@ k_geno_panel_tc(const __grid_constant__ CUtensorMap tm_b, const uint8_t *__restr
     uint32_t it = 0;
     bool ok = true;
     for (int32_t w = blockIdx.x; w < nitems && ok; w += gridDim.x) {
-      int32_t ks = w % ksplit, rt = w / (ksplit * nct);
+      int32_t ks = (w / nrt) % ksplit, rt = w % nrt;
       int32_t kb0 = ks * kb_per, kb1 = kb0 + kb_per < nkb ? kb0 + kb_per : nkb;
       const int32_t grow = rt * XT + r;
       const int64_t crow_idx = grow < nrows ? (row_map ? (int64_t)row_map[grow] : (int64_t)grow) : 0;
@@ -255,7 +257,7 @@ k_geno_panel_tc(const __grid_constant__ CUtensorMap tm_b, const uint8_t *__restr
     uint32_t chunk = 0;
     bool ok = true;
     for (int32_t w = blockIdx.x; w < nitems && ok; w += gridDim.x) {
-      int32_t ks = w % ksplit, ct = (w / ksplit) % nct, rt = w / (ksplit * nct);
+      int32_t ks = (w / nrt) % ksplit, ct = w / (nrt * ksplit), rt = w % nrt;
       int32_t kb0 = ks * kb_per, kb1 = kb0 + kb_per < nkb ? kb0 + kb_per : nkb;
       int32_t acc[64];
 #pragma unroll

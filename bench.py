@@ -530,6 +530,8 @@ def run_gpu(args, cfg, local):
     clk = clocks.stop()
     launches = h.launch_count(reset=True) / max(1, args.steps)
     step_ms = float(np.mean(times))
+    # kernel (a): the per-SNP counts of the last pass
+    c_ms, c_bytes = h.last_counts_time()
     # dominant kernel: the Gram of the last pass
     g_ms, g_launch, g_flops = h.last_gram_time()
     # e2e through the C ABI from pinned host memory
@@ -561,7 +563,7 @@ def run_gpu(args, cfg, local):
                tridiag_ms=float(np.mean(tri_ms)) if tri_ms else 0.0, tridiag_n=tri_n,
                gram_kernel_flops=g_flops, clocks=clk, e2e_ms=e2e_ms, h2d=h2d / n_e2e,
                d2h=d2h / n_e2e, run=r, gen_s=gen_s, peaks=peaks, peak_kind=peak_kind,
-               nind=nind, launches=launches, acc=acc, serving=serving)
+               nind=nind, launches=launches, acc=acc, serving=serving, counts=(c_ms, c_bytes))
     return res
 
 
@@ -848,6 +850,23 @@ def tridiag_roofline(res, peaks, peak_kind):
             "peak_kind": "HBM copy, %s" % peak_kind}
 
 
+def unpack_roofline(res, peaks):
+    """kernel (a), the per-SNP counts / kill rule / value table of the last pass (k_snp_stats):
+    HBM-bound; algorithmic bytes = one read of each selected record and the row mask plus the
+    61 bytes of counts and tables written per SNP, over its CUDA-event time"""
+    ms, nbytes = res.get("counts", (0.0, 0))
+    if ms <= 0.0 or nbytes <= 0:
+        return None
+    achieved = nbytes / (ms * 1e-3) / 1e9
+    peak = peaks.get("hbm_gbs", 6800.0)
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": None,
+            "kernel": "k_snp_stats (per-SNP counts and normalisation, %.3f ms by CUDA events)" % ms,
+            "algorithmic_bytes": nbytes,
+            "traffic_note": "DRAM bytes of an ncu capture at 200,000 SNPs: "
+                            "profiles/snp_stats_5000x200000.md"}
+
+
 def gram_traffic(args):
     """DRAM bytes per launch of the split Gram kernel from the committed ncu summary of the
     full workload (profiles/gram_split_fp16_full_dram.md, one-CTA schedule), or None for other
@@ -1031,7 +1050,8 @@ def main():
             "passes": r["npasses"], "outliers": len(r["outliers"]),
             "gram_kernel_ms": res["gram_ms"],
             "roofline": tridiag_roofline(res, peaks, res["peak_kind"]) or roof,
-            "roofline_gram": roof, "clocks": res["clocks"],
+            "roofline_gram": roof, "roofline_unpack": unpack_roofline(res, peaks),
+            "clocks": res["clocks"],
             "e2e": {"value": e2e, "unit": "TFLOP/s", "h2d_bytes_per_step": int(res["h2d"]),
                     "d2h_bytes_per_step": int(res["d2h"]), "wall_s": res["e2e_ms"] / 1e3},
             "accuracy_vs_fp64": res["acc"], "serving": res["serving"],

@@ -150,6 +150,8 @@ extern "C" int gp_open(int device, gp_ctx **out)
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_g0);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_tr0);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_tr1);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_c0);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_c1);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_g1);
   if (e != cudaSuccess) {
     gp_fail(NULL, GP_ERR_CUDA, "gp_open: %s", cudaGetErrorString(e));
@@ -185,6 +187,8 @@ extern "C" void gp_close(gp_ctx *ctx)
   if (ctx->ev_g0) cudaEventDestroy(ctx->ev_g0);
   if (ctx->ev_tr0) cudaEventDestroy(ctx->ev_tr0);
   if (ctx->ev_tr1) cudaEventDestroy(ctx->ev_tr1);
+  if (ctx->ev_c0) cudaEventDestroy(ctx->ev_c0);
+  if (ctx->ev_c1) cudaEventDestroy(ctx->ev_c1);
   if (ctx->ev_g1) cudaEventDestroy(ctx->ev_g1);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   free(ctx->h_rows);
@@ -1054,6 +1058,20 @@ extern "C" int gp_last_tridiag_time(const gp_ctx *ctx, double *ms, int32_t *n)
   if (!ctx) return GP_ERR_ARG;
   if (ms) *ms = ctx->tridiag_ms;
   if (n) *n = ctx->tridiag_n;
+  return GP_OK;
+}
+
+extern "C" int gp_last_counts_time(const gp_ctx *ctx, double *ms, int64_t *bytes)
+{
+  if (!ctx) return GP_ERR_ARG;
+  float f = 0.f;
+  if (ctx->counts_bytes > 0) {
+    if (cudaEventSynchronize(ctx->ev_c1) != cudaSuccess ||
+        cudaEventElapsedTime(&f, ctx->ev_c0, ctx->ev_c1) != cudaSuccess)
+      return GP_ERR_CUDA;
+  }
+  if (ms) *ms = f;
+  if (bytes) *bytes = ctx->counts_bytes;
   return GP_OK;
 }
 

@@ -582,9 +582,13 @@ k_snp_stats(const uint8_t *__restrict__ geno, int64_t rlen_dev,
 int gp_launch_snp_stats(gp_ctx *ctx, const gp_xtx_opts *o)
 {
   int64_t threads = ((int64_t)ctx->ncols + 31) / 32 * 32;  /* a warp per 32 columns */
+  GP_CUDA(ctx, cudaEventRecord(ctx->ev_c0, ctx->stream));
   k_snp_stats<<<grid_for(ctx, threads, 256), 256, 0, ctx->stream>>>(
       ctx->d_geno, ctx->rlen_dev, ctx->d_rowmask, ctx->d_cols, ctx->ncols, ctx->nrows, *o,
       ctx->d_cnt, ctx->d_killed, ctx->d_vtab, ctx->d_xmean, ctx->d_xfancy);
   GP_LAUNCH_CHECK(ctx, "k_snp_stats");
+  GP_CUDA(ctx, cudaEventRecord(ctx->ev_c1, ctx->stream));
+  /* one read of each selected record and the row mask, 61 bytes out per column */
+  ctx->counts_bytes = (int64_t)ctx->ncols * (ctx->rlen_dev + 61) + ctx->rlen_dev;
   return GP_OK;
 }

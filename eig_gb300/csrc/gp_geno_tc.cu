@@ -49,7 +49,8 @@
 #define XA_BYTES (XT * XK * 2)
 #define XB_BYTES (XT * XK * 2)
 #define XSTAGE_BYTES (XA_BYTES + XB_BYTES)
-#define X_THREADS 448       /* 14 warps */
+#define X_THREADS 576       /* 18 warps */
+#define X_DEC_WARPS 8       /* decoder warps: two threads per row of the A tile */
 #define X_SMEM (XSTAGES * XSTAGE_BYTES + 1024 + 256)
 #define X_CHUNK_KB 128      /* 8,192 k per exact FP32 chunk */
 #define XPF 8               /* k-blocks of codes a decoder thread loads ahead */
@@ -100,7 +101,7 @@ k_geno_panel_tc(const __grid_constant__ CUtensorMap tm_b, const uint8_t *__restr
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < XSTAGES; ++s) {
-      mbar_init(&full[s], 1 + XT);
+      mbar_init(&full[s], 1 + 32 * X_DEC_WARPS);
       mbar_init(&empty[s], 1);
     }
     for (int b = 0; b < 2; ++b) {
@@ -184,9 +185,9 @@ k_geno_panel_tc(const __grid_constant__ CUtensorMap tm_b, const uint8_t *__restr
         }
       }
     }
-  } else if (warp < 6) {
-    /* ---------------- A decoders: one row of the tile per thread ---------------- */
-    const int r = (warp - 2) * 32 + lane;
+  } else if (warp < 2 + X_DEC_WARPS) {
+    /* ---------------- A decoders: two threads per row of the tile ---------------- */
+    const int dt = (warp - 2) * 32 + lane, r = dt >> 1, hb = dt & 1;
     /* the 4-entry fp16 tables as byte tables for prmt: code c is bytes 2c, 2c+1 */
     const uint32_t tlo0 = (uint32_t)lut_lo, tlo1 = (uint32_t)(lut_lo >> 32);
     const uint32_t thi0 = (uint32_t)lut_hi, thi1 = (uint32_t)(lut_hi >> 32);
@@ -197,15 +198,16 @@ k_geno_panel_tc(const __grid_constant__ CUtensorMap tm_b, const uint8_t *__restr
       int32_t kb0 = ks * kb_per, kb1 = kb0 + kb_per < nkb ? kb0 + kb_per : nkb;
       const int32_t grow = rt * XT + r;
       const int64_t crow_idx = grow < nrows ? (row_map ? (int64_t)row_map[grow] : (int64_t)grow) : 0;
-      const uint8_t *crow = codes + crow_idx * ldc;
-      /* the row's codes of the next XPF k-blocks are loaded ahead of the stage waits (the
-       * k-block index wraps at kb_period, so loads past kb1 stay inside the row) */
+      const uint8_t *crow = codes + crow_idx * ldc + 8 * hb;
+      /* this thread's half (8 bytes, 32 codes) of the row's codes of the next XPF k-blocks are
+       * loaded ahead of the stage waits (the k-block index wraps at kb_period, so loads past
+       * kb1 stay inside the row) */
       const bool live = grow < nrows;
       auto ld_codes = [&](int32_t kbx) {
-        return live ? __ldg((const uint4 *)(crow + (int64_t)(kbx % kb_period) * 16))
-                    : make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
+        return live ? __ldg((const uint2 *)(crow + (int64_t)(kbx % kb_period) * 16))
+                    : make_uint2(0xFFFFFFFFu, 0xFFFFFFFFu);
       };
-      uint4 pf[XPF];
+      uint2 pf[XPF];
 #pragma unroll
       for (int u = 0; u < XPF; ++u) pf[u] = ld_codes(kb0 + u);
       for (int32_t kbb = kb0; kbb < kb1 && ok; kbb += XPF) {
@@ -213,7 +215,7 @@ k_geno_panel_tc(const __grid_constant__ CUtensorMap tm_b, const uint8_t *__restr
         for (int u = 0; u < XPF; ++u) {
           const int32_t kb = kbb + u;
           if (kb >= kb1) break;
-          const uint4 raw = pf[u];
+          const uint2 raw = pf[u];
           pf[u] = ld_codes(kb + XPF);
           uint32_t s = it % XSTAGES, ph = (it / XSTAGES) & 1u;
           ++it;
@@ -225,12 +227,14 @@ k_geno_panel_tc(const __grid_constant__ CUtensorMap tm_b, const uint8_t *__restr
           const bool hi_tab = kb >= kb_switch;
           const uint32_t t0 = hi_tab ? thi0 : tlo0, t1 = hi_tab ? thi1 : tlo1;
           uint8_t *row_base = smem + s * XSTAGE_BYTES + r * 128;
-          const uint32_t words[4] = {raw.x, raw.y, raw.z, raw.w};
+          const uint32_t words[2] = {raw.x, raw.y};
 #pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            /* codes 8j..8j+7: bytes 2j, 2j+1 of the 16 (little-endian words); a byte holds
-             * four codes, MSB first, and each code c selects bytes 2c, 2c+1 of the table */
-            const uint32_t wv = words[j >> 1] >> ((j & 1) * 16);
+          for (int jj = 0; jj < 4; ++jj) {
+            /* codes 8j..8j+7 (j = 4 hb + jj): bytes 2j, 2j+1 of the row's 16 (little-endian
+             * words); a byte holds four codes, MSB first, and each code c selects bytes 2c,
+             * 2c+1 of the table */
+            const int j = 4 * hb + jj;
+            const uint32_t wv = words[jj >> 1] >> ((jj & 1) * 16);
             uint32_t outv[4];
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
@@ -249,8 +253,8 @@ k_geno_panel_tc(const __grid_constant__ CUtensorMap tm_b, const uint8_t *__restr
       }
     }
   } else {
-    /* ---------------- epilogue: warps 6..13 ---------------- */
-    const int q = warp & 3, half = (warp - 6) >> 2;
+    /* ---------------- epilogue: warps 2 + X_DEC_WARPS .. (8 warps) ---------------- */
+    const int q = warp & 3, half = (warp - 2 - X_DEC_WARPS) >> 2;
     const int row = q * 32 + lane;
     const int col0 = half * 64;
     const uint32_t t_acc = tmem + ((uint32_t)(q * 32) << 16);

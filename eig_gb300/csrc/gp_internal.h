@@ -74,6 +74,8 @@ struct gp_ctx {
   double gram_flops;
   double encode_ms;      /* k_encode time of the last device-output gp_encode_records */
   cudaEvent_t ev_tr0, ev_tr1;
+  cudaEvent_t ev_c0, ev_c1; /* around the last k_snp_stats launch */
+  int64_t counts_bytes;     /* its algorithmic bytes (0: none yet) */
   double tridiag_ms;     /* k_tridiag time of the last eigensolve (0: cuSOLVER sytrd ran) */
   int32_t tridiag_n;     /* its order */
 

@@ -31,7 +31,8 @@ EXPORTED = ["gp_version", "gp_last_error", "gp_open", "gp_close", "gp_device_byt
             "gp_set_snps", "gp_xtx", "gp_eigvecs", "gp_ridoutlier", "gp_snp_weights",
             "gp_lsqproj", "gp_fastpca", "gp_smartpca_defaults", "gp_smartpca_run",
             "gp_fail_msg", "gp_genotype_shape", "gp_timer_start", "gp_timer_stop",
-            "gp_last_gram_time", "gp_last_tridiag_time", "gp_host_register",
+            "gp_last_gram_time", "gp_last_tridiag_time", "gp_last_counts_time",
+            "gp_host_register",
             "gp_host_unregister",
             "gp_transfer_bytes", "gp_launch_count", "gp_gram_fp64_noalloc",
             "gp_noalloc_last_error", "gp_serve_open", "gp_serve_layout",
@@ -126,6 +127,7 @@ def load_library():
         "gp_timer_stop": (C.c_int, [vp, f64p]),
         "gp_last_gram_time": (C.c_int, [vp, f64p, i32p, f64p]),
         "gp_last_tridiag_time": (C.c_int, [vp, f64p, i32p]),
+        "gp_last_counts_time": (C.c_int, [vp, f64p, i64p]),
         "gp_host_register": (C.c_int, [vp, C.c_size_t]),
         "gp_host_unregister": (C.c_int, [vp]),
         "gp_transfer_bytes": (C.c_int, [vp, i64p, i64p, C.c_int32]),
@@ -351,6 +353,13 @@ class Handle:
         self.check(self.lib.gp_last_tridiag_time(self.h, C.byref(ms), C.byref(n)),
                    "gp_last_tridiag_time")
         return ms.value, n.value
+
+    def last_counts_time(self):
+        """(ms, algorithmic bytes) of the last pass's per-SNP counts kernel"""
+        ms, b = C.c_double(), C.c_int64()
+        self.check(self.lib.gp_last_counts_time(self.h, C.byref(ms), C.byref(b)),
+                   "gp_last_counts_time")
+        return ms.value, b.value
 
     def encode_records(self, fmt, snps, samples=None, flip=None, nsamples=None, out=None):
         """convertf's genotype records (gp_encode_records) of the resident panel: SNP list,

@@ -266,6 +266,11 @@ int gp_last_gram_time(const gp_ctx *ctx, double *ms, int32_t *launches, double *
  * cuSOLVER's sytrd instead. */
 int gp_last_tridiag_time(const gp_ctx *ctx, double *ms, int32_t *n);
 
+/* Device time of the per-SNP counts kernel (k_snp_stats) of the last pass (CUDA events around
+ * its launch on the handle's stream; waits for it) and its algorithmic bytes: one read of
+ * each selected record and of the row mask, 61 bytes of counts and tables written per SNP. */
+int gp_last_counts_time(const gp_ctx *ctx, double *ms, int64_t *bytes);
+
 /* Device time of the k_encode launch of the last gp_encode_records call that wrote to
  * device memory (CUDA events around it on the handle's stream). */
 int gp_last_encode_time(const gp_ctx *ctx, double *ms);

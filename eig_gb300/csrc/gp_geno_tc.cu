@@ -26,12 +26,13 @@
  *   warp 0      TMA of the B tile (128 slice-columns x 64 k, fp16, 128-byte swizzle);
  *   warp 1      one thread issues 4 tcgen05.mma (128x128x16, f16 -> f32) per k-block into
  *               TMEM buffer (chunk & 1);
- *   warps 2-5   decode the A tile: one thread per row reads 16 bytes of codes (64 k; the
- *               next eight k-blocks' loads in flight) and writes 64 fp16 values into shared
- *               memory in the same swizzled layout, each code turned into its fp16 value by a
- *               byte permute of the 4-entry table held in two registers; then
- *               fence.proxy.async + mbarrier arrive;
- *   warps 6-13  epilogue: per chunk tcgen05.ld the exact FP32 sums, add into int32
+ *   warps 2-9   decode the A tile, two threads per row: each reads 8 bytes of codes (32 k;
+ *               the next eight k-blocks' loads in flight) and writes 32 fp16 values into
+ *               shared memory in the same swizzled layout, each code turned into its fp16
+ *               value by a byte permute of the 4-entry table held in two registers; then
+ *               fence.proxy.async + mbarrier arrive (the decode bounds the kernel: four
+ *               decoder warps, one thread per row, left the tensor pipe ~20% busy);
+ *   warps 10-17 epilogue: per chunk tcgen05.ld the exact FP32 sums, add into int32
  *               registers (64 columns per thread), flush with FP64 atomics per work item.
  */
 #include <cuda.h>

@@ -31,7 +31,7 @@ NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-ffp
 CUDA_SOURCES = ["gp_api.cu", "gp_geno.cu", "gp_gram_f64.cu", "gp_geno_gemm_f64.cu",
                 "gp_gram_bf16.cu", "gp_fast.cu",
                 "gp_noalloc.cu", "gp_geno_tc.cu", "gp_eig.cu", "gp_serve.cu", "gp_convert.cu",
-                "gp_fst.cu"]
+                "gp_fst.cu", "gp_popfill.cu"]
 HOST_LIB_SOURCES = ["gp_smartpca.c"]
 # no FMA contraction in host code: the reference's host arithmetic is plain multiply-add
 # (aarch64 would otherwise fuse it)

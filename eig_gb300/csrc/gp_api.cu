@@ -177,7 +177,7 @@ extern "C" void gp_close(gp_ctx *ctx)
                   ctx->d_killed, ctx->d_vtab,    ctx->d_xmean,   ctx->d_xfancy,  ctx->d_kept,
                   ctx->d_xtx,    ctx->d_evals,   ctx->d_evecs,   ctx->d_ffvecs,  ctx->d_fxscal,
                   ctx->d_scratch, ctx->d_scratch2, ctx->d_scratch3, ctx->d_scratch4, ctx->d_scratch5,
-                  ctx->d_err,   ctx->d_xtx_keep};
+                  ctx->d_err,   ctx->d_xtx_keep, ctx->d_rowpop, ctx->d_gtab, ctx->d_gfill};
   for (size_t i = 0; i < sizeof(bufs) / sizeof(bufs[0]); ++i)
     if (bufs[i]) cudaFree(bufs[i]);
   if (ctx->solver) cusolverDnDestroy(ctx->solver);
@@ -206,7 +206,8 @@ extern "C" int gp_release(gp_ctx *ctx)
                    (void **)&ctx->d_kept,    (void **)&ctx->d_xtx,      (void **)&ctx->d_evals,
                    (void **)&ctx->d_evecs,   (void **)&ctx->d_ffvecs,   (void **)&ctx->d_fxscal,
                    (void **)&ctx->d_scratch, (void **)&ctx->d_scratch2, (void **)&ctx->d_scratch3,
-                   (void **)&ctx->d_scratch4, (void **)&ctx->d_scratch5, (void **)&ctx->d_xtx_keep};
+                   (void **)&ctx->d_scratch4, (void **)&ctx->d_scratch5, (void **)&ctx->d_xtx_keep,
+                   (void **)&ctx->d_rowpop,  (void **)&ctx->d_gtab,     (void **)&ctx->d_gfill};
   for (size_t i = 0; i < sizeof(bufs) / sizeof(bufs[0]); ++i) {
     if (*bufs[i]) cudaFree(*bufs[i]);
     *bufs[i] = NULL;
@@ -222,6 +223,7 @@ extern "C" int gp_release(gp_ctx *ctx)
   ctx->nind_all = 0;
   ctx->rlen_dev = 0;
   ctx->nrows = ctx->ncols = ctx->nkept = ctx->nvec = ctx->nweights = 0;
+  ctx->npop = 0;
   ctx->xtx_valid = ctx->eig_valid = ctx->weights_valid = 0;
   return GP_OK;
 }
@@ -268,7 +270,19 @@ extern "C" int gp_xtx(gp_ctx *ctx, const gp_xtx_opts *opts, int32_t *n0, int32_t
   }
   ctx->xtx_valid = ctx->eig_valid = ctx->weights_valid = 0;
   ctx->precision = opts->precision;
-  int rc = gp_launch_snp_stats(ctx, opts);
+  int rc;
+  if (ctx->npop > 0) {
+    /* usepopsformissing: the observed counts first (the missing-count rule waits for the
+     * fill), then the filled tables, counts and kill flags */
+    if (opts->precision != GP_PREC_FP64)
+      return gp_fail(ctx, GP_ERR_ARG, "gp_xtx: usepopsformissing runs in FP64 precision only");
+    gp_xtx_opts o1 = *opts;
+    o1.maxmissing = 0x7FFFFFFF;
+    rc = gp_launch_snp_stats(ctx, &o1);
+    if (!rc) rc = gp_popfill_pass(ctx, opts);
+  } else {
+    rc = gp_launch_snp_stats(ctx, opts);
+  }
   if (rc) return rc;
 
   /* kept-column list (ascending) built from the kill flags */
@@ -936,8 +950,9 @@ __global__ void k_lsq_solve(const double *co, int32_t ldco, const double *rr, in
   }
 }
 
-extern "C" int gp_lsqproj(gp_ctx *ctx, int32_t numeigs, const int32_t *samples, int32_t nproj,
-                          double *acoeffs, double *bcoeffs, int32_t *nobs, int32_t *status)
+static int lsqproj_impl(gp_ctx *ctx, int32_t numeigs, const int32_t *samples,
+                        const int32_t *sample_pop, int32_t npop, int32_t nproj, double *acoeffs,
+                        double *bcoeffs, int32_t *nobs, int32_t *status)
 {
   if (!ctx || !acoeffs || (nproj > 0 && !samples)) return GP_ERR_ARG;
   if (!ctx->weights_valid)
@@ -955,8 +970,17 @@ extern "C" int gp_lsqproj(gp_ctx *ctx, int32_t numeigs, const int32_t *samples, 
   size_t nE = (size_t)nk * K, nP = (size_t)nk * ldp;
   size_t nco = (size_t)nproj * ldp, nrr = (size_t)nproj * K;
   size_t nwork = (size_t)nproj * (K * K + 2 * K);
+  const bool pf = sample_pop != NULL && npop > 0;
+  if (pf && ctx->precision != GP_PREC_FP64)
+    return gp_fail(ctx, GP_ERR_ARG, "gp_lsqproj_pops: usepopsformissing runs in FP64 precision only");
+  if (pf)
+    for (int32_t q = 0; q < nproj; ++q)
+      if (sample_pop[q] >= npop)
+        return gp_fail(ctx, GP_ERR_ARG, "gp_lsqproj_pops: population %d >= npop %d",
+                       sample_pop[q], npop);
+  const size_t off_fill = pf ? gp_lsq_fill_work_bytes(nproj, nk, npop) : 0;
   size_t bytes = off_tab + sizeof(double) * (nE + nP + nco + nrr + nwork + 2 * nrr) +
-                 sizeof(int32_t) * (3 * (size_t)nproj) + 1024;
+                 sizeof(int32_t) * (4 * (size_t)nproj) + off_fill + 1024;
   uint8_t *base;
   int rc = gp_scratch(ctx, bytes, (void **)&base);
   if (rc) return rc;
@@ -967,8 +991,18 @@ extern "C" int gp_lsqproj(gp_ctx *ctx, int32_t numeigs, const int32_t *samples, 
   double *d_P = d_E + nE, *d_co = d_P + nP, *d_rr = d_co + nco, *d_work = d_rr + nrr;
   double *d_a = d_work + nwork, *d_b = d_a + nrr;
   int32_t *d_samp = (int32_t *)(d_b + nrr), *d_nobs = d_samp + nproj, *d_st = d_nobs + nproj;
+  int32_t *d_spop = d_st + nproj;
+  void *fill_work = (void *)((((uintptr_t)(d_spop + nproj)) + 255) & ~(uintptr_t)255);
   GP_CUDA(ctx, gp_memcpy(ctx, d_samp, samples, sizeof(int32_t) * (size_t)nproj,
                                cudaMemcpyHostToDevice, ctx->stream));
+  double *d_raw = NULL, *d_of = NULL, *d_rf = NULL;
+  if (pf && nk > 0) {
+    GP_CUDA(ctx, gp_memcpy(ctx, d_spop, sample_pop, sizeof(int32_t) * (size_t)nproj,
+                           cudaMemcpyHostToDevice, ctx->stream));
+    rc = gp_lsq_fill_tables(ctx, d_samp, d_spop, nproj, npop, K, kt.snprec, kt.ot, nk,
+                            fill_work, &d_raw, &d_of, &d_rf);
+    if (rc) return rc;
+  }
   if (nk) {
     int blocks = (nk + EP_THREADS / 32 - 1) / (EP_THREADS / 32);
     if (blocks > ctx->num_sms * 16) blocks = ctx->num_sms * 16;
@@ -1000,6 +1034,14 @@ extern "C" int gp_lsqproj(gp_ctx *ctx, int32_t numeigs, const int32_t *samples, 
     gp_tc_panel pr[2] = {{tmp, K, 1.0, 1}, {tmp + (size_t)nk * K, K, -1.0, 0}};
     rc = gp_geno_panel_tc_codes(ctx, &A, 2, pr, K, d_rr, K);
     if (rc) return rc;
+  } else if (d_raw) {
+    /* usepopsformissing: a filled genotype counts as observed with its fixxrow value */
+    rc = gp_geno_gemm_f64_fill(ctx, d_samp, d_spop, nproj, kt.snprec, kt.ot, d_of, npop, nk,
+                               d_P, ldp, ldp, d_co, ldp);
+    if (rc) return rc;
+    rc = gp_geno_gemm_f64_fill(ctx, d_samp, d_spop, nproj, kt.snprec, kt.rt, d_rf, npop, nk,
+                               d_E, K, K, d_rr, K);
+    if (rc) return rc;
   } else {
     rc = gp_geno_gemm_f64(ctx, 1, d_samp, nproj, kt.snprec, kt.ot, nk, d_P, ldp, ldp, d_co, ldp);
     if (rc) return rc;
@@ -1020,17 +1062,47 @@ extern "C" int gp_lsqproj(gp_ctx *ctx, int32_t numeigs, const int32_t *samples, 
   if (bcoeffs)
     GP_CUDA(ctx, gp_memcpy(ctx, bcoeffs, d_b, sizeof(double) * nrr, cudaMemcpyDeviceToHost,
                                  ctx->stream));
-  if (nobs)
-    GP_CUDA(ctx, gp_memcpy(ctx, nobs, d_nobs, sizeof(int32_t) * (size_t)nproj,
-                                 cudaMemcpyDeviceToHost, ctx->stream));
+  std::vector<int32_t> hn((size_t)nproj);
+  GP_CUDA(ctx, gp_memcpy(ctx, hn.data(), d_nobs, sizeof(int32_t) * (size_t)nproj,
+                         cudaMemcpyDeviceToHost, ctx->stream));
+  std::vector<double> raw;
+  if (d_raw) {
+    raw.resize((size_t)nproj);
+    GP_CUDA(ctx, gp_memcpy(ctx, raw.data(), d_raw, sizeof(double) * (size_t)nproj,
+                           cudaMemcpyDeviceToHost, ctx->stream));
+  }
   GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   for (int32_t q = 0; q < nproj; ++q) {
+    if (d_raw && raw[(size_t)q] <= (double)K) {
+      /* the coverage check runs on the observed genotypes, before any fill */
+      st[(size_t)q] = 1;
+      hn[(size_t)q] = (int32_t)raw[(size_t)q];
+      if (bcoeffs)
+        for (int32_t j = 0; j < K; ++j) bcoeffs[(size_t)j * nproj + q] = 0.0;
+    }
+    if (nobs) nobs[q] = hn[(size_t)q];
     if (status) status[q] = st[(size_t)q];
     if (st[(size_t)q] == 2) continue; /* left untouched, as the reference keeps regans */
     for (int32_t j = 0; j < K; ++j)
-      acoeffs[(size_t)j * nproj + q] = ha[(size_t)j * nproj + q];
+      acoeffs[(size_t)j * nproj + q] = st[(size_t)q] == 1 ? 0.0 : ha[(size_t)j * nproj + q];
   }
   return GP_OK;
+}
+
+extern "C" int gp_lsqproj(gp_ctx *ctx, int32_t numeigs, const int32_t *samples, int32_t nproj,
+                          double *acoeffs, double *bcoeffs, int32_t *nobs, int32_t *status)
+{
+  return lsqproj_impl(ctx, numeigs, samples, NULL, 0, nproj, acoeffs, bcoeffs, nobs, status);
+}
+
+extern "C" int gp_lsqproj_pops(gp_ctx *ctx, int32_t numeigs, const int32_t *samples,
+                               const int32_t *sample_pop, int32_t npop, int32_t nproj,
+                               double *acoeffs, double *bcoeffs, int32_t *nobs, int32_t *status)
+{
+  if (!sample_pop || npop <= 0)
+    return gp_fail(ctx, GP_ERR_ARG, "gp_lsqproj_pops: sample populations are required");
+  return lsqproj_impl(ctx, numeigs, samples, sample_pop, npop, nproj, acoeffs, bcoeffs, nobs,
+                      status);
 }
 
 /* ------------------------------------------------------------------------------------ */

@@ -299,6 +299,7 @@ extern "C" int gp_set_samples(gp_ctx *ctx, const int32_t *xindex, int32_t nrows)
   memcpy(hr, xindex, sizeof(int32_t) * (size_t)nrows);
   ctx->h_rows = hr;
   ctx->nrows = nrows;
+  ctx->npop = 0; /* the row populations belong to the previous rows */
   ctx->codes4_rows = 0;
   ctx->xtx_valid = ctx->eig_valid = ctx->weights_valid = 0;
   GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));

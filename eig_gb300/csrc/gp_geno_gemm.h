@@ -13,4 +13,13 @@ int gp_geno_gemm_f64(gp_ctx *ctx, int sum_over_snps, const int32_t *d_samp, int3
                      const int32_t *d_snprec, const double *d_tab, int32_t nsnp,
                      const double *d_B, int64_t ldb, int32_t ncc, double *d_C, int64_t ldc);
 
+/*
+ * The sum over SNPs with usepopsformissing: a missing genotype of sample q takes
+ * d_fill[s*npop + d_spop[q]] instead of T_s[3] (T_s[3] when d_spop[q] < 0).
+ */
+int gp_geno_gemm_f64_fill(gp_ctx *ctx, const int32_t *d_samp, const int32_t *d_spop,
+                          int32_t nsamp, const int32_t *d_snprec, const double *d_tab,
+                          const double *d_fill, int32_t npop, int32_t nsnp, const double *d_B,
+                          int64_t ldb, int32_t ncc, double *d_C, int64_t ldc);
+
 #endif

@@ -27,24 +27,28 @@ __device__ __forceinline__ uint32_t code_at(const uint8_t *__restrict__ rec, int
 
 __global__ void __launch_bounds__(256)
 k_gemm_sum_snps(const uint8_t *__restrict__ geno, int64_t rlen, const int32_t *__restrict__ samp,
-                int32_t nsamp, const int32_t *__restrict__ snprec, const double *__restrict__ tab,
-                int32_t nsnp, const double *__restrict__ B, int64_t ldb, int32_t ncc, double *C,
-                int64_t ldc, int32_t kper, int64_t split_stride)
+                const int32_t *__restrict__ spop, int32_t nsamp,
+                const int32_t *__restrict__ snprec, const double *__restrict__ tab,
+                const double *__restrict__ fill, int32_t npop, int32_t nsnp,
+                const double *__restrict__ B, int64_t ldb, int32_t ncc, double *C, int64_t ldc,
+                int32_t kper, int64_t split_stride)
 {
   __shared__ double As[TK][TT + 1];
   __shared__ double Bs[TK][TT + 1];
   __shared__ double tabs[TK][4];
   __shared__ const uint8_t *recs[TK];
+  __shared__ const double *fills[TK];
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   const int32_t q0 = (int32_t)blockIdx.y * TT, c0 = (int32_t)blockIdx.x * TT;
   const int32_t kb = (int32_t)blockIdx.z * kper;
   const int32_t ke = kb + kper < nsnp ? kb + kper : nsnp;
   const int lk = tid & 15, lr = tid >> 4;
-  int32_t srow[4];
+  int32_t srow[4], sp[4];
 #pragma unroll
   for (int p = 0; p < 4; ++p) {
     int32_t q = q0 + lr + 16 * p;
     srow[p] = q < nsamp ? samp[q] : -1;
+    sp[p] = (fill && q < nsamp) ? spop[q] : -1;
   }
   double acc[4][4];
 #pragma unroll
@@ -61,16 +65,21 @@ k_gemm_sum_snps(const uint8_t *__restrict__ geno, int64_t rlen, const int32_t *_
         tabs[tid][1] = tab[4 * s + 1];
         tabs[tid][2] = tab[4 * s + 2];
         tabs[tid][3] = tab[4 * s + 3];
+        fills[tid] = fill ? fill + (int64_t)s * npop : NULL;
       } else {
         recs[tid] = NULL;
       }
     }
     __syncthreads();
     const uint8_t *rec = recs[lk];
+    const double *fl = fills[lk];
 #pragma unroll
     for (int p = 0; p < 4; ++p) {
       double v = 0.0;
-      if (rec && srow[p] >= 0) v = tabs[lk][code_at(rec, srow[p])];
+      if (rec && srow[p] >= 0) {
+        const uint32_t cd = code_at(rec, srow[p]);
+        v = (cd == 3u && fl && sp[p] >= 0) ? fl[sp[p]] : tabs[lk][cd];
+      }
       As[lk][lr + 16 * p] = v;
     }
     /* B tile: 16 SNP rows x 64 columns */
@@ -217,8 +226,9 @@ static int pick_split(const gp_ctx *ctx, int64_t out_tiles, int32_t depth)
   return nsplit;
 }
 
-int gp_geno_gemm_f64(gp_ctx *ctx, int sum_over_snps, const int32_t *d_samp, int32_t nsamp,
-                     const int32_t *d_snprec, const double *d_tab, int32_t nsnp,
+static int geno_gemm(gp_ctx *ctx, int sum_over_snps, const int32_t *d_samp,
+                     const int32_t *d_spop, int32_t nsamp, const int32_t *d_snprec,
+                     const double *d_tab, const double *d_fill, int32_t npop, int32_t nsnp,
                      const double *d_B, int64_t ldb, int32_t ncc, double *d_C, int64_t ldc)
 {
   int32_t out_rows = sum_over_snps ? nsamp : nsnp;
@@ -245,9 +255,9 @@ int gp_geno_gemm_f64(gp_ctx *ctx, int sum_over_snps, const int32_t *d_samp, int3
     if (rc) return rc;
   }
   if (sum_over_snps)
-    k_gemm_sum_snps<<<grid, 256, 0, ctx->stream>>>(ctx->d_geno, ctx->rlen_dev, d_samp, nsamp,
-                                                   d_snprec, d_tab, nsnp, d_B, ldb, ncc, dst, ld,
-                                                   kper, stride);
+    k_gemm_sum_snps<<<grid, 256, 0, ctx->stream>>>(ctx->d_geno, ctx->rlen_dev, d_samp, d_spop,
+                                                   nsamp, d_snprec, d_tab, d_fill, npop, nsnp,
+                                                   d_B, ldb, ncc, dst, ld, kper, stride);
   else
     k_gemm_sum_samples<<<grid, 256, 0, ctx->stream>>>(ctx->d_geno, ctx->rlen_dev, d_samp,
                                                       nsamp, d_snprec, d_tab, nsnp, d_B, ldb, ncc,
@@ -262,4 +272,21 @@ int gp_geno_gemm_f64(gp_ctx *ctx, int sum_over_snps, const int32_t *d_samp, int3
     GP_LAUNCH_CHECK(ctx, "k_sum_parts");
   }
   return GP_OK;
+}
+
+int gp_geno_gemm_f64(gp_ctx *ctx, int sum_over_snps, const int32_t *d_samp, int32_t nsamp,
+                     const int32_t *d_snprec, const double *d_tab, int32_t nsnp,
+                     const double *d_B, int64_t ldb, int32_t ncc, double *d_C, int64_t ldc)
+{
+  return geno_gemm(ctx, sum_over_snps, d_samp, NULL, nsamp, d_snprec, d_tab, NULL, 0, nsnp, d_B,
+                   ldb, ncc, d_C, ldc);
+}
+
+int gp_geno_gemm_f64_fill(gp_ctx *ctx, const int32_t *d_samp, const int32_t *d_spop,
+                          int32_t nsamp, const int32_t *d_snprec, const double *d_tab,
+                          const double *d_fill, int32_t npop, int32_t nsnp, const double *d_B,
+                          int64_t ldb, int32_t ncc, double *d_C, int64_t ldc)
+{
+  return geno_gemm(ctx, 1, d_samp, d_spop, nsamp, d_snprec, d_tab, d_fill, npop, nsnp, d_B, ldb,
+                   ncc, d_C, ldc);
 }

@@ -9,6 +9,9 @@
  * FP64 rate is low by design); it is the parity baseline the split-BF16 path is measured
  * against.  When the triangle has fewer tiles than the GPU has SMs the SNP range is split
  * and the partial triangles are summed in a fixed order (deterministic).
+ * With usepopsformissing (fill != NULL) a missing genotype of row i takes the value
+ * fill[c*npop + rowpop[i]] of its population (0 for a row without one), the getcolxz values
+ * of smartpca.c:3161-3184.
  */
 #include <cuda_runtime.h>
 
@@ -35,13 +38,15 @@ __device__ __forceinline__ void tri_index(int32_t t, int32_t *bi, int32_t *bj)
 __global__ void __launch_bounds__(256)
 k_gram_f64(const uint8_t *__restrict__ geno, int64_t rlen, const int32_t *__restrict__ rows,
            int32_t nrows, const int32_t *__restrict__ cols, const int32_t *__restrict__ kept,
-           int32_t nkept, const double *__restrict__ vtab, int32_t kper, double *out,
+           int32_t nkept, const double *__restrict__ vtab, const double *__restrict__ fill,
+           int32_t npop, const int32_t *__restrict__ rowpop, int32_t kper, double *out,
            int64_t ldo, int64_t split_stride)
 {
   __shared__ double As[GK][GT + 1];
   __shared__ double Bs[GK][GT + 1];
   __shared__ double tabs[GK][4];
   __shared__ const uint8_t *recs[GK];
+  __shared__ const double *fills[GK];
 
   int32_t bi, bj;
   tri_index((int32_t)blockIdx.x, &bi, &bj);
@@ -54,12 +59,14 @@ k_gram_f64(const uint8_t *__restrict__ geno, int64_t rlen, const int32_t *__rest
 
   /* rows this thread decodes for the A and B tiles */
   const int lk = tid & 15, lr = tid >> 4;
-  int32_t arow[4], brow[4];
+  int32_t arow[4], brow[4], apop[4], bpop[4];
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     int32_t ri = i0 + lr + 16 * q, rj = j0 + lr + 16 * q;
     arow[q] = ri < nrows ? rows[ri] : -1;
     brow[q] = rj < nrows ? rows[rj] : -1;
+    apop[q] = (fill && ri < nrows) ? rowpop[ri] : -1;
+    bpop[q] = (fill && rj < nrows) ? rowpop[rj] : -1;
   }
 
   double acc[4][4];
@@ -78,18 +85,26 @@ k_gram_f64(const uint8_t *__restrict__ geno, int64_t rlen, const int32_t *__rest
         tabs[tid][1] = vtab[4 * c + 1];
         tabs[tid][2] = vtab[4 * c + 2];
         tabs[tid][3] = 0.0;
+        fills[tid] = fill ? fill + (int64_t)c * npop : NULL;
       } else {
         recs[tid] = NULL;
       }
     }
     __syncthreads();
     const uint8_t *rec = recs[lk];
+    const double *fl = fills[lk];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       double va = 0.0, vb = 0.0;
       if (rec) {
-        if (arow[q] >= 0) va = tabs[lk][geno_code(rec, arow[q])];
-        if (brow[q] >= 0) vb = tabs[lk][geno_code(rec, brow[q])];
+        if (arow[q] >= 0) {
+          const uint32_t cd = geno_code(rec, arow[q]);
+          va = (cd == 3u && fl && apop[q] >= 0) ? fl[apop[q]] : tabs[lk][cd];
+        }
+        if (brow[q] >= 0) {
+          const uint32_t cd = geno_code(rec, brow[q]);
+          vb = (cd == 3u && fl && bpop[q] >= 0) ? fl[bpop[q]] : tabs[lk][cd];
+        }
       }
       As[lk][lr + 16 * q] = va;
       Bs[lk][lr + 16 * q] = vb;
@@ -181,11 +196,16 @@ int gp_gram_fp64(gp_ctx *ctx)
 
   GP_CUDA(ctx, cudaMemsetAsync(ctx->d_xtx, 0, sizeof(double) * (size_t)n * n, ctx->stream));
   if (ctx->nkept == 0) return GP_OK;
+  /* usepopsformissing: the filled values' table and the population fill values */
+  const bool pf = ctx->npop > 0;
+  const double *tab = pf ? ctx->d_gtab : ctx->d_vtab;
+  const double *fill = pf ? ctx->d_gfill : NULL;
+  const int32_t *rowpop = pf ? ctx->d_rowpop : NULL;
   if (nsplit == 1) {
     dim3 grid((unsigned)ntiles, 1);
     k_gram_f64<<<grid, 256, 0, ctx->stream>>>(ctx->d_geno, ctx->rlen_dev, ctx->d_rows, n,
-                                              ctx->d_cols, ctx->d_kept, ctx->nkept, ctx->d_vtab,
-                                              kper, ctx->d_xtx, n, 0);
+                                              ctx->d_cols, ctx->d_kept, ctx->nkept, tab, fill,
+                                              ctx->npop, rowpop, kper, ctx->d_xtx, n, 0);
     GP_LAUNCH_CHECK(ctx, "k_gram_f64");
     ctx->gram_launches = 1;
     return GP_OK;
@@ -197,8 +217,8 @@ int gp_gram_fp64(gp_ctx *ctx)
   GP_CUDA(ctx, cudaMemsetAsync(part, 0, sizeof(double) * (size_t)stride * nsplit, ctx->stream));
   dim3 grid((unsigned)ntiles, (unsigned)nsplit);
   k_gram_f64<<<grid, 256, 0, ctx->stream>>>(ctx->d_geno, ctx->rlen_dev, ctx->d_rows, n,
-                                            ctx->d_cols, ctx->d_kept, ctx->nkept, ctx->d_vtab, kper,
-                                            part, n, stride);
+                                            ctx->d_cols, ctx->d_kept, ctx->nkept, tab, fill,
+                                            ctx->npop, rowpop, kper, part, n, stride);
   GP_LAUNCH_CHECK(ctx, "k_gram_f64");
   ctx->gram_launches = 1;
   int blocks = (int)((stride + 255) / 256);

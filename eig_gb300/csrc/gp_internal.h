@@ -44,6 +44,12 @@ struct gp_ctx {
   double *d_xfancy;      /* [ncols] */
   int32_t *d_kept;       /* [ncols] compacted list of kept columns (positions in cols) */
   int32_t nkept;
+  /* usepopsformissing (gp_set_row_pops): the rows' population indices and, after gp_xtx,
+   * the Gram's table of the filled column and the populations' fill values */
+  int32_t *d_rowpop;     /* [nrows] (< 0: no population) */
+  int32_t npop;          /* 0: off (gp_set_samples turns it off) */
+  double *d_gtab;        /* [4*ncols] */
+  double *d_gfill;       /* [ncols*npop] */
   int xtx_valid;
   double trace;        /* unscaled trace of the last Gram */
 
@@ -131,6 +137,13 @@ int gp_realloc(gp_ctx *ctx, void **ptr, size_t bytes);
 int gp_launch_valid_counts(gp_ctx *ctx, const uint8_t *d_sample_use, const uint8_t *d_snp_use,
                            int32_t *d_snp_valid, int32_t *d_sample_valid);
 int gp_launch_snp_stats(gp_ctx *ctx, const gp_xtx_opts *o);
+/* usepopsformissing (gp_popfill.cu): the filled Gram tables of a pass, and lsqproj's fill
+ * tables (work: gp_lsq_fill_work_bytes; raw = observed kept genotypes per sample) */
+int gp_popfill_pass(gp_ctx *ctx, const gp_xtx_opts *o);
+size_t gp_lsq_fill_work_bytes(int32_t nproj, int32_t nk, int32_t npop);
+int gp_lsq_fill_tables(gp_ctx *ctx, const int32_t *d_samp, const int32_t *d_spop, int32_t nproj,
+                       int32_t npop, int32_t K, const int32_t *d_snprec, const double *d_ot,
+                       int32_t nk, void *work, double **d_raw, double **d_of, double **d_rf);
 int gp_gram_fp64(gp_ctx *ctx);
 int gp_gram_split(gp_ctx *ctx, int precision);
 int gp_launch_symmetrize_trace(gp_ctx *ctx, double *d_trace);

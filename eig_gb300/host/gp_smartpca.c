@@ -7,7 +7,10 @@
  *   (:869-881), loadindx/loadsnpx (:936-937), the outlier loop (:1077-1265: gp_xtx,
  *   gp_eigvecs, gp_ridoutlier), SNP weights (:1485-1525: gp_snp_weights), lsqproj
  *   (:1553: gp_lsqproj) with seteigscale (:4758-4782) and the rescale (:1556-1564), and
- *   fastmode (:950-980: gp_fastpca, printevecs normalisation :3845-3871).
+ *   fastmode (:950-980: gp_fastpca, printevecs normalisation :3845-3871);
+ *   usepopsformissing: the xtypes array (:928-943, :1095-1099, :1505-1508) handed to
+ *   gp_set_row_pops per pass and, indexed by the sample's .ind position as lsqproj reads it
+ *   (:4658-4690), to gp_lsqproj_pops.
  *
  * Parfile parsing and the .evec/.eval text live in the CLI (gpusmartpca_main.c); this file
  * works on in-memory arrays so the same flow serves the CLI and the ctypes callers.
@@ -48,6 +51,7 @@ void gp_smartpca_defaults(gp_smartpca_opts *o)
   o->fastiter = -1;
   o->seed = 0;
   o->missingmode = 0;
+  o->usepopsformissing = 0;
 }
 
 static int geno_at(const gp_panel *p, int64_t s, int32_t k)
@@ -79,7 +83,8 @@ int gp_smartpca_run(gp_ctx *ctx, const gp_smartpca_opts *o, const gp_panel *p,
   double t0 = now_s(), t;
   uint8_t *snp_ign = NULL, *ind_ign = NULL, *aff = NULL, *use = NULL, *kill = NULL;
   int32_t *valid_s = NULL, *valid_i = NULL, *xindex = NULL, *cols = NULL, *badlist = NULL;
-  int32_t *vecno = NULL, *nobs = NULL, *status = NULL, *projidx = NULL;
+  int32_t *vecno = NULL, *nobs = NULL, *status = NULL, *projidx = NULL, *xtypes = NULL;
+  int32_t *sampop = NULL, npop = 0;
   double *evals = NULL, *evecs = NULL, *score = NULL, *fxscal = NULL, *acoef = NULL,
          *bcoef = NULL;
   memset(r->t_phase, 0, sizeof r->t_phase);
@@ -105,6 +110,24 @@ int gp_smartpca_run(gp_ctx *ctx, const gp_smartpca_opts *o, const gp_panel *p,
   if (!snp_ign || !ind_ign || !aff || !use || !kill || !valid_s || !valid_i || !xindex || !cols ||
       !badlist || !vecno || !score)
     FAIL(GP_ERR_NOMEM);
+  if (o->usepopsformissing) {
+    if (!p->ind_pop)
+      FAIL(gp_fail_msg(ctx, GP_ERR_ARG, "usepopsformissing needs the samples' populations"));
+    if (o->precision != GP_PREC_FP64)
+      FAIL(gp_fail_msg(ctx, GP_ERR_ARG, "usepopsformissing runs in FP64 precision only"));
+    if (o->fastmode)
+      FAIL(gp_fail_msg(ctx, GP_ERR_ARG, "usepopsformissing with fastmode is not supported"));
+    /* xtypes[i]: population of row i, written for the rows of every pass and never cleared
+     * (-2 before the first), as the reference keeps it */
+    xtypes = (int32_t *)malloc(sizeof(int32_t) * (size_t)N);
+    sampop = (int32_t *)malloc(sizeof(int32_t) * (size_t)N);
+    if (!xtypes || !sampop) FAIL(GP_ERR_NOMEM);
+    for (int32_t k = 0; k < N; ++k) {
+      xtypes[k] = -2;
+      if (p->ind_pop[k] >= npop) npop = p->ind_pop[k] + 1;
+    }
+    if (npop < 1) npop = 1;
+  }
 
   /* ---- upload (inpack / getbedgenos) and the male-X-het rule -------------------------- */
   if (p->records) {
@@ -267,6 +290,10 @@ int gp_smartpca_run(gp_ctx *ctx, const gp_smartpca_opts *o, const gp_panel *p,
     t = now_s();
     rc = gp_set_samples(ctx, xindex, nrows);
     if (!rc) rc = gp_set_snps(ctx, cols, ncols);
+    if (!rc && xtypes) {
+      for (int32_t i = 0; i < nrows; ++i) xtypes[i] = p->ind_pop[xindex[i]];
+      rc = gp_set_row_pops(ctx, xtypes, npop);
+    }
     if (rc) goto done;
     double trace;
     int32_t nused;
@@ -349,7 +376,13 @@ int gp_smartpca_run(gp_ctx *ctx, const gp_smartpca_opts *o, const gp_panel *p,
     nobs = (int32_t *)calloc((size_t)nproj, sizeof(int32_t));
     status = (int32_t *)calloc((size_t)nproj, sizeof(int32_t));
     if (!acoef || !bcoef || !nobs || !status) FAIL(GP_ERR_NOMEM);
-    rc = gp_lsqproj(ctx, K, projidx, nproj, acoef, bcoef, nobs, status);
+    if (xtypes) {
+      /* lsqproj reads xtypes at the sample's .ind index (idnum), not at its row */
+      for (int32_t q = 0; q < nproj; ++q) sampop[q] = xtypes[projidx[q]];
+      rc = gp_lsqproj_pops(ctx, K, projidx, sampop, npop, nproj, acoef, bcoef, nobs, status);
+    } else {
+      rc = gp_lsqproj(ctx, K, projidx, nproj, acoef, bcoef, nobs, status);
+    }
     if (rc) goto done;
     /* the reference keeps the previous regans for a non-PD system (regsubs.c:51-53) */
     double prev[64];
@@ -422,5 +455,7 @@ done:
   free(nobs);
   free(status);
   free(projidx);
+  free(xtypes);
+  free(sampop);
   return rc;
 }

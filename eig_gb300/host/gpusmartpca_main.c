@@ -496,10 +496,7 @@ int main(int argc, char **argv)
   gp_par_int(&pf, "outliermode:", &o.outliermode);
   gp_par_int(&pf, "numchrom:", &o.numchrom);
   gp_par_int(&pf, "missingmode:", &o.missingmode);
-  if (gp_par_int(&pf, "usepopsformissing:", &t) && t) {
-    fprintf(stderr, "usepopsformissing: YES is not supported by this path\n");
-    return 1;
-  }
+  gp_par_int(&pf, "usepopsformissing:", &o.usepopsformissing);
   if (gp_par_int(&pf, "ldregress:", &t) && t > 0) {
     fprintf(stderr, "ldregress is not supported by this path\n");
     return 1;
@@ -568,6 +565,47 @@ int main(int argc, char **argv)
     for (int32_t k = 0; k < N; ++k) aff[k] = (uint8_t)in_list(inds.pop[k], names, nn);
   }
 
+  /* usepopsformissing: each sample's index in the population list (xtypes, smartpca.c:
+   * 928-943): the poplist order, else the order of first appearance among the samples not
+   * ignored (makeeglist); -1 when the population is not listed */
+  int32_t *ind_pop = NULL;
+  if (o.usepopsformissing) {
+    if (o.fastmode) {
+      fprintf(stderr, "usepopsformissing with fastmode is not supported by this path\n");
+      return 1;
+    }
+    char **eg = (char **)malloc(sizeof(char *) * (size_t)(N + 4096));
+    int numeg = 0;
+    if (poplistname) {
+      FILE *pl = fopen(poplistname, "r");
+      char line[1024];
+      while (pl && fgets(line, sizeof line, pl) && numeg < N + 4096) {
+        char w[256];
+        if (sscanf(line, "%255s", w) != 1 || w[0] == '#') continue;
+        eg[numeg++] = strdup(w);
+      }
+      if (pl) fclose(pl);
+    } else {
+      for (int32_t k = 0; k < N; ++k) {
+        if (inds.ignore[k]) continue;
+        int found = 0;
+        for (int e = 0; e < numeg && !found; ++e) found = strcmp(eg[e], inds.pop[k]) == 0;
+        if (!found) eg[numeg++] = strdup(inds.pop[k]);
+      }
+    }
+    ind_pop = (int32_t *)malloc(sizeof(int32_t) * (size_t)N);
+    for (int32_t k = 0; k < N; ++k) {
+      ind_pop[k] = -1;
+      for (int e = 0; e < numeg; ++e)
+        if (strcmp(eg[e], inds.pop[k]) == 0) {
+          ind_pop[k] = e;
+          break;
+        }
+    }
+    for (int e = 0; e < numeg; ++e) free(eg[e]);
+    free(eg);
+  }
+
   gp_panel p;
   memset(&p, 0, sizeof p);
   p.records = records;
@@ -579,6 +617,7 @@ int main(int argc, char **argv)
   p.ind_ignore = inds.ignore;
   p.ind_affstatus = aff;
   p.ind_male = male;
+  p.ind_pop = ind_pop;
 
   int32_t K = o.numeigs > 0 ? o.numeigs : 1;
   gp_run_result r;

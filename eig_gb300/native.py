@@ -40,7 +40,8 @@ EXPORTED = ["gp_version", "gp_last_error", "gp_open", "gp_close", "gp_device_byt
             "gp_serve_stats", "gp_serve_last_error", "gp_serve_close", "gp_serve_pause",
             "gp_serve_submit_pca", "gp_serve_pca_stats", "gp_smartpca_footprint", "gp_release",
             "gp_keep_gram", "gp_relate", "gp_record_bytes", "gp_encode_records",
-            "gp_last_encode_time", "gp_fst", "gp_set_blocks"]
+            "gp_last_encode_time", "gp_fst", "gp_set_blocks", "gp_set_row_pops",
+            "gp_lsqproj_pops"]
 
 i32p = C.POINTER(C.c_int32)
 i64p = C.POINTER(C.c_int64)
@@ -62,14 +63,15 @@ class SmartpcaOpts(C.Structure):
                 ("minallelecnt", C.c_int32), ("maxmissing", C.c_int32),
                 ("lsqproject", C.c_int32), ("noxdata", C.c_int32), ("numchrom", C.c_int32),
                 ("precision", C.c_int32), ("fastmode", C.c_int32), ("fastdim", C.c_int32),
-                ("fastiter", C.c_int32), ("seed", C.c_int64), ("missingmode", C.c_int32)]
+                ("fastiter", C.c_int32), ("seed", C.c_int64), ("missingmode", C.c_int32),
+                ("usepopsformissing", C.c_int32)]
 
 
 class Panel(C.Structure):
     _fields_ = [("records", u8p), ("record_bytes", C.c_int64), ("nsnp", C.c_int64),
                 ("nind", C.c_int32), ("code", C.c_int32), ("snp_chrom", i32p),
                 ("snp_ignore", u8p), ("ind_ignore", u8p), ("ind_affstatus", u8p),
-                ("ind_male", u8p)]
+                ("ind_male", u8p), ("ind_pop", i32p)]
 
 
 class ServeOpts(C.Structure):
@@ -119,6 +121,9 @@ def load_library():
                                     i32p, f64p]),
         "gp_snp_weights": (C.c_int, [vp, C.c_int32, f64p, f64p, f64p]),
         "gp_lsqproj": (C.c_int, [vp, C.c_int32, i32p, C.c_int32, f64p, f64p, i32p, i32p]),
+        "gp_set_row_pops": (C.c_int, [vp, i32p, C.c_int32]),
+        "gp_lsqproj_pops": (C.c_int, [vp, C.c_int32, i32p, i32p, C.c_int32, C.c_int32, f64p,
+                                      f64p, i32p, i32p]),
         "gp_fastpca": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, f64p,
                                  C.POINTER(XtxOpts), f64p, f64p]),
         "gp_smartpca_defaults": (None, [C.POINTER(SmartpcaOpts)]),
@@ -310,16 +315,32 @@ class Handle:
                    "gp_snp_weights")
         return ff, fx, sc
 
-    def lsqproj(self, numeigs, samples):
+    def set_row_pops(self, row_pop, npop):
+        """usepopsformissing: the current rows' population indices (< 0: none)"""
+        rp = None if row_pop is None else np.ascontiguousarray(row_pop, dtype=np.int32)
+        self.check(self.lib.gp_set_row_pops(self.h, ptr(rp, C.c_int32), int(npop)),
+                   "gp_set_row_pops")
+
+    def lsqproj(self, numeigs, samples, sample_pop=None, npop=0):
+        """lsqproject; with sample_pop (and npop) the usepopsformissing fill"""
         s = np.ascontiguousarray(samples, dtype=np.int32)
         q = len(s)
         a = np.zeros((numeigs, q))
         b = np.zeros((numeigs, q))
         nobs = np.zeros(q, np.int32)
         st = np.zeros(q, np.int32)
-        self.check(self.lib.gp_lsqproj(self.h, numeigs, ptr(s, C.c_int32), q, ptr(a, C.c_double),
-                                       ptr(b, C.c_double), ptr(nobs, C.c_int32),
-                                       ptr(st, C.c_int32)), "gp_lsqproj")
+        if sample_pop is None:
+            self.check(self.lib.gp_lsqproj(self.h, numeigs, ptr(s, C.c_int32), q,
+                                           ptr(a, C.c_double), ptr(b, C.c_double),
+                                           ptr(nobs, C.c_int32), ptr(st, C.c_int32)),
+                       "gp_lsqproj")
+        else:
+            sp = np.ascontiguousarray(sample_pop, dtype=np.int32)
+            self.check(self.lib.gp_lsqproj_pops(self.h, numeigs, ptr(s, C.c_int32),
+                                                ptr(sp, C.c_int32), int(npop), q,
+                                                ptr(a, C.c_double), ptr(b, C.c_double),
+                                                ptr(nobs, C.c_int32), ptr(st, C.c_int32)),
+                       "gp_lsqproj_pops")
         return a, b, nobs, st
 
     def timer_start(self):
@@ -600,7 +621,7 @@ class _RunArgs:
 
     def __init__(self, records, nind, opts, code=GP_CODE_PACKED, snp_chrom=None,
                  snp_ignore=None, ind_ignore=None, ind_affstatus=None, ind_male=None,
-                 want_xtx=False):
+                 want_xtx=False, ind_pop=None):
         self.keep = []
         if isinstance(records, tuple):  # (nsnp, record_bytes): the panel resident on the handle
             rec = None
@@ -623,7 +644,8 @@ class _RunArgs:
                            ptr(arr(snp_ignore, np.uint8), C.c_uint8),
                            ptr(arr(ind_ignore, np.uint8), C.c_uint8),
                            ptr(arr(ind_affstatus, np.uint8), C.c_uint8),
-                           ptr(arr(ind_male, np.uint8), C.c_uint8))
+                           ptr(arr(ind_male, np.uint8), C.c_uint8),
+                           ptr(arr(ind_pop, np.int32), C.c_int32))
         K = max(opts.numeigs, 1)
         out = dict(xindex=np.zeros(nind, np.int32), evals=np.zeros(nind),
                    evecs=np.zeros(K * nind), coords=np.zeros(K * nind),
@@ -661,10 +683,11 @@ class _RunArgs:
 
 def smartpca_run(handle, records, nind, opts, code=GP_CODE_PACKED, snp_chrom=None,
                  snp_ignore=None, ind_ignore=None, ind_affstatus=None, ind_male=None,
-                 want_xtx=False):
-    """Run the whole smartpca hot path (gp_smartpca_run) on in-memory records."""
+                 want_xtx=False, ind_pop=None):
+    """Run the whole smartpca hot path (gp_smartpca_run) on in-memory records.  ind_pop
+    (the samples' population indices) is read with opts.usepopsformissing."""
     a = _RunArgs(records, nind, opts, code, snp_chrom, snp_ignore, ind_ignore, ind_affstatus,
-                 ind_male, want_xtx)
+                 ind_male, want_xtx, ind_pop)
     handle.check(handle.lib.gp_smartpca_run(handle.h, C.byref(opts), C.byref(a.panel),
                                             C.byref(a.result)), "gp_smartpca_run")
     return a.collect()
@@ -675,7 +698,8 @@ def smartrel_run(handle, records, nind, numeigs=10, relthresh=0.05, minallelecnt
     """smartrel on in-memory records: the smartpca outlier loop with smartrel's SNP rule
     (dropped when min(n0, n1) <= minallelecnt, no missingness limit, no projection), then the
     relatedness scan.  Returns (pairs [(sample a, sample b, y)] highest first, run result)."""
-    panel_keys = ("snp_chrom", "snp_ignore", "ind_ignore", "ind_affstatus", "ind_male")
+    panel_keys = ("snp_chrom", "snp_ignore", "ind_ignore", "ind_affstatus", "ind_male",
+                  "ind_pop")
     panel = {k: kw.pop(k) for k in panel_keys if k in kw}
     opts = default_opts(numeigs=numeigs, minallelecnt=minallelecnt + 1, maxmissing=0x7fffffff,
                         lsqproject=0, fastmode=0, **kw)

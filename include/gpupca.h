@@ -177,6 +177,30 @@ int gp_lsqproj(gp_ctx *ctx, int32_t numeigs, const int32_t *samples, int32_t npr
                double *acoeffs, double *bcoeffs, int32_t *nobs, int32_t *status);
 
 /*
+ * usepopsformissing (smartpca's parfile option; FP64 precision only).
+ *
+ * gp_set_row_pops: the population index of each current row (row_pop [nrows]: the xtypes
+ * value, smartpca.c:1095-1099; < 0 = none) and npop > every index.  The next gp_xtx then
+ * fills a missing genotype of a row with its population's mean genotype over the rows
+ * observed in that column (getcolxz smartpca.c:3141-3184); the column's mean and fancy scale
+ * run over the observed and filled values in row order (fvadjust :2236-2279), and the kill
+ * rule's missing count is the count still missing after the fill.  The SNP weights keep the
+ * observed-only table (getcolxf :3564-3592); xmean/xfancy of gp_xtx are the filled ones.
+ * gp_set_samples turns the option off (call this after it); NULL or npop <= 0 turns it off.
+ *
+ * gp_lsqproj_pops: gp_lsqproj with lsqproj's fill (smartpca.c:4631-4746): sample_pop [nproj]
+ * is the population index the reference reads for each sample (xtypes at the sample's .ind
+ * index; < 0 = none).  Samples with at most numeigs observed genotypes are dropped
+ * (status 1) before the population sums; the others with a population add their observed
+ * genotypes to it, and a missing genotype of a sample whose population has observed ones in
+ * that column is filled with their mean and counts as observed (nobs includes it).
+ */
+int gp_set_row_pops(gp_ctx *ctx, const int32_t *row_pop, int32_t npop);
+int gp_lsqproj_pops(gp_ctx *ctx, int32_t numeigs, const int32_t *samples,
+                    const int32_t *sample_pop, int32_t npop, int32_t nproj, double *acoeffs,
+                    double *bcoeffs, int32_t *nobs, int32_t *status);
+
+/*
  * fastmode randomized block-Krylov PCA (kjg_fpca src/ksrc/kjg_fpca.c:24-102 with the data
  * table of setgval src/gval.c:31-87) over the current rows and columns: X (ncols x nrows)
  * holds ((g - mean) fancy)/sqrt(2), missing 0 (opts: fancynorm, altnormstyle and precision

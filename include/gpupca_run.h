@@ -36,6 +36,8 @@ typedef struct {
   int32_t fastiter;     /* fastiter (-1: numeigs) */
   int64_t seed;         /* seed (fastmode Omega) */
   int32_t missingmode;  /* missingmode (NO): PCA of the missingness indicators, no fancynorm */
+  int32_t usepopsformissing; /* usepopsformissing (NO): missing -> population mean (FP64
+                                precision, not with fastmode; needs gp_panel.ind_pop) */
 } gp_smartpca_opts;
 
 typedef struct {
@@ -50,6 +52,9 @@ typedef struct {
   const uint8_t *ind_ignore;   /* [nind] population "Ignore", may be NULL */
   const uint8_t *ind_affstatus;/* [nind] 1 = in a poplistname population (NULL = all) */
   const uint8_t *ind_male;     /* [nind] 1 = gender M (male-X-het rule), may be NULL */
+  const int32_t *ind_pop;      /* [nind] index of the sample's population in the population
+                                  list (poplistname order, else first appearance), -1 when
+                                  not listed; read only with usepopsformissing */
 } gp_panel;
 
 enum {

@@ -53,6 +53,17 @@ def lib():
         L.orc_lsqproj.argtypes = [u8p, C.c_int64, i32p, C.c_int32, u8p, f64p, f64p, f64p, f64p,
                                   C.c_int32, i32p, C.c_int32, f64p, f64p, i32p, i32p]
         L.orc_lsqproj.restype = None
+        L.orc_popfill_columns.argtypes = [u8p, C.c_int64, i32p, C.c_int32, i32p, C.c_int32, i32p,
+                                          C.c_int32, C.c_int, C.c_int, C.c_int, C.c_int, i32p,
+                                          i32p, i32p, u8p, f64p, f64p, f64p, f64p]
+        L.orc_popfill_columns.restype = None
+        L.orc_gram_fill.argtypes = [u8p, C.c_int64, i32p, C.c_int32, u8p, f64p, f64p, C.c_int32,
+                                    i32p, i32p, C.c_int32, f64p]
+        L.orc_gram_fill.restype = None
+        L.orc_lsqproj_fill.argtypes = [u8p, C.c_int64, i32p, C.c_int32, u8p, f64p, f64p, f64p,
+                                       f64p, C.c_int32, i32p, i32p, C.c_int32, C.c_int32, f64p,
+                                       f64p, i32p, i32p]
+        L.orc_lsqproj_fill.restype = None
         _lib = L
     return _lib
 
@@ -115,9 +126,38 @@ def pass_columns(records, cols, xindex, fancynorm=1, altnormstyle=1, minallelecn
     return s
 
 
+def popfill_columns(s, rowpop, npop, fancynorm=1, altnormstyle=1, minallelecnt=1,
+                    maxmissing=9999999):
+    """usepopsformissing on a pass: replaces s's counts, kill flags, xmean and xfancy by
+    the filled ones and adds the Gram table s.gtab [4 per column] and the population fill
+    values s.gfill [ncols x npop]; s.tab stays the observed-only table the SNP weights use
+    (getcolxf)."""
+    nc, n = len(s.cols), len(s.xindex)
+    s.rowpop = np.ascontiguousarray(rowpop, dtype=np.int32)
+    s.npop = int(npop)
+    s.gtab = np.zeros(4 * nc)
+    s.gfill = np.zeros(nc * max(npop, 1))
+    lib().orc_popfill_columns(_p(s.rec, C.c_uint8), s.rec.shape[1], _p(s.cols, C.c_int32), nc,
+                              _p(s.xindex, C.c_int32), n, _p(s.rowpop, C.c_int32), npop,
+                              fancynorm, altnormstyle, minallelecnt, maxmissing,
+                              _p(s.n0, C.c_int32), _p(s.n1, C.c_int32), _p(s.nmiss, C.c_int32),
+                              _p(s.killed, C.c_uint8), _p(s.gtab, C.c_double),
+                              _p(s.gfill, C.c_double), _p(s.xmean, C.c_double),
+                              _p(s.xfancy, C.c_double))
+    dead = s.killed == 1
+    s.tab.reshape(-1, 4)[dead] = 0.0
+    return s
+
+
 def gram(s, lookup=False, nthreads=1):
     n = len(s.xindex)
     X = np.zeros((n, n))
+    if getattr(s, "gfill", None) is not None:
+        lib().orc_gram_fill(_p(s.rec, C.c_uint8), s.rec.shape[1], _p(s.cols, C.c_int32),
+                            len(s.cols), _p(s.killed, C.c_uint8), _p(s.gtab, C.c_double),
+                            _p(s.gfill, C.c_double), s.npop, _p(s.rowpop, C.c_int32),
+                            _p(s.xindex, C.c_int32), n, _p(X, C.c_double))
+        return X
     args = (_p(s.rec, C.c_uint8), s.rec.shape[1], _p(s.cols, C.c_int32), len(s.cols),
             _p(s.killed, C.c_uint8), _p(s.tab, C.c_double), _p(s.xindex, C.c_int32), n)
     if lookup:
@@ -178,10 +218,29 @@ def lsqproj(s, ffvecs, fxscal, K, samples):
     return a, b, nobs, st
 
 
+def lsqproj_fill(s, ffvecs, fxscal, K, samples, sampop, npop):
+    smp = np.ascontiguousarray(samples, dtype=np.int32)
+    sp = np.ascontiguousarray(sampop, dtype=np.int32)
+    q = len(smp)
+    ff = np.ascontiguousarray(ffvecs[:K])
+    a = np.zeros((K, q))
+    b = np.zeros((K, q))
+    nobs = np.zeros(q, np.int32)
+    st = np.zeros(q, np.int32)
+    lib().orc_lsqproj_fill(_p(s.rec, C.c_uint8), s.rec.shape[1], _p(s.cols, C.c_int32),
+                           len(s.cols), _p(s.killed, C.c_uint8), _p(s.xmean, C.c_double),
+                           _p(s.xfancy, C.c_double), _p(ff, C.c_double),
+                           _p(np.ascontiguousarray(fxscal), C.c_double), K, _p(smp, C.c_int32),
+                           _p(sp, C.c_int32), q, npop, _p(a, C.c_double), _p(b, C.c_double),
+                           _p(nobs, C.c_int32), _p(st, C.c_int32))
+    return a, b, nobs, st
+
+
 def smartpca(records, nind, numeigs=10, numoutliter=5, numoutleigs=10, outlthresh=6.0,
              outliermode=0, fancynorm=1, altnormstyle=1, minallelecnt=1, maxmissing=9999999,
              lsqproject=1, snp_chrom=None, noxdata=1, numchrom=22, ind_ignore=None,
-             ind_affstatus=None, gram_lookup=False, nthreads=1, missingmode=0):
+             ind_affstatus=None, gram_lookup=False, nthreads=1, missingmode=0,
+             usepopsformissing=0, ind_pop=None):
     """The hot path of smartpca main() on packed records (sorted SNP order).
 
     Returns evals (all, descending), evecs (top K over the rows), xindex, the per-sample
@@ -219,13 +278,28 @@ def smartpca(records, nind, numeigs=10, numoutliter=5, numoutleigs=10, outlthres
 
     xindex = rows()
     cols = columns()
+    # xtypes (smartpca.c:928-943, :1095-1099, :1505-1508): the population index of row i,
+    # written for the current rows of every pass and never cleared (-2 before the first)
+    xtypes = np.full(nind, -2, np.int32)
+    npop = 0
+    if usepopsformissing:
+        ind_pop = np.asarray(ind_pop, np.int32)
+        npop = int(ind_pop.max()) + 1 if len(ind_pop) else 0
     numoutiter = numoutliter + 1 if numoutliter >= 1 else 1
     mode = outliermode if numoutliter >= 1 else 2
     outliers = []
     for it in range(1, numoutiter + 1):
         if it > 1:
             cols = columns()
-        s = pass_columns(rec, cols, xindex, fancynorm, altnormstyle, minallelecnt, maxmissing)
+        if usepopsformissing:
+            xtypes[:len(xindex)] = ind_pop[xindex]
+            s = pass_columns(rec, cols, xindex, fancynorm, altnormstyle, minallelecnt,
+                             0x7FFFFFFF)
+            popfill_columns(s, xtypes[:len(xindex)], npop, fancynorm, altnormstyle,
+                            minallelecnt, maxmissing)
+        else:
+            s = pass_columns(rec, cols, xindex, fancynorm, altnormstyle, minallelecnt,
+                             maxmissing)
         snp_ign[cols[s.killed == 1]] = 2
         X = gram(s, lookup=gram_lookup, nthreads=nthreads)
         evals, evecs = eig_scaled(X)
@@ -247,7 +321,11 @@ def smartpca(records, nind, numeigs=10, numoutliter=5, numoutleigs=10, outlthres
         ff, fx, fxscal = weights(s, evecs, K)
         if lsqproject:
             proj = np.nonzero(~ind_ign)[0].astype(np.int32)
-            a, b, nobs, st = lsqproj(s, ff, fxscal, K, proj)
+            if usepopsformissing:
+                # lsqproj reads xtypes at the sample's index in the .ind file (idnum)
+                a, b, nobs, st = lsqproj_fill(s, ff, fxscal, K, proj, xtypes[proj], npop)
+            else:
+                a, b, nobs, st = lsqproj(s, ff, fxscal, K, proj)
             prev = np.zeros(K)
             for q, k in enumerate(proj):
                 if st[q] == 1:

@@ -436,3 +436,206 @@ void orc_lsqproj(const uint8_t *records, int64_t rlen, const int32_t *cols, int3
     status[q] = 0;
   }
 }
+
+/* ---- usepopsformissing ------------------------------------------------------------------ */
+
+/*
+ * getcolxz with usepopsformissing (src/eigensrc/smartpca.c:3129-3216) and fvadjust
+ * (:2236-2279), per column over the rows in order: a missing genotype of a row whose
+ * population (rowpop, the xtypes index; < 0 = none) has observed genotypes in this column
+ * becomes that population's mean genotype; the mean and the fancy scale then run over the
+ * observed and filled values in row order.  Outputs (per column): n0, n1 (observed counts),
+ * nmiss (still missing after the fill), killed (the rule of :1131-1144 on those counts),
+ * gtab [4*c] (k - mean)*fancy, gfill [c*npop + k] (fill_k - mean)*fancy (0 where population
+ * k has no observed genotype), xmean = mean*fancy, xfancy = fancy.  A column with no
+ * observed genotype: n0 = n1 = -1, nmiss = nrows, killed, xmean = xfancy = 0.
+ */
+void orc_popfill_columns(const uint8_t *records, int64_t rlen, const int32_t *cols,
+                         int32_t ncols, const int32_t *xindex, int32_t nrows,
+                         const int32_t *rowpop, int32_t npop, int fancynorm, int altnormstyle,
+                         int minallelecnt, int maxmissing, int32_t *n0, int32_t *n1,
+                         int32_t *nmiss, uint8_t *killed, double *gtab, double *gfill,
+                         double *xmean, double *xfancy)
+{
+  double *psum = (double *)malloc(sizeof(double) * (size_t)(npop + 1));
+  double *pnum = (double *)malloc(sizeof(double) * (size_t)(npop + 1));
+  double *x = (double *)malloc(sizeof(double) * (size_t)(nrows + 1));
+  for (int32_t c = 0; c < ncols; ++c) {
+    const uint8_t *rec = records + (int64_t)cols[c] * rlen;
+    double *tab = gtab + 4 * (int64_t)c, *fill = gfill + (int64_t)c * npop;
+    memset(psum, 0, sizeof(double) * (size_t)npop);
+    memset(pnum, 0, sizeof(double) * (size_t)npop);
+    int c0 = 0, c1 = 0, miss = 0;
+    for (int32_t j = 0; j < nrows; ++j) {
+      const int g = orc_geno(rec, xindex[j]);
+      x[j] = (double)g;
+      if (g < 0) {
+        ++miss;
+        continue;
+      }
+      c0 += g;
+      c1 += 2 - g;
+      const int k = rowpop[j];
+      if (k >= 0) {
+        psum[k] += (double)g;
+        pnum[k] += 1.0;
+      }
+    }
+    if (miss > 0) {
+      miss = 0;
+      for (int32_t j = 0; j < nrows; ++j) {
+        if (x[j] >= 0.0) continue;
+        const int k = rowpop[j];
+        if (k >= 0 && pnum[k] > 0.5) x[j] = psum[k] / pnum[k];
+        else ++miss;
+      }
+    }
+    double ysum = 0.0, ynum = 0.0;
+    for (int32_t j = 0; j < nrows; ++j)
+      if (x[j] >= 0.0) {
+        ysum += x[j];
+        ynum += 1.0;
+      }
+    for (int k = 0; k < npop; ++k) fill[k] = 0.0;
+    tab[0] = tab[1] = tab[2] = tab[3] = 0.0;
+    if (ynum == 0.0) {
+      n0[c] = n1[c] = -1;
+      nmiss[c] = nrows;
+      killed[c] = 1;
+      xmean[c] = xfancy[c] = 0.0;
+      continue;
+    }
+    const double ymean = ysum / ynum;
+    double yfancy = 1.0;
+    if (fancynorm) {
+      double p = 0.5 * ymean;
+      if (altnormstyle == 0) p = (ysum + 1.0) / (2.0 * ynum + 2.0);
+      const double y = p * (1.0 - p);
+      if (y > 0.0) yfancy = 1.0 / sqrt(y);
+    }
+    n0[c] = c0;
+    n1[c] = c1;
+    nmiss[c] = miss;
+    xmean[c] = ymean * yfancy;
+    xfancy[c] = yfancy;
+    const int t = c0 < c1 ? c0 : c1;
+    killed[c] = (t < minallelecnt) || (miss > maxmissing) || (t == 0);
+    if (killed[c]) continue;
+    for (int g = 0; g < 3; ++g) tab[g] = ((double)g - ymean) * yfancy;
+    for (int k = 0; k < npop; ++k)
+      if (pnum[k] > 0.5) fill[k] = (psum[k] / pnum[k] - ymean) * yfancy;
+  }
+  free(psum);
+  free(pnum);
+  free(x);
+}
+
+/* XTX with the usepopsformissing values: the table for observed genotypes, the row's
+ * population fill (0 without one) for missing ones (smartpca.c:1116-1189 through getcolxz
+ * and domult_increment_normal :3498-3561); plain loops, lower triangle then mirrored. */
+void orc_gram_fill(const uint8_t *records, int64_t rlen, const int32_t *cols, int32_t ncols,
+                   const uint8_t *killed, const double *gtab, const double *gfill, int32_t npop,
+                   const int32_t *rowpop, const int32_t *xindex, int32_t n, double *XTX)
+{
+  double *v = (double *)malloc(sizeof(double) * (size_t)n);
+  memset(XTX, 0, sizeof(double) * (size_t)n * n);
+  for (int32_t c = 0; c < ncols; ++c) {
+    if (killed[c]) continue;
+    const uint8_t *rec = records + (int64_t)cols[c] * rlen;
+    for (int32_t i = 0; i < n; ++i) {
+      const int g = orc_geno(rec, xindex[i]);
+      v[i] = g >= 0 ? gtab[4 * (int64_t)c + g]
+                    : (rowpop[i] >= 0 ? gfill[(int64_t)c * npop + rowpop[i]] : 0.0);
+    }
+    for (int32_t i = 0; i < n; ++i) {
+      const double vi = v[i];
+      if (vi == 0.0) continue;
+      double *row = XTX + (int64_t)i * n;
+      for (int32_t j = 0; j <= i; ++j) row[j] += vi * v[j];
+    }
+  }
+  for (int32_t i = 0; i < n; ++i)
+    for (int32_t j = i + 1; j < n; ++j) XTX[(int64_t)i * n + j] = XTX[(int64_t)j * n + i];
+  free(v);
+}
+
+/*
+ * lsqproj with usepopsformissing (src/eigensrc/smartpca.c:4606-4757).  sampop[q] is the
+ * population index the reference reads for sample q (xtypes[idnum]; < 0 = none).  A sample
+ * with at most K observed genotypes over the kept columns is "ignored (insufficient data"
+ * (status 1, the first-call coverage check :4631-4647) and adds nothing to the population
+ * sums; the others with sampop >= 0 sum their observed genotypes per population and column
+ * (xnum, xden :4658-4677).  Each sample's missing genotypes are then filled with its
+ * population's mean where xden > 0.1 and count as observed in the regression (:4679-4716)
+ * and in bcoeffs (:4719-4746); fixxrow values (x fancy - xmean).
+ */
+void orc_lsqproj_fill(const uint8_t *records, int64_t rlen, const int32_t *cols, int32_t ncols,
+                      const uint8_t *killed, const double *xmean, const double *xfancy,
+                      const double *ffvecs, const double *fxscal, int32_t K,
+                      const int32_t *samples, const int32_t *sampop, int32_t nproj,
+                      int32_t npop, double *acoeffs, double *bcoeffs, int32_t *nobs,
+                      int32_t *status)
+{
+  double co[64 * 64], rr[64], ans[64], e[64], bsum[64];
+  double *xnum = (double *)calloc((size_t)npop * ncols + 1, sizeof(double));
+  double *xden = (double *)calloc((size_t)npop * ncols + 1, sizeof(double));
+  int32_t *raw = (int32_t *)calloc((size_t)nproj + 1, sizeof(int32_t));
+  for (int32_t q = 0; q < nproj; ++q)
+    for (int32_t c = 0; c < ncols; ++c)
+      if (!killed[c] && orc_geno(records + (int64_t)cols[c] * rlen, samples[q]) >= 0) ++raw[q];
+  for (int32_t q = 0; q < nproj; ++q) {
+    const int t = sampop[q];
+    if (raw[q] <= K || t < 0) continue;
+    for (int32_t c = 0; c < ncols; ++c) {
+      const int g = orc_geno(records + (int64_t)cols[c] * rlen, samples[q]);
+      if (g < 0) continue;
+      xnum[(int64_t)t * ncols + c] += (double)g;
+      xden[(int64_t)t * ncols + c] += 1.0;
+    }
+  }
+  for (int32_t q = 0; q < nproj; ++q) {
+    const int t = sampop[q];
+    memset(co, 0, sizeof(double) * (size_t)K * K);
+    memset(rr, 0, sizeof(double) * (size_t)K);
+    memset(bsum, 0, sizeof bsum);
+    if (raw[q] <= K) {
+      nobs[q] = raw[q];
+      status[q] = 1;
+      for (int j = 0; j < K; ++j) bcoeffs[(int64_t)j * nproj + q] = 0.0;
+      continue;
+    }
+    int32_t kk = 0;
+    for (int32_t c = 0; c < ncols; ++c) {
+      if (killed[c]) continue;
+      const int g = orc_geno(records + (int64_t)cols[c] * rlen, samples[q]);
+      double xr = (double)g;
+      if (g < 0) {
+        const int64_t u = (int64_t)t * ncols + c;
+        if (t < 0 || !(xden[u] > 0.1)) continue;
+        xr = xnum[u] / xden[u];
+      }
+      double x = xr * xfancy[c];
+      x = (x < -0.001) ? 0.0 : x - xmean[c];
+      for (int j = 0; j < K; ++j) {
+        e[j] = fxscal[j] * ffvecs[(int64_t)j * ncols + c];
+        bsum[j] += x * ffvecs[(int64_t)j * ncols + c];
+      }
+      for (int j = 0; j < K; ++j) {
+        rr[j] += e[j] * x;
+        for (int k = j; k < K; ++k) co[j * K + k] = co[k * K + j] += e[j] * e[k];
+      }
+      ++kk;
+    }
+    nobs[q] = kk;
+    for (int j = 0; j < K; ++j) bcoeffs[(int64_t)j * nproj + q] = fxscal[j] * bsum[j];
+    if (orc_cholsolve(co, K, rr, ans) < 0) {
+      status[q] = 2;
+      continue;
+    }
+    for (int j = 0; j < K; ++j) acoeffs[(int64_t)j * nproj + q] = ans[j];
+    status[q] = 0;
+  }
+  free(xnum);
+  free(xden);
+  free(raw);
+}

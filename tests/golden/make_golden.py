@@ -85,6 +85,19 @@ CASES = {
     "bn_missingmode": dict(nsnp=3000, pops=[70, 70, 60], fst=[0.01, 0.02, 0.03], miss=0.0,
                            miss_hi=0.4, seed=18, fmt="packed",
                            par={"numoutevec": "4", "missingmode": "YES"}),
+    # usepopsformissing: missing genotypes take their population's mean in the Gram and in
+    # lsqproj; per-sample missing rates ~U(0, 0.5), two planted 2-sample populations removed
+    # as outliers, maxmissing 1 applied to the count still missing after the fill (a SNP
+    # where a whole population is missing)
+    "bn_usepops": dict(nsnp=3000, pops=[60, 60, 50, 2, 2], fst=[0.01, 0.02, 0.03, 0.25, 0.25],
+                       miss=0.0, miss_hi=0.5, seed=19, fmt="packed",
+                       par={"numoutevec": "4", "usepopsformissing": "YES", "maxmissing": "1"}),
+    # the same option with a poplist (POP1, POP2): the other samples are projected, and
+    # lsqproj reads each sample's population at its .ind index among the row-indexed xtypes
+    "bn_usepops_pl": dict(nsnp=3000, pops=[60, 60, 50, 2, 2], fst=[0.01, 0.02, 0.03, 0.25, 0.25],
+                          miss=0.0, miss_hi=0.5, n_admixed=10, seed=20, fmt="packed",
+                          par={"numoutevec": "4", "usepopsformissing": "YES",
+                               "poplistname": "poplist"}, poplist=["POP1", "POP2"]),
 }
 
 # fastmode (kjg_fpca) through the reference built with oracle/gsl_shim: default L = 2K, I = K

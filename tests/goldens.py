@@ -4,7 +4,8 @@ import os
 import numpy as np
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = ["bn_outliers", "bn_bed_altnorm", "bn_project", "bn_grm", "bn_missingmode"]
+CASES = ["bn_outliers", "bn_bed_altnorm", "bn_project", "bn_grm", "bn_missingmode",
+         "bn_usepops", "bn_usepops_pl"]
 REL_CASES = ["bn_rel"]
 
 
@@ -51,8 +52,19 @@ class Case:
             self.records = np.frombuffer(raw, np.uint8).reshape(self.nsnp, rlen).copy()
         self.affstatus = None
         if "poplistname" in p:
-            keep = {l.strip() for l in open(os.path.join(d, p["poplistname"])) if l.strip()}
+            names = [l.split()[0] for l in open(os.path.join(d, p["poplistname"])) if l.strip()]
+            keep = set(names)
             self.affstatus = np.array([pp in keep for pp in self.pops], np.uint8)
+            eglist = names
+        else:
+            # makeeglist: populations in order of first appearance, "Ignore" left out
+            eglist = []
+            for pp in self.pops:
+                if pp != "Ignore" and pp not in eglist:
+                    eglist.append(pp)
+        # the sample's index in the population list (xtypes), -1 when not listed
+        self.ind_pop = np.array([eglist.index(pp) if pp in eglist else -1 for pp in self.pops],
+                                np.int32)
         if os.path.exists(os.path.join(d, "ref.eval")):
             self.ref_evals = np.loadtxt(os.path.join(d, "ref.eval"))
             lines = open(os.path.join(d, "ref.evec")).read().splitlines()
@@ -85,6 +97,8 @@ class Case:
             kw["maxmissing"] = int(p["maxmissing"])
         if "missingmode" in p:
             kw["missingmode"] = yesno(p["missingmode"])
+        if "usepopsformissing" in p:
+            kw["usepopsformissing"] = yesno(p["usepopsformissing"])
         return kw
 
     def rel_opts(self):

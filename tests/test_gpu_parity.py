@@ -156,7 +156,7 @@ def test_smartpca_run_matches_reference(gpu, case):
     c = Case(case)
     opts = native.default_opts(**c.opts())
     r = native.smartpca_run(gpu, c.records, c.nind, opts, code=c.code,
-                            ind_affstatus=c.affstatus)
+                            ind_affstatus=c.affstatus, ind_pop=c.ind_pop)
     assert r["nrows"] == len(c.ref_evals)
     scale = abs(c.ref_evals[0])
     assert np.max(np.abs(r["evals"] - c.ref_evals)) <= 1e-10 * scale
@@ -347,6 +347,12 @@ def test_smartpca_run_split_fp16_vs_reference(gpu, case):
     the top two coordinates (population structure) within 1e-4."""
     c = Case(case)
     opts = native.default_opts(precision=native.GP_PREC_SPLIT_FP16, **c.opts())
+    if opts.usepopsformissing:
+        # the population fill runs in the FP64 drop-in precision only, and says so
+        with pytest.raises(native.GpuError, match="FP64 precision only"):
+            native.smartpca_run(gpu, c.records, c.nind, opts, code=c.code,
+                                ind_affstatus=c.affstatus, ind_pop=c.ind_pop)
+        return
     r = native.smartpca_run(gpu, c.records, c.nind, opts, code=c.code,
                             ind_affstatus=c.affstatus)
     assert r["nrows"] == len(c.ref_evals)

@@ -45,7 +45,8 @@ def test_eigenstrat_example_eval():
 def test_oracle_matches_reference(case):
     c = Case(case)
     kw = c.opts()
-    r = O.smartpca(c.packed_records(), c.nind, ind_affstatus=c.affstatus, **kw)
+    r = O.smartpca(c.packed_records(), c.nind, ind_affstatus=c.affstatus, ind_pop=c.ind_pop,
+                   **kw)
     n = r["nrows"]
     assert len(c.ref_evals) == n
     scale = max(abs(c.ref_evals[0]), 1.0)

@@ -236,7 +236,11 @@ def run_serving(h, cfg, nreq=400, seed=11, n64=100):
                                        miss_hi=0.95, n_admixed=npool - per * npops,
                                        seed=cfg["seed"])
     gen_s = time.time() - t
+    # pinning host memory synchronises the device: done with the device-resident loop
+    # stopped (a paused server stops it)
+    srv.pause(True)
     native.host_register(rows)
+    srv.pause(False)
     rng = np.random.default_rng(seed)
 
     def draw(n):
@@ -274,7 +278,17 @@ def run_serving(h, cfg, nreq=400, seed=11, n64=100):
     # the tensor-core server's coordinates for the same requests
     sz_c, off_c = draw(n64)
     _, _, creqs = _serve_load(srv, rows, sz_c, off_c, np.zeros(n64))
+    on, launches, lbatches, idle = srv.loop_stats()
+    out["device_loop"] = {"running": bool(on), "graph_launches": launches, "batches": lbatches,
+                          "idle_polls": idle}
     srv.close()
+    # the same capacity run with the host-launched schedule (one set of launches per batch)
+    sh = native.Server(h, K, max_batch=4096, pool_samples=32768, host_loop=True)
+    sz_h, off_h = draw(nreq)
+    _, span_h, _ = _serve_load(sh, rows, sz_h, off_h, np.zeros(nreq))
+    sh.close()
+    out["capacity_host_loop"] = {"samples_per_s": float(sz_h.sum()) / span_h,
+                                 "req_per_s": nreq / span_h, "n": nreq}
     s64 = native.Server(h, K, max_batch=2048, pool_samples=4096, fp64_serial=True)
     lat64, span64, r64 = _serve_load(s64, rows, sz_c, off_c, np.zeros(n64))
     s64.close()
@@ -348,7 +362,9 @@ def run_mixed(args, cfg, local):
                                        srv.row_bytes, sample_seed=cfg["seed"] + 1000, miss=0.0,
                                        miss_hi=0.95, n_admixed=npool - per * npops,
                                        seed=cfg["seed"])
+    srv.pause(True)  # pinning host memory synchronises the device: loop stopped
     native.host_register(rows)
+    srv.pause(False)
     # warm-up: every dataset once through the server, a few projections
     for jb in jobs:
         srv.submit_pca(jb["rec"], jb["n"], jopts).wait(600.0)

@@ -889,8 +889,9 @@ k_build_EP(const double *ffvecs, const double *fxscal, const int32_t *kept, int3
  */
 __global__ void k_lsq_solve(const double *co, int32_t ldco, const double *rr, int32_t K,
                             int32_t nproj, double *acoef, double *bcoef, int32_t *nobs,
-                            int32_t *status, double *work)
+                            int32_t *status, double *work, const int32_t *d_nproj)
 {
+  if (d_nproj) nproj = *d_nproj; /* a device-resident loop's batch size */
   for (int32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nproj;
        q += gridDim.x * blockDim.x) {
     double *a = work + (int64_t)q * (K * K + 2 * K);
@@ -1051,7 +1052,7 @@ static int lsqproj_impl(gp_ctx *ctx, int32_t numeigs, const int32_t *samples,
   GP_CUDA(ctx, cudaMemsetAsync(d_a, 0, sizeof(double) * nrr, ctx->stream));
   int blocks = (nproj + 127) / 128;
   k_lsq_solve<<<blocks, 128, 0, ctx->stream>>>(d_co, ldp, d_rr, K, nproj, d_a, d_b, d_nobs, d_st,
-                                               d_work);
+                                               d_work, NULL);
   GP_LAUNCH_CHECK(ctx, "k_lsq_solve");
   std::vector<int32_t> st((size_t)nproj);
   std::vector<double> ha(nrr);

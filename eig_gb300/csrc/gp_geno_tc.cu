@@ -85,8 +85,18 @@ k_geno_panel_tc(const __grid_constant__ CUtensorMap tm_b, const uint8_t *__restr
                 int64_t ldc, const int32_t *__restrict__ row_map, int32_t nrows, int32_t ncols4,
                 int32_t nkb, int32_t kb_period,
                 int32_t kb_switch, uint64_t lut_lo, uint64_t lut_hi, int32_t ksplit,
-                double *zout, int64_t ldz, int *err)
+                double *zout, int64_t ldz, int *err, const gp_tc_batch *db)
 {
+  if (db) {
+    /* a device-resident loop's batch: rows and their count are read at run time, and the
+     * k split is chosen as gp_tc_apply chooses it for that count */
+    codes = db->codes;
+    nrows = db->nrows;
+    const int32_t tiles = ((nrows + XT - 1) / XT) * ((ncols4 + XT - 1) / XT);
+    ksplit = 1;
+    while (tiles * ksplit < 2 * (int32_t)gridDim.x && ksplit * 4 <= nkb) ksplit *= 2;
+    while ((int64_t)((nkb + ksplit - 1) / ksplit) * XK > (1 << 19)) ksplit *= 2;
+  }
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t *bars = (uint64_t *)(smem + XSTAGES * XSTAGE_BYTES);
@@ -557,8 +567,10 @@ k_panel_slices(const double *__restrict__ P, int64_t ldp, int32_t nk, int32_t nc
 
 /* Y[r][c] = 2^e_c sum_t Z[r][4c+t] 1024^-(t+1) */
 __global__ void k_panel_combine(const double *Z, int64_t ldz, int32_t nrows, int32_t ncols,
-                                const int32_t *expo, double *Y, int64_t ldy)
+                                const int32_t *expo, double *Y, int64_t ldy,
+                                const gp_tc_batch *db)
 {
+  if (db) nrows = db->nrows;
   int64_t total = (int64_t)nrows * ncols;
   for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
        idx += (int64_t)gridDim.x * blockDim.x) {
@@ -738,12 +750,12 @@ int gp_tc_apply(gp_ctx *ctx, const gp_tc_codes *A, const gp_tc_prepared *P, doub
   k_geno_panel_tc<<<grid, X_THREADS, X_SMEM, ctx->stream>>>(P->tmb, A->codes, A->ldc, A->row_map,
                                                            nrows, P->ncols4, nkb, P->kb0, P->kb0,
                                                            P->lut_lo, P->lut_hi, ksplit, Z, ldz,
-                                                           d_err);
+                                                           d_err, NULL);
   GP_LAUNCH_CHECK(ctx, "k_geno_panel_tc");
   {
     int64_t work = (int64_t)nrows * P->ncols;
     k_panel_combine<<<grid_cap(ctx, work, 256, 32), 256, 0, ctx->stream>>>(Z, ldz, nrows, P->ncols,
-                                                                            P->expo, d_Y, ldy);
+                                                                            P->expo, d_Y, ldy, NULL);
     GP_LAUNCH_CHECK(ctx, "k_panel_combine");
   }
   if (!sync) return GP_OK;
@@ -751,6 +763,39 @@ int gp_tc_apply(gp_ctx *ctx, const gp_tc_codes *A, const gp_tc_prepared *P, doub
   GP_CUDA(ctx, gp_memcpy(ctx, &herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   if (herr) return gp_fail(ctx, GP_ERR_TIMEOUT, "tensor-core product wait timed out (code %d)", herr);
+  return GP_OK;
+}
+
+/* Z[r][c] = 0 for the batch's rows */
+__global__ void k_zero_batch_rows(double *Z, int64_t ldz, const gp_tc_batch *db)
+{
+  const int64_t total = (int64_t)db->nrows * ldz;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x)
+    Z[i] = 0.0;
+}
+
+int gp_tc_apply_dev(gp_ctx *ctx, const gp_tc_batch *db, int32_t max_rows, int64_t ldc,
+                    const gp_tc_prepared *P, double *Z, double *d_Y, int64_t ldy)
+{
+  if (max_rows < 1) return GP_OK;
+  if (ldc < (int64_t)P->kb0 * XK / 4)
+    return gp_fail(ctx, GP_ERR_ARG, "gp_tc_apply_dev: code rows shorter than the panel");
+  const int64_t ldz = P->ncols4_pad;
+  k_zero_batch_rows<<<grid_cap(ctx, (int64_t)max_rows * ldz, 256, 8), 256, 0, ctx->stream>>>(
+      Z, ldz, db);
+  GP_LAUNCH_CHECK(ctx, "k_zero_batch_rows");
+  GP_CUDA(ctx, cudaFuncSetAttribute(k_geno_panel_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    X_SMEM));
+  const int32_t nkb = P->kb0 * P->npanels;
+  /* every SM: the kernel takes the batch's row count, and with it its work items, from db */
+  k_geno_panel_tc<<<ctx->num_sms, X_THREADS, X_SMEM, ctx->stream>>>(
+      P->tmb, NULL, ldc, NULL, 0, P->ncols4, nkb, P->kb0, P->kb0, P->lut_lo, P->lut_hi, 1, Z, ldz,
+      ctx->d_err, db);
+  GP_LAUNCH_CHECK(ctx, "k_geno_panel_tc");
+  k_panel_combine<<<grid_cap(ctx, (int64_t)max_rows * P->ncols, 256, 32), 256, 0, ctx->stream>>>(
+      Z, ldz, 0, P->ncols, P->expo, d_Y, ldy, db);
+  GP_LAUNCH_CHECK(ctx, "k_panel_combine");
   return GP_OK;
 }
 

@@ -48,6 +48,22 @@ int gp_tc_prepare(gp_ctx *ctx, int npanels, const gp_tc_panel *pp, int32_t ncols
 int gp_tc_apply(gp_ctx *ctx, const gp_tc_codes *A, const gp_tc_prepared *P, double *d_Y,
                 int64_t ldy, int sync);
 
+/* The batch a device-resident loop works on: nrows code rows at codes (ring position row0
+ * of the pool), requests [req_begin, req_end) of the loop's queue.  Written on the device
+ * by the loop's batch former and read by the kernels at run time, so that one captured
+ * launch serves every batch. */
+struct gp_tc_batch {
+  const uint8_t *codes;
+  int32_t nrows;
+  int32_t pad;
+  int64_t row0, req_begin, req_end;
+};
+/* gp_tc_apply inside a loop body: the rows come from db at run time (at most max_rows, row
+ * stride ldc); Z holds max_rows * P->ncols4_pad doubles of the caller's; errors of the
+ * bounded waits go to ctx->d_err */
+int gp_tc_apply_dev(gp_ctx *ctx, const gp_tc_batch *db, int32_t max_rows, int64_t ldc,
+                    const gp_tc_prepared *P, double *Z, double *d_Y, int64_t ldy);
+
 /* the code operand of gp_geno_panel_tc (built into scratch4, or the resident records when a
  * SNP-major operand covers every sample in order) */
 int gp_tc_codes_for(gp_ctx *ctx, int sum_over_snps, const int32_t *d_samp, int32_t nsamp,

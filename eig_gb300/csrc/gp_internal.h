@@ -151,10 +151,11 @@ int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, d
 int gp_eig_sym(gp_ctx *ctx, double *A, int32_t n, int32_t nvec, double *d_evals_desc,
                double *d_vecs);
 /* per-sample masked normal equations solve of lsqproj (gp_api.cu); co rows hold the K(K+1)/2
- * pair sums then the observed count, rr rows the K right-hand sides; acoef/bcoef are [K][nproj] */
+ * pair sums then the observed count, rr rows the K right-hand sides; acoef/bcoef are [K][nproj];
+ * d_nproj (device, may be NULL) replaces nproj at run time */
 __global__ void k_lsq_solve(const double *co, int32_t ldco, const double *rr, int32_t K,
                             int32_t nproj, double *acoef, double *bcoef, int32_t *nobs,
-                            int32_t *status, double *work);
+                            int32_t *status, double *work, const int32_t *d_nproj);
 int gp_launch_materialize_f64(gp_ctx *ctx, int32_t k0, int32_t kc, int32_t pitch, double *d_x,
                               double scale);
 

@@ -37,9 +37,27 @@ struct gp_req {
   int64_t row_start;  /* ring position of the first row */
   int64_t skip;       /* ring rows skipped before it (wrap) */
   cudaEvent_t copied;
+  int64_t seq;        /* position in the device loop's queue */
   int done;
   int error;
 };
+
+/* The device-resident loop's queue, in mapped pinned host memory.  The host writes request
+ * descriptors, then n_pub (release); the loop writes each request's error word, then n_done
+ * (release), and its counters. */
+#define SRV_QCAP 8192
+struct gp_srv_queue {
+  int64_t n_pub;
+  int64_t n_done;
+  int64_t batches;
+  int64_t idle_polls;
+  int32_t stop;
+  int32_t err;
+  int64_t req_row[SRV_QCAP];
+  int32_t req_n[SRV_QCAP];
+  int32_t req_err[SRV_QCAP];
+};
+#define SRV_POLL_NS 1000000ull /* one poll of the loop waits at most 1 ms for a request */
 /* tickets are released by the gp_serve_test / gp_serve_wait call that sees them complete */
 
 struct gp_batch {
@@ -92,6 +110,18 @@ struct gp_server {
   pthread_t thread;
   int stop, thread_started, paused;
   int64_t n_batches, n_samples, n_requests;
+  /* the device-resident loop */
+  int host_loop;
+  gp_srv_queue *hq, *dq;      /* host and device views of the queue */
+  double *h_res, *d_res;      /* [pool_cap*K] coordinates at the request rows (mapped) */
+  int32_t *h_rst, *d_rst;     /* [pool_cap] statuses (mapped) */
+  gp_tc_batch *d_batch;
+  double *d_Z, *d_escale;
+  cudaGraph_t graph;
+  cudaGraphExec_t gexec;
+  int loop_running;
+  int64_t loop_launches, n_pub, n_done_seen;
+  std::deque<gp_req *> published;
   char err[GP_ERRLEN];
 };
 
@@ -207,6 +237,99 @@ __global__ void k_serve_panel(const double *ffvecs, const double *fxscal, const 
   }
 }
 
+/* ---- the device-resident loop's kernels -------------------------------------------- */
+
+__device__ __forceinline__ uint64_t srv_globaltimer()
+{
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ int64_t ld_acquire_sys(const int64_t *p)
+{
+  int64_t v;
+  asm volatile("ld.acquire.sys.global.s64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void st_release_sys(int64_t *p, int64_t v)
+{
+  asm volatile("st.release.sys.global.s64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+/*
+ * The loop's batch former (one thread): waits, at most poll_ns, for requests published
+ * beyond those taken, then packs the published requests whose rows follow one another in
+ * the pool, up to max_batch rows, into the next batch.  Sets the loop's condition: 0 when the
+ * host asked it to stop and nothing is left, else 1 (an empty batch when the poll ran out).
+ */
+__global__ void k_srv_take(gp_srv_queue *q, gp_tc_batch *db, const uint8_t *pool,
+                           int64_t row_bytes, int32_t max_batch, cudaGraphConditionalHandle h,
+                           uint64_t poll_ns)
+{
+  if (threadIdx.x != 0) return;
+  const int64_t taken = db->req_end;
+  const uint64_t t0 = srv_globaltimer();
+  int64_t pub = ld_acquire_sys(&q->n_pub);
+  while (pub <= taken) {
+    const bool stop = *(volatile int32_t *)&q->stop != 0;
+    if (stop || srv_globaltimer() - t0 > poll_ns) {
+      db->nrows = 0;
+      db->req_begin = taken;
+      if (!stop) *(volatile int64_t *)&q->idle_polls = *(volatile int64_t *)&q->idle_polls + 1;
+      cudaGraphSetConditional(h, stop ? 0u : 1u);
+      return;
+    }
+    __nanosleep(256);
+    pub = ld_acquire_sys(&q->n_pub);
+  }
+  const int64_t row0 = *(volatile int64_t *)&q->req_row[taken % SRV_QCAP];
+  int32_t n = 0;
+  int64_t r = taken;
+  while (r < pub) {
+    const int64_t rs = *(volatile int64_t *)&q->req_row[r % SRV_QCAP];
+    const int32_t rn = *(volatile int32_t *)&q->req_n[r % SRV_QCAP];
+    if (r > taken && (rs != row0 + n || n + rn > max_batch)) break;
+    n += rn;
+    ++r;
+  }
+  db->codes = pool + row0 * row_bytes;
+  db->nrows = n;
+  db->row0 = row0;
+  db->req_begin = taken;
+  db->req_end = r;
+  cudaGraphSetConditional(h, 1u);
+}
+
+/* the batch's coordinates (scaled by eigscale) and statuses into the mapped result rows */
+__global__ void k_srv_emit(const gp_tc_batch *db, const double *a, const int32_t *st,
+                           const double *escale, int32_t K, double *res, int32_t *rst)
+{
+  const int32_t n = db->nrows;
+  const int64_t row0 = db->row0;
+  for (int32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    const int32_t sq = st[q];
+    double *o = res + (row0 + q) * K;
+    for (int32_t j = 0; j < K; ++j) o[j] = sq == 0 ? a[(int64_t)j * n + q] * escale[j] : 0.0;
+    rst[row0 + q] = sq;
+  }
+  __threadfence_system();
+}
+
+/* the batch's error word into its requests, then the completed count (release) */
+__global__ void k_srv_done(gp_srv_queue *q, const gp_tc_batch *db, int *err)
+{
+  if (db->req_end <= db->req_begin) return;
+  const int e = *err;
+  *err = 0;
+  for (int64_t r = db->req_begin; r < db->req_end; ++r) q->req_err[r % SRV_QCAP] = e;
+  if (e) q->err = e;
+  q->batches = q->batches + 1;
+  __threadfence_system();
+  st_release_sys(&q->n_done, db->req_end);
+}
+
 static int srv_fail(gp_server *s, int code, const char *msg)
 {
   snprintf(s->err, sizeof s->err, "%s", msg);
@@ -281,7 +404,7 @@ static int launch_batch(gp_server *s, gp_batch *b)
   }
   k_lsq_solve<<<(b->nrows + 127) / 128, 128, 0, ctx->stream>>>(
       s->d_co[sl], s->ldp, s->d_rr[sl], s->K, b->nrows, s->d_a[sl], s->d_b[sl], s->d_nobs[sl],
-      s->d_status[sl], s->d_work[sl]);
+      s->d_status[sl], s->d_work[sl], NULL);
   GP_LAUNCH_CHECK(ctx, "k_lsq_solve");
   GP_CUDA(ctx, cudaMemcpyAsync(s->h_a[sl], s->d_a[sl], sizeof(double) * (size_t)s->K * b->nrows,
                                cudaMemcpyDeviceToHost, ctx->stream));
@@ -323,58 +446,202 @@ static void complete_batch(gp_server *s, gp_batch *b, int rc)
   s->n_samples += n;
 }
 
+/* results of the device loop's completed requests into the callers' buffers; lock held */
+static bool complete_published(gp_server *s)
+{
+  const int64_t done = __atomic_load_n(&s->hq->n_done, __ATOMIC_ACQUIRE);
+  s->n_done_seen = done;
+  bool any = false;
+  const int32_t K = s->K;
+  while (!s->published.empty() && s->published.front()->seq < done) {
+    gp_req *r = s->published.front();
+    s->published.pop_front();
+    const int e = s->hq->req_err[r->seq % SRV_QCAP];
+    if (!r->error && e) r->error = GP_ERR_TIMEOUT;
+    if (!r->error) {
+      for (int32_t q = 0; q < r->nsamp; ++q) {
+        const int64_t row = r->row_start + q;
+        r->status[q] = s->h_rst[row];
+        memcpy(r->coords + (size_t)q * K, s->h_res + row * K, sizeof(double) * (size_t)K);
+      }
+    }
+    s->tail += r->skip + r->nsamp;
+    cudaEventDestroy(r->copied);
+    r->copied = NULL;
+    r->done = 1;
+    s->n_requests++;
+    s->n_samples += r->nsamp;
+    any = true;
+  }
+  s->n_batches = *(volatile int64_t *)&s->hq->batches;
+  return any;
+}
+
+/* every request still owned by the loop fails with rc (the loop's stream stopped); lock held */
+static void fail_loop_requests(gp_server *s, int rc)
+{
+  for (std::deque<gp_req *> *d : {&s->published, &s->admitted}) {
+    for (gp_req *r : *d) {
+      if (!r->error) r->error = rc;
+      s->tail += r->skip + r->nsamp;
+      if (r->copied) cudaEventDestroy(r->copied);
+      r->copied = NULL;
+      r->done = 1;
+    }
+    d->clear();
+  }
+}
+
+/* launch the device-resident loop (lock held); its queue counters carry on from the last run */
+static int start_loop(gp_server *s)
+{
+  __atomic_store_n(&s->hq->stop, 0, __ATOMIC_RELEASE);
+  cudaError_t e = cudaGraphLaunch(s->gexec, s->ctx->stream);
+  if (e != cudaSuccess) {
+    snprintf(s->err, sizeof s->err, "cudaGraphLaunch: %s", cudaGetErrorString(e));
+    return GP_ERR_CUDA;
+  }
+  s->loop_launches++;
+  s->loop_running = 1;
+  return GP_OK;
+}
+
+/* ask the loop to end, wait for it (it drains the published requests and sees the flag
+ * within one poll), and hand back what it completed; lock held, released while waiting */
+static void stop_loop(gp_server *s)
+{
+  __atomic_store_n(&s->hq->stop, 1, __ATOMIC_RELEASE);
+  pthread_mutex_unlock(&s->mu);
+  cudaError_t e = cudaStreamSynchronize(s->ctx->stream);
+  pthread_mutex_lock(&s->mu);
+  s->loop_running = 0;
+  complete_published(s);
+  if (e != cudaSuccess || !s->published.empty()) {
+    snprintf(s->err, sizeof s->err, "the device-resident serving loop stopped: %s",
+             cudaGetErrorString(e));
+    fail_loop_requests(s, GP_ERR_CUDA);
+  }
+  pthread_cond_broadcast(&s->cv);
+}
+
+/*
+ * The scheduler thread.  With the device-resident loop running it only admits requests into
+ * the pool (their copies start on the copy stream), publishes each, in order, once its copy
+ * has completed, and hands the loop's results back: it launches nothing.  The loop yields
+ * while full-PCA jobs wait or run and while the server is paused (calls that synchronise the
+ * whole device, such as cudaFree in a PCA job, would otherwise wait on it); then, and with
+ * host_loop or fp64_serial, the thread forms the batches itself and launches each one's
+ * kernels, two batches in flight.
+ */
 static void *scheduler(void *arg)
 {
   gp_server *s = (gp_server *)arg;
   cudaSetDevice(s->ctx->device);
   int next_slot = 0;
   pthread_mutex_lock(&s->mu);
-  while (!s->stop || !s->admitted.empty() || !s->inflight.empty() || !s->waiting.empty()) {
+  for (;;) {
     admit_waiting(s);
-    if (!s->paused && s->inflight.size() < 2 && !s->admitted.empty()) {
-      /* the next batch: admitted requests, contiguous in the pool, up to max_batch rows */
-      gp_batch *b = new gp_batch;
-      b->slot = next_slot;
-      next_slot ^= 1;
-      b->row_start = s->admitted.front()->row_start;
-      b->nrows = 0;
+    const bool yield = s->paused || !s->pca_waiting.empty() || s->pca_running > 0;
+    if (s->loop_running) {
+      if (yield || s->stop) {
+        if (s->stop && !yield && (!s->admitted.empty() || !s->waiting.empty())) {
+          /* closing: let the loop finish what is queued first */
+        } else {
+          stop_loop(s);
+          continue;
+        }
+      }
+      bool progress = false;
       while (!s->admitted.empty()) {
         gp_req *r = s->admitted.front();
-        if (!b->reqs.empty() && (s->fp64_serial || r->skip != 0 ||
-                                 r->row_start != b->row_start + b->nrows ||
-                                 b->nrows + r->nsamp > s->max_batch))
-          break;
-        b->reqs.push_back(r);
-        b->nrows += r->nsamp;
+        if (!r->error) {
+          cudaError_t q = cudaEventQuery(r->copied);
+          if (q == cudaErrorNotReady) break;
+          if (q != cudaSuccess) r->error = GP_ERR_CUDA;
+        }
+        if (s->n_pub - s->n_done_seen >= SRV_QCAP) break;
+        const int64_t i = s->n_pub % SRV_QCAP;
+        s->hq->req_row[i] = r->row_start;
+        s->hq->req_n[i] = r->nsamp;
+        r->seq = s->n_pub++;
+        __atomic_store_n(&s->hq->n_pub, s->n_pub, __ATOMIC_RELEASE);
         s->admitted.pop_front();
-        if (s->fp64_serial) break;
+        s->published.push_back(r);
+        progress = true;
       }
-      b->failed = 0;
-      cudaEventCreateWithFlags(&b->finished, cudaEventDisableTiming);
-      s->inflight.push_back(b);
-      pthread_mutex_unlock(&s->mu);
-      int rc = launch_batch(s, b);
-      if (rc) {
-        /* completes in order behind the batches before it, once the stream has drained */
-        cudaStreamSynchronize(s->ctx->stream);
-        b->failed = rc;
+      if (complete_published(s)) progress = true;
+      if (cudaStreamQuery(s->ctx->stream) != cudaErrorNotReady) {
+        /* the loop's graph ended without being asked to (a CUDA error) */
+        stop_loop(s);
+        progress = true;
       }
-      pthread_mutex_lock(&s->mu);
-      continue;
+      if (progress) {
+        pthread_cond_broadcast(&s->cv);
+        continue;
+      }
+      if (s->stop && s->waiting.empty() && s->admitted.empty() && s->published.empty()) {
+        stop_loop(s);
+        continue;
+      }
+      /* the loop is working on published requests, or a copy is in flight: poll */
+      if (!s->published.empty() || !s->admitted.empty()) {
+        pthread_mutex_unlock(&s->mu);
+        struct timespec ts = {0, 20 * 1000};
+        nanosleep(&ts, NULL);
+        pthread_mutex_lock(&s->mu);
+        continue;
+      }
+    } else {
+      if (s->gexec && !yield && !s->stop && s->inflight.empty()) {
+        if (start_loop(s) == GP_OK) continue;
+        cudaGraphExecDestroy(s->gexec); /* stay on the host-launched schedule */
+        s->gexec = NULL;
+      }
+      if (!s->paused && s->inflight.size() < 2 && !s->admitted.empty()) {
+        /* the next batch: admitted requests, contiguous in the pool, up to max_batch rows */
+        gp_batch *b = new gp_batch;
+        b->slot = next_slot;
+        next_slot ^= 1;
+        b->row_start = s->admitted.front()->row_start;
+        b->nrows = 0;
+        while (!s->admitted.empty()) {
+          gp_req *r = s->admitted.front();
+          if (!b->reqs.empty() && (s->fp64_serial || r->skip != 0 ||
+                                   r->row_start != b->row_start + b->nrows ||
+                                   b->nrows + r->nsamp > s->max_batch))
+            break;
+          b->reqs.push_back(r);
+          b->nrows += r->nsamp;
+          s->admitted.pop_front();
+          if (s->fp64_serial) break;
+        }
+        b->failed = 0;
+        cudaEventCreateWithFlags(&b->finished, cudaEventDisableTiming);
+        s->inflight.push_back(b);
+        pthread_mutex_unlock(&s->mu);
+        int rc = launch_batch(s, b);
+        if (rc) {
+          /* completes in order behind the batches before it, once the stream has drained */
+          cudaStreamSynchronize(s->ctx->stream);
+          b->failed = rc;
+        }
+        pthread_mutex_lock(&s->mu);
+        continue;
+      }
+      if (!s->inflight.empty()) {
+        gp_batch *b = s->inflight.front();
+        pthread_mutex_unlock(&s->mu);
+        cudaError_t e = b->failed ? cudaSuccess : cudaEventSynchronize(b->finished);
+        pthread_mutex_lock(&s->mu);
+        s->inflight.pop_front();
+        complete_batch(s, b, b->failed ? b->failed : (e == cudaSuccess ? GP_OK : GP_ERR_CUDA));
+        cudaEventDestroy(b->finished);
+        delete b;
+        pthread_cond_broadcast(&s->cv);
+        continue;
+      }
+      if (s->stop && s->waiting.empty() && s->admitted.empty()) break;
     }
-    if (!s->inflight.empty()) {
-      gp_batch *b = s->inflight.front();
-      pthread_mutex_unlock(&s->mu);
-      cudaError_t e = b->failed ? cudaSuccess : cudaEventSynchronize(b->finished);
-      pthread_mutex_lock(&s->mu);
-      s->inflight.pop_front();
-      complete_batch(s, b, b->failed ? b->failed : (e == cudaSuccess ? GP_OK : GP_ERR_CUDA));
-      cudaEventDestroy(b->finished);
-      delete b;
-      pthread_cond_broadcast(&s->cv);
-      continue;
-    }
-    if (s->stop) break;
     struct timespec ts;
     clock_gettime(CLOCK_REALTIME, &ts);
     ts.tv_nsec += 50 * 1000 * 1000;
@@ -386,6 +653,58 @@ static void *scheduler(void *arg)
   }
   pthread_mutex_unlock(&s->mu);
   return NULL;
+}
+
+/*
+ * The loop: one CUDA graph whose while node runs, per iteration, the batch former, the two
+ * exact tensor-core products of the batch's rows (normal equations and right-hand sides),
+ * the per-sample solves, the result write-back and the completion count.  Captured once;
+ * every kernel reads the batch from d_batch at run time.
+ */
+static int build_loop(gp_server *s)
+{
+  gp_ctx *ctx = s->ctx;
+  const int32_t K = s->K, mb = s->max_batch;
+  cudaGraph_t g = NULL;
+  GP_CUDA(ctx, cudaGraphCreate(&g, 0));
+  s->graph = g;
+  cudaGraphConditionalHandle h;
+  GP_CUDA(ctx, cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+  cudaGraphNodeParams np = {};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = h;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  GP_CUDA(ctx, cudaGraphAddNode(&node, g, NULL, NULL, 0, &np));
+  cudaGraph_t body = np.conditional.phGraph_out[0];
+  GP_CUDA(ctx, cudaStreamBeginCaptureToGraph(ctx->stream, body, NULL, NULL, 0,
+                                             cudaStreamCaptureModeRelaxed));
+  int rc = GP_OK;
+  k_srv_take<<<1, 32, 0, ctx->stream>>>(s->dq, s->d_batch, s->d_pool, s->row_bytes, mb, h,
+                                       SRV_POLL_NS);
+  if (cudaPeekAtLastError() != cudaSuccess) rc = GP_ERR_CUDA;
+  if (!rc) rc = gp_tc_apply_dev(ctx, s->d_batch, mb, s->row_bytes, &s->Pco, s->d_Z, s->d_co[0],
+                                s->ldp);
+  if (!rc) rc = gp_tc_apply_dev(ctx, s->d_batch, mb, s->row_bytes, &s->Prr, s->d_Z, s->d_rr[0], K);
+  if (!rc) {
+    k_lsq_solve<<<(mb + 127) / 128, 128, 0, ctx->stream>>>(
+        s->d_co[0], s->ldp, s->d_rr[0], K, 0, s->d_a[0], s->d_b[0], s->d_nobs[0],
+        s->d_status[0], s->d_work[0], &s->d_batch->nrows);
+    k_srv_emit<<<(mb + 127) / 128, 128, 0, ctx->stream>>>(s->d_batch, s->d_a[0], s->d_status[0],
+                                                          s->d_escale, K, s->d_res, s->d_rst);
+    k_srv_done<<<1, 1, 0, ctx->stream>>>(s->dq, s->d_batch, ctx->d_err);
+    if (cudaPeekAtLastError() != cudaSuccess) rc = GP_ERR_CUDA;
+  }
+  cudaGraph_t captured = NULL;
+  cudaError_t e = cudaStreamEndCapture(ctx->stream, &captured);
+  if (rc) return gp_fail(ctx, rc, "gp_serve_open: capturing the serving loop failed");
+  if (e != cudaSuccess) return gp_cuda_fail(ctx, e, "gp_serve_open: cudaStreamEndCapture");
+  GP_CUDA(ctx, cudaGraphInstantiate(&s->gexec, g, 0));
+  GP_CUDA(ctx, cudaMemsetAsync(s->d_batch, 0, sizeof(gp_tc_batch), ctx->stream));
+  GP_CUDA(ctx, cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
+  GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return GP_OK;
 }
 
 /* full-PCA worker: takes the front job when it fits the budget (or nothing else runs) */
@@ -404,7 +723,9 @@ static void *pca_worker(void *arg)
   pthread_mutex_lock(&s->mu);
   for (;;) {
     gp_req *j = NULL;
-    if (!s->pca_waiting.empty()) {
+    /* a job starts only while the device-resident loop is stopped (the scheduler stops it
+     * when jobs wait): the job's allocations synchronise the device */
+    if (!s->pca_waiting.empty() && !s->loop_running) {
       gp_req *f = s->pca_waiting.front();
       if (s->pca_running == 0 || s->pca_used + f->footprint <= s->pca_budget) {
         j = f;
@@ -479,11 +800,21 @@ extern "C" void gp_serve_close(gp_server *s)
   }
   for (gp_ctx *w : s->wctx) gp_close(w);
   if (s->ctx) cudaSetDevice(s->ctx->device);
+  if (s->ctx && s->loop_running && !s->thread_started) {
+    /* opened the loop but not the thread: stop the loop here */
+    __atomic_store_n(&s->hq->stop, 1, __ATOMIC_RELEASE);
+    cudaStreamSynchronize(s->ctx->stream);
+  }
+  if (s->gexec) cudaGraphExecDestroy(s->gexec);
+  if (s->graph) cudaGraphDestroy(s->graph);
+  if (s->hq) cudaFreeHost(s->hq);
+  if (s->h_res) cudaFreeHost(s->h_res);
+  if (s->h_rst) cudaFreeHost(s->h_rst);
   void *dev[] = {s->d_E,     s->d_P,      s->d_fE,     s->d_mE,     s->d_otab,   s->d_rtab,
                  s->stor_co, s->stor_rr,  s->d_pool,   s->d_co[0],  s->d_co[1],  s->d_rr[0],
                  s->d_rr[1], s->d_a[0],   s->d_a[1],   s->d_b[0],   s->d_b[1],   s->d_work[0],
                  s->d_work[1], s->d_part[0], s->d_part[1], s->d_nobs[0], s->d_nobs[1],
-                 s->d_status[0], s->d_status[1]};
+                 s->d_status[0], s->d_status[1], s->d_batch, s->d_Z, s->d_escale};
   for (size_t i = 0; i < sizeof(dev) / sizeof(dev[0]); ++i)
     if (dev[i]) cudaFree(dev[i]);
   for (int i = 0; i < 2; ++i) {
@@ -524,6 +855,7 @@ extern "C" int gp_serve_open(gp_ctx *src, const gp_serve_opts *o, gp_server **ou
   s->pool_cap = o->pool_samples > 0 ? o->pool_samples : 32768;
   if (s->pool_cap < s->max_batch) s->pool_cap = s->max_batch;
   s->fp64_serial = o->fp64_serial;
+  s->host_loop = o->host_loop || o->fp64_serial;
   s->eigscale.assign((size_t)K, 1.0);
   if (o->eigscale)
     for (int32_t j = 0; j < K; ++j) s->eigscale[(size_t)j] = o->eigscale[j];
@@ -562,6 +894,30 @@ extern "C" int gp_serve_open(gp_ctx *src, const gp_serve_opts *o, gp_server **ou
     size_t b1 = gp_tc_prepared_bytes(1, s->ldp, s->nk), b2 = gp_tc_prepared_bytes(2, K, s->nk);
     SALLOC(s->stor_co, b1);
     SALLOC(s->stor_rr, b2);
+  }
+  if (!s->host_loop) {
+    /* the loop's queue and result rows in mapped pinned host memory, its batch state and the
+     * products' slice-column buffer (normal-equation panel: the wider of the two) */
+    const int64_t ncols4_pad = ((int64_t)4 * s->ldp + 127) / 128 * 128;
+    SALLOC(s->d_batch, sizeof(gp_tc_batch));
+    SALLOC(s->d_Z, sizeof(double) * (size_t)s->max_batch * ncols4_pad);
+    SALLOC(s->d_escale, sizeof(double) * K);
+    if (e == cudaSuccess)
+      e = cudaHostAlloc((void **)&s->hq, sizeof(gp_srv_queue), cudaHostAllocMapped);
+    if (e == cudaSuccess)
+      e = cudaHostAlloc((void **)&s->h_res, sizeof(double) * (size_t)s->pool_cap * K,
+                        cudaHostAllocMapped);
+    if (e == cudaSuccess)
+      e = cudaHostAlloc((void **)&s->h_rst, sizeof(int32_t) * (size_t)s->pool_cap,
+                        cudaHostAllocMapped);
+    if (e == cudaSuccess) {
+      memset(s->hq, 0, sizeof(gp_srv_queue));
+      e = cudaHostGetDevicePointer((void **)&s->dq, s->hq, 0);
+    }
+    if (e == cudaSuccess) e = cudaHostGetDevicePointer((void **)&s->d_res, s->h_res, 0);
+    if (e == cudaSuccess) e = cudaHostGetDevicePointer((void **)&s->d_rst, s->h_rst, 0);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(s->d_escale, s->eigscale.data(), sizeof(double) * K, cudaMemcpyHostToDevice);
   }
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) {
@@ -614,12 +970,14 @@ extern "C" int gp_serve_open(gp_ctx *src, const gp_serve_opts *o, gp_server **ou
       return rc;
     }
   }
-  if (pthread_create(&s->thread, NULL, scheduler, s) != 0) {
-    gp_fail(src, GP_ERR_STATE, "gp_serve_open: could not start the scheduler thread");
-    gp_serve_close(s);
-    return GP_ERR_STATE;
+  if (!s->host_loop && s->nk > 0) {
+    rc = build_loop(s);
+    if (rc) {
+      snprintf(src->err, GP_ERRLEN, "%s", gp_last_error(ctx));
+      gp_serve_close(s);
+      return rc;
+    }
   }
-  s->thread_started = 1;
   /* full-PCA workers, each with its own handle (stream, solver) */
   s->pca_budget = o->pca_budget_bytes > 0 ? o->pca_budget_bytes : ((int64_t)64 << 30);
   const int nw = o->pca_workers > 0 ? (o->pca_workers > 8 ? 8 : o->pca_workers) : 1;
@@ -639,6 +997,18 @@ extern "C" int gp_serve_open(gp_ctx *src, const gp_serve_opts *o, gp_server **ou
     gp_fail(src, GP_ERR_STATE, "gp_serve_open: could not start a PCA worker");
     gp_serve_close(s);
     return GP_ERR_STATE;
+  }
+  if (pthread_create(&s->thread, NULL, scheduler, s) != 0) {
+    gp_fail(src, GP_ERR_STATE, "gp_serve_open: could not start the scheduler thread");
+    gp_serve_close(s);
+    return GP_ERR_STATE;
+  }
+  s->thread_started = 1;
+  if (s->gexec) {
+    /* the loop: launched once the workers' handles exist (their creation may allocate) */
+    pthread_mutex_lock(&s->mu);
+    if (!s->loop_running) start_loop(s);
+    pthread_mutex_unlock(&s->mu);
   }
   *out = s;
   return GP_OK;
@@ -778,7 +1148,25 @@ extern "C" int gp_serve_pause(gp_server *s, int32_t paused)
   pthread_mutex_lock(&s->mu);
   s->paused = paused ? 1 : 0;
   pthread_cond_broadcast(&s->cv);
+  /* a pause returns once the device-resident loop has stopped, so that the caller may then
+   * make calls that synchronise the device */
+  while (s->paused && s->loop_running && s->thread_started)
+    pthread_cond_wait(&s->cv, &s->mu);
   pthread_mutex_unlock(&s->mu);
+  return GP_OK;
+}
+
+extern "C" int gp_serve_loop_stats(const gp_server *s, int32_t *device_loop, int64_t *launches,
+                                   int64_t *batches, int64_t *idle_polls)
+{
+  if (!s) return GP_ERR_ARG;
+  gp_server *m = (gp_server *)s;
+  pthread_mutex_lock(&m->mu);
+  if (device_loop) *device_loop = s->loop_running;
+  if (launches) *launches = s->loop_launches;
+  if (batches) *batches = s->hq ? *(volatile int64_t *)&s->hq->batches : s->n_batches;
+  if (idle_polls) *idle_polls = s->hq ? *(volatile int64_t *)&s->hq->idle_polls : 0;
+  pthread_mutex_unlock(&m->mu);
   return GP_OK;
 }
 

@@ -41,7 +41,7 @@ EXPORTED = ["gp_version", "gp_last_error", "gp_open", "gp_close", "gp_device_byt
             "gp_serve_submit_pca", "gp_serve_pca_stats", "gp_smartpca_footprint", "gp_release",
             "gp_keep_gram", "gp_relate", "gp_record_bytes", "gp_encode_records",
             "gp_last_encode_time", "gp_fst", "gp_set_blocks", "gp_set_row_pops",
-            "gp_lsqproj_pops"]
+            "gp_lsqproj_pops", "gp_serve_loop_stats"]
 
 i32p = C.POINTER(C.c_int32)
 i64p = C.POINTER(C.c_int64)
@@ -77,7 +77,7 @@ class Panel(C.Structure):
 class ServeOpts(C.Structure):
     _fields_ = [("numeigs", C.c_int32), ("max_batch", C.c_int32), ("pool_samples", C.c_int64),
                 ("fp64_serial", C.c_int32), ("eigscale", f64p), ("pca_workers", C.c_int32),
-                ("pca_budget_bytes", C.c_int64)]
+                ("pca_budget_bytes", C.c_int64), ("host_loop", C.c_int32)]
 
 
 class RunResult(C.Structure):
@@ -150,6 +150,7 @@ def load_library():
         "gp_serve_submit_pca": (C.c_int, [vp, C.POINTER(Panel), C.POINTER(SmartpcaOpts),
                                           C.POINTER(RunResult), i64p]),
         "gp_serve_pca_stats": (C.c_int, [vp, i64p, i32p, i64p]),
+        "gp_serve_loop_stats": (C.c_int, [vp, i32p, i64p, i64p, i64p]),
         "gp_smartpca_footprint": (C.c_int64, [C.c_int32, C.c_int64, C.c_int32, C.c_int32]),
         "gp_release": (C.c_int, [vp]),
         "gp_keep_gram": (C.c_int, [vp, C.c_int32]),
@@ -496,12 +497,13 @@ class Server:
     """Projection server on the panel (SNP weights) resident in `handle` (gpupca_serve.h)."""
 
     def __init__(self, handle, numeigs, max_batch=0, pool_samples=0, fp64_serial=False,
-                 eigscale=None, pca_workers=0, pca_budget_bytes=0):
+                 eigscale=None, pca_workers=0, pca_budget_bytes=0, host_loop=False):
         self.lib = load_library()
         self.K = numeigs
         self._scale = None if eigscale is None else np.ascontiguousarray(eigscale, np.float64)
         o = ServeOpts(numeigs, max_batch, pool_samples, int(fp64_serial),
-                      ptr(self._scale, C.c_double), pca_workers, pca_budget_bytes)
+                      ptr(self._scale, C.c_double), pca_workers, pca_budget_bytes,
+                      int(host_loop))
         s = vp()
         handle.check(self.lib.gp_serve_open(handle.h, C.byref(o), C.byref(s)), "gp_serve_open")
         self.s = s
@@ -542,6 +544,13 @@ class Server:
                                                 C.byref(a.result), C.byref(t)),
                    "gp_serve_submit_pca")
         return PcaJob(self, t.value, a)
+
+    def loop_stats(self):
+        """(device loop running, graph launches, batches it ran, polls that ran out idle)"""
+        a, b, c, d = C.c_int32(), C.c_int64(), C.c_int64(), C.c_int64()
+        self.check(self.lib.gp_serve_loop_stats(self.s, C.byref(a), C.byref(b), C.byref(c),
+                                                C.byref(d)), "gp_serve_loop_stats")
+        return a.value, b.value, c.value, d.value
 
     def pca_stats(self):
         a, b, c = C.c_int64(), C.c_int32(), C.c_int64()

@@ -18,6 +18,15 @@
  * batch.  Products are exact integer sums, so a sample's coordinates do not depend on which
  * other requests share its batch.
  *
+ * The batches run in one persistent launch: a CUDA graph whose while-loop body takes the next
+ * batch from a request queue in mapped host memory (a device kernel waits, bounded by a poll
+ * interval, for published requests and packs every contiguous one up to max_batch rows), runs
+ * the two tensor-core products and the solves on that batch's rows, writes the coordinates
+ * and statuses into mapped host memory at the requests' pool rows and publishes the count of
+ * completed requests.  The host thread only copies request rows in, publishes them, and
+ * hands results back; the loop ends when the server closes.  host_loop = 1 keeps the
+ * previous schedule (one set of launches per batch from the host thread).
+ *
  * Full-PCA jobs (gp_serve_submit_pca) share the server: they are admitted by estimated device
  * footprint and run on worker handles beside the projection batches.
  *
@@ -48,6 +57,8 @@ typedef struct {
   const double *eigscale;/* [K] multiplies coordinate j (seteigscale); NULL = 1 */
   int32_t pca_workers;   /* full-PCA worker handles (default 1 when 0, at most 8) */
   int64_t pca_budget_bytes; /* device bytes the running PCA jobs may hold (default 64 GiB) */
+  int32_t host_loop;     /* 1: the scheduler thread launches each batch's kernels; 0 (default):
+                            one device-resident loop (below) forms and runs the batches */
 } gp_serve_opts;
 
 int gp_serve_open(gp_ctx *src, const gp_serve_opts *opts, gp_server **out);
@@ -73,6 +84,10 @@ int64_t gp_smartpca_footprint(int32_t nind, int64_t nsnp, int32_t precision, int
 /* PCA jobs completed, the largest number that ran at once, bytes admitted now */
 int gp_serve_pca_stats(const gp_server *srv, int64_t *jobs_done, int32_t *peak_running,
                        int64_t *bytes_in_use);
+/* the device-resident loop: 1 when it runs (0 with host_loop or fp64_serial), graph launches
+ * made (1 per server), batches it ran, polls that ran out with no request published */
+int gp_serve_loop_stats(const gp_server *srv, int32_t *device_loop, int64_t *launches,
+                        int64_t *batches, int64_t *idle_polls);
 
 /* 1 when the request has completed, 0 while pending, < 0 on error.  A call that reports
  * completion (1 or the request's error) releases the ticket; one waiter per ticket. */
@@ -81,7 +96,11 @@ int gp_serve_test(gp_server *srv, int64_t ticket);
  * passes (GP_ERR_TIMEOUT, the ticket stays valid) */
 int gp_serve_wait(gp_server *srv, int64_t ticket, double timeout_s);
 /* paused = 1: admission and copies go on but no new batch starts (batches in flight
- * finish); paused = 0 resumes.  gp_serve_close resumes and drains. */
+ * finish); it returns once the device-resident loop has stopped.  paused = 0 resumes (and
+ * relaunches the loop).  gp_serve_close resumes and drains.  While the loop runs, calls
+ * that synchronise the whole device (cudaFree, cudaHostRegister, cudaDeviceSynchronize, by
+ * any thread of the process) wait for it: pause the server around them, or open it with
+ * host_loop = 1.  Full-PCA jobs of the server stop the loop themselves while they run. */
 int gp_serve_pause(gp_server *srv, int32_t paused);
 /* counters: batches run, samples projected, requests completed */
 int gp_serve_stats(const gp_server *srv, int64_t *batches, int64_t *samples, int64_t *requests);

@@ -95,9 +95,39 @@ def test_serve_alone_equals_mixed(gpu, panel):
             r.wait(60.0)
         b, n, q = srv.stats()
         # ~1,900 samples in batches of <= 512 rows: a handful of batches for 42 requests
-        assert q == 42 and b <= 12
+        assert q == 42 and b <= 16
     assert np.array_equal(st_alone, sm)
     assert np.array_equal(alone, cm)
+
+
+def test_serve_device_loop_one_launch_bounded_polls(gpu, panel):
+    """the batches run in one persistent launch (the device-resident loop); with no request
+    its bounded poll runs out and the loop iterates instead of waiting for ever"""
+    import time
+    nind = panel["nind"]
+    with native.Server(gpu, K) as srv:
+        on, launches, b0, idle0 = srv.loop_stats()
+        assert on == 1 and launches == 1 and b0 == 0
+        time.sleep(0.05)
+        _, _, _, idle1 = srv.loop_stats()
+        assert idle1 > idle0
+        reqs = [(samp, srv.submit(_rows(srv, panel, samp)))
+                for samp in np.array_split(np.arange(nind), 5)]
+        for samp, r in reqs:
+            coords, status = r.wait(60.0)
+            _check_vs_lsqproj(panel, samp, coords, status)
+        on, launches, b1, _ = srv.loop_stats()
+        assert on == 1 and launches == 1 and 1 <= b1 <= 5
+
+
+def test_serve_host_loop_schedule(gpu, panel):
+    """the host-launched schedule (host_loop) gives the same coordinates"""
+    nind = panel["nind"]
+    with native.Server(gpu, K, host_loop=True) as srv:
+        assert srv.loop_stats()[0] == 0
+        samp = np.arange(nind)
+        coords, status = srv.submit(_rows(srv, panel, samp)).wait(60.0)
+        _check_vs_lsqproj(panel, samp, coords, status)
 
 
 def test_serve_small_pool_admission_and_eigscale(gpu, panel):

@@ -557,12 +557,14 @@ def run_gpu(args, cfg, local):
     step(True)
     torch.cuda.synchronize()
     h.transfer_bytes(reset=True)
+    e2e_phases = []
     for _ in range(max(1, min(args.steps, args.e2e_steps))):
         torch.cuda.synchronize()
         t = time.perf_counter()
         r2 = step(True)
         torch.cuda.synchronize()
         e2e_times.append((time.perf_counter() - t) * 1e3)
+        e2e_phases.append({k: round(v * 1e3, 2) for k, v in r2["t_phase"].items()})
     h2d, d2h = h.transfer_bytes(reset=True)
     n_e2e = len(e2e_times)
     native.host_unregister(rec)
@@ -581,6 +583,7 @@ def run_gpu(args, cfg, local):
     res = dict(step_ms=step_ms, gram_flops=total_flops, gram_ms=g_ms, gram_launches=g_launch,
                tridiag_ms=float(np.mean(tri_ms)) if tri_ms else 0.0, tridiag_n=tri_n,
                gram_kernel_flops=g_flops, clocks=clk, e2e_ms=e2e_ms, e2e_runs_ms=e2e_times,
+               e2e_phases=e2e_phases,
                h2d=h2d / n_e2e,
                d2h=d2h / n_e2e, run=r, gen_s=gen_s, peaks=peaks, peak_kind=peak_kind,
                nind=nind, launches=launches, acc=acc, serving=serving, counts=(c_ms, c_bytes))
@@ -915,7 +918,7 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--precision", default="fp16", choices=["fp64", "bf16", "bf16x4", "fp16"])
     ap.add_argument("--config", default="full", choices=list(CONFIGS))
@@ -1079,7 +1082,8 @@ def main():
             "clocks": res["clocks"],
             "e2e": {"value": e2e, "unit": "TFLOP/s", "h2d_bytes_per_step": int(res["h2d"]),
                     "d2h_bytes_per_step": int(res["d2h"]), "wall_s": res["e2e_ms"] / 1e3,
-                    "runs_ms": [round(x, 2) for x in res["e2e_runs_ms"]]},
+                    "runs_ms": [round(x, 2) for x in res["e2e_runs_ms"]],
+                    "runs_phases_ms": res["e2e_phases"]},
             "accuracy_vs_fp64": res["acc"], "serving": res["serving"],
             "gpu_launches": res["launches"],
             "gpu_launches_note": "own kernels per timed step (all kernels of the step are this "

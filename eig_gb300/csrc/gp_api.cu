@@ -110,16 +110,29 @@ int gp_scratch2(gp_ctx *ctx, size_t bytes, void **out)
   return rc;
 }
 
+/* a handle buffer of at least `bytes` (contents not kept): the allocation stays while it is
+ * large enough, so that the per-pass buffers of a run (sample and SNP lists, tables, vectors)
+ * cost no cudaFree / cudaMalloc, nor their device synchronisation, after the first pass */
 int gp_realloc(gp_ctx *ctx, void **ptr, size_t bytes)
 {
+  if (bytes < 256) bytes = 256;
+  int slot = -1;
+  for (int i = 0; i < ctx->ncaps; ++i)
+    if (ctx->caps[i].p == ptr) slot = i;
+  if (slot >= 0 && *ptr && ctx->caps[slot].bytes >= bytes) return GP_OK;
   if (*ptr) cudaFree(*ptr);
   *ptr = NULL;
-  cudaError_t e = cudaMalloc(ptr, bytes < 256 ? 256 : bytes);
+  cudaError_t e = cudaMalloc(ptr, bytes);
   if (e != cudaSuccess) {
     *ptr = NULL;
     return gp_fail(ctx, GP_ERR_NOMEM, "device allocation of %zu bytes failed: %s", bytes,
                    cudaGetErrorString(e));
   }
+  if (slot < 0 && ctx->ncaps < (int)(sizeof(ctx->caps) / sizeof(ctx->caps[0]))) {
+    slot = ctx->ncaps++;
+    ctx->caps[slot].p = ptr;
+  }
+  if (slot >= 0) ctx->caps[slot].bytes = bytes;
   return GP_OK;
 }
 

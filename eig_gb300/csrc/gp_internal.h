@@ -106,6 +106,12 @@ struct gp_ctx {
   int *d_err;          /* error word written by the tensor-core kernels' bounded waits */
   int precision;       /* precision of the last gp_xtx: split precisions use the tensor-core
                           exact products for weights and lsqproject */
+  /* capacities of the buffers gp_realloc manages (kept while large enough) */
+  struct {
+    void **p;
+    size_t bytes;
+  } caps[32];
+  int ncaps;
 };
 
 int gp_fail(gp_ctx *ctx, int code, const char *fmt, ...);

@@ -113,3 +113,47 @@ def test_error_statuses(gpu):
     with native.Handle(0) as h:
         with pytest.raises(native.GpuError):
             native.smartpca_run(h, mono, 6, native.default_opts(numeigs=2, numoutliter=0))
+
+
+def test_lsqproj_non_pd_and_unobserved_samples(gpu):
+    """host-planted failures of lsqproject: sample 7 is observed only at SNPs whose PCA rows
+    are all heterozygous, so their values and weights are exactly 0 and its normal matrix is
+    0 (not positive definite: status 2, the reference's regressit -1000, coefficients left
+    as they were); sample 8 has no genotype (status 1, dropped).  Both as the oracle, and
+    through the whole flow (which keeps the previous sample's coefficients for status 2)."""
+    rec, pop = native.synth_records(2000, [90, 90], [0.02, 0.04], miss=0.02, seed=81,
+                                    nthreads=4)
+    nind = len(pop)
+    g = O.unpack(rec, nind)
+    g[:30, :] = 1
+    g[30:, 7] = -1
+    g[:, 8] = -1
+    rec2 = O.pack(g)
+    rows = np.array([k for k in range(nind) if k not in (7, 8)], np.int32)
+    cols = np.arange(2000, dtype=np.int32)
+    gpu.load_genotypes(rec2, nind)
+    gpu.set_samples(rows)
+    gpu.set_snps(cols)
+    gpu.xtx()
+    ev, V = gpu.eigvecs(5)
+    K = 5
+    ff, fx, sc = gpu.snp_weights(K)
+    proj = np.arange(nind, dtype=np.int32)
+    a, b, nobs, st = gpu.lsqproj(K, proj)
+    s = O.pass_columns(rec2, cols, rows)
+    off, ofx, osc = O.weights(s, V, K)
+    oa, ob, onobs, ost = O.lsqproj(s, off, osc, K, proj)
+    assert st[7] == 2 and nobs[7] == 30 and st[8] == 1 and nobs[8] == 0
+    assert np.array_equal(st, ost) and np.array_equal(nobs, onobs)
+    ok = st == 0
+    assert np.max(np.abs(a[:, ok] - oa[:, ok])) <= 1e-11 * max(1.0, np.max(np.abs(oa)))
+    # the flow: 7 and 8 outside the PCA (affstatus 0); 8 has no data at all and is ignored
+    aff = np.ones(nind, np.uint8)
+    aff[[7, 8]] = 0
+    opts = native.default_opts(numeigs=K, numoutliter=0)
+    r = native.smartpca_run(gpu, rec2, nind, opts, ind_affstatus=aff)
+    ref = O.smartpca(rec2, nind, numeigs=K, numoutliter=0, ind_affstatus=aff)
+    assert np.array_equal(r["ind_out"], ref["ind_out"]) and not r["ind_out"][8]
+    sgn = np.sign(np.sum(r["coords"] * ref["coords"], axis=1))
+    assert np.max(np.abs(r["coords"] - ref["coords"] * sgn[:, None])) <= 1e-8
+    assert np.array_equal(r["coords"][:, 7], r["coords"][:, 6])  # the previous sample's

@@ -361,7 +361,21 @@ int gp_smartpca_run(gp_ctx *ctx, const gp_smartpca_opts *o, const gp_panel *p,
   t = now_s();
   fxscal = (double *)calloc((size_t)K, sizeof(double));
   if (!fxscal) FAIL(GP_ERR_NOMEM);
-  rc = gp_snp_weights(ctx, K, NULL, NULL, fxscal);
+  if (r->ffvecs) {
+    /* the weights over the last pass's columns, scattered to SNP order */
+    double *ff = (double *)malloc(sizeof(double) * (size_t)K * ncols);
+    if (!ff) FAIL(GP_ERR_NOMEM);
+    rc = gp_snp_weights(ctx, K, ff, NULL, fxscal);
+    if (!rc) {
+      memset(r->ffvecs, 0, sizeof(double) * (size_t)K * M);
+      for (int32_t j = 0; j < K; ++j)
+        for (int32_t c = 0; c < ncols; ++c)
+          r->ffvecs[(size_t)j * M + cols[c]] = ff[(size_t)j * ncols + c];
+    }
+    free(ff);
+  } else {
+    rc = gp_snp_weights(ctx, K, NULL, NULL, fxscal);
+  }
   if (rc) goto done;
   double tw = now_s();
   r->t_phase[GP_PH_WEIGHTS] = tw - t;

@@ -425,6 +425,69 @@ static int in_list(const char *pop, char **list, int n)
   return 0;
 }
 
+/*
+ * writesnpeigs (src/eigensrc/smartpca.c:3038-3106): each eigenvector's SNP weights scaled to
+ * mean square 1 over the last pass's columns (sum of squares in column order, then
+ * sqrt(ncols / sum)), the "eigbestsnp" log lines (per eigenvector the 10 largest |weight| of
+ * the SNPs still in use, the first of equal values first, none when ncols <= 10), and the
+ * snpweightoutname file when a path is given: per SNP in use its ID, chromosome, physical
+ * position and weights.
+ */
+static int snp_weights_tail(const char *path, gp_run_result *r, const gp_snplist *snps,
+                            int64_t M, int hiprec)
+{
+  const int32_t K = r->numeigs, ncols = r->ncols;
+  double *f = r->ffvecs;
+  if (!f || K < 1) return 0;
+  for (int32_t j = 0; j < K; ++j) {
+    double *w = f + (size_t)j * M, y = 0.0;
+    for (int64_t s = 0; s < M; ++s)
+      if (r->snp_state[s] == 0) y += w[s] * w[s];
+    double ysc = (double)ncols / y;
+    ysc = sqrt(ysc);
+    for (int64_t s = 0; s < M; ++s)
+      if (r->snp_state[s] == 0) w[s] = w[s] * ysc;
+  }
+  double *sc = (double *)malloc(sizeof(double) * (size_t)(M > 0 ? M : 1));
+  if (!sc) return -1;
+  for (int32_t j = 0; j < K; ++j) {
+    const double *w = f + (size_t)j * M;
+    for (int64_t s = 0; s < M; ++s) sc[s] = r->snp_state[s] == 0 ? fabs(w[s]) : -99999.0;
+    for (int k = 0; k < 10; ++k) {
+      if (ncols <= 10) break;
+      int64_t best = -1;
+      for (int64_t s = 0; s < M; ++s)
+        if (r->snp_state[s] == 0 && (best < 0 || sc[s] > sc[best])) best = s;
+      if (best < 0 || sc[best] < 0) break;
+      const int64_t row = snps->order[best];
+      printf("eigbestsnp %4d %20s %2d %12d %9.3f\n", j + 1, snps->id[row], snps->chrom[row],
+             (int)lrint(snps->ppos[row]), sc[best]);
+      sc[best] = -1.0;
+    }
+  }
+  free(sc);
+  if (!path) return 0;
+  FILE *fo = fopen(path, "w");
+  if (!fo) {
+    fprintf(stderr, "cannot write %s\n", path);
+    return -1;
+  }
+  for (int64_t s = 0; s < M; ++s) {
+    if (r->snp_state[s] != 0) continue;
+    const int64_t row = snps->order[s];
+    fprintf(fo, "%20s", snps->id[row]);
+    fprintf(fo, " %2d", snps->chrom[row]);
+    fprintf(fo, " %12d", (int)lrint(snps->ppos[row]));
+    for (int32_t j = 0; j < K; ++j) {
+      if (hiprec) fprintf(fo, " %12.6f", f[(size_t)j * M + s]);
+      else fprintf(fo, " %9.3f", f[(size_t)j * M + s]);
+    }
+    fprintf(fo, "\n");
+  }
+  fclose(fo);
+  return 0;
+}
+
 int main(int argc, char **argv)
 {
   const char *parname = NULL;
@@ -450,7 +513,7 @@ int main(int argc, char **argv)
   gp_smartpca_defaults(&o);
   const char *genotypename = NULL, *snpname = NULL, *indivname = NULL, *evecout = NULL,
              *evalout = NULL, *outlierout = NULL, *poplistname = NULL, *prec = NULL,
-             *grmout = NULL;
+             *grmout = NULL, *snpwtout = NULL;
   int32_t hiprec = 0, familynames = 1, hashcheck = 1, t = 0, xdata = -1, seed = 0,
           grmbinary = 0;
   gp_par_str(&pf, "genotypename:", &genotypename);
@@ -466,6 +529,8 @@ int main(int argc, char **argv)
   gp_par_str(&pf, "outlieroutname:", &outlierout);
   gp_par_str(&pf, "gpuprecision:", &prec);
   gp_par_str(&pf, "grmoutname:", &grmout);
+  gp_par_str(&pf, "snpeigname:", &snpwtout);
+  gp_par_str(&pf, "snpweightoutname:", &snpwtout);
   gp_par_int(&pf, "grmbinary:", &grmbinary);
   gp_par_int(&pf, "numeigs:", &o.numeigs);
   gp_par_int(&pf, "numoutevec:", &o.numeigs);
@@ -632,6 +697,18 @@ int main(int argc, char **argv)
   r.outlier_iter = (int32_t *)calloc((size_t)N, sizeof(int32_t));
   r.outlier_vec = (int32_t *)calloc((size_t)N, sizeof(int32_t));
   r.outlier_score = (double *)calloc((size_t)N, sizeof(double));
+  if (snpwtout && o.fastmode) {
+    fprintf(stderr, "snpweightoutname with fastmode is not supported by this path\n");
+    return 1;
+  }
+  if (!o.fastmode) {
+    /* the last pass's SNP weights: the eigbestsnp lines and snpweightoutname */
+    r.ffvecs = (double *)calloc((size_t)K * (size_t)M, sizeof(double));
+    if (!r.ffvecs) {
+      fprintf(stderr, "no memory for the SNP weights (%lld SNPs)\n", (long long)M);
+      return 1;
+    }
+  }
   if (grmout && !o.fastmode) {
     r.xtx = (double *)malloc(sizeof(double) * (size_t)N * N);
     if (!r.xtx) {
@@ -710,6 +787,10 @@ int main(int argc, char **argv)
     rc = fst_tail(ctx, &pf, &snps, &inds, &r, poplistname, M, N);
     if (rc) {
       fprintf(stderr, "fatalx:\n%s (code %d)\n", gp_last_error(ctx), rc);
+      gp_close(ctx);
+      return 1;
+    }
+    if (snp_weights_tail(snpwtout, &r, &snps, M, hiprec)) {
       gp_close(ctx);
       return 1;
     }

@@ -87,7 +87,8 @@ class RunResult(C.Structure):
                 ("nrows", C.c_int32), ("ncols", C.c_int32), ("numeigs", C.c_int32),
                 ("noutliers", C.c_int32), ("npasses", C.c_int32),
                 ("t_phase", C.c_double * 8), ("gram_flops", C.c_double),
-                ("gram_ms", C.c_double), ("xtx", f64p), ("nused", C.c_int32)]
+                ("gram_ms", C.c_double), ("xtx", f64p), ("nused", C.c_int32),
+                ("ffvecs", f64p)]
 
 
 _lib = None
@@ -630,7 +631,7 @@ class _RunArgs:
 
     def __init__(self, records, nind, opts, code=GP_CODE_PACKED, snp_chrom=None,
                  snp_ignore=None, ind_ignore=None, ind_affstatus=None, ind_male=None,
-                 want_xtx=False, ind_pop=None):
+                 want_xtx=False, ind_pop=None, want_ffvecs=False):
         self.keep = []
         if isinstance(records, tuple):  # (nsnp, record_bytes): the panel resident on the handle
             rec = None
@@ -669,6 +670,10 @@ class _RunArgs:
         if want_xtx:
             out["xtx"] = np.zeros(nind * nind)
             r.xtx = ptr(out["xtx"], C.c_double)
+        if want_ffvecs:
+            out["ffvecs"] = np.zeros(K * nsnp)
+            r.ffvecs = ptr(out["ffvecs"], C.c_double)
+        self.nsnp = nsnp
         self.out, self.result = out, r
 
     def collect(self):
@@ -687,16 +692,19 @@ class _RunArgs:
                    gram_flops=r.gram_flops, gram_ms=r.gram_ms, nused=r.nused)
         if self.want_xtx:
             res["xtx"] = out["xtx"][: n * n].reshape(n, n).copy()
+        if "ffvecs" in out:
+            res["ffvecs"] = out["ffvecs"][: k * self.nsnp].reshape(k, self.nsnp).copy()
         return res
 
 
 def smartpca_run(handle, records, nind, opts, code=GP_CODE_PACKED, snp_chrom=None,
                  snp_ignore=None, ind_ignore=None, ind_affstatus=None, ind_male=None,
-                 want_xtx=False, ind_pop=None):
+                 want_xtx=False, ind_pop=None, want_ffvecs=False):
     """Run the whole smartpca hot path (gp_smartpca_run) on in-memory records.  ind_pop
-    (the samples' population indices) is read with opts.usepopsformissing."""
+    (the samples' population indices) is read with opts.usepopsformissing; want_ffvecs
+    returns the last pass's SNP weights (K x nsnp, 0 for SNPs it did not use)."""
     a = _RunArgs(records, nind, opts, code, snp_chrom, snp_ignore, ind_ignore, ind_affstatus,
-                 ind_male, want_xtx, ind_pop)
+                 ind_male, want_xtx, ind_pop, want_ffvecs)
     handle.check(handle.lib.gp_smartpca_run(handle.h, C.byref(opts), C.byref(a.panel),
                                             C.byref(a.result)), "gp_smartpca_run")
     return a.collect()

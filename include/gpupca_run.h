@@ -89,6 +89,10 @@ typedef struct {
   double *xtx;             /* [nind*nind] or NULL: the last pass's unscaled XTX, nrows x nrows
                               row-major in xindex order (for the GRM dump, smartpca.c:1297) */
   int32_t nused;           /* SNPs in the last pass's Gram (ynumsnps, smartpca.c:1172-1181) */
+  double *ffvecs;          /* [numeigs*nsnp] or NULL: the SNP weights of the last pass
+                              (ffvecs, smartpca.c:1485-1493), weight j of SNP s (sorted order)
+                              at j*nsnp + s, 0 for a SNP the last pass did not use; the
+                              writesnpeigs normalisation (:3047-3053) is the caller's */
 } gp_run_result;
 
 void gp_smartpca_defaults(gp_smartpca_opts *o);

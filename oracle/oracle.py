@@ -317,6 +317,7 @@ def smartpca(records, nind, numeigs=10, numoutliter=5, numoutleigs=10, outlthres
     K = min(numeigs, n, len(cols))
     coords = np.zeros((K, nind))
     out = ~ind_ign
+    ff = np.zeros((0, len(cols)))
     if K > 0:
         ff, fx, fxscal = weights(s, evecs, K)
         if lsqproject:
@@ -345,7 +346,34 @@ def smartpca(records, nind, numeigs=10, numoutliter=5, numoutleigs=10, outlthres
         out = ~ind_ign
     return dict(evals=evals, evecs=evecs[:K], xindex=xindex, coords=coords, ind_out=out,
                 outliers=outliers, ncols=len(cols), nrows=n, numeigs=K, snp_state=snp_ign,
-                xtx=X, nused=int((s.killed == 0).sum()))
+                xtx=X, nused=int((s.killed == 0).sum()), ffvecs=ff, cols=cols,
+                killed=s.killed.copy())
+
+
+def snpeigs(ffvecs, killed):
+    """writesnpeigs (src/eigensrc/smartpca.c:3038-3081): each weight vector scaled to mean
+    square 1 over the last pass's columns (sequential sum of squares), and per vector the 10
+    columns of largest |weight| among the kept ones (first of equal values first; none when
+    there are at most 10 columns).  Returns (scaled weights, [(vector, column, |w|)])."""
+    ff = np.array(ffvecs, dtype=np.float64, copy=True)
+    K, nc = ff.shape
+    for j in range(K):
+        y = 0.0
+        for v in ff[j]:
+            y += v * v
+        ff[j] = ff[j] * np.sqrt(nc / y)
+    best = []
+    for j in range(K):
+        sc = np.where(np.asarray(killed) == 1, -99999.0, np.abs(ff[j]))
+        for _ in range(10):
+            if nc <= 10:
+                break
+            k = int(np.argmax(sc))  # first index of the maximum
+            if sc[k] < 0:
+                break
+            best.append((j, k, float(sc[k])))
+            sc[k] = -1.0
+    return ff, best
 
 
 def grm(X):

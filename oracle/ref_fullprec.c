@@ -3,9 +3,9 @@
  * unchanged.  With EIG_REF_FULLPREC=1 the number formats of the .eval file
  * (src/eigensrc/smartpca.c:1428 "%12.6f\n"), the .evec header (:1435 "%9.3f ") and the
  * .evec coordinates (:1584-1585 "%10.4f  " / "%12.6f  ") and the GRM text values
- * (:3803 "%0.6f\n") and the fstdetails values (:1897 "F_st ... %12.6f %12.6f %12.6f") are
- * printed as %.17g, so that the reference's own results can be
- * compared at 1e-10 instead of at 6 printed decimals.  The smartrel binary is also linked
+ * (:3803 "%0.6f\n"), the fstdetails values (:1897 "F_st ... %12.6f %12.6f %12.6f") and the
+ * hiprecision SNP weights (:3096 " %12.6f") are printed as %.17g, so that the reference's
+ * own results can be compared at 1e-10 instead of at 6 printed decimals.  The smartrel binary is also linked
  * with -Wl,--wrap=printf: its relatedness score (src/eigensrc/smartrel.c:614 " %9.3f")
  * prints as %.17g in the same mode. */
 #include <stdarg.h>
@@ -37,6 +37,8 @@ int __wrap_fprintf(FILE *f, const char *fmt, ...)
       use = "%.17g ";
     else if (strcmp(fmt, "F_st %20s %20s %12.6f %12.6f %12.6f") == 0)
       use = "F_st %20s %20s %.17g %.17g %.17g";
+    else if (strcmp(fmt, " %12.6f") == 0)
+      use = " %.17g";
   }
   va_start(ap, fmt);
   r = vfprintf(f, use, ap);

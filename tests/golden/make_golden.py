@@ -13,6 +13,7 @@ EIG_REF_FULLPREC=1 prints .eval/.evec numbers as %.17g).  Writes, per case:
   <case>/ref.grm[.txt], ref.grm.id, ref.grm.bin, ref.grm.N.bin   GRM dumps (grm cases)
   <case>/ref.fstdetails[.txt], ref.mega   Fst files (bn_fst; ref_par_pl.log, ref.phylip and
                                           ref_pl.fstdetails from its second parfile par_pl)
+  <case>/ref.snpwt[.txt]                  the snpweightoutname file (cases that set it)
   <case>/ref.rel, ref.rel.txt             smartrel "rel:" lines (tool == "smartrel": the case
                                           runs oracle/_ref/smartrel; relatives are planted by
                                           copying a share of one sample's genotypes to another)
@@ -92,6 +93,12 @@ CASES = {
     "bn_usepops": dict(nsnp=3000, pops=[60, 60, 50, 2, 2], fst=[0.01, 0.02, 0.03, 0.25, 0.25],
                        miss=0.0, miss_hi=0.5, seed=19, fmt="packed",
                        par={"numoutevec": "4", "usepopsformissing": "YES", "maxmissing": "1"}),
+    # snpweightoutname: the SNP weights file (writesnpeigs) of a run on two chromosomes with
+    # outlier removal and a maxmissing filter, hiprecision (weights at 6 decimals)
+    "bn_snpwt": dict(nsnp=2500, pops=[60, 60, 50, 2], fst=[0.01, 0.02, 0.03, 0.3], miss=0.02,
+                     seed=21, fmt="packed", relocate=(2, 4e-4),
+                     par={"numoutevec": "3", "snpweightoutname": "out.snpwt",
+                          "hiprecision": "YES", "maxmissing": "6"}),
     # the same option with a poplist (POP1, POP2): the other samples are projected, and
     # lsqproj reads each sample's population at its .ind index among the row-indexed xtypes
     "bn_usepops_pl": dict(nsnp=3000, pops=[60, 60, 50, 2, 2], fst=[0.01, 0.02, 0.03, 0.25, 0.25],
@@ -225,7 +232,9 @@ def make_case(name, spec):
     if spec.get("tool") == "smartrel":
         run_smartrel(d)
         return
-    run_reference(d, spec.get("grm", False), extra=("fstdetails",) if "fstdetailsname" in par else ())
+    extra = (("fstdetails",) if "fstdetailsname" in par else ()) + \
+        (("snpwt",) if "snpweightoutname" in par else ())
+    run_reference(d, spec.get("grm", False), extra=extra)
     for rname, extra_par in spec.get("runs2", {}).items():
         with open(os.path.join(d, rname), "w") as f:
             for k, v in par.items():

@@ -5,7 +5,7 @@ import numpy as np
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 CASES = ["bn_outliers", "bn_bed_altnorm", "bn_project", "bn_grm", "bn_missingmode",
-         "bn_usepops", "bn_usepops_pl"]
+         "bn_usepops", "bn_usepops_pl", "bn_snpwt"]
 REL_CASES = ["bn_rel"]
 
 
@@ -317,3 +317,30 @@ class FastCase:
         V = np.array([[float(x) for x in l.split()[1:-1]] for l in lines[1:]]).T
         return dict(K=K, L=L, I=I, seed=seed, evals=ev, evecs=V,
                     text=open(os.path.join(self.dir, "ref%s.evec.txt" % tag)).read().splitlines())
+
+
+def snp_rows(case):
+    """(ID, chrom, physpos) of each SNP of a case, in file order (the records' order)"""
+    c = Case(case)
+    path = os.path.join(c.dir, c.par["snpname"])
+    rows = []
+    for l in open(path):
+        t = l.split()
+        if not t:
+            continue
+        if path.endswith(".bim"):
+            rows.append((t[1], int(t[0]), int(round(float(t[3])))))
+        else:
+            rows.append((t[0], int(t[1]), int(round(float(t[3])))))
+    return rows
+
+
+def eigbestsnp_lines(text):
+    """the "eigbestsnp" log lines as (vector, ID, chrom, physpos, value)"""
+    out = []
+    for l in text.splitlines():
+        if l.startswith("eigbestsnp"):
+            t = l.split()
+            out.append((int(t[1]), t[2], int(t[3]), int(t[4]), float(t[5])))
+    return out
+

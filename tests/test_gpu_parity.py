@@ -196,6 +196,21 @@ def test_cli_dropin_matches_reference_text(case, tmp_path):
     for g, x in zip(got, exp):
         assert g[:8] == x[:8] and g[9:] == x[9:]
         assert g[8].lstrip("-") == x[8].lstrip("-")
+    # writesnpeigs: the eigbestsnp log lines, and the snpweightoutname file when the parfile
+    # names one (weights up to each vector's sign, at the printed precision)
+    from tests.goldens import eigbestsnp_lines
+    mine_b = eigbestsnp_lines(out.stdout)
+    want_b = eigbestsnp_lines(open(d / "ref.log").read())
+    assert [m[:4] for m in mine_b] == [w[:4] for w in want_b]
+    assert all(abs(m[4] - w[4]) <= 1.01e-3 for m, w in zip(mine_b, want_b))
+    if "snpweightoutname" in c.par:
+        mw = [l.split() for l in open(d / "out.snpwt").read().splitlines()]
+        ww = [l.split() for l in open(d / "ref.snpwt.txt").read().splitlines()]
+        assert [l[:3] for l in mw] == [l[:3] for l in ww]
+        A = np.array([[float(x) for x in l[3:]] for l in ww])
+        B = np.array([[float(x) for x in l[3:]] for l in mw])
+        sg = np.sign(np.sum(A * B, axis=0))
+        assert np.max(np.abs(A - B * sg)) <= 1.01e-6
 
 
 @pytest.mark.parametrize("binary", [False, True])

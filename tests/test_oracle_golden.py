@@ -5,7 +5,8 @@ import numpy as np
 import pytest
 
 from oracle import oracle as O
-from tests.goldens import CASES, GOLDEN, REL_CASES, Case, compare_coords, coords_by_id
+from tests.goldens import (CASES, GOLDEN, REL_CASES, Case, compare_coords, coords_by_id,
+                           eigbestsnp_lines, snp_rows)
 
 EX = os.path.join(GOLDEN, "ref_examples")
 
@@ -199,3 +200,27 @@ def test_oracle_fastmode_matches_reference(par):
     Vn = V / np.linalg.norm(V, axis=1, keepdims=True)
     cos = np.abs(np.sum(Vn * r["evecs"], axis=1)) / np.linalg.norm(r["evecs"], axis=1)
     assert np.all(cos > 1 - 1e-12)
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_oracle_snp_weights_match_reference(case):
+    """writesnpeigs: the scaled weights' best SNPs of every case (the log's eigbestsnp lines)
+    and, for bn_snpwt, the snpweightoutname file at full precision"""
+    c = Case(case)
+    r = O.smartpca(c.packed_records(), c.nind, ind_affstatus=c.affstatus, ind_pop=c.ind_pop,
+                   **c.opts())
+    ff, best = O.snpeigs(r["ffvecs"], r["killed"])
+    rows = snp_rows(case)
+    want = eigbestsnp_lines(open(os.path.join(c.dir, "ref.log")).read())
+    got = [(j + 1,) + rows[r["cols"][k]] + (v,) for j, k, v in best]
+    assert [g[:4] for g in got] == [w[:4] for w in want]
+    assert max(abs(g[4] - w[4]) for g, w in zip(got, want)) <= 5.0001e-4
+    if "snpweightoutname" in c.par:
+        lines = [l.split() for l in open(os.path.join(c.dir, "ref.snpwt")) if l.strip()]
+        kept = [k for k in range(len(r["cols"])) if not r["killed"][k]]
+        assert [l[0] for l in lines] == [rows[r["cols"][k]][0] for k in kept]
+        ref = np.array([[float(x) for x in l[3:]] for l in lines])
+        mine = ff[:, kept].T
+        sgn = np.sign(np.sum(ref * mine, axis=0))  # the eigenvectors' signs are arbitrary
+        assert np.max(np.abs(ref - mine * sgn)) <= 1e-9 * np.max(np.abs(ref))
+

@@ -353,6 +353,10 @@ int gp_smartpca_run(gp_ctx *ctx, const gp_smartpca_opts *o, const gp_panel *p,
   r->numeigs = K;
   memcpy(r->evecs, evecs, sizeof(double) * (size_t)K * nrows);
   for (int64_t s = 0; s < M; ++s) r->snp_state[s] = snp_ign[s];
+  if (r->snp_lastpass) {
+    memset(r->snp_lastpass, 0, (size_t)M);
+    for (int32_t c = 0; c < ncols; ++c) r->snp_lastpass[cols[c]] = 1;
+  }
   memset(r->ind_out, 0, (size_t)N);
   memset(r->coords, 0, sizeof(double) * (size_t)K * N);
   if (K <= 0) goto done;

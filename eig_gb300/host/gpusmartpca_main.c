@@ -425,6 +425,52 @@ static int in_list(const char *pop, char **list, int n)
   return 0;
 }
 
+/* kurtosis (src/admutils.c:995-1017): the mean fourth power of the standardised values,
+ * every sum in index order */
+static double kurtosis_of(const double *a, int64_t n)
+{
+  double y1 = 0.0, y2 = 0.0, y4 = 0.0;
+  for (int64_t i = 0; i < n; ++i) y1 += a[i];
+  y1 = y1 / (double)n;
+  for (int64_t i = 0; i < n; ++i) {
+    const double w = a[i] + -y1;
+    y2 += w * w;
+  }
+  y2 = y2 / (double)n;
+  const double sc = 1.0 / sqrt(y2);
+  for (int64_t i = 0; i < n; ++i) {
+    double w = (a[i] + -y1) * sc;
+    w = w * w;
+    y4 += w * w;
+  }
+  return y4 / (double)n;
+}
+
+/*
+ * The kurtosis lines of the log (smartpca.c:1496-1501, :1541-1546): per eigenvector the
+ * kurtosis of its SNP weights over the last pass's columns (zeros for the SNPs that pass
+ * dropped) and of 10 x its entries over the rows.
+ */
+static int kurtosis_lines(const gp_run_result *r, int64_t M)
+{
+  const int32_t K = r->numeigs, n = r->nrows, nc = r->ncols;
+  if (!r->ffvecs || !r->snp_lastpass || K < 1) return 0;
+  double *col = (double *)malloc(sizeof(double) * (size_t)(nc > n ? nc : n) + 8);
+  if (!col) return -1;
+  printf("%12s %4s %9s %9s\n", "kurtosis", "", "snps", "indivs");
+  for (int32_t j = 0; j < K; ++j) {
+    int64_t m = 0;
+    for (int64_t s = 0; s < M; ++s)
+      if (r->snp_lastpass[s]) col[m++] = r->ffvecs[(size_t)j * M + s];
+    const double ks = kurtosis_of(col, m);
+    for (int32_t i = 0; i < n; ++i) col[i] = r->evecs[(size_t)j * n + i] * 10.0;
+    const double ki = kurtosis_of(col, n);
+    printf("%12s %4d %9.3f %9.3f\n", "eigenvector", j + 1, ks, ki);
+  }
+  free(col);
+  return 0;
+}
+
 /*
  * writesnpeigs (src/eigensrc/smartpca.c:3038-3106): each eigenvector's SNP weights scaled to
  * mean square 1 over the last pass's columns (sum of squares in column order, then
@@ -704,7 +750,8 @@ int main(int argc, char **argv)
   if (!o.fastmode) {
     /* the last pass's SNP weights: the eigbestsnp lines and snpweightoutname */
     r.ffvecs = (double *)calloc((size_t)K * (size_t)M, sizeof(double));
-    if (!r.ffvecs) {
+    r.snp_lastpass = (uint8_t *)calloc((size_t)M, 1);
+    if (!r.ffvecs || !r.snp_lastpass) {
       fprintf(stderr, "no memory for the SNP weights (%lld SNPs)\n", (long long)M);
       return 1;
     }
@@ -784,6 +831,10 @@ int main(int argc, char **argv)
   }
   if (ef != stdout) fclose(ef);
   if (!o.fastmode && nK > 0) {
+    if (kurtosis_lines(&r, M)) {
+      gp_close(ctx);
+      return 1;
+    }
     rc = fst_tail(ctx, &pf, &snps, &inds, &r, poplistname, M, N);
     if (rc) {
       fprintf(stderr, "fatalx:\n%s (code %d)\n", gp_last_error(ctx), rc);

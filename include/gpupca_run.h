@@ -93,6 +93,8 @@ typedef struct {
                               (ffvecs, smartpca.c:1485-1493), weight j of SNP s (sorted order)
                               at j*nsnp + s, 0 for a SNP the last pass did not use; the
                               writesnpeigs normalisation (:3047-3053) is the caller's */
+  uint8_t *snp_lastpass;   /* [nsnp] or NULL: 1 for the columns of the last pass (xsnplist,
+                              including SNPs its allele-count rule dropped), else 0 */
 } gp_run_result;
 
 void gp_smartpca_defaults(gp_smartpca_opts *o);

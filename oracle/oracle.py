@@ -634,3 +634,26 @@ def gsl_omega(seed, nrows, L):
         if L % 2:
             om[i, L - 1] = r.uniform_pos()
     return om
+
+
+def kurtosis(a):
+    """kurtosis (src/admutils.c:995-1017): mean fourth power of the standardised values,
+    sums in index order"""
+    a = np.asarray(a, dtype=np.float64)
+    n = len(a)
+    y1 = 0.0
+    for v in a:
+        y1 += v
+    y1 = y1 / n
+    w = a + (-y1)
+    y2 = 0.0
+    for v in w:
+        y2 += v * v
+    y2 = y2 / n
+    w = w * (1.0 / np.sqrt(y2))
+    w = w * w
+    y4 = 0.0
+    for v in w:
+        y4 += v * v
+    return y4 / n
+

@@ -344,3 +344,19 @@ def eigbestsnp_lines(text):
             out.append((int(t[1]), t[2], int(t[3]), int(t[4]), float(t[5])))
     return out
 
+
+def kurtosis_lines(text):
+    """the log's "eigenvector j kurt_snps kurt_indivs" lines after its kurtosis header"""
+    out, on = [], False
+    for l in text.splitlines():
+        t = l.split()
+        if t[:3] == ["kurtosis", "snps", "indivs"]:
+            on = True
+            continue
+        if on:
+            if len(t) == 4 and t[0] == "eigenvector":
+                out.append((int(t[1]), float(t[2]), float(t[3])))
+            else:
+                break
+    return out
+

@@ -198,7 +198,12 @@ def test_cli_dropin_matches_reference_text(case, tmp_path):
         assert g[8].lstrip("-") == x[8].lstrip("-")
     # writesnpeigs: the eigbestsnp log lines, and the snpweightoutname file when the parfile
     # names one (weights up to each vector's sign, at the printed precision)
-    from tests.goldens import eigbestsnp_lines
+    from tests.goldens import eigbestsnp_lines, kurtosis_lines
+    mine_k = kurtosis_lines(out.stdout)
+    want_k = kurtosis_lines(open(d / "ref.log").read())
+    assert [k[0] for k in mine_k] == [k[0] for k in want_k] and len(want_k) > 0
+    assert all(abs(a[1] - b[1]) <= 1.01e-3 and abs(a[2] - b[2]) <= 1.01e-3
+               for a, b in zip(mine_k, want_k))
     mine_b = eigbestsnp_lines(out.stdout)
     want_b = eigbestsnp_lines(open(d / "ref.log").read())
     assert [m[:4] for m in mine_b] == [w[:4] for w in want_b]

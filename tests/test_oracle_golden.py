@@ -6,7 +6,7 @@ import pytest
 
 from oracle import oracle as O
 from tests.goldens import (CASES, GOLDEN, REL_CASES, Case, compare_coords, coords_by_id,
-                           eigbestsnp_lines, snp_rows)
+                           eigbestsnp_lines, kurtosis_lines, snp_rows)
 
 EX = os.path.join(GOLDEN, "ref_examples")
 
@@ -223,4 +223,17 @@ def test_oracle_snp_weights_match_reference(case):
         mine = ff[:, kept].T
         sgn = np.sign(np.sum(ref * mine, axis=0))  # the eigenvectors' signs are arbitrary
         assert np.max(np.abs(ref - mine * sgn)) <= 1e-9 * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_oracle_kurtosis_lines_match_reference(case):
+    """the log's kurtosis of each eigenvector's SNP weights and of its sample entries"""
+    c = Case(case)
+    r = O.smartpca(c.packed_records(), c.nind, ind_affstatus=c.affstatus, ind_pop=c.ind_pop,
+                   **c.opts())
+    want = kurtosis_lines(open(os.path.join(c.dir, "ref.log")).read())
+    assert len(want) == r["numeigs"]
+    for j, ks, ki in want:
+        assert abs(O.kurtosis(r["ffvecs"][j - 1]) - ks) <= 5.0001e-4
+        assert abs(O.kurtosis(10.0 * r["evecs"][j - 1]) - ki) <= 5.0001e-4
 

@@ -190,7 +190,8 @@ extern "C" void gp_close(gp_ctx *ctx)
                   ctx->d_killed, ctx->d_vtab,    ctx->d_xmean,   ctx->d_xfancy,  ctx->d_kept,
                   ctx->d_xtx,    ctx->d_evals,   ctx->d_evecs,   ctx->d_ffvecs,  ctx->d_fxscal,
                   ctx->d_scratch, ctx->d_scratch2, ctx->d_scratch3, ctx->d_scratch4, ctx->d_scratch5,
-                  ctx->d_err,   ctx->d_xtx_keep, ctx->d_rowpop, ctx->d_gtab, ctx->d_gfill};
+                  ctx->d_err,   ctx->d_xtx_keep, ctx->d_rowpop, ctx->d_gtab, ctx->d_gfill,
+                  ctx->d_tri};
   for (size_t i = 0; i < sizeof(bufs) / sizeof(bufs[0]); ++i)
     if (bufs[i]) cudaFree(bufs[i]);
   if (ctx->solver) cusolverDnDestroy(ctx->solver);
@@ -220,7 +221,8 @@ extern "C" int gp_release(gp_ctx *ctx)
                    (void **)&ctx->d_evecs,   (void **)&ctx->d_ffvecs,   (void **)&ctx->d_fxscal,
                    (void **)&ctx->d_scratch, (void **)&ctx->d_scratch2, (void **)&ctx->d_scratch3,
                    (void **)&ctx->d_scratch4, (void **)&ctx->d_scratch5, (void **)&ctx->d_xtx_keep,
-                   (void **)&ctx->d_rowpop,  (void **)&ctx->d_gtab,     (void **)&ctx->d_gfill};
+                   (void **)&ctx->d_rowpop,  (void **)&ctx->d_gtab,     (void **)&ctx->d_gfill,
+                   (void **)&ctx->d_tri};
   for (size_t i = 0; i < sizeof(bufs) / sizeof(bufs[0]); ++i) {
     if (*bufs[i]) cudaFree(*bufs[i]);
     *bufs[i] = NULL;

@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 #include <cusolverDn.h>
 #include <float.h>
+#include <algorithm>
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -524,36 +525,41 @@ struct tr_step {
  * storage.  On exit the reflectors are FP64 again in A(c+2:n, c) and e on the subdiagonal, as
  * dormtr (lower) reads them; the upper triangle is left in float-float form.
  */
-__global__ void __launch_bounds__(TR_THREADS, 1)
-k_tridiag(double *A, int n, double *d, double *e, double *tau, double *vbuf, double *wbuf,
-          double *ybuf, double *part_dot2, unsigned *bar, int *err,
-          unsigned long long *phase_ns)
+/*
+ * Steps c_begin .. n-2 of the whole-matrix reduction (k_tridiag's step; the tail steps of
+ * k_tridiag_tiled): A holds the trailing matrix (indices >= c_begin) as float-float pairs in
+ * whole columns, both triangles.  svp/swp/svc: the block's vectors in shared memory (at least
+ * n pairs each).  tau_pf, scale_pf, e_pf, have_p and target carry the previous step's state.
+ * dot0 (when not NULL) holds the previous step's y.v parts at [dot0_k0, dot0_k1) instead of
+ * part_dot2 (the step before c_begin was a tiled one).  sph (block 0, thread 0 only; else
+ * NULL): phase times as in k_tridiag, sph[5] the last time stamp.  False when the grid
+ * barrier failed.
+ */
+__device__ __forceinline__ bool tr_full_steps(double *A, int n, int c_begin, double *d, double *e,
+                                              double *tau, double *vbuf, double *wbuf,
+                                              double *ybuf, double *part_dot2, unsigned *count,
+                                              unsigned &target, int *err, double *svp,
+                                              double *swp, double *svc, ff2 &tau_pf,
+                                              ff2 &scale_pf, ff2 &e_pf, bool &have_p,
+                                              const double *dot0, int dot0_k0, int dot0_k1,
+                                              unsigned long long *sph)
 {
-  extern __shared__ double sh[];
-  double *svp = sh, *swp = sh + n, *svc = sh + 2 * n; /* float-float pairs */
   __shared__ ff2 red[TR_WARPS];
   __shared__ ff2 sdotp[TR_B1_SLOTS];
   __shared__ tr_step st;
+  __shared__ ff2 s_slotf;
   const int G = gridDim.x, b = blockIdx.x;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const ff2 ONE = ff_make(1.f, 0.f), ZERO = ff_make(0.f, 0.f);
-  unsigned *count = bar;
-  unsigned target = 0;
-  ff2 tau_pf = ZERO, scale_pf = ZERO, e_pf = ZERO;
-  __shared__ ff2 s_slotf;
-  bool have_p = false;
-  /* phase_ns (optional, block 0): time in A, B (entry 1; entry 2 for the first 30% of the
-   * steps) and the barrier (entry 4) */
-  const bool stamp = phase_ns != NULL && b == 0 && threadIdx.x == 0;
-  unsigned long long t_prev = stamp ? globaltimer_ns() : 0ull, ph[5] = {0, 0, 0, 0, 0};
-#define TR_STAMP(i)                                  \
-  if (stamp) {                                       \
+  const bool stamp = sph != NULL;
+#define TR_STAMP(i)                                    \
+  if (stamp) {                                         \
     const unsigned long long t_now = globaltimer_ns(); \
-    ph[i] += t_now - t_prev;                         \
-    t_prev = t_now;                                  \
+    sph[i] += t_now - sph[5];                          \
+    sph[5] = t_now;                                    \
   }
   const int early = (int)((3LL * n) / 10);
-  for (int c = 0; c < n - 1; ++c) {
+  for (int c = c_begin; c < n - 1; ++c) {
     /* ---- A (every block, no grid barrier): v and w of step c-1, the pending update of
      * column c and its norm, rebuilt from y, the stored x of step c-1 and column c; each
      * block also writes its share of the reflector storage and of x_c (double buffer) ---- */
@@ -569,8 +575,14 @@ k_tridiag(double *A, int n, double *d, double *e, double *tau, double *vbuf, dou
     ff2 pacc = ZERO;
     if (have_p && warp == TR_WARPS - 1) {
       const double *pprev = part_dot2 + (size_t)((c + 1) & 1) * G;
+      int g0 = 0, g1 = G;
+      if (c == c_begin && dot0 != NULL) { /* the previous step was a tiled one */
+        pprev = dot0;
+        g0 = dot0_k0;
+        g1 = dot0_k1;
+      }
 #pragma unroll 4
-      for (int g = lane; g < G; g += 32) pacc = ff_add(pacc, ff_load(pprev + g));
+      for (int g = g0 + lane; g < g1; g += 32) pacc = ff_add(pacc, ff_load(pprev + g));
     }
     /* loads (v_p needs only step c-1's scale; y is kept raw in swp for now) */
 #pragma unroll 4
@@ -717,22 +729,580 @@ k_tridiag(double *A, int n, double *d, double *e, double *tau, double *vbuf, dou
     }
     TR_STAMP(c < early ? 2 : 1)
     target += G;
-    if (!tr_grid_sync(count, target, err)) return;
+    if (!tr_grid_sync(count, target, err)) return false;
     TR_STAMP(4)
     tau_pf = tau_c;
     scale_pf = scale_cf;
     e_pf = beta;
     have_p = true;
   }
-  if (stamp)
-    for (int i = 0; i < 5; ++i) phase_ns[i] = ph[i];
 #undef TR_STAMP
-  /* last diagonal entry and the storage of the last reflector */
+  return true;
+}
+
+/* the last diagonal entry and the storage of the last reflector after the whole-matrix steps
+ * (block 0) */
+__device__ __forceinline__ void tr_full_last(double *A, int n, double *d, double *ybuf,
+                                             double *part_dot2, ff2 tau_pf, ff2 e_pf,
+                                             bool have_p)
+{
+  __shared__ ff2 s_slotf;
+  const int G = gridDim.x, b = blockIdx.x;
+  const ff2 ZERO = ff_make(0.f, 0.f);
   if (b == 0) {
     ff2 dsum = ZERO;
     if (have_p) dsum = ff_sum_partials(part_dot2 + (size_t)((n - 2) & 1) * G, G, &s_slotf);
     if (threadIdx.x == 0) {
       ff2 a = ff_load(A + (int64_t)(n - 1) * n + n - 1);
+      if (have_p) {
+        const ff2 alpha_p = ff_scale(ff_mul(ff_mul(tau_pf, tau_pf), dsum), -0.5f);
+        const ff2 wp =
+            ff_fma(tau_pf, ff_load(ybuf + (int64_t)((n - 2) & 1) * n + n - 1), alpha_p);
+        a = ff_add(a, ff_neg(wp));
+        a = ff_add(a, ff_neg(wp));
+        A[(int64_t)(n - 2) * n + n - 1] = ff_to_double(e_pf);
+      }
+      d[n - 1] = ff_to_double(a);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(TR_THREADS, 1)
+k_tridiag(double *A, int n, double *d, double *e, double *tau, double *vbuf, double *wbuf,
+          double *ybuf, double *part_dot2, unsigned *bar, int *err,
+          unsigned long long *phase_ns)
+{
+  extern __shared__ double sh[];
+  const ff2 ZERO = ff_make(0.f, 0.f);
+  unsigned target = 0;
+  ff2 tau_pf = ZERO, scale_pf = ZERO, e_pf = ZERO;
+  bool have_p = false;
+  /* phase_ns (optional, block 0): time in A, B (entry 1; entry 2 for the first 30% of the
+   * steps) and the barrier (entry 4) */
+  __shared__ unsigned long long s_ph[6];
+  const bool stamp = phase_ns != NULL && blockIdx.x == 0 && threadIdx.x == 0;
+  if (stamp) {
+    for (int i = 0; i < 5; ++i) s_ph[i] = 0ull;
+    s_ph[5] = globaltimer_ns();
+  }
+  if (!tr_full_steps(A, n, 0, d, e, tau, vbuf, wbuf, ybuf, part_dot2, bar, target, err, sh,
+                     sh + n, sh + 2 * n, tau_pf, scale_pf, e_pf, have_p, NULL, 0, 0,
+                     stamp ? s_ph : NULL))
+    return;
+  if (stamp)
+    for (int i = 0; i < 5; ++i) phase_ns[i] = s_ph[i];
+  tr_full_last(A, n, d, ybuf, part_dot2, tau_pf, e_pf, have_p);
+}
+
+/* ---------------------------------------------------------------------------------- */
+/*
+ * The same reduction (dsytd2, lower) with the trailing matrix held as its lower triangle only,
+ * in TT x TT tiles: half the bytes per column step and two thirds of the float-float work of
+ * k_tridiag, whose whole-column product needs both triangles.  Tile (I, J), I >= J, of the
+ * lower triangle is TT*TT float-float pairs at Tm + tt_tile(I, J)*TT*TT, column-major inside
+ * the tile (element (i, j) at j*TT + i); diagonal tiles are held in full; rows and columns
+ * beyond n are zero padding.
+ *
+ * Per column step the product y = A'v needs, for index block K, the row parts of the tiles in
+ * tile row K (A(K, J) v(J), the diagonal tile included) and the column parts of the tiles in
+ * tile column K below the diagonal (A(I, K)^T v(I)).  The blocks form a pr x pc grid: block
+ * (a, b) owns the tiles (I, J) with rg(I) = a and cg(J) = b, where rg assigns the active tile
+ * rows to the pr row groups longest first to the group with the least work (cg the same for
+ * the columns over pc groups; recomputed each time the first active tile index J0 moves).  So
+ * index block K has pc row-part contributors (blocks (rg(K), *)) and pr column-part ones
+ * (blocks (*, cg(K))).  Per step:
+ *   A   as in k_tridiag (every block: v and w of step c-1, the pending update of column c read
+ *       from the tiles, its norm, the reflector; y.v from the index blocks' partial dots)
+ *   B   each warp takes halves (32 columns) of the block's tiles: the pending rank-2 update of
+ *       step c-1 (written back), the row dots (two rows per lane) and, off the diagonal, the
+ *       column dots (a reduce-scatter over the warp per 4 columns); the block sums its halves'
+ *       parts per index block in a fixed order and publishes one row part per tile row and one
+ *       column part per tile column it owns; each publication is an arrival on the index
+ *       block's counter (release/acquire), and the block whose arrival completes an index
+ *       block sums its pr + pc parts in a fixed order into y and its partial y.v
+ *   --- grid barrier
+ * Rows and columns up to c keep their values (the pending-update vectors and v are zero there),
+ * so that phase A of a block that is still reading column c never sees it change.  Sums have
+ * a fixed order: the result does not depend on which block completes an index block.
+ */
+#define TT 64
+#define TT_R 64     /* tile halves per round (two per warp) */
+#define TT_MAXG 32  /* row or column groups at most */
+#define TR_ERR_LISTS 12
+
+__host__ __device__ __forceinline__ int64_t tt_tile(int I, int J)
+{
+  return (int64_t)I * (I + 1) / 2 + J;
+}
+
+/* longest-first assignment of the active tile rows (I - J0 + 1 tiles each) to pr groups and of
+ * the active tile columns (nt - J tiles each) to pc groups, each to the group with the least
+ * work so far (ties: the lowest group) */
+__host__ __device__ inline void tt_assign(int nt, int J0, int pr, int pc, unsigned char *rg,
+                                          unsigned char *cg)
+{
+  int sum[TT_MAXG];
+  for (int g = 0; g < pr; ++g) sum[g] = 0;
+  for (int I = nt - 1; I >= J0; --I) {
+    int best = 0;
+    for (int g = 1; g < pr; ++g)
+      if (sum[g] < sum[best]) best = g;
+    rg[I] = (unsigned char)best;
+    sum[best] += I - J0 + 1;
+  }
+  for (int g = 0; g < pc; ++g) sum[g] = 0;
+  for (int J = J0; J < nt; ++J) {
+    int best = 0;
+    for (int g = 1; g < pc; ++g)
+      if (sum[g] < sum[best]) best = g;
+    cg[J] = (unsigned char)best;
+    sum[best] += nt - J;
+  }
+}
+
+__device__ __forceinline__ unsigned atom_add_acq_rel_gpu(unsigned *p, unsigned v)
+{
+  unsigned old;
+  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;"
+               : "=r"(old)
+               : "l"(p), "r"(v)
+               : "memory");
+  return old;
+}
+
+/* the lower triangle of the symmetric FP64 matrix A (column-major, both triangles valid) into
+ * float-float tiles, padding zero */
+__global__ void k_tri_to_tiles(const double *A, int n, int nt, double *Tm)
+{
+  const int64_t ntiles = (int64_t)nt * (nt + 1) / 2;
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    int I = (int)((sqrtf(8.f * (float)t + 1.f) - 1.f) * 0.5f);
+    while ((int64_t)(I + 1) * (I + 2) / 2 <= t) ++I;
+    while ((int64_t)I * (I + 1) / 2 > t) --I;
+    const int J = (int)(t - (int64_t)I * (I + 1) / 2);
+    double *tile = Tm + t * (TT * TT);
+    for (int idx = threadIdx.x; idx < TT * TT; idx += blockDim.x) {
+      const int j = idx / TT, i = idx - j * TT;
+      const int r = I * TT + i, q = J * TT + j;
+      const double v = (r < n && q < n) ? A[(int64_t)q * n + r] : 0.0;
+      ff_store(tile + idx, ff_from_double(v));
+    }
+  }
+}
+
+/* one half (32 columns from TT*J + 32h) of tile (I, J) by one warp: the pending update of step
+ * c-1 (have_p), written back; the row dots with v over these columns into rs[TT] (rows 2 lane,
+ * 2 lane + 1); unless the tile is diagonal, the column dots with v over the tile's rows into
+ * cs[32] */
+__device__ __forceinline__ void tt_half(double *tile, int I, int J, int h, bool diag, bool have_p,
+                                        const double *svp, const double *swp, const double *svc,
+                                        double *rs, double *cs, int lane)
+{
+  const ff2 ZERO = ff_make(0.f, 0.f);
+  const int r = I * TT + 2 * lane;
+  const ff2 vr0 = ff_load(svc + r), vr1 = ff_load(svc + r + 1);
+  const ff2 pr0 = ff_load(svp + r), pr1 = ff_load(svp + r + 1);
+  const ff2 qr0 = ff_load(swp + r), qr1 = ff_load(swp + r + 1);
+  ff2 ra0 = ZERO, ra1 = ZERO;
+  const int j0 = h * (TT / 2);
+  const int col0 = J * TT + j0;
+  double *p0 = tile + (size_t)j0 * TT + 2 * lane;
+  for (int cb = 0; cb < TT / 2; cb += 4) {
+    float4 a[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) a[k] = *reinterpret_cast<const float4 *>(p0 + (size_t)(cb + k) * TT);
+    ff2 cp[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int col = col0 + cb + k;
+      ff2 a0 = ff_make(a[k].x, a[k].y), a1 = ff_make(a[k].z, a[k].w);
+      if (have_p) {
+        const ff2 nvc = ff_neg(ff_load(svp + col)), nwc = ff_neg(ff_load(swp + col));
+        a0 = ff_fma(pr0, nwc, a0);
+        a0 = ff_fma(qr0, nvc, a0);
+        a1 = ff_fma(pr1, nwc, a1);
+        a1 = ff_fma(qr1, nvc, a1);
+        *reinterpret_cast<float4 *>(p0 + (size_t)(cb + k) * TT) = make_float4(a0.h, a0.l, a1.h, a1.l);
+      }
+      const ff2 vc = ff_load(svc + col);
+      ra0 = ff_fma(a0, vc, ra0);
+      ra1 = ff_fma(a1, vc, ra1);
+      cp[k] = ff_fma(a1, vr1, ff_mul(a0, vr0));
+    }
+    if (!diag) {
+      /* reduce-scatter over the warp: lanes 8t..8t+7 end with column cb + t (lane bits 4 and 3
+       * pick the column, bits 2..0 are summed) */
+      const bool b4 = (lane & 16) != 0, b3 = (lane & 8) != 0;
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        const ff2 send = b4 ? cp[k] : cp[k + 2];
+        const ff2 keep = b4 ? cp[k + 2] : cp[k];
+        cp[k] = ff_add(keep, ff_shfl_xor(send, 16));
+      }
+      {
+        const ff2 send = b3 ? cp[0] : cp[1];
+        const ff2 keep = b3 ? cp[1] : cp[0];
+        cp[0] = ff_add(keep, ff_shfl_xor(send, 8));
+      }
+      cp[0] = ff_add(cp[0], ff_shfl_xor(cp[0], 4));
+      cp[0] = ff_add(cp[0], ff_shfl_xor(cp[0], 2));
+      cp[0] = ff_add(cp[0], ff_shfl_xor(cp[0], 1));
+      if ((lane & 7) == 0) ff_store(cs + cb + (lane >> 3), cp[0]);
+    }
+  }
+  ff_store(rs + 2 * lane, ra0);
+  ff_store(rs + 2 * lane + 1, ra1);
+}
+
+/* shared-memory bytes of k_tridiag_tiled (the host sizes the launch with the same layout) */
+__host__ __device__ inline size_t tt_smem_bytes(int nt, int maxr, int maxc, int maxi)
+{
+  const size_t npad = (size_t)nt * TT;
+  size_t dbl = 3 * npad + (size_t)TT_R * TT + (size_t)TT_R * (TT / 2) +
+               (size_t)(maxr + maxc) * TT;
+  size_t bytes = dbl * sizeof(double) + (size_t)maxi * sizeof(int4) +
+                 sizeof(int) * (size_t)(2 * (maxr + maxc)) + 2 * (size_t)nt;
+  return (bytes + 15) & ~(size_t)15;
+}
+
+/*
+ * Tm: the tiles (k_tri_to_tiles); A receives the reflectors in FP64 in A(c+2:n, c) and e on the
+ * subdiagonal, as dormtr (lower) reads them.  prow [nt][pc][TT], pcol [nt][pr][TT]: the
+ * published row and column parts; dotp [2][nt]: the index blocks' partial y.v of alternate
+ * steps; kcnt [nt]: arrival counters (zero at launch; pr + pc arrivals per active index block
+ * and step).  maxr/maxc/maxi bound a block's tile rows, tile columns and tile halves over all
+ * steps (tt_assign evaluated by the host).
+ */
+__global__ void __launch_bounds__(TR_THREADS, 1)
+k_tridiag_tiled(double *A, double *Tm, int n, int nt, int pr, int pc, int maxr, int maxc,
+                int maxi, int cs, double *d, double *e, double *tau, double *vbuf, double *wbuf,
+                double *ybuf, double *prow, double *pcol, double *dotp, unsigned *kcnt,
+                double *part_dot2, unsigned *bar, int *err, unsigned long long *phase_ns)
+{
+  extern __shared__ double sh[];
+  const int npad = nt * TT;
+  double *svp = sh, *swp = sh + npad, *svc = sh + 2 * npad; /* float-float pairs */
+  double *rslot = sh + 3 * (size_t)npad;                  /* [TT_R][TT] */
+  double *cslot = rslot + (size_t)TT_R * TT;              /* [TT_R][TT/2] */
+  double *racc = cslot + (size_t)TT_R * (TT / 2);         /* [maxr][TT] */
+  double *cacc = racc + (size_t)maxr * TT;                /* [maxc][TT] */
+  int4 *items = reinterpret_cast<int4 *>(cacc + (size_t)maxc * TT);
+  int *rowl = reinterpret_cast<int *>(items + maxi);
+  int *coll = rowl + maxr;
+  int *lastl = coll + maxc;
+  unsigned char *rg = reinterpret_cast<unsigned char *>(lastl + maxr + maxc);
+  unsigned char *cg = rg + nt;
+  __shared__ ff2 red[TR_WARPS];
+  __shared__ ff2 s_dot[TR_WARPS];
+  __shared__ tr_step st;
+  __shared__ ff2 s_slotf, s_dc;
+  __shared__ int s_nr, s_nc, s_ni, s_nl;
+  const int G = gridDim.x, b = blockIdx.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const bool active = b < pr * pc;
+  const int ga = active ? b / pc : 0, gb = active ? b - (b / pc) * pc : 0;
+  const ff2 ONE = ff_make(1.f, 0.f), ZERO = ff_make(0.f, 0.f);
+  unsigned *count = bar;
+  unsigned target = 0;
+  /* the previous step's reflector scalars (block-uniform, kept in shared memory) */
+  __shared__ ff2 s_tau_p, s_scale_p, s_e_p;
+  bool have_p = false;
+  /* phase_ns (optional, block 0): time in A, B (entry 1; entry 2 for the first 30% of the
+   * steps) and the barrier (entry 4), accumulated in shared memory */
+  __shared__ unsigned long long s_ph[6];
+  const bool stamp = phase_ns != NULL && b == 0 && threadIdx.x == 0;
+  if (stamp) {
+    for (int i = 0; i < 5; ++i) s_ph[i] = 0ull;
+    s_ph[5] = globaltimer_ns();
+  }
+  if (threadIdx.x == 0) s_tau_p = s_scale_p = s_e_p = ZERO;
+#define TT_STAMP(i)                                    \
+  if (stamp) {                                         \
+    const unsigned long long t_now = globaltimer_ns(); \
+    s_ph[i] += t_now - s_ph[5];                        \
+    s_ph[5] = t_now;                                   \
+  }
+  const int early = (int)((3LL * n) / 10);
+  for (int q = threadIdx.x; q < 3 * npad; q += blockDim.x) sh[q] = 0.0; /* padding stays 0 */
+  int j0_lists = -1;
+  for (int c = 0; c < cs; ++c) {
+    const int J0 = (c + 1) / TT;
+    if (J0 != j0_lists) {
+      /* the block's tile rows, tile columns and tile halves from J0 on */
+      if (threadIdx.x == 0) {
+        tt_assign(nt, J0, pr, pc, rg, cg);
+        int nr = 0, nc = 0, ni = 0, bad = 0;
+        if (active) {
+          for (int I = J0; I < nt; ++I)
+            if (rg[I] == ga) {
+              if (nr < maxr) rowl[nr++] = I; else bad = 1;
+            }
+          for (int J = J0; J < nt; ++J)
+            if (cg[J] == gb) {
+              if (nc < maxc) coll[nc++] = J; else bad = 1;
+            }
+          for (int kr = 0; kr < nr; ++kr)
+            for (int kc = 0; kc < nc && coll[kc] <= rowl[kr]; ++kc)
+              for (int h = 0; h < 2; ++h) {
+                if (ni < maxi)
+                  items[ni++] = make_int4(rowl[kr], coll[kc], h + 2 * kr,
+                                          rowl[kr] == coll[kc] ? -1 : kc);
+                else
+                  bad = 1;
+              }
+        }
+        if (bad) atomicExch(err, TR_ERR_LISTS);
+        s_nr = nr;
+        s_nc = nc;
+        s_ni = ni;
+      }
+      __syncthreads();
+      j0_lists = J0;
+    }
+    /* ---- A: as in k_tridiag, with column c read from the tiles ---- */
+    double *xcur = (c & 1) ? wbuf : vbuf, *xprev = (c & 1) ? vbuf : wbuf;
+    double *ycur = ybuf + (int64_t)(c & 1) * n, *yprev = ybuf + (int64_t)((c + 1) & 1) * n;
+    ff2 pacc = ZERO;
+    const ff2 tau_pf = s_tau_p, scale_pf = s_scale_p, e_pf = s_e_p;
+    if (have_p && warp == TR_WARPS - 1) {
+      /* y.v of step c-1: its index blocks' partial dots (from (c-1+1)/TT on), in order */
+      const double *pprev = dotp + (size_t)((c + 1) & 1) * nt;
+      for (int k = c / TT + lane; k < nt; k += 32) pacc = ff_add(pacc, ff_load(pprev + k));
+    }
+    {
+      const int Jc = c / TT, jc = c - Jc * TT;
+#pragma unroll 4
+      for (int q = c + threadIdx.x; q < n; q += blockDim.x) {
+        ff2 vp = ZERO, yq = ZERO;
+        if (have_p) {
+          vp = (q == c) ? ONE : ff_mul(ff_load(xprev + q), scale_pf);
+          yq = ff_load(yprev + q);
+        }
+        ff_store(svp + q, vp);
+        ff_store(swp + q, yq);
+        const int I = q / TT;
+        ff_store(svc + q, ff_load(Tm + (tt_tile(I, Jc) * TT + jc) * TT + (q - I * TT)));
+      }
+    }
+    if (have_p && warp == TR_WARPS - 1) {
+      for (int o = 16; o; o >>= 1) pacc = ff_add(pacc, ff_shfl_xor(pacc, o));
+      if (lane == 0) s_slotf = pacc;
+    }
+    __syncthreads();
+    ff2 wpc = ZERO, alpha_pf = ZERO;
+    if (have_p) {
+      const ff2 dsum = s_slotf;
+      alpha_pf = ff_scale(ff_mul(ff_mul(tau_pf, tau_pf), dsum), -0.5f);
+      wpc = ff_fma(tau_pf, ff_load(swp + c), alpha_pf);
+    }
+    {
+      const int cnt = n - c, per = (cnt + G - 1) / G;
+      const int r0 = c + b * per, r1 = min(n, r0 + per);
+      ff2 nrm = ZERO;
+      for (int q = c + threadIdx.x; q < n; q += blockDim.x) {
+        ff2 x = ff_load(svc + q);
+        const bool mine = q >= r0 && q < r1;
+        if (have_p) {
+          const ff2 vp = ff_load(svp + q);
+          const ff2 wp = ff_fma(tau_pf, ff_load(swp + q), ff_mul(alpha_pf, vp));
+          ff_store(swp + q, wp);
+          x = ff_fma(ff_neg(vp), wpc, x);
+          x = ff_add(x, ff_neg(wp));
+          if (mine) A[(int64_t)(c - 1) * n + q] = ff_to_double(q == c ? e_pf : vp);
+        }
+        ff_store(svc + q, x);
+        if (mine) ff_store(xcur + q, x);
+        if (q >= c + 2) nrm = ff_fma(x, x, nrm);
+      }
+      const ff2 xn2 = ff_block_sum2(nrm, red);
+      if (threadIdx.x == 0) {
+        const ff2 alpha = ff_load(svc + c + 1);
+        s_dc = ff_load(svc + c);
+        if (xn2.h == 0.f) {
+          st.beta = alpha;
+          st.tau_c = ZERO;
+          st.scale_c = ZERO;
+        } else {
+          const ff2 nrm2 = ff_sqrt(ff_fma(alpha, alpha, xn2));
+          const ff2 beta = alpha.h >= 0.f ? ff_neg(nrm2) : nrm2;
+          const ff2 am = ff_add(alpha, ff_neg(beta));
+          st.beta = beta;
+          st.tau_c = ff_div(ff_neg(am), beta);
+          st.scale_c = ff_div(ONE, am);
+        }
+      }
+      __syncthreads();
+      if (b == 0 && threadIdx.x == 32) {
+        d[c] = ff_to_double(s_dc);
+        e[c] = ff_to_double(st.beta);
+        tau[c] = ff_to_double(st.tau_c);
+      }
+    }
+    const ff2 beta = st.beta, tau_c = st.tau_c;
+    const ff2 scale_cf = st.scale_c;
+    TT_STAMP(0)
+    /* ---- B ---- v of step c; the vectors zero at indices J0*TT .. c (rows and columns up to
+     * c keep their values, and take no part in the dots) */
+    for (int q = c + 1 + threadIdx.x; q < n; q += blockDim.x)
+      ff_store(svc + q, (q == c + 1) ? ONE : ff_mul(ff_load(svc + q), scale_cf));
+    for (int q = J0 * TT + threadIdx.x; q <= c; q += blockDim.x) {
+      ff_store(svc + q, ZERO);
+      ff_store(svp + q, ZERO);
+      ff_store(swp + q, ZERO);
+    }
+    const int nr = s_nr, nc = s_nc, ni = s_ni;
+    for (int idx = threadIdx.x; idx < (nr + nc) * TT; idx += blockDim.x)
+      ff_store(idx < nr * TT ? racc + idx : cacc + (idx - nr * TT), ZERO);
+    __syncthreads();
+    for (int rb = 0; rb < ni; rb += TT_R) {
+      const int re = min(ni, rb + TT_R);
+      for (int u = warp; rb + u < re; u += TR_WARPS) {
+        const int4 it = items[rb + u];
+        const int I = it.x, J = it.y, h = it.z & 1;
+        double *rs = rslot + (size_t)u * TT, *cs = cslot + (size_t)u * (TT / 2);
+        if (h == 0 && J == J0 && J0 * TT + TT / 2 <= c + 1) {
+          /* every column of this half is at or before c */
+          ff_store(rs + 2 * lane, ZERO);
+          ff_store(rs + 2 * lane + 1, ZERO);
+          ff_store(cs + lane, ZERO);
+        } else {
+          tt_half(Tm + tt_tile(I, J) * (TT * TT), I, J, h, I == J, have_p, svp, swp, svc, rs, cs,
+                  lane);
+        }
+      }
+      __syncthreads();
+      /* the round's parts into the block's per-index-block sums, in item order */
+      for (int idx = threadIdx.x; idx < nr * TT; idx += blockDim.x) {
+        const int kr = idx / TT, i = idx - kr * TT;
+        ff2 s = ff_load(racc + idx);
+        for (int t = rb; t < re; ++t)
+          if ((items[t].z >> 1) == kr) s = ff_add(s, ff_load(rslot + (size_t)(t - rb) * TT + i));
+        ff_store(racc + idx, s);
+      }
+      for (int idx = threadIdx.x; idx < nc * TT; idx += blockDim.x) {
+        const int kc = idx / TT, j = idx - kc * TT, hh = j / (TT / 2), jj = j - hh * (TT / 2);
+        ff2 s = ff_load(cacc + idx);
+        for (int t = rb; t < re; ++t) {
+          const int4 it = items[t];
+          if (it.w == kc && (it.z & 1) == hh)
+            s = ff_add(s, ff_load(cslot + (size_t)(t - rb) * (TT / 2) + jj));
+        }
+        ff_store(cacc + idx, s);
+      }
+      __syncthreads();
+    }
+    /* publish the block's parts: row parts of its tile rows, column parts of its tile columns */
+    if (active) {
+      for (int idx = threadIdx.x; idx < nr * TT; idx += blockDim.x) {
+        const int kr = idx / TT, i = idx - kr * TT;
+        ff_store(prow + ((size_t)rowl[kr] * pc + gb) * TT + i, ff_load(racc + idx));
+      }
+      for (int idx = threadIdx.x; idx < nc * TT; idx += blockDim.x) {
+        const int kc = idx / TT, j = idx - kc * TT;
+        ff_store(pcol + ((size_t)coll[kc] * pr + ga) * TT + j, ff_load(cacc + idx));
+      }
+    }
+    if (threadIdx.x == 0) s_nl = 0;
+    __syncthreads();
+    if (active) {
+      const unsigned ktarget = (unsigned)(pr + pc) * (unsigned)(c + 1);
+      int K = -1;
+      if ((int)threadIdx.x < nr) /* nr, nc <= 512 (host check) */
+        K = rowl[threadIdx.x];
+      else if (threadIdx.x >= 512 && (int)threadIdx.x - 512 < nc)
+        K = coll[threadIdx.x - 512];
+      if (K >= 0 && atom_add_acq_rel_gpu(kcnt + K, 1u) + 1u == ktarget)
+        lastl[atomicAdd(&s_nl, 1)] = K;
+    }
+    __syncthreads();
+    {
+      /* the index blocks this block completed: y over the block's TT indices (pc row parts,
+       * then pr column parts, in order) and its partial y.v */
+      const int nl = s_nl;
+      for (int s0 = 0; s0 < nl; s0 += TR_THREADS / TT) {
+        const int s = s0 + (int)(threadIdx.x / TT), i = threadIdx.x & (TT - 1);
+        ff2 dv = ZERO;
+        if (s < nl) {
+          const int K = lastl[s];
+          ff2 y = ZERO;
+          const double *p1 = prow + (size_t)K * pc * TT + i;
+          for (int g = 0; g < pc; ++g) y = ff_add(y, ff_load(p1 + (size_t)g * TT));
+          const double *p2 = pcol + (size_t)K * pr * TT + i;
+          for (int g = 0; g < pr; ++g) y = ff_add(y, ff_load(p2 + (size_t)g * TT));
+          const int q = K * TT + i;
+          if (q < n) ff_store(ycur + q, y);
+          dv = ff_mul(y, ff_load(svc + q));
+        }
+        for (int o = 16; o; o >>= 1) dv = ff_add(dv, ff_shfl_xor(dv, o));
+        if (lane == 0) s_dot[warp] = dv;
+        __syncthreads();
+        if (threadIdx.x < TR_THREADS / TT && s0 + (int)threadIdx.x < nl)
+          ff_store(dotp + (size_t)(c & 1) * nt + lastl[s0 + threadIdx.x],
+                   ff_add(s_dot[2 * threadIdx.x], s_dot[2 * threadIdx.x + 1]));
+        __syncthreads();
+      }
+    }
+    TT_STAMP(c < early ? 2 : 1)
+    if (threadIdx.x == 0) { /* read again only after the grid barrier's block barriers */
+      s_tau_p = tau_c;
+      s_scale_p = scale_cf;
+      s_e_p = beta;
+    }
+    target += G;
+    if (!tr_grid_sync(count, target, err)) return;
+    TT_STAMP(4)
+    have_p = true;
+  }
+  if (cs < n - 1) {
+    /* the switch to whole columns: the trailing block (indices >= cs) of the block's tiles
+     * into A as float-float pairs, both triangles (the pending update of step cs-1 is applied
+     * by the first whole-matrix step, as in k_tridiag) */
+    const int ni = s_ni;
+    for (int64_t idx = threadIdx.x; idx < (int64_t)ni * (TT * TT / 2); idx += blockDim.x) {
+      const int u = (int)(idx / (TT * TT / 2)), rem = (int)(idx - (int64_t)u * (TT * TT / 2));
+      const int j = rem / TT, i = rem - j * TT;
+      const int4 it = items[u];
+      const int h = it.z & 1;
+      const int r = it.x * TT + i, q = it.y * TT + h * (TT / 2) + j;
+      if (r >= cs && q >= cs && r < n && q < n) {
+        const double v = Tm[(tt_tile(it.x, it.y) * TT + h * (TT / 2) + j) * TT + i];
+        A[(int64_t)q * n + r] = v;
+        if (it.x != it.y) A[(int64_t)r * n + q] = v;
+      }
+    }
+    target += G;
+    if (!tr_grid_sync(count, target, err)) return;
+    ff2 tau_pf = s_tau_p, scale_pf = s_scale_p, e_pf = s_e_p;
+    if (!tr_full_steps(A, n, cs, d, e, tau, vbuf, wbuf, ybuf, part_dot2, count, target, err, svp,
+                       swp, svc, tau_pf, scale_pf, e_pf, have_p,
+                       dotp + (size_t)((cs + 1) & 1) * nt, cs / TT, nt, stamp ? s_ph : NULL))
+      return;
+    if (stamp)
+      for (int i = 0; i < 5; ++i) phase_ns[i] = s_ph[i];
+    tr_full_last(A, n, d, ybuf, part_dot2, tau_pf, e_pf, have_p);
+    return;
+  }
+  if (stamp)
+    for (int i = 0; i < 5; ++i) phase_ns[i] = s_ph[i];
+#undef TT_STAMP
+  /* last diagonal entry and the storage of the last reflector */
+  if (b == 0) {
+    ff2 dsum = ZERO;
+    if (have_p) {
+      if (threadIdx.x < 32) {
+        ff2 s = ZERO;
+        const double *pl = dotp + (size_t)((n - 2) & 1) * nt;
+        for (int k = (n - 1) / TT + (int)threadIdx.x; k < nt; k += 32) s = ff_add(s, ff_load(pl + k));
+        for (int o = 16; o; o >>= 1) s = ff_add(s, ff_shfl_xor(s, o));
+        if (threadIdx.x == 0) s_slotf = s;
+      }
+      __syncthreads();
+      dsum = s_slotf;
+    }
+    if (threadIdx.x == 0) {
+      const int Il = (n - 1) / TT, il = n - 1 - Il * TT;
+      ff2 a = ff_load(Tm + (tt_tile(Il, Il) * TT + il) * TT + il);
+      const ff2 tau_pf = s_tau_p, e_pf = s_e_p;
       if (have_p) {
         const ff2 alpha_p = ff_scale(ff_mul(ff_mul(tau_pf, tau_pf), dsum), -0.5f);
         const ff2 wp =
@@ -1112,6 +1682,49 @@ __global__ void k_reverse(const double *w, double *out, int n)
     out[i] = w[n - 1 - i];
 }
 
+/* the pr x pc block grid of k_tridiag_tiled: the largest pr * pc <= G with both at most
+ * TT_MAXG (ties: the smaller pr + pc, so that an index block has fewer parts) */
+static void tt_grid(int G, int *pr, int *pc)
+{
+  int best = 0;
+  *pr = *pc = 0;
+  for (int c = 1; c * c <= G; ++c) {
+    const int r = G / c;
+    if (r > TT_MAXG || c > TT_MAXG) continue;
+    if (r * c > best || (r * c == best && r + c < *pr + *pc)) {
+      best = r * c;
+      *pr = r;
+      *pc = c;
+    }
+  }
+}
+
+/* a block's most tile rows, tile columns and tile halves over every first active tile index
+ * (the lists k_tridiag_tiled builds with tt_assign) */
+static void tt_bounds(int nt, int pr, int pc, int *maxr, int *maxc, int *maxi)
+{
+  std::vector<unsigned char> rg((size_t)nt), cg((size_t)nt);
+  std::vector<int> cnt((size_t)pr * pc), nrow((size_t)pr), ncol((size_t)pc);
+  int mr = 1, mc = 1, mi = 2;
+  for (int J0 = 0; J0 < nt; ++J0) {
+    tt_assign(nt, J0, pr, pc, rg.data(), cg.data());
+    std::fill(cnt.begin(), cnt.end(), 0);
+    std::fill(nrow.begin(), nrow.end(), 0);
+    std::fill(ncol.begin(), ncol.end(), 0);
+    for (int I = J0; I < nt; ++I) {
+      ++nrow[rg[I]];
+      ++ncol[cg[I]];
+      for (int J = J0; J <= I; ++J) cnt[(size_t)rg[I] * pc + cg[J]] += 2;
+    }
+    for (int g = 0; g < pr; ++g) mr = std::max(mr, nrow[g]);
+    for (int g = 0; g < pc; ++g) mc = std::max(mc, ncol[g]);
+    for (size_t k = 0; k < cnt.size(); ++k) mi = std::max(mi, cnt[k]);
+  }
+  *maxr = mr;
+  *maxc = mc;
+  *maxi = mi;
+}
+
 int gp_eig_tridiag(gp_ctx *ctx, int32_t n, int32_t nvec, double *d_evals_desc, double *d_vecs)
 {
   return gp_eig_sym(ctx, ctx->d_xtx, n, nvec, d_evals_desc, d_vecs);
@@ -1186,11 +1799,103 @@ int gp_eig_sym(gp_ctx *ctx, double *A_in, int32_t n, int32_t nvec, double *d_eva
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tridiag, TR_THREADS, tr_smem);
     coop = dev_coop && per_sm >= 1;
   }
+  /* the lower-triangle tiled variant (k_tridiag_tiled) where its shared memory fits, unless
+   * GP_TRIDIAG_TILED=0; the whole-matrix k_tridiag otherwise */
+  const char *tt_env = getenv("GP_TRIDIAG_TILED");
+  const int nt = (n + TT - 1) / TT;
+  int tt_pr = 0, tt_pc = 0, tt_maxr = 0, tt_maxc = 0, tt_maxi = 0;
+  size_t tt_smem = 0;
+  /* the tiled steps run while the trailing order exceeds tt_switch (GP_TRIDIAG_SWITCH), where
+   * the whole-column steps, with more rows per block than tile rows, take over */
+  const char *sw_env = getenv("GP_TRIDIAG_SWITCH");
+  const int tt_switch = sw_env && sw_env[0] ? atoi(sw_env) : 2500;
+  const int tt_cs = n - 1 - std::max(1, tt_switch); /* first whole-column step */
+  int tiled = !(senv && senv[0] == '1') && !(tt_env && tt_env[0] == '0') && tt_cs >= 1 &&
+              tr_smem <= 200 * 1024;
+  if (tiled) {
+    tt_grid((int)G, &tt_pr, &tt_pc);
+    tiled = tt_pr >= 1 && tt_pc >= 1;
+  }
+  if (tiled) {
+    tt_bounds(nt, tt_pr, tt_pc, &tt_maxr, &tt_maxc, &tt_maxi);
+    tt_smem = tt_smem_bytes(nt, tt_maxr, tt_maxc, tt_maxi);
+    tiled = tt_maxr <= 512 && tt_maxc <= 512 && tt_smem <= 220 * 1024;
+  }
+  if (tiled) {
+    int dev_coop = 0, per_sm = 0;
+    cudaDeviceGetAttribute(&dev_coop, cudaDevAttrCooperativeLaunch, ctx->device);
+    tiled = dev_coop && cudaFuncSetAttribute(k_tridiag_tiled,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)tt_smem) == cudaSuccess;
+    if (tiled) {
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tridiag_tiled, TR_THREADS,
+                                                    tt_smem);
+      tiled = per_sm >= 1;
+    }
+    (void)cudaGetLastError();
+  }
+  if (tiled) coop = 1;
   if (!coop && !may_fallback)
     return gp_fail(ctx, GP_ERR_CUDA, "eigensolve: the cooperative tridiagonalisation cannot run");
   GP_EIG_MARK(0);
   int info = 0;
-  if (coop) {
+  if (tiled) {
+    const int64_t ntiles = (int64_t)nt * (nt + 1) / 2;
+    const size_t tile_d = (size_t)ntiles * TT * TT;
+    const size_t part_d = (size_t)(tt_pr + tt_pc) * nt * TT;
+    const size_t tri_bytes = sizeof(double) * (tile_d + part_d + 2 * (size_t)nt) +
+                             sizeof(unsigned) * (size_t)nt;
+    int rc2 = gp_realloc(ctx, (void **)&ctx->d_tri, tri_bytes);
+    if (rc2) return rc2;
+    double *Tm = ctx->d_tri, *prow = Tm + tile_d, *pcol = prow + (size_t)nt * tt_pc * TT;
+    double *dotp = pcol + (size_t)nt * tt_pr * TT;
+    unsigned *kcnt = (unsigned *)(dotp + 2 * (size_t)nt);
+    int *d_err = ctx->d_err;
+    GP_CUDA(ctx, cudaMemsetAsync(d_err, 0, sizeof(int), ctx->stream));
+    GP_CUDA(ctx, cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), ctx->stream));
+    GP_CUDA(ctx, cudaMemsetAsync(kcnt, 0, sizeof(unsigned) * (size_t)nt, ctx->stream));
+    {
+      int blocks = (int)std::min<int64_t>(ntiles, (int64_t)ctx->num_sms * 8);
+      k_tri_to_tiles<<<blocks, 256, 0, ctx->stream>>>(A_in, n, nt, Tm);
+      GP_LAUNCH_CHECK(ctx, "k_tri_to_tiles");
+    }
+    unsigned long long *phase = NULL;
+    if (timing) {
+      phase = (unsigned long long *)(bar + 8);
+      GP_CUDA(ctx, cudaMemsetAsync(phase, 0, 5 * sizeof(unsigned long long), ctx->stream));
+    }
+    double *A = A_in, *pd2 = parts;
+    int nn = n, nt_ = nt, cs = tt_cs;
+    void *args[] = {&A,    &Tm,   &nn,   &nt_,  &tt_pr, &tt_pc, &tt_maxr, &tt_maxc,
+                    &tt_maxi, &cs, &d,   &e,    &tau,   &vbuf,  &wbuf,    &ybuf,
+                    &prow, &pcol, &dotp, &kcnt, &pd2,   &bar,   &d_err,   &phase};
+    GP_CUDA(ctx, cudaEventRecord(ctx->ev_tr0, ctx->stream));
+    GP_CUDA(ctx, cudaLaunchCooperativeKernel((const void *)k_tridiag_tiled, dim3((unsigned)G),
+                                             dim3(TR_THREADS), args, tt_smem, ctx->stream));
+    GP_CUDA(ctx, cudaEventRecord(ctx->ev_tr1, ctx->stream));
+    ctx->launches++;
+    int herr = 0;
+    GP_CUDA(ctx, gp_memcpy(ctx, &herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (herr == TR_ERR_LISTS)
+      return gp_fail(ctx, GP_ERR_CUDA, "tiled tridiagonalisation: a block's tile lists overflowed");
+    if (herr) return gp_fail(ctx, GP_ERR_TIMEOUT, "tridiagonalisation grid barrier timed out");
+    float tms = 0.f;
+    GP_CUDA(ctx, cudaEventElapsedTime(&tms, ctx->ev_tr0, ctx->ev_tr1));
+    if (A_in == ctx->d_xtx) {
+      ctx->tridiag_ms = tms;
+      ctx->tridiag_n = n;
+    }
+    if (timing) {
+      unsigned long long hp[5];
+      cudaMemcpy(hp, phase, sizeof hp, cudaMemcpyDeviceToHost);
+      fprintf(stderr,
+              "k_tridiag_tiled n=%d grid %dx%d, whole columns from step %d (block 0): A %.1f ms, "
+              "B %.1f (first 30%% of steps %.1f), barrier %.1f\n",
+              n, tt_pr, tt_pc, tt_cs, hp[0] * 1e-6, (hp[1] + hp[2]) * 1e-6, hp[2] * 1e-6,
+              hp[4] * 1e-6);
+    }
+  } else if (coop) {
     int *d_err = ctx->d_err;
     GP_CUDA(ctx, cudaMemsetAsync(d_err, 0, sizeof(int), ctx->stream));
     GP_CUDA(ctx, cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), ctx->stream));

@@ -58,6 +58,7 @@ struct gp_ctx {
   int64_t xtx_cap;
   double *d_evals;       /* [nrows] */
   double *d_evecs;       /* [nvec*nrows] top vectors, descending */
+  double *d_tri;         /* the tiled tridiagonalisation's lower-triangle tiles and parts */
   int keep_gram;         /* gp_keep_gram: copy the scaled Gram before the eigensolve */
   double *d_xtx_keep;    /* [nrows*nrows] that copy (the relatedness scan reads it) */
   int64_t keep_cap;

@@ -382,15 +382,19 @@ def test_smartpca_run_split_fp16_vs_reference(gpu, case):
     compare_coords(c.ref_coords, mine, 2, 1e-4)
 
 
-@pytest.mark.parametrize("path", ["default", "GP_EIG_NO_FF", "GP_EIG_II_GLOBAL"])
+@pytest.mark.parametrize("path", ["default", "GP_EIG_NO_FF=1", "GP_EIG_II_GLOBAL=1",
+                                  "GP_TRIDIAG_SWITCH=300", "GP_TRIDIAG_SWITCH=1"])
 def test_eig_tridiag_all_values_top_vectors(gpu, monkeypatch, path):
     """sytrd + bisection + inverse iteration + ormtr: every eigenvalue within 1e-12 of the
     largest against LAPACK (numpy eigh), 24 top eigenvectors with small residuals, orthonormal,
     and equal (up to sign) to LAPACK's where the eigenvalues are separated; also through the
-    multisection without its float-float phase and the inverse iteration with its factors in
-    global memory (the paths of larger N)"""
+    multisection without its float-float phase, the inverse iteration with its factors in
+    global memory (the paths of larger N), and the lower-triangle tiled reduction switching to
+    whole columns at trailing order 300 or only for the last step (at N = 1,200 the default
+    runs whole columns throughout)"""
     if path != "default":
-        monkeypatch.setenv(path, "1")
+        key, val = path.split("=")
+        monkeypatch.setenv(key, val)
     rec, pop = synth(6000, [500, 400, 300], [0.01, 0.02, 0.04], miss=0.02, seed=27)
     nind = len(pop)
     gpu.load_genotypes(rec, nind)

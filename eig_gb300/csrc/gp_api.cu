@@ -191,7 +191,7 @@ extern "C" void gp_close(gp_ctx *ctx)
                   ctx->d_xtx,    ctx->d_evals,   ctx->d_evecs,   ctx->d_ffvecs,  ctx->d_fxscal,
                   ctx->d_scratch, ctx->d_scratch2, ctx->d_scratch3, ctx->d_scratch4, ctx->d_scratch5,
                   ctx->d_err,   ctx->d_xtx_keep, ctx->d_rowpop, ctx->d_gtab, ctx->d_gfill,
-                  ctx->d_tri};
+                  ctx->d_tri,   ctx->d_tt};
   for (size_t i = 0; i < sizeof(bufs) / sizeof(bufs[0]); ++i)
     if (bufs[i]) cudaFree(bufs[i]);
   if (ctx->solver) cusolverDnDestroy(ctx->solver);
@@ -222,7 +222,7 @@ extern "C" int gp_release(gp_ctx *ctx)
                    (void **)&ctx->d_scratch, (void **)&ctx->d_scratch2, (void **)&ctx->d_scratch3,
                    (void **)&ctx->d_scratch4, (void **)&ctx->d_scratch5, (void **)&ctx->d_xtx_keep,
                    (void **)&ctx->d_rowpop,  (void **)&ctx->d_gtab,     (void **)&ctx->d_gfill,
-                   (void **)&ctx->d_tri};
+                   (void **)&ctx->d_tri,     (void **)&ctx->d_tt};
   for (size_t i = 0; i < sizeof(bufs) / sizeof(bufs[0]); ++i) {
     if (*bufs[i]) cudaFree(*bufs[i]);
     *bufs[i] = NULL;
@@ -230,6 +230,7 @@ extern "C" int gp_release(gp_ctx *ctx)
   ctx->scratch_cap = ctx->scratch2_cap = ctx->scratch3_cap = ctx->scratch4_cap =
       ctx->scratch5_cap = 0;
   ctx->xtx_cap = 0;
+  ctx->tt_n = 0;
   ctx->geno_cap = 0;
   ctx->codes4_rows = 0;
   ctx->keep_cap = 0;

@@ -798,76 +798,43 @@ k_tridiag(double *A, int n, double *d, double *e, double *tau, double *vbuf, dou
 /*
  * The same reduction (dsytd2, lower) with the trailing matrix held as its lower triangle only,
  * in TT x TT tiles: half the bytes per column step and two thirds of the float-float work of
- * k_tridiag, whose whole-column product needs both triangles.  Tile (I, J), I >= J, of the
+ * the whole-column step, whose product needs both triangles.  Tile (I, J), I >= J, of the
  * lower triangle is TT*TT float-float pairs at Tm + tt_tile(I, J)*TT*TT, column-major inside
  * the tile (element (i, j) at j*TT + i); diagonal tiles are held in full; rows and columns
  * beyond n are zero padding.
  *
- * Per column step the product y = A'v needs, for index block K, the row parts of the tiles in
- * tile row K (A(K, J) v(J), the diagonal tile included) and the column parts of the tiles in
- * tile column K below the diagonal (A(I, K)^T v(I)).  The blocks form a pr x pc grid: block
- * (a, b) owns the tiles (I, J) with rg(I) = a and cg(J) = b, where rg assigns the active tile
- * rows to the pr row groups longest first to the group with the least work (cg the same for
- * the columns over pc groups; recomputed each time the first active tile index J0 moves).  So
- * index block K has pc row-part contributors (blocks (rg(K), *)) and pr column-part ones
- * (blocks (*, cg(K))).  Per step:
- *   A   as in k_tridiag (every block: v and w of step c-1, the pending update of column c read
- *       from the tiles, its norm, the reflector; y.v from the index blocks' partial dots)
- *   B   each warp takes halves (32 columns) of the block's tiles: the pending rank-2 update of
- *       step c-1 (written back), the row dots (two rows per lane) and, off the diagonal, the
- *       column dots (a reduce-scatter over the warp per 4 columns); the block sums its halves'
- *       parts per index block in a fixed order and publishes one row part per tile row and one
- *       column part per tile column it owns; each publication is an arrival on the index
- *       block's counter (release/acquire), and the block whose arrival completes an index
- *       block sums its pr + pc parts in a fixed order into y and its partial y.v
+ * Work is split into parts: tile row I (TT rows) x column unit u (TT_U columns, u = 0 ..
+ * nt*TT/TT_U - 1, in tile column u/(TT/TT_U)).  The blocks form a pr x pc grid: block (a, b)
+ * owns the parts of the tile rows in row group a and the column units in column group b
+ * (tables computed by the host for each first active tile index J0, balanced so that every
+ * block has about the same number of parts).  So the product's index block K (TT indices)
+ * has pc row-part contributors (blocks (rg(K), *)) and, for each of its units, pr column-part
+ * contributors (blocks (*, cg(u))).  Per step:
+ *   A   as in the whole-column step (every block: v and w of step c-1, the pending update of
+ *       column c read from the tiles, its norm, the reflector; y.v from the index blocks'
+ *       partial dots)
+ *   B   each warp takes parts of the block: the pending rank-2 update of step c-1 (written
+ *       back), the row dots (two rows per lane) and, off the diagonal, the column dots (a
+ *       reduce-scatter over the warp per 4 columns); the block sums its parts per tile row and
+ *       per column unit in a fixed order and publishes them, one arrival (release) on the
+ *       index block's counter per published sum; block K mod G waits (acquire, bounded) for
+ *       index block K's pc + (TT/TT_U)*pr arrivals and sums them in a fixed order into y and
+ *       the index block's partial y.v
  *   --- grid barrier
  * Rows and columns up to c keep their values (the pending-update vectors and v are zero there),
- * so that phase A of a block that is still reading column c never sees it change.  Sums have
- * a fixed order: the result does not depend on which block completes an index block.
+ * so that phase A of a block still reading column c never sees it change.  Every sum has a
+ * fixed order.
  */
 #define TT 64
-#define TT_R 64     /* tile halves per round (two per warp) */
-#define TT_MAXG 32  /* row or column groups at most */
+#define TT_U 16                /* columns per column unit */
+#define TT_UPT (TT / TT_U)     /* column units per tile column */
+#define TT_MAXG 32             /* row or column groups at most */
 #define TR_ERR_LISTS 12
+#define TR_ERR_WAIT 13
 
 __host__ __device__ __forceinline__ int64_t tt_tile(int I, int J)
 {
   return (int64_t)I * (I + 1) / 2 + J;
-}
-
-/* longest-first assignment of the active tile rows (I - J0 + 1 tiles each) to pr groups and of
- * the active tile columns (nt - J tiles each) to pc groups, each to the group with the least
- * work so far (ties: the lowest group) */
-__host__ __device__ inline void tt_assign(int nt, int J0, int pr, int pc, unsigned char *rg,
-                                          unsigned char *cg)
-{
-  int sum[TT_MAXG];
-  for (int g = 0; g < pr; ++g) sum[g] = 0;
-  for (int I = nt - 1; I >= J0; --I) {
-    int best = 0;
-    for (int g = 1; g < pr; ++g)
-      if (sum[g] < sum[best]) best = g;
-    rg[I] = (unsigned char)best;
-    sum[best] += I - J0 + 1;
-  }
-  for (int g = 0; g < pc; ++g) sum[g] = 0;
-  for (int J = J0; J < nt; ++J) {
-    int best = 0;
-    for (int g = 1; g < pc; ++g)
-      if (sum[g] < sum[best]) best = g;
-    cg[J] = (unsigned char)best;
-    sum[best] += nt - J;
-  }
-}
-
-__device__ __forceinline__ unsigned atom_add_acq_rel_gpu(unsigned *p, unsigned v)
-{
-  unsigned old;
-  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;"
-               : "=r"(old)
-               : "l"(p), "r"(v)
-               : "memory");
-  return old;
 }
 
 /* the lower triangle of the symmetric FP64 matrix A (column-major, both triangles valid) into
@@ -890,13 +857,13 @@ __global__ void k_tri_to_tiles(const double *A, int n, int nt, double *Tm)
   }
 }
 
-/* one half (32 columns from TT*J + 32h) of tile (I, J) by one warp: the pending update of step
- * c-1 (have_p), written back; the row dots with v over these columns into rs[TT] (rows 2 lane,
- * 2 lane + 1); unless the tile is diagonal, the column dots with v over the tile's rows into
- * cs[32] */
-__device__ __forceinline__ void tt_half(double *tile, int I, int J, int h, bool diag, bool have_p,
-                                        const double *svp, const double *swp, const double *svc,
-                                        double *rs, double *cs, int lane)
+/* one part (TT_U columns from TT*J + j0) of tile (I, J) by one warp: the pending update of
+ * step c-1 (have_p), written back; the row dots with v over these columns into rs[TT] (rows
+ * 2 lane, 2 lane + 1); unless the tile is diagonal, the column dots with v over the tile's
+ * rows into cs[TT_U] */
+__device__ __forceinline__ void tt_part(double *tile, int I, int J, int j0, bool diag,
+                                        bool have_p, const double *svp, const double *swp,
+                                        const double *svc, double *rs, double *cs, int lane)
 {
   const ff2 ZERO = ff_make(0.f, 0.f);
   const int r = I * TT + 2 * lane;
@@ -904,10 +871,10 @@ __device__ __forceinline__ void tt_half(double *tile, int I, int J, int h, bool 
   const ff2 pr0 = ff_load(svp + r), pr1 = ff_load(svp + r + 1);
   const ff2 qr0 = ff_load(swp + r), qr1 = ff_load(swp + r + 1);
   ff2 ra0 = ZERO, ra1 = ZERO;
-  const int j0 = h * (TT / 2);
   const int col0 = J * TT + j0;
   double *p0 = tile + (size_t)j0 * TT + 2 * lane;
-  for (int cb = 0; cb < TT / 2; cb += 4) {
+#pragma unroll 1
+  for (int cb = 0; cb < TT_U; cb += 4) {
     float4 a[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) a[k] = *reinterpret_cast<const float4 *>(p0 + (size_t)(cb + k) * TT);
@@ -954,49 +921,53 @@ __device__ __forceinline__ void tt_half(double *tile, int I, int J, int h, bool 
   ff_store(rs + 2 * lane + 1, ra1);
 }
 
-/* shared-memory bytes of k_tridiag_tiled (the host sizes the launch with the same layout) */
-__host__ __device__ inline size_t tt_smem_bytes(int nt, int maxr, int maxc, int maxi)
+/* shared-memory bytes of k_tridiag_tiled for round size R (parts per round) and the bounds of
+ * a block's tile rows, column units and parts */
+__host__ __device__ inline size_t tt_smem_bytes(int nt, int R, int maxr, int maxc, int maxi)
 {
   const size_t npad = (size_t)nt * TT;
-  size_t dbl = 3 * npad + (size_t)TT_R * TT + (size_t)TT_R * (TT / 2) +
-               (size_t)(maxr + maxc) * TT;
-  size_t bytes = dbl * sizeof(double) + (size_t)maxi * sizeof(int4) +
-                 sizeof(int) * (size_t)(2 * (maxr + maxc)) + 2 * (size_t)nt;
+  const size_t dbl = 3 * npad + (size_t)R * (TT + TT_U) + (size_t)maxr * TT + (size_t)maxc * TT_U;
+  const size_t bytes = dbl * sizeof(double) + (size_t)maxi * sizeof(int4) +
+                       sizeof(int) * (size_t)(3 * maxr + maxc) + (size_t)nt * (1 + TT_UPT);
   return (bytes + 15) & ~(size_t)15;
 }
 
 /*
  * Tm: the tiles (k_tri_to_tiles); A receives the reflectors in FP64 in A(c+2:n, c) and e on the
- * subdiagonal, as dormtr (lower) reads them.  prow [nt][pc][TT], pcol [nt][pr][TT]: the
- * published row and column parts; dotp [2][nt]: the index blocks' partial y.v of alternate
- * steps; kcnt [nt]: arrival counters (zero at launch; pr + pc arrivals per active index block
- * and step).  maxr/maxc/maxi bound a block's tile rows, tile columns and tile halves over all
- * steps (tt_assign evaluated by the host).
+ * subdiagonal, as dormtr (lower) reads them.  rgt [nt][nt], cgt [nt][nt*TT_UPT]: the row group
+ * of each tile row and the column group of each column unit for first active tile index J0
+ * (row J0 of each table).  prow [nt][pc][TT], pcol [nt*TT_UPT][pr][TT_U]: the published row
+ * and column parts; dotp [2][nt]: the index blocks' partial y.v of alternate steps; kcnt [nt]:
+ * arrival counters (zero at launch).  maxr/maxc/maxi bound a block's tile rows, column units
+ * and parts over all J0; R parts per round.  Steps from cs on run whole columns
+ * (tr_full_steps), part_dot2 [2G] their block partials.
  */
 __global__ void __launch_bounds__(TR_THREADS, 1)
 k_tridiag_tiled(double *A, double *Tm, int n, int nt, int pr, int pc, int maxr, int maxc,
-                int maxi, int cs, double *d, double *e, double *tau, double *vbuf, double *wbuf,
-                double *ybuf, double *prow, double *pcol, double *dotp, unsigned *kcnt,
-                double *part_dot2, unsigned *bar, int *err, unsigned long long *phase_ns)
+                int maxi, int R, int cs, const unsigned char *rgt, const unsigned char *cgt,
+                double *d, double *e, double *tau, double *vbuf, double *wbuf, double *ybuf,
+                double *prow, double *pcol, double *dotp, unsigned *kcnt, double *part_dot2,
+                unsigned *bar, int *err, unsigned long long *phase_ns)
 {
   extern __shared__ double sh[];
-  const int npad = nt * TT;
+  const int npad = nt * TT, nu = nt * TT_UPT;
   double *svp = sh, *swp = sh + npad, *svc = sh + 2 * npad; /* float-float pairs */
-  double *rslot = sh + 3 * (size_t)npad;                  /* [TT_R][TT] */
-  double *cslot = rslot + (size_t)TT_R * TT;              /* [TT_R][TT/2] */
-  double *racc = cslot + (size_t)TT_R * (TT / 2);         /* [maxr][TT] */
-  double *cacc = racc + (size_t)maxr * TT;                /* [maxc][TT] */
-  int4 *items = reinterpret_cast<int4 *>(cacc + (size_t)maxc * TT);
-  int *rowl = reinterpret_cast<int *>(items + maxi);
-  int *coll = rowl + maxr;
-  int *lastl = coll + maxc;
-  unsigned char *rg = reinterpret_cast<unsigned char *>(lastl + maxr + maxc);
+  double *rslot = sh + 3 * (size_t)npad;      /* [R][TT] */
+  double *cslot = rslot + (size_t)R * TT;     /* [R][TT_U] */
+  double *racc = cslot + (size_t)R * TT_U;    /* [maxr][TT] */
+  double *cacc = racc + (size_t)maxr * TT;    /* [maxc][TT_U] */
+  int4 *items = reinterpret_cast<int4 *>(cacc + (size_t)maxc * TT_U);
+  int *rowl = reinterpret_cast<int *>(items + maxi); /* tile rows */
+  int *rowb = rowl + maxr;                           /* first part of each tile row */
+  int *rown = rowb + maxr;                           /* parts of each tile row */
+  int *coll = rown + maxr;                           /* column units */
+  unsigned char *rg = reinterpret_cast<unsigned char *>(coll + maxc);
   unsigned char *cg = rg + nt;
   __shared__ ff2 red[TR_WARPS];
   __shared__ ff2 s_dot[TR_WARPS];
   __shared__ tr_step st;
   __shared__ ff2 s_slotf, s_dc;
-  __shared__ int s_nr, s_nc, s_ni, s_nl;
+  __shared__ int s_nr, s_nc, s_ni, s_ok;
   const int G = gridDim.x, b = blockIdx.x;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const bool active = b < pr * pc;
@@ -1023,33 +994,39 @@ k_tridiag_tiled(double *A, double *Tm, int n, int nt, int pr, int pc, int maxr, 
     s_ph[5] = t_now;                                   \
   }
   const int early = (int)((3LL * n) / 10);
+  const unsigned arrivals = (unsigned)(pc + TT_UPT * pr); /* per index block and step */
   for (int q = threadIdx.x; q < 3 * npad; q += blockDim.x) sh[q] = 0.0; /* padding stays 0 */
   int j0_lists = -1;
   for (int c = 0; c < cs; ++c) {
     const int J0 = (c + 1) / TT;
     if (J0 != j0_lists) {
-      /* the block's tile rows, tile columns and tile halves from J0 on */
+      /* the block's tile rows, column units and parts from J0 on (row J0 of the tables) */
+      for (int I = threadIdx.x; I < nt; I += blockDim.x) rg[I] = rgt[(size_t)J0 * nt + I];
+      for (int u = threadIdx.x; u < nu; u += blockDim.x) cg[u] = cgt[(size_t)J0 * nu + u];
+      __syncthreads();
       if (threadIdx.x == 0) {
-        tt_assign(nt, J0, pr, pc, rg, cg);
         int nr = 0, nc = 0, ni = 0, bad = 0;
         if (active) {
           for (int I = J0; I < nt; ++I)
             if (rg[I] == ga) {
               if (nr < maxr) rowl[nr++] = I; else bad = 1;
             }
-          for (int J = J0; J < nt; ++J)
-            if (cg[J] == gb) {
-              if (nc < maxc) coll[nc++] = J; else bad = 1;
+          for (int u = J0 * TT_UPT; u < nu; ++u)
+            if (cg[u] == gb) {
+              if (nc < maxc) coll[nc++] = u; else bad = 1;
             }
-          for (int kr = 0; kr < nr; ++kr)
-            for (int kc = 0; kc < nc && coll[kc] <= rowl[kr]; ++kc)
-              for (int h = 0; h < 2; ++h) {
-                if (ni < maxi)
-                  items[ni++] = make_int4(rowl[kr], coll[kc], h + 2 * kr,
-                                          rowl[kr] == coll[kc] ? -1 : kc);
-                else
-                  bad = 1;
-              }
+          for (int kr = 0; kr < nr; ++kr) {
+            rowb[kr] = ni;
+            int k = 0;
+            for (; k < nc && coll[k] / TT_UPT <= rowl[kr]; ++k) {
+              if (ni < maxi)
+                items[ni++] = make_int4(rowl[kr], coll[k], kr,
+                                        coll[k] / TT_UPT == rowl[kr] ? -1 : k);
+              else
+                bad = 1;
+            }
+            rown[kr] = k;
+          }
         }
         if (bad) atomicExch(err, TR_ERR_LISTS);
         s_nr = nr;
@@ -1059,11 +1036,11 @@ k_tridiag_tiled(double *A, double *Tm, int n, int nt, int pr, int pc, int maxr, 
       __syncthreads();
       j0_lists = J0;
     }
-    /* ---- A: as in k_tridiag, with column c read from the tiles ---- */
+    /* ---- A: as in the whole-column step, with column c read from the tiles ---- */
+    const ff2 tau_pf = s_tau_p, scale_pf = s_scale_p, e_pf = s_e_p;
     double *xcur = (c & 1) ? wbuf : vbuf, *xprev = (c & 1) ? vbuf : wbuf;
     double *ycur = ybuf + (int64_t)(c & 1) * n, *yprev = ybuf + (int64_t)((c + 1) & 1) * n;
     ff2 pacc = ZERO;
-    const ff2 tau_pf = s_tau_p, scale_pf = s_scale_p, e_pf = s_e_p;
     if (have_p && warp == TR_WARPS - 1) {
       /* y.v of step c-1: its index blocks' partial dots (from (c-1+1)/TT on), in order */
       const double *pprev = dotp + (size_t)((c + 1) & 1) * nt;
@@ -1151,94 +1128,118 @@ k_tridiag_tiled(double *A, double *Tm, int n, int nt, int pr, int pc, int maxr, 
       ff_store(swp + q, ZERO);
     }
     const int nr = s_nr, nc = s_nc, ni = s_ni;
-    for (int idx = threadIdx.x; idx < (nr + nc) * TT; idx += blockDim.x)
+    for (int idx = threadIdx.x; idx < nr * TT + nc * TT_U; idx += blockDim.x)
       ff_store(idx < nr * TT ? racc + idx : cacc + (idx - nr * TT), ZERO);
     __syncthreads();
-    for (int rb = 0; rb < ni; rb += TT_R) {
-      const int re = min(ni, rb + TT_R);
+    for (int rb = 0; rb < ni; rb += R) {
+      const int re = min(ni, rb + R);
       for (int u = warp; rb + u < re; u += TR_WARPS) {
         const int4 it = items[rb + u];
-        const int I = it.x, J = it.y, h = it.z & 1;
-        double *rs = rslot + (size_t)u * TT, *cs = cslot + (size_t)u * (TT / 2);
-        if (h == 0 && J == J0 && J0 * TT + TT / 2 <= c + 1) {
-          /* every column of this half is at or before c */
+        const int I = it.x, J = it.y / TT_UPT, j0 = (it.y - J * TT_UPT) * TT_U;
+        double *rs = rslot + (size_t)u * TT, *cs_ = cslot + (size_t)u * TT_U;
+        if (J == J0 && J0 * TT + j0 + TT_U <= c + 1) {
+          /* every column of this part is at or before c */
           ff_store(rs + 2 * lane, ZERO);
           ff_store(rs + 2 * lane + 1, ZERO);
-          ff_store(cs + lane, ZERO);
+          if (lane < TT_U) ff_store(cs_ + lane, ZERO);
         } else {
-          tt_half(Tm + tt_tile(I, J) * (TT * TT), I, J, h, I == J, have_p, svp, swp, svc, rs, cs,
-                  lane);
+          tt_part(Tm + tt_tile(I, J) * (TT * TT), I, J, j0, I == J, have_p, svp, swp, svc, rs,
+                  cs_, lane);
         }
       }
       __syncthreads();
-      /* the round's parts into the block's per-index-block sums, in item order */
+      /* the round's parts into the block's sums, in part order: tile row kr owns parts
+       * rowb[kr] .. rowb[kr] + rown[kr] - 1, its k-th column unit at rowb[kr] + k */
       for (int idx = threadIdx.x; idx < nr * TT; idx += blockDim.x) {
         const int kr = idx / TT, i = idx - kr * TT;
         ff2 s = ff_load(racc + idx);
-        for (int t = rb; t < re; ++t)
-          if ((items[t].z >> 1) == kr) s = ff_add(s, ff_load(rslot + (size_t)(t - rb) * TT + i));
+        const int t0 = max(rb, rowb[kr]), t1 = min(re, rowb[kr] + rown[kr]);
+        for (int t = t0; t < t1; ++t) s = ff_add(s, ff_load(rslot + (size_t)(t - rb) * TT + i));
         ff_store(racc + idx, s);
       }
-      for (int idx = threadIdx.x; idx < nc * TT; idx += blockDim.x) {
-        const int kc = idx / TT, j = idx - kc * TT, hh = j / (TT / 2), jj = j - hh * (TT / 2);
+      for (int idx = threadIdx.x; idx < nc * TT_U; idx += blockDim.x) {
+        const int kc = idx / TT_U, j = idx - kc * TT_U;
         ff2 s = ff_load(cacc + idx);
-        for (int t = rb; t < re; ++t) {
-          const int4 it = items[t];
-          if (it.w == kc && (it.z & 1) == hh)
-            s = ff_add(s, ff_load(cslot + (size_t)(t - rb) * (TT / 2) + jj));
+        for (int kr = 0; kr < nr; ++kr) {
+          const int t = rowb[kr] + kc;
+          if (kc < rown[kr] && coll[kc] / TT_UPT != rowl[kr] && t >= rb && t < re)
+            s = ff_add(s, ff_load(cslot + (size_t)(t - rb) * TT_U + j));
         }
         ff_store(cacc + idx, s);
       }
       __syncthreads();
     }
-    /* publish the block's parts: row parts of its tile rows, column parts of its tile columns */
+    /* publish the block's sums: row parts of its tile rows, column parts of its units; then
+     * one arrival per published sum on its index block's counter */
     if (active) {
       for (int idx = threadIdx.x; idx < nr * TT; idx += blockDim.x) {
         const int kr = idx / TT, i = idx - kr * TT;
         ff_store(prow + ((size_t)rowl[kr] * pc + gb) * TT + i, ff_load(racc + idx));
       }
-      for (int idx = threadIdx.x; idx < nc * TT; idx += blockDim.x) {
-        const int kc = idx / TT, j = idx - kc * TT;
-        ff_store(pcol + ((size_t)coll[kc] * pr + ga) * TT + j, ff_load(cacc + idx));
+      for (int idx = threadIdx.x; idx < nc * TT_U; idx += blockDim.x) {
+        const int kc = idx / TT_U, j = idx - kc * TT_U;
+        ff_store(pcol + ((size_t)coll[kc] * pr + ga) * TT_U + j, ff_load(cacc + idx));
       }
     }
-    if (threadIdx.x == 0) s_nl = 0;
     __syncthreads();
     if (active) {
-      const unsigned ktarget = (unsigned)(pr + pc) * (unsigned)(c + 1);
-      int K = -1;
       if ((int)threadIdx.x < nr) /* nr, nc <= 512 (host check) */
-        K = rowl[threadIdx.x];
+        red_release_gpu(kcnt + rowl[threadIdx.x], 1u);
       else if (threadIdx.x >= 512 && (int)threadIdx.x - 512 < nc)
-        K = coll[threadIdx.x - 512];
-      if (K >= 0 && atom_add_acq_rel_gpu(kcnt + K, 1u) + 1u == ktarget)
-        lastl[atomicAdd(&s_nl, 1)] = K;
+        red_release_gpu(kcnt + coll[threadIdx.x - 512] / TT_UPT, 1u);
     }
-    __syncthreads();
+    /* index blocks K = b, b + G, ...: wait for their arrivals, then y over the TT indices
+     * (pc row parts, then pr column parts of the index's unit, in order: 16 threads per index
+     * with two terms each and a fixed shuffle tree) and the partial y.v */
     {
-      /* the index blocks this block completed: y over the block's TT indices (pc row parts,
-       * then pr column parts, in order) and its partial y.v */
-      const int nl = s_nl;
-      for (int s0 = 0; s0 < nl; s0 += TR_THREADS / TT) {
-        const int s = s0 + (int)(threadIdx.x / TT), i = threadIdx.x & (TT - 1);
+      const unsigned ktarget = arrivals * (unsigned)(c + 1);
+      for (int K = b; K < nt; K += G) {
+        if (K < J0) continue;
+        if (threadIdx.x == 0) {
+          int ok = 1;
+          volatile int *verr = err;
+          const uint64_t t0 = globaltimer_ns();
+          for (unsigned it = 1; ld_acquire_gpu(kcnt + K) < ktarget; ++it) {
+            if ((it & 63u) == 0) {
+              if (*verr) {
+                ok = 0;
+                break;
+              }
+              if (globaltimer_ns() - t0 > GP_WAIT_NS) {
+                atomicExch(err, TR_ERR_WAIT);
+                ok = 0;
+                break;
+              }
+            }
+          }
+          s_ok = ok;
+        }
+        __syncthreads();
+        if (!s_ok) return;
+        const int i = threadIdx.x >> 4, g = threadIdx.x & 15;
+        const int nterm = pc + pr;
+        ff2 y = ZERO;
+        for (int t = g; t < nterm; t += 16) {
+          const double *src = t < pc ? prow + ((size_t)K * pc + t) * TT + i
+                                     : pcol + ((size_t)(K * TT_UPT + i / TT_U) * pr + (t - pc)) *
+                                                  TT_U + (i & (TT_U - 1));
+          y = ff_add(y, ff_load(src));
+        }
+        for (int o = 8; o; o >>= 1) y = ff_add(y, ff_shfl_xor(y, o));
+        const int q = K * TT + i;
         ff2 dv = ZERO;
-        if (s < nl) {
-          const int K = lastl[s];
-          ff2 y = ZERO;
-          const double *p1 = prow + (size_t)K * pc * TT + i;
-          for (int g = 0; g < pc; ++g) y = ff_add(y, ff_load(p1 + (size_t)g * TT));
-          const double *p2 = pcol + (size_t)K * pr * TT + i;
-          for (int g = 0; g < pr; ++g) y = ff_add(y, ff_load(p2 + (size_t)g * TT));
-          const int q = K * TT + i;
+        if (g == 0) {
           if (q < n) ff_store(ycur + q, y);
           dv = ff_mul(y, ff_load(svc + q));
         }
-        for (int o = 16; o; o >>= 1) dv = ff_add(dv, ff_shfl_xor(dv, o));
+        dv = ff_add(dv, ff_shfl_xor(dv, 16)); /* the warp's two indices, lanes 0 and 16 */
         if (lane == 0) s_dot[warp] = dv;
         __syncthreads();
-        if (threadIdx.x < TR_THREADS / TT && s0 + (int)threadIdx.x < nl)
-          ff_store(dotp + (size_t)(c & 1) * nt + lastl[s0 + threadIdx.x],
-                   ff_add(s_dot[2 * threadIdx.x], s_dot[2 * threadIdx.x + 1]));
+        if (threadIdx.x < 32) {
+          ff2 t = s_dot[threadIdx.x];
+          for (int o = 16; o; o >>= 1) t = ff_add(t, ff_shfl_xor(t, o));
+          if (threadIdx.x == 0) ff_store(dotp + (size_t)(c & 1) * nt + K, t);
+        }
         __syncthreads();
       }
     }
@@ -1254,20 +1255,20 @@ k_tridiag_tiled(double *A, double *Tm, int n, int nt, int pr, int pc, int maxr, 
     have_p = true;
   }
   if (cs < n - 1) {
-    /* the switch to whole columns: the trailing block (indices >= cs) of the block's tiles
+    /* the switch to whole columns: the trailing block (indices >= cs) of the block's parts
      * into A as float-float pairs, both triangles (the pending update of step cs-1 is applied
-     * by the first whole-matrix step, as in k_tridiag) */
+     * by the first whole-column step) */
     const int ni = s_ni;
-    for (int64_t idx = threadIdx.x; idx < (int64_t)ni * (TT * TT / 2); idx += blockDim.x) {
-      const int u = (int)(idx / (TT * TT / 2)), rem = (int)(idx - (int64_t)u * (TT * TT / 2));
+    for (int64_t idx = threadIdx.x; idx < (int64_t)ni * (TT * TT_U); idx += blockDim.x) {
+      const int u = (int)(idx / (TT * TT_U)), rem = (int)(idx - (int64_t)u * (TT * TT_U));
       const int j = rem / TT, i = rem - j * TT;
       const int4 it = items[u];
-      const int h = it.z & 1;
-      const int r = it.x * TT + i, q = it.y * TT + h * (TT / 2) + j;
+      const int J = it.y / TT_UPT, jt = (it.y - J * TT_UPT) * TT_U + j;
+      const int r = it.x * TT + i, q = J * TT + jt;
       if (r >= cs && q >= cs && r < n && q < n) {
-        const double v = Tm[(tt_tile(it.x, it.y) * TT + h * (TT / 2) + j) * TT + i];
+        const double v = Tm[(tt_tile(it.x, J) * TT + jt) * TT + i];
         A[(int64_t)q * n + r] = v;
-        if (it.x != it.y) A[(int64_t)r * n + q] = v;
+        if (it.x != J) A[(int64_t)r * n + q] = v;
       }
     }
     target += G;
@@ -1682,14 +1683,14 @@ __global__ void k_reverse(const double *w, double *out, int n)
     out[i] = w[n - 1 - i];
 }
 
-/* the pr x pc block grid of k_tridiag_tiled: the largest pr * pc <= G with both at most
- * TT_MAXG (ties: the smaller pr + pc, so that an index block has fewer parts) */
+/* the pr x pc block grid of k_tridiag_tiled: the largest pr * pc <= G with pr <= pc, both at
+ * most TT_MAXG (ties: the smaller pr + pc, so that an index block has fewer parts) */
 static void tt_grid(int G, int *pr, int *pc)
 {
   int best = 0;
   *pr = *pc = 0;
-  for (int c = 1; c * c <= G; ++c) {
-    const int r = G / c;
+  for (int r = 1; r * r <= G; ++r) {
+    const int c = G / r;
     if (r > TT_MAXG || c > TT_MAXG) continue;
     if (r * c > best || (r * c == best && r + c < *pr + *pc)) {
       best = r * c;
@@ -1699,26 +1700,65 @@ static void tt_grid(int G, int *pr, int *pc)
   }
 }
 
-/* a block's most tile rows, tile columns and tile halves over every first active tile index
- * (the lists k_tridiag_tiled builds with tt_assign) */
-static void tt_bounds(int nt, int pr, int pc, int *maxr, int *maxc, int *maxi)
+/* the assignment tables of k_tridiag_tiled for every first active tile index J0 (row J0 of
+ * rgt [nt][nt] and cgt [nt][nt*TT_UPT]): the active tile rows go to the pr row groups longest
+ * first, each to the group with the fewest parts so far (ties: the lower group); then the
+ * column units, longest first, each to the column group whose largest block part count grows
+ * least (ties: the smaller growth of the sum of squares, then the lower group).  Also the
+ * bounds of a block's tile rows, column units and parts over all J0. */
+static void tt_tables(int nt, int pr, int pc, std::vector<unsigned char> &rgt,
+                      std::vector<unsigned char> &cgt, int *maxr, int *maxc, int *maxi)
 {
-  std::vector<unsigned char> rg((size_t)nt), cg((size_t)nt);
-  std::vector<int> cnt((size_t)pr * pc), nrow((size_t)pr), ncol((size_t)pc);
-  int mr = 1, mc = 1, mi = 2;
+  const int nu = nt * TT_UPT;
+  rgt.assign((size_t)nt * nt, 0);
+  cgt.assign((size_t)nt * nu, 0);
+  std::vector<int> sum((size_t)pr), L((size_t)pr * pc), suf((size_t)(nt + 1) * pr),
+      nrow((size_t)pr), ncol((size_t)pc);
+  int mr = 1, mc = 1, mi = 1;
   for (int J0 = 0; J0 < nt; ++J0) {
-    tt_assign(nt, J0, pr, pc, rg.data(), cg.data());
-    std::fill(cnt.begin(), cnt.end(), 0);
-    std::fill(nrow.begin(), nrow.end(), 0);
-    std::fill(ncol.begin(), ncol.end(), 0);
-    for (int I = J0; I < nt; ++I) {
-      ++nrow[rg[I]];
-      ++ncol[cg[I]];
-      for (int J = J0; J <= I; ++J) cnt[(size_t)rg[I] * pc + cg[J]] += 2;
+    unsigned char *rg = &rgt[(size_t)J0 * nt], *cg = &cgt[(size_t)J0 * nu];
+    std::fill(sum.begin(), sum.end(), 0);
+    for (int I = nt - 1; I >= J0; --I) {
+      int best = 0;
+      for (int g = 1; g < pr; ++g)
+        if (sum[g] < sum[best]) best = g;
+      rg[I] = (unsigned char)best;
+      sum[best] += TT_UPT * (I - J0 + 1);
     }
+    /* suf[J][a]: active tile rows I >= J in row group a (the parts of a unit of tile column J) */
+    for (int g = 0; g < pr; ++g) suf[(size_t)nt * pr + g] = 0;
+    for (int J = nt - 1; J >= J0; --J) {
+      for (int g = 0; g < pr; ++g) suf[(size_t)J * pr + g] = suf[(size_t)(J + 1) * pr + g];
+      ++suf[(size_t)J * pr + rg[J]];
+    }
+    std::fill(L.begin(), L.end(), 0);
+    std::fill(ncol.begin(), ncol.end(), 0);
+    for (int u = J0 * TT_UPT; u < nu; ++u) {
+      const int *v = &suf[(size_t)(u / TT_UPT) * pr];
+      int best = 0;
+      long long bmax = -1, bsq = 0;
+      for (int g = 0; g < pc; ++g) {
+        long long mx = 0, sq = 0;
+        for (int a = 0; a < pr; ++a) {
+          const long long l = L[(size_t)a * pc + g];
+          mx = std::max(mx, l + v[a]);
+          sq += 2 * l * v[a] + (long long)v[a] * v[a];
+        }
+        if (bmax < 0 || mx < bmax || (mx == bmax && sq < bsq)) {
+          bmax = mx;
+          bsq = sq;
+          best = g;
+        }
+      }
+      cg[u] = (unsigned char)best;
+      ++ncol[best];
+      for (int a = 0; a < pr; ++a) L[(size_t)a * pc + best] += v[a];
+    }
+    std::fill(nrow.begin(), nrow.end(), 0);
+    for (int I = J0; I < nt; ++I) ++nrow[rg[I]];
     for (int g = 0; g < pr; ++g) mr = std::max(mr, nrow[g]);
     for (int g = 0; g < pc; ++g) mc = std::max(mc, ncol[g]);
-    for (size_t k = 0; k < cnt.size(); ++k) mi = std::max(mi, cnt[k]);
+    for (size_t k = 0; k < L.size(); ++k) mi = std::max(mi, L[k]);
   }
   *maxr = mr;
   *maxc = mc;
@@ -1816,9 +1856,31 @@ int gp_eig_sym(gp_ctx *ctx, double *A_in, int32_t n, int32_t nvec, double *d_eva
     tt_grid((int)G, &tt_pr, &tt_pc);
     tiled = tt_pr >= 1 && tt_pc >= 1;
   }
+  int tt_R = 0;
+  if (tiled && !(ctx->d_tt && ctx->tt_n == n && ctx->tt_G == (int)G)) {
+    /* the assignment tables, once per order and grid */
+    std::vector<unsigned char> rgt, cgt;
+    tt_tables(nt, tt_pr, tt_pc, rgt, cgt, &ctx->tt_maxr, &ctx->tt_maxc, &ctx->tt_maxi);
+    ctx->tt_n = 0;
+    int rc3 = gp_realloc(ctx, (void **)&ctx->d_tt, rgt.size() + cgt.size());
+    if (rc3) return rc3;
+    GP_CUDA(ctx, gp_memcpy(ctx, ctx->d_tt, rgt.data(), rgt.size(), cudaMemcpyHostToDevice,
+                           ctx->stream));
+    GP_CUDA(ctx, gp_memcpy(ctx, ctx->d_tt + rgt.size(), cgt.data(), cgt.size(),
+                           cudaMemcpyHostToDevice, ctx->stream));
+    GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->tt_n = n;
+    ctx->tt_G = (int)G;
+  }
   if (tiled) {
-    tt_bounds(nt, tt_pr, tt_pc, &tt_maxr, &tt_maxc, &tt_maxi);
-    tt_smem = tt_smem_bytes(nt, tt_maxr, tt_maxc, tt_maxi);
+    tt_maxr = ctx->tt_maxr;
+    tt_maxc = ctx->tt_maxc;
+    tt_maxi = ctx->tt_maxi;
+    /* parts per round: all of a block's parts in one round where shared memory allows */
+    tt_R = std::min(128, (tt_maxi + TR_WARPS - 1) / TR_WARPS * TR_WARPS);
+    while (tt_R > TR_WARPS && tt_smem_bytes(nt, tt_R, tt_maxr, tt_maxc, tt_maxi) > 220 * 1024)
+      tt_R -= TR_WARPS;
+    tt_smem = tt_smem_bytes(nt, tt_R, tt_maxr, tt_maxc, tt_maxi);
     tiled = tt_maxr <= 512 && tt_maxc <= 512 && tt_smem <= 220 * 1024;
   }
   if (tiled) {
@@ -1842,7 +1904,7 @@ int gp_eig_sym(gp_ctx *ctx, double *A_in, int32_t n, int32_t nvec, double *d_eva
   if (tiled) {
     const int64_t ntiles = (int64_t)nt * (nt + 1) / 2;
     const size_t tile_d = (size_t)ntiles * TT * TT;
-    const size_t part_d = (size_t)(tt_pr + tt_pc) * nt * TT;
+    const size_t part_d = (size_t)(tt_pr + tt_pc) * nt * TT; /* prow + pcol */
     const size_t tri_bytes = sizeof(double) * (tile_d + part_d + 2 * (size_t)nt) +
                              sizeof(unsigned) * (size_t)nt;
     int rc2 = gp_realloc(ctx, (void **)&ctx->d_tri, tri_bytes);
@@ -1866,9 +1928,11 @@ int gp_eig_sym(gp_ctx *ctx, double *A_in, int32_t n, int32_t nvec, double *d_eva
     }
     double *A = A_in, *pd2 = parts;
     int nn = n, nt_ = nt, cs = tt_cs;
+    const unsigned char *rgt = ctx->d_tt, *cgt = ctx->d_tt + (size_t)nt * nt;
     void *args[] = {&A,    &Tm,   &nn,   &nt_,  &tt_pr, &tt_pc, &tt_maxr, &tt_maxc,
-                    &tt_maxi, &cs, &d,   &e,    &tau,   &vbuf,  &wbuf,    &ybuf,
-                    &prow, &pcol, &dotp, &kcnt, &pd2,   &bar,   &d_err,   &phase};
+                    &tt_maxi, &tt_R, &cs, &rgt, &cgt,  &d,     &e,       &tau,
+                    &vbuf, &wbuf, &ybuf, &prow, &pcol, &dotp,  &kcnt,    &pd2,
+                    &bar,  &d_err, &phase};
     GP_CUDA(ctx, cudaEventRecord(ctx->ev_tr0, ctx->stream));
     GP_CUDA(ctx, cudaLaunchCooperativeKernel((const void *)k_tridiag_tiled, dim3((unsigned)G),
                                              dim3(TR_THREADS), args, tt_smem, ctx->stream));
@@ -1879,6 +1943,9 @@ int gp_eig_sym(gp_ctx *ctx, double *A_in, int32_t n, int32_t nvec, double *d_eva
     GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (herr == TR_ERR_LISTS)
       return gp_fail(ctx, GP_ERR_CUDA, "tiled tridiagonalisation: a block's tile lists overflowed");
+    if (herr == TR_ERR_WAIT)
+      return gp_fail(ctx, GP_ERR_TIMEOUT, "tiled tridiagonalisation: an index block's parts "
+                                          "did not arrive in time");
     if (herr) return gp_fail(ctx, GP_ERR_TIMEOUT, "tridiagonalisation grid barrier timed out");
     float tms = 0.f;
     GP_CUDA(ctx, cudaEventElapsedTime(&tms, ctx->ev_tr0, ctx->ev_tr1));

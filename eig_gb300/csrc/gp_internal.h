@@ -59,6 +59,8 @@ struct gp_ctx {
   double *d_evals;       /* [nrows] */
   double *d_evecs;       /* [nvec*nrows] top vectors, descending */
   double *d_tri;         /* the tiled tridiagonalisation's lower-triangle tiles and parts */
+  unsigned char *d_tt;   /* its assignment tables, for order tt_n on a grid of tt_G blocks */
+  int tt_n, tt_G, tt_maxr, tt_maxc, tt_maxi;
   int keep_gram;         /* gp_keep_gram: copy the scaled Gram before the eigensolve */
   double *d_xtx_keep;    /* [nrows*nrows] that copy (the relatedness scan reads it) */
   int64_t keep_cap;

@@ -63,6 +63,8 @@ def test_tridiag_roofline_figures():
     assert abs(roof["algorithmic_bytes"] - alg) < 1.0
     assert abs(roof["achieved"] - alg / 0.150 / 1e9) < 1e-6
     assert abs(roof["frac"] - roof["achieved"] / 6000.0) < 1e-12
-    assert roof["traffic"] == bench.tridiag_traffic(5000) and roof["traffic"] > alg
+    # the tiled kernel's lower triangle mostly stays in L2: DRAM traffic below the algorithmic
+    # bytes (the committed ncu summary's figure, 130 GB against 333 GB)
+    assert roof["traffic"] == bench.tridiag_traffic(5000) and 0 < roof["traffic"] < alg
     assert bench.tridiag_traffic(4000) is None
     assert bench.tridiag_roofline({"tridiag_n": 5000, "tridiag_ms": 0.0}, {}, "x") is None

@@ -857,6 +857,72 @@ __global__ void k_tri_to_tiles(const double *A, int n, int nt, double *Tm)
   }
 }
 
+/* a - (p q + r s) in float-float (the rank-2 update of one element): the two high products
+ * exactly (TwoProd with FMA), their cross terms and the errors of two TwoSums gathered in one
+ * FP32 term, one renormalisation: 27 FP32 operations against 30 for two ff_fma, of the same
+ * error order.  With p = r = 0 or q = s = 0 it returns a normalised a unchanged. */
+__device__ __forceinline__ ff2 ff_sub2prod(ff2 a, ff2 p, ff2 q, ff2 r, ff2 s)
+{
+  const float p1 = __fmul_rn(p.h, q.h);
+  float e = __fmaf_rn(p.h, q.h, -p1);
+  e = __fmaf_rn(p.h, q.l, e);
+  e = __fmaf_rn(p.l, q.h, e);
+  const float p2 = __fmul_rn(r.h, s.h);
+  e = __fadd_rn(__fmaf_rn(r.h, s.h, -p2), e);
+  e = __fmaf_rn(r.h, s.l, e);
+  e = __fmaf_rn(r.l, s.h, e);
+  const float t1 = __fsub_rn(a.h, p1);
+  const float b1 = __fsub_rn(t1, a.h);
+  const float r1 = __fadd_rn(__fsub_rn(a.h, __fsub_rn(t1, b1)), __fsub_rn(-p1, b1));
+  const float t2 = __fsub_rn(t1, p2);
+  const float b2 = __fsub_rn(t2, t1);
+  const float r2 = __fadd_rn(__fsub_rn(t1, __fsub_rn(t2, b2)), __fsub_rn(-p2, b2));
+  const float low = __fadd_rn(__fsub_rn(a.l, e), __fadd_rn(r1, r2));
+  const float h = __fadd_rn(t2, low);
+  return ff_make(h, __fsub_rn(low, __fsub_rn(h, t2)));
+}
+
+/* a x + b y in float-float: two exact high products, one TwoSum, the cross terms and errors
+ * in one FP32 term (19 FP32 operations against 22 for ff_mul + ff_fma) */
+__device__ __forceinline__ ff2 ff_dot2(ff2 a, ff2 x, ff2 b, ff2 y)
+{
+  const float p1 = __fmul_rn(a.h, x.h);
+  float e = __fmaf_rn(a.h, x.h, -p1);
+  e = __fmaf_rn(a.h, x.l, e);
+  e = __fmaf_rn(a.l, x.h, e);
+  const float p2 = __fmul_rn(b.h, y.h);
+  e = __fadd_rn(__fmaf_rn(b.h, y.h, -p2), e);
+  e = __fmaf_rn(b.h, y.l, e);
+  e = __fmaf_rn(b.l, y.h, e);
+  const float s = __fadd_rn(p1, p2);
+  const float bb = __fsub_rn(s, p1);
+  const float er = __fadd_rn(__fsub_rn(p1, __fsub_rn(s, bb)), __fsub_rn(p2, bb));
+  const float low = __fadd_rn(e, er);
+  const float h = __fadd_rn(s, low);
+  return ff_make(h, __fsub_rn(low, __fsub_rn(h, s)));
+}
+
+/* acc += a x with the accumulator left unnormalised (acc.h the running TwoSum of the high
+ * products, acc.l every lower-order term): 12 FP32 operations against 15 for ff_fma; over a
+ * short dot (16 terms here) its error stays of the order of the normalised accumulation's.
+ * ff_renorm makes the pair normalised again. */
+__device__ __forceinline__ ff2 ff_acc_lazy(ff2 acc, ff2 a, ff2 x)
+{
+  const float p = __fmul_rn(a.h, x.h);
+  float e = __fmaf_rn(a.h, x.h, -p);
+  e = __fmaf_rn(a.h, x.l, e);
+  e = __fmaf_rn(a.l, x.h, e);
+  const float s = __fadd_rn(acc.h, p);
+  const float bb = __fsub_rn(s, acc.h);
+  const float er = __fadd_rn(__fsub_rn(acc.h, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+  return ff_make(s, __fadd_rn(acc.l, __fadd_rn(e, er)));
+}
+__device__ __forceinline__ ff2 ff_renorm(ff2 a)
+{
+  const float h = __fadd_rn(a.h, a.l);
+  return ff_make(h, __fsub_rn(a.l, __fsub_rn(h, a.h)));
+}
+
 /* one part (TT_U columns from TT*J + j0) of tile (I, J) by one warp: the pending update of
  * step c-1 (have_p), written back; the row dots with v over these columns into rs[TT] (rows
  * 2 lane, 2 lane + 1); unless the tile is diagonal, the column dots with v over the tile's
@@ -884,17 +950,15 @@ __device__ __forceinline__ void tt_part(double *tile, int I, int J, int j0, bool
       const int col = col0 + cb + k;
       ff2 a0 = ff_make(a[k].x, a[k].y), a1 = ff_make(a[k].z, a[k].w);
       if (have_p) {
-        const ff2 nvc = ff_neg(ff_load(svp + col)), nwc = ff_neg(ff_load(swp + col));
-        a0 = ff_fma(pr0, nwc, a0);
-        a0 = ff_fma(qr0, nvc, a0);
-        a1 = ff_fma(pr1, nwc, a1);
-        a1 = ff_fma(qr1, nvc, a1);
+        const ff2 vpc = ff_load(svp + col), wpc = ff_load(swp + col);
+        a0 = ff_sub2prod(a0, pr0, wpc, qr0, vpc);
+        a1 = ff_sub2prod(a1, pr1, wpc, qr1, vpc);
         *reinterpret_cast<float4 *>(p0 + (size_t)(cb + k) * TT) = make_float4(a0.h, a0.l, a1.h, a1.l);
       }
       const ff2 vc = ff_load(svc + col);
-      ra0 = ff_fma(a0, vc, ra0);
-      ra1 = ff_fma(a1, vc, ra1);
-      cp[k] = ff_fma(a1, vr1, ff_mul(a0, vr0));
+      ra0 = ff_acc_lazy(ra0, a0, vc);
+      ra1 = ff_acc_lazy(ra1, a1, vc);
+      cp[k] = ff_dot2(a0, vr0, a1, vr1);
     }
     if (!diag) {
       /* reduce-scatter over the warp: lanes 8t..8t+7 end with column cb + t (lane bits 4 and 3
@@ -917,8 +981,8 @@ __device__ __forceinline__ void tt_part(double *tile, int I, int J, int j0, bool
       if ((lane & 7) == 0) ff_store(cs + cb + (lane >> 3), cp[0]);
     }
   }
-  ff_store(rs + 2 * lane, ra0);
-  ff_store(rs + 2 * lane + 1, ra1);
+  ff_store(rs + 2 * lane, ff_renorm(ra0));
+  ff_store(rs + 2 * lane + 1, ff_renorm(ra1));
 }
 
 /* shared-memory bytes of k_tridiag_tiled for round size R (parts per round) and the bounds of

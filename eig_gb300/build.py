@@ -32,7 +32,7 @@ CUDA_SOURCES = ["gp_api.cu", "gp_geno.cu", "gp_gram_f64.cu", "gp_geno_gemm_f64.c
                 "gp_gram_bf16.cu", "gp_fast.cu",
                 "gp_noalloc.cu", "gp_geno_tc.cu", "gp_eig.cu", "gp_serve.cu", "gp_convert.cu",
                 "gp_fst.cu", "gp_popfill.cu"]
-HOST_LIB_SOURCES = ["gp_smartpca.c"]
+HOST_LIB_SOURCES = ["gp_smartpca.c", "gp_tw.c"]
 # no FMA contraction in host code: the reference's host arithmetic is plain multiply-add
 # (aarch64 would otherwise fuse it)
 CFLAGS = ["-O2", "-fPIC", "-std=gnu11", "-Wall", "-Wno-unused-result", "-ffp-contract=off",
@@ -89,7 +89,7 @@ def build(verbose=False, force=False):
     lib = os.path.join(LIB, "libgpupca.so")
     if force or _newer(lib, objs):
         _run([nvcc] + ARCH + ["-shared", "-o", lib] + objs +
-             ["-lcusolver", "-lcublas", "-lcudart", "-lpthread"])
+             ["-lcusolver", "-lcublas", "-lcudart", "-lpthread", "-lm"])
     synth = os.path.join(LIB, "libgpsynth.so")
     ss = [os.path.join(HOST, "gp_synth.c"), os.path.join(HOST, "gp_stats.c")]
     if force or _newer(synth, ss + hdrs):

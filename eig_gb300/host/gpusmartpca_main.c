@@ -447,6 +447,56 @@ static double kurtosis_of(const double *a, int64_t n)
 }
 
 /*
+ * The mpstats line and the Tracy-Widom section of the log (smartpca.c:1306-1367; mpestimate
+ * :4532-4560): over the m eigenvalues of the last pass above 1e-6 (numgtz), the quartile line
+ * when m >= 10, then per eigenvalue its difference to the previous one, the statistic, the TW1
+ * tail and the effective number of markers (NA where fewer than nostatslim eigenvalues
+ * remain).  The statistics come from gp_twstats / gp_mpstats.
+ */
+static int tw_lines(const gp_run_result *r, int nostatslim)
+{
+  const int32_t n = r->nrows;
+  int32_t m = 0;
+  for (int32_t i = 0; i < n; ++i)
+    if (r->evals[i] > 0.000001) ++m;
+  if (m == 0) return 0;
+  double q[4];
+  if (gp_mpstats(r->evals, m, q) == GP_OK)
+    printf("mpstats: %9.3f%9.3f%9.3f%12.6f\n", q[0], q[1], q[2], q[3]);
+  double *tw = (double *)malloc(sizeof(double) * 3 * (size_t)m);
+  if (!tw) return -1;
+  double *pv = tw + m, *zn = pv + m;
+  if (gp_twstats(r->evals, m, n, -1.0, nostatslim, tw, pv, zn) != GP_OK) {
+    free(tw);
+    return -1;
+  }
+  printf("\n## Tracy-Widom statistics: rows: %d  cols: %d\n", n, r->ncols);
+  printf("%4s  %12s", "#N", "eigenvalue");
+  printf("%12s", "difference");
+  printf(" %9s %12s", "twstat", "p-value");
+  printf(" %9s", "effect. n");
+  printf("\n");
+  for (int32_t i = 0; i < m; ++i) {
+    printf("%4d  %12.6f", i + 1, r->evals[i]);
+    if (i == 0)
+      printf("%12s", "NA");
+    else
+      printf("%12.6f", r->evals[i] - r->evals[i - 1]);
+    if (pv[i] >= 0.0)
+      printf(" %9.3f %12.6g", tw[i], pv[i]);
+    else
+      printf(" %9s %12s", "NA", "NA");
+    if (zn[i] > 0.0)
+      printf(" %9.3f", zn[i]);
+    else
+      printf(" %9s", "NA");
+    printf("\n");
+  }
+  free(tw);
+  return 0;
+}
+
+/*
  * The kurtosis lines of the log (smartpca.c:1496-1501, :1541-1546): per eigenvector the
  * kurtosis of its SNP weights over the last pass's columns (zeros for the SNPs that pass
  * dropped) and of 10 x its entries over the rows.
@@ -561,7 +611,7 @@ int main(int argc, char **argv)
              *evalout = NULL, *outlierout = NULL, *poplistname = NULL, *prec = NULL,
              *grmout = NULL, *snpwtout = NULL;
   int32_t hiprec = 0, familynames = 1, hashcheck = 1, t = 0, xdata = -1, seed = 0,
-          grmbinary = 0;
+          grmbinary = 0, nostatslim = 10;
   gp_par_str(&pf, "genotypename:", &genotypename);
   gp_par_str(&pf, "snpname:", &snpname);
   gp_par_str(&pf, "indivname:", &indivname);
@@ -580,6 +630,7 @@ int main(int argc, char **argv)
   gp_par_int(&pf, "grmbinary:", &grmbinary);
   gp_par_int(&pf, "numeigs:", &o.numeigs);
   gp_par_int(&pf, "numoutevec:", &o.numeigs);
+  gp_par_int(&pf, "nostatslim:", &nostatslim);
   gp_par_int(&pf, "fancynorm:", &o.fancynorm);
   gp_par_int(&pf, "usenorm:", &o.fancynorm);
   gp_par_int(&pf, "altnormstyle:", &o.altnormstyle);
@@ -831,6 +882,11 @@ int main(int argc, char **argv)
   }
   if (ef != stdout) fclose(ef);
   if (!o.fastmode && nK > 0) {
+    if (tw_lines(&r, nostatslim < 3 ? 3 : nostatslim)) {
+      fprintf(stderr, "no memory for the Tracy-Widom statistics\n");
+      gp_close(ctx);
+      return 1;
+    }
     if (kurtosis_lines(&r, M)) {
       gp_close(ctx);
       return 1;

@@ -41,7 +41,8 @@ EXPORTED = ["gp_version", "gp_last_error", "gp_open", "gp_close", "gp_device_byt
             "gp_serve_submit_pca", "gp_serve_pca_stats", "gp_smartpca_footprint", "gp_release",
             "gp_keep_gram", "gp_relate", "gp_record_bytes", "gp_encode_records",
             "gp_last_encode_time", "gp_fst", "gp_set_blocks", "gp_set_row_pops",
-            "gp_lsqproj_pops", "gp_serve_loop_stats"]
+            "gp_lsqproj_pops", "gp_serve_loop_stats", "gp_twstats", "gp_tw_tail",
+            "gp_mpstats"]
 
 i32p = C.POINTER(C.c_int32)
 i64p = C.POINTER(C.c_int64)
@@ -152,6 +153,10 @@ def load_library():
                                           C.POINTER(RunResult), i64p]),
         "gp_serve_pca_stats": (C.c_int, [vp, i64p, i32p, i64p]),
         "gp_serve_loop_stats": (C.c_int, [vp, i32p, i64p, i64p, i64p]),
+        "gp_twstats": (C.c_int, [f64p, C.c_int32, C.c_int32, C.c_double, C.c_int32, f64p, f64p,
+                                 f64p]),
+        "gp_tw_tail": (C.c_double, [C.c_double]),
+        "gp_mpstats": (C.c_int, [f64p, C.c_int32, f64p]),
         "gp_smartpca_footprint": (C.c_int64, [C.c_int32, C.c_int64, C.c_int32, C.c_int32]),
         "gp_release": (C.c_int, [vp]),
         "gp_keep_gram": (C.c_int, [vp, C.c_int32]),
@@ -815,3 +820,33 @@ def host_register(a):
 
 def host_unregister(a):
     load_library().gp_host_unregister(a.ctypes.data_as(vp))
+
+
+def twstats(evals, nrows, nostatslim=10, znval=-1.0):
+    """smartpca's Tracy-Widom statistics of a spectrum (gp_twstats, host only): for each of the
+    eigenvalues above 1e-6 (descending) a (twstat, p-value, effective n) tuple, None where the
+    reference prints NA"""
+    lam = np.ascontiguousarray(evals, dtype=np.float64)
+    m = int(np.sum(lam > 1e-6))
+    tw, pv, zn = np.zeros(m), np.zeros(m), np.zeros(m)
+    lib = load_library()
+    rc = lib.gp_twstats(ptr(lam, C.c_double), m, int(nrows), float(znval), int(nostatslim),
+                        ptr(tw, C.c_double), ptr(pv, C.c_double), ptr(zn, C.c_double))
+    if rc != GP_OK:
+        raise GpuError("gp_twstats failed (%d)" % rc)
+    return [None if pv[i] < 0.0 else (float(tw[i]), float(pv[i]), float(zn[i]))
+            for i in range(m)]
+
+
+def tw_tail(x):
+    """the right tail of TW1 at x as smartpca reads it (gp_tw_tail, host only)"""
+    return float(load_library().gp_tw_tail(float(x)))
+
+
+def mpstats(evals):
+    """the mpstats quartiles of the eigenvalues above 1e-6 (gp_mpstats), None below 10"""
+    lam = np.ascontiguousarray(evals, dtype=np.float64)
+    m = int(np.sum(lam > 1e-6))
+    q = np.zeros(4)
+    rc = load_library().gp_mpstats(ptr(lam, C.c_double), m, ptr(q, C.c_double))
+    return None if rc != GP_OK else [float(v) for v in q]

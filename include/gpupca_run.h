@@ -104,6 +104,26 @@ int gp_smartpca_run(gp_ctx *ctx, const gp_smartpca_opts *o, const gp_panel *p,
 /* set the handle's error text (used by host code layered on the ABI) and return code */
 int gp_fail_msg(gp_ctx *ctx, int code, const char *fmt, ...);
 
+/* Tracy-Widom statistics of a spectrum, as smartpca's log prints them
+ * (src/eigensrc/smartpca.c:1336-1366; dotwcalc src/nicksrc/statsubs.c:1680-1725): lambda[0..m)
+ * the positive eigenvalues of the last pass in descending order (numgtz, > 1e-6), nrows the
+ * pass's samples, znval the fixed number of markers (<= 0: estimated per eigenvalue, the
+ * default), nostatslim the shortest tail of the spectrum that gets a statistic (smartpca's
+ * default 10).  For each i: twstat[i] (Johnstone's normalisation of lambda[i] within
+ * lambda[i..m)), pvalue[i] (the right tail of TW1 there, computed on the host; see gp_tw.c)
+ * and effn[i] (the effective number of markers); all three -1 where the reference prints NA.
+ * Host only; no device is touched. */
+int gp_twstats(const double *lambda, int32_t m, int32_t nrows, double znval,
+               int32_t nostatslim, double *twstat, double *pvalue, double *effn);
+/* the right tail of TW1 at x as smartpca reads it: 1 below -8, the cubic Hermite
+ * interpolant of TW1's tail and density on -8.0, -7.9, ..., 8.0 between (statsubs.c:1811-1905),
+ * and from 8 on the Margetis-Edelman density (the reference's own value there) */
+double gp_tw_tail(double x);
+/* the mpstats line (mpestimate, smartpca.c:4532-4560): the 0.25, 0.5 and 0.75 quartiles of
+ * lambda[0..m) (linear interpolation of the sorted values at q (m-1)) and (q3 - q1) / q2 in
+ * out4; returns 1 (nothing printed by the reference) when m < 10 */
+int gp_mpstats(const double *lambda, int32_t m, double *out4);
+
 #ifdef __cplusplus
 }
 #endif

@@ -657,3 +657,145 @@ def kurtosis(a):
         y4 += v * v
     return y4 / n
 
+
+
+# ---------------------------------------------------------------------------------------
+# Tracy-Widom statistics of the log (src/eigensrc/smartpca.c:1306-1367): the statistic and
+# effective number of markers of dotwcalc (src/nicksrc/statsubs.c:1680-1725) with twnorm
+# (:1658-1677), and the TW1 right tail read as gettw does (:1811-1905: cubic Hermite between
+# the points -8.0, -7.9, ..., 8.0 of a tail/density table; 1 below it; from 8 on the
+# Margetis-Edelman density, which the reference returns there).  The table is computed here
+# with scipy's Airy function and numpy determinants: F1(s) = det(I - K_s) on L2(0, inf),
+# K_s(x, y) = Ai(x + y + s) (Ferrari & Spohn 2005), Gauss-Legendre Nystrom discretisation
+# (Bornemann 2010), density F1 * d/ds log det from Jacobi's formula.
+
+_TW = None
+
+
+def tw1(s, m=80):
+    """(right tail, density) of TW1 at s"""
+    from scipy.special import airy
+    L = 16.0 - s if s < 16.0 else 4.0
+    z, w = np.polynomial.legendre.leggauss(m)
+    x = 0.5 * L * (z + 1.0)
+    w = 0.5 * L * w
+    sw = np.sqrt(w)
+    arg = x[:, None] + x[None, :] + s
+    ai, aip, _, _ = airy(arg)
+    K = sw[:, None] * ai * sw[None, :]
+    Kp = sw[:, None] * aip * sw[None, :]
+    if s >= 3.0:
+        # log det(I - K) = -sum tr(K^n)/n where K is small (keeps a small tail's accuracy)
+        ev = np.linalg.eigvalsh((K + K.T) * 0.5)
+        logdet = float(np.sum(np.log1p(-ev)))
+    else:
+        sign, logdet = np.linalg.slogdet(np.eye(m) - K)
+    dlog = -float(np.trace(np.linalg.solve(np.eye(m) - K, Kp)))
+    F = np.exp(logdet)
+    return float(-np.expm1(logdet)), float(F * dlog)
+
+
+def _tw_table():
+    global _TW
+    if _TW is None:
+        xs = np.round(np.arange(161) * 0.1 - 8.0, 1)
+        vals = np.array([tw1(float(x)) for x in xs])
+        _TW = (xs, vals[:, 0], vals[:, 1])
+    return _TW
+
+
+def _first_above(tab, lo, hi, val):
+    """statsubs.c fgtx: the bisection for the first table entry above val"""
+    if val >= tab[hi]:
+        return hi + 1
+    if val < tab[lo]:
+        return lo
+    k = (lo + hi) // 2
+    if val <= tab[k]:
+        return _first_above(tab, lo + 1, k, val)
+    return _first_above(tab, k, hi - 1, val)
+
+
+def tw_tail(x):
+    xs, tail, dens = _tw_table()
+    n = len(xs)
+    k = _first_above(xs, 0, n - 1, x)
+    if k <= 0:
+        return 1.0
+    if k >= n:
+        if x <= 0.0:
+            return 0.0
+        return float(np.exp(-0.25 * np.log(x) - 2.0 * x ** 1.5 / 3.0 - np.log(4.0 * np.sqrt(np.pi))))
+    x0, x1 = xs[k - 1], xs[k]
+    inc = x1 - x0
+    y = (x - x0) / inc
+    a0, a1 = tail[k - 1], -dens[k - 1] * inc
+    cc0, cc1 = tail[k] - (a0 + a1), -dens[k] * inc - a1
+    a2, a3 = 3 * cc0 - cc1, cc1 - 2 * cc0
+    return float(((a3 * y + a2) * y + a1) * y + a0)
+
+
+def _twnorm(lam, p, n):
+    if n < 0 or p < 0:
+        return -10.0
+    if n < p:
+        return _twnorm(lam, n, p)
+    y1 = np.sqrt(n - 1.0) + np.sqrt(p)
+    mu = y1 * y1
+    phi = y1 * (1.0 / np.sqrt(n - 1.0) + 1.0 / np.sqrt(p)) ** (1.0 / 3.0)
+    return (lam - mu) / phi
+
+
+def twstats(lam, nostatslim=10):
+    """per positive eigenvalue (descending, > 1e-6): (twstat, p-value, effective n), None
+    where the reference prints NA"""
+    lam = np.asarray(lam, dtype=np.float64)
+    m = int(np.sum(lam > 1e-6))
+    out = []
+    for i in range(m):
+        t = lam[i:m]
+        if len(t) < nostatslim or t.sum() <= 0.0:
+            out.append(None)
+            continue
+        y = len(t) / float(sum(t))
+        e = t * y
+        zn = len(t) * (len(t) + 2) / (float(sum(e * e)) - len(t))
+        tw = _twnorm(e[0] * zn, float(len(t)), zn)
+        out.append((tw, tw_tail(tw), zn))
+    return out
+
+
+def mpstats(lam):
+    """the mpstats line (mpestimate smartpca.c:4532-4560): quartiles 0.25, 0.5, 0.75 of the
+    positive eigenvalues and (q3 - q1) / q2, or None for fewer than 10"""
+    lam = np.asarray(lam, dtype=np.float64)
+    t = np.sort(lam[lam > 1e-6])
+    n = len(t)
+    if n < 10:
+        return None
+    q = [float(np.interp(f * (n - 1), np.arange(n), t)) for f in (0.25, 0.5, 0.75)]
+    return q + [(q[2] - q[0]) / q[1]]
+
+
+def tw_lines(lam, nrows, ncols, nostatslim=10):
+    """the log's mpstats line and Tracy-Widom section as text"""
+    lam = np.asarray(lam, dtype=np.float64)
+    m = int(np.sum(lam > 1e-6))
+    lines = []
+    mp = mpstats(lam)
+    if mp is not None:
+        lines.append("mpstats: %9.3f%9.3f%9.3f%12.6f" % tuple(mp))
+    lines.append("")
+    lines.append("## Tracy-Widom statistics: rows: %d  cols: %d" % (nrows, ncols))
+    lines.append("%4s  %12s%12s %9s %12s %9s" % ("#N", "eigenvalue", "difference", "twstat",
+                                                 "p-value", "effect. n"))
+    st = twstats(lam, nostatslim)
+    for i in range(m):
+        s = "%4d  %12.6f" % (i + 1, lam[i])
+        s += "%12s" % "NA" if i == 0 else "%12.6f" % (lam[i] - lam[i - 1])
+        if st[i] is None:
+            s += " %9s %12s %9s" % ("NA", "NA", "NA")
+        else:
+            s += " %9.3f %12.6g %9.3f" % st[i]
+        lines.append(s)
+    return lines

@@ -360,3 +360,26 @@ def kurtosis_lines(text):
                 break
     return out
 
+
+
+def tw_section(text):
+    """the log's mpstats quartiles (or None) and Tracy-Widom rows: per row (index, eigenvalue,
+    difference or None, twstat or None, p-value or None, effective n or None), plus the
+    section's (rows, cols); a section that runs to the end of a stored log that was cut short
+    returns only the rows it holds"""
+    lines = text.splitlines()
+    mp, rows, shape = None, [], None
+    for k, l in enumerate(lines):
+        if l.startswith("mpstats:"):
+            mp = [float(v) for v in l.split()[1:]]
+        if l.startswith("## Tracy-Widom statistics:"):
+            t = l.split()
+            shape = (int(t[4]), int(t[6]))
+            for r in lines[k + 2:]:
+                f = r.split()
+                if len(f) != 6 or not f[0].isdigit():
+                    break
+                val = [None if v == "NA" else float(v) for v in f[2:]]
+                rows.append((int(f[0]), float(f[1])) + tuple(val))
+            break
+    return mp, shape, rows

@@ -204,6 +204,20 @@ def test_cli_dropin_matches_reference_text(case, tmp_path):
     assert [k[0] for k in mine_k] == [k[0] for k in want_k] and len(want_k) > 0
     assert all(abs(a[1] - b[1]) <= 1.01e-3 and abs(a[2] - b[2]) <= 1.01e-3
                for a, b in zip(mine_k, want_k))
+    # the mpstats line and the Tracy-Widom section: eigenvalues at the printed 6 decimals,
+    # statistics and effective n at 3 decimals (1.01e-3: the GPU eigenvalues differ from the
+    # reference's in the 13th digit, which can move a printed last digit), p-values 1e-4
+    from tests.goldens import tw_section
+    mine_mp, mine_shape, mine_tw = tw_section(out.stdout)
+    want_mp, want_shape, want_tw = tw_section(open(d / "ref.log").read())
+    assert mine_shape == want_shape and len(mine_tw) == len(want_tw) > 0
+    assert all(abs(a - b) <= 1.01e-3 for a, b in zip(mine_mp, want_mp))
+    for a, b in zip(mine_tw, want_tw):
+        assert a[0] == b[0] and abs(a[1] - b[1]) <= 1.01e-6
+        assert (a[3] is None) == (b[3] is None) and (a[5] is None) == (b[5] is None)
+        if b[3] is not None:
+            assert abs(a[3] - b[3]) <= 1.01e-3 and abs(a[5] - b[5]) <= 1.01e-3 * max(1.0, b[5] * 1e-6)
+            assert abs(a[4] - b[4]) <= 1e-4 * max(b[4], 1e-6)
     mine_b = eigbestsnp_lines(out.stdout)
     want_b = eigbestsnp_lines(open(d / "ref.log").read())
     assert [m[:4] for m in mine_b] == [w[:4] for w in want_b]

@@ -237,3 +237,65 @@ def test_oracle_kurtosis_lines_match_reference(case):
         assert abs(O.kurtosis(r["ffvecs"][j - 1]) - ks) <= 5.0001e-4
         assert abs(O.kurtosis(10.0 * r["evecs"][j - 1]) - ki) <= 5.0001e-4
 
+
+
+def _tw_logs():
+    """golden logs with a Tracy-Widom section whose spectrum is stored in full"""
+    out = []
+    for case in sorted(os.listdir(GOLDEN)):
+        d = os.path.join(GOLDEN, case)
+        for name in sorted(os.listdir(d)) if os.path.isdir(d) else []:
+            if not (name.startswith("ref") and name.endswith(".log")):
+                continue
+            ev = os.path.join(d, name[:-4] + ".eval")
+            if os.path.exists(ev) and "Tracy-Widom" in open(os.path.join(d, name)).read():
+                out.append((case, name))
+    return out
+
+
+TW_LOGS = _tw_logs()
+
+
+def log_cut(d, name):
+    """the stored log ends inside its Tracy-Widom section (the full-size cases keep only the
+    head of the reference's log)"""
+    last = open(os.path.join(d, name)).read().splitlines()[-1].split()
+    return len(last) == 6 and last[0].isdigit()
+
+
+def compare_tw(mine_mp, mine_rows, want_mp, want_rows, prefix=False):
+    """text-exact statistics (3 decimals) and effective n; p-values within 1e-5 relative (the
+    6th significant digit of a value on a rounding boundary); prefix: the stored log was cut
+    short inside the section, so only its first rows are compared"""
+    assert (mine_mp is None) == (want_mp is None)
+    if want_mp is not None:
+        assert ["%.3f" % v for v in mine_mp[:3]] == ["%.3f" % v for v in want_mp[:3]]
+        assert "%.6f" % mine_mp[3] == "%.6f" % want_mp[3]
+    if prefix:
+        assert len(want_rows) > 10
+        mine_rows = mine_rows[:len(want_rows)]
+    assert len(mine_rows) == len(want_rows)
+    for got, want in zip(mine_rows, want_rows):
+        if want[3] is None:
+            assert got is None, want
+            continue
+        tw, p, zn = got
+        assert "%.3f" % tw == "%.3f" % want[3] and "%.3f" % zn == "%.3f" % want[5], (got, want)
+        assert abs(p - want[4]) <= 1e-5 * max(want[4], 1e-300) or "%.6g" % p == "%.6g" % want[4]
+
+
+@pytest.mark.parametrize("case,name", TW_LOGS)
+def test_oracle_tw_section_matches_reference(case, name):
+    """the log's mpstats line and Tracy-Widom section (smartpca.c:1306-1367): the oracle's
+    statistics from the reference's own eigenvalues (full precision) against its log"""
+    from tests.goldens import tw_section
+    d = os.path.join(GOLDEN, case)
+    lam = np.loadtxt(os.path.join(d, name[:-4] + ".eval"))
+    want_mp, shape, want_rows = tw_section(open(os.path.join(d, name)).read())
+    if len(lam) != shape[0]:
+        pytest.skip("the stored spectrum is truncated")
+    compare_tw(O.mpstats(lam), O.twstats(lam), want_mp, want_rows, prefix=log_cut(d, name))
+
+
+def test_tw_logs_are_exercised():
+    assert len(TW_LOGS) >= 10

@@ -84,6 +84,7 @@ int gp_smartpca_run(gp_ctx *ctx, const gp_smartpca_opts *o, const gp_panel *p,
   uint8_t *snp_ign = NULL, *ind_ign = NULL, *aff = NULL, *use = NULL, *kill = NULL;
   int32_t *valid_s = NULL, *valid_i = NULL, *xindex = NULL, *cols = NULL, *badlist = NULL;
   int32_t *vecno = NULL, *nobs = NULL, *status = NULL, *projidx = NULL, *xtypes = NULL;
+  int32_t *pc0 = NULL, *pc1 = NULL, *pcm = NULL; /* per-column counts for pass_stats */
   int32_t *sampop = NULL, npop = 0;
   double *evals = NULL, *evecs = NULL, *score = NULL, *fxscal = NULL, *acoef = NULL,
          *bcoef = NULL;
@@ -189,8 +190,12 @@ int gp_smartpca_run(gp_ctx *ctx, const gp_smartpca_opts *o, const gp_panel *p,
   for (int32_t k = 0; k < N; ++k) use[k] = (uint8_t)(!ind_ign[k] && aff[k]);
   rc = gp_valid_counts(ctx, use, NULL, valid_s, NULL);
   if (rc) goto done;
+  r->nodata = 0;
   for (int64_t s = 0; s < M; ++s)
-    if (!snp_ign[s] && valid_s[s] <= 1) snp_ign[s] = 1;
+    if (!snp_ign[s] && valid_s[s] <= 1) {
+      snp_ign[s] = 1;
+      ++r->nodata;
+    }
   /* samples with no valid genotype over the remaining SNPs -> ignore (numvalidgtallind) */
   for (int64_t s = 0; s < M; ++s) use[s] = (uint8_t)!snp_ign[s];
   rc = gp_valid_counts(ctx, NULL, use, NULL, valid_i);
@@ -216,6 +221,8 @@ int gp_smartpca_run(gp_ctx *ctx, const gp_smartpca_opts *o, const gp_panel *p,
   for (int64_t s = 0; s < M; ++s)
     if (!snp_ign[s] && valid_s[s] > 0) cols[ncols++] = (int32_t)s;
   if (nrows < 2 || ncols < 1) FAIL(gp_fail_msg(ctx, GP_ERR_NODATA, "no data (rows %d, snps %d)", nrows, ncols));
+  r->nrows0 = nrows;
+  r->ncols0 = ncols;
   r->t_phase[GP_PH_FILTER] = now_s() - t;
 
   int32_t K = o->numeigs;
@@ -277,6 +284,12 @@ int gp_smartpca_run(gp_ctx *ctx, const gp_smartpca_opts *o, const gp_panel *p,
   xo.minallelecnt = o->minallelecnt;
   xo.maxmissing = o->maxmissing;
   xo.precision = o->precision;
+  if (r->pass_stats) {
+    pc0 = (int32_t *)malloc(sizeof(int32_t) * (size_t)M);
+    pc1 = (int32_t *)malloc(sizeof(int32_t) * (size_t)M);
+    pcm = (int32_t *)malloc(sizeof(int32_t) * (size_t)M);
+    if (!pc0 || !pc1 || !pcm) FAIL(GP_ERR_NOMEM);
+  }
   for (int32_t it = 1; it <= numoutiter; ++it) {
     if (it > 1) {
       for (int32_t k = 0; k < N; ++k) use[k] = (uint8_t)!ind_ign[k];
@@ -297,9 +310,30 @@ int gp_smartpca_run(gp_ctx *ctx, const gp_smartpca_opts *o, const gp_panel *p,
     if (rc) goto done;
     double trace;
     int32_t nused;
-    rc = gp_xtx(ctx, &xo, NULL, NULL, NULL, kill, NULL, NULL, r->xtx, &trace, &nused);
+    rc = gp_xtx(ctx, &xo, pc0, pc1, pcm, kill, NULL, NULL, r->xtx, &trace, &nused);
     if (rc) goto done;
     r->nused = nused;
+    if (r->pass_stats) {
+      /* the pass's dropped SNPs and its first 10 (smartpca.c:1134-1143) */
+      int32_t *ps = r->pass_stats + (size_t)GP_PASS_STATS * (it - 1);
+      int32_t *pk = r->pass_kills ? r->pass_kills + (size_t)30 * (it - 1) : NULL;
+      int32_t nk = 0, nl = 0;
+      for (int32_t c = 0; c < ncols; ++c) {
+        if (!kill[c]) continue;
+        if (pk && nl < 10) {
+          const int32_t mn = pc0[c] < pc1[c] ? pc0[c] : pc1[c];
+          pk[3 * nl] = cols[c];
+          pk[3 * nl + 1] = mn > 0 ? mn : 0;
+          pk[3 * nl + 2] = pcm[c] > 0 ? pcm[c] : 0;
+          ++nl;
+        }
+        ++nk;
+      }
+      ps[0] = nk;
+      ps[1] = nused;
+      ps[2] = -1;
+      ps[3] = nl;
+    }
     {
       double gms = 0.0, gfl = 0.0;
       gp_last_gram_time(ctx, &gms, NULL, &gfl);
@@ -340,6 +374,7 @@ int gp_smartpca_run(gp_ctx *ctx, const gp_smartpca_opts *o, const gp_panel *p,
     nrows = 0;
     for (int32_t k = 0; k < N; ++k)
       if (!ind_ign[k] && aff[k]) xindex[nrows++] = k;
+    if (r->pass_stats) r->pass_stats[(size_t)GP_PASS_STATS * (it - 1) + 2] = nrows;
     if (nrows < 2) FAIL(gp_fail_msg(ctx, GP_ERR_NODATA, "outlier removal left %d samples", nrows));
   }
 
@@ -475,5 +510,8 @@ done:
   free(projidx);
   free(xtypes);
   free(sampop);
+  free(pc0);
+  free(pc1);
+  free(pcm);
   return rc;
 }

@@ -231,6 +231,34 @@ static void anova_tail(const gp_run_result *r, char **eg, int numeg, const int32
  * block count, the Fst matrix and its jackknife standard errors (gp_fst), and the optional
  * phylip / mega / fstdetails files.
  */
+/* the number of populations of the eglist (smartpca.c:774-784): the poplist's entries, else
+ * the distinct populations of the samples not ignored */
+static int count_eglist(const gp_indlist *inds, const char *poplistname, int32_t N)
+{
+  int numeg = 0;
+  if (poplistname) {
+    FILE *pl = fopen(poplistname, "r");
+    char line[1024];
+    while (pl && fgets(line, sizeof line, pl)) {
+      char w[256];
+      if (sscanf(line, "%255s", w) != 1 || w[0] == '#') continue;
+      ++numeg;
+    }
+    if (pl) fclose(pl);
+    return numeg;
+  }
+  const char **eg = (const char **)malloc(sizeof(char *) * (size_t)(N + 1));
+  if (!eg) return 0;
+  for (int32_t k = 0; k < N; ++k) {
+    if (inds->ignore[k]) continue;
+    int found = 0;
+    for (int e = 0; e < numeg && !found; ++e) found = strcmp(eg[e], inds->pop[k]) == 0;
+    if (!found) eg[numeg++] = inds->pop[k];
+  }
+  free(eg);
+  return numeg;
+}
+
 static int fst_tail(gp_ctx *ctx, const gp_parfile *pf, const gp_snplist *snps,
                     const gp_indlist *inds, const gp_run_result *r, const char *poplistname,
                     int64_t M, int32_t N)
@@ -815,6 +843,15 @@ int main(int argc, char **argv)
     }
   }
 
+  const int32_t npass_max = (o.numoutliter >= 1 ? o.numoutliter + 1 : 1) + 1;
+  r.pass_stats = (int32_t *)calloc((size_t)GP_PASS_STATS * npass_max, sizeof(int32_t));
+  r.pass_kills = (int32_t *)calloc((size_t)30 * npass_max, sizeof(int32_t));
+  if (!r.pass_stats || !r.pass_kills) {
+    fprintf(stderr, "no memory for the pass records\n");
+    return 1;
+  }
+  const int numeg_axes = count_eglist(&inds, poplistname, N);
+
   gp_ctx *ctx = NULL;
   int rc = gp_open(0, &ctx);
   if (rc) {
@@ -827,15 +864,47 @@ int main(int argc, char **argv)
     gp_close(ctx);
     return 1;
   }
-  printf("number of samples used: %d number of snps used: %d\n", r.nrows, r.ncols);
-  printf("passes: %d  outliers removed: %d\n", r.npasses, r.noutliers);
-
+  /* the reference's progress lines (smartpca.c:715-719, mcio.c:2842/2877 or :3987,
+   * smartpca.c:851, :945-946, then per pass :1140-1141, :1223, :1259-1264) */
+  printf(o.fancynorm ? "norm used\n\n" : "no norm used\n\n");
+  if (o.lsqproject) printf("lsqproject used\n");
+  if (code == GP_CODE_BED)
+    printf("genotype file processed\n");
+  else
+    printf("packed geno read OK\nend of inpack\n");
+  printf("snps deleted (nodata): %d.  deletesnpoutname: for details", r.nodata);
+  printf("number of samples used: %d number of snps used: %d\n", r.nrows0, r.ncols0);
+  printf("number of pops for axes: %d\n", numeg_axes);
   FILE *ol = stdout;
   if (outlierout) ol = fopen(outlierout, "w");
-  for (int32_t i = 0; i < r.noutliers && ol; ++i) {
-    int32_t k = r.outlier_idx[i];
-    fprintf(ol, "REMOVED outlier %s iter %d evec %d sigmage %.3f pop: %s\n", inds.id[k],
-            r.outlier_iter[i], r.outlier_vec[i], r.outlier_score[i], inds.pop[k]);
+  if (o.fastmode) {
+    printf("writing eigenvecotrs for  %d samples\n", r.nrows);
+  } else {
+    /* the reference's kill count starts at 0 once, before the passes (smartpca.c:1074): its
+     * "killed in pass" is the running total, and only the first 10 kills of the run are
+     * listed */
+    int32_t io = 0, nkill = 0;
+    for (int32_t pass = 0; pass < r.npasses; ++pass) {
+      const int32_t *ps = r.pass_stats + (size_t)GP_PASS_STATS * pass;
+      const int32_t *pk = r.pass_kills + (size_t)30 * pass;
+      for (int32_t j = 0; j < ps[3] && nkill + j < 10; ++j)
+        printf(" snp %20s ignored . allelecnt: %5d  missing: %5d\n", snps.id[pk[3 * j]],
+               pk[3 * j + 1], pk[3 * j + 2]);
+      nkill += ps[0];
+      printf("total number of snps killed in pass: %d  used: %d\n", nkill, ps[1]);
+      if (ps[2] < 0) continue;
+      for (; io < r.noutliers && r.outlier_iter[io] == pass + 1 && ol; ++io) {
+        int32_t k = r.outlier_idx[io];
+        fprintf(ol, "REMOVED outlier %s iter %d evec %d sigmage %.3f pop: %s\n", inds.id[k],
+                r.outlier_iter[io], r.outlier_vec[io], r.outlier_score[io], inds.pop[k]);
+      }
+      printf("number of samples after outlier removal: %d\n", ps[2]);
+    }
+    for (; io < r.noutliers && ol; ++io) { /* none expected: every removal ends a pass */
+      int32_t k = r.outlier_idx[io];
+      fprintf(ol, "REMOVED outlier %s iter %d evec %d sigmage %.3f pop: %s\n", inds.id[k],
+              r.outlier_iter[io], r.outlier_vec[io], r.outlier_score[io], inds.pop[k]);
+    }
   }
   if (ol && ol != stdout) fclose(ol);
 
@@ -891,6 +960,7 @@ int main(int argc, char **argv)
       gp_close(ctx);
       return 1;
     }
+    if (o.lsqproject) printf("lsqproj called!\n");
     rc = fst_tail(ctx, &pf, &snps, &inds, &r, poplistname, M, N);
     if (rc) {
       fprintf(stderr, "fatalx:\n%s (code %d)\n", gp_last_error(ctx), rc);
@@ -902,6 +972,7 @@ int main(int argc, char **argv)
       return 1;
     }
   }
+  if (o.fastmode) printf("end of smartpca(fastmode)\n");
   printf("## phase seconds: load %.3f filter %.3f gram %.3f eig %.3f outlier %.3f weights %.3f "
          "lsqproj %.3f total %.3f\n",
          r.t_phase[0], r.t_phase[1], r.t_phase[2], r.t_phase[3], r.t_phase[4], r.t_phase[5],

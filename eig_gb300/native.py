@@ -89,7 +89,9 @@ class RunResult(C.Structure):
                 ("noutliers", C.c_int32), ("npasses", C.c_int32),
                 ("t_phase", C.c_double * 8), ("gram_flops", C.c_double),
                 ("gram_ms", C.c_double), ("xtx", f64p), ("nused", C.c_int32),
-                ("ffvecs", f64p), ("snp_lastpass", u8p)]
+                ("ffvecs", f64p), ("snp_lastpass", u8p), ("pass_stats", i32p),
+                ("pass_kills", i32p), ("nodata", C.c_int32), ("nrows0", C.c_int32),
+                ("ncols0", C.c_int32)]
 
 
 _lib = None

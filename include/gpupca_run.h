@@ -95,7 +95,21 @@ typedef struct {
                               writesnpeigs normalisation (:3047-3053) is the caller's */
   uint8_t *snp_lastpass;   /* [nsnp] or NULL: 1 for the columns of the last pass (xsnplist,
                               including SNPs its allele-count rule dropped), else 0 */
+  /* the progress lines of the reference's log (smartpca.c:851, :945-946, :1140-1141, :1223,
+   * :1264), recorded when pass_stats is set */
+  int32_t *pass_stats;     /* [GP_PASS_STATS * (numoutliter + 1)] or NULL: per pass the SNPs its
+                              allele-count / missingness rule dropped in that pass (the
+                              reference's log prints the running total), the SNPs it used, the
+                              samples left by its outlier removal (-1: none removed), and how
+                              many dropped SNPs pass_kills lists (at most 10) */
+  int32_t *pass_kills;     /* [3 * 10 * (numoutliter + 1)] or NULL (with pass_stats): per pass
+                              the first 10 dropped SNPs as (record index, min(n0, n1) clamped at
+                              0, missing count) */
+  int32_t nodata;          /* SNPs dropped before the passes for at most one valid genotype */
+  int32_t nrows0, ncols0;  /* samples and SNPs of the first pass */
 } gp_run_result;
+
+#define GP_PASS_STATS 4
 
 void gp_smartpca_defaults(gp_smartpca_opts *o);
 int gp_smartpca_run(gp_ctx *ctx, const gp_smartpca_opts *o, const gp_panel *p,

@@ -383,3 +383,16 @@ def tw_section(text):
                 rows.append((int(f[0]), float(f[1])) + tuple(val))
             break
     return mp, shape, rows
+
+
+PROGRESS_PREFIXES = ("norm used", "no norm used", "lsqproject used", "packed geno read OK",
+                     "end of inpack", "genotype file processed", "snps deleted (nodata):",
+                     "number of pops for axes:", " snp ", "total number of snps killed in pass:",
+                     "number of samples after outlier removal:", "lsqproj called!",
+                     "writing eigenvecotrs for", "end of smartpca(fastmode)")
+
+
+def progress_lines(text):
+    """the log's run-progress lines (the preamble after the parameters, the per-pass kill and
+    outlier-removal lines, lsqproj's and fastmode's markers), in order"""
+    return [l for l in text.splitlines() if l.startswith(PROGRESS_PREFIXES)]

@@ -43,6 +43,9 @@ def test_cli_fastmode_matches_reference_text(tmp_path, par):
     cli = os.path.join(native.LIB_DIR, "gpusmartpca")
     out = subprocess.run([cli, "-p", par], cwd=d, capture_output=True, text=True)
     assert out.returncode == 0, out.stderr + out.stdout
+    from tests.goldens import progress_lines
+    ref_log = "ref.log" if par == "par" else "ref_odd.log"
+    assert progress_lines(out.stdout) == progress_lines(open(d / ref_log).read())
     mine = open(d / "out.evec").read().splitlines()
     want = r["text"]
     assert len(mine) == len(want)

@@ -204,6 +204,10 @@ def test_cli_dropin_matches_reference_text(case, tmp_path):
     assert [k[0] for k in mine_k] == [k[0] for k in want_k] and len(want_k) > 0
     assert all(abs(a[1] - b[1]) <= 1.01e-3 and abs(a[2] - b[2]) <= 1.01e-3
                for a, b in zip(mine_k, want_k))
+    # the run-progress lines (preamble, per-pass kills and outlier removals, lsqproj's
+    # marker): the reference's text
+    from tests.goldens import progress_lines
+    assert progress_lines(out.stdout) == progress_lines(open(d / "ref.log").read())
     # the mpstats line and the Tracy-Widom section: eigenvalues at the printed 6 decimals,
     # statistics and effective n at 3 decimals (1.01e-3: the GPU eigenvalues differ from the
     # reference's in the 13th digit, which can move a printed last digit), p-values 1e-4

@@ -136,6 +136,19 @@ int gp_realloc(gp_ctx *ctx, void **ptr, size_t bytes)
   return GP_OK;
 }
 
+cudaError_t gp_allow_smem(gp_ctx *ctx, const void *func)
+{
+  int optin = 0;
+  cudaError_t e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin,
+                                         ctx->device);
+  if (e != cudaSuccess) return e;
+  cudaFuncAttributes fa;
+  e = cudaFuncGetAttributes(&fa, func);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              optin - (int)fa.sharedSizeBytes);
+}
+
 extern "C" int gp_open(int device, gp_ctx **out)
 {
   if (!out) return gp_fail(NULL, GP_ERR_ARG, "gp_open: out is NULL");

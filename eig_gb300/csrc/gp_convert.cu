@@ -317,20 +317,17 @@ extern "C" int gp_encode_records(gp_ctx *ctx, int32_t format, const int32_t *sam
       if (blocks > cap) blocks = cap;
       switch (format) {
       case GP_OUT_PACKEDANCESTRYMAP:
-        GP_CUDA(ctx, cudaFuncSetAttribute(k_encode_tile<GP_OUT_PACKEDANCESTRYMAP>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        GP_CUDA(ctx, gp_allow_smem(ctx, (const void *)k_encode_tile<GP_OUT_PACKEDANCESTRYMAP>));
         k_encode_tile<GP_OUT_PACKEDANCESTRYMAP><<<(unsigned)blocks, threads, smem, ctx->stream>>>(
             ctx->d_geno, ctx->rlen_dev, d_idx, nsamples, d_snps, fl, nc, rb, dst, (int32_t)R);
         break;
       case GP_OUT_PACKEDPED:
-        GP_CUDA(ctx, cudaFuncSetAttribute(k_encode_tile<GP_OUT_PACKEDPED>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        GP_CUDA(ctx, gp_allow_smem(ctx, (const void *)k_encode_tile<GP_OUT_PACKEDPED>));
         k_encode_tile<GP_OUT_PACKEDPED><<<(unsigned)blocks, threads, smem, ctx->stream>>>(
             ctx->d_geno, ctx->rlen_dev, d_idx, nsamples, d_snps, fl, nc, rb, dst, (int32_t)R);
         break;
       default:
-        GP_CUDA(ctx, cudaFuncSetAttribute(k_encode_tile<GP_OUT_EIGENSTRAT>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        GP_CUDA(ctx, gp_allow_smem(ctx, (const void *)k_encode_tile<GP_OUT_EIGENSTRAT>));
         k_encode_tile<GP_OUT_EIGENSTRAT><<<(unsigned)blocks, threads, smem, ctx->stream>>>(
             ctx->d_geno, ctx->rlen_dev, d_idx, nsamples, d_snps, fl, nc, rb, dst, (int32_t)R);
         break;

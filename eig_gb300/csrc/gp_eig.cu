@@ -1898,8 +1898,7 @@ int gp_eig_sym(gp_ctx *ctx, double *A_in, int32_t n, int32_t nvec, double *d_eva
   if (coop) {
     int dev_coop = 0, per_sm = 0;
     cudaDeviceGetAttribute(&dev_coop, cudaDevAttrCooperativeLaunch, ctx->device);
-    GP_CUDA(ctx, cudaFuncSetAttribute(k_tridiag, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)tr_smem));
+    GP_CUDA(ctx, gp_allow_smem(ctx, (const void *)k_tridiag));
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tridiag, TR_THREADS, tr_smem);
     coop = dev_coop && per_sm >= 1;
   }
@@ -1950,9 +1949,7 @@ int gp_eig_sym(gp_ctx *ctx, double *A_in, int32_t n, int32_t nvec, double *d_eva
   if (tiled) {
     int dev_coop = 0, per_sm = 0;
     cudaDeviceGetAttribute(&dev_coop, cudaDevAttrCooperativeLaunch, ctx->device);
-    tiled = dev_coop && cudaFuncSetAttribute(k_tridiag_tiled,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)tt_smem) == cudaSuccess;
+    tiled = dev_coop && gp_allow_smem(ctx, (const void *)k_tridiag_tiled) == cudaSuccess;
     if (tiled) {
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tridiag_tiled, TR_THREADS,
                                                     tt_smem);
@@ -2125,8 +2122,7 @@ int gp_eig_sym(gp_ctx *ctx, double *A_in, int32_t n, int32_t nvec, double *d_eva
     /* FP64 brackets end at 1e-13 ||T||: the counts' own backward error is ~6e-14 ||T|| */
     const double tol = 1e-13 * tnorm;
     if (use_smem)
-      GP_CUDA(ctx, cudaFuncSetAttribute(k_multisect, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)smem));
+      GP_CUDA(ctx, gp_allow_smem(ctx, (const void *)k_multisect));
     k_multisect<<<blocks, 128, use_smem ? smem : 0, ctx->stream>>>(d, e2, n, gl, gu, tnorm, pivmin,
                                                                    tol, use_smem, epw, P, w);
     GP_LAUNCH_CHECK(ctx, "k_multisect");
@@ -2143,8 +2139,7 @@ int gp_eig_sym(gp_ctx *ctx, double *A_in, int32_t n, int32_t nvec, double *d_eva
     const char *iienv = getenv("GP_EIG_II_GLOBAL");
     const int ii_in_smem = ii_smem + 2048 <= (size_t)smem_optin && !(iienv && iienv[0] == '1');
     if (ii_in_smem)
-      GP_CUDA(ctx, cudaFuncSetAttribute(k_inverse_iteration,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ii_smem));
+      GP_CUDA(ctx, gp_allow_smem(ctx, (const void *)k_inverse_iteration));
     k_inverse_iteration<<<nvec, 256, ii_in_smem ? ii_smem : 0, ctx->stream>>>(
         d, e, n, w, nvec, tnorm, d_vecs, iw, ii_in_smem);
     GP_LAUNCH_CHECK(ctx, "k_inverse_iteration");
@@ -2164,8 +2159,7 @@ int gp_eig_sym(gp_ctx *ctx, double *A_in, int32_t n, int32_t nvec, double *d_eva
     if (qcoop) {
       int dev_coop = 0, per_sm = 0;
       cudaDeviceGetAttribute(&dev_coop, cudaDevAttrCooperativeLaunch, ctx->device);
-      GP_CUDA(ctx, cudaFuncSetAttribute(k_apply_q, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)q_smem));
+      GP_CUDA(ctx, gp_allow_smem(ctx, (const void *)k_apply_q));
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_apply_q, WY_THREADS, q_smem);
       qcoop = dev_coop && per_sm >= 1;
     }

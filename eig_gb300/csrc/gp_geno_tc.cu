@@ -642,8 +642,7 @@ int gp_tc_build_codes(gp_ctx *ctx, int sum_over_snps, const int32_t *d_samp, int
       return gp_fail(ctx, GP_ERR_ARG, "gp_tc_build_codes: records of %lld bytes are too long",
                      (long long)ctx->rlen_dev);
     const size_t smem = (size_t)warps * ctx->rlen_dev;
-    GP_CUDA(ctx, cudaFuncSetAttribute(k_codes_by_snp, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem));
+    GP_CUDA(ctx, gp_allow_smem(ctx, (const void *)k_codes_by_snp));
     int blocks = (int)((nrows_pad + warps - 1) / warps);
     if (blocks > ctx->num_sms * 16) blocks = ctx->num_sms * 16;
     k_codes_by_snp<<<blocks, 32 * warps, smem, ctx->stream>>>(ctx->d_geno, ctx->rlen_dev, d_samp,

@@ -128,6 +128,12 @@ int gp_scratch_aux(gp_ctx *ctx, size_t bytes, void **out);
 int gp_scratch4(gp_ctx *ctx, size_t bytes, void **out);
 int gp_scratch5(gp_ctx *ctx, size_t bytes, void **out);
 int gp_realloc(gp_ctx *ctx, void **ptr, size_t bytes);
+/* allow a kernel the device's largest dynamic shared memory (the opt-in maximum less its static
+ * shared memory).  The limit is a process-wide attribute of the function: setting it to one
+ * fixed value instead of each call's own size keeps concurrent handles (serving workers) from
+ * lowering it between another call's check and launch.  Each launch still requests, and
+ * occupies, only its own size. */
+cudaError_t gp_allow_smem(gp_ctx *ctx, const void *func);
 
 #define GP_CUDA(ctx, call)                                   \
   do {                                                       \

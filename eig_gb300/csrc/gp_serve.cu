@@ -763,7 +763,11 @@ extern "C" int64_t gp_smartpca_footprint(int32_t nind, int64_t nsnp, int32_t pre
   const int64_t rec = m * ((n + 63) / 64 * 16);
   const int64_t gram = 8 * n * n;
   const int64_t k = numeigs > 0 ? numeigs : 1;
-  const int64_t eig = 8 * n * 64 + 48 * n * (k > 10 ? k : 10) + 8 * n * k;
+  /* the eigensolve's vectors and workspace, plus the tiled tridiagonalisation's lower-triangle
+   * tiles (64 x 64 float-float pairs) and its parts (27 x 64 per index block of 64) */
+  const int64_t nt = (n + 63) / 64;
+  const int64_t eig = 8 * n * 64 + 48 * n * (k > 10 ? k : 10) + 8 * n * k +
+                      8 * (nt * (nt + 1) / 2 * 64 * 64 + 27 * nt * 64 + 3 * nt) + 5 * nt * nt;
   int64_t work;
   if (precision == GP_PREC_FP64) {
     work = 8 * m * (k * (k + 1) / 2 + 1) + 8 * n * 256;

@@ -28,6 +28,7 @@
  * term.
  */
 #include <math.h>
+#include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -231,18 +232,19 @@ static void tw1(double s, double *tail, double *dens)
 }
 
 static double tw_x[TW_GRID_N], tw_tail_tab[TW_GRID_N], tw_dens_tab[TW_GRID_N];
-static int tw_ready = 0;
+static pthread_once_t tw_once = PTHREAD_ONCE_INIT;
 
-static void tw_table(void)
+static void tw_build(void)
 {
-  if (tw_ready) return;
   for (int k = 0; k < TW_GRID_N; ++k) {
     tw_x[k] = TW_GRID_X0 + TW_GRID_DX * k;
     tw_x[k] = round(tw_x[k] * 10.0) / 10.0;
     tw1(tw_x[k], &tw_tail_tab[k], &tw_dens_tab[k]);
   }
-  tw_ready = 1;
 }
+
+/* the table, built once per process (callers on several threads wait for the first) */
+static void tw_table(void) { pthread_once(&tw_once, tw_build); }
 
 /* the reference's bisection for the first table entry above val (statsubs.c:1745-1764) */
 static int first_above(const double *tab, int lo, int hi, double val)

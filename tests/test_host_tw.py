@@ -64,3 +64,26 @@ def test_twstats_na_rows_and_mpstats_floor():
         assert (a is None) == (b is None)
         if a is not None:
             assert abs(a[0] - b[0]) <= 1e-12 * abs(b[0]) + 1e-12 and abs(a[2] - b[2]) <= 1e-9 * b[2]
+
+
+def test_tw_table_first_use_from_many_threads():
+    """the table is built once even when the first calls come from several threads at once
+    (ctypes releases the GIL): every thread reads the finished table"""
+    import subprocess
+    import sys
+    code = (
+        "import threading, numpy as np\n"
+        "from eig_gb300 import native\n"
+        "xs = np.linspace(-7.9, 7.9, 41)\n"
+        "out = [None] * 8\n"
+        "def run(i):\n"
+        "    out[i] = [native.tw_tail(x) for x in xs]\n"
+        "ts = [threading.Thread(target=run, args=(i,)) for i in range(8)]\n"
+        "[t.start() for t in ts]; [t.join() for t in ts]\n"
+        "assert all(o == out[0] for o in out), 'threads disagree'\n"
+        "print(repr(out[0][20]))\n")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", code], cwd=root, capture_output=True, text=True,
+                       timeout=120)
+    assert r.returncode == 0, r.stderr
+    assert abs(float(r.stdout.strip()) - native.tw_tail(0.0)) == 0.0

@@ -877,7 +877,8 @@ def tridiag_roofline(res, peaks, peak_kind):
             "algorithmic_bytes": alg,
             "note": "DRAM traffic is below the algorithmic bytes: the tiled lower triangle "
                     "(103 MB at N=5,000) mostly stays in L2; the tiled steps are bound by "
-                    "FP32-pipe issue (~70 instructions per lower-triangle element and step)",
+                    "the per-step chain of phase A, part sums and the grid barrier, and FP32-pipe "
+                    "issue (~62 instructions per lower-triangle element and step)",
             "peak_kind": "HBM copy, %s" % peak_kind}
 
 

@@ -1939,8 +1939,12 @@ int gp_eig_sym(gp_ctx *ctx, double *A_in, int32_t n, int32_t nvec, double *d_eva
     tt_maxr = ctx->tt_maxr;
     tt_maxc = ctx->tt_maxc;
     tt_maxi = ctx->tt_maxi;
-    /* parts per round: all of a block's parts in one round where shared memory allows */
+    /* parts per round: all of a block's parts in one round where shared memory allows
+     * (GP_TT_ROUND caps it, to run the several-round path at smaller orders) */
     tt_R = std::min(128, (tt_maxi + TR_WARPS - 1) / TR_WARPS * TR_WARPS);
+    const char *r_env = getenv("GP_TT_ROUND");
+    if (r_env && atoi(r_env) >= TR_WARPS)
+      tt_R = std::min(tt_R, atoi(r_env) / TR_WARPS * TR_WARPS);
     while (tt_R > TR_WARPS && tt_smem_bytes(nt, tt_R, tt_maxr, tt_maxc, tt_maxi) > 220 * 1024)
       tt_R -= TR_WARPS;
     tt_smem = tt_smem_bytes(nt, tt_R, tt_maxr, tt_maxc, tt_maxi);

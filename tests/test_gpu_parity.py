@@ -520,11 +520,16 @@ def test_split_gram_rare_variants(gpu, prec, etol, vtol):
     assert np.max(np.abs(w1 - w0) / w0) <= vtol
 
 
-def test_eig_n5000_vs_lapack(gpu):
+@pytest.mark.parametrize("rounds", ["one", "three"])
+def test_eig_n5000_vs_lapack(gpu, monkeypatch, rounds):
     """the eigensolver at the benchmark's order, N=5,000, where the float-float
     tridiagonalisation first streams a trailing matrix larger than L2: every eigenvalue within
     1e-12 of the largest against LAPACK (numpy eigh on the host), the top 20 eigenvectors with
-    small residuals, orthonormal and equal (up to sign) to LAPACK's where separated"""
+    small residuals, orthonormal and equal (up to sign) to LAPACK's where separated; also with
+    the tiled steps' parts cut into rounds of 32 per CTA (the path of orders above ~6,000,
+    where a CTA's parts do not fit shared memory at once)"""
+    if rounds == "three":
+        monkeypatch.setenv("GP_TT_ROUND", "32")
     rec, pop = synth(7000, [1800, 1700, 1500], [0.01, 0.02, 0.04], miss=0.02, seed=43)
     nind = len(pop)
     gpu.load_genotypes(rec, nind)
